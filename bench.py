@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""Benchmark: STS DOF-stages/s and time-to-solution at 8192^2, mixed vs FP64 GPU.
+
+Workload (the configuration the headline metric is quoted on): the manufactured 2-D heat
+problem u_t = kx u_xx + ky u_yy + b on [0,1]^2, 8192 x 8192 interior nodes (67.1M DOF),
+kx = 1, ky = 1e-2, RKL2 super-time-stepping with adaptive steps (rtol 1e-6, atol 1e-10,
+at most 200 stages), t in [0, 0.05]; inputs are synthetic (the analytic initial state).
+
+A "step" is one adaptive LSRK time step (s fused stencil+stage kernels, the fused step-end
+kernel and the host step control). value = DOF-stages/s of the mixed path (FP32 stage
+increments, FP64 step update) with the state resident in HBM; e2e = the same metric through
+the C-ABI with the state copied in from pinned host memory and back out every step;
+"fp64" gives the plain FP64 GPU path on the same step sequence. Each FP32 stage buffer is
+256 MiB (> 129 MB L2), so no L2 flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference algorithm (the oracle, FP64,
+all host threads) on the same problem: each step is one fixed-step RKL2 step of 20 stages.
+--full runs the whole t in [0, 0.05] solve for both precisions (time-to-solution).
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 8192
+TF = 0.05
+KX, KY = 1.0, 1e-2
+RTOL, ATOL = 1e-6, 1e-10
+METHOD = 1  # RKL2
+SMAX = 200
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region (clocks and throttle reasons)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cuda_timer(stream_ptr):
+    import torch
+    s = torch.cuda.ExternalStream(stream_ptr)
+
+    class T:
+        def __enter__(self):
+            self.e0 = torch.cuda.Event(enable_timing=True)
+            self.e1 = torch.cuda.Event(enable_timing=True)
+            self.e0.record(s)
+            return self
+
+        def __exit__(self, *a):
+            self.e1.record(s)
+            self.e1.synchronize()
+            self.ms = self.e0.elapsed_time(self.e1)
+    return T
+
+
+def traffic_from_profiles():
+    """Per-launch DRAM bytes of the mixed stage kernel at 8192^2 from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "stage_kernels_ncu.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch_mixed_8192:"):
+            try:
+                return float(line.split(":")[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_gpu(args):
+    import numpy as np
+    import ceda_demonstrations_gb300 as sts
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    import torch
+    torch.cuda.set_device(local)
+    ctx = sts.Context(local)
+    timer = cuda_timer(ctx.stream)
+    n = args.n
+    G = sts.Problem(ctx, sts.MANUFACTURED, n, n, KX, KY)
+    N2 = n * n
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if ws == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    res = {}
+    clocks = Clocks(local)
+    for mixed in (True, False):
+        I = sts.LSRKStep(ctx, G, 0.0, G.initial(), method=METHOD, rtol=RTOL, atol=ATOL,
+                         smax=SMAX, mixed=mixed, graphs=True, maxsteps=1000000)
+        y = G.vector()
+        for _ in range(args.warmup):
+            I.evolve(TF, y, sts.ONE_STEP)
+        ctx.synchronize()
+        barrier()
+        s0 = I.stats()
+        if mixed:
+            clocks.start()
+        with timer() as tm:
+            for _ in range(args.steps):
+                I.evolve(TF, y, sts.ONE_STEP)
+        if mixed:
+            clk = clocks.stop()
+        s1 = I.stats()
+        ms = max_over_ranks(tm.ms)
+        launches = (s1["stages_total"] - s0["stages_total"]) + (s1["nst_attempts"] - s0["nst_attempts"])
+        dof_stages = N2 * (s1["nfe"] - s0["nfe"])
+        stage_ms = I.time_stage_kernel(20)
+        res[mixed] = dict(ms=ms, dof_stages=dof_stages, launches=launches, stage_ms=stage_ms,
+                          t=s1["t"], s=s1["stage_max"], stats=s1, y=y.numpy(), I=I,
+                          steps=s1["nst"] - s0["nst"])
+        if mixed:
+            res[mixed]["clocks"] = clk
+
+    # end to end (mixed): state in from pinned host memory, one step, state back out
+    import torch
+    I = res[True]["I"]
+    host_in = torch.empty(N2, dtype=torch.float64, pin_memory=True)
+    host_out = torch.empty(N2, dtype=torch.float64, pin_memory=True)
+    host_in.numpy()[:] = res[True]["y"]
+    yv = G.vector()
+    L = sts.lib()
+    pin = C.cast(host_in.data_ptr(), sts._dp)
+    pout = C.cast(host_out.data_ptr(), sts._dp)
+    t_cur = res[True]["t"]
+    for _ in range(2):
+        L.N_VCopyFromHost_Sts(yv.h, pin)
+        I.reset(t_cur, yv)
+        t_cur, _ = I.evolve(TF, yv, sts.ONE_STEP)
+        L.N_VCopyToHost_Sts(yv.h, pout)
+        host_in.copy_(host_out)
+    barrier()
+    s0 = I.stats()
+    with timer() as tm:
+        for _ in range(args.steps):
+            L.N_VCopyFromHost_Sts(yv.h, pin)
+            I.reset(t_cur, yv)
+            t_cur, _ = I.evolve(TF, yv, sts.ONE_STEP)
+            L.N_VCopyToHost_Sts(yv.h, pout)
+            host_in.copy_(host_out)
+    s1 = I.stats()
+    e2e_ms = max_over_ranks(tm.ms)
+    e2e_dof = N2 * (s1["nfe"] - s0["nfe"])
+
+    # accuracy on the timed step sequence
+    ex = G.exact(res[True]["t"]).numpy()
+    out = {}
+    for mixed in (True, False):
+        yv_ = res[mixed]["y"]
+        out[mixed] = float(np.linalg.norm(yv_ - ex) / np.linalg.norm(ex))
+    same_t = res[True]["t"] == res[False]["t"]
+    mix_vs_64 = float(np.linalg.norm(res[True]["y"] - res[False]["y"]) /
+                      np.linalg.norm(res[False]["y"])) if same_t else None
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    m, d = res[True], res[False]
+    value = ws * m["dof_stages"] / (m["ms"] / 1e3)
+    fp64_value = ws * d["dof_stages"] / (d["ms"] / 1e3)
+    stage_bytes_mixed = 16.0 * N2
+    stage_bytes_fp64 = 40.0 * N2
+    ach = stage_bytes_mixed / (m["stage_ms"] / 1e3) / 1e9
+    traffic = traffic_from_profiles()
+    fp64_flops = 17.0 * N2 / (d["stage_ms"] / 1e3)
+    line = {
+        "metric": "STS DOF-stages/s & solve time at 8192^2: mixed vs FP64 GPU at 1e-6 rel L2 err",
+        "value": value,
+        "unit": "DOF-stages/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": m["ms"] / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 stage increments + f64 step update",
+        "data": "synthetic (manufactured-solution initial state, no dataset)",
+        "config": {"workload": "manufactured 2-D heat %dx%d, kx=1 ky=1e-2, RKL2 adaptive, rtol=1e-6 "
+                               "atol=1e-10, smax=200, t in [0,0.05]" % (n, n),
+                   "nx": n, "ny": n, "method": "RKL2", "stages_per_step": m["s"],
+                   "inputs_exceed_l2": True, "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "e2e": {"value": ws * e2e_dof / (e2e_ms / 1e3), "unit": "DOF-stages/s",
+                "h2d_bytes_per_step": 8 * N2, "d2h_bytes_per_step": 8 * N2},
+        "gpu_launches": m["launches"],
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": ach / peak, "traffic": traffic,
+                     "kernel": "stage32_kernel (mixed stage, 16 B/DOF-stage)",
+                     "peak_source": peak_kind},
+        "clocks": m.get("clocks"),
+        "fp64": {"value": fp64_value, "unit": "DOF-stages/s", "ms_per_step": d["ms"] / args.steps,
+                 "stage_kernel_ms": d["stage_ms"],
+                 "stage_kernel_hbm_gbs": stage_bytes_fp64 / (d["stage_ms"] / 1e3) / 1e9,
+                 "stage_kernel_fp64_tflops": fp64_flops / 1e12,
+                 "stage_kernel_fp64_frac": fp64_flops / 1.195e12,
+                 "fp64_peak_note": "1.195 TFLOP/s FP64 FMA rate measured on this GB300 pool"},
+        "speedup_mixed_vs_fp64": value / fp64_value,
+        "accuracy": {"t": m["t"], "mixed_rel_l2_vs_exact": out[True], "fp64_rel_l2_vs_exact": out[False],
+                     "mixed_vs_fp64_rel_l2": mix_vs_64},
+    }
+    cpu = cpu_baseline(args) if not args.no_cpu else None
+    line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def cpu_step_setup(n, stages):
+    """Oracle integrator at n^2 with a fixed step that needs exactly `stages` RKL2 stages."""
+    from oracle import pyoracle as po
+    P = po.Problem(po.MANUFACTURED, n, n, kx=KX, ky=KY)
+    rho = 1.01 * abs(P.dom_eig())
+    s = stages
+    h = (s * s + s - 2) / (2.0 * rho) * 0.999
+    I = po.Integrator(P, P.initial(), method=po.RKL, rtol=RTOL, atol=ATOL, hfixed=h, maxsteps=1)
+    return po, P, I, h
+
+
+def cpu_baseline(args, stages=20):
+    po, P, I, h = cpu_step_setup(args.n, stages)
+    I.evolve(TF)  # initialisation + first step (untimed)
+    s0 = I.stats()
+    t0 = time.perf_counter()
+    I.evolve(TF)
+    dt = time.perf_counter() - t0
+    s1 = I.stats()
+    dof = args.n * args.n * (s1["nfe"] - s0["nfe"])
+    return {"value": dof / dt, "unit": "DOF-stages/s", "cores": po.lib().orc_nthreads(),
+            "kind": "port",
+            "sample": "one fixed-step RKL2 step (%d stages) of the %d^2 FP64 problem on the CPU oracle"
+                      % (s1["nfe"] - s0["nfe"], args.n)}
+
+
+def run_reference(args):
+    ws, rank, local = dist_info()
+    if rank != 0:
+        return
+    po, P, I, h = cpu_step_setup(args.n, 20)
+    I.evolve(TF)
+    for _ in range(args.warmup):
+        I.evolve(TF)
+    s0 = I.stats()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        I.evolve(TF)
+    dt = time.perf_counter() - t0
+    s1 = I.stats()
+    dof = args.n * args.n * (s1["nfe"] - s0["nfe"])
+    v = dof / dt
+    sample = ("fixed-step RKL2 steps of 20 stages on the %d^2 FP64 problem; CPU restatement of the "
+              "reference algorithm (SUNDIALS is not vendored in the reference, so the reference "
+              "binary cannot be built)" % args.n)
+    line = {
+        "metric": "STS DOF-stages/s & solve time at 8192^2: mixed vs FP64 GPU at 1e-6 rel L2 err",
+        "value": v, "unit": "DOF-stages/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "manufactured 2-D heat %dx%d, kx=1 ky=1e-2, RKL2" % (args.n, args.n),
+                   "nx": args.n, "ny": args.n, "method": "RKL2"},
+        "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": "DOF-stages/s", "cores": po.lib().orc_nthreads(),
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "DOF-stages/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_full(args):
+    """Time-to-solution on [0, 0.05] for both precisions (one run each)."""
+    import numpy as np
+    import ceda_demonstrations_gb300 as sts
+    ctx = sts.Context(0)
+    timer = cuda_timer(ctx.stream)
+    n = args.n
+    G = sts.Problem(ctx, sts.MANUFACTURED, n, n, KX, KY)
+    ex = G.exact(TF).numpy()
+    out = {}
+    for method in ([1, 0] if args.both_methods else [1]):
+        for rtol in ([1e-6, 1e-4] if args.both_rtols else [1e-6]):
+            ys = {}
+            for mixed in (True, False):
+                I = sts.LSRKStep(ctx, G, 0.0, G.initial(), method=method, rtol=rtol, atol=ATOL,
+                                 smax=SMAX, mixed=mixed, graphs=True, maxsteps=1000000)
+                y = G.vector()
+                with timer() as tm:
+                    I.evolve(TF, y)
+                st = I.stats()
+                ys[mixed] = y.numpy()
+                key = "%s_rtol%g_%s" % ("RKL2" if method else "RKC2", rtol, "mixed" if mixed else "fp64")
+                out[key] = {"time_to_solution_s": tm.ms / 1e3, "steps": st["nst"], "netf": st["netf"],
+                            "rhs_evals": st["nfe"], "stage_max": st["stage_max"],
+                            "dof_stages_per_s": n * n * st["nfe"] / (tm.ms / 1e3),
+                            "rel_l2_vs_exact": float(np.linalg.norm(ys[mixed] - ex) / np.linalg.norm(ex))}
+                print(key, json.dumps(out[key]), flush=True)
+            rel = float(np.linalg.norm(ys[True] - ys[False]) / np.linalg.norm(ys[False]))
+            out["%s_rtol%g_mixed_vs_fp64_rel_l2" % ("RKL2" if method else "RKC2", rtol)] = rel
+            print("mixed vs fp64 rel L2", rel, flush=True)
+    print(json.dumps({"full_solve": out, "n": n}), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--full", action="store_true")
+    ap.add_argument("--both-methods", action="store_true")
+    ap.add_argument("--both-rtols", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    elif args.full:
+        run_full(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

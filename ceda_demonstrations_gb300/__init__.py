@@ -1,0 +1,526 @@
+"""GB300-native diffusion_2D super-time-stepping path: Python host interface.
+
+This package is a thin ctypes layer over ``libstsgpu.so`` (C ABI declared in
+``include/stsgpu.h``). It mirrors the reference's interfaces for the path:
+
+* :class:`NVector`  - N_Vector ops (gkeyll_diffusion/src/nvector_gkylzero.c:45-514)
+* :class:`Problem`  - UserData + the diffusion/dom_eig/PSetup/PSolve callbacks
+  (diffusion_2D/diffusion_2D.hpp:66-214, diffusion_2D.cpp:23, main.cpp:536,
+  preconditioner_jacobi.cpp)
+* :class:`LSRKStep` - LSRKStepCreateSTS + ARKode* (diffusion_2D/main.cpp:257-486)
+* :func:`implicit_solve_pcg`, :func:`sdirk2_evolve`, :class:`PCGSolver` - SUNLinSol_PCG with
+  the Jacobi preconditioner (main.cpp:207-231)
+
+There is no CPU fallback: if the CUDA library cannot be built or loaded, importing the
+compute entry points raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["lib", "Context", "NVector", "Problem", "LSRKStep", "PCGSolver", "implicit_solve_pcg",
+           "sdirk2_evolve", "RKC", "RKL", "PID", "PI", "I", "MANUFACTURED", "UNFORCED", "PERIODIC",
+           "STSError"]
+
+RKC, RKL = 0, 1
+PID, PI, I = 0, 1, 2
+MANUFACTURED, UNFORCED, PERIODIC = 0, 1, 2
+NORMAL, ONE_STEP = 1, 2
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+_ll = C.c_longlong
+
+
+class STSError(RuntimeError):
+    pass
+
+
+class NVOps(C.Structure):
+    pass
+
+
+class NVStruct(C.Structure):
+    _fields_ = [("content", _vp), ("ops", C.POINTER(NVOps)), ("sunctx", _vp)]
+
+
+_NV = C.POINTER(NVStruct)
+RHSFN = C.CFUNCTYPE(C.c_int, C.c_double, _NV, _NV, _vp)
+DOMEIGFN = C.CFUNCTYPE(C.c_int, C.c_double, _NV, _NV, _dp, _dp, _vp, _NV, _NV, _NV)
+ATIMESFN = C.CFUNCTYPE(C.c_int, _vp, _NV, _NV)
+PSOLVEFN = C.CFUNCTYPE(C.c_int, _vp, _NV, _NV, C.c_double, C.c_int)
+
+
+class Stats(C.Structure):
+    _fields_ = [("nst", _ll), ("nst_attempts", _ll), ("netf", _ll), ("nfe", _ll),
+                ("nfe_dee", _ll), ("ndee", _ll), ("nst_exp", _ll), ("stage_max", _ll),
+                ("stages_total", _ll), ("t", C.c_double), ("hlast", C.c_double),
+                ("hnext", C.c_double), ("spectral_radius", C.c_double)]
+
+
+# (name, restype, argtypes) for every entry point of include/stsgpu.h
+SIGNATURES = [
+    ("STS_ContextCreate", C.c_int, [C.c_int, C.POINTER(_vp)]),
+    ("STS_ContextFree", C.c_int, [C.POINTER(_vp)]),
+    ("STS_ContextSynchronize", C.c_int, [_vp]),
+    ("STS_ContextGetStream", _vp, [_vp]),
+    ("STS_GetLastError", C.c_char_p, []),
+    ("STS_DeviceCount", C.c_int, []),
+    ("N_VNew_Sts", _NV, [_ll, _vp]),
+    ("N_VNewEmpty_Sts", _NV, [_vp]),
+    ("N_VMake_Sts", _NV, [_ll, _vp, _vp]),
+    ("N_VCloneEmpty_Sts", _NV, [_NV]),
+    ("N_VClone_Sts", _NV, [_NV]),
+    ("N_VDestroy_Sts", None, [_NV]),
+    ("N_VGetDeviceArrayPointer_Sts", _vp, [_NV]),
+    ("N_VGetLength_Sts", _ll, [_NV]),
+    ("N_VSpace_Sts", None, [_NV, C.POINTER(_ll), C.POINTER(_ll)]),
+    ("N_VSetShape_Sts", C.c_int, [_NV, _ll, _ll]),
+    ("N_VCopyFromHost_Sts", C.c_int, [_NV, _dp]),
+    ("N_VCopyToHost_Sts", C.c_int, [_NV, _dp]),
+    ("N_VLinearSum_Sts", None, [C.c_double, _NV, C.c_double, _NV, _NV]),
+    ("N_VConst_Sts", None, [C.c_double, _NV]),
+    ("N_VProd_Sts", None, [_NV, _NV, _NV]),
+    ("N_VDiv_Sts", None, [_NV, _NV, _NV]),
+    ("N_VScale_Sts", None, [C.c_double, _NV, _NV]),
+    ("N_VAbs_Sts", None, [_NV, _NV]),
+    ("N_VInv_Sts", None, [_NV, _NV]),
+    ("N_VAddConst_Sts", None, [_NV, C.c_double, _NV]),
+    ("N_VDotProd_Sts", C.c_double, [_NV, _NV]),
+    ("N_VMaxNorm_Sts", C.c_double, [_NV]),
+    ("N_VWrmsNorm_Sts", C.c_double, [_NV, _NV]),
+    ("N_VLinearCombination_Sts", C.c_int, [C.c_int, _dp, C.POINTER(_NV), _NV]),
+    ("STS_ProblemCreate", _vp, [_vp, C.c_int, _ll, _ll, C.c_double, C.c_double, C.c_int,
+                                C.c_double, C.c_double, C.c_double, C.c_double]),
+    ("STS_ProblemFree", C.c_int, [C.POINTER(_vp)]),
+    ("STS_ProblemGetInfo", C.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    ("STS_Initial", C.c_int, [C.c_double, _NV, _vp]),
+    ("STS_InitialModes", C.c_int, [_NV, _vp, C.c_int, _ip, _ip, _dp]),
+    ("STS_Exact", C.c_int, [C.c_double, _NV, _vp]),
+    ("STS_Diffusion", C.c_int, [C.c_double, _NV, _NV, _vp]),
+    ("STS_JacTimes", C.c_int, [_NV, _NV, C.c_double, _NV, _NV, _vp, _NV]),
+    ("STS_DomEig", C.c_int, [C.c_double, _NV, _NV, _dp, _dp, _vp, _NV, _NV, _NV]),
+    ("STS_PowerIteration", C.c_int, [_vp, _NV, C.c_int, C.c_double, _dp, _ip]),
+    ("STS_PSetup", C.c_int, [C.c_double, _NV, _NV, C.c_int, _ip, C.c_double, _vp]),
+    ("STS_PSolve", C.c_int, [C.c_double, _NV, _NV, _NV, _NV, C.c_double, C.c_double, C.c_int,
+                             _vp]),
+    ("STS_LSRKStepCreateSTS", _vp, [_vp, C.c_double, _NV, _vp]),
+    ("STS_LSRKStepSetSTSMethod", C.c_int, [_vp, C.c_int]),
+    ("STS_ARKodeSStolerances", C.c_int, [_vp, C.c_double, C.c_double]),
+    ("STS_ARKodeSetUserData", C.c_int, [_vp, _vp]),
+    ("STS_LSRKStepSetDomEigFn", C.c_int, [_vp, _vp]),
+    ("STS_LSRKStepSetDomEigEstimatorPower", C.c_int, [_vp, C.c_int, C.c_double]),
+    ("STS_LSRKStepSetDomEigFrequency", C.c_int, [_vp, _ll]),
+    ("STS_LSRKStepSetMaxNumStages", C.c_int, [_vp, C.c_int]),
+    ("STS_LSRKStepSetDomEigSafetyFactor", C.c_int, [_vp, C.c_double]),
+    ("STS_ARKodeSetAdaptController", C.c_int, [_vp, C.c_int]),
+    ("STS_ARKodeSetFixedStep", C.c_int, [_vp, C.c_double]),
+    ("STS_ARKodeSetMaxNumSteps", C.c_int, [_vp, _ll]),
+    ("STS_ARKodeSetStopTime", C.c_int, [_vp, C.c_double]),
+    ("STS_LSRKStepSetMixedPrecision", C.c_int, [_vp, C.c_int]),
+    ("STS_LSRKStepSetUseGraphs", C.c_int, [_vp, C.c_int]),
+    ("STS_ARKodeEvolve", C.c_int, [_vp, C.c_double, _NV, _dp, C.c_int]),
+    ("STS_ARKodeReset", C.c_int, [_vp, C.c_double, _NV]),
+    ("STS_LSRKStepTimeStageKernel", C.c_int, [_vp, C.c_int, _dp]),
+    ("STS_ARKodeGetStats", C.c_int, [_vp, C.POINTER(Stats)]),
+    ("STS_ARKodePrintAllStats", C.c_int, [_vp, C.c_char_p, C.c_int]),
+    ("STS_ARKodeFree", None, [C.POINTER(_vp)]),
+    ("STS_LSRKStageCoeffs", C.c_int, [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]),
+    ("STS_LSRKStagesNeeded", C.c_int, [C.c_int, C.c_double, C.c_double, C.c_int, _dp]),
+    ("STS_AdaptControllerEstimate", C.c_double, [C.c_int, C.c_double, C.c_double, C.c_double,
+                                                 C.c_double, _ll]),
+    ("STS_ManufacturedTables", C.c_int, [_ll, C.c_double, _dp, _dp]),
+    ("STS_ExactSumHost", C.c_double, [_dp, _ll]),
+    ("STS_SUNLinSol_PCG", _vp, [_NV, C.c_int, C.c_int, _vp]),
+    ("STS_SUNLinSolSetATimes", C.c_int, [_vp, _vp, _vp]),
+    ("STS_SUNLinSolSetPreconditioner", C.c_int, [_vp, _vp, _vp]),
+    ("STS_SUNLinSolSolve", C.c_int, [_vp, _NV, _NV, C.c_double]),
+    ("STS_SUNLinSolNumIters", C.c_int, [_vp]),
+    ("STS_SUNLinSolResNorm", C.c_double, [_vp]),
+    ("STS_SUNLinSolFree", C.c_int, [_vp]),
+    ("STS_ImplicitSolvePCG", C.c_int, [_vp, C.c_double, _NV, _NV, C.c_double, C.c_int, C.c_int,
+                                       _ip, _dp]),
+    ("STS_SDIRK2Evolve", C.c_int, [_vp, _NV, C.c_double, C.c_double, C.c_int, C.c_double,
+                                   C.c_int, C.POINTER(_ll)]),
+]
+
+_lib = None
+
+
+def lib(build=True):
+    """Load libstsgpu.so (building it first if needed)."""
+    global _lib
+    if _lib is None:
+        path = _build.build() if build else _build.LIB
+        if not os.path.exists(path):
+            raise STSError("libstsgpu.so is not built: run __graft_entry__.build()")
+        L = C.CDLL(path)
+        for name, res, args in SIGNATURES:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _err(msg):
+    e = lib().STS_GetLastError()
+    raise STSError("%s: %s" % (msg, e.decode() if e else ""))
+
+
+def _dptr(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+class Context:
+    """STS_Context (SUNContext analogue): CUDA stream + reduction workspace of one device."""
+
+    def __init__(self, device=0):
+        self.h = _vp()
+        if lib().STS_ContextCreate(device, C.byref(self.h)) != 0:
+            _err("STS_ContextCreate")
+
+    def synchronize(self):
+        lib().STS_ContextSynchronize(self.h)
+
+    @property
+    def stream(self):
+        return lib().STS_ContextGetStream(self.h)
+
+    def free(self):
+        if self.h:
+            lib().STS_ContextFree(C.byref(self.h))
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class NVector:
+    """Device N_Vector (owned unless wrapping an existing device pointer)."""
+
+    def __init__(self, ctx, n=None, handle=None, own=True):
+        self.ctx = ctx
+        if handle is not None:
+            self.h = handle
+        else:
+            self.h = lib().N_VNew_Sts(n, ctx.h)
+            if not self.h:
+                _err("N_VNew_Sts")
+        self.own = own
+
+    @classmethod
+    def from_numpy(cls, ctx, a):
+        a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+        v = cls(ctx, a.size)
+        v.copy_from(a)
+        return v
+
+    @classmethod
+    def wrap(cls, ctx, handle):
+        return cls(ctx, handle=handle, own=False)
+
+    def __len__(self):
+        return lib().N_VGetLength_Sts(self.h)
+
+    @property
+    def ptr(self):
+        return lib().N_VGetDeviceArrayPointer_Sts(self.h)
+
+    def copy_from(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+        assert a.size == len(self)
+        if lib().N_VCopyFromHost_Sts(self.h, _dptr(a)) != 0:
+            _err("N_VCopyFromHost_Sts")
+
+    def numpy(self):
+        out = np.empty(len(self))
+        if lib().N_VCopyToHost_Sts(self.h, _dptr(out)) != 0:
+            _err("N_VCopyToHost_Sts")
+        return out
+
+    def clone(self):
+        return NVector(self.ctx, handle=lib().N_VClone_Sts(self.h))
+
+    def destroy(self):
+        if self.own and self.h:
+            lib().N_VDestroy_Sts(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    # ops (N_VLinearSum etc.)
+    def linear_sum(self, a, x, b, y):
+        lib().N_VLinearSum_Sts(a, x.h, b, y.h, self.h)
+
+    def const(self, c):
+        lib().N_VConst_Sts(c, self.h)
+
+    def prod(self, x, y):
+        lib().N_VProd_Sts(x.h, y.h, self.h)
+
+    def div(self, x, y):
+        lib().N_VDiv_Sts(x.h, y.h, self.h)
+
+    def scale(self, c, x):
+        lib().N_VScale_Sts(c, x.h, self.h)
+
+    def abs(self, x):
+        lib().N_VAbs_Sts(x.h, self.h)
+
+    def inv(self, x):
+        lib().N_VInv_Sts(x.h, self.h)
+
+    def add_const(self, x, b):
+        lib().N_VAddConst_Sts(x.h, b, self.h)
+
+    def dot(self, y):
+        return lib().N_VDotProd_Sts(self.h, y.h)
+
+    def max_norm(self):
+        return lib().N_VMaxNorm_Sts(self.h)
+
+    def wrms_norm(self, w):
+        return lib().N_VWrmsNorm_Sts(self.h, w.h)
+
+    def linear_combination(self, coeffs, vecs):
+        n = len(vecs)
+        c = (C.c_double * n)(*coeffs)
+        X = (_NV * n)(*[v.h for v in vecs])
+        if lib().N_VLinearCombination_Sts(n, c, X, self.h) != 0:
+            _err("N_VLinearCombination_Sts")
+
+
+class Problem:
+    """The diffusion_2D problem (UserData + RHS/DomEig/PSetup/PSolve callbacks)."""
+
+    def __init__(self, ctx, kind=MANUFACTURED, nx=128, ny=None, kx=1.0, ky=1.0,
+                 inhomogeneous=False, xl=-np.pi, xu=np.pi, yl=-6.0, yu=6.0):
+        ny = nx if ny is None else ny
+        self.ctx, self.nx, self.ny, self.kind = ctx, nx, ny, kind
+        self.h = lib().STS_ProblemCreate(ctx.h, kind, nx, ny, kx, ky, int(inhomogeneous), xl, xu,
+                                         yl, yu)
+        if not self.h:
+            _err("STS_ProblemCreate")
+
+    @property
+    def n(self):
+        return self.nx * self.ny
+
+    def vector(self):
+        v = NVector(self.ctx, self.n)
+        lib().N_VSetShape_Sts(v.h, self.nx, self.ny)
+        return v
+
+    def initial(self, t=0.0):
+        v = self.vector()
+        if lib().STS_Initial(t, v.h, self.h) != 0:
+            _err("STS_Initial")
+        return v
+
+    def initial_modes(self, pm, qm, amp):
+        v = self.vector()
+        pm = np.ascontiguousarray(pm, dtype=np.int32)
+        qm = np.ascontiguousarray(qm, dtype=np.int32)
+        amp = np.ascontiguousarray(amp, dtype=np.float64)
+        if lib().STS_InitialModes(v.h, self.h, len(amp), pm.ctypes.data_as(_ip),
+                                  qm.ctypes.data_as(_ip), _dptr(amp)) != 0:
+            _err("STS_InitialModes")
+        return v
+
+    def exact(self, t):
+        v = self.vector()
+        if lib().STS_Exact(t, v.h, self.h) != 0:
+            _err("STS_Exact")
+        return v
+
+    def rhs(self, t, u, f):
+        return lib().STS_Diffusion(t, u.h, f.h, self.h)
+
+    def jac_times(self, v, Jv):
+        return lib().STS_JacTimes(v.h, Jv.h, 0.0, None, None, self.h, None)
+
+    def dom_eig(self):
+        lr, li = C.c_double(), C.c_double()
+        lib().STS_DomEig(0.0, None, None, C.byref(lr), C.byref(li), self.h, None, None, None)
+        return lr.value
+
+    def power_iteration(self, v, maxiters=100, reltol=0.01):
+        lam, it = C.c_double(), C.c_int()
+        if lib().STS_PowerIteration(self.h, v.h, maxiters, reltol, C.byref(lam), C.byref(it)):
+            _err("STS_PowerIteration")
+        return lam.value, it.value
+
+    def psetup(self, gamma):
+        jc = C.c_int()
+        return lib().STS_PSetup(0.0, None, None, 0, C.byref(jc), gamma, self.h)
+
+    def psolve(self, r, z, gamma):
+        return lib().STS_PSolve(0.0, None, None, r.h, z.h, gamma, 0.0, 2, self.h)
+
+    def free(self):
+        if self.h:
+            lib().STS_ProblemFree(C.byref(C.c_void_p(self.h)))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class LSRKStep:
+    """LSRKStepCreateSTS + ARKode* configuration and evolve (diffusion_2D/main.cpp:257-486).
+
+    ``rhs`` is either a :class:`Problem` (its built-in STS_Diffusion RHS; fused kernels) or a
+    Python callable ``f(t, y: NVector, ydot: NVector) -> int`` (generic path)."""
+
+    def __init__(self, ctx, rhs, t0, y0, method=RKC, rtol=1e-6, atol=1e-10, controller=PID,
+                 smax=200, mixed=False, graphs=True, dom_eig=None, power=None, maxsteps=100000,
+                 hfixed=0.0):
+        self.ctx = ctx
+        L = lib()
+        self._keep = []
+        if isinstance(rhs, Problem):
+            fn = C.cast(L.STS_Diffusion, _vp)
+            ud = rhs.h
+            self.problem = rhs
+        else:
+            def tramp(t, y, ydot, _ud):
+                return int(rhs(t, NVector.wrap(ctx, y), NVector.wrap(ctx, ydot)) or 0)
+            cb = RHSFN(tramp)
+            self._keep.append(cb)
+            fn = C.cast(cb, _vp)
+            ud = None
+            self.problem = None
+        self.mem = L.STS_LSRKStepCreateSTS(fn, t0, y0.h, ctx.h)
+        if not self.mem:
+            _err("STS_LSRKStepCreateSTS")
+        self.n = len(y0)
+        L.STS_ARKodeSetUserData(self.mem, ud)
+        L.STS_LSRKStepSetSTSMethod(self.mem, method)
+        L.STS_ARKodeSStolerances(self.mem, rtol, atol)
+        L.STS_ARKodeSetAdaptController(self.mem, controller)
+        L.STS_LSRKStepSetMaxNumStages(self.mem, smax)
+        L.STS_LSRKStepSetMixedPrecision(self.mem, int(mixed))
+        L.STS_LSRKStepSetUseGraphs(self.mem, int(graphs))
+        L.STS_ARKodeSetMaxNumSteps(self.mem, maxsteps)
+        if hfixed > 0:
+            L.STS_ARKodeSetFixedStep(self.mem, hfixed)
+        if power is not None:
+            L.STS_LSRKStepSetDomEigEstimatorPower(self.mem, power[0], power[1])
+        elif dom_eig is not None:
+            def dtramp(t, y, fn_, lr, li, _ud, t1, t2, t3):
+                lam = dom_eig(t)
+                lr[0] = lam
+                li[0] = 0.0
+                return 0
+            cb = DOMEIGFN(dtramp)
+            self._keep.append(cb)
+            L.STS_LSRKStepSetDomEigFn(self.mem, C.cast(cb, _vp))
+        elif isinstance(rhs, Problem):
+            L.STS_LSRKStepSetDomEigFn(self.mem, C.cast(L.STS_DomEig, _vp))
+
+    def evolve(self, tout, yout, itask=NORMAL):
+        t = C.c_double()
+        rc = lib().STS_ARKodeEvolve(self.mem, tout, yout.h, C.byref(t), itask)
+        if rc < 0:
+            _err("STS_ARKodeEvolve returned %d" % rc)
+        return t.value, rc
+
+    def reset(self, t, y):
+        rc = lib().STS_ARKodeReset(self.mem, t, y.h)
+        if rc != 0:
+            _err("STS_ARKodeReset returned %d" % rc)
+
+    def time_stage_kernel(self, nlaunch=20):
+        ms = C.c_double()
+        if lib().STS_LSRKStepTimeStageKernel(self.mem, nlaunch, C.byref(ms)) != 0:
+            _err("STS_LSRKStepTimeStageKernel")
+        return ms.value
+
+    def set_stop_time(self, tstop):
+        lib().STS_ARKodeSetStopTime(self.mem, tstop)
+
+    def stats(self):
+        s = Stats()
+        lib().STS_ARKodeGetStats(self.mem, C.byref(s))
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def print_stats(self):
+        buf = C.create_string_buffer(4096)
+        lib().STS_ARKodePrintAllStats(self.mem, buf, 4096)
+        return buf.value.decode()
+
+    def free(self):
+        if self.mem:
+            m = _vp(self.mem)
+            lib().STS_ARKodeFree(C.byref(m))
+            self.mem = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class PCGSolver:
+    """SUNLinSol_PCG through ATimes / PSolve callbacks (generic path)."""
+
+    def __init__(self, ctx, y, atimes, psolve=None, maxl=100):
+        L = lib()
+        self.ctx = ctx
+        self.LS = L.STS_SUNLinSol_PCG(y.h, 2 if psolve else 0, maxl, ctx.h)
+        self._keep = []
+
+        def at(_d, v, z):
+            return int(atimes(NVector.wrap(ctx, v), NVector.wrap(ctx, z)) or 0)
+        cb = ATIMESFN(at)
+        self._keep.append(cb)
+        L.STS_SUNLinSolSetATimes(self.LS, None, C.cast(cb, _vp))
+        if psolve:
+            def ps(_d, r, z, tol, lr):
+                return int(psolve(NVector.wrap(ctx, r), NVector.wrap(ctx, z)) or 0)
+            cb2 = PSOLVEFN(ps)
+            self._keep.append(cb2)
+            L.STS_SUNLinSolSetPreconditioner(self.LS, None, C.cast(cb2, _vp))
+
+    def solve(self, x, b, delta):
+        rc = lib().STS_SUNLinSolSolve(self.LS, x.h, b.h, delta)
+        return rc, lib().STS_SUNLinSolNumIters(self.LS), lib().STS_SUNLinSolResNorm(self.LS)
+
+    def __del__(self):
+        try:
+            lib().STS_SUNLinSolFree(self.LS)
+        except Exception:
+            pass
+
+
+def implicit_solve_pcg(problem, gamma, b, x, tol=1e-8, maxit=100000, jacobi=True):
+    it, rel = C.c_int(), C.c_double()
+    rc = lib().STS_ImplicitSolvePCG(problem.h, gamma, b.h, x.h, tol, maxit, int(jacobi),
+                                    C.byref(it), C.byref(rel))
+    if rc < 0:
+        _err("STS_ImplicitSolvePCG")
+    return it.value, rel.value, rc
+
+
+def sdirk2_evolve(problem, y, t0, h, nsteps, tol=1e-10, maxit=100000):
+    it = _ll()
+    rc = lib().STS_SDIRK2Evolve(problem.h, y.h, t0, h, nsteps, tol, maxit, C.byref(it))
+    if rc < 0:
+        _err("STS_SDIRK2Evolve")
+    return it.value

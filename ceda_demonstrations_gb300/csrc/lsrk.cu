@@ -1,0 +1,1149 @@
+// LSRKStep super-time-stepping integrator (RKC2 / RKL2) with ARKODE-style step control.
+//
+// Replaces the SUNDIALS objects the reference driver builds in diffusion_2D/main.cpp:257-400
+// and advances with ARKodeEvolve (main.cpp:442). Two execution paths:
+//   fused   - RHS is STS_Diffusion on an STS_Problem: one fused stencil+stage kernel per
+//             stage, a fused step-end kernel (F(y_{n+1}) + error estimate + exact WRMS), the
+//             stage loop of each distinct stage count captured once in a CUDA graph;
+//             optionally FP32 stage increments relative to the FP64 step start;
+//   generic - any other ARKRhsFn: stages through the user callback and N_Vector ops.
+// Step control runs on the host after one device sync per step (the WRMS lands in mapped
+// pinned memory). Constants and formulas are restated from the RKC/RKL2 papers and the
+// ARKODE documentation (SUNDIALS itself is an empty submodule in the reference tree):
+//   stage count   RKC: s = max(2, 1 + floor(sqrt(1 + 1.54 h rho)))  (rkc.f)
+//                 RKL: s = max(2, ceil((sqrt(9 + 8 h rho) - 1)/2))
+//   stage cap     h <= 0.96 (smax^2-1)/(1.54 rho) (RKC), 0.96 (smax^2+smax-2)/(2 rho) (RKL)
+//   controllers   PID (0.58, 0.21, 0.1), PI (0.8, 0.31), I (1.0), error bias 1.5, order 3
+//   step limits   safety 0.96, growth 20 (10^4 on the first step, 1 after a failure),
+//                 eta in [1, 1.5] -> 1, failures: eta <= 1, <= 0.3 after 2, >= 0.1
+//   spectral radius = 1.01 |lambda|, refreshed every 25 accepted steps (0: computed once)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "kernels.cuh"
+#include "sts_internal.cuh"
+
+void sts_f64_to_f32(STS_Context ctx, const double* a, float* b, long long n);
+
+// ---------------------------------------------------------------------------------------
+// coefficient and step-size rules (host)
+// ---------------------------------------------------------------------------------------
+extern "C" int STS_LSRKStageCoeffs(int method, int s, double* mu, double* nu, double* mus, double* ajm1,
+                                   double* cjm1)
+{
+  if (s < 2) return -1;
+  if (method == STS_LSRK_RKC_2)
+  {
+    const double sd    = (double)s;
+    const double w0    = 1.0 + 2.0 / (13.0 * (sd * sd));
+    const double temp1 = w0 * w0 - 1.0;
+    const double temp2 = sqrt(temp1);
+    const double arg   = sd * log(w0 + temp2);
+    const double w1    = sinh(arg) * temp1 / (cosh(arg) * sd * temp2 - w0 * sinh(arg));
+    double bjm1        = 1.0 / ((2.0 * w0) * (2.0 * w0));
+    double bjm2        = bjm1;
+    mu[1]              = 0.0;
+    nu[1]              = 0.0;
+    mus[1]             = w1 * bjm1;
+    ajm1[1]            = 0.0;
+    cjm1[1]            = 0.0;
+    double thjm2 = 0.0, thjm1 = mus[1];
+    double zjm1 = w0, zjm2 = 1.0, dzjm1 = 1.0, dzjm2 = 0.0, d2zjm1 = 0.0, d2zjm2 = 0.0;
+    for (int j = 2; j <= s; ++j)
+    {
+      const double zj   = 2.0 * w0 * zjm1 - zjm2;
+      const double dzj  = 2.0 * w0 * dzjm1 - dzjm2 + 2.0 * zjm1;
+      const double d2zj = 2.0 * w0 * d2zjm1 - d2zjm2 + 4.0 * dzjm1;
+      const double bj   = d2zj / (dzj * dzj);
+      const double a    = 1.0 - zjm1 * bjm1;
+      const double m    = 2.0 * w0 * bj / bjm1;
+      const double n    = -bj / bjm2;
+      const double ms   = m * w1 / w0;
+      mu[j]             = m;
+      nu[j]             = n;
+      mus[j]            = ms;
+      ajm1[j]           = a;
+      cjm1[j]           = thjm1;
+      const double thj  = m * thjm1 + n * thjm2 + ms * (1.0 - a);
+      thjm2             = thjm1;
+      thjm1             = thj;
+      bjm2              = bjm1;
+      bjm1              = bj;
+      zjm2              = zjm1;
+      zjm1              = zj;
+      dzjm2             = dzjm1;
+      dzjm1             = dzj;
+      d2zjm2            = d2zjm1;
+      d2zjm1            = d2zj;
+    }
+  }
+  else if (method == STS_LSRK_RKL_2)
+  {
+    const double sd = (double)s;
+    const double w1 = 4.0 / ((sd + 2.0) * (sd - 1.0));
+    double bjm2 = 1.0 / 3.0, bjm1 = 1.0 / 3.0;
+    mu[1]      = 0.0;
+    nu[1]      = 0.0;
+    mus[1]     = w1 * bjm1;
+    ajm1[1]    = 0.0;
+    cjm1[1]    = 0.0;
+    double cj1 = mus[1];
+    for (int j = 2; j <= s; ++j)
+    {
+      const double jd   = (double)j;
+      const double temj = (jd + 2.0) * (jd - 1.0);
+      const double cj   = temj * w1 / 4.0;
+      const double bj   = temj / (2.0 * jd * (jd + 1.0));
+      const double a    = 1.0 - bjm1;
+      const double m    = (2.0 * jd - 1.0) / jd * (bj / bjm1);
+      const double n    = -(jd - 1.0) / jd * (bj / bjm2);
+      mu[j]             = m;
+      nu[j]             = n;
+      mus[j]            = w1 * m;
+      ajm1[j]           = a;
+      cjm1[j]           = cj1;
+      cj1               = cj;
+      bjm2              = bjm1;
+      bjm1              = bj;
+    }
+  }
+  else return -1;
+  return 0;
+}
+
+extern "C" int STS_LSRKStagesNeeded(int method, double h, double rho, int smax, double* hmax)
+{
+  double ss;
+  const double sm = (double)smax;
+  if (method == STS_LSRK_RKC_2)
+  {
+    ss    = 1.0 + floor(sqrt(1.0 + 1.54 * h * rho));
+    *hmax = (rho > 0.0) ? 0.96 * (sm * sm - 1.0) / (1.54 * rho) : INFINITY;
+  }
+  else
+  {
+    ss    = ceil((sqrt(9.0 + 8.0 * h * rho) - 1.0) / 2.0);
+    *hmax = (rho > 0.0) ? 0.96 * (sm * sm + sm - 2.0) / (2.0 * rho) : INFINITY;
+  }
+  if (ss < 2.0) ss = 2.0;
+  if (ss > 1e9) ss = 1e9;
+  return (int)ss;
+}
+
+static constexpr double ORD = 3.0, BIAS = 1.5, TINYE = 1.0e-10;
+extern "C" double STS_AdaptControllerEstimate(int controller, double h, double dsm, double ep1, double ep2,
+                                              long long nhist)
+{
+  double e1 = BIAS * dsm;
+  if (e1 < TINYE) e1 = TINYE;
+  double e2 = BIAS * ep1;
+  if (e2 < TINYE) e2 = TINYE;
+  double e3 = BIAS * ep2;
+  if (e3 < TINYE) e3 = TINYE;
+  if (controller == STS_ADAPT_PID)
+  {
+    if (nhist < 1) return h * pow(e1, -0.58 / ORD);
+    if (nhist < 2) return h * pow(e1, -0.58 / ORD) * pow(e2, 0.21 / ORD);
+    return h * pow(e1, -0.58 / ORD) * pow(e2, 0.21 / ORD) * pow(e3, -0.1 / ORD);
+  }
+  if (controller == STS_ADAPT_PI)
+  {
+    if (nhist < 1) return h * pow(e1, -0.8 / ORD);
+    return h * pow(e1, -0.8 / ORD) * pow(e2, 0.31 / ORD);
+  }
+  return h * pow(e1, -1.0 / ORD);
+}
+
+static constexpr double SAFETY = 0.96, GROWTH = 20.0, ETAMX1 = 10000.0, ETAMXF = 0.3, ETAMIN = 0.1;
+static constexpr double LBOUND = 1.0, UBOUND = 1.5;
+static constexpr int SMALL_NEF = 2;
+
+// ---------------------------------------------------------------------------------------
+// integrator memory
+// ---------------------------------------------------------------------------------------
+struct GraphKey {
+  int s, parity;
+  bool operator<(const GraphKey& o) const { return s != o.s ? s < o.s : parity < o.parity; }
+};
+
+struct LSRKMem {
+  STS_Context ctx       = nullptr;
+  STS_ARKRhsFn rhs      = nullptr;
+  void* user_data       = nullptr;
+  STS_ARKDomEigFn domeig = nullptr;
+  bool power            = false;
+  int dee_maxiters      = 100;
+  double dee_reltol     = 0.01;
+  int method            = STS_LSRK_RKC_2;
+  int controller        = STS_ADAPT_PID;
+  int smax              = 200;
+  double rtol = 1e-4, atol = 1e-9; // ARKODE defaults until SStolerances is called
+  double hfixed         = 0.0;
+  double eig_safety     = 1.01;
+  long long dom_eig_freq = 25;
+  long long maxsteps    = 500;
+  double tstop          = INFINITY;
+  bool mixed            = false;
+  bool use_graphs       = true;
+  long long n           = 0;
+
+  // state (mirrors the oracle's orc_state)
+  double t = 0, hnext = 0, hlast = 0, rho = 0, ep1 = 0, ep2 = 0;
+  long long ncf = 0;
+  long long nst = 0, nst_att = 0, netf = 0, nfe = 0, nfe_dee = 0, ndee = 0, nst_exp = 0, stage_max = 0,
+            stages_total = 0, nhist = 0, steps_since_dee = -1;
+  bool initialized = false, after_fail = false;
+  int last_s = 0;
+
+  // device buffers
+  double* yb[2] = {nullptr, nullptr}; // y_n / y_{n+1} (parity)
+  double* Fb[2] = {nullptr, nullptr}; // F_n / F_{n+1}
+  float* Ffb[2] = {nullptr, nullptr}; // FP32 copies (mixed)
+  double* Y[3]  = {nullptr, nullptr, nullptr};
+  float* D[3]   = {nullptr, nullptr, nullptr};
+  double* evec  = nullptr;
+  int par       = 0; // current parity: yb[par] = y_n
+  N_Vector nv_y = nullptr, nv_F = nullptr, nv_tmp[3] = {nullptr, nullptr, nullptr};
+
+  // stage parameters: [StepArgs][StageArgs x (smax+1)] on the device and pinned on the host
+  void* d_par = nullptr;
+  void* h_par = nullptr;
+  size_t par_bytes = 0;
+  std::map<GraphKey, cudaGraphExec_t> graphs;
+
+  // generic path temporaries
+  N_Vector g_Y[3] = {nullptr, nullptr, nullptr}, g_F = nullptr, g_Fnew = nullptr, g_err = nullptr,
+           g_ewt = nullptr, g_y = nullptr, g_Fn = nullptr;
+};
+
+static bool fused(const LSRKMem* m)
+{
+  return m->rhs == STS_Diffusion && m->user_data != nullptr &&
+         ((STS_Problem)m->user_data)->kind != STS_PROBLEM_PERIODIC;
+}
+
+static void free_device(LSRKMem* m)
+{
+  for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+  m->graphs.clear();
+  for (int b = 0; b < 2; ++b)
+  {
+    cudaFree(m->yb[b]);
+    cudaFree(m->Fb[b]);
+    cudaFree(m->Ffb[b]);
+    m->yb[b] = m->Fb[b] = nullptr;
+    m->Ffb[b]           = nullptr;
+  }
+  for (int b = 0; b < 3; ++b)
+  {
+    cudaFree(m->Y[b]);
+    cudaFree(m->D[b]);
+    m->Y[b] = nullptr;
+    m->D[b] = nullptr;
+  }
+  cudaFree(m->evec);
+  m->evec = nullptr;
+  cudaFree(m->d_par);
+  cudaFreeHost(m->h_par);
+  m->d_par = m->h_par = nullptr;
+  N_Vector* vs[] = {&m->nv_y, &m->nv_F, &m->nv_tmp[0], &m->nv_tmp[1], &m->nv_tmp[2], &m->g_Y[0], &m->g_Y[1],
+                    &m->g_Y[2], &m->g_F, &m->g_Fnew, &m->g_err, &m->g_ewt, &m->g_y, &m->g_Fn};
+  for (N_Vector* v : vs)
+  {
+    if (*v) N_VDestroy_Sts(*v);
+    *v = nullptr;
+  }
+}
+
+static StepArgs* hstep(LSRKMem* m) { return (StepArgs*)m->h_par; }
+static StageArgs* hstage(LSRKMem* m) { return (StageArgs*)((char*)m->h_par + sizeof(StepArgs) + 8); }
+static StepArgs* dstep(LSRKMem* m) { return (StepArgs*)m->d_par; }
+static StageArgs* dstage(LSRKMem* m) { return (StageArgs*)((char*)m->d_par + sizeof(StepArgs) + 8); }
+
+// allocate the fused-path buffers (y0 copied into yb[0])
+static int alloc_fused(LSRKMem* m, const double* y0dev)
+{
+  const size_t n8 = m->n * sizeof(double), n4 = m->n * sizeof(float);
+  cudaStream_t st = m->ctx->stream;
+  for (int b = 0; b < 2; ++b)
+  {
+    if (!STS_CUDA_OK(cudaMalloc(&m->yb[b], n8)) || !STS_CUDA_OK(cudaMalloc(&m->Fb[b], n8)) ||
+        !STS_CUDA_OK(cudaMalloc(&m->Ffb[b], n4)))
+      return -1;
+  }
+  m->par_bytes = sizeof(StepArgs) + 8 + sizeof(StageArgs) * (size_t)(m->smax + 1);
+  if (!STS_CUDA_OK(cudaMalloc(&m->d_par, m->par_bytes)) ||
+      !STS_CUDA_OK(cudaHostAlloc(&m->h_par, m->par_bytes, cudaHostAllocDefault)))
+    return -1;
+  memset(m->h_par, 0, m->par_bytes);
+  if (!STS_CUDA_OK(cudaMemcpyAsync(m->yb[0], y0dev, n8, cudaMemcpyDeviceToDevice, st))) return -1;
+  m->par = 0;
+  return 0;
+}
+
+static int ensure_stage_buffers(LSRKMem* m)
+{
+  const size_t n8 = m->n * sizeof(double), n4 = m->n * sizeof(float);
+  for (int b = 0; b < 3; ++b)
+  {
+    if (!m->mixed && !m->Y[b] && !STS_CUDA_OK(cudaMalloc(&m->Y[b], n8))) return -1;
+    if (m->mixed && !m->D[b] && !STS_CUDA_OK(cudaMalloc(&m->D[b], n4))) return -1;
+  }
+  return 0;
+}
+
+static int ensure_par(LSRKMem* m)
+{
+  size_t need = sizeof(StepArgs) + 8 + sizeof(StageArgs) * (size_t)(m->smax + 1);
+  if (need <= m->par_bytes && m->d_par) return 0;
+  for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+  m->graphs.clear();
+  cudaFree(m->d_par);
+  cudaFreeHost(m->h_par);
+  m->par_bytes = need;
+  if (!STS_CUDA_OK(cudaMalloc(&m->d_par, need)) || !STS_CUDA_OK(cudaHostAlloc(&m->h_par, need, cudaHostAllocDefault)))
+    return -1;
+  memset(m->h_par, 0, need);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// fused stage loop
+// ---------------------------------------------------------------------------------------
+// launch shapes: FP64 stage 64x4 threads, 2 columns x 8 rows per thread; FP32 stage 64x4
+// threads, 4 columns x 8 rows per thread; scalar-column variants when nx is not a
+// multiple of the vector width.
+static constexpr int RY = 8;
+
+template <typename F>
+static void dispatch_forced(bool forced, F&& f)
+{
+  if (forced) f(std::true_type{});
+  else f(std::false_type{});
+}
+
+static void launch_stage64(LSRKMem* m, STS_Problem p, const StageArgs* A, const double* ym1, const double* ym2,
+                           const double* y0, const double* f0, double* yj)
+{
+  const bool forced = p->kind == STS_PROBLEM_MANUFACTURED;
+  dim3 b(64, 4);
+  if (p->nx % 2 == 0)
+  {
+    dim3 g((unsigned)((p->nx / 2 + b.x - 1) / b.x), (unsigned)((p->ny + b.y * RY - 1) / (b.y * RY)));
+    dispatch_forced(forced, [&](auto F) {
+      stage64_kernel<2, RY, decltype(F)::value><<<g, b, 0, m->ctx->stream>>>(p->dev, A, ym1, ym2, y0, f0, yj);
+    });
+  }
+  else
+  {
+    dim3 g((unsigned)((p->nx + b.x - 1) / b.x), (unsigned)((p->ny + b.y * RY - 1) / (b.y * RY)));
+    dispatch_forced(forced, [&](auto F) {
+      stage64_kernel<1, RY, decltype(F)::value><<<g, b, 0, m->ctx->stream>>>(p->dev, A, ym1, ym2, y0, f0, yj);
+    });
+  }
+}
+
+static void launch_stage32(LSRKMem* m, STS_Problem p, const StageArgs* A, const float* dm1, const float* dm2,
+                           const float* f0f, float* dj)
+{
+  const bool forced = p->kind == STS_PROBLEM_MANUFACTURED;
+  dim3 b(64, 4);
+  auto go = [&](auto VECc) {
+    constexpr int VEC = decltype(VECc)::value;
+    dim3 g((unsigned)((p->nx / VEC + b.x - 1) / b.x), (unsigned)((p->ny + b.y * RY - 1) / (b.y * RY)));
+    dispatch_forced(forced, [&](auto F) {
+      if (dm2)
+        stage32_kernel<VEC, RY, decltype(F)::value, true><<<g, b, 0, m->ctx->stream>>>(p->dev, A, dm1, dm2, f0f, dj);
+      else
+        stage32_kernel<VEC, RY, decltype(F)::value, false><<<g, b, 0, m->ctx->stream>>>(p->dev, A, dm1, dm2, f0f, dj);
+    });
+  };
+  if (p->nx % 4 == 0) go(std::integral_constant<int, 4>{});
+  else go(std::integral_constant<int, 1>{});
+}
+
+static void launch_stepend(LSRKMem* m, STS_Problem p, int par, const double* Ys, const float* ds)
+{
+  const bool forced = p->kind == STS_PROBLEM_MANUFACTURED;
+  dim3 b(256, 1);
+  unsigned gx      = (unsigned)((p->nx + 255) / 256);
+  long long gy_cap = std::max<long long>(1, (long long)m->ctx->num_sms * 8 / gx);
+  unsigned gy      = (unsigned)std::min<long long>(p->ny, gy_cap);
+  dim3 g(gx, gy);
+  const int nxt = 1 - par;
+  RedWork* w    = m->ctx->d_work;
+  double* slot  = m->ctx->d_slots + SLOT_DSM;
+  dispatch_forced(forced, [&](auto F) {
+    if (m->mixed)
+      stepend_kernel<true, decltype(F)::value><<<g, b, 0, m->ctx->stream>>>(
+        p->dev, dstep(m), m->yb[par], nullptr, ds, m->Fb[par], m->yb[nxt], m->Fb[nxt], m->Ffb[nxt], w, slot);
+    else
+      stepend_kernel<false, decltype(F)::value><<<g, b, 0, m->ctx->stream>>>(
+        p->dev, dstep(m), m->yb[par], Ys, nullptr, m->Fb[par], nullptr, m->Fb[nxt], nullptr, w, slot);
+  });
+}
+
+// Record the whole step (parameter upload, s stages, step end) on the stream. Buffers
+// rotate Y_{j-1} -> Y_j through three stage buffers; in the FP64 form the last stage
+// writes into yb[1-par] so that acceptance only flips the parity.
+static void record_step(LSRKMem* m, STS_Problem p, int s, int par)
+{
+  cudaStream_t st = m->ctx->stream;
+  const long long n = m->n;
+  const int nxt     = 1 - par;
+  cudaMemcpyAsync(m->d_par, m->h_par, sizeof(StepArgs) + 8 + sizeof(StageArgs) * (size_t)(s + 1),
+                  cudaMemcpyHostToDevice, st);
+  const int eb = ew_blocks(m->ctx, n, 256 * 4);
+  if (!m->mixed)
+  {
+    // stage 1 into Y[0]; stages j = 2..s rotate Y[1], Y[2], Y[0], ...; the final stage
+    // writes yb[nxt]
+    double* bufs[3] = {m->Y[0], m->Y[1], m->Y[2]};
+    double* y1      = bufs[0];
+    stage1_64_kernel<<<eb, 256, 0, st>>>(n, dstep(m), m->yb[par], m->Fb[par], y1);
+    const double* ym2 = m->yb[par];
+    const double* ym1 = y1;
+    int bi            = 1;
+    for (int j = 2; j <= s; ++j)
+    {
+      double* yj = (j == s) ? m->yb[nxt] : bufs[bi];
+      bi         = (bi + 1) % 3;
+      launch_stage64(m, p, dstage(m) + j, ym1, ym2, m->yb[par], m->Fb[par], yj);
+      ym2 = ym1;
+      ym1 = yj;
+    }
+    launch_stepend(m, p, par, m->yb[nxt], nullptr);
+  }
+  else
+  {
+    float* bufs[3] = {m->D[0], m->D[1], m->D[2]};
+    stage1_32_kernel<<<eb, 256, 0, st>>>(n, dstep(m), m->Ffb[par], bufs[0]);
+    const float* dm2 = nullptr;
+    const float* dm1 = bufs[0];
+    int bi           = 1;
+    for (int j = 2; j <= s; ++j)
+    {
+      float* dj = bufs[bi];
+      bi        = (bi + 1) % 3;
+      launch_stage32(m, p, dstage(m) + j, dm1, dm2, m->Ffb[par], dj);
+      dm2 = dm1;
+      dm1 = dj;
+    }
+    launch_stepend(m, p, par, nullptr, dm1);
+  }
+}
+
+static int run_step_fused(LSRKMem* m, STS_Problem p, int s)
+{
+  cudaStream_t st = m->ctx->stream;
+  if (m->use_graphs)
+  {
+    GraphKey key{s, m->par};
+    auto it = m->graphs.find(key);
+    if (it == m->graphs.end())
+    {
+      cudaGraph_t g;
+      if (!STS_CUDA_OK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal))) return -1;
+      record_step(m, p, s, m->par);
+      if (!STS_CUDA_OK(cudaStreamEndCapture(st, &g))) return -1;
+      cudaGraphExec_t ge;
+      if (!STS_CUDA_OK(cudaGraphInstantiate(&ge, g, 0))) return -1;
+      cudaGraphDestroy(g);
+      it = m->graphs.emplace(key, ge).first;
+    }
+    if (!STS_CUDA_OK(cudaGraphLaunch(it->second, st))) return -1;
+  }
+  else record_step(m, p, s, m->par);
+  return STS_CUDA_OK(cudaGetLastError()) ? 0 : -1;
+}
+
+// fill the host parameter block for a step of size h with s stages from t
+static void fill_params(LSRKMem* m, STS_Problem p, double t, double h, int s, const std::vector<double>& mu,
+                        const std::vector<double>& nu, const std::vector<double>& mus,
+                        const std::vector<double>& ajm1, const std::vector<double>& cjm1)
+{
+  StepArgs* S = hstep(m);
+  S->hm1      = h * mus[1];
+  S->hm1f     = (float)(h * mus[1]);
+  S->p4h      = 0.4 * h;
+  S->rtol     = m->rtol;
+  S->atol     = m->atol;
+  {
+    const double c = sts_c(t + h), cd = sts_cdot(t + h);
+    S->al          = 1.0 * cd;
+    S->be          = -(1.0 * c) * p->kx;
+    S->ga          = -(1.0 * c) * p->ky;
+  }
+  const double c0 = sts_c(t), cd0 = sts_cdot(t);
+  StageArgs* A    = hstage(m);
+  for (int j = 2; j <= s; ++j)
+  {
+    StageArgs& a    = A[j];
+    const double hm = h * mus[j];
+    const double tj = t + h * cjm1[j];
+    const double tm = hm * p->cc;
+    a.gc            = mu[j] + tm;
+    a.gx            = hm * p->cx;
+    a.gy            = hm * p->cy;
+    a.gn            = nu[j];
+    a.g0            = (1.0 - mu[j]) - nu[j];
+    a.gf            = -(hm * ajm1[j]);
+    const double c = sts_c(tj), cd = sts_cdot(tj);
+    a.al            = hm * cd;
+    a.be            = -(hm * c) * p->kx;
+    a.ga            = -(hm * c) * p->ky;
+    a.gcf           = (float)a.gc;
+    a.gxf           = (float)a.gx;
+    a.gyf           = (float)a.gy;
+    a.gnf           = (float)a.gn;
+    a.gFf           = (float)(hm * (1.0 - ajm1[j]));
+    const double dc  = c - c0;
+    const double dcd = cd - cd0;
+    a.alf           = (float)(hm * dcd);
+    a.bef           = (float)(-(hm * dc) * p->kx);
+    a.gaf           = (float)(-(hm * dc) * p->ky);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// shared evolve logic
+// ---------------------------------------------------------------------------------------
+static int dee_update(LSRKMem* m, N_Vector ycur, N_Vector fcur)
+{
+  double lam = 0.0, lami = 0.0;
+  if (m->power)
+  {
+    STS_Problem p = (STS_Problem)m->user_data;
+    if (!m->evec)
+    {
+      if (!STS_CUDA_OK(cudaMalloc(&m->evec, m->n * sizeof(double)))) return -1;
+      cudaMemcpyAsync(m->evec, N_VGetDeviceArrayPointer_Sts(ycur), m->n * sizeof(double), cudaMemcpyDeviceToDevice,
+                      m->ctx->stream);
+    }
+    N_Vector ev = N_VMake_Sts(m->n, m->evec, m->ctx);
+    int it      = 0;
+    int rc      = STS_PowerIteration(p, ev, m->dee_maxiters, m->dee_reltol, &lam, &it);
+    N_VDestroy_Sts(ev);
+    if (rc) return -1;
+    m->nfe_dee += it;
+  }
+  else if (m->domeig)
+  {
+    if (!m->nv_tmp[0])
+      for (int k = 0; k < 3; ++k) m->nv_tmp[k] = N_VClone_Sts(ycur);
+    int rc = m->domeig(m->t, ycur, fcur, &lam, &lami, m->user_data, m->nv_tmp[0], m->nv_tmp[1], m->nv_tmp[2]);
+    if (rc) return -1;
+  }
+  else
+  {
+    sts_set_error("LSRKStep: no dominant eigenvalue function or estimator");
+    return -1;
+  }
+  m->rho = m->eig_safety * fabs(lam);
+  m->ndee++;
+  m->steps_since_dee = 0;
+  return 0;
+}
+
+// Initial step (Hairer, Norsett & Wanner II.4) with the probe capped at 1/rho.
+static double initial_step(LSRKMem* m, const double* y0, const double* F0, double tdist)
+{
+  STS_Context ctx = m->ctx;
+  const long long n = m->n;
+  double d0 = sts_wrms_ewt(ctx, y0, nullptr, y0, n, m->rtol, m->atol, SLOT_D0);
+  double d1 = sts_wrms_ewt(ctx, F0, nullptr, y0, n, m->rtol, m->atol, SLOT_D1);
+  double h0 = (d0 < 1.0e-5 || d1 < 1.0e-5) ? 1.0e-6 : 0.01 * (d0 / d1);
+  if (m->rho > 0.0 && h0 * m->rho > 1.0) h0 = 1.0 / m->rho;
+  if (h0 > tdist) h0 = tdist;
+  double *y1 = nullptr, *F1 = nullptr;
+  cudaMallocAsync(&y1, n * sizeof(double), ctx->stream);
+  cudaMallocAsync(&F1, n * sizeof(double), ctx->stream);
+  N_Vector vy1 = N_VMake_Sts(n, y1, ctx), vF1 = N_VMake_Sts(n, F1, ctx);
+  N_Vector vy0 = N_VMake_Sts(n, (double*)y0, ctx), vF0 = N_VMake_Sts(n, (double*)F0, ctx);
+  N_VLinearSum_Sts(h0, vF0, 1.0, vy0, vy1); // fma(h0, F0, 1*y0) = fma(h0, F0, y0)
+  int rc = m->rhs(m->t + h0, vy1, vF1, m->user_data);
+  m->nfe++;
+  double d2 = sts_wrms_ewt(ctx, F1, F0, y0, n, m->rtol, m->atol, SLOT_D2) / h0;
+  N_VDestroy_Sts(vy1);
+  N_VDestroy_Sts(vF1);
+  N_VDestroy_Sts(vy0);
+  N_VDestroy_Sts(vF0);
+  cudaFreeAsync(y1, ctx->stream);
+  cudaFreeAsync(F1, ctx->stream);
+  if (rc < 0) return -1.0;
+  const double dm = d1 > d2 ? d1 : d2;
+  double h1       = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : pow(0.01 / dm, 1.0 / ORD);
+  if (!(h1 > 0.0) || !(h1 < INFINITY)) h1 = h0;
+  double h = (100.0 * h0 < h1) ? 100.0 * h0 : h1;
+  if (h > tdist) h = tdist;
+  return h;
+}
+
+double sts_wrms_ewt(STS_Context ctx, const double* a, const double* b, const double* y, long long n, double rtol,
+                    double atol, int slot)
+{
+  ctx_activate(ctx);
+  const int g = ew_blocks(ctx, n, 256 * 4);
+  if (b) wrms_ewt_kernel<1><<<g, 256, 0, ctx->stream>>>(n, a, b, y, rtol, atol, ctx->d_work, ctx->d_slots + slot);
+  else wrms_ewt_kernel<0><<<g, 256, 0, ctx->stream>>>(n, a, b, y, rtol, atol, ctx->d_work, ctx->d_slots + slot);
+  if (!STS_CUDA_OK(cudaStreamSynchronize(ctx->stream))) return NAN;
+  return ((volatile double*)ctx->h_slots)[slot];
+}
+
+// controller update after an accepted step of size h with error dsm
+static void accept_control(LSRKMem* m, double h, double dsm)
+{
+  if (m->hfixed > 0.0)
+  {
+    m->hnext = m->hfixed;
+  }
+  else
+  {
+    double hn  = STS_AdaptControllerEstimate(m->controller, h, dsm, m->ep1, m->ep2, m->nhist);
+    double eta = SAFETY * hn / h;
+    double emx = (m->nst == 0) ? ETAMX1 : (m->after_fail ? 1.0 : GROWTH);
+    if (eta > emx) eta = emx;
+    if (eta >= LBOUND && eta <= UBOUND) eta = 1.0;
+    m->hnext = h * eta;
+    m->ep2   = m->ep1;
+    m->ep1   = dsm;
+    m->nhist++;
+  }
+  m->after_fail = false;
+}
+
+static void reject_control(LSRKMem* m, double h, double dsm, int nef)
+{
+  double hn  = STS_AdaptControllerEstimate(m->controller, h, dsm, m->ep1, m->ep2, m->nhist);
+  double eta = SAFETY * hn / h;
+  if (eta > 1.0) eta = 1.0;
+  if (nef >= SMALL_NEF && eta > ETAMXF) eta = ETAMXF;
+  if (eta < ETAMIN) eta = ETAMIN;
+  m->hnext      = h * eta;
+  m->after_fail = true;
+}
+
+// one attempt's stage count and step size (returns -2 if a fixed step needs > smax stages)
+static int choose_step(LSRKMem* m, double target, double* hout, int* sout, bool* clipped)
+{
+  double h = m->hnext, hmax;
+  *clipped = false;
+  int s    = STS_LSRKStagesNeeded(m->method, h, m->rho, m->smax, &hmax);
+  if (s > m->smax)
+  {
+    if (m->hfixed > 0.0)
+    {
+      sts_set_error("LSRKStep: fixed step needs %d stages > max %d", s, m->smax);
+      return -2;
+    }
+    h = hmax;
+    m->nst_exp++;
+  }
+  if (m->t + h >= target)
+  {
+    h        = target - m->t;
+    *clipped = true;
+  }
+  s     = STS_LSRKStagesNeeded(m->method, h, m->rho, m->smax, &hmax);
+  *hout = h;
+  *sout = s;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// fused evolve
+// ---------------------------------------------------------------------------------------
+static int evolve_fused(LSRKMem* m, double target, int itask)
+{
+  STS_Problem p   = (STS_Problem)m->user_data;
+  cudaStream_t st = m->ctx->stream;
+  const long long n = m->n;
+  if (ensure_stage_buffers(m) || ensure_par(m)) return STS_ERR_FAILURE;
+  if (!m->nv_y) m->nv_y = N_VMake_Sts(n, nullptr, m->ctx);
+  if (!m->nv_F) m->nv_F = N_VMake_Sts(n, nullptr, m->ctx);
+  NVC(m->nv_y)->nx = p->nx;
+  NVC(m->nv_y)->ny = p->ny;
+  if (!m->initialized)
+  {
+    sts_rhs_launch(p, m->t, m->yb[m->par], m->Fb[m->par], true, st);
+    m->nfe++;
+    if (m->mixed) sts_f64_to_f32(m->ctx, m->Fb[m->par], m->Ffb[m->par], n);
+    m->hnext           = (m->hfixed > 0.0) ? m->hfixed : 0.0;
+    m->initialized     = true;
+    m->steps_since_dee = -1;
+  }
+  std::vector<double> mu(m->smax + 1), nu(m->smax + 1), mus(m->smax + 1), ajm1(m->smax + 1), cjm1(m->smax + 1);
+  long long nsteps_call = 0;
+  int ret               = STS_SUCCESS;
+  while (m->t < target)
+  {
+    if (nsteps_call >= (m->maxsteps > 0 ? m->maxsteps : 500))
+    {
+      ret = STS_TOO_MUCH_WORK;
+      break;
+    }
+    NVC(m->nv_y)->data = m->yb[m->par];
+    NVC(m->nv_F)->data = m->Fb[m->par];
+    const long long freq = m->dom_eig_freq; // <= 0: computed once
+    if (m->steps_since_dee < 0 || (freq > 0 && m->steps_since_dee >= freq))
+      if (dee_update(m, m->nv_y, m->nv_F)) return STS_ERR_FAILURE;
+    if (!(m->hnext > 0.0))
+    {
+      double h0 = initial_step(m, m->yb[m->par], m->Fb[m->par], target - m->t);
+      if (!(h0 > 0.0)) return STS_ERR_FAILURE;
+      m->hnext = h0;
+    }
+    int nef = 0;
+    for (;;)
+    {
+      double h;
+      int s;
+      bool clipped;
+      int rc = choose_step(m, target, &h, &s, &clipped);
+      if (rc) return STS_ILL_INPUT;
+      STS_LSRKStageCoeffs(m->method, s, mu.data(), nu.data(), mus.data(), ajm1.data(), cjm1.data());
+      m->nst_att++;
+      fill_params(m, p, m->t, h, s, mu, nu, mus, ajm1, cjm1);
+      if (run_step_fused(m, p, s)) return STS_ERR_FAILURE;
+      if (!STS_CUDA_OK(cudaStreamSynchronize(st))) return STS_ERR_FAILURE;
+      const double dsm = ((volatile double*)m->ctx->h_slots)[SLOT_DSM];
+      m->nfe += s;
+      m->stages_total += s;
+      if (s > m->stage_max) m->stage_max = s;
+      m->last_s = s;
+      if (m->hfixed > 0.0 || dsm <= 1.0)
+      {
+        m->t     = clipped ? target : m->t + h;
+        m->par   = 1 - m->par;
+        m->hlast = h;
+        accept_control(m, h, dsm);
+        m->nst++;
+        m->steps_since_dee++;
+        nsteps_call++;
+        break;
+      }
+      m->netf++;
+      nef++;
+      if (!(dsm == dsm) || nef > 20) return STS_ERR_FAILURE;
+      reject_control(m, h, dsm, nef);
+    }
+    if (itask == STS_ONE_STEP) break;
+  }
+  return ret;
+}
+
+// ---------------------------------------------------------------------------------------
+// generic evolve (user RHS through N_Vector ops)
+// ---------------------------------------------------------------------------------------
+static int evolve_generic(LSRKMem* m, double target, int itask)
+{
+  N_Vector y = m->g_y, F = m->g_Fn;
+  if (!m->g_Y[0])
+  {
+    for (int k = 0; k < 3; ++k) m->g_Y[k] = N_VClone_Sts(y);
+    m->g_F    = N_VClone_Sts(y);
+    m->g_Fnew = N_VClone_Sts(y);
+    m->g_err  = N_VClone_Sts(y);
+    m->g_ewt  = N_VClone_Sts(y);
+  }
+  if (!m->initialized)
+  {
+    if (m->rhs(m->t, y, F, m->user_data) != 0) return STS_RHSFUNC_FAIL;
+    m->nfe++;
+    m->hnext           = (m->hfixed > 0.0) ? m->hfixed : 0.0;
+    m->initialized     = true;
+    m->steps_since_dee = -1;
+  }
+  std::vector<double> mu(m->smax + 1), nu(m->smax + 1), mus(m->smax + 1), ajm1(m->smax + 1), cjm1(m->smax + 1);
+  long long nsteps_call = 0;
+  int ret               = STS_SUCCESS;
+  while (m->t < target)
+  {
+    if (nsteps_call >= (m->maxsteps > 0 ? m->maxsteps : 500))
+    {
+      ret = STS_TOO_MUCH_WORK;
+      break;
+    }
+    const long long freq = m->dom_eig_freq; // <= 0: computed once
+    if (m->steps_since_dee < 0 || (freq > 0 && m->steps_since_dee >= freq))
+      if (dee_update(m, y, F)) return STS_ERR_FAILURE;
+    if (!(m->hnext > 0.0))
+    {
+      double h0 = initial_step(m, NVD(y), NVD(F), target - m->t);
+      if (!(h0 > 0.0)) return STS_ERR_FAILURE;
+      m->hnext = h0;
+    }
+    int nef = 0, ncf_step = 0;
+    for (;;)
+    {
+      double h;
+      int s;
+      bool clipped;
+      if (choose_step(m, target, &h, &s, &clipped)) return STS_ILL_INPUT;
+      STS_LSRKStageCoeffs(m->method, s, mu.data(), nu.data(), mus.data(), ajm1.data(), cjm1.data());
+      m->nst_att++;
+      // Y_1 = y_n + h mus_1 F_n
+      N_VLinearSum_Sts(h * mus[1], F, 1.0, y, m->g_Y[0]);
+      N_Vector ym2 = y, ym1 = m->g_Y[0], yj = m->g_Y[0];
+      int bi = 1, frc = 0;
+      for (int j = 2; j <= s && frc == 0; ++j)
+      {
+        frc = m->rhs(m->t + h * cjm1[j], ym1, m->g_F, m->user_data);
+        if (frc != 0) break;
+        yj             = m->g_Y[bi];
+        bi             = (bi + 1) % 3;
+        const double hm = h * mus[j];
+        double c[5]    = {mu[j], nu[j], (1.0 - mu[j]) - nu[j], hm, -(hm * ajm1[j])};
+        N_Vector X[5]  = {ym1, ym2, y, m->g_F, F};
+        N_VLinearCombination_Sts(5, c, X, yj);
+        ym2 = ym1;
+        ym1 = yj;
+      }
+      if (frc == 0) frc = m->rhs(m->t + h, yj, m->g_Fnew, m->user_data);
+      m->nfe += s;
+      if (frc < 0) return STS_RHSFUNC_FAIL;
+      if (frc > 0)
+      { // recoverable RHS failure (diffusion_2D.cpp:900-933 convention): retry with h/4
+        m->ncf++;
+        if (++ncf_step > 10) return STS_RHSFUNC_FAIL;
+        m->hnext      = 0.25 * h;
+        m->after_fail = true;
+        continue;
+      }
+      // err = 0.8 (y_n - y_{n+1}) + 0.4 h (F_n + F_{n+1}); ewt = 1/(rtol |y_n| + atol)
+      {
+        double c[4]   = {0.8, -0.8, 0.4 * h, 0.4 * h};
+        N_Vector X[4] = {y, yj, F, m->g_Fnew};
+        N_VLinearCombination_Sts(4, c, X, m->g_err);
+        N_VAbs_Sts(y, m->g_ewt);
+        N_VScale_Sts(m->rtol, m->g_ewt, m->g_ewt);
+        N_VAddConst_Sts(m->g_ewt, m->atol, m->g_ewt);
+        N_VInv_Sts(m->g_ewt, m->g_ewt);
+      }
+      const double dsm = N_VWrmsNorm_Sts(m->g_err, m->g_ewt);
+      m->stages_total += s;
+      if (s > m->stage_max) m->stage_max = s;
+      if (m->hfixed > 0.0 || dsm <= 1.0)
+      {
+        m->t = clipped ? target : m->t + h;
+        cudaMemcpyAsync(NVD(y), NVD(yj), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
+        cudaMemcpyAsync(NVD(F), NVD(m->g_Fnew), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
+        m->hlast = h;
+        accept_control(m, h, dsm);
+        m->nst++;
+        m->steps_since_dee++;
+        nsteps_call++;
+        break;
+      }
+      m->netf++;
+      nef++;
+      if (!(dsm == dsm) || nef > 20) return STS_ERR_FAILURE;
+      reject_control(m, h, dsm, nef);
+    }
+    if (itask == STS_ONE_STEP) break;
+  }
+  return ret;
+}
+
+// ---------------------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------------------
+#define MEM(v) ((LSRKMem*)(v))
+#define CHECK_MEM(v)                                  \
+  do                                                  \
+  {                                                   \
+    if (!(v))                                         \
+    {                                                 \
+      sts_set_error("LSRKStep: NULL integrator memory"); \
+      return STS_MEM_NULL;                            \
+    }                                                 \
+  } while (0)
+
+extern "C" void* STS_LSRKStepCreateSTS(STS_ARKRhsFn rhs, double t0, N_Vector y0, STS_Context ctx)
+{
+  if (!rhs || !y0 || !ctx)
+  {
+    sts_set_error("LSRKStepCreateSTS: NULL argument");
+    return nullptr;
+  }
+  ctx_activate(ctx);
+  LSRKMem* m = new LSRKMem();
+  m->ctx     = ctx;
+  m->rhs     = rhs;
+  m->t       = t0;
+  m->n       = NVL(y0);
+  m->g_y     = N_VClone_Sts(y0);
+  m->g_Fn    = N_VClone_Sts(y0);
+  if (!m->g_y || !m->g_Fn)
+  {
+    delete m;
+    return nullptr;
+  }
+  cudaMemcpyAsync(NVD(m->g_y), NVD(y0), m->n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  return m;
+}
+
+extern "C" int STS_LSRKStepSetSTSMethod(void* mem, int method)
+{
+  CHECK_MEM(mem);
+  if (method != STS_LSRK_RKC_2 && method != STS_LSRK_RKL_2) return STS_ILL_INPUT;
+  MEM(mem)->method = method;
+  return 0;
+}
+extern "C" int STS_ARKodeSStolerances(void* mem, double rtol, double atol)
+{
+  CHECK_MEM(mem);
+  if (rtol < 0 || atol < 0) return STS_ILL_INPUT;
+  MEM(mem)->rtol = rtol;
+  MEM(mem)->atol = atol;
+  return 0;
+}
+extern "C" int STS_ARKodeSetUserData(void* mem, void* ud)
+{
+  CHECK_MEM(mem);
+  MEM(mem)->user_data = ud;
+  return 0;
+}
+extern "C" int STS_LSRKStepSetDomEigFn(void* mem, STS_ARKDomEigFn fn)
+{
+  CHECK_MEM(mem);
+  MEM(mem)->domeig = fn;
+  MEM(mem)->power  = false;
+  return 0;
+}
+extern "C" int STS_LSRKStepSetDomEigEstimatorPower(void* mem, int maxiters, double reltol)
+{
+  CHECK_MEM(mem);
+  MEM(mem)->power        = true;
+  MEM(mem)->dee_maxiters = maxiters > 0 ? maxiters : 100;
+  MEM(mem)->dee_reltol   = reltol > 0 ? reltol : 0.01;
+  return 0;
+}
+extern "C" int STS_LSRKStepSetDomEigFrequency(void* mem, long long nsteps)
+{
+  CHECK_MEM(mem);
+  MEM(mem)->dom_eig_freq = nsteps;
+  return 0;
+}
+extern "C" int STS_LSRKStepSetMaxNumStages(void* mem, int smax)
+{
+  CHECK_MEM(mem);
+  if (smax < 2) return STS_ILL_INPUT;
+  MEM(mem)->smax = smax;
+  return 0;
+}
+extern "C" int STS_LSRKStepSetDomEigSafetyFactor(void* mem, double safety)
+{
+  CHECK_MEM(mem);
+  if (safety < 1.0) return STS_ILL_INPUT;
+  MEM(mem)->eig_safety = safety;
+  return 0;
+}
+extern "C" int STS_ARKodeSetAdaptController(void* mem, int controller)
+{
+  CHECK_MEM(mem);
+  if (controller < 0 || controller > 2) return STS_ILL_INPUT;
+  MEM(mem)->controller = controller;
+  return 0;
+}
+extern "C" int STS_ARKodeSetFixedStep(void* mem, double h)
+{
+  CHECK_MEM(mem);
+  MEM(mem)->hfixed = h;
+  if (h > 0.0) MEM(mem)->hnext = h;
+  return 0;
+}
+extern "C" int STS_ARKodeSetMaxNumSteps(void* mem, long long mxsteps)
+{
+  CHECK_MEM(mem);
+  MEM(mem)->maxsteps = mxsteps;
+  return 0;
+}
+extern "C" int STS_ARKodeSetStopTime(void* mem, double tstop)
+{
+  CHECK_MEM(mem);
+  MEM(mem)->tstop = tstop;
+  return 0;
+}
+extern "C" int STS_LSRKStepSetMixedPrecision(void* mem, int on)
+{
+  CHECK_MEM(mem);
+  if (MEM(mem)->initialized && MEM(mem)->mixed != (on != 0))
+  {
+    sts_set_error("LSRKStep: precision must be chosen before the first evolve");
+    return STS_ILL_INPUT;
+  }
+  MEM(mem)->mixed = on != 0;
+  return 0;
+}
+extern "C" int STS_LSRKStepSetUseGraphs(void* mem, int on)
+{
+  CHECK_MEM(mem);
+  MEM(mem)->use_graphs = on != 0;
+  return 0;
+}
+
+extern "C" int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* tret, int itask)
+{
+  CHECK_MEM(mem);
+  LSRKMem* m = MEM(mem);
+  if (!yout || NVL(yout) != m->n)
+  {
+    sts_set_error("ARKodeEvolve: output vector length mismatch");
+    return STS_ILL_INPUT;
+  }
+  ctx_activate(m->ctx);
+  double target = tout < m->tstop ? tout : m->tstop;
+  int ret;
+  if (fused(m))
+  {
+    if (!m->yb[0])
+    {
+      if (m->mixed && ((STS_Problem)m->user_data)->kind == STS_PROBLEM_PERIODIC) return STS_ILL_INPUT;
+      if (alloc_fused(m, NVD(m->g_y))) return STS_ERR_FAILURE;
+    }
+    ret = evolve_fused(m, target, itask);
+    cudaMemcpyAsync(NVD(yout), m->yb[m->par], m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
+  }
+  else
+  {
+    ret = evolve_generic(m, target, itask);
+    cudaMemcpyAsync(NVD(yout), NVD(m->g_y), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
+  }
+  if (!STS_CUDA_OK(cudaStreamSynchronize(m->ctx->stream))) return STS_ERR_FAILURE;
+  if (tret) *tret = m->t;
+  if (ret == STS_SUCCESS && m->t >= m->tstop) ret = STS_TSTOP_RETURN;
+  return ret;
+}
+
+extern "C" int STS_ARKodeReset(void* mem, double t, N_Vector y)
+{
+  CHECK_MEM(mem);
+  LSRKMem* m = MEM(mem);
+  if (!y || NVL(y) != m->n) return STS_ILL_INPUT;
+  ctx_activate(m->ctx);
+  m->t = t;
+  if (fused(m) && m->yb[0])
+  {
+    if (!STS_CUDA_OK(cudaMemcpyAsync(m->yb[m->par], NVD(y), m->n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     m->ctx->stream)))
+      return STS_ERR_FAILURE;
+  }
+  else if (!STS_CUDA_OK(cudaMemcpyAsync(NVD(m->g_y), NVD(y), m->n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                        m->ctx->stream)))
+    return STS_ERR_FAILURE;
+  if (m->initialized)
+  { // F(t, y) for the restarted state
+    if (fused(m))
+    {
+      STS_Problem p = (STS_Problem)m->user_data;
+      sts_rhs_launch(p, m->t, m->yb[m->par], m->Fb[m->par], true, m->ctx->stream);
+      if (m->mixed) sts_f64_to_f32(m->ctx, m->Fb[m->par], m->Ffb[m->par], m->n);
+    }
+    else if (m->rhs(m->t, m->g_y, m->g_Fn, m->user_data) != 0)
+      return STS_RHSFUNC_FAIL;
+    m->nfe++;
+  }
+  return STS_CUDA_OK(cudaStreamSynchronize(m->ctx->stream)) ? 0 : STS_ERR_FAILURE;
+}
+
+extern "C" int STS_LSRKStepTimeStageKernel(void* mem, int nlaunch, double* ms_per_launch)
+{
+  CHECK_MEM(mem);
+  LSRKMem* m = MEM(mem);
+  if (!fused(m) || m->last_s < 2 || nlaunch < 1 || !ms_per_launch) return STS_ILL_INPUT;
+  ctx_activate(m->ctx);
+  STS_Problem p   = (STS_Problem)m->user_data;
+  cudaStream_t st = m->ctx->stream;
+  const int j     = m->last_s / 2 > 2 ? m->last_s / 2 : 2;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  // the parameter block of the last step is still on the device
+  auto one = [&](int k) {
+    if (m->mixed) launch_stage32(m, p, dstage(m) + j, m->D[k % 3], m->D[(k + 1) % 3], m->Ffb[m->par], m->D[(k + 2) % 3]);
+    else launch_stage64(m, p, dstage(m) + j, m->Y[k % 3], m->Y[(k + 1) % 3], m->yb[m->par], m->Fb[m->par], m->Y[(k + 2) % 3]);
+  };
+  one(0); // warm
+  cudaEventRecord(e0, st);
+  for (int k = 0; k < nlaunch; ++k) one(k);
+  cudaEventRecord(e1, st);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms_per_launch = (double)ms / nlaunch;
+  return STS_CUDA_OK(cudaGetLastError()) ? 0 : STS_ERR_FAILURE;
+}
+
+extern "C" int STS_ARKodeGetStats(void* mem, STS_Stats* s)
+{
+  CHECK_MEM(mem);
+  LSRKMem* m        = MEM(mem);
+  s->nst            = m->nst;
+  s->nst_attempts   = m->nst_att;
+  s->netf           = m->netf;
+  s->nfe            = m->nfe;
+  s->nfe_dee        = m->nfe_dee;
+  s->ndee           = m->ndee;
+  s->nst_exp        = m->nst_exp;
+  s->stage_max      = m->stage_max;
+  s->stages_total   = m->stages_total;
+  s->t              = m->t;
+  s->hlast          = m->hlast;
+  s->hnext          = m->hnext;
+  s->spectral_radius = m->rho;
+  return 0;
+}
+
+// table format of ARKodePrintAllStats (main.cpp:486) for the counters this integrator keeps
+extern "C" int STS_ARKodePrintAllStats(void* mem, char* buf, int buflen)
+{
+  CHECK_MEM(mem);
+  LSRKMem* m = MEM(mem);
+  int k      = snprintf(buf, buflen,
+                        "Current time                  = %.16g\n"
+                        "Steps                         = %lld\n"
+                        "Step attempts                 = %lld\n"
+                        "Stability limited steps       = %lld\n"
+                        "Error test fails              = %lld\n"
+                        "RHS fn evals                  = %lld\n"
+                        "Number of dom_eig updates     = %lld\n"
+                        "Max. num. of stages used      = %lld\n"
+                        "Last step size                = %.16g\n"
+                        "Current step size             = %.16g\n",
+                        m->t, m->nst, m->nst_att, m->nst_exp, m->netf, m->nfe + m->nfe_dee, m->ndee,
+                        m->stage_max, m->hlast, m->hnext);
+  return k < buflen ? 0 : -1;
+}
+
+extern "C" void STS_ARKodeFree(void** mem)
+{
+  if (!mem || !*mem) return;
+  LSRKMem* m = MEM(*mem);
+  ctx_activate(m->ctx);
+  cudaStreamSynchronize(m->ctx->stream);
+  free_device(m);
+  delete m;
+  *mem = nullptr;
+}
+
+// ---------------------------------------------------------------------------------------
+__global__ void f64_to_f32_kernel(long long n, const double* __restrict__ a, float* __restrict__ b)
+{
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) b[k] = (float)a[k];
+}
+
+void sts_f64_to_f32(STS_Context ctx, const double* a, float* b, long long n)
+{
+  f64_to_f32_kernel<<<ew_blocks(ctx, n, 256 * 4), 256, 0, ctx->stream>>>(n, a, b);
+}

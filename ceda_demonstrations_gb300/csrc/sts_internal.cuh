@@ -1,0 +1,195 @@
+// Internal declarations shared by the translation units of libstsgpu.so.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "../../include/stsgpu.h"
+#include "xsum.cuh"
+
+// ---------------------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------------------
+void sts_set_error(const char* fmt, ...);
+
+#define STS_CUDA_OK(call)                                                                  \
+  ([&]() -> bool {                                                                         \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+    {                                                                                      \
+      sts_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));    \
+      return false;                                                                        \
+    }                                                                                      \
+    return true;                                                                           \
+  }())
+
+// ---------------------------------------------------------------------------------------
+// context: stream + reduction workspace. Each reduction kernel adds its per-block partial
+// limbs into `limbs` with integer atomics, takes a ticket, and the last block converts the
+// total into a double written to a result slot (mapped pinned host memory) and clears the
+// workspace for the next reduction on the stream.
+// ---------------------------------------------------------------------------------------
+constexpr int STS_NSLOTS = 16;
+enum ResultSlot {
+  SLOT_GENERIC = 0,
+  SLOT_DSM     = 1,
+  SLOT_D0      = 2,
+  SLOT_D1      = 3,
+  SLOT_D2      = 4,
+  SLOT_LAM     = 5,
+  SLOT_NRM     = 6,
+  SLOT_PCG0    = 8,
+  SLOT_PCG1    = 9,
+  SLOT_PCG2    = 10,
+  SLOT_PCG3    = 11,
+};
+
+struct RedWork {
+  unsigned long long limbs[xsum::NL];
+  unsigned long long maxbits;
+  unsigned int flags;
+  unsigned int ticket;
+};
+
+struct STS_Context_ {
+  int device        = 0;
+  int num_sms       = 0;
+  cudaStream_t stream = nullptr;
+  RedWork* d_work   = nullptr;    // device
+  double* h_slots   = nullptr;    // pinned, mapped
+  double* d_slots   = nullptr;    // device alias of h_slots
+};
+
+bool ctx_activate(STS_Context ctx);
+
+// grid size for grid-stride elementwise / reduction kernels
+inline int ew_blocks(STS_Context ctx, long long n, int per_block)
+{
+  long long b = (n + per_block - 1) / per_block;
+  long long cap = (long long)ctx->num_sms * 8;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+// ---------------------------------------------------------------------------------------
+// device-side reduction helpers
+// ---------------------------------------------------------------------------------------
+#ifdef __CUDACC__
+__device__ __forceinline__ long long shfl_xor_ll(long long v, int m)
+{
+  return (long long)__shfl_xor_sync(0xffffffffu, (unsigned long long)v, m);
+}
+
+// Block-level combine of per-thread limbs, then global atomics + last-block finalisation.
+// Every thread of the block must call it. `post` selects the final transform:
+//   0: value, 1: sqrt(value / n) (WRMS). The result goes to slot_out.
+template <int NT>
+__device__ __forceinline__ void xsum_block_finish(xsum::Limbs& a, unsigned flags, RedWork* w,
+                                                  double* slot_out, int post, double n)
+{
+  __shared__ long long sm[NT / 32][xsum::NL];
+  __shared__ unsigned sflags;
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) sflags = 0;
+#pragma unroll
+  for (int k = 0; k < xsum::NL; ++k)
+  {
+    long long v = a.l[k];
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) v += shfl_xor_ll(v, m);
+    if (lane == 0) sm[warp][k] = v;
+  }
+  __syncthreads();
+  if (flags) atomicOr(&sflags, flags);
+  if (warp == 0)
+  {
+#pragma unroll
+    for (int k = 0; k < xsum::NL; ++k)
+    {
+      long long v = (lane < NT / 32) ? sm[lane][k] : 0LL;
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) v += shfl_xor_ll(v, m);
+      if (lane == 0 && v != 0) atomicAdd(&w->limbs[k], (unsigned long long)v);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    if (sflags) atomicOr(&w->flags, sflags);
+    __threadfence();
+    unsigned t = atomicAdd(&w->ticket, 1u);
+    last       = (t == gridDim.x * gridDim.y * gridDim.z - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0)
+  {
+    __threadfence();
+    long long tot[xsum::NL];
+#pragma unroll
+    for (int k = 0; k < xsum::NL; ++k)
+    {
+      tot[k]       = (long long)atomicAdd(&w->limbs[k], 0ULL);
+      w->limbs[k]  = 0ULL;
+    }
+    unsigned f = atomicOr(&w->flags, 0u);
+    double v   = xsum::finalize(tot, f);
+    if (post == 1) v = sqrt(v / n);
+    *slot_out = v;
+    w->flags  = 0u;
+    w->ticket = 0u;
+    __threadfence();
+  }
+}
+#endif
+
+// ---------------------------------------------------------------------------------------
+// problem
+// ---------------------------------------------------------------------------------------
+struct ProbDev {
+  long long nx, ny;
+  int kind, inhom;
+  double kx, ky, cx, cy, cc;
+  const double *Sx, *Sxx, *Sy, *Syy;
+  const float *Sxf, *Sxxf, *Syf, *Syyf;
+  const double *Dxw, *Dxe, *Dys, *Dyn;
+};
+
+struct STS_Problem_ {
+  STS_Context ctx = nullptr;
+  int kind = 0, inhom = 0;
+  long long nx = 0, ny = 0;
+  double kx = 1, ky = 1, xl = 0, xu = 1, yl = 0, yu = 1, dx = 0, dy = 0, cx = 0, cy = 0, cc = 0;
+  double* d_tab   = nullptr; // Sx | Sxx | Sy | Syy | Dxw | Dxe | Dys | Dyn (doubles)
+  float* d_tabf   = nullptr; // Sxf | Sxxf | Syf | Syyf
+  double* d_jacobi = nullptr; // PSetup output (constant Jacobi scale, 1 entry)
+  double jacobi_scale = 1.0;
+  ProbDev dev{};
+};
+
+static inline double sts_c(double t)
+{
+  double cs = cos(2.0 * 3.14159265358979323846 * t);
+  return cs * cs;
+}
+static inline double sts_cdot(double t) { return -2.0 * 3.14159265358979323846 * sin(4.0 * 3.14159265358979323846 * t); }
+
+// N_Vector content
+struct NVContent {
+  long long length = 0;
+  long long nx = 0, ny = 0;
+  bool own = false;
+  double* data = nullptr;
+};
+inline NVContent* NVC(N_Vector v) { return (NVContent*)v->content; }
+inline double* NVD(N_Vector v) { return NVC(v)->data; }
+inline long long NVL(N_Vector v) { return NVC(v)->length; }
+
+// problem-level kernels used by the integrator and the solvers (diffusion.cu)
+int sts_rhs_launch(STS_Problem p, double t, const double* u, double* f, bool forcing, cudaStream_t s);
+double sts_dot_exact(STS_Context ctx, const double* x, const double* y, long long n, int slot);
+double sts_wrms_ewt(STS_Context ctx, const double* a, const double* b, const double* y, long long n,
+                    double rtol, double atol, int slot);

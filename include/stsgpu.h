@@ -1,0 +1,246 @@
+/* stsgpu.h — C ABI of the GB300 (sm_103a) diffusion_2D super-time-stepping library.
+ *
+ * The entry points mirror the interfaces through which the reference's diffusion_2D
+ * driver reaches its hot path (SUNDIALS ARKODE/LSRKStep, NVECTOR, SUNLinearSolver and the
+ * problem callbacks). Each declaration names the reference interface it replaces
+ * (file:line, paths relative to the sundials-codes/ceda-demonstrations tree). SUNDIALS is
+ * an empty submodule there, so SUNDIALS functions are cited at their call sites in
+ * diffusion_2D/main.cpp and gkeyll_diffusion/*.c.
+ *
+ * Conventions
+ *   - plain C types only: double, float, int, long long, opaque handles, raw pointers;
+ *   - all vector data lives in device (HBM) memory; N_Vector ops are asynchronous on the
+ *     context's CUDA stream except reductions, which synchronise and return host doubles;
+ *   - functions returning int use 0 = success, > 0 = recoverable, < 0 = failure
+ *     (the ARKODE / callback convention of diffusion_2D.cpp:900-933);
+ *   - constructors return NULL on failure; STS_GetLastError() gives the reason.
+ */
+#ifndef STSGPU_H
+#define STSGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef long long sts_index; /* sunindextype (64-bit index build) */
+
+/* ------------------------------------------------------------------------------------
+ * Context. Replaces SUNContext (SUNContext_Create, diffusion_2D/main.cpp:79): owns the
+ * CUDA stream and the reduction workspace of one device.
+ * ----------------------------------------------------------------------------------*/
+typedef struct STS_Context_* STS_Context;
+int STS_ContextCreate(int device, STS_Context* ctx);
+int STS_ContextFree(STS_Context* ctx);
+int STS_ContextSynchronize(STS_Context ctx);
+void* STS_ContextGetStream(STS_Context ctx); /* cudaStream_t */
+const char* STS_GetLastError(void);
+int STS_DeviceCount(void);
+
+/* ------------------------------------------------------------------------------------
+ * N_Vector (device). Layout {content, ops, sunctx} as SUNDIALS' generic N_Vector; the ops
+ * table holds the subset LSRKStep, the PCG solver and the Jacobi PSolve use
+ * (gkeyll_diffusion/src/nvector_gkylzero.c:45-60, + nvprod for
+ * diffusion_2D/preconditioner_jacobi.cpp:58, + nvlinearcombination).
+ * ----------------------------------------------------------------------------------*/
+typedef struct _generic_N_Vector* N_Vector;
+typedef struct _generic_N_Vector_Ops* N_Vector_Ops;
+
+struct _generic_N_Vector_Ops {
+  N_Vector (*nvclone)(N_Vector);
+  N_Vector (*nvcloneempty)(N_Vector);
+  void (*nvdestroy)(N_Vector);
+  void (*nvspace)(N_Vector, sts_index*, sts_index*);
+  double* (*nvgetarraypointer)(N_Vector);
+  sts_index (*nvgetlength)(N_Vector);
+  void (*nvlinearsum)(double, N_Vector, double, N_Vector, N_Vector);
+  void (*nvconst)(double, N_Vector);
+  void (*nvprod)(N_Vector, N_Vector, N_Vector);
+  void (*nvdiv)(N_Vector, N_Vector, N_Vector);
+  void (*nvscale)(double, N_Vector, N_Vector);
+  void (*nvabs)(N_Vector, N_Vector);
+  void (*nvinv)(N_Vector, N_Vector);
+  void (*nvaddconst)(N_Vector, double, N_Vector);
+  double (*nvdotprod)(N_Vector, N_Vector);
+  double (*nvmaxnorm)(N_Vector);
+  double (*nvwrmsnorm)(N_Vector, N_Vector);
+  int (*nvlinearcombination)(int, double*, N_Vector*, N_Vector);
+};
+
+struct _generic_N_Vector {
+  void* content;
+  N_Vector_Ops ops;
+  STS_Context sunctx;
+};
+
+/* N_VNew_Parallel (diffusion_2D/main.cpp:176): owned device vector, zero-filled */
+N_Vector N_VNew_Sts(sts_index length, STS_Context ctx);
+/* N_VNewEmpty_Gkylzero (nvector_gkylzero.c:32-82) */
+N_Vector N_VNewEmpty_Sts(STS_Context ctx);
+/* N_VMake_Gkylzero (nvector_gkylzero.c:85-99): wrap caller-owned device memory */
+N_Vector N_VMake_Sts(sts_index length, double* device_data, STS_Context ctx);
+/* N_VCloneEmpty/Clone/Destroy_Gkylzero (nvector_gkylzero.c:111-203) */
+N_Vector N_VCloneEmpty_Sts(N_Vector w);
+N_Vector N_VClone_Sts(N_Vector w);
+void N_VDestroy_Sts(N_Vector v);
+/* N_VGetArrayPointer (diffusion_2D/diffusion.cpp:24,27): DEVICE pointer */
+double* N_VGetDeviceArrayPointer_Sts(N_Vector v);
+sts_index N_VGetLength_Sts(N_Vector v);
+/* N_VSpace_Gkylzero (nvector_gkylzero.c:407-411) */
+void N_VSpace_Sts(N_Vector v, sts_index* lrw, sts_index* liw);
+/* 2-D shape (nx fastest, IDX(i,j,nx) = nx*j + i, diffusion_2D.hpp:55); informational */
+int N_VSetShape_Sts(N_Vector v, sts_index nx, sts_index ny);
+/* host <-> device copies (synchronous on the context stream) */
+int N_VCopyFromHost_Sts(N_Vector v, const double* host);
+int N_VCopyToHost_Sts(N_Vector v, double* host);
+
+/* nvector_gkylzero.c:205-514 */
+void N_VLinearSum_Sts(double a, N_Vector x, double b, N_Vector y, N_Vector z);
+void N_VConst_Sts(double c, N_Vector z);
+void N_VProd_Sts(N_Vector x, N_Vector y, N_Vector z);
+void N_VDiv_Sts(N_Vector x, N_Vector y, N_Vector z);
+void N_VScale_Sts(double c, N_Vector x, N_Vector z);
+void N_VAbs_Sts(N_Vector x, N_Vector z);
+void N_VInv_Sts(N_Vector x, N_Vector z);
+void N_VAddConst_Sts(N_Vector x, double b, N_Vector z);
+/* reductions: exact, order-independent accumulation (terms truncated to 2^-160, summed
+ * exactly, rounded once); the values do not depend on the launch shape */
+double N_VDotProd_Sts(N_Vector x, N_Vector y);
+double N_VMaxNorm_Sts(N_Vector x);
+double N_VWrmsNorm_Sts(N_Vector x, N_Vector w);
+int N_VLinearCombination_Sts(int nvec, double* c, N_Vector* X, N_Vector z);
+
+/* ------------------------------------------------------------------------------------
+ * Problem and callbacks (diffusion_2D). STS_Problem replaces UserData
+ * (diffusion_2D/diffusion_2D.hpp:66-214) for the single-device case.
+ * ----------------------------------------------------------------------------------*/
+#define STS_PROBLEM_MANUFACTURED 0 /* [0,1]^2 Dirichlet, u = sin^2(pi x) sin^2(pi y) cos^2(2 pi t) */
+#define STS_PROBLEM_UNFORCED 1     /* [0,1]^2 Dirichlet, no forcing */
+#define STS_PROBLEM_PERIODIC 2     /* reference mode: periodic, initial.cpp:42-43 IC */
+
+typedef struct STS_Problem_* STS_Problem;
+STS_Problem STS_ProblemCreate(STS_Context ctx, int kind, sts_index nx, sts_index ny, double kx,
+                              double ky, int inhomogeneous, double xl, double xu, double yl,
+                              double yu);
+int STS_ProblemFree(STS_Problem* p);
+int STS_ProblemGetInfo(STS_Problem p, double* dx, double* dy, double* cx, double* cy);
+/* Initial (diffusion_2D/initial.cpp:20-47) */
+int STS_Initial(double t, N_Vector u, STS_Problem p);
+/* sum_k a_k sin(p_k pi x) sin(q_k pi y) (batched initial condition) */
+int STS_InitialModes(N_Vector u, STS_Problem p, int nmodes, const int* pm, const int* qm,
+                     const double* amp);
+int STS_Exact(double t, N_Vector u, STS_Problem p);
+/* ARKRhsFn diffusion (diffusion_2D/diffusion_2D.cpp:23-35 -> diffusion.cpp:9-209) */
+int STS_Diffusion(double t, N_Vector u, N_Vector f, void* user_data);
+/* J v = A v (the RHS is affine) */
+int STS_JacTimes(N_Vector v, N_Vector Jv, double t, N_Vector y, N_Vector fy, void* user_data,
+                 N_Vector tmp);
+/* ARKDomEigFn dom_eig (diffusion_2D/main.cpp:536-550) */
+int STS_DomEig(double t, N_Vector y, N_Vector fn, double* lambdaR, double* lambdaI,
+               void* user_data, N_Vector temp1, N_Vector temp2, N_Vector temp3);
+/* SUNDomEigEstimator_Power (diffusion_2D/main.cpp:344): power iteration on A from v */
+int STS_PowerIteration(STS_Problem p, N_Vector v, int maxiters, double reltol, double* lambda,
+                       int* iters);
+/* ARKLsPrecSetupFn / ARKLsPrecSolveFn (diffusion_2D/preconditioner_jacobi.cpp:9-61) */
+int STS_PSetup(double t, N_Vector u, N_Vector f, int jok, int* jcurPtr, double gamma,
+               void* user_data);
+int STS_PSolve(double t, N_Vector u, N_Vector f, N_Vector r, N_Vector z, double gamma,
+               double delta, int lr, void* user_data);
+
+/* ------------------------------------------------------------------------------------
+ * LSRKStep STS integrator (ARKODE). Replaces LSRKStepCreateSTS and the ARKode* calls of
+ * diffusion_2D/main.cpp:257-400,442,486. When the RHS is STS_Diffusion with an STS_Problem
+ * as user data, stages run as fused stencil+stage kernels; any other ARKRhsFn runs through
+ * the N_Vector ops (generic path).
+ * ----------------------------------------------------------------------------------*/
+typedef int (*STS_ARKRhsFn)(double t, N_Vector y, N_Vector ydot, void* user_data);
+typedef int (*STS_ARKDomEigFn)(double t, N_Vector y, N_Vector fn, double* lambdaR,
+                               double* lambdaI, void* user_data, N_Vector temp1,
+                               N_Vector temp2, N_Vector temp3);
+
+#define STS_LSRK_RKC_2 0 /* ARKODE_LSRK_RKC_2 */
+#define STS_LSRK_RKL_2 1 /* ARKODE_LSRK_RKL_2 */
+#define STS_ADAPT_PID 0  /* ARK_ADAPT_PID */
+#define STS_ADAPT_PI 1   /* ARK_ADAPT_PI */
+#define STS_ADAPT_I 2    /* ARK_ADAPT_I */
+#define STS_NORMAL 1     /* ARK_NORMAL */
+#define STS_ONE_STEP 2   /* ARK_ONE_STEP */
+#define STS_SUCCESS 0
+#define STS_TSTOP_RETURN 1
+#define STS_TOO_MUCH_WORK -1
+#define STS_ERR_FAILURE -3
+#define STS_RHSFUNC_FAIL -8
+#define STS_ILL_INPUT -22
+#define STS_MEM_NULL -21
+
+typedef struct STS_Stats {
+  long long nst, nst_attempts, netf, nfe, nfe_dee, ndee, nst_exp, stage_max, stages_total;
+  double t, hlast, hnext, spectral_radius;
+} STS_Stats;
+
+void* STS_LSRKStepCreateSTS(STS_ARKRhsFn rhs, double t0, N_Vector y0, STS_Context ctx); /* main.cpp:257 */
+int STS_LSRKStepSetSTSMethod(void* mem, int method);                 /* main.cpp:336-338 */
+int STS_ARKodeSStolerances(void* mem, double rtol, double atol);      /* main.cpp:262 */
+int STS_ARKodeSetUserData(void* mem, void* user_data);                /* main.cpp:266 */
+int STS_LSRKStepSetDomEigFn(void* mem, STS_ARKDomEigFn fn);           /* main.cpp:352 */
+int STS_LSRKStepSetDomEigEstimatorPower(void* mem, int maxiters, double reltol); /* main.cpp:344-348 */
+int STS_LSRKStepSetDomEigFrequency(void* mem, long long nsteps);      /* gk_diffusion_1x1v_p1.c / analytic_CR_test.c:320 */
+int STS_LSRKStepSetMaxNumStages(void* mem, int smax);                 /* analytic_CR_test.c:324 */
+int STS_LSRKStepSetDomEigSafetyFactor(void* mem, double safety);      /* analytic_CR_test.c:332 */
+int STS_ARKodeSetAdaptController(void* mem, int controller);          /* main.cpp:366-376 */
+int STS_ARKodeSetFixedStep(void* mem, double h);                      /* main.cpp:361 */
+int STS_ARKodeSetMaxNumSteps(void* mem, long long mxsteps);           /* main.cpp:380 */
+int STS_ARKodeSetStopTime(void* mem, double tstop);                   /* main.cpp:384 */
+/* new: FP32 stage increments relative to the FP64 step-start state (fused path only) */
+int STS_LSRKStepSetMixedPrecision(void* mem, int on);
+/* new: capture the fixed-s stage loop of the fused path in CUDA graphs (default on) */
+int STS_LSRKStepSetUseGraphs(void* mem, int on);
+int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* tret, int itask); /* main.cpp:442 */
+/* ARKodeReset: restart from (t, y) keeping options, counters and the step size; F(t, y) is
+ * re-evaluated on the next step */
+int STS_ARKodeReset(void* mem, double t, N_Vector y);
+/* CUDA-event timing of the fused stage kernel on the integrator's current buffers (after at
+ * least one evolve): average milliseconds per launch over nlaunch launches of stage j = s/2
+ * of the last step, launched on the context stream exactly as the integrator does */
+int STS_LSRKStepTimeStageKernel(void* mem, int nlaunch, double* ms_per_launch);
+int STS_ARKodeGetStats(void* mem, STS_Stats* stats);                  /* ARKodePrintAllStats main.cpp:486 */
+int STS_ARKodePrintAllStats(void* mem, char* buf, int buflen);
+void STS_ARKodeFree(void** mem);                                     /* main.cpp:505 */
+
+/* host-only helpers (no device work): the integrator's coefficient and step-size rules */
+int STS_LSRKStageCoeffs(int method, int s, double* mu, double* nu, double* mus, double* ajm1,
+                        double* cjm1);
+int STS_LSRKStagesNeeded(int method, double h, double rho, int smax, double* hmax);
+double STS_AdaptControllerEstimate(int controller, double h, double dsm, double ep1, double ep2,
+                                   long long nhist);
+int STS_ManufacturedTables(sts_index n, double d, double* S, double* Sdd);
+double STS_ExactSumHost(const double* x, sts_index n);
+
+/* ------------------------------------------------------------------------------------
+ * Implicit comparator: SUNLinSol_PCG with the Jacobi preconditioner
+ * (diffusion_2D/main.cpp:207-212, 305-316; preconditioner_jacobi.cpp). The fused solver
+ * solves (I - gamma A) x = b for the problem's operator A with x0 = 0.
+ * ----------------------------------------------------------------------------------*/
+#define STS_PREC_NONE 0  /* SUN_PREC_NONE */
+#define STS_PREC_RIGHT 2 /* SUN_PREC_RIGHT */
+typedef int (*STS_ATimesFn)(void* A_data, N_Vector v, N_Vector z);
+typedef int (*STS_PSolveFn)(void* P_data, N_Vector r, N_Vector z, double tol, int lr);
+
+void* STS_SUNLinSol_PCG(N_Vector y, int pretype, int maxl, STS_Context ctx); /* main.cpp:211 */
+int STS_SUNLinSolSetATimes(void* LS, void* A_data, STS_ATimesFn atimes);
+int STS_SUNLinSolSetPreconditioner(void* LS, void* P_data, STS_PSolveFn psolve);
+/* generic PCG through the callbacks; stop when ||r||_2 <= delta ||b||_2 */
+int STS_SUNLinSolSolve(void* LS, N_Vector x, N_Vector b, double delta);
+int STS_SUNLinSolNumIters(void* LS);
+double STS_SUNLinSolResNorm(void* LS);
+int STS_SUNLinSolFree(void* LS);
+/* fused (I - gamma A) x = b solve with Jacobi (jacobi=1) or no preconditioner */
+int STS_ImplicitSolvePCG(STS_Problem p, double gamma, N_Vector b, N_Vector x, double tol,
+                         int maxit, int jacobi, int* iters, double* relres);
+/* fixed-step SDIRK2 with fused Jacobi-PCG stage solves (ARKStep DIRK, main.cpp:242,272) */
+int STS_SDIRK2Evolve(STS_Problem p, N_Vector y, double t0, double h, int nsteps, double tol,
+                     int maxit, long long* total_iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1229 @@
+/* CPU oracle for the diffusion_2D super-time-stepping path — TEST INFRASTRUCTURE ONLY.
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this file's
+ * shared library; the CUDA product never calls it. See sts_oracle.h for the parity status
+ * (SUNDIALS parity unpinned: deps/sundials is an empty submodule in the reference).
+ *
+ * Arithmetic contract. Every floating-point expression that the CUDA kernels also
+ * evaluate is written here in the same order with explicit fma()/fmaf(), and the file is
+ * compiled with -ffp-contract=off, so the GPU FP64 and mixed paths can be compared bit for
+ * bit. Reductions use an exact fixed-point accumulator (every term truncated to a multiple
+ * of 2^-160, summed exactly, rounded once), so their value does not depend on the order of
+ * summation, the thread count or the GPU launch shape.
+ */
+#include "sts_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define PI 3.14159265358979323846
+
+int orc_nthreads(void)
+{
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------------------
+ * Exact accumulation. Replaces the MPI_Allreduce-backed sums of NVECTOR_PARALLEL and the
+ * gkyl_array_reduce_range + gkyl_comm_allreduce pair of nvector_gkylzero.c:234-404.
+ * ----------------------------------------------------------------------------------*/
+#define XW 5 /* 320-bit accumulators: grid 2^-160, terms below 2^128 */
+typedef struct {
+  uint64_t p[XW], n[XW];
+  int nan, ovf;
+} xacc;
+
+static void xacc_zero(xacc* a) { memset(a, 0, sizeof(*a)); }
+
+static void add_at(uint64_t a[XW], int k, uint64_t lo, uint64_t hi)
+{
+  unsigned __int128 s = (unsigned __int128)a[k] + lo;
+  a[k]                = (uint64_t)s;
+  uint64_t carry      = (uint64_t)(s >> 64);
+  for (int m = k + 1; m < XW; ++m)
+  {
+    uint64_t add = (m == k + 1) ? hi : 0;
+    s            = (unsigned __int128)a[m] + add + carry;
+    a[m]         = (uint64_t)s;
+    carry        = (uint64_t)(s >> 64);
+  }
+}
+
+static void xacc_add(xacc* a, double x)
+{
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  int neg    = (int)(b >> 63);
+  int e      = (int)((b >> 52) & 0x7ff);
+  uint64_t m = b & ((1ULL << 52) - 1);
+  int exp2;
+  if (e == 0x7ff)
+  {
+    if (m) a->nan = 1;
+    else a->ovf = 1;
+    return;
+  }
+  if (e == 0)
+  {
+    if (m == 0) return;
+    exp2 = -1074;
+  }
+  else
+  {
+    m |= (1ULL << 52);
+    exp2 = e - 1075;
+  }
+  if (exp2 + 53 > 128)
+  { /* |x| >= 2^128: outside the accumulator's range */
+    a->ovf = 1;
+    return;
+  }
+  int sh = exp2 + 160;
+  uint64_t lo, hi;
+  int k;
+  if (sh < 0)
+  {
+    if (sh <= -64) return;
+    lo = m >> (-sh);
+    hi = 0;
+    k  = 0;
+  }
+  else
+  {
+    k       = sh >> 6;
+    int bsh = sh & 63;
+    lo      = m << bsh;
+    hi      = bsh ? (m >> (64 - bsh)) : 0;
+  }
+  add_at(neg ? a->n : a->p, k, lo, hi);
+}
+
+static void xacc_merge(xacc* a, const xacc* b)
+{
+  for (int k = 0; k < XW; ++k)
+  {
+    add_at(a->p, k, b->p[k], 0);
+    add_at(a->n, k, b->n[k], 0);
+  }
+  a->nan |= b->nan;
+  a->ovf |= b->ovf;
+}
+
+static double xacc_result(const xacc* a)
+{
+  if (a->nan) return NAN;
+  if (a->ovf) return INFINITY;
+  /* d = p - n in two's complement */
+  uint64_t d[XW];
+  unsigned __int128 borrow = 0;
+  for (int k = 0; k < XW; ++k)
+  {
+    unsigned __int128 s = (unsigned __int128)a->p[k] - a->n[k] - borrow;
+    d[k]                = (uint64_t)s;
+    borrow              = (s >> 64) ? 1 : 0;
+  }
+  double sign = 1.0;
+  if (d[XW - 1] >> 63)
+  {
+    sign = -1.0;
+    unsigned __int128 c = 1;
+    for (int k = 0; k < XW; ++k)
+    {
+      unsigned __int128 s = (unsigned __int128)(~d[k]) + c;
+      d[k]                = (uint64_t)s;
+      c                   = s >> 64;
+    }
+  }
+  int top = -1;
+  for (int k = XW - 1; k >= 0; --k)
+    if (d[k])
+    {
+      top = k * 64 + 63 - __builtin_clzll(d[k]);
+      break;
+    }
+  if (top < 0) return 0.0;
+  if (top <= 52) return sign * ldexp((double)d[0], -160);
+  int shift = top - 52;
+  /* mantissa = bits [shift, top] */
+  uint64_t mant;
+  {
+    int k = shift >> 6, bsh = shift & 63;
+    mant = d[k] >> bsh;
+    if (bsh && k + 1 < XW) mant |= d[k + 1] << (64 - bsh);
+    mant &= ((1ULL << 53) - 1);
+  }
+  int rpos   = shift - 1;
+  int rbit   = (int)((d[rpos >> 6] >> (rpos & 63)) & 1);
+  int sticky = 0;
+  for (int k = 0; k <= (rpos >> 6) && !sticky; ++k)
+  {
+    uint64_t w = d[k];
+    if (k == (rpos >> 6)) w &= ((rpos & 63) ? ((1ULL << (rpos & 63)) - 1) : 0);
+    if (w) sticky = 1;
+  }
+  if (rbit && (sticky || (mant & 1)))
+  {
+    mant++;
+    if (mant == (1ULL << 53))
+    {
+      mant >>= 1;
+      shift++;
+    }
+  }
+  return sign * ldexp((double)mant, shift - 160);
+}
+
+/* Parallel exact reductions; the value is independent of the thread partition. */
+#define XREDUCE(N, TERM)                                       \
+  xacc tot;                                                    \
+  xacc_zero(&tot);                                             \
+  _Pragma("omp parallel")                                      \
+  {                                                            \
+    xacc loc;                                                  \
+    xacc_zero(&loc);                                           \
+    _Pragma("omp for schedule(static)") for (long i = 0; i < (N); ++i) \
+    {                                                          \
+      xacc_add(&loc, (TERM));                                  \
+    }                                                          \
+    _Pragma("omp critical") xacc_merge(&tot, &loc);            \
+  }
+
+double orc_xsum(const double* x, long n)
+{
+  XREDUCE(n, x[i]);
+  return xacc_result(&tot);
+}
+
+/* N_VDotProd (nvector_gkylzero.c:349-404): sum_i x_i*y_i */
+double orc_xdot(const double* x, const double* y, long n)
+{
+  XREDUCE(n, x[i] * y[i]);
+  return xacc_result(&tot);
+}
+
+/* N_VWrmsNorm (nvector_gkylzero.c:234-290): sqrt(sum (x_i w_i)^2 / n) */
+double orc_wrms(const double* x, const double* w, long n)
+{
+  double s;
+  {
+    XREDUCE(n, (x[i] * w[i]) * (x[i] * w[i]));
+    s = xacc_result(&tot);
+  }
+  return sqrt(s / (double)n);
+}
+
+/* N_VMaxNorm (nvector_gkylzero.c:453-498) */
+double orc_maxnorm(const double* x, long n)
+{
+  double m = 0.0;
+  int nan  = 0;
+  for (long i = 0; i < n; ++i)
+  {
+    double a = fabs(x[i]);
+    if (a != a) nan = 1;
+    if (a > m) m = a;
+  }
+  return nan ? NAN : m;
+}
+
+/* ------------------------------------------------------------------------------------
+ * Problem definition.
+ *   manufactured: u = S(x)S(y)c(t), S = sin^2(pi .), c = cos^2(2 pi t),
+ *                 b = S S c' - c (kx S'' S + ky S S''), S'' = 2 pi^2 cos(2 pi .)
+ *                 (form of diffusion_2D/README.md:13-34 with the cos^2(2 pi t) time factor)
+ *   grid:         N interior nodes per direction on [0,1], d = 1/(N+1), x_i = (i+1) d
+ *   periodic:     diffusion_2D.cpp:155-160 (d = (xu-xl)/(n-1)), initial.cpp:42-43,
+ *                 Diffusion_Coeff_X/Y diffusion_2D.cpp:887-897
+ * ----------------------------------------------------------------------------------*/
+double orc_c(double t)
+{
+  double cs = cos(2.0 * PI * t);
+  return cs * cs;
+}
+
+double orc_cdot(double t) { return -2.0 * PI * sin(4.0 * PI * t); }
+
+static void manufactured_tables(int n, double d, double* S, double* Sdd)
+{
+  for (int i = 0; i < n; ++i)
+  {
+    double x = (i + 1) * d;
+    double s = sin(PI * x);
+    S[i]     = s * s;
+    Sdd[i]   = 2.0 * PI * PI * cos(2.0 * PI * x);
+  }
+}
+
+static double coeff(double k, double x, int inhom)
+{
+  return inhom ? (k * (1.0 + 0.99 * sin(x))) : k;
+}
+
+orc_prob* orc_prob_create(int kind, int nx, int ny, double kx, double ky, int inhomogeneous,
+                          double xl, double xu, double yl, double yu)
+{
+  if (nx < 1 || ny < 1) return NULL;
+  orc_prob* p = (orc_prob*)calloc(1, sizeof(orc_prob));
+  p->nx = nx;
+  p->ny = ny;
+  p->kind = kind;
+  p->kx   = kx;
+  p->ky   = ky;
+  p->inhomogeneous = (kind == ORC_PERIODIC) ? inhomogeneous : 0;
+  if (kind == ORC_PERIODIC)
+  {
+    p->xl = xl;
+    p->xu = xu;
+    p->yl = yl;
+    p->yu = yu;
+    p->dx = (xu - xl) / (nx - 1);
+    p->dy = (yu - yl) / (ny - 1);
+  }
+  else
+  {
+    p->xl = 0.0;
+    p->xu = 1.0;
+    p->yl = 0.0;
+    p->yu = 1.0;
+    p->dx = 1.0 / (nx + 1);
+    p->dy = 1.0 / (ny + 1);
+  }
+  p->cx  = kx / (p->dx * p->dx);
+  p->cy  = ky / (p->dy * p->dy);
+  p->cc  = -2.0 * (p->cx + p->cy);
+  p->Sx  = (double*)calloc(nx, sizeof(double));
+  p->Sxx = (double*)calloc(nx, sizeof(double));
+  p->Sy  = (double*)calloc(ny, sizeof(double));
+  p->Syy = (double*)calloc(ny, sizeof(double));
+  manufactured_tables(nx, p->dx, p->Sx, p->Sxx);
+  manufactured_tables(ny, p->dy, p->Sy, p->Syy);
+  p->Dxw = (double*)calloc(nx, sizeof(double));
+  p->Dxe = (double*)calloc(nx, sizeof(double));
+  p->Dys = (double*)calloc(ny, sizeof(double));
+  p->Dyn = (double*)calloc(ny, sizeof(double));
+  for (int i = 0; i < nx; ++i)
+  { /* diffusion.cpp:43-46 (global index, is = 0) */
+    double xlo = p->xl + (i - 0.5) * p->dx, xhi = p->xl + (i + 0.5) * p->dx;
+    p->Dxw[i]  = coeff(kx, xlo, p->inhomogeneous) / (p->dx * p->dx);
+    p->Dxe[i]  = coeff(kx, xhi, p->inhomogeneous) / (p->dx * p->dx);
+  }
+  for (int j = 0; j < ny; ++j)
+  { /* diffusion.cpp:36-39 */
+    double ylo = p->yl + (j - 0.5) * p->dy, yhi = p->yl + (j + 0.5) * p->dy;
+    p->Dys[j]  = coeff(ky, ylo, p->inhomogeneous) / (p->dy * p->dy);
+    p->Dyn[j]  = coeff(ky, yhi, p->inhomogeneous) / (p->dy * p->dy);
+  }
+  return p;
+}
+
+void orc_prob_free(orc_prob* p)
+{
+  if (!p) return;
+  free(p->Sx);
+  free(p->Sxx);
+  free(p->Sy);
+  free(p->Syy);
+  free(p->Dxw);
+  free(p->Dxe);
+  free(p->Dys);
+  free(p->Dyn);
+  free(p);
+}
+
+void orc_initial(const orc_prob* p, double* u)
+{
+  long nx = p->nx;
+  for (long j = 0; j < p->ny; ++j)
+    for (long i = 0; i < nx; ++i)
+    {
+      if (p->kind == ORC_PERIODIC)
+      { /* initial.cpp:39-43 */
+        double x     = p->xl + i * p->dx;
+        double y     = p->yl + j * p->dy;
+        u[j * nx + i] = (1.0 + 0.3 * sin(2.0 * x)) / sqrt(5.5 * PI) * exp(-(y * y) / 5.5);
+      }
+      else u[j * nx + i] = p->Sx[i] * p->Sy[j];
+    }
+}
+
+/* sum_k a_k sin(p_k pi x) sin(q_k pi y) (batched initial condition) */
+void orc_initial_modes(const orc_prob* p, int nmodes, const int* pm, const int* qm,
+                       const double* amp, double* u)
+{
+  long nx = p->nx;
+  for (long j = 0; j < p->ny; ++j)
+    for (long i = 0; i < nx; ++i)
+    {
+      double x = (i + 1) * p->dx, y = (j + 1) * p->dy, v = 0.0;
+      for (int k = 0; k < nmodes; ++k) v += amp[k] * sin(pm[k] * PI * x) * sin(qm[k] * PI * y);
+      u[j * nx + i] = v;
+    }
+}
+
+void orc_exact(const orc_prob* p, double t, double* u)
+{
+  double c = orc_c(t);
+  long nx  = p->nx;
+  for (long j = 0; j < p->ny; ++j)
+    for (long i = 0; i < nx; ++i) u[j * nx + i] = (p->Sx[i] * p->Sy[j]) * c;
+}
+
+/* Forcing tables for a scale hm at time t: b*hm at (i,j) = Sy_j P_i + Syy_j Q_i. */
+static void forcing_scalars(const orc_prob* p, double hm, double t, double* al, double* be,
+                            double* ga)
+{
+  double c  = orc_c(t);
+  double cd = orc_cdot(t);
+  *al       = hm * cd;
+  *be       = -(hm * c) * p->kx;
+  *ga       = -(hm * c) * p->ky;
+}
+
+/* Kernel-form RHS F(t,u) = A u + b(t) (the arithmetic of the CUDA RHS kernel). */
+static inline double lap_point(const orc_prob* p, const double* u, long i, long j)
+{
+  long nx = p->nx, ny = p->ny;
+  double uc = u[j * nx + i];
+  double uw = (i > 0) ? u[j * nx + i - 1] : 0.0;
+  double ue = (i < nx - 1) ? u[j * nx + i + 1] : 0.0;
+  double us = (j > 0) ? u[(j - 1) * nx + i] : 0.0;
+  double un = (j < ny - 1) ? u[(j + 1) * nx + i] : 0.0;
+  double sx = uw + ue, sy = us + un;
+  double acc = p->cc * uc;
+  acc        = fma(p->cx, sx, acc);
+  acc        = fma(p->cy, sy, acc);
+  return acc;
+}
+
+void orc_rhs(const orc_prob* p, double t, const double* u, double* f)
+{
+  if (p->kind == ORC_PERIODIC)
+  {
+    orc_rhs_ref(p, t, u, f);
+    return;
+  }
+  long nx = p->nx, ny = p->ny;
+  double al, be, ga;
+  forcing_scalars(p, 1.0, t, &al, &be, &ga);
+  int forced = (p->kind == ORC_MANUFACTURED);
+#pragma omp parallel for schedule(static)
+  for (long j = 0; j < ny; ++j)
+    for (long i = 0; i < nx; ++i)
+    {
+      double acc = lap_point(p, u, i, j);
+      if (forced)
+      {
+        double P = fma(al, p->Sx[i], be * p->Sxx[i]);
+        double Q = ga * p->Sx[i];
+        acc      = fma(p->Sy[j], P, acc);
+        acc      = fma(p->Syy[j], Q, acc);
+      }
+      f[j * nx + i] = acc;
+    }
+}
+
+/* Literal restatement of laplacian() (diffusion.cpp:9-209): f = -((Dxw+Dxe)+(Dys+Dyn)) u
+ * + Dxw uW + Dxe uE + Dys uS + Dyn uN, neighbours periodic (kind PERIODIC) or zero
+ * (Dirichlet kinds), plus the manufactured forcing where present. */
+void orc_rhs_ref(const orc_prob* p, double t, const double* u, double* f)
+{
+  long nx = p->nx, ny = p->ny;
+  int per = (p->kind == ORC_PERIODIC);
+#pragma omp parallel for schedule(static)
+  for (long j = 0; j < ny; ++j)
+    for (long i = 0; i < nx; ++i)
+    {
+      long iw = i - 1, ie = i + 1, js = j - 1, jn = j + 1;
+      double uw, ue, us, un;
+      if (per)
+      {
+        uw = u[j * nx + (iw < 0 ? nx - 1 : iw)];
+        ue = u[j * nx + (ie >= nx ? 0 : ie)];
+        us = u[(js < 0 ? ny - 1 : js) * nx + i];
+        un = u[(jn >= ny ? 0 : jn) * nx + i];
+      }
+      else
+      {
+        uw = iw >= 0 ? u[j * nx + iw] : 0.0;
+        ue = ie < nx ? u[j * nx + ie] : 0.0;
+        us = js >= 0 ? u[js * nx + i] : 0.0;
+        un = jn < ny ? u[jn * nx + i] : 0.0;
+      }
+      double Dxw = per ? p->Dxw[i] : p->cx, Dxe = per ? p->Dxe[i] : p->cx;
+      double Dys = per ? p->Dys[j] : p->cy, Dyn = per ? p->Dyn[j] : p->cy;
+      double v = -((Dxw + Dxe) + (Dys + Dyn)) * u[j * nx + i];
+      v        = v + Dxw * uw;
+      v        = v + Dxe * ue;
+      v        = v + Dys * us;
+      v        = v + Dyn * un;
+      if (p->kind == ORC_MANUFACTURED)
+      {
+        double c = orc_c(t), cd = orc_cdot(t);
+        v += p->Sx[i] * p->Sy[j] * cd - c * (p->kx * p->Sxx[i] * p->Sy[j] + p->ky * p->Sx[i] * p->Syy[j]);
+      }
+      f[j * nx + i] = v;
+    }
+}
+
+/* Jacobian-vector product J v = A v (the RHS is affine in u). */
+void orc_apply_A(const orc_prob* p, const double* v, double* w)
+{
+  long nx = p->nx, ny = p->ny;
+  if (p->kind == ORC_PERIODIC)
+  {
+    orc_prob q = *p;
+    q.kind     = ORC_PERIODIC;
+    orc_rhs_ref(&q, 0.0, v, w);
+    return;
+  }
+#pragma omp parallel for schedule(static)
+  for (long j = 0; j < ny; ++j)
+    for (long i = 0; i < nx; ++i) w[j * nx + i] = lap_point(p, v, i, j);
+}
+
+/* dom_eig (main.cpp:536-550): lambda = -8 max(kx/dx^2, ky/dy^2) */
+double orc_dom_eig(const orc_prob* p)
+{
+  double a = p->kx / p->dx / p->dx, b = p->ky / p->dy / p->dy;
+  return -8.0 * (a > b ? a : b);
+}
+
+/* Power iteration (SUNDomEigEstimator_Power(u, maxiters, reltol), main.cpp:344):
+ * v <- v/||v||; repeat: w = A v; lambda = v.w; stop when |lambda - lambda_old| <
+ * reltol |lambda|; v <- w / ||w||. Returns the number of iterations (A products). */
+int orc_power_iteration(const orc_prob* p, double* v, int maxiters, double reltol, double* lambda)
+{
+  long n    = (long)p->nx * p->ny;
+  double* w = (double*)malloc(n * sizeof(double));
+  double nrm = sqrt(orc_xdot(v, v, n));
+  if (!(nrm > 0.0))
+  {
+    for (long i = 0; i < n; ++i) v[i] = 1.0;
+    nrm = sqrt(orc_xdot(v, v, n));
+  }
+  double inv = 1.0 / nrm;
+  for (long i = 0; i < n; ++i) v[i] = inv * v[i];
+  double lam = 0.0, lam_old = 0.0;
+  int k;
+  for (k = 1; k <= maxiters; ++k)
+  {
+    orc_apply_A(p, v, w);
+    lam = orc_xdot(v, w, n);
+    double wn = sqrt(orc_xdot(w, w, n));
+    double wi = 1.0 / wn;
+    for (long i = 0; i < n; ++i) v[i] = wi * w[i];
+    if (k > 1 && fabs(lam - lam_old) < reltol * fabs(lam)) break;
+    lam_old = lam;
+  }
+  if (k > maxiters) k = maxiters;
+  free(w);
+  *lambda = lam;
+  return k;
+}
+
+/* ------------------------------------------------------------------------------------
+ * LSRKStep STS methods, restated.
+ *   RKC2: Sommeijer, Shampine & Verwer (1998), damping eps = 2/13; coefficient recurrence
+ *         and stage count 1 + floor(sqrt(1 + 1.54 h rho)) as in the published rkc.f.
+ *   RKL2: Meyer, Balsara & Aslam (2014). Stage count ceil((sqrt(9 + 8 h rho) - 1)/2).
+ * Arrays are indexed by stage j = 1..s; entry 0 unused. cjm1[j] is the time fraction of
+ * Y_{j-1} (where F is evaluated for stage j).
+ * ----------------------------------------------------------------------------------*/
+int orc_stage_coeffs(int method, int s, double* mu, double* nu, double* mus, double* ajm1,
+                     double* cjm1)
+{
+  if (s < 2) return -1;
+  if (method == 0)
+  {
+    double sd    = (double)s;
+    double w0    = 1.0 + 2.0 / (13.0 * (sd * sd));
+    double temp1 = w0 * w0 - 1.0;
+    double temp2 = sqrt(temp1);
+    double arg   = sd * log(w0 + temp2);
+    double w1    = sinh(arg) * temp1 / (cosh(arg) * sd * temp2 - w0 * sinh(arg));
+    double bjm1  = 1.0 / ((2.0 * w0) * (2.0 * w0));
+    double bjm2  = bjm1;
+    mu[1]   = 0.0;
+    nu[1]   = 0.0;
+    mus[1]  = w1 * bjm1;
+    ajm1[1] = 0.0;
+    cjm1[1] = 0.0;
+    double thjm2 = 0.0, thjm1 = mus[1];
+    double zjm1 = w0, zjm2 = 1.0, dzjm1 = 1.0, dzjm2 = 0.0, d2zjm1 = 0.0, d2zjm2 = 0.0;
+    for (int j = 2; j <= s; ++j)
+    {
+      double zj   = 2.0 * w0 * zjm1 - zjm2;
+      double dzj  = 2.0 * w0 * dzjm1 - dzjm2 + 2.0 * zjm1;
+      double d2zj = 2.0 * w0 * d2zjm1 - d2zjm2 + 4.0 * dzjm1;
+      double bj   = d2zj / (dzj * dzj);
+      double a    = 1.0 - zjm1 * bjm1;
+      double m    = 2.0 * w0 * bj / bjm1;
+      double n    = -bj / bjm2;
+      double ms   = m * w1 / w0;
+      mu[j]   = m;
+      nu[j]   = n;
+      mus[j]  = ms;
+      ajm1[j] = a;
+      cjm1[j] = thjm1;
+      double thj = m * thjm1 + n * thjm2 + ms * (1.0 - a);
+      thjm2      = thjm1;
+      thjm1      = thj;
+      bjm2       = bjm1;
+      bjm1       = bj;
+      zjm2       = zjm1;
+      zjm1       = zj;
+      dzjm2      = dzjm1;
+      dzjm1      = dzj;
+      d2zjm2     = d2zjm1;
+      d2zjm1     = d2zj;
+    }
+  }
+  else
+  {
+    double sd   = (double)s;
+    double w1   = 4.0 / ((sd + 2.0) * (sd - 1.0));
+    double bjm2 = 1.0 / 3.0, bjm1 = 1.0 / 3.0;
+    mu[1]   = 0.0;
+    nu[1]   = 0.0;
+    mus[1]  = w1 * bjm1;
+    ajm1[1] = 0.0;
+    cjm1[1] = 0.0;
+    double cj1 = mus[1];
+    for (int j = 2; j <= s; ++j)
+    {
+      double jd   = (double)j;
+      double temj = (jd + 2.0) * (jd - 1.0);
+      double cj   = temj * w1 / 4.0;
+      double bj   = temj / (2.0 * jd * (jd + 1.0));
+      double a    = 1.0 - bjm1;
+      double m    = (2.0 * jd - 1.0) / jd * (bj / bjm1);
+      double n    = -(jd - 1.0) / jd * (bj / bjm2);
+      mu[j]   = m;
+      nu[j]   = n;
+      mus[j]  = w1 * m;
+      ajm1[j] = a;
+      cjm1[j] = cj1;
+      cj1     = cj;
+      bjm2    = bjm1;
+      bjm1    = bj;
+    }
+  }
+  return 0;
+}
+
+/* Stage count for h and spectral radius rho; *hmax = the largest h the stage limit admits
+ * (0.96 * (smax^2-1)/(1.54 rho) for RKC, 0.96 * (smax^2+smax-2)/(2 rho) for RKL). */
+int orc_stages_needed(int method, double h, double rho, int smax, double* hmax)
+{
+  double ss;
+  double sm = (double)smax;
+  if (method == 0)
+  {
+    ss    = 1.0 + floor(sqrt(1.0 + 1.54 * h * rho));
+    *hmax = (rho > 0.0) ? 0.96 * (sm * sm - 1.0) / (1.54 * rho) : INFINITY;
+  }
+  else
+  {
+    ss    = ceil((sqrt(9.0 + 8.0 * h * rho) - 1.0) / 2.0);
+    *hmax = (rho > 0.0) ? 0.96 * (sm * sm + sm - 2.0) / (2.0 * rho) : INFINITY;
+  }
+  if (ss < 2.0) ss = 2.0;
+  if (ss > 1e9) ss = 1e9;
+  return (int)ss;
+}
+
+/* ARKODE-style controllers (SUNAdaptController PID/PI/I), error bias 1.5, method order
+ * ord = p + 1 = 3 (the RKC/RKL embedding estimates an O(h^3) local error). The history
+ * length nhist selects I -> PI -> PID forms on the first steps. */
+#define ORD 3.0
+#define BIAS 1.5
+#define TINYE 1.0e-10
+double orc_controller(int controller, double h, double dsm, double ep1, double ep2, long nhist)
+{
+  double e1 = BIAS * dsm;
+  if (e1 < TINYE) e1 = TINYE;
+  double e2 = BIAS * ep1;
+  if (e2 < TINYE) e2 = TINYE;
+  double e3 = BIAS * ep2;
+  if (e3 < TINYE) e3 = TINYE;
+  if (controller == 0)
+  {
+    if (nhist < 1) return h * pow(e1, -0.58 / ORD);
+    if (nhist < 2) return h * pow(e1, -0.58 / ORD) * pow(e2, 0.21 / ORD);
+    return h * pow(e1, -0.58 / ORD) * pow(e2, 0.21 / ORD) * pow(e3, -0.1 / ORD);
+  }
+  if (controller == 1)
+  {
+    if (nhist < 1) return h * pow(e1, -0.8 / ORD);
+    return h * pow(e1, -0.8 / ORD) * pow(e2, 0.31 / ORD);
+  }
+  return h * pow(e1, -1.0 / ORD);
+}
+
+#define SAFETY 0.96
+#define GROWTH 20.0
+#define ETAMX1 10000.0
+#define ETAMXF 0.3
+#define ETAMIN 0.1
+#define SMALL_NEF 2
+#define LBOUND 1.0
+#define UBOUND 1.5
+
+void orc_state_init(orc_state* st, double t0)
+{
+  memset(st, 0, sizeof(*st));
+  st->t = t0;
+}
+
+void orc_state_free(orc_state* st)
+{
+  free(st->F);
+  free(st->Ff);
+  free(st->evec);
+  st->F    = NULL;
+  st->Ff   = NULL;
+  st->evec = NULL;
+}
+
+/* ---- stage arithmetic (mirrors the CUDA stage kernels) ---- */
+typedef struct {
+  double gc, gx, gy, gn, g0, gf, al, be, ga;
+  float gcf, gxf, gyf, gnf, gFf, alf, bef, gaf;
+} stage_c;
+
+static void stage_coeffs_j(const orc_prob* p, double t, double h, const double* mu, const double* nu,
+                           const double* mus, const double* ajm1, const double* cjm1, int j,
+                           stage_c* c)
+{
+  double hm = h * mus[j];
+  double tj = t + h * cjm1[j];
+  double tm = hm * p->cc;
+  c->gc     = mu[j] + tm;
+  c->gx     = hm * p->cx;
+  c->gy     = hm * p->cy;
+  c->gn     = nu[j];
+  c->g0     = (1.0 - mu[j]) - nu[j];
+  c->gf     = -(hm * ajm1[j]);
+  forcing_scalars(p, hm, tj, &c->al, &c->be, &c->ga);
+  /* mixed (increment) form */
+  c->gcf    = (float)c->gc;
+  c->gxf    = (float)c->gx;
+  c->gyf    = (float)c->gy;
+  c->gnf    = (float)c->gn;
+  c->gFf    = (float)(hm * (1.0 - ajm1[j]));
+  double dc  = orc_c(tj) - orc_c(t);
+  double dcd = orc_cdot(tj) - orc_cdot(t);
+  c->alf     = (float)(hm * dcd);
+  c->bef     = (float)(-(hm * dc) * p->kx);
+  c->gaf     = (float)(-(hm * dc) * p->ky);
+}
+
+static void stage64(const orc_prob* p, const stage_c* c, const double* ym1, const double* ym2,
+                    const double* y0, const double* f0, double* yj)
+{
+  long nx = p->nx, ny = p->ny;
+  int forced = (p->kind == ORC_MANUFACTURED);
+#pragma omp parallel for schedule(static)
+  for (long j = 0; j < ny; ++j)
+    for (long i = 0; i < nx; ++i)
+    {
+      long k     = j * nx + i;
+      double uw  = (i > 0) ? ym1[k - 1] : 0.0;
+      double ue  = (i < nx - 1) ? ym1[k + 1] : 0.0;
+      double us  = (j > 0) ? ym1[k - nx] : 0.0;
+      double un  = (j < ny - 1) ? ym1[k + nx] : 0.0;
+      double sx  = uw + ue, sy = us + un;
+      double acc = c->gc * ym1[k];
+      acc        = fma(c->gx, sx, acc);
+      acc        = fma(c->gy, sy, acc);
+      acc        = fma(c->gn, ym2[k], acc);
+      acc        = fma(c->g0, y0[k], acc);
+      acc        = fma(c->gf, f0[k], acc);
+      if (forced)
+      {
+        double P = fma(c->al, p->Sx[i], c->be * p->Sxx[i]);
+        double Q = c->ga * p->Sx[i];
+        acc      = fma(p->Sy[j], P, acc);
+        acc      = fma(p->Syy[j], Q, acc);
+      }
+      yj[k] = acc;
+    }
+}
+
+static void stage32(const orc_prob* p, const stage_c* c, const float* dm1, const float* dm2,
+                    const float* f0f, const float* Sxf, const float* Sxxf, const float* Syf,
+                    const float* Syyf, float* dj)
+{
+  long nx = p->nx, ny = p->ny;
+  int forced = (p->kind == ORC_MANUFACTURED);
+#pragma omp parallel for schedule(static)
+  for (long j = 0; j < ny; ++j)
+    for (long i = 0; i < nx; ++i)
+    {
+      long k    = j * nx + i;
+      float dw  = (i > 0) ? dm1[k - 1] : 0.0f;
+      float de  = (i < nx - 1) ? dm1[k + 1] : 0.0f;
+      float ds  = (j > 0) ? dm1[k - nx] : 0.0f;
+      float dn  = (j < ny - 1) ? dm1[k + nx] : 0.0f;
+      float sx  = dw + de, sy = ds + dn;
+      float acc = c->gcf * dm1[k];
+      acc       = fmaf(c->gxf, sx, acc);
+      acc       = fmaf(c->gyf, sy, acc);
+      if (dm2) acc = fmaf(c->gnf, dm2[k], acc);
+      acc = fmaf(c->gFf, f0f[k], acc);
+      if (forced)
+      {
+        float P = fmaf(c->alf, Sxf[i], c->bef * Sxxf[i]);
+        float Q = c->gaf * Sxf[i];
+        acc     = fmaf(Syf[j], P, acc);
+        acc     = fmaf(Syyf[j], Q, acc);
+      }
+      dj[k] = acc;
+    }
+}
+
+/* Step end: Fnew = F(t+h, ynew), err = 0.8 (yn - ynew) + 0.4 h (Fn + Fnew),
+ * dsm = ||err||_WRMS with ewt = 1/(rtol |yn| + atol). For the mixed form ynew = yn + ds. */
+static double step_end(const orc_prob* p, const orc_opts* o, double t, double h, const double* yn,
+                       const double* Fn, double* ynew, const float* ds, double* Fnew, float* Fnewf)
+{
+  long nx = p->nx, ny = p->ny, n = nx * ny;
+  if (ds)
+  {
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < n; ++k) ynew[k] = yn[k] + (double)ds[k];
+  }
+  orc_rhs(p, t + h, ynew, Fnew);
+  if (Fnewf)
+  {
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < n; ++k) Fnewf[k] = (float)Fnew[k];
+  }
+  double p4h = 0.4 * h;
+  double s;
+  {
+    XREDUCE(n, ({
+              double d = yn[i] - ynew[i];
+              double e = 0.8 * d;
+              e        = fma(p4h, Fn[i], e);
+              e        = fma(p4h, Fnew[i], e);
+              double w = 1.0 / (o->rtol * fabs(yn[i]) + o->atol);
+              double x = e * w;
+              x * x;
+            }));
+    s = xacc_result(&tot);
+  }
+  return sqrt(s / (double)n);
+}
+
+/* WRMS of v with ewt(y) (used by the initial step estimate) */
+static double wrms_ewt(const orc_opts* o, const double* v, const double* y, long n)
+{
+  XREDUCE(n, ({
+            double w = 1.0 / (o->rtol * fabs(y[i]) + o->atol);
+            double x = v[i] * w;
+            x * x;
+          }));
+  return sqrt(xacc_result(&tot) / (double)n);
+}
+
+static double wrms_diff_ewt(const orc_opts* o, const double* a, const double* b, const double* y, long n)
+{
+  XREDUCE(n, ({
+            double w = 1.0 / (o->rtol * fabs(y[i]) + o->atol);
+            double x = (a[i] - b[i]) * w;
+            x * x;
+          }));
+  return sqrt(xacc_result(&tot) / (double)n);
+}
+
+/* Initial step (Hairer, Norsett & Wanner, "Solving ODEs I", II.4), WRMS norms on ewt(y0),
+ * order ORD; the explicit-Euler probe step is capped at 1/rho so that it stays stable, a
+ * non-finite second-derivative estimate falls back to the probe step, and the result is
+ * capped at tdist. */
+static double initial_step(const orc_prob* p, const orc_opts* o, double t0, const double* y0,
+                           const double* F0, double tdist, double rho, long* nfe)
+{
+  long n = (long)p->nx * p->ny;
+  double d0 = wrms_ewt(o, y0, y0, n);
+  double d1 = wrms_ewt(o, F0, y0, n);
+  double h0 = (d0 < 1.0e-5 || d1 < 1.0e-5) ? 1.0e-6 : 0.01 * (d0 / d1);
+  if (rho > 0.0 && h0 * rho > 1.0) h0 = 1.0 / rho;
+  if (h0 > tdist) h0 = tdist;
+  double* y1 = (double*)malloc(n * sizeof(double));
+  double* F1 = (double*)malloc(n * sizeof(double));
+  for (long k = 0; k < n; ++k) y1[k] = fma(h0, F0[k], y0[k]);
+  orc_rhs(p, t0 + h0, y1, F1);
+  (*nfe)++;
+  double d2  = wrms_diff_ewt(o, F1, F0, y0, n) / h0;
+  double dm  = d1 > d2 ? d1 : d2;
+  double h1  = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : pow(0.01 / dm, 1.0 / ORD);
+  if (!(h1 > 0.0) || !(h1 < INFINITY)) h1 = h0;
+  double h   = (100.0 * h0 < h1) ? 100.0 * h0 : h1;
+  if (h > tdist) h = tdist;
+  free(y1);
+  free(F1);
+  return h;
+}
+
+int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double tout, double* y)
+{
+  long n    = (long)p->nx * p->ny;
+  int smax  = o->smax > 1 ? o->smax : 200;
+  long maxs = o->maxsteps > 0 ? o->maxsteps : 500;
+  double* mu   = (double*)malloc((smax + 1) * sizeof(double));
+  double* nu   = (double*)malloc((smax + 1) * sizeof(double));
+  double* mus  = (double*)malloc((smax + 1) * sizeof(double));
+  double* ajm1 = (double*)malloc((smax + 1) * sizeof(double));
+  double* cjm1 = (double*)malloc((smax + 1) * sizeof(double));
+  double *Ya = NULL, *Yb = NULL, *Yc = NULL, *ynew = NULL, *Fnew = NULL;
+  float *da = NULL, *db = NULL, *dc = NULL, *Fnewf = NULL, *Sxf = NULL, *Sxxf = NULL, *Syf = NULL,
+        *Syyf = NULL;
+  int ret = 0;
+  ynew = (double*)malloc(n * sizeof(double));
+  Fnew = (double*)malloc(n * sizeof(double));
+  if (o->mixed)
+  {
+    da    = (float*)malloc(n * sizeof(float));
+    db    = (float*)malloc(n * sizeof(float));
+    dc    = (float*)malloc(n * sizeof(float));
+    Fnewf = (float*)malloc(n * sizeof(float));
+    Sxf   = (float*)malloc(p->nx * sizeof(float));
+    Sxxf  = (float*)malloc(p->nx * sizeof(float));
+    Syf   = (float*)malloc(p->ny * sizeof(float));
+    Syyf  = (float*)malloc(p->ny * sizeof(float));
+    for (int i = 0; i < p->nx; ++i)
+    {
+      Sxf[i]  = (float)p->Sx[i];
+      Sxxf[i] = (float)p->Sxx[i];
+    }
+    for (int j = 0; j < p->ny; ++j)
+    {
+      Syf[j]  = (float)p->Sy[j];
+      Syyf[j] = (float)p->Syy[j];
+    }
+  }
+  else
+  {
+    Ya = (double*)malloc(n * sizeof(double));
+    Yb = (double*)malloc(n * sizeof(double));
+    Yc = (double*)malloc(n * sizeof(double));
+  }
+
+  if (!st->initialized)
+  {
+    st->F  = (double*)malloc(n * sizeof(double));
+    st->Ff = (float*)malloc(n * sizeof(float));
+    orc_rhs(p, st->t, y, st->F);
+    st->nfe++;
+    for (long k = 0; k < n; ++k) st->Ff[k] = (float)st->F[k];
+    st->hnext           = (o->hfixed > 0.0) ? o->hfixed : 0.0;
+    st->initialized     = 1;
+    st->steps_since_dee = -1;
+  }
+
+  long nsteps_call = 0;
+  while (st->t < tout)
+  {
+    if (nsteps_call >= maxs)
+    {
+      ret = -1; /* ARK_TOO_MUCH_WORK */
+      break;
+    }
+    /* dominant eigenvalue: first step, then every dom_eig_freq accepted steps */
+    /* dom_eig_freq <= 0: the eigenvalue is computed once (LSRKStepSetDomEigFrequency(0)) */
+    int freq = o->dom_eig_freq;
+    if (st->steps_since_dee < 0 || (freq > 0 && st->steps_since_dee >= freq))
+    {
+      double lam;
+      if (o->internaleig)
+      {
+        if (!st->evec)
+        {
+          st->evec = (double*)malloc(n * sizeof(double));
+          memcpy(st->evec, y, n * sizeof(double));
+        }
+        int it = orc_power_iteration(p, st->evec, o->dee_maxiters > 0 ? o->dee_maxiters : 100,
+                                     o->dee_reltol > 0.0 ? o->dee_reltol : 0.01, &lam);
+        st->nfe_dee += it;
+      }
+      else lam = orc_dom_eig(p);
+      double saf          = o->eig_safety > 0.0 ? o->eig_safety : 1.01;
+      st->spectral_radius = saf * fabs(lam);
+      st->ndee++;
+      st->steps_since_dee = 0;
+    }
+    if (!(st->hnext > 0.0))
+      st->hnext = initial_step(p, o, st->t, y, st->F, tout - st->t, st->spectral_radius, &st->nfe);
+
+    int nef = 0;
+    for (;;)
+    {
+      double h = st->hnext, hmax;
+      int clipped = 0;
+      int s       = orc_stages_needed(o->method, h, st->spectral_radius, smax, &hmax);
+      if (s > smax)
+      {
+        if (o->hfixed > 0.0)
+        {
+          ret = -2;
+          goto done;
+        }
+        h = hmax;
+        st->nst_exp++;
+      }
+      if (st->t + h >= tout)
+      {
+        h       = tout - st->t;
+        clipped = 1;
+      }
+      s = orc_stages_needed(o->method, h, st->spectral_radius, smax, &hmax);
+      orc_stage_coeffs(o->method, s, mu, nu, mus, ajm1, cjm1);
+      st->nst_attempts++;
+      double dsm;
+      if (!o->mixed)
+      {
+        /* Y_1 = Y_0 + h mus_1 F_0 ; Y_j from Y_{j-1}, Y_{j-2} (Y_{-1} := Y_0) */
+        double hm1 = h * mus[1];
+        for (long k = 0; k < n; ++k) Ya[k] = fma(hm1, st->F[k], y[k]);
+        const double *ym2 = y, *ym1 = Ya;
+        double* bufs[3] = {Yb, Yc, Ya};
+        int bi          = 0;
+        double* yj      = Ya;
+        for (int j = 2; j <= s; ++j)
+        {
+          stage_c c;
+          stage_coeffs_j(p, st->t, h, mu, nu, mus, ajm1, cjm1, j, &c);
+          yj = bufs[bi];
+          bi = (bi + 1) % 3;
+          stage64(p, &c, ym1, ym2, y, st->F, yj);
+          ym2 = ym1;
+          ym1 = yj;
+        }
+        st->nfe += s; /* F_0 reused (FSAL); s - 1 stage RHS + 1 step-end RHS */
+        memcpy(ynew, yj, n * sizeof(double));
+        dsm = step_end(p, o, st->t, h, y, st->F, ynew, NULL, Fnew, NULL);
+      }
+      else
+      {
+        float hm1 = (float)(h * mus[1]);
+        for (long k = 0; k < n; ++k) da[k] = hm1 * st->Ff[k];
+        const float *dm2 = NULL, *dm1 = da;
+        float* bufs[3] = {db, dc, da};
+        int bi         = 0;
+        float* dj      = da;
+        for (int j = 2; j <= s; ++j)
+        {
+          stage_c c;
+          stage_coeffs_j(p, st->t, h, mu, nu, mus, ajm1, cjm1, j, &c);
+          dj = bufs[bi];
+          bi = (bi + 1) % 3;
+          stage32(p, &c, dm1, dm2, st->Ff, Sxf, Sxxf, Syf, Syyf, dj);
+          dm2 = dm1;
+          dm1 = dj;
+        }
+        st->nfe += s;
+        dsm = step_end(p, o, st->t, h, y, st->F, ynew, dj, Fnew, Fnewf);
+      }
+      st->stages_total += s;
+      if (s > st->stage_max) st->stage_max = s;
+
+      if (o->hfixed > 0.0 || dsm <= 1.0)
+      {
+        /* accept */
+        st->t = clipped ? tout : st->t + h;
+        memcpy(y, ynew, n * sizeof(double));
+        memcpy(st->F, Fnew, n * sizeof(double));
+        if (o->mixed) memcpy(st->Ff, Fnewf, n * sizeof(float));
+        else
+          for (long k = 0; k < n; ++k) st->Ff[k] = (float)Fnew[k];
+        st->hlast = h;
+        if (o->hfixed > 0.0) st->hnext = o->hfixed;
+        else
+        {
+          double hn  = orc_controller(o->controller, h, dsm, st->ep1, st->ep2, st->nhist);
+          double eta = SAFETY * hn / h;
+          double emx = (st->nst == 0) ? ETAMX1 : (st->after_fail ? 1.0 : GROWTH);
+          if (eta > emx) eta = emx;
+          if (eta >= LBOUND && eta <= UBOUND) eta = 1.0;
+          st->hnext = h * eta;
+          st->ep2   = st->ep1;
+          st->ep1   = dsm;
+          st->nhist++;
+        }
+        st->after_fail = 0;
+        st->nst++;
+        st->steps_since_dee++;
+        nsteps_call++;
+        break;
+      }
+      /* reject */
+      st->netf++;
+      nef++;
+      if (!(dsm == dsm) || nef > 20)
+      {
+        ret = -3; /* ARK_ERR_FAILURE */
+        goto done;
+      }
+      double hn  = orc_controller(o->controller, h, dsm, st->ep1, st->ep2, st->nhist);
+      double eta = SAFETY * hn / h;
+      if (eta > 1.0) eta = 1.0;
+      if (nef >= SMALL_NEF && eta > ETAMXF) eta = ETAMXF;
+      if (eta < ETAMIN) eta = ETAMIN;
+      st->hnext      = h * eta;
+      st->after_fail = 1;
+    }
+  }
+done:
+  free(mu);
+  free(nu);
+  free(mus);
+  free(ajm1);
+  free(cjm1);
+  free(Ya);
+  free(Yb);
+  free(Yc);
+  free(ynew);
+  free(Fnew);
+  free(da);
+  free(db);
+  free(dc);
+  free(Fnewf);
+  free(Sxf);
+  free(Sxxf);
+  free(Syf);
+  free(Syyf);
+  return ret;
+}
+
+/* ------------------------------------------------------------------------------------
+ * Implicit comparator: (I - gamma A) x = b by preconditioned CG with the Jacobi
+ * preconditioner of preconditioner_jacobi.cpp:21-40 (D = 1/(1 - gamma diag),
+ * diag = -((Dxw+Dxe)+(Dys+Dyn)) = cc) and PSolve z = D r (preconditioner_jacobi.cpp:58).
+ * x starts at zero; stop when ||r||_2 <= tol ||b||_2. Arithmetic mirrors the fused CUDA
+ * kernels: K1 forms p = beta p + D r, q = M p, p.q; K2 updates x, r and r.r, r.(D r).
+ * ----------------------------------------------------------------------------------*/
+static void apply_M(const orc_prob* p, double gamma, const double* v, double* w)
+{
+  long nx = p->nx, ny = p->ny;
+#pragma omp parallel for schedule(static)
+  for (long j = 0; j < ny; ++j)
+    for (long i = 0; i < nx; ++i)
+    {
+      double a      = lap_point(p, v, i, j);
+      w[j * nx + i] = fma(-gamma, a, v[j * nx + i]);
+    }
+}
+
+int orc_pcg(const orc_prob* p, double gamma, int jacobi, const double* b, double* x,
+            double tol, int maxit, double* relres)
+{
+  long n    = (long)p->nx * p->ny;
+  double D  = jacobi ? 1.0 / (1.0 - gamma * p->cc) : 1.0;
+  double* r  = (double*)malloc(n * sizeof(double));
+  double* pv = (double*)calloc(n, sizeof(double));
+  double* q  = (double*)malloc(n * sizeof(double));
+  for (long k = 0; k < n; ++k)
+  {
+    x[k] = 0.0;
+    r[k] = b[k];
+  }
+  double bnorm = sqrt(orc_xdot(b, b, n));
+  if (!(bnorm > 0.0))
+  {
+    *relres = 0.0;
+    free(r);
+    free(pv);
+    free(q);
+    return 0;
+  }
+  double rz;
+  {
+    XREDUCE(n, r[i] * (D * r[i]));
+    rz = xacc_result(&tot);
+  }
+  double beta = 0.0, rr = 0.0;
+  int it;
+  for (it = 1; it <= maxit; ++it)
+  {
+    for (long k = 0; k < n; ++k) pv[k] = fma(beta, pv[k], D * r[k]);
+    apply_M(p, gamma, pv, q);
+    double pq    = orc_xdot(pv, q, n);
+    double alpha = rz / pq;
+    for (long k = 0; k < n; ++k)
+    {
+      x[k] = fma(alpha, pv[k], x[k]);
+      r[k] = fma(-alpha, q[k], r[k]);
+    }
+    double rzn;
+    {
+      XREDUCE(n, r[i] * r[i]);
+      rr = xacc_result(&tot);
+    }
+    {
+      XREDUCE(n, r[i] * (D * r[i]));
+      rzn = xacc_result(&tot);
+    }
+    if (sqrt(rr) <= tol * bnorm) break;
+    beta = rzn / rz;
+    rz   = rzn;
+  }
+  if (it > maxit) it = maxit;
+  *relres = sqrt(rr) / bnorm;
+  free(r);
+  free(pv);
+  free(q);
+  return it;
+}
+
+/* Fixed-step SDIRK2 (Alexander; gamma = 1 - 1/sqrt(2), stiffly accurate) with each stage's
+ * linear Newton correction solved by Jacobi-PCG (ARKStep DIRK + SUNLinSol_PCG,
+ * main.cpp:199-231,242,302-329; the RHS is linear so one Newton iteration is exact). */
+int orc_sdirk2(const orc_prob* p, double t0, double h, int nsteps, double tol, int maxit,
+               double* y, long* total_iters)
+{
+  long n     = (long)p->nx * p->ny;
+  double g   = 1.0 - sqrt(0.5);
+  double* f  = (double*)malloc(n * sizeof(double));
+  double* f1 = (double*)malloc(n * sizeof(double));
+  double* rhs = (double*)malloc(n * sizeof(double));
+  double* d   = (double*)malloc(n * sizeof(double));
+  double* Y1  = (double*)malloc(n * sizeof(double));
+  double relres;
+  long iters = 0;
+  double t   = t0;
+  for (int s = 0; s < nsteps; ++s)
+  {
+    double hg = h * g;
+    /* stage 1: (I - hg A) d1 = hg f(t + g h, y_n), Y1 = y_n + d1 */
+    orc_rhs(p, t + g * h, y, f);
+    for (long k = 0; k < n; ++k) rhs[k] = hg * f[k];
+    iters += orc_pcg(p, hg, 1, rhs, d, tol, maxit, &relres);
+    for (long k = 0; k < n; ++k) Y1[k] = y[k] + d[k];
+    orc_rhs(p, t + g * h, Y1, f1);
+    /* stage 2: (I - hg A) d2 = h(1-g) F1 + hg f(t+h, y_n), y_{n+1} = y_n + d2 */
+    orc_rhs(p, t + h, y, f);
+    double h1g = h * (1.0 - g);
+    for (long k = 0; k < n; ++k) rhs[k] = fma(h1g, f1[k], hg * f[k]);
+    iters += orc_pcg(p, hg, 1, rhs, d, tol, maxit, &relres);
+    for (long k = 0; k < n; ++k) y[k] = y[k] + d[k];
+    t = t0 + (s + 1) * h;
+  }
+  *total_iters = iters;
+  free(f);
+  free(f1);
+  free(rhs);
+  free(d);
+  free(Y1);
+  return 0;
+}

@@ -1,0 +1,99 @@
+/* CPU oracle for the diffusion_2D super-time-stepping path — TEST INFRASTRUCTURE ONLY.
+ *
+ * This library restates, in plain C on the host, the arithmetic of the path that the
+ * reference runs through SUNDIALS (ARKODE LSRKStep + NVECTOR + PCG) and its own
+ * problem callbacks (diffusion_2D/diffusion.cpp, preconditioner_jacobi.cpp, main.cpp).
+ * It is the checker for the CUDA library in ceda_demonstrations_gb300/csrc: tests,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg are the only callers.
+ * Nothing in the product links or calls it.
+ *
+ * Parity status: SUNDIALS (git submodule deps/sundials) is empty in the reference
+ * tree, so the integrator constants are restated from the RKC/RKL2 papers and the
+ * SUNDIALS/ARKODE documentation; results cannot be compared with a SUNDIALS build
+ * ("parity unpinned" with respect to SUNDIALS). The oracle is pinned against the
+ * reference's own known-answer tests (gkeyll_diffusion/test_nvector_gkylzero.c,
+ * gkeyll_diffusion/analytic_CR_test.c) and analytic facts of the discretisation.
+ */
+#ifndef STS_ORACLE_H
+#define STS_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Problem kinds. */
+#define ORC_MANUFACTURED 0 /* [0,1]^2, homogeneous Dirichlet, u=sin^2(pi x)sin^2(pi y)cos^2(2 pi t) */
+#define ORC_UNFORCED 1     /* [0,1]^2, homogeneous Dirichlet, no forcing (batched instances) */
+#define ORC_PERIODIC 2     /* reference mode: periodic, Gaussian x sine IC, optional k(1+0.99 sin) */
+
+typedef struct orc_prob {
+  int nx, ny, kind, inhomogeneous;
+  double kx, ky, xl, xu, yl, yu, dx, dy;
+  double cx, cy, cc; /* kx/dx^2, ky/dy^2, -2(cx+cy) */
+  double *Sx, *Sxx, *Sy, *Syy;
+  double *Dxw, *Dxe, *Dys, *Dyn; /* periodic-mode face coefficients / d^2 */
+} orc_prob;
+
+typedef struct orc_opts {
+  int method;      /* 0 = RKC2, 1 = RKL2 */
+  int mixed;       /* 0 = FP64 stages, 1 = FP32 increments relative to the FP64 step start */
+  int controller;  /* 0 = PID, 1 = PI, 2 = I (ARK_ADAPT_PID / PI / I) */
+  int smax;        /* stage limit (SUNDIALS default 200) */
+  int internaleig; /* 0 = analytic dom_eig (main.cpp:536-550), 1 = power iteration */
+  int dee_maxiters;
+  int dom_eig_freq;
+  int pad_;
+  long maxsteps;   /* per evolve call; <= 0 means 500 */
+  double rtol, atol, hfixed, eig_safety, dee_reltol;
+} orc_opts;
+
+typedef struct orc_state {
+  double t, hnext, hlast, spectral_radius, ep1, ep2;
+  long nst, nst_attempts, netf, nfe, nfe_dee, ndee, nst_exp, stage_max, stages_total;
+  long nhist, steps_since_dee;
+  int initialized, after_fail;
+  double *F;  /* F(t_n, y_n) in FP64 (FSAL) */
+  float *Ff;  /* FP32 copy used by the mixed stages */
+  double *evec; /* power-iteration eigenvector (warm start) */
+} orc_state;
+
+/* exact, order-independent reductions (value = RN(sum of trunc(x_i * 2^160)) * 2^-160) */
+double orc_xsum(const double* x, long n);
+double orc_xdot(const double* x, const double* y, long n);
+double orc_wrms(const double* x, const double* w, long n);
+double orc_maxnorm(const double* x, long n);
+
+orc_prob* orc_prob_create(int kind, int nx, int ny, double kx, double ky, int inhomogeneous,
+                          double xl, double xu, double yl, double yu);
+void orc_prob_free(orc_prob* p);
+void orc_initial(const orc_prob* p, double* u);
+void orc_initial_modes(const orc_prob* p, int nmodes, const int* pm, const int* qm,
+                       const double* amp, double* u);
+void orc_exact(const orc_prob* p, double t, double* u);
+double orc_c(double t);
+double orc_cdot(double t);
+void orc_rhs(const orc_prob* p, double t, const double* u, double* f);
+void orc_rhs_ref(const orc_prob* p, double t, const double* u, double* f);
+void orc_apply_A(const orc_prob* p, const double* v, double* w);
+double orc_dom_eig(const orc_prob* p);
+int orc_power_iteration(const orc_prob* p, double* v, int maxiters, double reltol, double* lambda);
+
+int orc_stage_coeffs(int method, int s, double* mu, double* nu, double* mus, double* ajm1,
+                     double* cjm1);
+int orc_stages_needed(int method, double h, double rho, int smax, double* hmax);
+double orc_controller(int controller, double h, double dsm, double ep1, double ep2, long nhist);
+
+void orc_state_init(orc_state* st, double t0);
+void orc_state_free(orc_state* st);
+int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double tout, double* y);
+
+int orc_pcg(const orc_prob* p, double gamma, int jacobi, const double* b, double* x,
+            double tol, int maxit, double* relres);
+int orc_sdirk2(const orc_prob* p, double t0, double h, int nsteps, double tol, int maxit,
+               double* y, long* total_iters);
+
+int orc_nthreads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,235 @@
+"""LSRKStep STS integration on the GPU against the CPU oracle.
+
+Fused FP64 path: bit-for-bit equal to the oracle (same stage arithmetic, exact WRMS, same
+host step control), hence also within the 1e-12 relative-L2 bar of the target. Mixed path:
+bit-for-bit equal to the oracle's restatement of the FP32-increment scheme, and within
+1e-6 relative L2 of the FP64 solution. Generic path (any ARKRhsFn): the reference's scalar
+known-answer problem gkeyll_diffusion/analytic_CR_test.c."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+STAT_KEYS = ("nst", "nst_attempts", "netf", "nfe", "ndee", "nst_exp", "stage_max", "stages_total")
+
+
+def run_pair(ctx, stslib, oracle, pk, ok, touts, graphs=True):
+    G = stslib.Problem(ctx, **pk)
+    O = oracle.Problem(**pk)
+    y0 = G.initial()
+    I = stslib.LSRKStep(ctx, G, 0.0, y0, graphs=graphs, **ok)
+    J = oracle.Integrator(O, O.initial(), **ok)
+    yout = G.vector()
+    for tout in touts:
+        t, rc = I.evolve(tout, yout)
+        rc_o = J.evolve(tout)
+        assert rc_o == 0 and rc >= 0
+        assert t == J.stats()["t"]
+        yg = yout.numpy()
+        sg, so = I.stats(), J.stats()
+        for k in STAT_KEYS:
+            assert sg[k] == so[k], (k, sg[k], so[k])
+        assert sg["hnext"] == so["hnext"]
+        assert np.array_equal(yg, J.y), np.max(np.abs(yg - J.y))
+    return yg, J.y, I.stats()
+
+
+@pytest.mark.parametrize("nx,ny", [(8, 8), (17, 9), (33, 32), (64, 64), (130, 66)])
+@pytest.mark.parametrize("method", [0, 1])
+def test_fused_fp64_bitwise(ctx, stslib, oracle, nx, ny, method):
+    pk = dict(kind=0, nx=nx, ny=ny, kx=1.0, ky=0.3)
+    ok = dict(method=method, rtol=1e-6, atol=1e-10)
+    run_pair(ctx, stslib, oracle, pk, ok, [0.02, 0.05])
+
+
+@pytest.mark.parametrize("controller", [0, 1, 2])
+def test_controllers_bitwise(ctx, stslib, oracle, controller):
+    pk = dict(kind=0, nx=48, ny=40, kx=1.0, ky=0.01)
+    ok = dict(method=1, rtol=1e-5, atol=1e-9, controller=controller)
+    run_pair(ctx, stslib, oracle, pk, ok, [0.03])
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_mixed_bitwise(ctx, stslib, oracle, method):
+    pk = dict(kind=0, nx=96, ny=64, kx=1.0, ky=0.01)
+    ok = dict(method=method, rtol=1e-6, atol=1e-10, mixed=True)
+    run_pair(ctx, stslib, oracle, pk, ok, [0.01, 0.03])
+
+
+def test_unforced_and_small_stage_cap_bitwise(ctx, stslib, oracle):
+    pk = dict(kind=1, nx=64, ny=48, kx=0.2, ky=0.9)
+    ok = dict(method=1, rtol=1e-6, atol=1e-12, smax=12)
+    G = stslib.Problem(ctx, **pk)
+    O = oracle.Problem(**pk)
+    pm, qm, amp = [1, 3, 7], [2, 5, 1], [1.0, -0.5, 0.25]
+    y0 = G.initial_modes(pm, qm, amp)
+    I = stslib.LSRKStep(ctx, G, 0.0, y0, **ok)
+    J = oracle.Integrator(O, O.initial_modes(pm, qm, amp), **ok)
+    yout = G.vector()
+    I.evolve(0.01, yout)
+    assert J.evolve(0.01) == 0
+    assert I.stats()["stage_max"] == 12
+    assert np.array_equal(yout.numpy(), J.y)
+
+
+def test_power_iteration_estimator_bitwise(ctx, stslib, oracle):
+    pk = dict(kind=0, nx=40, ny=40, kx=1.0, ky=1.0)
+    ok = dict(method=0, rtol=1e-6, atol=1e-10, power=(100, 0.01))
+    G = stslib.Problem(ctx, **pk)
+    O = oracle.Problem(**pk)
+    I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), **ok)
+    J = oracle.Integrator(O, O.initial(), method=0, rtol=1e-6, atol=1e-10, internaleig=True)
+    yout = G.vector()
+    I.evolve(0.02, yout)
+    assert J.evolve(0.02) == 0
+    assert I.stats()["spectral_radius"] == J.stats()["spectral_radius"]
+    assert np.array_equal(yout.numpy(), J.y)
+
+
+def test_graphs_do_not_change_results(ctx, stslib, oracle):
+    pk = dict(kind=0, nx=64, ny=32, kx=1.0, ky=1.0)
+    ok = dict(method=1, rtol=1e-6, atol=1e-10)
+    a, _, _ = run_pair(ctx, stslib, oracle, pk, ok, [0.02], graphs=True)
+    b, _, _ = run_pair(ctx, stslib, oracle, pk, ok, [0.02], graphs=False)
+    assert np.array_equal(a, b)
+
+
+def test_golden_fixtures(ctx, stslib):
+    for name in ("oracle_rkc_17x9", "oracle_rkl_32", "oracle_rkl_mixed_32"):
+        g = np.load(os.path.join(GOLD, name + ".npz"))
+        pk = json.loads(str(g["problem"]))
+        ok = json.loads(str(g["opts"]))
+        G = stslib.Problem(ctx, **pk)
+        I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), **ok)
+        yout = G.vector()
+        I.evolve(float(g["tf"]), yout)
+        assert I.stats()["nst"] == int(g["nst"])
+        assert np.max(np.abs(yout.numpy() - g["y"])) <= 1e-12 * np.max(np.abs(g["y"]))
+
+
+def test_mixed_within_1e6_of_fp64(ctx, stslib):
+    """Same step sequence (fixed h): the FP32-increment error stays below 1e-6 rel L2."""
+    pk = dict(kind=0, nx=512, ny=512, kx=1.0, ky=0.01)
+    out = {}
+    for mixed in (False, True):
+        G = stslib.Problem(ctx, **pk)
+        I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), method=1, mixed=mixed, hfixed=1e-3)
+        y = G.vector()
+        I.evolve(0.05, y)
+        out[mixed] = y.numpy()
+    rel = np.linalg.norm(out[True] - out[False]) / np.linalg.norm(out[False])
+    assert rel < 1e-6
+
+
+def test_4096_rkl2_first_steps_bitwise(ctx, stslib, oracle):
+    """Config-2 size (4096^2, RKL2, rtol 1e-6, atol 1e-10): the first steps bit for bit."""
+    pk = dict(kind=0, nx=4096, ny=4096, kx=1.0, ky=1.0)
+    ok = dict(method=1, rtol=1e-6, atol=1e-10, maxsteps=2)
+    G = stslib.Problem(ctx, **pk)
+    O = oracle.Problem(**pk)
+    I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), **ok)
+    J = oracle.Integrator(O, O.initial(), **ok)
+    yout = G.vector()
+    I.evolve(0.1, yout)
+    J.evolve(0.1)
+    sg, so = I.stats(), J.stats()
+    assert sg["nst"] == so["nst"] == 2
+    assert sg["stage_max"] == so["stage_max"] and sg["stage_max"] > 100
+    assert np.array_equal(yout.numpy(), J.y)
+
+
+def test_8192_mixed_properties(ctx, stslib):
+    """Full config-3 size: a few mixed steps stay finite, near the exact solution, and
+    agree with the FP64 path on the same step sequence to 1e-6."""
+    pk = dict(kind=0, nx=8192, ny=8192, kx=1.0, ky=0.01)
+    out = {}
+    for mixed in (True, False):
+        G = stslib.Problem(ctx, **pk)
+        I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), method=1, rtol=1e-6, atol=1e-10,
+                            mixed=mixed, maxsteps=3)
+        y = G.vector()
+        t, rc = I.evolve(0.05, y)
+        out[mixed] = (y.numpy(), t, I.stats())
+        ex = G.exact(t).numpy()
+        err = np.linalg.norm(out[mixed][0] - ex) / np.linalg.norm(ex)
+        assert np.isfinite(out[mixed][0]).all() and err < 1e-4
+    assert out[True][1] == out[False][1]
+    rel = np.linalg.norm(out[True][0] - out[False][0]) / np.linalg.norm(out[False][0])
+    assert rel < 1e-6
+
+
+def test_generic_path_analytic_cr(ctx, stslib):
+    """analytic_CR_test.c: y' = lambda (y - atan t) + 1/(1+t^2), exact atan t."""
+    with open(os.path.join(GOLD, "reference_kats.json")) as f:
+        k = json.load(f)["analytic_CR"]
+    lam = k["lambda"]
+    L = stslib.lib()
+
+    def f(t, y, ydot):
+        L.N_VScale_Sts(lam, y.h, ydot.h)
+        L.N_VAddConst_Sts(ydot.h, 1.0 / (1.0 + t * t) - lam * math.atan(t), ydot.h)
+        return 0
+
+    y0 = stslib.NVector.from_numpy(ctx, np.array([k["y0"]]))
+    I = stslib.LSRKStep(ctx, f, 0.0, y0, method=1, rtol=k["rtol"], atol=k["atol"],
+                        smax=k["stage_max_limit"], dom_eig=lambda t: lam)
+    stslib.lib().STS_LSRKStepSetDomEigSafetyFactor(I.mem, k["eigsafety"])
+    stslib.lib().STS_LSRKStepSetDomEigFrequency(I.mem, k["eigfrequency"])
+    y = stslib.NVector(ctx, 1)
+    maxerr = 0.0
+    for i in range(1, k["nout"] + 1):
+        tout = k["tf"] * i / k["nout"]
+        t, rc = I.evolve(tout, y)
+        assert abs(t - tout) < 1e-14
+        maxerr = max(maxerr, abs(y.numpy()[0] - math.atan(t)))
+    assert maxerr < 1e-5
+    assert I.stats()["ndee"] == 1
+
+
+def test_generic_path_matches_fused(ctx, stslib):
+    pk = dict(kind=0, nx=32, ny=24, kx=1.0, ky=0.5)
+    G = stslib.Problem(ctx, **pk)
+    L = stslib.lib()
+
+    def f(t, y, ydot):
+        return L.STS_Diffusion(t, y.h, ydot.h, G.h)
+
+    out = []
+    for rhs in (G, f):
+        I = stslib.LSRKStep(ctx, rhs, 0.0, G.initial(), method=0, rtol=1e-6, atol=1e-10,
+                            dom_eig=lambda t: G.dom_eig())
+        y = G.vector()
+        I.evolve(0.05, y)
+        out.append(y.numpy())
+    assert np.linalg.norm(out[0] - out[1]) / np.linalg.norm(out[0]) < 1e-10
+
+
+def test_recoverable_rhs_failure_retries(ctx, stslib):
+    """Host-side fault injection: an RHS that returns +1 once (recoverable,
+    diffusion_2D.cpp:900-933 convention) makes the step retry with a smaller h; -1 aborts."""
+    pk = dict(kind=0, nx=16, ny=16)
+    G = stslib.Problem(ctx, **pk)
+    L = stslib.lib()
+    calls = {"n": 0}
+
+    def flaky(t, y, ydot):
+        calls["n"] += 1
+        if calls["n"] == 6:
+            return 1
+        return L.STS_Diffusion(t, y.h, ydot.h, G.h)
+
+    I = stslib.LSRKStep(ctx, flaky, 0.0, G.initial(), method=0, dom_eig=lambda t: G.dom_eig())
+    y = G.vector()
+    t, rc = I.evolve(0.01, y)
+    assert t == 0.01 and rc >= 0
+
+    def broken(t, y, ydot):
+        return -1
+
+    J = stslib.LSRKStep(ctx, broken, 0.0, G.initial(), method=0, dom_eig=lambda t: G.dom_eig())
+    with pytest.raises(stslib.STSError):
+        J.evolve(0.01, y)

@@ -1,0 +1,264 @@
+"""CPU tests: the oracle against the reference's known answers and analytic facts, and the
+product's host-side rules (stage coefficients, stage counts, controllers, tables, exact sum)
+against the oracle bit for bit. No GPU is used here."""
+import json
+import math
+import os
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def kats():
+    with open(os.path.join(GOLD, "reference_kats.json")) as f:
+        return json.load(f)
+
+
+# ---------------------------------------------------------------- exact reductions
+def exact_round(xs):
+    return float(sum((Fraction(float(x)) for x in xs), Fraction(0)))
+
+
+def test_xsum_is_exact_and_order_independent(oracle):
+    rng = np.random.default_rng(1)
+    for trial in range(20):
+        n = int(rng.integers(1, 3000))
+        e = rng.integers(-60, 40, size=n)
+        x = rng.standard_normal(n) * np.exp2(e)
+        want = exact_round(x)
+        assert oracle.xsum(x) == want
+        assert oracle.xsum(x[::-1]) == want
+        assert oracle.xsum(rng.permutation(x)) == want
+
+
+def test_xsum_edges(oracle):
+    assert oracle.xsum(np.zeros(0)) == 0.0
+    assert oracle.xsum(np.array([1e18, 1.0, -1e18])) == 1.0
+    assert oracle.xsum(np.array([2.0 ** -170])) == 0.0  # below the 2^-160 grid
+    assert math.isnan(oracle.xsum(np.array([1.0, np.nan])))
+    assert math.isinf(oracle.xsum(np.array([1.0, np.inf])))
+    assert oracle.xsum(np.array([2.0 ** 70])) == 2.0 ** 70
+    assert math.isinf(oracle.xsum(np.array([2.0 ** 130])))
+
+
+def test_product_host_exact_sum_matches_oracle(oracle, stslib):
+    L = stslib.lib()
+    rng = np.random.default_rng(2)
+    for trial in range(20):
+        n = int(rng.integers(1, 2000))
+        x = rng.standard_normal(n) * np.exp2(rng.integers(-150, 125, size=n))
+        x[np.abs(x) > 2.0 ** 127] = 1.0
+        got = L.STS_ExactSumHost(x.ctypes.data_as(stslib._dp), n)
+        assert got == oracle.xsum(x)
+    for special in ([np.nan, 1.0], [np.inf], [2.0 ** 128], [2.0 ** 100, -1.0], []):
+        a = np.array(special, dtype=np.float64)
+        g = L.STS_ExactSumHost(a.ctypes.data_as(stslib._dp), a.size)
+        o = oracle.xsum(a)
+        assert (math.isnan(g) and math.isnan(o)) or g == o
+
+
+def test_nvector_reduction_kats(oracle):
+    """WRMS and max-norm known answers of test_nvector_gkylzero.c:185-198, 292-303."""
+    k = kats()
+    n = k["shape"][0] * k["shape"][1]
+    x = np.full(n, k["wrms"]["x"])
+    w = np.full(n, k["wrms"]["w"])
+    assert abs(oracle.wrms(x, w) - k["wrms"]["expect"]) <= k["tolerance"]
+    assert oracle.maxnorm(np.zeros(n)) == k["maxnorm"]["expect"]
+    r = np.arange(n, dtype=np.float64)
+    assert oracle.xdot(r, r) == exact_round(r * r)
+
+
+# ---------------------------------------------------------------- method coefficients
+def stability_function(c, z):
+    mu, nu, mus, ajm1, _ = c
+    s = len(mu) - 1
+    y0, f0 = 1.0, z
+    ym2, ym1 = y0, y0 + mus[1] * f0
+    for j in range(2, s + 1):
+        yj = mu[j] * ym1 + nu[j] * ym2 + (1 - mu[j] - nu[j]) * y0 + mus[j] * (z * ym1) - mus[j] * ajm1[j] * f0
+        ym2, ym1 = ym1, yj
+    return ym1
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_stage_coefficients_second_order_and_stable(oracle, method):
+    for s in (2, 3, 5, 10, 40, 120, 200):
+        c = oracle.stage_coeffs(method, s)
+        for z in (-1e-2, -2e-2):
+            R = stability_function(c, z)
+            assert abs(R - (1 + z + z * z / 2)) < 0.3 * abs(z) ** 3 + 1e-15
+        if method == 0:  # RKC stability boundary (1 + w0)/w1
+            w0 = 1 + 2 / (13 * s * s)
+            w1 = c[2][1] * (2 * w0) ** 2
+            beta = (1 + w0) / w1
+        else:
+            beta = (s * s + s - 2) / 2.0
+        for z in np.linspace(-beta * 0.999, 0.0, 401):
+            assert abs(stability_function(c, z)) <= 1.0 + 1e-9
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_product_coefficients_equal_oracle(oracle, stslib, method):
+    L = stslib.lib()
+    for s in range(2, 201):
+        o = oracle.stage_coeffs(method, s)
+        g = [np.zeros(s + 1) for _ in range(5)]
+        assert L.STS_LSRKStageCoeffs(method, s, *[a.ctypes.data_as(stslib._dp) for a in g]) == 0
+        for a, b in zip(o, g):
+            assert np.array_equal(a[1:], b[1:])
+
+
+def test_product_step_rules_equal_oracle(oracle, stslib):
+    import ctypes as C
+    L = stslib.lib()
+    rng = np.random.default_rng(3)
+    for _ in range(500):
+        method = int(rng.integers(0, 2))
+        h = float(10 ** rng.uniform(-8, -1))
+        rho = float(10 ** rng.uniform(2, 9))
+        smax = int(rng.integers(2, 400))
+        hm = C.c_double()
+        s = L.STS_LSRKStagesNeeded(method, h, rho, smax, C.byref(hm))
+        so, hmo = oracle.stages_needed(method, h, rho, smax)
+        assert s == so and hm.value == hmo
+        ctrl = int(rng.integers(0, 3))
+        dsm, ep1, ep2 = (float(10 ** rng.uniform(-4, 1)) for _ in range(3))
+        nh = int(rng.integers(0, 4))
+        assert L.STS_AdaptControllerEstimate(ctrl, h, dsm, ep1, ep2, nh) == \
+            oracle.controller(ctrl, h, dsm, ep1, ep2, nh)
+
+
+def test_product_tables_equal_oracle(oracle, stslib):
+    L = stslib.lib()
+    for nx, ny in ((17, 9), (128, 128), (1000, 3)):
+        P = oracle.Problem(oracle.MANUFACTURED, nx, ny)
+        Sx, Sxx, Sy, Syy = P.tables()
+        for n, S0, D0 in ((nx, Sx, Sxx), (ny, Sy, Syy)):
+            S = np.zeros(n)
+            D = np.zeros(n)
+            L.STS_ManufacturedTables(n, 1.0 / (n + 1), S.ctypes.data_as(stslib._dp),
+                                     D.ctypes.data_as(stslib._dp))
+            assert np.array_equal(S, S0) and np.array_equal(D, D0)
+
+
+# ---------------------------------------------------------------- oracle physics
+def test_kernel_form_rhs_matches_reference_form(oracle):
+    for kx, ky in ((1.0, 1.0), (1.0, 0.01)):
+        P = oracle.Problem(oracle.MANUFACTURED, 33, 17, kx=kx, ky=ky)
+        rng = np.random.default_rng(4)
+        u = rng.standard_normal(P.n)
+        for t in (0.0, 0.13):
+            a = P.rhs(t, u)
+            b = P.rhs(t, u, ref=True)
+            assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
+
+
+def test_manufactured_rhs_is_consistent(oracle):
+    """F(t, u_exact) -> u_exact_t as the grid is refined (second order)."""
+    errs = []
+    for n in (32, 64, 128):
+        P = oracle.Problem(oracle.MANUFACTURED, n)
+        t = 0.1
+        f = P.rhs(t, P.exact(t))
+        Sx, _, Sy, _ = P.tables()
+        ut = np.outer(Sy, Sx).ravel() * oracle.lib().orc_cdot(t)
+        errs.append(np.max(np.abs(f - ut)))
+    assert errs[0] / errs[1] > 3.5 and errs[1] / errs[2] > 3.5
+
+
+def test_spatial_convergence_second_order(oracle):
+    """Discretisation error of the full STS run decreases as O(dx^2)."""
+    errs = []
+    for n in (16, 32, 64):
+        P = oracle.Problem(oracle.MANUFACTURED, n)
+        I = oracle.Integrator(P, P.initial(), method=oracle.RKC, rtol=1e-9, atol=1e-12)
+        assert I.evolve(0.25) == 0
+        ex = P.exact(0.25)
+        errs.append(np.linalg.norm(I.y - ex) / np.linalg.norm(ex))
+    assert errs[0] / errs[1] > 3.5 and errs[1] / errs[2] > 3.5
+
+
+def test_power_iteration_closed_form_spectral_radius(oracle):
+    nx, ny, kx, ky = 16, 12, 1.0, 0.3
+    P = oracle.Problem(oracle.MANUFACTURED, nx, ny, kx=kx, ky=ky)
+    dx, dy = 1.0 / (nx + 1), 1.0 / (ny + 1)
+    rho = 4 * kx / dx ** 2 * math.sin(nx * math.pi / (2 * (nx + 1))) ** 2 + \
+        4 * ky / dy ** 2 * math.sin(ny * math.pi / (2 * (ny + 1))) ** 2
+    v0 = np.random.default_rng(6).standard_normal(P.n)
+    lam, it, _ = P.power_iteration(v0, maxiters=5000, reltol=1e-12)
+    assert abs(-lam - rho) / rho < 1e-4
+    assert -P.dom_eig() >= rho  # main.cpp:544 is an upper bound
+
+
+def test_pcg_solves_shifted_operator(oracle):
+    P = oracle.Problem(oracle.MANUFACTURED, 64, 48, kx=1.0, ky=0.05)
+    gamma = 1e-3
+    rng = np.random.default_rng(5)
+    xs = rng.standard_normal(P.n)
+    b = xs - gamma * P.apply_A(xs)
+    for jac in (True, False):
+        x, it, rel = P.pcg(gamma, b, tol=1e-10, jacobi=jac)
+        assert rel <= 1e-10
+        assert np.linalg.norm(x - xs) / np.linalg.norm(xs) < 1e-7
+        assert 1 <= it < 2000
+
+
+def test_sdirk2_second_order_in_time(oracle):
+    P = oracle.Problem(oracle.MANUFACTURED, 24)
+    y0 = P.initial()
+    ref, _ = P.sdirk2(y0, 0.0, 0.2 / 256, 256, tol=1e-13)
+    e = []
+    for m in (8, 16):
+        y, _ = P.sdirk2(y0, 0.0, 0.2 / m, m, tol=1e-13)
+        e.append(np.linalg.norm(y - ref))
+    assert 3.0 < e[0] / e[1] < 5.0
+
+
+def test_mixed_matches_fp64_for_equal_steps(oracle):
+    P = oracle.Problem(oracle.MANUFACTURED, 96, kx=1.0, ky=0.01)
+    out = {}
+    for mixed in (False, True):
+        I = oracle.Integrator(P, P.initial(), method=oracle.RKL, mixed=mixed, hfixed=2e-3)
+        assert I.evolve(0.05) == 0
+        out[mixed] = I.y
+    rel = np.linalg.norm(out[True] - out[False]) / np.linalg.norm(out[False])
+    assert rel < 1e-6
+
+
+def test_oracle_reproduces_golden_runs(oracle):
+    """Pins the oracle's integrator across machines (libm may differ by an ulp)."""
+    for name in ("oracle_rkc_17x9", "oracle_rkl_32", "oracle_rkl_mixed_32"):
+        g = np.load(os.path.join(GOLD, name + ".npz"))
+        pk = json.loads(str(g["problem"]))
+        ok = json.loads(str(g["opts"]))
+        P = oracle.Problem(**pk)
+        I = oracle.Integrator(P, P.initial(), **ok)
+        assert I.evolve(float(g["tf"])) == 0
+        assert I.stats()["nst"] == int(g["nst"])
+        assert np.max(np.abs(I.y - g["y"])) <= 1e-12 * np.max(np.abs(g["y"]))
+
+
+# ---------------------------------------------------------------- the C ABI
+def header_functions():
+    import re
+    root = os.path.dirname(GOLD)
+    src = open(os.path.join(os.path.dirname(root), "include", "stsgpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"struct _generic_N_Vector_Ops \{.*?\};", "", src, flags=re.S)
+    typedefs = set(re.findall(r"\(\s*\*\s*(\w+)\s*\)", src))
+    names = re.findall(r"\b((?:STS|N_V)\w+)\s*\(", src)
+    return sorted(set(n for n in names if n not in typedefs))
+
+
+def test_library_exports_every_declared_symbol(stslib):
+    L = stslib.lib()
+    names = header_functions()
+    assert len(names) > 60
+    for n in names:
+        assert hasattr(L, n), n
+    declared = {s[0] for s in stslib.SIGNATURES}
+    assert set(names) == declared
