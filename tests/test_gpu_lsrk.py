@@ -61,8 +61,8 @@ def test_mixed_bitwise(ctx, stslib, oracle, method):
 
 
 def test_unforced_and_small_stage_cap_bitwise(ctx, stslib, oracle):
-    pk = dict(kind=1, nx=64, ny=48, kx=0.2, ky=0.9)
-    ok = dict(method=1, rtol=1e-6, atol=1e-12, smax=12)
+    pk = dict(kind=1, nx=128, ny=80, kx=0.2, ky=0.9)
+    ok = dict(method=1, rtol=1e-3, atol=1e-6, smax=4)
     G = stslib.Problem(ctx, **pk)
     O = oracle.Problem(**pk)
     pm, qm, amp = [1, 3, 7], [2, 5, 1], [1.0, -0.5, 0.25]
@@ -72,7 +72,9 @@ def test_unforced_and_small_stage_cap_bitwise(ctx, stslib, oracle):
     yout = G.vector()
     I.evolve(0.01, yout)
     assert J.evolve(0.01) == 0
-    assert I.stats()["stage_max"] == 12
+    sg, so = I.stats(), J.stats()
+    assert sg["stage_max"] == so["stage_max"] == 4
+    assert sg["nst_exp"] == so["nst_exp"] > 0
     assert np.array_equal(yout.numpy(), J.y)
 
 
