@@ -29,6 +29,7 @@ RKC, RKL = 0, 1
 PID, PI, I = 0, 1, 2
 MANUFACTURED, UNFORCED, PERIODIC = 0, 1, 2
 NORMAL, ONE_STEP = 1, 2
+TOO_MUCH_WORK = -1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -149,6 +150,19 @@ SIGNATURES = [
 ]
 
 _lib = None
+_exiting = False
+
+
+def _at_exit():
+    # At interpreter exit the order in which objects are finalised is arbitrary; a vector
+    # finalised after its context would touch freed memory. The process is ending, so the
+    # driver reclaims everything: stop freeing from finalisers.
+    global _exiting
+    _exiting = True
+
+
+import atexit  # noqa: E402
+atexit.register(_at_exit)
 
 
 def lib(build=True):
@@ -193,7 +207,7 @@ class Context:
         return lib().STS_ContextGetStream(self.h)
 
     def free(self):
-        if self.h:
+        if self.h and not _exiting:
             lib().STS_ContextFree(C.byref(self.h))
 
     def __del__(self):
@@ -250,7 +264,7 @@ class NVector:
         return NVector(self.ctx, handle=lib().N_VClone_Sts(self.h))
 
     def destroy(self):
-        if self.own and self.h:
+        if self.own and self.h and not _exiting:
             lib().N_VDestroy_Sts(self.h)
             self.h = None
 
@@ -370,7 +384,7 @@ class Problem:
         return lib().STS_PSolve(0.0, None, None, r.h, z.h, gamma, 0.0, 2, self.h)
 
     def free(self):
-        if self.h:
+        if self.h and not _exiting:
             lib().STS_ProblemFree(C.byref(C.c_void_p(self.h)))
             self.h = None
 
@@ -434,9 +448,11 @@ class LSRKStep:
             L.STS_LSRKStepSetDomEigFn(self.mem, C.cast(L.STS_DomEig, _vp))
 
     def evolve(self, tout, yout, itask=NORMAL):
+        """Returns (t, flag); flag TOO_MUCH_WORK (-1) means the step limit of this call was
+        reached before tout (the state at t is valid); other negative flags raise."""
         t = C.c_double()
         rc = lib().STS_ARKodeEvolve(self.mem, tout, yout.h, C.byref(t), itask)
-        if rc < 0:
+        if rc < TOO_MUCH_WORK:
             _err("STS_ARKodeEvolve returned %d" % rc)
         return t.value, rc
 
@@ -465,7 +481,7 @@ class LSRKStep:
         return buf.value.decode()
 
     def free(self):
-        if self.mem:
+        if self.mem and not _exiting:
             m = _vp(self.mem)
             lib().STS_ARKodeFree(C.byref(m))
             self.mem = None
@@ -504,7 +520,8 @@ class PCGSolver:
 
     def __del__(self):
         try:
-            lib().STS_SUNLinSolFree(self.LS)
+            if not _exiting:
+                lib().STS_SUNLinSolFree(self.LS)
         except Exception:
             pass
 

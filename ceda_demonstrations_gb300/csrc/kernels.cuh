@@ -403,3 +403,27 @@ __global__ void __launch_bounds__(256) wrms_ewt_kernel(long long n, const double
   }
   xsum_block_finish<256>(acc, flags, w, slot, 1, (double)n);
 }
+
+// exact reductions: mode 0 = sum x*y, 1 = sum (x*w)^2 -> sqrt(./n)
+template <int MODE>
+__global__ void __launch_bounds__(256) xred_kernel(long long n, const double* __restrict__ x,
+                                                   const double* __restrict__ y, RedWork* w,
+                                                   double* slot)
+{
+  xsum::Limbs acc;
+  xsum::zero(acc);
+  unsigned flags         = 0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
+  {
+    double v;
+    if constexpr (MODE == 0) v = __dmul_rn(x[k], y[k]);
+    else
+    {
+      double q = __dmul_rn(x[k], y[k]);
+      v        = __dmul_rn(q, q);
+    }
+    xsum::add(acc, v, flags);
+  }
+  xsum_block_finish<256>(acc, flags, w, slot, MODE, (double)n);
+}
