@@ -123,6 +123,7 @@ SIGNATURES = [
     ("STS_ARKodeSetMaxNumSteps", C.c_int, [_vp, _ll]),
     ("STS_ARKodeSetStopTime", C.c_int, [_vp, C.c_double]),
     ("STS_LSRKStepSetMixedPrecision", C.c_int, [_vp, C.c_int]),
+    ("STS_LSRKStepSetStageKernel", C.c_int, [_vp, C.c_int]),
     ("STS_LSRKStepSetUseGraphs", C.c_int, [_vp, C.c_int]),
     ("STS_ARKodeEvolve", C.c_int, [_vp, C.c_double, _NV, _dp, C.c_int]),
     ("STS_ARKodeReset", C.c_int, [_vp, C.c_double, _NV]),
@@ -196,6 +197,7 @@ class Context:
 
     def __init__(self, device=0):
         self.h = _vp()
+        self.live = 0  # objects holding C resources of this context
         if lib().STS_ContextCreate(device, C.byref(self.h)) != 0:
             _err("STS_ContextCreate")
 
@@ -207,8 +209,12 @@ class Context:
         return lib().STS_ContextGetStream(self.h)
 
     def free(self):
-        if self.h and not _exiting:
+        # Garbage collection of reference cycles (for example frames kept by a traceback)
+        # may finalise the context before objects that still use it; then it is left for
+        # process exit instead of being freed under them.
+        if self.h and not _exiting and self.live <= 0:
             lib().STS_ContextFree(C.byref(self.h))
+            self.h = None
 
     def __del__(self):
         try:
@@ -229,6 +235,8 @@ class NVector:
             if not self.h:
                 _err("N_VNew_Sts")
         self.own = own
+        if own:
+            ctx.live += 1
 
     @classmethod
     def from_numpy(cls, ctx, a):
@@ -267,6 +275,7 @@ class NVector:
         if self.own and self.h and not _exiting:
             lib().N_VDestroy_Sts(self.h)
             self.h = None
+            self.ctx.live -= 1
 
     def __del__(self):
         try:
@@ -327,6 +336,7 @@ class Problem:
                                          yl, yu)
         if not self.h:
             _err("STS_ProblemCreate")
+        ctx.live += 1
 
     @property
     def n(self):
@@ -387,6 +397,7 @@ class Problem:
         if self.h and not _exiting:
             lib().STS_ProblemFree(C.byref(C.c_void_p(self.h)))
             self.h = None
+            self.ctx.live -= 1
 
     def __del__(self):
         try:
@@ -403,7 +414,7 @@ class LSRKStep:
 
     def __init__(self, ctx, rhs, t0, y0, method=RKC, rtol=1e-6, atol=1e-10, controller=PID,
                  smax=200, mixed=False, graphs=True, dom_eig=None, power=None, maxsteps=100000,
-                 hfixed=0.0):
+                 hfixed=0.0, stage_kernel=0):
         self.ctx = ctx
         L = lib()
         self._keep = []
@@ -422,6 +433,7 @@ class LSRKStep:
         self.mem = L.STS_LSRKStepCreateSTS(fn, t0, y0.h, ctx.h)
         if not self.mem:
             _err("STS_LSRKStepCreateSTS")
+        ctx.live += 1
         self.n = len(y0)
         L.STS_ARKodeSetUserData(self.mem, ud)
         L.STS_LSRKStepSetSTSMethod(self.mem, method)
@@ -430,6 +442,7 @@ class LSRKStep:
         L.STS_LSRKStepSetMaxNumStages(self.mem, smax)
         L.STS_LSRKStepSetMixedPrecision(self.mem, int(mixed))
         L.STS_LSRKStepSetUseGraphs(self.mem, int(graphs))
+        L.STS_LSRKStepSetStageKernel(self.mem, int(stage_kernel))
         L.STS_ARKodeSetMaxNumSteps(self.mem, maxsteps)
         if hfixed > 0:
             L.STS_ARKodeSetFixedStep(self.mem, hfixed)
@@ -485,6 +498,7 @@ class LSRKStep:
             m = _vp(self.mem)
             lib().STS_ARKodeFree(C.byref(m))
             self.mem = None
+            self.ctx.live -= 1
 
     def __del__(self):
         try:
@@ -500,6 +514,7 @@ class PCGSolver:
         L = lib()
         self.ctx = ctx
         self.LS = L.STS_SUNLinSol_PCG(y.h, 2 if psolve else 0, maxl, ctx.h)
+        ctx.live += 1
         self._keep = []
 
         def at(_d, v, z):
@@ -520,8 +535,10 @@ class PCGSolver:
 
     def __del__(self):
         try:
-            if not _exiting:
+            if not _exiting and self.LS:
                 lib().STS_SUNLinSolFree(self.LS)
+                self.LS = None
+                self.ctx.live -= 1
         except Exception:
             pass
 

@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "stage_tma.cuh"
 #include "sts_internal.cuh"
 
 void sts_f64_to_f32(STS_Context ctx, const double* a, float* b, long long n);
@@ -191,6 +192,8 @@ struct LSRKMem {
   double tstop          = INFINITY;
   bool mixed            = false;
   bool use_graphs       = true;
+  int stage_variant     = 0; // 0: TMA-pipelined mixed stage where supported, 1: register marching
+  TmaStage32 tma;
   long long n           = 0;
 
   // state (mirrors the oracle's orc_state)
@@ -295,6 +298,11 @@ static int ensure_stage_buffers(LSRKMem* m)
     if (!m->mixed && !m->Y[b] && !STS_CUDA_OK(cudaMalloc(&m->Y[b], n8))) return -1;
     if (m->mixed && !m->D[b] && !STS_CUDA_OK(cudaMalloc(&m->D[b], n4))) return -1;
   }
+  if (m->mixed && !m->tma.ok && m->stage_variant == 0)
+  {
+    STS_Problem p = (STS_Problem)m->user_data;
+    if (tma_stage32_supported(p->nx, p->ny)) tma_stage32_prepare(&m->tma, m->D, m->Ffb, p->nx, p->ny);
+  }
   return 0;
 }
 
@@ -347,6 +355,19 @@ static void launch_stage64(LSRKMem* m, STS_Problem p, const StageArgs* A, const 
       stage64_kernel<1, RY, decltype(F)::value><<<g, b, 0, m->ctx->stream>>>(p->dev, A, ym1, ym2, y0, f0, yj);
     });
   }
+}
+
+static void launch_stage32(LSRKMem* m, STS_Problem p, const StageArgs* A, const float* dm1, const float* dm2,
+                           const float* f0f, float* dj);
+
+// mixed stage by buffer index (TMA path when prepared)
+static void launch_stage32_idx(LSRKMem* m, STS_Problem p, const StageArgs* A, int im1, int im2, int par, int iout)
+{
+  if (m->stage_variant == 0 && m->tma.ok &&
+      tma_stage32_launch(&m->tma, m->ctx->num_sms, p->dev, A, im1, im2, par, m->D[iout], m->ctx->d_err,
+                         m->ctx->stream))
+    return;
+  launch_stage32(m, p, A, m->D[im1], im2 >= 0 ? m->D[im2] : nullptr, m->Ffb[par], m->D[iout]);
 }
 
 static void launch_stage32(LSRKMem* m, STS_Problem p, const StageArgs* A, const float* dm1, const float* dm2,
@@ -422,20 +443,17 @@ static void record_step(LSRKMem* m, STS_Problem p, int s, int par)
   }
   else
   {
-    float* bufs[3] = {m->D[0], m->D[1], m->D[2]};
-    stage1_32_kernel<<<eb, 256, 0, st>>>(n, dstep(m), m->Ffb[par], bufs[0]);
-    const float* dm2 = nullptr;
-    const float* dm1 = bufs[0];
-    int bi           = 1;
+    stage1_32_kernel<<<eb, 256, 0, st>>>(n, dstep(m), m->Ffb[par], m->D[0]);
+    int im2 = -1, im1 = 0, bi = 1;
     for (int j = 2; j <= s; ++j)
     {
-      float* dj = bufs[bi];
-      bi        = (bi + 1) % 3;
-      launch_stage32(m, p, dstage(m) + j, dm1, dm2, m->Ffb[par], dj);
-      dm2 = dm1;
-      dm1 = dj;
+      const int ij = bi;
+      bi           = (bi + 1) % 3;
+      launch_stage32_idx(m, p, dstage(m) + j, im1, im2, par, ij);
+      im2 = im1;
+      im1 = ij;
     }
-    launch_stepend(m, p, par, nullptr, dm1);
+    launch_stepend(m, p, par, nullptr, m->D[im1]);
   }
 }
 
@@ -712,6 +730,12 @@ static int evolve_fused(LSRKMem* m, double target, int itask)
       fill_params(m, p, m->t, h, s, mu, nu, mus, ajm1, cjm1);
       if (run_step_fused(m, p, s)) return STS_ERR_FAILURE;
       if (!STS_CUDA_OK(cudaStreamSynchronize(st))) return STS_ERR_FAILURE;
+      if (*(volatile int*)m->ctx->h_err)
+      {
+        *m->ctx->h_err = 0;
+        sts_set_error("LSRKStep: a stage kernel's pipeline wait timed out");
+        return STS_ERR_FAILURE;
+      }
       const double dsm = ((volatile double*)m->ctx->h_slots)[SLOT_DSM];
       m->nfe += s;
       m->stages_total += s;
@@ -983,6 +1007,20 @@ extern "C" int STS_LSRKStepSetMixedPrecision(void* mem, int on)
   MEM(mem)->mixed = on != 0;
   return 0;
 }
+extern "C" int STS_LSRKStepSetStageKernel(void* mem, int variant)
+{
+  CHECK_MEM(mem);
+  if (variant < 0 || variant > 1) return STS_ILL_INPUT;
+  LSRKMem* m = MEM(mem);
+  if (m->stage_variant != variant)
+  {
+    for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+    m->graphs.clear();
+  }
+  m->stage_variant = variant;
+  return 0;
+}
+
 extern "C" int STS_LSRKStepSetUseGraphs(void* mem, int on)
 {
   CHECK_MEM(mem);
@@ -1068,7 +1106,7 @@ extern "C" int STS_LSRKStepTimeStageKernel(void* mem, int nlaunch, double* ms_pe
   cudaEventCreate(&e1);
   // the parameter block of the last step is still on the device
   auto one = [&](int k) {
-    if (m->mixed) launch_stage32(m, p, dstage(m) + j, m->D[k % 3], m->D[(k + 1) % 3], m->Ffb[m->par], m->D[(k + 2) % 3]);
+    if (m->mixed) launch_stage32_idx(m, p, dstage(m) + j, k % 3, (k + 1) % 3, m->par, (k + 2) % 3);
     else launch_stage64(m, p, dstage(m) + j, m->Y[k % 3], m->Y[(k + 1) % 3], m->yb[m->par], m->Fb[m->par], m->Y[(k + 2) % 3]);
   };
   one(0); // warm

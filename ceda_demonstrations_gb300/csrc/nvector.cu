@@ -68,6 +68,9 @@ extern "C" int STS_ContextCreate(int device, STS_Context* out)
     goto fail;
   if (!STS_CUDA_OK(cudaHostGetDevicePointer(&c->d_slots, c->h_slots, 0))) goto fail;
   memset(c->h_slots, 0, STS_NSLOTS * sizeof(double));
+  if (!STS_CUDA_OK(cudaHostAlloc(&c->h_err, sizeof(int), cudaHostAllocMapped))) goto fail;
+  if (!STS_CUDA_OK(cudaHostGetDevicePointer(&c->d_err, c->h_err, 0))) goto fail;
+  *c->h_err = 0;
   *out = c;
   return 0;
 fail:
@@ -83,6 +86,7 @@ extern "C" int STS_ContextFree(STS_Context* pc)
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->d_work) cudaFree(c->d_work);
   if (c->h_slots) cudaFreeHost(c->h_slots);
+  if (c->h_err) cudaFreeHost(c->h_err);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   *pc = nullptr;
@@ -268,6 +272,7 @@ extern "C" N_Vector N_VNewEmpty_Sts(STS_Context ctx)
   v->ops     = make_ops();
   v->content = new NVContent();
   v->sunctx  = ctx;
+  NVC(v)->device = ctx->device;
   return v;
 }
 
@@ -341,9 +346,11 @@ extern "C" void N_VDestroy_Sts(N_Vector v)
   if (c)
   {
     if (c->own && c->data)
-    {
-      ctx_activate(v->sunctx);
-      cudaStreamSynchronize(v->sunctx->stream);
+    { // cudaFree waits for work using the buffer; the context is not touched, so a vector
+      // may outlive the context that made it
+      int cur = -1;
+      cudaGetDevice(&cur);
+      if (cur != c->device) cudaSetDevice(c->device);
       cudaFree(c->data);
     }
     delete c;

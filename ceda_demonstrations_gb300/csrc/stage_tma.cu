@@ -1,0 +1,333 @@
+// Mixed (FP32-increment) stage kernel with TMA tile loads and an mbarrier pipeline.
+//
+// Persistent CTAs (one per SM, 256 threads) walk 128 x 32 output tiles. For each tile the
+// CTA's issuing thread starts three bulk tensor copies into one slot of a 3-deep shared
+// memory ring: the d_{j-1} tile with a 4-column / 1-row halo (its out-of-range parts are
+// zero-filled by the copy engine, which is exactly the homogeneous Dirichlet boundary), the
+// d_{j-2} tile and the F_0 tile. Two tiles are always in flight while the CTA computes a
+// third, so the bytes in flight per SM no longer depend on registers or occupancy. Each warp
+// computes four rows: a lane owns four consecutive columns, the west/east neighbours come
+// from the neighbouring lanes by shuffle (the halo columns from shared memory), and the
+// rows above/below march through registers. The result goes straight to global memory with
+// 16-byte stores. The arithmetic per point is the one of stage32_kernel (kernels.cuh), so
+// both kernels give identical bits.
+//
+// Waits on the pipeline barriers are bounded: a wait that does not complete sets the
+// context's error word, the CTA stops issuing, drains (again bounded) the copies it has in
+// flight and returns; the host turns the error word into a failed step.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+
+#include "kernels.cuh"
+#include "stage_tma.cuh"
+#include "sts_internal.cuh"
+
+namespace {
+
+constexpr int TW = 128, TH = 32;          // output tile
+constexpr int HW = TW + 8, HH = TH + 2;   // halo tile (x from x0-4 keeps 16-byte alignment)
+constexpr int NST = 3;                    // pipeline depth
+constexpr int HALO_BYTES = HW * HH * 4;   // 18496
+constexpr int HALO_PAD   = 18560;         // rounded to 128 B
+constexpr int PL_BYTES   = TW * TH * 4;   // 16384
+constexpr int SLOT_BYTES = HALO_PAD + 2 * PL_BYTES;
+constexpr int SMEM_BYTES = NST * SLOT_BYTES + 64; // + the NST pipeline barriers
+constexpr long long WAIT_LIMIT = 1LL << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile(
+    "{\n\t.reg .pred p;\n\t"
+    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+    "selp.u32 %0, 1, 0, p;\n\t}"
+    : "=r"(ok)
+    : "r"(smem_u32(bar)), "r"(parity)
+    : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+{
+  for (long long i = 0; i < WAIT_LIMIT; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y)
+{
+  asm volatile(
+    "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+      smem_u32(dst)),
+    "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+    : "memory");
+}
+
+template <bool HAS_M2>
+__device__ __forceinline__ void issue_tile(unsigned char* slot, uint64_t* bar, const CUtensorMap* mh,
+                                           const CUtensorMap* mm2, const CUtensorMap* mf0, int tile,
+                                           int tiles_x)
+{
+  const int x0 = (tile % tiles_x) * TW;
+  const int y0 = (tile / tiles_x) * TH;
+  mbar_expect_tx(bar, HALO_BYTES + (HAS_M2 ? 2 : 1) * PL_BYTES);
+  tma_load_2d(slot, mh, bar, x0 - 4, y0 - 1);
+  if (HAS_M2) tma_load_2d(slot + HALO_PAD, mm2, bar, x0, y0);
+  tma_load_2d(slot + HALO_PAD + PL_BYTES, mf0, bar, x0, y0);
+}
+
+template <bool FORCED, bool HAS_M2>
+__global__ void __launch_bounds__(256, 1)
+  stage32_tma_kernel(const __grid_constant__ CUtensorMap mh, const __grid_constant__ CUtensorMap mm2,
+                     const __grid_constant__ CUtensorMap mf0, ProbDev P, const StageArgs* __restrict__ A,
+                     float* __restrict__ out, int* err)
+{
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NST * SLOT_BYTES);
+  const int nx = (int)P.nx, ny = (int)P.ny;
+  const int tiles_x = (nx + TW - 1) / TW;
+  const int ntiles  = tiles_x * ((ny + TH - 1) / TH);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  if (tid == 0)
+  {
+    for (int s = 0; s < NST; ++s) mbar_init(&bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int k = 0; k < NST; ++k)
+    {
+      const int t = blockIdx.x + k * gridDim.x;
+      if (t < ntiles) issue_tile<HAS_M2>(smem + k * SLOT_BYTES, &bar[k], &mh, &mm2, &mf0, t, tiles_x);
+    }
+
+  const float gc = A->gcf, gx = A->gxf, gy = A->gyf, gn = A->gnf, gF = A->gFf;
+  const float al = A->alf, be = A->bef, ga = A->gaf;
+  bool failed = false;
+  int k       = 0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++k)
+  {
+    const int s             = k % NST;
+    const uint32_t parity   = (uint32_t)((k / NST) & 1);
+    const bool ok           = mbar_wait_bounded(&bar[s], parity);
+    if (__syncthreads_or(!ok))
+    {
+      failed = true;
+      break;
+    }
+    const float* halo = reinterpret_cast<const float*>(smem + s * SLOT_BYTES);
+    const float* m2s  = reinterpret_cast<const float*>(smem + s * SLOT_BYTES + HALO_PAD);
+    const float* f0s  = reinterpret_cast<const float*>(smem + s * SLOT_BYTES + HALO_PAD + PL_BYTES);
+    const int x0 = (t % tiles_x) * TW, y0 = (t / tiles_x) * TH;
+    const int x  = x0 + lane * 4;
+    const int c  = 4 + lane * 4; // column of x in the halo tile
+    float Pi[4], Qi[4];
+    if (FORCED)
+    {
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+      {
+        const bool in = x + v < nx;
+        const float sx = in ? __ldg(P.Sxf + x + v) : 0.0f, sxx = in ? __ldg(P.Sxxf + x + v) : 0.0f;
+        Pi[v] = __fmaf_rn(al, sx, be * sxx);
+        Qi[v] = ga * sx;
+      }
+    }
+    const int r0 = warp * 4; // tile rows r0 .. r0+3 -> halo rows r0+1 .. r0+4
+    float4 up  = *reinterpret_cast<const float4*>(halo + (r0 + 0) * HW + c);
+    float4 cur = *reinterpret_cast<const float4*>(halo + (r0 + 1) * HW + c);
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr)
+    {
+      const int r    = r0 + rr;
+      const float4 dn = *reinterpret_cast<const float4*>(halo + (r + 2) * HW + c);
+      float w         = __shfl_up_sync(0xffffffffu, cur.w, 1);
+      float e         = __shfl_down_sync(0xffffffffu, cur.x, 1);
+      if (lane == 0) w = halo[(r + 1) * HW + 3];
+      if (lane == 31) e = halo[(r + 1) * HW + 4 + TW];
+      float4 m2 = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (HAS_M2) m2 = *reinterpret_cast<const float4*>(m2s + r * TW + lane * 4);
+      const float4 q0 = *reinterpret_cast<const float4*>(f0s + r * TW + lane * 4);
+      const int y     = y0 + r;
+      float syj = 0.0f, syyj = 0.0f;
+      if (FORCED && y < ny)
+      {
+        syj  = __ldg(P.Syf + y);
+        syyj = __ldg(P.Syyf + y);
+      }
+      const float cv[4]  = {cur.x, cur.y, cur.z, cur.w};
+      const float uv[4]  = {up.x, up.y, up.z, up.w};
+      const float dv[4]  = {dn.x, dn.y, dn.z, dn.w};
+      const float mv[4]  = {m2.x, m2.y, m2.z, m2.w};
+      const float qv[4]  = {q0.x, q0.y, q0.z, q0.w};
+      float o[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+      {
+        const float uw = (v == 0) ? w : cv[v - 1];
+        const float ue = (v == 3) ? e : cv[v + 1];
+        const float sx = uw + ue, sy = uv[v] + dv[v];
+        float acc      = gc * cv[v];
+        acc            = __fmaf_rn(gx, sx, acc);
+        acc            = __fmaf_rn(gy, sy, acc);
+        if (HAS_M2) acc = __fmaf_rn(gn, mv[v], acc);
+        acc = __fmaf_rn(gF, qv[v], acc);
+        if (FORCED)
+        {
+          acc = __fmaf_rn(syj, Pi[v], acc);
+          acc = __fmaf_rn(syyj, Qi[v], acc);
+        }
+        o[v] = acc;
+      }
+      if (y < ny && x < nx)
+        *reinterpret_cast<float4*>(out + (long long)y * nx + x) = make_float4(o[0], o[1], o[2], o[3]);
+      up  = cur;
+      cur = dn;
+    }
+    __syncthreads(); // slot s fully read
+    if (tid == 0)
+    {
+      const int tn = t + NST * gridDim.x;
+      if (tn < ntiles)
+      {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue_tile<HAS_M2>(smem + s * SLOT_BYTES, &bar[s], &mh, &mm2, &mf0, tn, tiles_x);
+      }
+    }
+  }
+  if (failed && tid == 0)
+  {
+    *(volatile int*)err = 1;
+    // drain the copies this CTA still has in flight (bounded)
+    for (int kk = k; kk < k + NST; ++kk)
+    {
+      const int tt = blockIdx.x + kk * gridDim.x;
+      if (tt >= ntiles) break;
+      mbar_wait_bounded(&bar[kk % NST], (uint32_t)((kk / NST) & 1));
+    }
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+  static EncodeTiledFn fn = nullptr;
+  if (!fn)
+  {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+          cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+bool encode(CUtensorMap* m, const float* base, long long nx, long long ny, int bw, int bh)
+{
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2]    = {(cuuint64_t)nx, (cuuint64_t)ny};
+  cuuint64_t strides[1] = {(cuuint64_t)nx * 4};
+  cuuint32_t box[2]     = {(cuuint32_t)bw, (cuuint32_t)bh};
+  cuuint32_t es[2]      = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+template <bool F, bool M2>
+bool set_smem_attr()
+{
+  static bool done = false;
+  if (!done)
+    done = cudaFuncSetAttribute(stage32_tma_kernel<F, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                SMEM_BYTES) == cudaSuccess;
+  return done;
+}
+
+} // namespace
+
+bool tma_stage32_supported(long long nx, long long ny)
+{
+  // 16-byte row pitch and 16-byte aligned x coordinates (multiples of 4 floats); the tile
+  // coordinates must fit the copy engine's signed 32-bit coordinates
+  return nx % 4 == 0 && nx >= 8 && ny >= 2 && nx < (1LL << 30) && ny < (1LL << 30) && encode_fn() != nullptr;
+}
+
+bool tma_stage32_prepare(TmaStage32* t, float* const D[3], float* const Ff[2], long long nx, long long ny)
+{
+  t->ok = false;
+  if (!tma_stage32_supported(nx, ny)) return false;
+  for (int b = 0; b < 3; ++b)
+  {
+    if (!encode(&t->halo[b], D[b], nx, ny, HW, HH)) return false;
+    if (!encode(&t->plain[b], D[b], nx, ny, TW, TH)) return false;
+  }
+  for (int b = 0; b < 2; ++b)
+    if (!encode(&t->f0[b], Ff[b], nx, ny, TW, TH)) return false;
+  t->ok = true;
+  return true;
+}
+
+bool tma_stage32_launch(const TmaStage32* t, int num_sms, const ProbDev& P, const StageArgs* A, int im1, int im2,
+                        int if0, float* out, int* err, cudaStream_t st)
+{
+  const bool forced = P.kind == STS_PROBLEM_MANUFACTURED;
+  const CUtensorMap& mm2 = (im2 >= 0) ? t->plain[im2] : t->plain[im1];
+  const long long tiles = ((P.nx + TW - 1) / TW) * ((P.ny + TH - 1) / TH);
+  const int grid        = (int)(tiles < num_sms ? tiles : num_sms);
+  if (forced)
+  {
+    if (im2 >= 0)
+    {
+      if (!set_smem_attr<true, true>()) return false;
+      stage32_tma_kernel<true, true><<<grid, 256, SMEM_BYTES, st>>>(t->halo[im1], mm2, t->f0[if0], P, A, out, err);
+    }
+    else
+    {
+      if (!set_smem_attr<true, false>()) return false;
+      stage32_tma_kernel<true, false><<<grid, 256, SMEM_BYTES, st>>>(t->halo[im1], mm2, t->f0[if0], P, A, out, err);
+    }
+  }
+  else
+  {
+    if (im2 >= 0)
+    {
+      if (!set_smem_attr<false, true>()) return false;
+      stage32_tma_kernel<false, true><<<grid, 256, SMEM_BYTES, st>>>(t->halo[im1], mm2, t->f0[if0], P, A, out, err);
+    }
+    else
+    {
+      if (!set_smem_attr<false, false>()) return false;
+      stage32_tma_kernel<false, false><<<grid, 256, SMEM_BYTES, st>>>(t->halo[im1], mm2, t->f0[if0], P, A, out,
+                                                                     err);
+    }
+  }
+  return true;
+}

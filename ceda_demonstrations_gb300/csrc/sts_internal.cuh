@@ -60,6 +60,8 @@ struct STS_Context_ {
   RedWork* d_work   = nullptr;    // device
   double* h_slots   = nullptr;    // pinned, mapped
   double* d_slots   = nullptr;    // device alias of h_slots
+  int* h_err        = nullptr;    // pinned, mapped: kernels report a bounded wait that timed out
+  int* d_err        = nullptr;
 };
 
 bool ctx_activate(STS_Context ctx);
@@ -182,6 +184,7 @@ struct NVContent {
   long long length = 0;
   long long nx = 0, ny = 0;
   bool own = false;
+  int device = 0; // owner device: destroying a vector must not need its context
   double* data = nullptr;
 };
 inline NVContent* NVC(N_Vector v) { return (NVContent*)v->content; }
