@@ -95,6 +95,7 @@ SIGNATURES = [
     ("N_VMaxNorm_Sts", C.c_double, [_NV]),
     ("N_VWrmsNorm_Sts", C.c_double, [_NV, _NV]),
     ("N_VLinearCombination_Sts", C.c_int, [C.c_int, _dp, C.POINTER(_NV), _NV]),
+    ("STS_WrmsNormNoAlloc", C.c_int, [_vp, _vp, _ll, _vp, _vp]),
     ("STS_ProblemCreate", _vp, [_vp, C.c_int, _ll, _ll, C.c_double, C.c_double, C.c_int,
                                 C.c_double, C.c_double, C.c_double, C.c_double]),
     ("STS_ProblemFree", C.c_int, [C.POINTER(_vp)]),

@@ -109,6 +109,21 @@ double N_VMaxNorm_Sts(N_Vector x);
 double N_VWrmsNorm_Sts(N_Vector x, N_Vector w);
 int N_VLinearCombination_Sts(int nvec, double* c, N_Vector* X, N_Vector z);
 
+/* Allocation-free WRMS norm. No counterpart in the reference: it exists for callers that
+ * cannot allocate device or pinned memory when they need a norm (work recorded into another
+ * runtime's CUDA graph or fixed memory pool, real-time loops, foreign vector libraries that
+ * hold raw device pointers but no STS_Context). Computes the same exact value as
+ * N_VWrmsNorm_Sts: sqrt(sum_i (x_i w_i)^2 / n) over device arrays x, w of length n, written
+ * to the device location `result`, asynchronously on `stream` (a cudaStream_t, NULL = the
+ * default stream). It calls no cudaMalloc/cudaFree: its scratch is one fixed 96-byte block
+ * per device in a static device array held until the library is unloaded. The first call
+ * on each device looks up that block (cudaGetSymbolAddress) and must come before any stream
+ * capture. Each call clears the block first; calls that overlap on the GPU race on it.
+ * n must lie in [1, STS_NOALLOC_MAX_N]; otherwise -1 and STS_GetLastError() says why. */
+#define STS_NOALLOC_MAX_N 2147483647LL
+int STS_WrmsNormNoAlloc(const double* x, const double* w, sts_index n, double* result,
+                        void* stream);
+
 /* ------------------------------------------------------------------------------------
  * Problem and callbacks (diffusion_2D). STS_Problem replaces UserData
  * (diffusion_2D/diffusion_2D.hpp:66-214) for the single-device case.
