@@ -199,7 +199,8 @@ def run_gpu(args):
         launches = (s1["stages_total"] - s0["stages_total"]) + (s1["nst_attempts"] - s0["nst_attempts"])
         dof_stages = N2 * (s1["nfe"] - s0["nfe"])
         stage_ms = I.time_stage_kernel(20)
-        res[mixed] = dict(ms=ms, dof_stages=dof_stages, launches=launches, stage_ms=stage_ms,
+        kinfo = I.stage_kernel_info()
+        res[mixed] = dict(ms=ms, dof_stages=dof_stages, launches=launches, stage_ms=stage_ms, kinfo=kinfo,
                           t=s1["t"], s=s1["stage_max"], stats=s1, y=y.numpy(), I=I,
                           steps=s1["nst"] - s0["nst"])
 
@@ -276,7 +277,7 @@ def run_gpu(args):
         "gpu_launches": m["launches"],
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": ach / peak, "traffic": traffic,
-                     "kernel": "stage32_kernel (mixed stage, 16 B/DOF-stage)",
+                     "kernel": "mixed stage kernel (16 B/DOF-stage), autotuned: %s" % m["kinfo"]["name"],
                      "peak_source": peak_kind},
         "clocks": merge_clocks(clock_samples),
         "fp64": {"value": fp64_value, "unit": "DOF-stages/s", "ms_per_step": d["ms"] / args.steps,

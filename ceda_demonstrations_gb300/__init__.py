@@ -125,6 +125,7 @@ SIGNATURES = [
     ("STS_ARKodeSetStopTime", C.c_int, [_vp, C.c_double]),
     ("STS_LSRKStepSetMixedPrecision", C.c_int, [_vp, C.c_int]),
     ("STS_LSRKStepSetStageKernel", C.c_int, [_vp, C.c_int]),
+    ("STS_LSRKStepGetStageKernelInfo", C.c_int, [_vp, _ip, _dp, C.c_char_p, C.c_int]),
     ("STS_LSRKStepSetUseGraphs", C.c_int, [_vp, C.c_int]),
     ("STS_ARKodeEvolve", C.c_int, [_vp, C.c_double, _NV, _dp, C.c_int]),
     ("STS_ARKodeReset", C.c_int, [_vp, C.c_double, _NV]),
@@ -474,6 +475,12 @@ class LSRKStep:
         rc = lib().STS_ARKodeReset(self.mem, t, y.h)
         if rc != 0:
             _err("STS_ARKodeReset returned %d" % rc)
+
+    def stage_kernel_info(self):
+        v, ms = C.c_int(), C.c_double()
+        buf = C.create_string_buffer(64)
+        lib().STS_LSRKStepGetStageKernelInfo(self.mem, C.byref(v), C.byref(ms), buf, 64)
+        return {"variant": v.value, "ms": ms.value, "name": buf.value.decode()}
 
     def time_stage_kernel(self, nlaunch=20):
         ms = C.c_double()

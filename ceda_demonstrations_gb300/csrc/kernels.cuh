@@ -383,6 +383,138 @@ __global__ void __launch_bounds__(256) stepend_kernel(ProbDev P, const StepArgs*
   xsum_block_finish<256>(acc, flags, w, slot, 1, (double)(nx * ny));
 }
 
+// Step end, row-marching form (nx even): a thread owns 2 consecutive columns and 16 rows,
+// keeps rows j-1, j, j+1 of y_{n+1} in registers (formed once per point, yn + ds in the
+// mixed form), and gets the west/east neighbours from the neighbouring lanes; per point the
+// arithmetic is identical to stepend_kernel.
+template <bool MIXED, bool FORCED>
+__global__ void __launch_bounds__(256) stepend_march_kernel(ProbDev P, const StepArgs* __restrict__ S,
+                                                            const double* __restrict__ yn,
+                                                            const double* __restrict__ Ys,
+                                                            const float* __restrict__ ds,
+                                                            const double* __restrict__ Fn,
+                                                            double* __restrict__ ynew,
+                                                            double* __restrict__ Fnew,
+                                                            float* __restrict__ Fnewf, RedWork* w,
+                                                            double* slot)
+{
+  constexpr int RYS = 16;
+  const long long nx = P.nx, ny = P.ny;
+  const long long i0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+  const long long jb = ((long long)blockIdx.y * blockDim.y + threadIdx.y) * RYS;
+  const int lane     = threadIdx.x & 31;
+  const double p4h = S->p4h, rtol = S->rtol, atol = S->atol;
+  xsum::Limbs acc;
+  xsum::zero(acc);
+  unsigned flags   = 0;
+  const bool colok = i0 < nx; // nx even: both columns valid
+  const bool active = colok && jb < ny;
+  // y_{n+1} at (row, i0..i0+1); zero outside the domain
+  auto row2 = [&](long long j, double (&v)[2]) {
+    if (!active || j < 0 || j >= ny)
+    {
+      v[0] = v[1] = 0.0;
+      return;
+    }
+    const long long k = j * nx + i0;
+    if (MIXED)
+    {
+      const double2 a = __ldg(reinterpret_cast<const double2*>(yn + k));
+      const float2 b  = __ldg(reinterpret_cast<const float2*>(ds + k));
+      v[0]            = a.x + (double)b.x;
+      v[1]            = a.y + (double)b.y;
+    }
+    else
+    {
+      const double2 a = __ldg(reinterpret_cast<const double2*>(Ys + k));
+      v[0]            = a.x;
+      v[1]            = a.y;
+    }
+  };
+  auto point = [&](long long j, long long i) -> double { // single y_{n+1} value (edges)
+    if (i < 0 || i >= nx || j < 0 || j >= ny) return 0.0;
+    const long long k = j * nx + i;
+    return MIXED ? yn[k] + (double)ds[k] : Ys[k];
+  };
+  double Pi[2] = {0.0, 0.0}, Qi[2] = {0.0, 0.0};
+  if (FORCED && colok)
+  {
+    const double al = S->al, be = S->be, ga = S->ga;
+#pragma unroll
+    for (int v = 0; v < 2; ++v)
+    {
+      Pi[v] = __fma_rn(al, P.Sx[i0 + v], be * P.Sxx[i0 + v]);
+      Qi[v] = ga * P.Sx[i0 + v];
+    }
+  }
+  double up[2], cur[2], dn[2];
+  row2(jb - 1, up);
+  row2(jb, cur);
+  for (int r = 0; r < RYS; ++r)
+  {
+    const long long j = jb + r;
+    row2(j + 1, dn);
+    // west/east neighbours from the neighbouring lanes (the warp spans 64 consecutive columns)
+    double wv = __shfl_up_sync(0xffffffffu, cur[1], 1);
+    double ev = __shfl_down_sync(0xffffffffu, cur[0], 1);
+    if (lane == 0) wv = active && j < ny ? point(j, i0 - 1) : 0.0;
+    if (lane == 31) ev = active && j < ny ? point(j, i0 + 2) : 0.0;
+    if (active && j < ny)
+    {
+      if (i0 + 2 >= nx) ev = 0.0;
+      if (i0 == 0) wv = 0.0;
+      const long long k = j * nx + i0;
+      const double2 ynv = __ldg(reinterpret_cast<const double2*>(yn + k));
+      const double2 fnv = __ldg(reinterpret_cast<const double2*>(Fn + k));
+      const double yv[2] = {ynv.x, ynv.y}, fv[2] = {fnv.x, fnv.y};
+      double syj = 0.0, syyj = 0.0;
+      if (FORCED)
+      {
+        syj  = P.Sy[j];
+        syyj = P.Syy[j];
+      }
+      double fo[2];
+#pragma unroll
+      for (int v = 0; v < 2; ++v)
+      {
+        const double uc = cur[v];
+        const double uw = (v == 0) ? wv : cur[0];
+        const double ue = (v == 1) ? ev : cur[1];
+        const double sx = uw + ue, sy = up[v] + dn[v];
+        double f        = P.cc * uc;
+        f               = __fma_rn(P.cx, sx, f);
+        f               = __fma_rn(P.cy, sy, f);
+        if (FORCED)
+        {
+          f = __fma_rn(syj, Pi[v], f);
+          f = __fma_rn(syyj, Qi[v], f);
+        }
+        fo[v]           = f;
+        const double d  = yv[v] - uc;
+        double e        = 0.8 * d;
+        e               = __fma_rn(p4h, fv[v], e);
+        e               = __fma_rn(p4h, f, e);
+        const double wt = 1.0 / (rtol * fabs(yv[v]) + atol);
+        const double x  = e * wt;
+        xsum::add(acc, x * x, flags);
+      }
+      *reinterpret_cast<double2*>(Fnew + k) = make_double2(fo[0], fo[1]);
+      if (MIXED)
+      {
+        *reinterpret_cast<double2*>(ynew + k) = make_double2(cur[0], cur[1]);
+        *reinterpret_cast<float2*>(Fnewf + k) = make_float2((float)fo[0], (float)fo[1]);
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < 2; ++v)
+    {
+      up[v]  = cur[v];
+      cur[v] = dn[v];
+    }
+  }
+  xsum_block_finish<256>(acc, flags, w, slot, 1, (double)(nx * ny));
+}
+
 // WRMS with ewt(y): mode 0 -> x = a w(y), mode 1 -> x = (a - b) w(y)
 template <int MODE>
 __global__ void __launch_bounds__(256) wrms_ewt_kernel(long long n, const double* __restrict__ a,

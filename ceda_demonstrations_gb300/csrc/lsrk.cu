@@ -192,8 +192,11 @@ struct LSRKMem {
   double tstop          = INFINITY;
   bool mixed            = false;
   bool use_graphs       = true;
-  int stage_variant     = 0; // 0: TMA-pipelined mixed stage where supported, 1: register marching
+  int stage_variant     = 0; // 0: autotuned (TMA configurations + register kernel), 1: register marching
   TmaStage32 tma;
+  int tma_variant       = -1; // chosen TMA configuration (-1: register-marching kernel)
+  bool tuned            = false;
+  double tune_ms[TMA_STAGE32_NVARIANTS + 1] = {};
   long long n           = 0;
 
   // state (mirrors the oracle's orc_state)
@@ -298,7 +301,7 @@ static int ensure_stage_buffers(LSRKMem* m)
     if (!m->mixed && !m->Y[b] && !STS_CUDA_OK(cudaMalloc(&m->Y[b], n8))) return -1;
     if (m->mixed && !m->D[b] && !STS_CUDA_OK(cudaMalloc(&m->D[b], n4))) return -1;
   }
-  if (m->mixed && !m->tma.ok && m->stage_variant == 0)
+  if (m->mixed && !m->tma.ok && m->stage_variant != 1)
   {
     STS_Problem p = (STS_Problem)m->user_data;
     if (tma_stage32_supported(p->nx, p->ny)) tma_stage32_prepare(&m->tma, m->D, m->Ffb, p->nx, p->ny);
@@ -361,13 +364,67 @@ static void launch_stage32(LSRKMem* m, STS_Problem p, const StageArgs* A, const 
                            const float* f0f, float* dj);
 
 // mixed stage by buffer index (TMA path when prepared)
-static void launch_stage32_idx(LSRKMem* m, STS_Problem p, const StageArgs* A, int im1, int im2, int par, int iout)
+static void launch_stage32_idx(LSRKMem* m, STS_Problem p, const StageArgs* A, int im1, int im2, int par, int iout,
+                               int variant)
 {
-  if (m->stage_variant == 0 && m->tma.ok &&
-      tma_stage32_launch(&m->tma, m->ctx->num_sms, p->dev, A, im1, im2, par, m->D[iout], m->ctx->d_err,
+  if (variant >= 0 && m->tma.ok &&
+      tma_stage32_launch(&m->tma, variant, m->ctx->num_sms, p->dev, A, im1, im2, par, m->D[iout], m->ctx->d_err,
                          m->ctx->stream))
     return;
   launch_stage32(m, p, A, m->D[im1], im2 >= 0 ? m->D[im2] : nullptr, m->Ffb[par], m->D[iout]);
+}
+
+static void launch_stage32_idx(LSRKMem* m, STS_Problem p, const StageArgs* A, int im1, int im2, int par, int iout)
+{
+  const int v = m->stage_variant == 0 ? m->tma_variant : (m->stage_variant >= 2 ? m->stage_variant - 2 : -1);
+  launch_stage32_idx(m, p, A, im1, im2, par, iout, v);
+}
+
+// Autotuner for the mixed stage kernel: times every TMA configuration and the register
+// kernel on the integrator's own buffers (a realistic stage, CUDA events on the context
+// stream, 2 warm + 5 timed launches each) and keeps the fastest for this problem.
+static void autotune_stage32(LSRKMem* m, STS_Problem p)
+{
+  m->tuned       = true;
+  m->tma_variant = -1;
+  if (m->stage_variant != 0 || !m->tma.ok) return;
+  cudaStream_t st = m->ctx->stream;
+  // stage coefficients of a mid stage of a 100-stage RKL2 step (any finite values time alike)
+  memset(m->h_par, 0, m->par_bytes);
+  StageArgs* a = hstage(m) + 2;
+  a->gcf = 0.5f;
+  a->gxf = 0.2f;
+  a->gyf = 0.05f;
+  a->gnf = -0.9f;
+  a->gFf = 1e-5f;
+  cudaMemcpyAsync(m->d_par, m->h_par, m->par_bytes, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(m->D[0], 0, m->n * sizeof(float), st);
+  cudaMemsetAsync(m->D[1], 0, m->n * sizeof(float), st);
+  cudaMemsetAsync(m->Ffb[m->par], 0, m->n * sizeof(float), st);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 1e30;
+  for (int v = -1; v < TMA_STAGE32_NVARIANTS; ++v)
+  {
+    for (int k = 0; k < 2; ++k) launch_stage32_idx(m, p, dstage(m) + 2, 0, 1, m->par, 2, v);
+    cudaEventRecord(e0, st);
+    for (int k = 0; k < 5; ++k) launch_stage32_idx(m, p, dstage(m) + 2, 0, 1, m->par, 2, v);
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double per = ms / 5.0;
+    m->tune_ms[v + 1] = per;
+    if (per < best)
+    {
+      best           = per;
+      m->tma_variant = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaGetLastError();
 }
 
 static void launch_stage32(LSRKMem* m, STS_Problem p, const StageArgs* A, const float* dm1, const float* dm2,
@@ -392,6 +449,23 @@ static void launch_stage32(LSRKMem* m, STS_Problem p, const StageArgs* A, const 
 static void launch_stepend(LSRKMem* m, STS_Problem p, int par, const double* Ys, const float* ds)
 {
   const bool forced = p->kind == STS_PROBLEM_MANUFACTURED;
+  if (p->nx % 2 == 0)
+  { // row-marching form: 64 x 4 threads, 2 columns x 16 rows each
+    dim3 b(64, 4);
+    dim3 g((unsigned)((p->nx / 2 + 63) / 64), (unsigned)((p->ny + 63) / 64));
+    const int nxt = 1 - par;
+    RedWork* w    = m->ctx->d_work;
+    double* slot  = m->ctx->d_slots + SLOT_DSM;
+    dispatch_forced(forced, [&](auto F) {
+      if (m->mixed)
+        stepend_march_kernel<true, decltype(F)::value><<<g, b, 0, m->ctx->stream>>>(
+          p->dev, dstep(m), m->yb[par], nullptr, ds, m->Fb[par], m->yb[nxt], m->Fb[nxt], m->Ffb[nxt], w, slot);
+      else
+        stepend_march_kernel<false, decltype(F)::value><<<g, b, 0, m->ctx->stream>>>(
+          p->dev, dstep(m), m->yb[par], Ys, nullptr, m->Fb[par], nullptr, m->Fb[nxt], nullptr, w, slot);
+    });
+    return;
+  }
   dim3 b(256, 1);
   unsigned gx      = (unsigned)((p->nx + 255) / 256);
   long long gy_cap = std::max<long long>(1, (long long)m->ctx->num_sms * 8 / gx);
@@ -683,6 +757,7 @@ static int evolve_fused(LSRKMem* m, double target, int itask)
   cudaStream_t st = m->ctx->stream;
   const long long n = m->n;
   if (ensure_stage_buffers(m) || ensure_par(m)) return STS_ERR_FAILURE;
+  if (m->mixed && !m->tuned) autotune_stage32(m, p);
   if (!m->nv_y) m->nv_y = N_VMake_Sts(n, nullptr, m->ctx);
   if (!m->nv_F) m->nv_F = N_VMake_Sts(n, nullptr, m->ctx);
   NVC(m->nv_y)->nx = p->nx;
@@ -1010,7 +1085,7 @@ extern "C" int STS_LSRKStepSetMixedPrecision(void* mem, int on)
 extern "C" int STS_LSRKStepSetStageKernel(void* mem, int variant)
 {
   CHECK_MEM(mem);
-  if (variant < 0 || variant > 1) return STS_ILL_INPUT;
+  if (variant < 0 || variant > 1 + TMA_STAGE32_NVARIANTS) return STS_ILL_INPUT;
   LSRKMem* m = MEM(mem);
   if (m->stage_variant != variant)
   {
@@ -1018,6 +1093,22 @@ extern "C" int STS_LSRKStepSetStageKernel(void* mem, int variant)
     m->graphs.clear();
   }
   m->stage_variant = variant;
+  m->tuned         = false;
+  return 0;
+}
+
+extern "C" int STS_LSRKStepGetStageKernelInfo(void* mem, int* variant, double* ms_per_launch, char* name, int namelen)
+{
+  CHECK_MEM(mem);
+  LSRKMem* m = MEM(mem);
+  const int v = m->stage_variant == 0 ? m->tma_variant : (m->stage_variant >= 2 ? m->stage_variant - 2 : -1);
+  if (variant) *variant = v;
+  if (ms_per_launch) *ms_per_launch = m->tuned ? m->tune_ms[m->tma_variant + 1] : 0.0;
+  if (name && namelen > 0)
+  {
+    const char* nm = m->mixed ? tma_stage32_variant_name(v) : "fp64_register_marching";
+    snprintf(name, namelen, "%s", nm);
+  }
   return 0;
 }
 
@@ -1038,6 +1129,8 @@ extern "C" int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* t
     return STS_ILL_INPUT;
   }
   ctx_activate(m->ctx);
+  // start every evolve from a clean reduction workspace (a failed launch could leave it dirty)
+  cudaMemsetAsync(m->ctx->d_work, 0, sizeof(RedWork), m->ctx->stream);
   double target = tout < m->tstop ? tout : m->tstop;
   int ret;
   if (fused(m))

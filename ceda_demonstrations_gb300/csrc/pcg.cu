@@ -56,8 +56,9 @@ __device__ __forceinline__ void pcg_block_finish(xsum::Limbs* a, unsigned* fl, P
   __shared__ long long sm[NT / 32][NACC][xsum::NL];
   __shared__ unsigned sflags[NACC];
   __shared__ bool last;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x < NACC) sflags[threadIdx.x] = 0;
+  const int tid  = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int lane = tid & 31, warp = tid >> 5;
+  if (tid < NACC) sflags[tid] = 0;
 #pragma unroll
   for (int c = 0; c < NACC; ++c)
 #pragma unroll
@@ -86,7 +87,7 @@ __device__ __forceinline__ void pcg_block_finish(xsum::Limbs* a, unsigned* fl, P
       }
   }
   __syncthreads();
-  if (threadIdx.x == 0)
+  if (tid == 0)
   {
 #pragma unroll
     for (int c = 0; c < NACC; ++c)
@@ -96,7 +97,7 @@ __device__ __forceinline__ void pcg_block_finish(xsum::Limbs* a, unsigned* fl, P
     last       = (t == gridDim.x * gridDim.y - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0)
+  if (last && tid == 0)
   {
     __threadfence();
     double v[NACC];

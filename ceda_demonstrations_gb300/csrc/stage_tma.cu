@@ -1,6 +1,8 @@
 // Mixed (FP32-increment) stage kernel with TMA tile loads and an mbarrier pipeline.
 //
-// Persistent CTAs (one per SM, 256 threads) walk 128 x 32 output tiles. For each tile the
+// Persistent CTAs (256 threads, one or two per SM) walk 128-column output tiles of 8-32 rows
+// (the tile height, ring depth and CTAs per SM form the configurations the autotuner in
+// lsrk.cu times on the problem's own buffers). For each tile the
 // CTA's issuing thread starts three bulk tensor copies into one slot of a 3-deep shared
 // memory ring: the d_{j-1} tile with a 4-column / 1-row halo (its out-of-range parts are
 // zero-filled by the copy engine, which is exactly the homogeneous Dirichlet boundary), the
@@ -27,15 +29,24 @@
 
 namespace {
 
-constexpr int TW = 128, TH = 32;          // output tile
-constexpr int HW = TW + 8, HH = TH + 2;   // halo tile (x from x0-4 keeps 16-byte alignment)
-constexpr int NST = 3;                    // pipeline depth
-constexpr int HALO_BYTES = HW * HH * 4;   // 18496
-constexpr int HALO_PAD   = 18560;         // rounded to 128 B
-constexpr int PL_BYTES   = TW * TH * 4;   // 16384
-constexpr int SLOT_BYTES = HALO_PAD + 2 * PL_BYTES;
-constexpr int SMEM_BYTES = NST * SLOT_BYTES + 64; // + the NST pipeline barriers
+constexpr int TW = 128;                   // output tile width (floats)
+constexpr int HW = TW + 8;                // halo tile width (x from x0-4 keeps 16-byte alignment)
 constexpr long long WAIT_LIMIT = 1LL << 24;
+
+// Tile / pipeline configuration: TH output rows per tile, NST slots in the shared-memory
+// ring, MINB CTAs per SM. The autotuner picks one per problem size.
+template <int TH_, int NST_, int MINB_>
+struct Cfg {
+  static constexpr int TH = TH_, NST = NST_, MINB = MINB_;
+  static constexpr int HH = TH + 2;
+  static constexpr int HALO_BYTES = HW * HH * 4;
+  static constexpr int HALO_PAD   = (HALO_BYTES + 127) / 128 * 128;
+  static constexpr int PL_BYTES   = TW * TH * 4;
+  static constexpr int SLOT_BYTES = HALO_PAD + 2 * PL_BYTES;
+  static constexpr int SMEM_BYTES = NST * SLOT_BYTES + 64; // + the NST pipeline barriers
+  static constexpr int RPW = TH / 8;                       // rows per warp (8 warps)
+  static_assert(TH % 8 == 0, "8 warps share the tile rows");
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
 {
@@ -82,43 +93,43 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
     : "memory");
 }
 
-template <bool HAS_M2>
+template <class K, bool HAS_M2>
 __device__ __forceinline__ void issue_tile(unsigned char* slot, uint64_t* bar, const CUtensorMap* mh,
                                            const CUtensorMap* mm2, const CUtensorMap* mf0, int tile,
                                            int tiles_x)
 {
   const int x0 = (tile % tiles_x) * TW;
-  const int y0 = (tile / tiles_x) * TH;
-  mbar_expect_tx(bar, HALO_BYTES + (HAS_M2 ? 2 : 1) * PL_BYTES);
+  const int y0 = (tile / tiles_x) * K::TH;
+  mbar_expect_tx(bar, K::HALO_BYTES + (HAS_M2 ? 2 : 1) * K::PL_BYTES);
   tma_load_2d(slot, mh, bar, x0 - 4, y0 - 1);
-  if (HAS_M2) tma_load_2d(slot + HALO_PAD, mm2, bar, x0, y0);
-  tma_load_2d(slot + HALO_PAD + PL_BYTES, mf0, bar, x0, y0);
+  if (HAS_M2) tma_load_2d(slot + K::HALO_PAD, mm2, bar, x0, y0);
+  tma_load_2d(slot + K::HALO_PAD + K::PL_BYTES, mf0, bar, x0, y0);
 }
 
-template <bool FORCED, bool HAS_M2>
-__global__ void __launch_bounds__(256, 1)
+template <class K, bool FORCED, bool HAS_M2>
+__global__ void __launch_bounds__(256, K::MINB)
   stage32_tma_kernel(const __grid_constant__ CUtensorMap mh, const __grid_constant__ CUtensorMap mm2,
                      const __grid_constant__ CUtensorMap mf0, ProbDev P, const StageArgs* __restrict__ A,
                      float* __restrict__ out, int* err)
 {
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NST * SLOT_BYTES);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + K::NST * K::SLOT_BYTES);
   const int nx = (int)P.nx, ny = (int)P.ny;
   const int tiles_x = (nx + TW - 1) / TW;
-  const int ntiles  = tiles_x * ((ny + TH - 1) / TH);
+  const int ntiles  = tiles_x * ((ny + K::TH - 1) / K::TH);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if (tid == 0)
   {
-    for (int s = 0; s < NST; ++s) mbar_init(&bar[s], 1);
+    for (int s = 0; s < K::NST; ++s) mbar_init(&bar[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
   if (tid == 0)
-    for (int k = 0; k < NST; ++k)
+    for (int k = 0; k < K::NST; ++k)
     {
       const int t = blockIdx.x + k * gridDim.x;
-      if (t < ntiles) issue_tile<HAS_M2>(smem + k * SLOT_BYTES, &bar[k], &mh, &mm2, &mf0, t, tiles_x);
+      if (t < ntiles) issue_tile<K, HAS_M2>(smem + k * K::SLOT_BYTES, &bar[k], &mh, &mm2, &mf0, t, tiles_x);
     }
 
   const float gc = A->gcf, gx = A->gxf, gy = A->gyf, gn = A->gnf, gF = A->gFf;
@@ -127,18 +138,18 @@ __global__ void __launch_bounds__(256, 1)
   int k       = 0;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++k)
   {
-    const int s             = k % NST;
-    const uint32_t parity   = (uint32_t)((k / NST) & 1);
+    const int s             = k % K::NST;
+    const uint32_t parity   = (uint32_t)((k / K::NST) & 1);
     const bool ok           = mbar_wait_bounded(&bar[s], parity);
     if (__syncthreads_or(!ok))
     {
       failed = true;
       break;
     }
-    const float* halo = reinterpret_cast<const float*>(smem + s * SLOT_BYTES);
-    const float* m2s  = reinterpret_cast<const float*>(smem + s * SLOT_BYTES + HALO_PAD);
-    const float* f0s  = reinterpret_cast<const float*>(smem + s * SLOT_BYTES + HALO_PAD + PL_BYTES);
-    const int x0 = (t % tiles_x) * TW, y0 = (t / tiles_x) * TH;
+    const float* halo = reinterpret_cast<const float*>(smem + s * K::SLOT_BYTES);
+    const float* m2s  = reinterpret_cast<const float*>(smem + s * K::SLOT_BYTES + K::HALO_PAD);
+    const float* f0s  = reinterpret_cast<const float*>(smem + s * K::SLOT_BYTES + K::HALO_PAD + K::PL_BYTES);
+    const int x0 = (t % tiles_x) * TW, y0 = (t / tiles_x) * K::TH;
     const int x  = x0 + lane * 4;
     const int c  = 4 + lane * 4; // column of x in the halo tile
     float Pi[4], Qi[4];
@@ -153,11 +164,11 @@ __global__ void __launch_bounds__(256, 1)
         Qi[v] = ga * sx;
       }
     }
-    const int r0 = warp * 4; // tile rows r0 .. r0+3 -> halo rows r0+1 .. r0+4
+    const int r0 = warp * K::RPW; // tile rows r0 .. r0+RPW-1 -> halo rows r0+1 ..
     float4 up  = *reinterpret_cast<const float4*>(halo + (r0 + 0) * HW + c);
     float4 cur = *reinterpret_cast<const float4*>(halo + (r0 + 1) * HW + c);
 #pragma unroll
-    for (int rr = 0; rr < 4; ++rr)
+    for (int rr = 0; rr < K::RPW; ++rr)
     {
       const int r    = r0 + rr;
       const float4 dn = *reinterpret_cast<const float4*>(halo + (r + 2) * HW + c);
@@ -207,11 +218,11 @@ __global__ void __launch_bounds__(256, 1)
     __syncthreads(); // slot s fully read
     if (tid == 0)
     {
-      const int tn = t + NST * gridDim.x;
+      const int tn = t + K::NST * gridDim.x;
       if (tn < ntiles)
       {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        issue_tile<HAS_M2>(smem + s * SLOT_BYTES, &bar[s], &mh, &mm2, &mf0, tn, tiles_x);
+        issue_tile<K, HAS_M2>(smem + s * K::SLOT_BYTES, &bar[s], &mh, &mm2, &mf0, tn, tiles_x);
       }
     }
   }
@@ -219,11 +230,11 @@ __global__ void __launch_bounds__(256, 1)
   {
     *(volatile int*)err = 1;
     // drain the copies this CTA still has in flight (bounded)
-    for (int kk = k; kk < k + NST; ++kk)
+    for (int kk = k; kk < k + K::NST; ++kk)
     {
       const int tt = blockIdx.x + kk * gridDim.x;
       if (tt >= ntiles) break;
-      mbar_wait_bounded(&bar[kk % NST], (uint32_t)((kk / NST) & 1));
+      mbar_wait_bounded(&bar[kk % K::NST], (uint32_t)((kk / K::NST) & 1));
     }
   }
 }
@@ -261,17 +272,58 @@ bool encode(CUtensorMap* m, const float* base, long long nx, long long ny, int b
   return r == CUDA_SUCCESS;
 }
 
-template <bool F, bool M2>
+template <class K, bool F, bool M2>
 bool set_smem_attr()
 {
   static bool done = false;
   if (!done)
-    done = cudaFuncSetAttribute(stage32_tma_kernel<F, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                SMEM_BYTES) == cudaSuccess;
+    done = cudaFuncSetAttribute(stage32_tma_kernel<K, F, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                K::SMEM_BYTES) == cudaSuccess;
   return done;
 }
 
+template <class K, bool F, bool M2>
+bool launch_cfg(const TmaStage32* t, int num_sms, const ProbDev& P, const StageArgs* A, int im1, int im2, int if0,
+                float* out, int* err, cudaStream_t st)
+{
+  if (!set_smem_attr<K, F, M2>()) return false;
+  const CUtensorMap& mm2 = (im2 >= 0) ? t->plain[K::TH][im2] : t->plain[K::TH][im1];
+  const long long tiles = ((P.nx + TW - 1) / TW) * ((P.ny + K::TH - 1) / K::TH);
+  const long long cap   = (long long)num_sms * K::MINB;
+  const int grid        = (int)(tiles < cap ? tiles : cap);
+  stage32_tma_kernel<K, F, M2><<<grid, 256, K::SMEM_BYTES, st>>>(t->halo[K::TH][im1], mm2, t->f0[K::TH][if0], P, A,
+                                                                  out, err);
+  return true;
+}
+
+template <class K>
+bool launch_any(const TmaStage32* t, int num_sms, const ProbDev& P, const StageArgs* A, int im1, int im2, int if0,
+                float* out, int* err, cudaStream_t st)
+{
+  const bool forced = P.kind == STS_PROBLEM_MANUFACTURED;
+  if (forced)
+    return (im2 >= 0) ? launch_cfg<K, true, true>(t, num_sms, P, A, im1, im2, if0, out, err, st)
+                      : launch_cfg<K, true, false>(t, num_sms, P, A, im1, im2, if0, out, err, st);
+  return (im2 >= 0) ? launch_cfg<K, false, true>(t, num_sms, P, A, im1, im2, if0, out, err, st)
+                    : launch_cfg<K, false, false>(t, num_sms, P, A, im1, im2, if0, out, err, st);
+}
+
+// the configurations the autotuner chooses from (rows per tile, ring depth, CTAs per SM)
+using C0 = Cfg<32, 3, 1>;
+using C1 = Cfg<16, 4, 2>;
+using C2 = Cfg<16, 6, 1>;
+using C3 = Cfg<8, 8, 2>;
+using C4 = Cfg<32, 2, 2>;
+using C5 = Cfg<24, 4, 1>;
+
 } // namespace
+
+const char* tma_stage32_variant_name(int v)
+{
+  static const char* names[] = {"tile128x32_ring3_1cta", "tile128x16_ring4_2cta", "tile128x16_ring6_1cta",
+                                "tile128x8_ring8_2cta",  "tile128x32_ring2_2cta", "tile128x24_ring4_1cta"};
+  return (v >= 0 && v < TMA_STAGE32_NVARIANTS) ? names[v] : "register_marching";
+}
 
 bool tma_stage32_supported(long long nx, long long ny)
 {
@@ -284,50 +336,32 @@ bool tma_stage32_prepare(TmaStage32* t, float* const D[3], float* const Ff[2], l
 {
   t->ok = false;
   if (!tma_stage32_supported(nx, ny)) return false;
-  for (int b = 0; b < 3; ++b)
+  const int heights[] = {8, 16, 24, 32};
+  for (int th : heights)
   {
-    if (!encode(&t->halo[b], D[b], nx, ny, HW, HH)) return false;
-    if (!encode(&t->plain[b], D[b], nx, ny, TW, TH)) return false;
+    for (int b = 0; b < 3; ++b)
+    {
+      if (!encode(&t->halo[th][b], D[b], nx, ny, HW, th + 2)) return false;
+      if (!encode(&t->plain[th][b], D[b], nx, ny, TW, th)) return false;
+    }
+    for (int b = 0; b < 2; ++b)
+      if (!encode(&t->f0[th][b], Ff[b], nx, ny, TW, th)) return false;
   }
-  for (int b = 0; b < 2; ++b)
-    if (!encode(&t->f0[b], Ff[b], nx, ny, TW, TH)) return false;
   t->ok = true;
   return true;
 }
 
-bool tma_stage32_launch(const TmaStage32* t, int num_sms, const ProbDev& P, const StageArgs* A, int im1, int im2,
-                        int if0, float* out, int* err, cudaStream_t st)
+bool tma_stage32_launch(const TmaStage32* t, int variant, int num_sms, const ProbDev& P, const StageArgs* A, int im1,
+                        int im2, int if0, float* out, int* err, cudaStream_t st)
 {
-  const bool forced = P.kind == STS_PROBLEM_MANUFACTURED;
-  const CUtensorMap& mm2 = (im2 >= 0) ? t->plain[im2] : t->plain[im1];
-  const long long tiles = ((P.nx + TW - 1) / TW) * ((P.ny + TH - 1) / TH);
-  const int grid        = (int)(tiles < num_sms ? tiles : num_sms);
-  if (forced)
+  switch (variant)
   {
-    if (im2 >= 0)
-    {
-      if (!set_smem_attr<true, true>()) return false;
-      stage32_tma_kernel<true, true><<<grid, 256, SMEM_BYTES, st>>>(t->halo[im1], mm2, t->f0[if0], P, A, out, err);
-    }
-    else
-    {
-      if (!set_smem_attr<true, false>()) return false;
-      stage32_tma_kernel<true, false><<<grid, 256, SMEM_BYTES, st>>>(t->halo[im1], mm2, t->f0[if0], P, A, out, err);
-    }
+  case 0: return launch_any<C0>(t, num_sms, P, A, im1, im2, if0, out, err, st);
+  case 1: return launch_any<C1>(t, num_sms, P, A, im1, im2, if0, out, err, st);
+  case 2: return launch_any<C2>(t, num_sms, P, A, im1, im2, if0, out, err, st);
+  case 3: return launch_any<C3>(t, num_sms, P, A, im1, im2, if0, out, err, st);
+  case 4: return launch_any<C4>(t, num_sms, P, A, im1, im2, if0, out, err, st);
+  case 5: return launch_any<C5>(t, num_sms, P, A, im1, im2, if0, out, err, st);
+  default: return false;
   }
-  else
-  {
-    if (im2 >= 0)
-    {
-      if (!set_smem_attr<false, true>()) return false;
-      stage32_tma_kernel<false, true><<<grid, 256, SMEM_BYTES, st>>>(t->halo[im1], mm2, t->f0[if0], P, A, out, err);
-    }
-    else
-    {
-      if (!set_smem_attr<false, false>()) return false;
-      stage32_tma_kernel<false, false><<<grid, 256, SMEM_BYTES, st>>>(t->halo[im1], mm2, t->f0[if0], P, A, out,
-                                                                     err);
-    }
-  }
-  return true;
 }

@@ -95,8 +95,10 @@ __device__ __forceinline__ void xsum_block_finish(xsum::Limbs& a, unsigned flags
   __shared__ long long sm[NT / 32][xsum::NL];
   __shared__ unsigned sflags;
   __shared__ bool last;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) sflags = 0;
+  // linear thread index: blocks may be 1-D or 2-D (NT threads in total)
+  const int tid  = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) sflags = 0;
 #pragma unroll
   for (int k = 0; k < xsum::NL; ++k)
   {
@@ -119,7 +121,7 @@ __device__ __forceinline__ void xsum_block_finish(xsum::Limbs& a, unsigned flags
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0)
+  if (tid == 0)
   {
     if (sflags) atomicOr(&w->flags, sflags);
     __threadfence();
@@ -127,7 +129,7 @@ __device__ __forceinline__ void xsum_block_finish(xsum::Limbs& a, unsigned flags
     last       = (t == gridDim.x * gridDim.y * gridDim.z - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0)
+  if (last && tid == 0)
   {
     __threadfence();
     long long tot[xsum::NL];

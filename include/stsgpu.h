@@ -207,9 +207,14 @@ int STS_ARKodeSetMaxNumSteps(void* mem, long long mxsteps);           /* main.cp
 int STS_ARKodeSetStopTime(void* mem, double tstop);                   /* main.cpp:384 */
 /* new: FP32 stage increments relative to the FP64 step-start state (fused path only) */
 int STS_LSRKStepSetMixedPrecision(void* mem, int on);
-/* new: mixed-stage kernel variant: 0 = TMA + mbarrier pipelined tiles where the row length
- * is a multiple of 4 (default), 1 = register-marching kernel; both give identical bits */
+/* new: mixed-stage kernel selection: 0 = autotuned at the first step among the TMA +
+ * mbarrier pipelined tile configurations (rows per tile, ring depth, CTAs per SM; row length
+ * a multiple of 4) and the register-marching kernel (default), 1 = register-marching kernel,
+ * 2 + k = TMA configuration k (k < 6). All variants give identical bits. */
 int STS_LSRKStepSetStageKernel(void* mem, int variant);
+/* new: the autotuner's choice (-1 = register-marching), its time per launch and its name */
+int STS_LSRKStepGetStageKernelInfo(void* mem, int* variant, double* ms_per_launch, char* name,
+                                   int namelen);
 /* new: capture the fixed-s stage loop of the fused path in CUDA graphs (default on) */
 int STS_LSRKStepSetUseGraphs(void* mem, int on);
 int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* tret, int itask); /* main.cpp:442 */
