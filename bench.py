@@ -356,24 +356,26 @@ def run_reference(args):
 
 
 def run_full(args):
-    """Time-to-solution on [0, 0.05] for both precisions (one run each)."""
+    """Time-to-solution on [0, tf] for both precisions (one run each per method / rtol)."""
     import numpy as np
     import ceda_demonstrations_gb300 as sts
     ctx = sts.Context(0)
     timer = cuda_timer(ctx.stream)
-    n = args.n
-    G = sts.Problem(ctx, sts.MANUFACTURED, n, n, KX, KY)
-    ex = G.exact(TF).numpy()
+    n, tf, kx, ky = args.n, args.tf, args.kx, args.ky
+    G = sts.Problem(ctx, sts.MANUFACTURED, n, n, kx, ky)
+    ex = G.exact(tf).numpy()
     out = {}
-    for method in ([1, 0] if args.both_methods else [1]):
-        for rtol in ([1e-6, 1e-4] if args.both_rtols else [1e-6]):
+    methods = [1, 0] if args.both_methods else [1]
+    rtols = [1e-6, 1e-4] if args.both_rtols else [1e-6]
+    for method in methods:
+        for rtol in rtols:
             ys = {}
             for mixed in (True, False):
                 I = sts.LSRKStep(ctx, G, 0.0, G.initial(), method=method, rtol=rtol, atol=ATOL,
                                  smax=SMAX, mixed=mixed, graphs=True, maxsteps=1000000)
                 y = G.vector()
                 with timer() as tm:
-                    I.evolve(TF, y)
+                    I.evolve(tf, y)
                 st = I.stats()
                 ys[mixed] = y.numpy()
                 key = "%s_rtol%g_%s" % ("RKL2" if method else "RKC2", rtol, "mixed" if mixed else "fp64")
@@ -382,10 +384,57 @@ def run_full(args):
                             "dof_stages_per_s": n * n * st["nfe"] / (tm.ms / 1e3),
                             "rel_l2_vs_exact": float(np.linalg.norm(ys[mixed] - ex) / np.linalg.norm(ex))}
                 print(key, json.dumps(out[key]), flush=True)
+                I.free()
             rel = float(np.linalg.norm(ys[True] - ys[False]) / np.linalg.norm(ys[False]))
-            out["%s_rtol%g_mixed_vs_fp64_rel_l2" % ("RKL2" if method else "RKC2", rtol)] = rel
-            print("mixed vs fp64 rel L2", rel, flush=True)
-    print(json.dumps({"full_solve": out, "n": n}), flush=True)
+            tag = "%s_rtol%g" % ("RKL2" if method else "RKC2", rtol)
+            out[tag + "_mixed_vs_fp64_rel_l2"] = rel
+            out[tag + "_speedup"] = out[tag + "_fp64"]["time_to_solution_s"] / out[tag + "_mixed"]["time_to_solution_s"]
+            print(tag, "mixed vs fp64 rel L2", rel, "speedup", out[tag + "_speedup"], flush=True)
+    print(json.dumps({"full_solve": out, "n": n, "tf": tf, "kx": kx, "ky": ky}), flush=True)
+
+
+def run_batch(args):
+    """512 independent heat problems in one persistent launch (n uniform from
+    {64,...,512}, kx, ky log-uniform in [1e-2, 1], 8 random sine modes, RKL2 rtol 1e-6 to
+    t = 0.01, per-instance step control on the device)."""
+    import numpy as np
+    import ceda_demonstrations_gb300 as sts
+    from oracle import pyoracle as po
+    ctx = sts.Context(0)
+    inst = sts.make_batch_instances(count=args.batch_count, seed=20261203)
+    B = sts.Batch(ctx, inst)
+    th, cp, tune_ms = B.autotune(0.1 * args.batch_tf)
+    ms = B.evolve(args.batch_tf, method=sts.RKL, rtol=1e-6, atol=1e-10, smax=SMAX)
+    y = B.state()
+    nfe = [B.stats(i)["nfe"] for i in range(len(inst))]
+    nst = [B.stats(i)["nst"] for i in range(len(inst))]
+    dof_stages = float(sum(inst[i][0] ** 2 * nfe[i] for i in range(len(inst))))
+    # CPU oracle on a sample of instances (all host threads), and parity on that sample
+    sample = list(range(0, len(inst), max(1, len(inst) // 16)))[:16]
+    t0 = time.perf_counter()
+    cpu_dof = 0.0
+    maxrel = 0.0
+    for i in sample:
+        n, kx, ky, p, q, a = inst[i]
+        P = po.Problem(po.UNFORCED, n, n, kx=kx, ky=ky)
+        J = po.Integrator(P, P.initial_modes(p, q, a), method=po.RKL, rtol=1e-6, atol=1e-10)
+        J.evolve(args.batch_tf)
+        cpu_dof += n * n * J.stats()["nfe"]
+        yi = B.instance_state(y, i)
+        maxrel = max(maxrel, float(np.linalg.norm(yi - J.y) / np.linalg.norm(J.y)))
+    cpu_s = time.perf_counter() - t0
+    line = {
+        "metric": "batched STS: DOF-stages/s and time for %d independent problems in one launch" % len(inst),
+        "value": dof_stages / (ms / 1e3), "unit": "DOF-stages/s", "time_s": ms / 1e3,
+        "total_dof": int(B.total), "dof_stages": dof_stages, "steps_total": int(sum(nst)),
+        "steps_max": int(max(nst)), "launch": {"threads": th, "ctas_per_sm": cp, "probe_ms": tune_ms},
+        "dtype": "f64", "data": "synthetic (seeded sine-mode initial states, seed 20261203)",
+        "parity_sample_max_rel_l2_vs_oracle": maxrel,
+        "cpu_baseline": {"value": cpu_dof / cpu_s, "unit": "DOF-stages/s", "cores": po.lib().orc_nthreads(),
+                         "kind": "port", "sample": "%d of the %d instances, integrated one after another"
+                                                   % (len(sample), len(inst))},
+    }
+    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -396,9 +445,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--full", action="store_true")
+    ap.add_argument("--tf", type=float, default=TF)
+    ap.add_argument("--kx", type=float, default=KX)
+    ap.add_argument("--ky", type=float, default=KY)
     ap.add_argument("--both-methods", action="store_true")
     ap.add_argument("--both-rtols", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--batch-tf", type=float, default=0.01)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -406,6 +461,8 @@ def main():
         run_reference(args)
     elif args.full:
         run_full(args)
+    elif args.batch:
+        run_batch(args)
     else:
         run_gpu(args)
 

@@ -23,7 +23,7 @@ from . import build as _build
 
 __all__ = ["lib", "Context", "NVector", "Problem", "LSRKStep", "PCGSolver", "implicit_solve_pcg",
            "sdirk2_evolve", "RKC", "RKL", "PID", "PI", "I", "MANUFACTURED", "UNFORCED", "PERIODIC",
-           "STSError"]
+           "Net", "fcg_solve", "harvest_pcg_pairs", "net_features", "STSError"]
 
 RKC, RKL = 0, 1
 PID, PI, I = 0, 1, 2
@@ -32,6 +32,7 @@ NORMAL, ONE_STEP = 1, 2
 TOO_MUCH_WORK = -1
 
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int)
 _vp = C.c_void_p
 _ll = C.c_longlong
@@ -150,6 +151,32 @@ SIGNATURES = [
                                        _ip, _dp]),
     ("STS_SDIRK2Evolve", C.c_int, [_vp, _NV, C.c_double, C.c_double, C.c_int, C.c_double,
                                    C.c_int, C.POINTER(_ll)]),
+    ("STS_BatchCreate", _vp, [_vp, C.c_int, _ip, _dp, _dp]),
+    ("STS_BatchFree", C.c_int, [C.POINTER(_vp)]),
+    ("STS_BatchTotalDOF", _ll, [_vp]),
+    ("STS_BatchSetState", C.c_int, [_vp, _dp]),
+    ("STS_BatchGetState", C.c_int, [_vp, _dp]),
+    ("STS_BatchSetInitialModes", C.c_int, [_vp, C.c_int, _ip, _ip, _dp]),
+    ("STS_BatchEvolve", C.c_int, [_vp, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int,
+                                  C.c_int, _ll]),
+    ("STS_BatchLastMilliseconds", C.c_double, [_vp]),
+    ("STS_BatchGetInstanceStats", C.c_int, [_vp, C.c_int, C.POINTER(Stats)]),
+    ("STS_BatchSetLaunch", C.c_int, [_vp, C.c_int, C.c_int]),
+    ("STS_BatchAutotune", C.c_int, [_vp, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int,
+                                    _ip, _ip, _dp]),
+    ("STS_NetCreate", _vp, [_vp, C.c_int, C.c_ulonglong]),
+    ("STS_NetFree", C.c_int, [C.POINTER(_vp)]),
+    ("STS_NetSetWeights", C.c_int, [_vp, _fp]),
+    ("STS_NetGetWeights", C.c_int, [_vp, _fp]),
+    ("STS_NetApply", C.c_int, [_vp, C.c_int, _vp, _vp, C.c_double, C.c_double, C.c_double,
+                               C.c_double]),
+    ("STS_NetLossGrad", C.c_int, [_vp, C.c_int, _vp, _vp, C.c_double, C.c_double, C.c_double,
+                                  _dp, _fp]),
+    ("STS_NetTrain", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, C.c_int, C.c_float,
+                               C.c_ulonglong, _dp]),
+    ("STS_HarvestPCGPairs", C.c_int, [_vp, C.c_double, _NV, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      _vp, _vp, C.c_ulonglong, _ip, _ip]),
+    ("STS_FCGSolve", C.c_int, [_vp, C.c_double, _vp, _NV, _NV, C.c_double, C.c_int, _ip, _dp]),
 ]
 
 _lib = None
@@ -566,3 +593,198 @@ def sdirk2_evolve(problem, y, t0, h, nsteps, tol=1e-10, maxit=100000):
     if rc < 0:
         _err("STS_SDIRK2Evolve")
     return it.value
+
+
+def make_batch_instances(count=512, seed=20261203, sizes=(64, 96, 128, 192, 256, 384, 512),
+                         nmodes=8, pmax=16):
+    """The batched workload: n uniform from `sizes`, kx, ky log-uniform in [1e-2, 1], initial
+    state a sum of `nmodes` sine modes sin(p pi x) sin(q pi y), p, q in [1, pmax], N(0,1)
+    amplitudes; numpy's PCG64 generator with the given seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(rng.choice(sizes))
+        kx = float(10 ** rng.uniform(-2, 0))
+        ky = float(10 ** rng.uniform(-2, 0))
+        p = rng.integers(1, pmax + 1, nmodes)
+        q = rng.integers(1, pmax + 1, nmodes)
+        a = rng.standard_normal(nmodes)
+        out.append((n, kx, ky, p, q, a))
+    return out
+
+
+class Batch:
+    """STS_Batch: independent problems advanced in one persistent launch."""
+
+    def __init__(self, ctx, instances):
+        L = lib()
+        self.ctx = ctx
+        self.instances = instances
+        k = len(instances)
+        ns = np.array([i[0] for i in instances], dtype=np.int32)
+        kx = np.array([i[1] for i in instances], dtype=np.float64)
+        ky = np.array([i[2] for i in instances], dtype=np.float64)
+        self.h = L.STS_BatchCreate(ctx.h, k, ns.ctypes.data_as(_ip), _dptr(kx), _dptr(ky))
+        if not self.h:
+            _err("STS_BatchCreate")
+        ctx.live += 1
+        nm = len(instances[0][3])
+        p = np.concatenate([i[3] for i in instances]).astype(np.int32)
+        q = np.concatenate([i[4] for i in instances]).astype(np.int32)
+        a = np.concatenate([i[5] for i in instances]).astype(np.float64)
+        if L.STS_BatchSetInitialModes(self.h, nm, p.ctypes.data_as(_ip), q.ctypes.data_as(_ip),
+                                      _dptr(a)) != 0:
+            _err("STS_BatchSetInitialModes")
+        self.total = L.STS_BatchTotalDOF(self.h)
+        self.offsets = np.concatenate([[0], np.cumsum([i[0] ** 2 for i in instances])])
+
+    def evolve(self, tf, method=RKL, rtol=1e-6, atol=1e-10, smax=200, controller=PID, maxsteps=0):
+        rc = lib().STS_BatchEvolve(self.h, tf, method, rtol, atol, smax, controller, maxsteps)
+        if rc < 0:
+            _err("STS_BatchEvolve returned %d" % rc)
+        return lib().STS_BatchLastMilliseconds(self.h)
+
+    def autotune(self, tf_probe, method=RKL, rtol=1e-6, atol=1e-10, smax=200):
+        th, cp, ms = C.c_int(), C.c_int(), C.c_double()
+        lib().STS_BatchAutotune(self.h, tf_probe, method, rtol, atol, smax, C.byref(th), C.byref(cp),
+                                C.byref(ms))
+        return th.value, cp.value, ms.value
+
+    def set_launch(self, threads, ctas_per_sm):
+        return lib().STS_BatchSetLaunch(self.h, threads, ctas_per_sm)
+
+    def state(self):
+        out = np.empty(self.total)
+        if lib().STS_BatchGetState(self.h, _dptr(out)) != 0:
+            _err("STS_BatchGetState")
+        return out
+
+    def set_state(self, y):
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        lib().STS_BatchSetState(self.h, _dptr(y))
+
+    def instance_state(self, y, i):
+        n = self.instances[i][0]
+        return y[self.offsets[i]:self.offsets[i + 1]]
+
+    def stats(self, i):
+        s = Stats()
+        lib().STS_BatchGetInstanceStats(self.h, i, C.byref(s))
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def free(self):
+        if self.h and not _exiting:
+            lib().STS_BatchFree(C.byref(_vp(self.h)))
+            self.h = None
+            self.ctx.live -= 1
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+
+# ---------------------------------------------------------------------------------------
+# learned multilevel preconditioner
+# ---------------------------------------------------------------------------------------
+NET_LAYERS = ["W_in", "W_d1", "W_d2", "W_d3", "W_c", "W_u2", "W_u1", "W_u0", "W_out"]
+NET_WSZ = 16 * 16 * 9
+
+
+def net_features(kx, ky, gamma, dx):
+    """(sk, sg, jacobi) of the shifted system (I - gamma A): the normalised anisotropy
+    log10(ky/kx), the normalised log10(gamma/dx^2) and the Jacobi factor 1/(1 - gamma cc)."""
+    cc = -2.0 * (kx + ky) / (dx * dx)
+    sk = (np.log10(ky / kx) + 1.5) / 1.5
+    sg = np.log10(gamma / (dx * dx)) - 3.6
+    return sk, sg, 1.0 / (1.0 - gamma * cc)
+
+
+class Net:
+    """STS_Net: the linear multilevel convolutional preconditioner (BF16 tensor-core kernels).
+
+    Device arrays are passed as raw device pointers (ints), e.g. ``NVector.ptr`` or a
+    ``torch`` CUDA tensor's ``data_ptr()``; the caller orders work on other streams."""
+
+    def __init__(self, ctx, nmax, seed=0):
+        self.ctx = ctx
+        self.h = lib().STS_NetCreate(ctx.h, nmax, seed)
+        if not self.h:
+            _err("STS_NetCreate")
+        ctx.live += 1
+        self.nmax = nmax
+
+    def weights(self):
+        """FP32 master weights as a dict name -> (16, 16, 3, 3) array."""
+        w = np.empty(len(NET_LAYERS) * NET_WSZ, dtype=np.float32)
+        if lib().STS_NetGetWeights(self.h, w.ctypes.data_as(_fp)) != 0:
+            _err("STS_NetGetWeights")
+        return {nm: w[i * NET_WSZ:(i + 1) * NET_WSZ].reshape(16, 16, 3, 3).copy()
+                for i, nm in enumerate(NET_LAYERS)}
+
+    def set_weights(self, W):
+        """W: dict name -> array of shape (co, ci, 3, 3) with co, ci <= 16 (zero padded)."""
+        w = np.zeros((len(NET_LAYERS), 16, 16, 3, 3), dtype=np.float32)
+        for i, nm in enumerate(NET_LAYERS):
+            a = np.asarray(W[nm], dtype=np.float32)
+            w[i, :a.shape[0], :a.shape[1]] = a
+        w = np.ascontiguousarray(w.ravel())
+        if lib().STS_NetSetWeights(self.h, w.ctypes.data_as(_fp)) != 0:
+            _err("STS_NetSetWeights")
+
+    def apply(self, n, r_ptr, z_ptr, sk, sg, jacobi, scale=1.0):
+        if lib().STS_NetApply(self.h, n, r_ptr, z_ptr, sk, sg, jacobi, scale) != 0:
+            _err("STS_NetApply")
+
+    def loss_grad(self, n, r_ptr, e_ptr, sk, sg, jacobi):
+        loss = C.c_double()
+        g = np.empty(len(NET_LAYERS) * NET_WSZ, dtype=np.float32)
+        if lib().STS_NetLossGrad(self.h, n, r_ptr, e_ptr, sk, sg, jacobi, C.byref(loss),
+                                 g.ctypes.data_as(_fp)) != 0:
+            _err("STS_NetLossGrad")
+        return loss.value, {nm: g[i * NET_WSZ:(i + 1) * NET_WSZ].reshape(16, 16, 3, 3).copy()
+                            for i, nm in enumerate(NET_LAYERS)}
+
+    def train(self, n, nsamples, r_ptr, e_ptr, meta_ptr, epochs, batch, lr, seed=0):
+        loss = C.c_double()
+        if lib().STS_NetTrain(self.h, n, nsamples, r_ptr, e_ptr, meta_ptr, epochs, batch, lr, seed,
+                              C.byref(loss)) != 0:
+            _err("STS_NetTrain")
+        return loss.value
+
+    def free(self):
+        if self.h and not _exiting:
+            lib().STS_NetFree(C.byref(_vp(self.h)))
+            self.h = None
+            self.ctx.live -= 1
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def harvest_pcg_pairs(problem, gamma, b, ncrops, crop, every, max_pairs, r_ptr, e_ptr, seed=0):
+    """Run Jacobi-PCG to 1e-10 on (I - gamma A) x = b, recording crop x crop windows of r_k
+    and e_k = x* - x_k every `every` batches of 8 iterations (device FP32 buffers of
+    max_pairs * crop^2). Returns (pairs recorded, PCG iterations)."""
+    npairs, iters = C.c_int(), C.c_int()
+    rc = lib().STS_HarvestPCGPairs(problem.h, gamma, b.h, ncrops, crop, every, max_pairs, r_ptr,
+                                   e_ptr, seed, C.byref(npairs), C.byref(iters))
+    if rc < 0:
+        _err("STS_HarvestPCGPairs")
+    return npairs.value, iters.value
+
+
+def fcg_solve(problem, gamma, net, b, x, tol=1e-8, maxit=10000):
+    """Flexible CG on (I - gamma A) x = b with the network as preconditioner; returns
+    (iterations, true relative residual, status)."""
+    it, rel = C.c_int(), C.c_double()
+    rc = lib().STS_FCGSolve(problem.h, gamma, net.h, b.h, x.h, tol, maxit, C.byref(it),
+                            C.byref(rel))
+    if rc < 0:
+        _err("STS_FCGSolve")
+    return it.value, rel.value, rc

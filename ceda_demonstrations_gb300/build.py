@@ -29,15 +29,19 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
+CLI_SRC = os.path.join(HERE, "cli", "diffusion_2D_gpu.cpp")
+CLI = os.path.join(OUT_DIR, "diffusion_2D_gpu")
+
+
 def _deps():
     return sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")] + \
-        [os.path.join(HERE, "..", "include", "stsgpu.h"), os.path.abspath(__file__)]
+        [os.path.join(HERE, "..", "include", "stsgpu.h"), os.path.abspath(__file__), CLI_SRC]
 
 
 def up_to_date():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return False
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
@@ -71,6 +75,14 @@ def build(force=False, verbose=False, extra=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    # command-line driver (reference flags and output format), linked against the library
+    cmd = [nvcc, "-O2", "-std=c++17", "-x", "c++", CLI_SRC, "-o", CLI + ".tmp",
+           "-I" + os.path.join(HERE, "..", "include"), "-L" + OUT_DIR, "-lstsgpu",
+           "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

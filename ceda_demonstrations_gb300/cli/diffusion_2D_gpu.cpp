@@ -1,0 +1,343 @@
+// diffusion_2D_gpu: command-line driver with the flags and the stdout format of the
+// reference driver (diffusion_2D/main.cpp, diffusion_2D.cpp UserData/UserOutput), running
+// on one GB300 through libstsgpu.so. runtests-diffusion2d.py parses its output unchanged
+// (Steps, Error test fails, RHS fn evals, Total simulation time, Maximum relative error).
+//
+// Problems: --problem periodic (default; the reference code's problem: periodic domain
+// [-pi,pi]x[-6,6], Gaussian x sine initial state, optional --inhomogeneous coefficients),
+// --problem manufactured (BASELINE manufactured Dirichlet problem on [0,1]^2) or unforced.
+// Integrators: rkc, rkl (LSRKStep STS, fused kernels for the Dirichlet problems) and dirk
+// (fixed-step SDIRK2 with the fused Jacobi-PCG, Dirichlet problems, --fixedstep required).
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <iomanip>
+#include <iostream>
+#include <limits>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "stsgpu.h"
+
+using namespace std;
+
+struct Opts {
+  // problem (diffusion_2D.hpp:70-93, diffusion_2D.cpp:42-163)
+  string problem = "periodic";
+  long long nx = 64, ny = 64;
+  double kx = 1.0, ky = 1.0, tf = 1.0;
+  double xl = -M_PI, xu = M_PI, yl = -6.0, yu = 6.0;
+  bool inhomogeneous = false;
+  // integrator (main.cpp:24-51)
+  string integrator = "rkc";
+  double rtol = 1.0e-5, atol = 1.0e-10, hfixed = 0.0, epslin = 0.0;
+  int order = 2, controller = 0, maxsteps = 0, onestep = 0, liniters = 20, msbp = 0, smax = 200;
+  bool error = false, linear = true, lsinfo = false, prec = true, internaleig = false;
+  bool mixed = false, graphs = true;
+  string ls = "cg";
+  // output (UserOutput)
+  int output = 1, nout = 20;
+};
+
+static bool take(vector<string>& a, const string& key, string* val)
+{
+  for (size_t i = 0; i < a.size(); ++i)
+    if (a[i] == key)
+    {
+      if (val)
+      {
+        if (i + 1 >= a.size()) return false;
+        *val = a[i + 1];
+        a.erase(a.begin() + i, a.begin() + i + 2);
+      }
+      else a.erase(a.begin() + i);
+      return true;
+    }
+  return false;
+}
+
+static void help()
+{
+  cout << "\nProblem setup command line options:\n"
+          "  --problem <periodic|manufactured|unforced>\n"
+          "  --nx <nx>  --ny <ny>  --xl --xu --yl --yu  --kx <kx>  --ky <ky>\n"
+          "  --inhomogeneous : use spatially-varying diffusion coefficients\n"
+          "  --tf <time>     : final time\n"
+          "\nIntegrator command line options:\n"
+          "  --integrator <dirk|rkc|rkl> --rtol --atol --fixedstep --controller <0|1|2>\n"
+          "  --maxsteps --onestep <n> --error --internaleig --smax <stages> --mixed --nographs\n"
+          "\nDIRK solver command line options:\n"
+          "  --order --nonlinear --ls <cg> --lsinfo --liniters --epslin --noprec --msbp\n"
+          "\nOutput command line options:\n"
+          "  --output <level> (0 = none, 1 = stats, 2 = solution)  --nout <nout>\n";
+}
+
+static int parse(int argc, char** argv, Opts& o)
+{
+  vector<string> a(argv + 1, argv + argc);
+  if (take(a, "--help", nullptr))
+  {
+    help();
+    return 1;
+  }
+  string v;
+  take(a, "--npx", &v); // single GPU: the process grid options are accepted and ignored
+  take(a, "--npy", &v);
+  if (take(a, "--problem", &v)) o.problem = v;
+  if (take(a, "--nx", &v)) o.nx = stoll(v);
+  if (take(a, "--ny", &v)) o.ny = stoll(v);
+  if (take(a, "--xl", &v)) o.xl = stod(v);
+  if (take(a, "--xu", &v)) o.xu = stod(v);
+  if (take(a, "--yl", &v)) o.yl = stod(v);
+  if (take(a, "--yu", &v)) o.yu = stod(v);
+  if (take(a, "--kx", &v)) o.kx = stod(v);
+  if (take(a, "--ky", &v)) o.ky = stod(v);
+  if (take(a, "--inhomogeneous", nullptr)) o.inhomogeneous = true;
+  if (take(a, "--tf", &v)) o.tf = stod(v);
+  if (take(a, "--integrator", &v)) o.integrator = v;
+  if (take(a, "--rtol", &v)) o.rtol = stod(v);
+  if (take(a, "--atol", &v)) o.atol = stod(v);
+  if (take(a, "--fixedstep", &v)) o.hfixed = stod(v);
+  if (take(a, "--order", &v)) o.order = stoi(v);
+  if (take(a, "--controller", &v)) o.controller = stoi(v);
+  if (take(a, "--maxsteps", &v)) o.maxsteps = stoi(v);
+  if (take(a, "--onestep", &v)) o.onestep = stoi(v);
+  if (take(a, "--error", nullptr)) o.error = true;
+  if (take(a, "--nonlinear", nullptr)) o.linear = false;
+  if (take(a, "--ls", &v)) o.ls = v;
+  if (take(a, "--lsinfo", nullptr)) o.lsinfo = true;
+  if (take(a, "--liniters", &v)) o.liniters = stoi(v);
+  if (take(a, "--msbp", &v)) o.msbp = stoi(v);
+  if (take(a, "--epslin", &v)) o.epslin = stod(v);
+  if (take(a, "--noprec", nullptr)) o.prec = false;
+  if (take(a, "--internaleig", nullptr)) o.internaleig = true;
+  if (take(a, "--smax", &v)) o.smax = stoi(v);
+  if (take(a, "--mixed", nullptr)) o.mixed = true;
+  if (take(a, "--nographs", nullptr)) o.graphs = false;
+  if (take(a, "--output", &v)) o.output = stoi(v);
+  if (take(a, "--nout", &v)) o.nout = stoi(v);
+  if (!a.empty())
+  { // main.cpp:116-132
+    cerr << "ERROR: Unknown inputs: ";
+    for (auto& s : a) cerr << s << ' ';
+    cerr << endl;
+    return -1;
+  }
+  return 0;
+}
+
+static int kind_of(const string& p)
+{
+  if (p == "manufactured") return STS_PROBLEM_MANUFACTURED;
+  if (p == "unforced") return STS_PROBLEM_UNFORCED;
+  if (p == "periodic") return STS_PROBLEM_PERIODIC;
+  return -1;
+}
+
+static double urms(N_Vector u, long long nx, long long ny)
+{
+  return sqrt(N_VDotProd_Sts(u, u) / nx / ny); // diffusion_2D.cpp:801
+}
+
+int main(int argc, char** argv)
+{
+  Opts o;
+  int pr = parse(argc, argv, o);
+  if (pr > 0) return 0;
+  if (pr < 0) return 1;
+  const int kind = kind_of(o.problem);
+  if (kind < 0)
+  {
+    cerr << "ERROR: illegal problem" << endl;
+    return 1;
+  }
+  const bool sts  = (o.integrator == "rkc" || o.integrator == "rkl");
+  const bool impl = (o.integrator == "dirk");
+  if (!sts && !impl)
+  {
+    cerr << "ERROR: illegal integrator (this build provides rkc, rkl and dirk)" << endl;
+    return 1;
+  }
+  if (impl && (kind == STS_PROBLEM_PERIODIC || !(o.hfixed > 0.0)))
+  {
+    cerr << "ERROR: dirk runs fixed steps (--fixedstep) on the Dirichlet problems" << endl;
+    return 1;
+  }
+  STS_Context ctx;
+  if (STS_ContextCreate(0, &ctx))
+  {
+    cerr << "ERROR: " << STS_GetLastError() << endl;
+    return 1;
+  }
+  STS_Problem P = STS_ProblemCreate(ctx, kind, o.nx, o.ny, o.kx, o.ky, o.inhomogeneous, o.xl, o.xu, o.yl, o.yu);
+  if (!P)
+  {
+    cerr << "ERROR: " << STS_GetLastError() << endl;
+    return 1;
+  }
+  double dx, dy, cx, cy;
+  STS_ProblemGetInfo(P, &dx, &dy, &cx, &cy);
+  const long long N = o.nx * o.ny;
+  if (o.output > 0)
+  { // UserData::print / UserOptions::print / UserOutput::print
+    cout << "\n Problem options:\n --------------------------------- \n";
+    cout << "  nprocs         = 1\n  kx             = " << o.kx << "\n  ky             = " << o.ky << "\n";
+    cout << (o.inhomogeneous ? "  spatially-varying diffusion\n" : "  homogeneous diffusion\n");
+    cout << "  tf             = " << o.tf << "\n  nx             = " << o.nx << "\n  ny             = " << o.ny
+         << "\n  dx             = " << dx << "\n  dy             = " << dy << "\n";
+    cout << " --------------------------------- \n\n Integrator: " << o.integrator << "\n rtol        = " << o.rtol
+         << "\n atol        = " << o.atol << "\n controller  = " << o.controller << "\n hfixed      = " << o.hfixed
+         << "\n max steps   = " << o.maxsteps << "\n";
+    if (sts) cout << (o.internaleig ? " internal eigenvalue estimation\n" : " user-provided dominant eigenvalue\n");
+    cout << " --------------------------------- \n";
+  }
+  N_Vector u = N_VNew_Sts(N, ctx);
+  STS_Initial(0.0, u, P);
+  N_Vector uref = nullptr, uerr = nullptr;
+  if (o.error)
+  {
+    uref = N_VClone_Sts(u);
+    uerr = N_VClone_Sts(u);
+    N_VScale_Sts(1.0, u, uref);
+  }
+  void* mem = nullptr;
+  void* ref = nullptr;
+  if (sts)
+  {
+    mem = STS_LSRKStepCreateSTS(STS_Diffusion, 0.0, u, ctx);
+    STS_ARKodeSStolerances(mem, o.rtol, o.atol);
+    STS_ARKodeSetUserData(mem, P);
+    STS_LSRKStepSetSTSMethod(mem, o.integrator == "rkc" ? STS_LSRK_RKC_2 : STS_LSRK_RKL_2);
+    if (o.internaleig) STS_LSRKStepSetDomEigEstimatorPower(mem, 100, 0.01); // main.cpp:344
+    else STS_LSRKStepSetDomEigFn(mem, STS_DomEig);
+    if (o.hfixed > 0.0) STS_ARKodeSetFixedStep(mem, o.hfixed);
+    else STS_ARKodeSetAdaptController(mem, o.controller);
+    STS_ARKodeSetMaxNumSteps(mem, o.maxsteps > 0 ? o.maxsteps : 500);
+    STS_ARKodeSetStopTime(mem, o.tf);
+    STS_LSRKStepSetMaxNumStages(mem, o.smax);
+    STS_LSRKStepSetMixedPrecision(mem, o.mixed);
+    STS_LSRKStepSetUseGraphs(mem, o.graphs);
+    if (o.error)
+    { // main.cpp:387-400: reference integrator at rtol 1e-12
+      ref = STS_LSRKStepCreateSTS(STS_Diffusion, 0.0, u, ctx);
+      STS_ARKodeSStolerances(ref, 1.e-12, o.atol);
+      STS_ARKodeSetUserData(ref, P);
+      STS_LSRKStepSetDomEigFn(ref, STS_DomEig);
+      STS_ARKodeSetMaxNumSteps(ref, 100000LL * (o.maxsteps > 0 ? o.maxsteps : 500));
+    }
+  }
+  int nout      = o.nout;
+  int itask     = STS_NORMAL;
+  if (o.onestep)
+  {
+    nout  = o.onestep;
+    itask = STS_ONE_STEP;
+  }
+  double t = 0.0, dTout = o.tf / nout, tout = dTout, errtot = 0.0, simtime = 0.0;
+  long long lin_iters = 0;
+  FILE* sol = nullptr;
+  cout << scientific << setprecision(numeric_limits<double>::digits10);
+  if (o.output > 0)
+  {
+    cout << "\n          t                     ||u||_rms      \n";
+    cout << " ----------------------------------------------\n";
+    cout << setw(22) << t << setw(25) << urms(u, o.nx, o.ny) << "\n";
+  }
+  vector<double> host;
+  if (o.output == 2)
+  { // UserOutput::open (diffusion_2D.cpp:729-757)
+    sol = fopen("diffusion_2d_solution.00000.txt", "w");
+    fprintf(sol, "# title Diffusion 2D\n# nvar 1\n# vars u\n# nt  %d\n# nx  %lld\n# xl  %.17g\n# xu  %.17g\n"
+                 "# ny  %lld\n# yl  %.17g\n# yu  %.17g\n# px  1\n# py  1\n# np  1\n# is  0\n# ie  %lld\n"
+                 "# js  0\n# je  %lld\n",
+            nout + 1, o.nx, o.xl, o.xu, o.ny, o.yl, o.yu, o.nx - 1, o.ny - 1);
+    host.resize(N);
+    N_VCopyToHost_Sts(u, host.data());
+    fprintf(sol, "%.15e", t);
+    for (double x : host) fprintf(sol, " %.15e", x);
+    fprintf(sol, "\n");
+  }
+  for (int iout = 0; iout < nout; ++iout)
+  {
+    auto t0 = chrono::steady_clock::now();
+    int flag = 0;
+    if (sts)
+    {
+      flag = STS_ARKodeEvolve(mem, tout, u, &t, itask);
+    }
+    else
+    {
+      const double h    = o.hfixed;
+      const int nsteps  = (int)llround((tout - t) / h);
+      long long its     = 0;
+      flag              = STS_SDIRK2Evolve(P, u, t, h, nsteps, o.epslin > 0 ? o.epslin : 1e-10, 100000, &its);
+      lin_iters += its;
+      t += nsteps * h;
+    }
+    STS_ContextSynchronize(ctx);
+    simtime += chrono::duration<double>(chrono::steady_clock::now() - t0).count();
+    if (flag < 0)
+    {
+      cerr << "\nERROR: ARKodeEvolve returned with flag = " << flag << " (" << STS_GetLastError() << ")\n";
+      return 1;
+    }
+    if (o.error && ref)
+    {
+      double t2 = 0.0;
+      STS_ARKodeSetStopTime(ref, t);
+      STS_ARKodeEvolve(ref, t, uref, &t2, STS_NORMAL);
+      N_VLinearSum_Sts(1.0, uref, -1.0, u, uerr);
+      const double e = N_VMaxNorm_Sts(uerr) / N_VMaxNorm_Sts(uref);
+      if (e > errtot) errtot = e;
+    }
+    if (o.output > 0) cout << setw(22) << t << setw(25) << urms(u, o.nx, o.ny) << "\n";
+    if (sol)
+    {
+      N_VCopyToHost_Sts(u, host.data());
+      fprintf(sol, "%.15e", t);
+      for (double x : host) fprintf(sol, " %.15e", x);
+      fprintf(sol, "\n");
+    }
+    tout += dTout;
+    tout = (tout > o.tf) ? o.tf : tout;
+  }
+  if (sol) fclose(sol);
+  if (o.output > 0) cout << " ----------------------------------------------\n\n";
+  if (o.error) cout << "Maximum relative error = " << errtot << endl;
+  cout << "Total simulation time = " << simtime << endl << endl;
+  cout << "Final integrator statistics:" << endl;
+  if (sts)
+  {
+    char buf[2048];
+    STS_ARKodePrintAllStats(mem, buf, sizeof(buf));
+    cout << buf;
+  }
+  else
+  {
+    cout << "Steps                         = " << llround(t / o.hfixed) << "\n"
+         << "Error test fails              = 0\n"
+         << "Linear solver iterations      = " << lin_iters << "\n";
+  }
+  if (kind == STS_PROBLEM_MANUFACTURED)
+  {
+    N_Vector ex = N_VClone_Sts(u);
+    STS_Exact(t, ex, P);
+    N_VLinearSum_Sts(1.0, u, -1.0, ex, ex);
+    N_Vector e2 = N_VClone_Sts(u);
+    STS_Exact(t, e2, P);
+    cout << "Relative L2 error vs exact    = " << sqrt(N_VDotProd_Sts(ex, ex) / N_VDotProd_Sts(e2, e2)) << "\n";
+    N_VDestroy_Sts(ex);
+    N_VDestroy_Sts(e2);
+  }
+  if (mem) STS_ARKodeFree(&mem);
+  if (ref) STS_ARKodeFree(&ref);
+  N_VDestroy_Sts(u);
+  if (uref) N_VDestroy_Sts(uref);
+  if (uerr) N_VDestroy_Sts(uerr);
+  STS_ProblemFree(&P);
+  STS_ContextFree(&ctx);
+  return 0;
+}

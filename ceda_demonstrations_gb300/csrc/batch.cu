@@ -1,0 +1,747 @@
+// Batched STS: many independent 2-D heat problems (homogeneous Dirichlet, no forcing, their
+// own grid size and diffusivities) advanced to a common final time in ONE persistent launch.
+//
+// Work distribution: instances are ordered by an estimate of their cost (largest first) and
+// CTAs take the next instance from a device-side counter. A CTA integrates its instance
+// completely: RKL2/RKC2 stages as grid sweeps separated by __syncthreads, the step end
+// (F(y_{n+1}), embedded error, exact WRMS reduced inside the CTA) and the step control
+// (controller, stage cap, stop time, rejections) run on the device with the rules of the
+// single-problem integrator (lsrk.cu). No host round trip happens per step; the host only
+// launches the batch and reads the per-instance statistics afterwards.
+//
+// Precision: FP64 throughout (the path is FP64-ALU-bound on GB300). The device controller
+// uses the CUDA math library's pow, so step sequences can differ from the CPU oracle's in the
+// last bit of h; the parity tests compare with a tolerance.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "kernels.cuh"
+#include "sts_internal.cuh"
+
+struct BatchInst {
+  int n;           // interior nodes per direction
+  int status;      // 0 running/finished ok, < 0 failure
+  long long off;   // offset of the instance in each state array
+  double kx, ky, cx, cy, cc, rho;
+  // statistics
+  long long nst, nst_att, netf, nfe, nst_exp, stage_max, stages_total;
+  double t, hlast, hnext;
+};
+
+struct BatchArrays {
+  double* y;    // state y_n (input and output)
+  double* buf[5]; // F_n, F_{n+1} / Y work buffers (instance-local regions)
+};
+
+struct BatchParams {
+  double tf, rtol, atol, eig_safety;
+  int method, smax, controller, maxsteps;
+};
+
+struct STS_Batch_ {
+  STS_Context ctx = nullptr;
+  int ninst       = 0;
+  long long total = 0;
+  std::vector<BatchInst> hinst;
+  BatchInst* dinst = nullptr;
+  int* dorder      = nullptr;
+  int* dqueue      = nullptr;
+  double* y        = nullptr;
+  double* work     = nullptr; // 5 x total
+  int block        = 512;
+  int ctas_per_sm  = 2;
+  double last_ms   = 0.0;
+};
+
+// ---------------------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------------------
+namespace {
+
+constexpr double B_ORD = 3.0, B_BIAS = 1.5, B_TINY = 1.0e-10;
+constexpr double B_SAFETY = 0.96, B_GROWTH = 20.0, B_ETAMX1 = 10000.0, B_ETAMXF = 0.3, B_ETAMIN = 0.1;
+
+__device__ double d_controller(int controller, double h, double dsm, double ep1, double ep2, long long nhist)
+{
+  double e1 = fmax(B_BIAS * dsm, B_TINY), e2 = fmax(B_BIAS * ep1, B_TINY), e3 = fmax(B_BIAS * ep2, B_TINY);
+  if (controller == 0)
+  {
+    if (nhist < 1) return h * pow(e1, -0.58 / B_ORD);
+    if (nhist < 2) return h * pow(e1, -0.58 / B_ORD) * pow(e2, 0.21 / B_ORD);
+    return h * pow(e1, -0.58 / B_ORD) * pow(e2, 0.21 / B_ORD) * pow(e3, -0.1 / B_ORD);
+  }
+  if (controller == 1)
+  {
+    if (nhist < 1) return h * pow(e1, -0.8 / B_ORD);
+    return h * pow(e1, -0.8 / B_ORD) * pow(e2, 0.31 / B_ORD);
+  }
+  return h * pow(e1, -1.0 / B_ORD);
+}
+
+__device__ int d_stages(int method, double h, double rho, int smax, double* hmax)
+{
+  double ss;
+  const double sm = (double)smax;
+  if (method == 0)
+  {
+    ss    = 1.0 + floor(sqrt(1.0 + 1.54 * h * rho));
+    *hmax = (rho > 0.0) ? 0.96 * (sm * sm - 1.0) / (1.54 * rho) : 1e300;
+  }
+  else
+  {
+    ss    = ceil((sqrt(9.0 + 8.0 * h * rho) - 1.0) / 2.0);
+    *hmax = (rho > 0.0) ? 0.96 * (sm * sm + sm - 2.0) / (2.0 * rho) : 1e300;
+  }
+  if (ss < 2.0) ss = 2.0;
+  if (ss > 1e9) ss = 1e9;
+  return (int)ss;
+}
+
+// Per-stage coefficients, generated on the fly (same recurrences as STS_LSRKStageCoeffs)
+struct Coef {
+  // RKC state
+  double w0, w1, bjm1, bjm2, zjm1, zjm2, dzjm1, dzjm2, d2zjm1, d2zjm2, thjm1, thjm2;
+  // RKL state
+  double cj1;
+  int method, s;
+  double mus1;
+};
+
+__device__ void coef_init(Coef& c, int method, int s)
+{
+  c.method = method;
+  c.s      = s;
+  const double sd = (double)s;
+  if (method == 0)
+  {
+    c.w0               = 1.0 + 2.0 / (13.0 * (sd * sd));
+    const double temp1 = c.w0 * c.w0 - 1.0;
+    const double temp2 = sqrt(temp1);
+    const double arg   = sd * log(c.w0 + temp2);
+    c.w1               = sinh(arg) * temp1 / (cosh(arg) * sd * temp2 - c.w0 * sinh(arg));
+    c.bjm1             = 1.0 / ((2.0 * c.w0) * (2.0 * c.w0));
+    c.bjm2             = c.bjm1;
+    c.mus1             = c.w1 * c.bjm1;
+    c.thjm2            = 0.0;
+    c.thjm1            = c.mus1;
+    c.zjm1 = c.w0;
+    c.zjm2 = 1.0;
+    c.dzjm1 = 1.0;
+    c.dzjm2 = 0.0;
+    c.d2zjm1 = 0.0;
+    c.d2zjm2 = 0.0;
+  }
+  else
+  {
+    c.w1   = 4.0 / ((sd + 2.0) * (sd - 1.0));
+    c.bjm2 = 1.0 / 3.0;
+    c.bjm1 = 1.0 / 3.0;
+    c.mus1 = c.w1 * c.bjm1;
+    c.cj1  = c.mus1;
+  }
+}
+
+// coefficients of stage j (2..s), advancing the recurrence
+__device__ void coef_next(Coef& c, int j, double* mu, double* nu, double* mus, double* ajm1, double* cjm1)
+{
+  if (c.method == 0)
+  {
+    const double zj   = 2.0 * c.w0 * c.zjm1 - c.zjm2;
+    const double dzj  = 2.0 * c.w0 * c.dzjm1 - c.dzjm2 + 2.0 * c.zjm1;
+    const double d2zj = 2.0 * c.w0 * c.d2zjm1 - c.d2zjm2 + 4.0 * c.dzjm1;
+    const double bj   = d2zj / (dzj * dzj);
+    const double a    = 1.0 - c.zjm1 * c.bjm1;
+    const double m    = 2.0 * c.w0 * bj / c.bjm1;
+    const double n    = -bj / c.bjm2;
+    const double ms   = m * c.w1 / c.w0;
+    *mu = m;
+    *nu = n;
+    *mus = ms;
+    *ajm1 = a;
+    *cjm1 = c.thjm1;
+    const double thj = m * c.thjm1 + n * c.thjm2 + ms * (1.0 - a);
+    c.thjm2 = c.thjm1;
+    c.thjm1 = thj;
+    c.bjm2 = c.bjm1;
+    c.bjm1 = bj;
+    c.zjm2 = c.zjm1;
+    c.zjm1 = zj;
+    c.dzjm2 = c.dzjm1;
+    c.dzjm1 = dzj;
+    c.d2zjm2 = c.d2zjm1;
+    c.d2zjm1 = d2zj;
+  }
+  else
+  {
+    const double jd   = (double)j;
+    const double temj = (jd + 2.0) * (jd - 1.0);
+    const double cj   = temj * c.w1 / 4.0;
+    const double bj   = temj / (2.0 * jd * (jd + 1.0));
+    const double a    = 1.0 - c.bjm1;
+    const double m    = (2.0 * jd - 1.0) / jd * (bj / c.bjm1);
+    const double n    = -(jd - 1.0) / jd * (bj / c.bjm2);
+    *mu = m;
+    *nu = n;
+    *mus = c.w1 * m;
+    *ajm1 = a;
+    *cjm1 = c.cj1;
+    c.cj1 = cj;
+    c.bjm2 = c.bjm1;
+    c.bjm1 = bj;
+  }
+}
+
+// CTA-wide exact sum of per-thread limbs; returns the rounded total to every thread
+template <int NT>
+__device__ double cta_exact_sum(xsum::Limbs& a, unsigned flags, long long (*sm)[xsum::NL], unsigned* sflags,
+                                double* sres)
+{
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) *sflags = 0;
+#pragma unroll
+  for (int k = 0; k < xsum::NL; ++k)
+  {
+    long long v = a.l[k];
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) v += shfl_xor_ll(v, m);
+    if (lane == 0) sm[warp][k] = v;
+  }
+  __syncthreads();
+  if (flags) atomicOr(sflags, flags);
+  __syncthreads();
+  if (tid == 0)
+  {
+    long long tot[xsum::NL];
+    for (int k = 0; k < xsum::NL; ++k)
+    {
+      long long v = 0;
+      for (int w = 0; w < NT / 32; ++w) v += sm[w][k];
+      tot[k] = v;
+    }
+    *sres = xsum::finalize(tot, *sflags);
+  }
+  __syncthreads();
+  const double r = *sres;
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double lap(const double* __restrict__ u, int n, int i, int j, double cx, double cy,
+                                      double cc)
+{
+  const long long k = (long long)j * n + i;
+  const double uc = u[k];
+  const double uw = (i > 0) ? u[k - 1] : 0.0;
+  const double ue = (i < n - 1) ? u[k + 1] : 0.0;
+  const double us = (j > 0) ? u[k - n] : 0.0;
+  const double un = (j < n - 1) ? u[k + n] : 0.0;
+  const double sx = uw + ue, sy = us + un;
+  double acc      = cc * uc;
+  acc             = __fma_rn(cx, sx, acc);
+  acc             = __fma_rn(cy, sy, acc);
+  return acc;
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts, const int* __restrict__ order,
+                                                   int ninst, int* queue, double* __restrict__ yall,
+                                                   double* __restrict__ work, long long total, BatchParams prm)
+{
+  __shared__ long long sm[NT / 32][xsum::NL];
+  __shared__ unsigned sflags;
+  __shared__ double sres;
+  __shared__ int sidx;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = NT / 32;
+
+  for (;;)
+  {
+    if (tid == 0) sidx = atomicAdd(queue, 1);
+    __syncthreads();
+    const int idx = sidx;
+    __syncthreads();
+    if (idx >= ninst) break;
+    BatchInst& I = insts[order[idx]];
+    const int n = I.n;
+    const long long N = (long long)n * n;
+    const double cx = I.cx, cy = I.cy, cc = I.cc, rho = I.rho;
+    // six instance-local regions: the y array and five work regions; roles are indices
+    double* P[6];
+    P[0] = yall + I.off;
+    for (int q = 0; q < 5; ++q) P[q + 1] = work + (long long)q * total + I.off;
+    int iy = 0, iF = 1, iFn = 2;
+    int bufs[3] = {3, 4, 5}; // stage buffers (rotated like the single-problem integrator)
+
+    // F_0 = A y_0
+    for (int j = warp; j < n; j += NW)
+      for (int i = lane; i < n; i += 32) P[iF][(long long)j * n + i] = lap(P[iy], n, i, j, cx, cy, cc);
+    __syncthreads();
+    long long nfe = 1, nst = 0, natt = 0, netf = 0, nexp = 0, stmax = 0, sttot = 0, nhist = 0;
+    double t = 0.0, hnext = 0.0, hlast = 0.0, ep1 = 0.0, ep2 = 0.0;
+    bool after_fail = false;
+    int status      = 0;
+
+    // initial step (Hairer-Norsett-Wanner II.4, probe capped at 1/rho)
+    {
+      const double* yc = P[iy];
+      const double* F0 = P[iF];
+      xsum::Limbs a0, a1;
+      xsum::zero(a0);
+      xsum::zero(a1);
+      unsigned f0 = 0, f1 = 0;
+      for (int j = warp; j < n; j += NW)
+        for (int i = lane; i < n; i += 32)
+        {
+          const long long k = (long long)j * n + i;
+          const double wt   = 1.0 / (prm.rtol * fabs(yc[k]) + prm.atol);
+          const double x0 = yc[k] * wt, x1 = F0[k] * wt;
+          xsum::add(a0, x0 * x0, f0);
+          xsum::add(a1, x1 * x1, f1);
+        }
+      const double d0 = sqrt(cta_exact_sum<NT>(a0, f0, sm, &sflags, &sres) / (double)N);
+      const double d1 = sqrt(cta_exact_sum<NT>(a1, f1, sm, &sflags, &sres) / (double)N);
+      double h0       = (d0 < 1.0e-5 || d1 < 1.0e-5) ? 1.0e-6 : 0.01 * (d0 / d1);
+      if (rho > 0.0 && h0 * rho > 1.0) h0 = 1.0 / rho;
+      if (h0 > prm.tf) h0 = prm.tf;
+      double* y1 = P[bufs[0]];
+      for (int j = warp; j < n; j += NW)
+        for (int i = lane; i < n; i += 32)
+        {
+          const long long k = (long long)j * n + i;
+          y1[k]             = __fma_rn(h0, F0[k], yc[k]);
+        }
+      __syncthreads();
+      xsum::Limbs a2;
+      xsum::zero(a2);
+      unsigned f2 = 0;
+      for (int j = warp; j < n; j += NW)
+        for (int i = lane; i < n; i += 32)
+        {
+          const long long k = (long long)j * n + i;
+          const double f1v  = lap(y1, n, i, j, cx, cy, cc);
+          const double wt   = 1.0 / (prm.rtol * fabs(yc[k]) + prm.atol);
+          const double x    = (f1v - F0[k]) * wt;
+          xsum::add(a2, x * x, f2);
+        }
+      nfe++;
+      const double d2 = sqrt(cta_exact_sum<NT>(a2, f2, sm, &sflags, &sres) / (double)N) / h0;
+      const double dm = d1 > d2 ? d1 : d2;
+      double h1       = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : pow(0.01 / dm, 1.0 / B_ORD);
+      if (!(h1 > 0.0) || !(h1 < 1e300)) h1 = h0;
+      double h = (100.0 * h0 < h1) ? 100.0 * h0 : h1;
+      if (h > prm.tf) h = prm.tf;
+      hnext = h;
+    }
+
+    while (t < prm.tf && status == 0)
+    {
+      if (nst >= prm.maxsteps)
+      {
+        status = -1;
+        break;
+      }
+      int nef = 0;
+      for (;;)
+      {
+        double h = hnext, hmax;
+        bool clipped = false;
+        int s        = d_stages(prm.method, h, rho, prm.smax, &hmax);
+        if (s > prm.smax)
+        {
+          h = hmax;
+          nexp++;
+        }
+        if (t + h >= prm.tf)
+        {
+          h       = prm.tf - t;
+          clipped = true;
+        }
+        s = d_stages(prm.method, h, rho, prm.smax, &hmax);
+        natt++;
+        Coef co;
+        coef_init(co, prm.method, s);
+        const double* yc = P[iy];
+        const double* F0 = P[iF];
+        // stage 1 -> bufs[0]
+        {
+          const double hm1 = h * co.mus1;
+          double* y1       = P[bufs[0]];
+          for (int j = warp; j < n; j += NW)
+            for (int i = lane; i < n; i += 32)
+            {
+              const long long k = (long long)j * n + i;
+              y1[k]             = __fma_rn(hm1, F0[k], yc[k]);
+            }
+          __syncthreads();
+        }
+        const double* ym2 = yc;
+        int last          = 0; // index into bufs of Y_{j-1}
+        for (int jst = 2; jst <= s; ++jst)
+        {
+          double mu, nu, mus, ajm1, cjm1;
+          coef_next(co, jst, &mu, &nu, &mus, &ajm1, &cjm1);
+          const double hm = h * mus;
+          const double tm = hm * cc;
+          const double gc = mu + tm, gx = hm * cx, gy = hm * cy, gn = nu, g0 = (1.0 - mu) - nu;
+          const double gf = -(hm * ajm1);
+          const double* ym1 = P[bufs[last]];
+          const int nxt     = (last + 1) % 3;
+          double* yj        = P[bufs[nxt]];
+          for (int j = warp; j < n; j += NW)
+            for (int i = lane; i < n; i += 32)
+            {
+              const long long k = (long long)j * n + i;
+              const double uw = (i > 0) ? ym1[k - 1] : 0.0;
+              const double ue = (i < n - 1) ? ym1[k + 1] : 0.0;
+              const double us = (j > 0) ? ym1[k - n] : 0.0;
+              const double un = (j < n - 1) ? ym1[k + n] : 0.0;
+              const double sx = uw + ue, sy = us + un;
+              double acc      = gc * ym1[k];
+              acc             = __fma_rn(gx, sx, acc);
+              acc             = __fma_rn(gy, sy, acc);
+              acc             = __fma_rn(gn, ym2[k], acc);
+              acc             = __fma_rn(g0, yc[k], acc);
+              acc             = __fma_rn(gf, F0[k], acc);
+              yj[k]           = acc;
+            }
+          __syncthreads();
+          ym2  = ym1;
+          last = nxt;
+        }
+        const double* Ys = P[bufs[last]];
+        double* Fnew     = P[iFn];
+        // step end: Fnew = A Ys, err = 0.8 (y - Ys) + 0.4 h (F + Fnew), exact WRMS
+        xsum::Limbs ae;
+        xsum::zero(ae);
+        unsigned fe      = 0;
+        const double p4h = 0.4 * h;
+        for (int j = warp; j < n; j += NW)
+          for (int i = lane; i < n; i += 32)
+          {
+            const long long k = (long long)j * n + i;
+            const double f    = lap(Ys, n, i, j, cx, cy, cc);
+            Fnew[k]           = f;
+            const double yv   = yc[k];
+            const double d    = yv - Ys[k];
+            double e          = 0.8 * d;
+            e                 = __fma_rn(p4h, F0[k], e);
+            e                 = __fma_rn(p4h, f, e);
+            const double wt   = 1.0 / (prm.rtol * fabs(yv) + prm.atol);
+            const double x    = e * wt;
+            xsum::add(ae, x * x, fe);
+          }
+        const double dsm = sqrt(cta_exact_sum<NT>(ae, fe, sm, &sflags, &sres) / (double)N);
+        nfe += s;
+        sttot += s;
+        if (s > stmax) stmax = s;
+        if (dsm <= 1.0)
+        { // accept: y <- Ys (role swap with its stage buffer), F <- Fnew
+          t = clipped ? prm.tf : t + h;
+          const int ys = bufs[last];
+          bufs[last]   = iy;
+          iy           = ys;
+          const int tf_ = iF;
+          iF           = iFn;
+          iFn          = tf_;
+          hlast        = h;
+          double hn    = d_controller(prm.controller, h, dsm, ep1, ep2, nhist);
+          double eta   = B_SAFETY * hn / h;
+          const double emx = (nst == 0) ? B_ETAMX1 : (after_fail ? 1.0 : B_GROWTH);
+          if (eta > emx) eta = emx;
+          if (eta >= 1.0 && eta <= 1.5) eta = 1.0;
+          hnext      = h * eta;
+          ep2        = ep1;
+          ep1        = dsm;
+          nhist++;
+          after_fail = false;
+          nst++;
+          break;
+        }
+        netf++;
+        nef++;
+        if (!(dsm == dsm) || nef > 20)
+        {
+          status = -3;
+          break;
+        }
+        double hn  = d_controller(prm.controller, h, dsm, ep1, ep2, nhist);
+        double eta = B_SAFETY * hn / h;
+        if (eta > 1.0) eta = 1.0;
+        if (nef >= 2 && eta > B_ETAMXF) eta = B_ETAMXF;
+        if (eta < B_ETAMIN) eta = B_ETAMIN;
+        hnext      = h * eta;
+        after_fail = true;
+      }
+    }
+    // final state into the y array
+    if (iy != 0)
+    {
+      const double* yc = P[iy];
+      for (int j = warp; j < n; j += NW)
+        for (int i = lane; i < n; i += 32)
+        {
+          const long long k = (long long)j * n + i;
+          P[0][k]           = yc[k];
+        }
+    }
+    __syncthreads();
+    if (tid == 0)
+    {
+      I.status       = status;
+      I.nst          = nst;
+      I.nst_att      = natt;
+      I.netf         = netf;
+      I.nfe          = nfe;
+      I.nst_exp      = nexp;
+      I.stage_max    = stmax;
+      I.stages_total = sttot;
+      I.t            = t;
+      I.hlast        = hlast;
+      I.hnext        = hnext;
+    }
+    __syncthreads();
+  }
+}
+
+} // namespace
+// ---------------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------------
+static bool batch_launch(STS_Batch b, const BatchParams& prm, int threads, int ctas_per_sm)
+{
+  STS_Context ctx = b->ctx;
+  cudaStream_t st = ctx->stream;
+  if (!STS_CUDA_OK(cudaMemsetAsync(b->dqueue, 0, sizeof(int), st))) return false;
+  const int grid = std::max(1, std::min(b->ninst, ctx->num_sms * ctas_per_sm));
+  if (threads == 256)
+    batch_kernel<256><<<grid, 256, 0, st>>>(b->dinst, b->dorder, b->ninst, b->dqueue, b->y, b->work, b->total, prm);
+  else
+    batch_kernel<512><<<grid, 512, 0, st>>>(b->dinst, b->dorder, b->ninst, b->dqueue, b->y, b->work, b->total, prm);
+  return STS_CUDA_OK(cudaGetLastError());
+}
+
+extern "C" STS_Batch STS_BatchCreate(STS_Context ctx, int ninst, const int* n, const double* kx, const double* ky)
+{
+  if (!ctx || ninst < 1 || !n || !kx || !ky)
+  {
+    sts_set_error("STS_BatchCreate: invalid arguments");
+    return nullptr;
+  }
+  ctx_activate(ctx);
+  STS_Batch b = new STS_Batch_();
+  b->ctx      = ctx;
+  b->ninst    = ninst;
+  b->hinst.resize(ninst);
+  long long off = 0;
+  std::vector<double> cost(ninst);
+  for (int i = 0; i < ninst; ++i)
+  {
+    if (n[i] < 2 || n[i] > 46340)
+    {
+      sts_set_error("STS_BatchCreate: instance %d: grid size %d out of range", i, n[i]);
+      delete b;
+      return nullptr;
+    }
+    BatchInst& I = b->hinst[i];
+    memset(&I, 0, sizeof(I));
+    I.n          = n[i];
+    I.off        = off;
+    const double d = 1.0 / (n[i] + 1);
+    I.kx         = kx[i];
+    I.ky         = ky[i];
+    I.cx         = kx[i] / (d * d);
+    I.cy         = ky[i] / (d * d);
+    I.cc         = -2.0 * (I.cx + I.cy);
+    // analytic dominant eigenvalue (diffusion_2D/main.cpp:544) with the 1.01 safety factor
+    const double a = kx[i] / d / d, c = ky[i] / d / d;
+    I.rho        = 1.01 * fabs(-8.0 * (a > c ? a : c));
+    off += (long long)n[i] * n[i];
+    cost[i] = (double)n[i] * n[i] * sqrt(I.rho);
+  }
+  b->total = off;
+  std::vector<int> order(ninst);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+  bool ok = STS_CUDA_OK(cudaMalloc(&b->dinst, ninst * sizeof(BatchInst))) &&
+            STS_CUDA_OK(cudaMalloc(&b->dorder, ninst * sizeof(int))) &&
+            STS_CUDA_OK(cudaMalloc(&b->dqueue, sizeof(int))) &&
+            STS_CUDA_OK(cudaMalloc(&b->y, b->total * sizeof(double))) &&
+            STS_CUDA_OK(cudaMalloc(&b->work, 5 * b->total * sizeof(double))) &&
+            STS_CUDA_OK(cudaMemcpy(b->dinst, b->hinst.data(), ninst * sizeof(BatchInst), cudaMemcpyHostToDevice)) &&
+            STS_CUDA_OK(cudaMemcpy(b->dorder, order.data(), ninst * sizeof(int), cudaMemcpyHostToDevice)) &&
+            STS_CUDA_OK(cudaMemset(b->y, 0, b->total * sizeof(double)));
+  if (!ok)
+  {
+    STS_BatchFree(&b);
+    return nullptr;
+  }
+  return b;
+}
+
+extern "C" int STS_BatchFree(STS_Batch* pb)
+{
+  if (!pb || !*pb) return 0;
+  STS_Batch b = *pb;
+  cudaSetDevice(b->ctx->device);
+  cudaFree(b->dinst);
+  cudaFree(b->dorder);
+  cudaFree(b->dqueue);
+  cudaFree(b->y);
+  cudaFree(b->work);
+  delete b;
+  *pb = nullptr;
+  return 0;
+}
+
+extern "C" long long STS_BatchTotalDOF(STS_Batch b) { return b ? b->total : 0; }
+
+extern "C" int STS_BatchSetState(STS_Batch b, const double* host_y)
+{
+  if (!b || !host_y) return -1;
+  ctx_activate(b->ctx);
+  return STS_CUDA_OK(cudaMemcpy(b->y, host_y, b->total * sizeof(double), cudaMemcpyHostToDevice)) ? 0 : -1;
+}
+
+extern "C" int STS_BatchGetState(STS_Batch b, double* host_y)
+{
+  if (!b || !host_y) return -1;
+  ctx_activate(b->ctx);
+  if (!STS_CUDA_OK(cudaStreamSynchronize(b->ctx->stream))) return -1;
+  return STS_CUDA_OK(cudaMemcpy(host_y, b->y, b->total * sizeof(double), cudaMemcpyDeviceToHost)) ? 0 : -1;
+}
+
+// initial states sum_k a_k sin(p_k pi x) sin(q_k pi y), nmodes per instance (host tabulated)
+extern "C" int STS_BatchSetInitialModes(STS_Batch b, int nmodes, const int* p, const int* q, const double* a)
+{
+  if (!b || nmodes < 0) return -1;
+  std::vector<double> h(b->total);
+  const double PI = 3.14159265358979323846;
+  for (int i = 0; i < b->ninst; ++i)
+  {
+    const BatchInst& I = b->hinst[i];
+    const int n        = I.n;
+    const double d     = 1.0 / (n + 1);
+    for (int jj = 0; jj < n; ++jj)
+      for (int ii = 0; ii < n; ++ii)
+      {
+        const double x = (ii + 1) * d, y = (jj + 1) * d;
+        double v       = 0.0;
+        for (int k = 0; k < nmodes; ++k)
+        {
+          const int m = i * nmodes + k;
+          v += a[m] * sin(p[m] * PI * x) * sin(q[m] * PI * y);
+        }
+        h[I.off + (long long)jj * n + ii] = v;
+      }
+  }
+  return STS_BatchSetState(b, h.data());
+}
+
+extern "C" int STS_BatchEvolve(STS_Batch b, double tf, int method, double rtol, double atol, int smax, int controller,
+                               long long maxsteps)
+{
+  if (!b || !(tf > 0.0) || smax < 2) return STS_ILL_INPUT;
+  ctx_activate(b->ctx);
+  BatchParams prm;
+  prm.tf         = tf;
+  prm.rtol       = rtol;
+  prm.atol       = atol;
+  prm.eig_safety = 1.01;
+  prm.method     = method;
+  prm.smax       = smax;
+  prm.controller = controller;
+  prm.maxsteps   = (int)(maxsteps > 0 ? std::min<long long>(maxsteps, 1LL << 30) : 1000000);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, b->ctx->stream);
+  const bool ok = batch_launch(b, prm, b->block, b->ctas_per_sm);
+  cudaEventRecord(e1, b->ctx->stream);
+  if (!ok || !STS_CUDA_OK(cudaEventSynchronize(e1)))
+  {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return STS_ERR_FAILURE;
+  }
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  b->last_ms = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!STS_CUDA_OK(cudaMemcpy(b->hinst.data(), b->dinst, b->ninst * sizeof(BatchInst), cudaMemcpyDeviceToHost)))
+    return STS_ERR_FAILURE;
+  for (const BatchInst& I : b->hinst)
+    if (I.status < 0) return I.status;
+  return STS_SUCCESS;
+}
+
+extern "C" double STS_BatchLastMilliseconds(STS_Batch b) { return b ? b->last_ms : 0.0; }
+
+extern "C" int STS_BatchGetInstanceStats(STS_Batch b, int inst, STS_Stats* s)
+{
+  if (!b || inst < 0 || inst >= b->ninst || !s) return -1;
+  const BatchInst& I = b->hinst[inst];
+  memset(s, 0, sizeof(*s));
+  s->nst             = I.nst;
+  s->nst_attempts    = I.nst_att;
+  s->netf            = I.netf;
+  s->nfe             = I.nfe;
+  s->nst_exp         = I.nst_exp;
+  s->stage_max       = I.stage_max;
+  s->stages_total    = I.stages_total;
+  s->t               = I.t;
+  s->hlast           = I.hlast;
+  s->hnext           = I.hnext;
+  s->spectral_radius = I.rho;
+  return 0;
+}
+
+extern "C" int STS_BatchSetLaunch(STS_Batch b, int threads, int ctas_per_sm)
+{
+  if (!b || (threads != 256 && threads != 512) || ctas_per_sm < 1 || ctas_per_sm > 8)
+    return STS_ILL_INPUT;
+  b->block       = threads;
+  b->ctas_per_sm = ctas_per_sm;
+  return 0;
+}
+
+// Autotuner: runs the batch from its current state to tf_probe with every launch shape,
+// restores the state after each probe, and keeps the fastest shape.
+extern "C" int STS_BatchAutotune(STS_Batch b, double tf_probe, int method, double rtol, double atol, int smax,
+                                 int* threads, int* ctas_per_sm, double* ms_best)
+{
+  if (!b) return -1;
+  ctx_activate(b->ctx);
+  double* save = nullptr;
+  if (!STS_CUDA_OK(cudaMalloc(&save, b->total * sizeof(double)))) return -1;
+  cudaMemcpyAsync(save, b->y, b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->ctx->stream);
+  const int shapes[][2] = {{256, 1}, {256, 2}, {512, 1}, {512, 2}};
+  double best           = 1e30;
+  int bt = b->block, bc = b->ctas_per_sm;
+  for (auto& sh : shapes)
+  {
+    b->block       = sh[0];
+    b->ctas_per_sm = sh[1];
+    const int rc   = STS_BatchEvolve(b, tf_probe, method, rtol, atol, smax, 2, 0);
+    cudaMemcpyAsync(b->y, save, b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->ctx->stream);
+    if (rc == 0 && b->last_ms < best)
+    {
+      best = b->last_ms;
+      bt   = sh[0];
+      bc   = sh[1];
+    }
+  }
+  cudaStreamSynchronize(b->ctx->stream);
+  cudaFree(save);
+  b->block       = bt;
+  b->ctas_per_sm = bc;
+  if (threads) *threads = bt;
+  if (ctas_per_sm) *ctas_per_sm = bc;
+  if (ms_best) *ms_best = best;
+  return 0;
+}

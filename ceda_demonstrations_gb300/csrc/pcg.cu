@@ -16,6 +16,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <functional>
 
 #include "kernels.cuh"
 #include "sts_internal.cuh"
@@ -278,8 +279,10 @@ static void pcg_record_batch(PcgWork* w, STS_Problem p, double* x)
   }
 }
 
-extern "C" int STS_ImplicitSolvePCG(STS_Problem p, double gamma, N_Vector b, N_Vector x, double tol, int maxit,
-                                    int jacobi, int* iters, double* relres)
+// Fused PCG solve; `batch_cb` (optional) is called after every graph batch of PCG_BATCH
+// iterations with the device pointers of the current iterate and residual.
+int sts_pcg_run(STS_Problem p, double gamma, N_Vector b, N_Vector x, double tol, int maxit, int jacobi, int* iters,
+                double* relres, const std::function<void(int, const double*, const double*)>& batch_cb)
 {
   if (!p || !b || !x || NVL(b) != p->nx * p->ny || NVL(x) != NVL(b) || maxit < 1)
   {
@@ -340,6 +343,7 @@ extern "C" int STS_ImplicitSolvePCG(STS_Problem p, double gamma, N_Vector b, N_V
       ret = -1;
       break;
     }
+    if (batch_cb) batch_cb(((volatile PcgOut*)w->h_out)->iters, NVD(x), w->r);
     if (((volatile PcgOut*)w->h_out)->state != 0) break;
   }
   const int state = w->h_out->state;
@@ -349,6 +353,12 @@ extern "C" int STS_ImplicitSolvePCG(STS_Problem p, double gamma, N_Vector b, N_V
   if (ret == 0 && state == 2) ret = 1; // iteration limit: recoverable
   pcg_free(w);
   return ret;
+}
+
+extern "C" int STS_ImplicitSolvePCG(STS_Problem p, double gamma, N_Vector b, N_Vector x, double tol, int maxit,
+                                    int jacobi, int* iters, double* relres)
+{
+  return sts_pcg_run(p, gamma, b, x, tol, maxit, jacobi, iters, relres, nullptr);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -1,0 +1,971 @@
+// Learned multilevel preconditioner: a small linear convolutional network (4 levels, 16
+// channels, 3x3 kernels, BF16 weights, FP32 accumulation) with hand-written training and
+// inference kernels. The architecture and the gradient formulas follow the CPU reference
+// oracle/convnet.py, against which the tests check the forward output and the gradients.
+//
+//   a0 = conv(x, W_in)            x = [r, r s_k, r s_g] * scale      (3 -> 16, n)
+//   a1 = conv(pool(a0), W_d1)     a2 = conv(pool(a1), W_d2)           (n/2, n/4)
+//   a3 = conv(conv(pool(a2), W_d3), W_c)                               (n/8)
+//   b2 = conv(up(a3) + a2, W_u2)  b1 = conv(up(b2) + a1, W_u1)  b0 = conv(up(b1) + a0, W_u0)
+//   z  = conv(b0, W_out) * jacobi / scale                              (16 -> 1, n)
+//
+// Activations are NHWC BF16 with 16 channels (32 bytes per pixel). The 3x3 convolutions are
+// implicit GEMMs on the tensor cores (mma.sync m16n8k16 BF16 -> FP32): a CTA stages a
+// (rows+2) x (64+2) pixel tile in shared memory (16-byte halves XOR-swizzled by pixel so
+// ldmatrix is conflict-free), each warp computes 16-pixel x 16-channel tiles over the nine
+// taps with the weights held in registers as MMA fragments. The input gradient is the same
+// kernel with the flipped, transposed weights; the weight gradient is a per-tile FP32
+// reduction added to global memory with atomics.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "sts_internal.cuh"
+
+namespace net {
+
+constexpr int CH = 16;
+constexpr int NLAYER = 9; // W_in, W_d1, W_d2, W_d3, W_c, W_u2, W_u1, W_u0, W_out
+constexpr int WSZ = CH * CH * 9; // every layer stored as 16 x 16 x 3 x 3 (zero padded)
+enum { L_IN = 0, L_D1, L_D2, L_D3, L_C, L_U2, L_U1, L_U0, L_OUT };
+
+// conv tile: CTA = 4 warps, tile = TR rows x 64 columns, each warp one row at a time
+constexpr int TC = 64;
+constexpr int TR = 4;
+constexpr int NTHR = 128;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// swizzled byte offset of (pixel p of the tile row, channel half h) within a tile row
+__device__ __forceinline__ int swz(int p, int h) { return p * 32 + ((h ^ ((p >> 2) & 1)) << 4); }
+
+// Weight fragments: wf[(tap * 2 + nh) * 32 + lane] = {b0b1, b2b3} for n-half nh
+// (B[k = ci][n = co], b0b1 = ci (lane%4)*2..+1, b2b3 = ci (lane%4)*2+8..+9, co = nh*8 + lane/4)
+
+// Per-sample metadata of a training batch: {sk, sg, jacobi, scale, 1/||e||^2}
+constexpr int META = 5;
+__device__ __forceinline__ double meta_out_scale(const float* meta, int img)
+{
+  return (double)meta[META * img + 2] / (double)meta[META * img + 3];
+}
+
+// out[p][co] = sum_{tap, ci} w[co][ci][tap] * in[p + tap - 1][ci], for each image of a batch
+// (blockIdx.z; images of H x W pixels stored one after another, zero padding at every edge)
+// mode 0: BF16 NHWC output (16 channels); mode 1: FP64 output of channel 0 times the image's
+// output scale (meta, or out_scale when meta is null)
+template <int MODE>
+__global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __restrict__ in, int H, int W,
+                                                       const uint2* __restrict__ wf, __nv_bfloat16* __restrict__ out,
+                                                       double* __restrict__ out64, double out_scale,
+                                                       const float* __restrict__ meta)
+{
+  __shared__ __align__(128) unsigned char tile[(TR + 2) * (TC + 2) * 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int x0 = blockIdx.x * TC, y0 = blockIdx.y * TR;
+  const long long img_pix = (long long)H * W * blockIdx.z;
+  in += img_pix * CH;
+  if (MODE == 0) out += img_pix * CH;
+  else
+  {
+    out64 += img_pix;
+    if (meta) out_scale = meta_out_scale(meta, blockIdx.z);
+  }
+  // stage the input tile with a one-pixel halo (16-byte chunks, zero outside the image)
+  for (int c = tid; c < (TR + 2) * (TC + 2) * 2; c += NTHR)
+  {
+    const int h = c & 1, pix = c >> 1;
+    const int ty = pix / (TC + 2), tx = pix % (TC + 2);
+    const int gy = y0 + ty - 1, gx = x0 + tx - 1;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+      v = *reinterpret_cast<const uint4*>(in + ((long long)gy * W + gx) * CH + h * 8);
+    *reinterpret_cast<uint4*>(tile + ty * (TC + 2) * 32 + swz(tx, h)) = v;
+  }
+  // weights into registers
+  uint2 wr[9][2];
+#pragma unroll
+  for (int t = 0; t < 9; ++t)
+#pragma unroll
+    for (int nh = 0; nh < 2; ++nh) wr[t][nh] = wf[(t * 2 + nh) * 32 + lane];
+  __syncthreads();
+  const int row = warp; // one tile row per warp (TR == 4 warps)
+  const int gy  = y0 + row;
+#pragma unroll 1
+  for (int mt = 0; mt < TC / 16; ++mt)
+  {
+    float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+    for (int t = 0; t < 9; ++t)
+    {
+      const int dy = t / 3, dx = t % 3;
+      // ldmatrix.x4 row addresses: lanes 0-7 pixels 0-7 half 0, 8-15 pixels 8-15 half 0,
+      // 16-23 pixels 0-7 half 1, 24-31 pixels 8-15 half 1
+      const int pi = (lane & 7) + ((lane >> 3) & 1) * 8;
+      const int hh = lane >> 4;
+      const int px = mt * 16 + pi + dx; // tile column (halo offset included via dx)
+      const unsigned char* rp = tile + (row + dy) * (TC + 2) * 32 + swz(px, hh);
+      uint32_t a0, a1, a2, a3;
+      asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                   : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3)
+                   : "r"(smem_u32(rp)));
+#pragma unroll
+      for (int nh = 0; nh < 2; ++nh)
+      {
+        asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                     "{%0,%1,%2,%3};"
+                     : "+f"(acc[nh][0]), "+f"(acc[nh][1]), "+f"(acc[nh][2]), "+f"(acc[nh][3])
+                     : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(wr[t][nh].x), "r"(wr[t][nh].y));
+      }
+    }
+    // accumulator layout: c0,c1 -> pixel lane/4, channels (lane%4)*2..+1; c2,c3 -> pixel lane/4+8
+    if (gy < H)
+    {
+      const int pr0 = lane >> 2;
+#pragma unroll
+      for (int half = 0; half < 2; ++half)
+      {
+        const int gx = x0 + mt * 16 + pr0 + half * 8;
+        if (gx >= W) continue;
+        const long long p = (long long)gy * W + gx;
+        if (MODE == 0)
+        {
+#pragma unroll
+          for (int nh = 0; nh < 2; ++nh)
+          {
+            const int co = nh * 8 + (lane & 3) * 2;
+            __nv_bfloat162 v = __floats2bfloat162_rn(acc[nh][half * 2], acc[nh][half * 2 + 1]);
+            *reinterpret_cast<__nv_bfloat162*>(out + p * CH + co) = v;
+          }
+        }
+        else if ((lane & 3) == 0)
+          out64[p] = (double)acc[0][half * 2] * out_scale;
+      }
+    }
+  }
+}
+
+// 2x2 mean pooling (FP32 arithmetic, BF16 storage); W, H of the fine level
+__global__ void pool_kernel(const __nv_bfloat16* __restrict__ in, int H, int W, __nv_bfloat16* __restrict__ out)
+{
+  const int Wc = W / 2, Hc = H / 2;
+  const long long n = (long long)Hc * Wc * CH;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+  {
+    const int c = (int)(k % CH);
+    const long long p = k / CH;
+    const int x = (int)(p % Wc), y = (int)(p / Wc);
+    const long long f = ((long long)(2 * y) * W + 2 * x) * CH + c;
+    const float s = __bfloat162float(in[f]) + __bfloat162float(in[f + CH]) + __bfloat162float(in[f + (long long)W * CH]) +
+                    __bfloat162float(in[f + (long long)W * CH + CH]);
+    out[k] = __float2bfloat16_rn(0.25f * s);
+  }
+}
+
+// s = up(coarse) + fine (nearest-neighbour upsampling)
+__global__ void upadd_kernel(const __nv_bfloat16* __restrict__ coarse, const __nv_bfloat16* __restrict__ fine, int H,
+                             int W, __nv_bfloat16* __restrict__ out)
+{
+  const long long n = (long long)H * W * CH;
+  const int Wc      = W / 2;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+  {
+    const int c = (int)(k % CH);
+    const long long p = k / CH;
+    const int x = (int)(p % W), y = (int)(p / W);
+    const float v = __bfloat162float(coarse[((long long)(y / 2) * Wc + x / 2) * CH + c]) + __bfloat162float(fine[k]);
+    out[k] = __float2bfloat16_rn(v);
+  }
+}
+
+// backward helpers (FP32 gradients stored as BF16 activations-gradients for the conv kernel)
+// g_coarse = up^T(g) (2x2 sum); g_coarse += pool^T adds 0.25 g to each fine pixel
+__global__ void upT_kernel(const __nv_bfloat16* __restrict__ g, int H, int W, __nv_bfloat16* __restrict__ gc,
+                           int accumulate)
+{
+  const int Wc = W / 2, Hc = H / 2;
+  const long long n = (long long)Hc * Wc * CH;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+  {
+    const int c = (int)(k % CH);
+    const long long p = k / CH;
+    const int x = (int)(p % Wc), y = (int)(p / Wc);
+    const long long f = ((long long)(2 * y) * W + 2 * x) * CH + c;
+    float s = __bfloat162float(g[f]) + __bfloat162float(g[f + CH]) + __bfloat162float(g[f + (long long)W * CH]) +
+              __bfloat162float(g[f + (long long)W * CH + CH]);
+    if (accumulate) s += __bfloat162float(gc[k]);
+    gc[k] = __float2bfloat16_rn(s);
+  }
+}
+
+// g_fine += 0.25 * repeat(g_coarse)   (adjoint of the 2x2 mean pooling)
+__global__ void poolT_add_kernel(const __nv_bfloat16* __restrict__ gcoarse, int H, int W, __nv_bfloat16* __restrict__ gf)
+{
+  const long long n = (long long)H * W * CH;
+  const int Wc      = W / 2;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+  {
+    const int c = (int)(k % CH);
+    const long long p = k / CH;
+    const int x = (int)(p % W), y = (int)(p / W);
+    const float v = __bfloat162float(gf[k]) + 0.25f * __bfloat162float(gcoarse[((long long)(y / 2) * Wc + x / 2) * CH + c]);
+    gf[k] = __float2bfloat16_rn(v);
+  }
+}
+
+// dL/dz (FP64, one channel) -> BF16 NHWC gradient (channel 0) times scale; with meta, the
+// image's scale is out_scale * (1/||e||^2) * scale
+__global__ void gradz_kernel(long long npix, long long img_pix, const double* __restrict__ z,
+                             const float* __restrict__ e, double scale, const float* __restrict__ meta,
+                             __nv_bfloat16* __restrict__ g)
+{
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x)
+  {
+    double sc = scale;
+    if (meta)
+    {
+      const int img = (int)(p / img_pix);
+      sc *= meta_out_scale(meta, img) * (double)meta[META * img + 4];
+    }
+    const float d = (float)((z[p] - (double)e[p]) * sc);
+    __align__(16) __nv_bfloat16 o[CH];
+    o[0] = __float2bfloat16_rn(d);
+#pragma unroll
+    for (int c = 1; c < CH; ++c) o[c] = __float2bfloat16_rn(0.f);
+    uint4* dst = reinterpret_cast<uint4*>(g + p * CH);
+    dst[0]     = reinterpret_cast<uint4*>(o)[0];
+    dst[1]     = reinterpret_cast<uint4*>(o)[1];
+  }
+}
+
+// weight gradient: dW[co][ci][tap] += sum_p g[p][co] * x[p + tap - 1][ci] over every image
+// of the batch. Each CTA walks 16 x 16 tiles (grid-stride over tiles of all images), keeps
+// its partial sums in registers and adds them to dW with one atomicAdd per weight.
+__global__ void __launch_bounds__(256) wgrad_kernel(const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ g,
+                                                   int H, int W, int nimg, float* __restrict__ dW)
+{
+  __shared__ float xs[18][18][CH];
+  __shared__ float gs[16][16][CH];
+  const int tid = threadIdx.x;
+  const int tx_n = (W + 15) / 16, ty_n = (H + 15) / 16;
+  const long long ntiles = (long long)tx_n * ty_n * nimg;
+  // 2304 weights / 256 threads = 9 per thread: thread -> (co, ci) pair, all 9 taps
+  const int co = tid / CH, ci = tid % CH;
+  float acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (long long tl = blockIdx.x; tl < ntiles; tl += gridDim.x)
+  {
+    const int img = (int)(tl / ((long long)tx_n * ty_n));
+    const int rem = (int)(tl % ((long long)tx_n * ty_n));
+    const int x0 = (rem % tx_n) * 16, y0 = (rem / tx_n) * 16;
+    const __nv_bfloat16* xi = x + (long long)img * H * W * CH;
+    const __nv_bfloat16* gi = g + (long long)img * H * W * CH;
+    __syncthreads(); // previous tile consumed
+    for (int k = tid; k < 18 * 18 * CH; k += 256)
+    {
+      const int c = k % CH, px = (k / CH) % 18, py = k / (CH * 18);
+      const int gx = x0 + px - 1, gy = y0 + py - 1;
+      xs[py][px][c] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? __bfloat162float(xi[((long long)gy * W + gx) * CH + c]) : 0.f;
+    }
+    for (int k = tid; k < 16 * 16 * CH; k += 256)
+    {
+      const int c = k % CH, px = (k / CH) % 16, py = k / (CH * 16);
+      const int gx = x0 + px, gy = y0 + py;
+      gs[py][px][c] = (gx < W && gy < H) ? __bfloat162float(gi[((long long)gy * W + gx) * CH + c]) : 0.f;
+    }
+    __syncthreads();
+    for (int py = 0; py < 16; ++py)
+      for (int px = 0; px < 16; ++px)
+      {
+        const float gv = gs[py][px][co];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) acc[t] = fmaf(gv, xs[py + t / 3][px + t % 3][ci], acc[t]);
+      }
+  }
+#pragma unroll
+  for (int t = 0; t < 9; ++t)
+    if (acc[t] != 0.f) atomicAdd(&dW[(co * CH + ci) * 9 + t], acc[t]);
+}
+
+// Adam on FP32 master weights; mask keeps padded entries at zero; writes the BF16 copy
+__global__ void adam_kernel(int n, float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                            const float* __restrict__ g, const float* __restrict__ mask, float lr, float b1, float b2,
+                            float eps, float bc1, float bc2, float gscale)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float gk = g[k] * gscale;
+  m[k] = b1 * m[k] + (1.f - b1) * gk;
+  v[k] = b2 * v[k] + (1.f - b2) * gk * gk;
+  const float mh = m[k] / bc1, vh = v[k] / bc2;
+  w[k] = (w[k] - lr * mh / (sqrtf(vh) + eps)) * mask[k];
+}
+
+} // namespace net
+
+// ---------------------------------------------------------------------------------------
+// host side: network state, forward / backward, training, inference
+// ---------------------------------------------------------------------------------------
+namespace net {
+
+// fragment layout of one layer's weights (BF16, see conv3x3_kernel); transpose = 1 builds
+// the input-gradient weights W'[ci][co][8 - t] = W[co][ci][t]
+__global__ void frag_kernel(const float* __restrict__ W, uint2* __restrict__ wf, int transpose)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x; // 0 .. 9*2*32
+  if (k >= 9 * 2 * 32) return;
+  const int lane = k & 31, nh = (k >> 5) & 1, t = k >> 6;
+  const int co = nh * 8 + (lane >> 2), ci0 = (lane & 3) * 2;
+  auto w = [&](int o, int i) -> float {
+    return transpose ? W[(i * CH + o) * 9 + (8 - t)] : W[(o * CH + i) * 9 + t];
+  };
+  __nv_bfloat162 lo = __floats2bfloat162_rn(w(co, ci0), w(co, ci0 + 1));
+  __nv_bfloat162 hi = __floats2bfloat162_rn(w(co, ci0 + 8), w(co, ci0 + 9));
+  uint2 v;
+  v.x   = *reinterpret_cast<uint32_t*>(&lo);
+  v.y   = *reinterpret_cast<uint32_t*>(&hi);
+  wf[k] = v;
+}
+
+// x = [r, r sk, r sg] * scale (BF16 NHWC, channels 3..15 zero); with meta, sk, sg and scale
+// are the image's
+template <typename T>
+__global__ void input_kernel_t(long long npix, long long img_pix, const T* __restrict__ r, double scale, float sk,
+                               float sg, const float* __restrict__ meta, __nv_bfloat16* __restrict__ x)
+{
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x)
+  {
+    if (meta)
+    {
+      const int img = (int)(p / img_pix);
+      sk            = meta[META * img];
+      sg            = meta[META * img + 1];
+      scale         = (double)meta[META * img + 3];
+    }
+    const float v = (float)((double)r[p] * scale);
+    __align__(16) __nv_bfloat16 o[CH];
+    o[0] = __float2bfloat16_rn(v);
+    o[1] = __float2bfloat16_rn(v * sk);
+    o[2] = __float2bfloat16_rn(v * sg);
+#pragma unroll
+    for (int c = 3; c < CH; ++c) o[c] = __float2bfloat16_rn(0.f);
+    uint4* dst = reinterpret_cast<uint4*>(x + p * CH);
+    dst[0]     = reinterpret_cast<uint4*>(o)[0];
+    dst[1]     = reinterpret_cast<uint4*>(o)[1];
+  }
+}
+
+// acc += sum_p w_img (z_p - e_p)^2 with w_img = 1/||e||^2 of the image (meta) or 1
+__global__ void sq_diff_kernel(long long n, long long img_pix, const double* __restrict__ z,
+                               const float* __restrict__ e, const float* __restrict__ meta, double* acc)
+{
+  double s = 0.0;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
+  {
+    const double d = z[p] - (double)e[p];
+    s += d * d * (meta ? (double)meta[META * (int)(p / img_pix) + 4] : 1.0);
+  }
+  for (int m = 16; m >= 1; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+  if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
+}
+
+// dst[q] = src[idx[q]] for q < nb samples of `len` floats each (and their metadata)
+__global__ void gather_kernel(const float* __restrict__ r, const float* __restrict__ e, const float* __restrict__ meta,
+                              const int* __restrict__ idx, int nb, long long len, float* __restrict__ rb,
+                              float* __restrict__ eb, float* __restrict__ mb)
+{
+  const long long n = (long long)nb * len;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+  {
+    const int q = (int)(k / len);
+    const long long off = (long long)idx[q] * len + (k % len);
+    rb[k] = r[off];
+    eb[k] = e[off];
+    if (k % len < META) mb[META * q + k % len] = meta[META * idx[q] + k % len];
+  }
+}
+
+struct Level {
+  int n = 0;
+  __nv_bfloat16 *x = nullptr, *a = nullptr, *p = nullptr, *c = nullptr, *s = nullptr, *b = nullptr;
+  __nv_bfloat16 *ga = nullptr, *gb = nullptr, *gt = nullptr; // gradient buffers
+};
+
+} // namespace net
+
+struct STS_Net_ {
+  STS_Context ctx = nullptr;
+  int nmax        = 0;
+  long long cap   = 0;       // pixels the level-0 buffers hold (images x n x n)
+  float* w        = nullptr; // FP32 master weights, 9 x 2304
+  float* mask     = nullptr;
+  float *m = nullptr, *v = nullptr, *g = nullptr;
+  uint2* wf       = nullptr; // forward fragments, 9 x 576
+  uint2* wt       = nullptr; // input-gradient fragments
+  net::Level L[4];
+  double* z       = nullptr; // FP64 output at the finest level
+  double* dacc    = nullptr;
+  float *rb = nullptr, *eb = nullptr, *mb = nullptr; // minibatch staging
+  int* idx        = nullptr;
+  long long adam_t = 0;
+};
+
+using net::CH;
+using net::WSZ;
+using net::NLAYER;
+using net::META;
+
+static void* dalloc(size_t bytes, bool* ok)
+{
+  void* p = nullptr;
+  if (!STS_CUDA_OK(cudaMalloc(&p, bytes))) *ok = false;
+  return p;
+}
+
+static int grid_for(long long n) { return (int)std::min<long long>((n + 255) / 256, 4096); }
+
+static void free_levels(STS_Net nt)
+{
+  for (auto& L : nt->L)
+  {
+    cudaFree(L.x);
+    cudaFree(L.a);
+    cudaFree(L.p);
+    cudaFree(L.c);
+    cudaFree(L.s);
+    cudaFree(L.b);
+    cudaFree(L.ga);
+    cudaFree(L.gb);
+    cudaFree(L.gt);
+    L = net::Level();
+  }
+  cudaFree(nt->z);
+  cudaFree(nt->rb);
+  cudaFree(nt->eb);
+  nt->z = nullptr;
+  nt->rb = nt->eb = nullptr;
+  nt->cap = 0;
+}
+
+// activation buffers for `pix` level-0 pixels (a batch of images of one size)
+static bool ensure_capacity(STS_Net nt, long long pix)
+{
+  if (pix <= nt->cap) return true;
+  cudaStreamSynchronize(nt->ctx->stream);
+  free_levels(nt);
+  bool ok = true;
+  for (int l = 0; l < 4 && ok; ++l)
+  {
+    const long long np = (pix >> (2 * l)) * CH * 2;
+    nt->L[l].x  = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].a  = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].p  = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].c  = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].s  = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].b  = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].ga = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].gb = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].gt = (__nv_bfloat16*)dalloc(np, &ok);
+  }
+  nt->z  = (double*)dalloc((size_t)pix * 8, &ok);
+  nt->rb = (float*)dalloc((size_t)pix * 4, &ok);
+  nt->eb = (float*)dalloc((size_t)pix * 4, &ok);
+  if (!ok)
+  {
+    free_levels(nt);
+    return false;
+  }
+  nt->cap = pix;
+  return true;
+}
+
+static void refresh_frags(STS_Net nt)
+{
+  cudaStream_t st = nt->ctx->stream;
+  for (int l = 0; l < NLAYER; ++l)
+  {
+    net::frag_kernel<<<3, 256, 0, st>>>(nt->w + l * WSZ, nt->wf + l * 576, 0);
+    net::frag_kernel<<<3, 256, 0, st>>>(nt->w + l * WSZ, nt->wt + l * 576, 1);
+  }
+}
+
+extern "C" STS_Net STS_NetCreate(STS_Context ctx, int nmax, unsigned long long seed)
+{
+  if (!ctx || nmax < 16 || nmax % 16 != 0)
+  {
+    sts_set_error("STS_NetCreate: nmax must be a positive multiple of 16");
+    return nullptr;
+  }
+  ctx_activate(ctx);
+  STS_Net nt = new STS_Net_();
+  nt->ctx    = ctx;
+  nt->nmax   = nmax;
+  bool ok    = true;
+  nt->w    = (float*)dalloc(NLAYER * WSZ * 4, &ok);
+  nt->mask = (float*)dalloc(NLAYER * WSZ * 4, &ok);
+  nt->m    = (float*)dalloc(NLAYER * WSZ * 4, &ok);
+  nt->v    = (float*)dalloc(NLAYER * WSZ * 4, &ok);
+  nt->g    = (float*)dalloc(NLAYER * WSZ * 4, &ok);
+  nt->wf   = (uint2*)dalloc(NLAYER * 576 * 8, &ok);
+  nt->wt   = (uint2*)dalloc(NLAYER * 576 * 8, &ok);
+  nt->dacc = (double*)dalloc(8, &ok);
+  if (!ok || !ensure_capacity(nt, (long long)nmax * nmax))
+  {
+    STS_NetFree(&nt);
+    return nullptr;
+  }
+  // initial weights: N(0, 1/fan_in), zero outside the real channels (W_in: 3 inputs, W_out: 1 output)
+  std::vector<float> w(NLAYER * WSZ, 0.f), mask(NLAYER * WSZ, 0.f);
+  std::mt19937_64 rng(seed);
+  std::normal_distribution<float> nd(0.f, 1.f);
+  for (int l = 0; l < NLAYER; ++l)
+  {
+    const int ci_n = (l == net::L_IN) ? 3 : CH, co_n = (l == net::L_OUT) ? 1 : CH;
+    const float sd = std::sqrt(1.0f / (ci_n * 9));
+    for (int co = 0; co < co_n; ++co)
+      for (int ci = 0; ci < ci_n; ++ci)
+        for (int t = 0; t < 9; ++t)
+        {
+          const int k = l * WSZ + (co * CH + ci) * 9 + t;
+          w[k]        = nd(rng) * sd;
+          mask[k]     = 1.f;
+        }
+  }
+  cudaMemcpy(nt->w, w.data(), w.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(nt->mask, mask.data(), mask.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemset(nt->m, 0, NLAYER * WSZ * 4);
+  cudaMemset(nt->v, 0, NLAYER * WSZ * 4);
+  refresh_frags(nt);
+  if (!STS_CUDA_OK(cudaStreamSynchronize(ctx->stream)))
+  {
+    STS_NetFree(&nt);
+    return nullptr;
+  }
+  return nt;
+}
+
+extern "C" int STS_NetFree(STS_Net* pn)
+{
+  if (!pn || !*pn) return 0;
+  STS_Net nt = *pn;
+  cudaSetDevice(nt->ctx->device);
+  cudaStreamSynchronize(nt->ctx->stream);
+  cudaFree(nt->w);
+  cudaFree(nt->mask);
+  cudaFree(nt->m);
+  cudaFree(nt->v);
+  cudaFree(nt->g);
+  cudaFree(nt->wf);
+  cudaFree(nt->wt);
+  cudaFree(nt->dacc);
+  cudaFree(nt->mb);
+  cudaFree(nt->idx);
+  free_levels(nt);
+  delete nt;
+  *pn = nullptr;
+  return 0;
+}
+
+// Weights in the order W_in, W_d1, W_d2, W_d3, W_c, W_u2, W_u1, W_u0, W_out, each stored
+// as [co][ci][3][3] with 16 x 16 entries (unused channels zero).
+extern "C" int STS_NetSetWeights(STS_Net nt, const float* w)
+{
+  if (!nt || !w) return -1;
+  ctx_activate(nt->ctx);
+  std::vector<float> mask(NLAYER * WSZ);
+  cudaMemcpy(mask.data(), nt->mask, mask.size() * 4, cudaMemcpyDeviceToHost);
+  std::vector<float> wm(w, w + NLAYER * WSZ);
+  for (size_t k = 0; k < wm.size(); ++k) wm[k] *= mask[k];
+  if (!STS_CUDA_OK(cudaMemcpy(nt->w, wm.data(), wm.size() * 4, cudaMemcpyHostToDevice))) return -1;
+  refresh_frags(nt);
+  return STS_CUDA_OK(cudaStreamSynchronize(nt->ctx->stream)) ? 0 : -1;
+}
+
+extern "C" int STS_NetGetWeights(STS_Net nt, float* w)
+{
+  if (!nt || !w) return -1;
+  ctx_activate(nt->ctx);
+  cudaStreamSynchronize(nt->ctx->stream);
+  return STS_CUDA_OK(cudaMemcpy(w, nt->w, NLAYER * WSZ * 4, cudaMemcpyDeviceToHost)) ? 0 : -1;
+}
+
+static void conv(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, int layer, bool transposed, __nv_bfloat16* out)
+{
+  dim3 g((unsigned)((n + net::TC - 1) / net::TC), (unsigned)((n + net::TR - 1) / net::TR), (unsigned)nimg);
+  net::conv3x3_kernel<0><<<g, net::NTHR, 0, nt->ctx->stream>>>(in, n, n, (transposed ? nt->wt : nt->wf) + layer * 576,
+                                                               out, nullptr, 0.0, nullptr);
+}
+
+// forward pass over nimg images of n x n; meta (device, per image) or the scalars
+template <typename T>
+static void net_forward(STS_Net nt, int n, int nimg, const T* r, double scale, float sk, float sg, double out_scale,
+                        const float* meta)
+{
+  cudaStream_t st = nt->ctx->stream;
+  net::Level* L   = nt->L;
+  const long long ip = (long long)n * n, np = ip * nimg;
+  net::input_kernel_t<T><<<grid_for(np), 256, 0, st>>>(np, ip, r, scale, sk, sg, meta, L[0].x);
+  conv(nt, L[0].x, n, nimg, net::L_IN, false, L[0].a);                                           // a0
+  net::pool_kernel<<<grid_for(np / 4 * CH), 256, 0, st>>>(L[0].a, n * nimg, n, L[1].p);          // p0
+  conv(nt, L[1].p, n / 2, nimg, net::L_D1, false, L[1].a);                                       // a1
+  net::pool_kernel<<<grid_for(np / 16 * CH), 256, 0, st>>>(L[1].a, n / 2 * nimg, n / 2, L[2].p); // p1
+  conv(nt, L[2].p, n / 4, nimg, net::L_D2, false, L[2].a);                                       // a2
+  net::pool_kernel<<<grid_for(np / 64 * CH), 256, 0, st>>>(L[2].a, n / 4 * nimg, n / 4, L[3].p); // p2
+  conv(nt, L[3].p, n / 8, nimg, net::L_D3, false, L[3].c);                                       // c3
+  conv(nt, L[3].c, n / 8, nimg, net::L_C, false, L[3].a);                                        // a3
+  net::upadd_kernel<<<grid_for(np / 16 * CH), 256, 0, st>>>(L[3].a, L[2].a, n / 4 * nimg, n / 4, L[2].s); // s2
+  conv(nt, L[2].s, n / 4, nimg, net::L_U2, false, L[2].b);                                       // b2
+  net::upadd_kernel<<<grid_for(np / 4 * CH), 256, 0, st>>>(L[2].b, L[1].a, n / 2 * nimg, n / 2, L[1].s); // s1
+  conv(nt, L[1].s, n / 2, nimg, net::L_U1, false, L[1].b);                                       // b1
+  net::upadd_kernel<<<grid_for(np * CH), 256, 0, st>>>(L[1].b, L[0].a, n * nimg, n, L[0].s);      // s0
+  conv(nt, L[0].s, n, nimg, net::L_U0, false, L[0].b);                                           // b0
+  dim3 g((unsigned)((n + net::TC - 1) / net::TC), (unsigned)((n + net::TR - 1) / net::TR), (unsigned)nimg);
+  net::conv3x3_kernel<1><<<g, net::NTHR, 0, st>>>(L[0].b, n, n, nt->wf + net::L_OUT * 576, nullptr, nt->z, out_scale,
+                                                  meta);
+}
+
+static void wgrad(STS_Net nt, const __nv_bfloat16* x, const __nv_bfloat16* g, int n, int nimg, int layer)
+{
+  const long long tiles = (long long)((n + 15) / 16) * ((n + 15) / 16) * nimg;
+  const int grid        = (int)std::min<long long>(tiles, 2LL * nt->ctx->num_sms);
+  net::wgrad_kernel<<<grid, 256, 0, nt->ctx->stream>>>(x, g, n, n, nimg, nt->g + layer * WSZ);
+}
+
+// gradient of the loss w.r.t. the weights, accumulated into nt->g; needs the preceding
+// forward; the output gradient is (z - e) * gscale (times the image's out_scale / ||e||^2
+// when meta is given)
+static void net_backward(STS_Net nt, int n, int nimg, const float* e, double gscale, const float* meta)
+{
+  cudaStream_t st = nt->ctx->stream;
+  net::Level* L   = nt->L;
+  const long long ip = (long long)n * n, np = ip * nimg;
+  const int m = nimg;
+  net::gradz_kernel<<<grid_for(np), 256, 0, st>>>(np, ip, nt->z, e, gscale, meta, L[0].gt);     // g (channel 0)
+  wgrad(nt, L[0].b, L[0].gt, n, m, net::L_OUT);
+  conv(nt, L[0].gt, n, m, net::L_OUT, true, L[0].gb);                                          // gb0
+  wgrad(nt, L[0].s, L[0].gb, n, m, net::L_U0);
+  conv(nt, L[0].gb, n, m, net::L_U0, true, L[0].ga);                                           // gs0 = ga0
+  net::upT_kernel<<<grid_for(np / 4 * CH), 256, 0, st>>>(L[0].ga, n * m, n, L[1].gb, 0);        // gb1
+  wgrad(nt, L[1].s, L[1].gb, n / 2, m, net::L_U1);
+  conv(nt, L[1].gb, n / 2, m, net::L_U1, true, L[1].ga);                                       // gs1 = ga1
+  net::upT_kernel<<<grid_for(np / 16 * CH), 256, 0, st>>>(L[1].ga, n / 2 * m, n / 2, L[2].gb, 0); // gb2
+  wgrad(nt, L[2].s, L[2].gb, n / 4, m, net::L_U2);
+  conv(nt, L[2].gb, n / 4, m, net::L_U2, true, L[2].ga);                                       // gs2 = ga2
+  net::upT_kernel<<<grid_for(np / 64 * CH), 256, 0, st>>>(L[2].ga, n / 4 * m, n / 4, L[3].gb, 0); // ga3
+  wgrad(nt, L[3].c, L[3].gb, n / 8, m, net::L_C);
+  conv(nt, L[3].gb, n / 8, m, net::L_C, true, L[3].ga);                                        // gc3
+  wgrad(nt, L[3].p, L[3].ga, n / 8, m, net::L_D3);
+  conv(nt, L[3].ga, n / 8, m, net::L_D3, true, L[3].gt);                                       // gp2
+  net::poolT_add_kernel<<<grid_for(np / 16 * CH), 256, 0, st>>>(L[3].gt, n / 4 * m, n / 4, L[2].ga); // ga2 += pool^T
+  wgrad(nt, L[2].p, L[2].ga, n / 4, m, net::L_D2);
+  conv(nt, L[2].ga, n / 4, m, net::L_D2, true, L[2].gt);                                       // gp1
+  net::poolT_add_kernel<<<grid_for(np / 4 * CH), 256, 0, st>>>(L[2].gt, n / 2 * m, n / 2, L[1].ga); // ga1 += pool^T
+  wgrad(nt, L[1].p, L[1].ga, n / 2, m, net::L_D1);
+  conv(nt, L[1].ga, n / 2, m, net::L_D1, true, L[1].gt);                                       // gp0
+  net::poolT_add_kernel<<<grid_for(np * CH), 256, 0, st>>>(L[1].gt, n * m, n, L[0].ga);         // ga0 += pool^T
+  wgrad(nt, L[0].x, L[0].ga, n, m, net::L_IN);
+}
+
+static bool net_size_ok(STS_Net nt, int n)
+{
+  if (!nt || n < 16 || n % 16 != 0 || n > nt->nmax)
+  {
+    sts_set_error("STS_Net: size %d must be a multiple of 16 not above %d", n, nt ? nt->nmax : 0);
+    return false;
+  }
+  return true;
+}
+
+// z = M r for one n x n residual (device pointers): z = jacobi * net(scale r) / scale
+extern "C" int STS_NetApply(STS_Net nt, int n, const double* r, double* z, double sk, double sg, double jacobi,
+                            double scale)
+{
+  if (!net_size_ok(nt, n) || !r || !z || !(scale > 0.0)) return -1;
+  ctx_activate(nt->ctx);
+  net_forward<double>(nt, n, 1, r, scale, (float)sk, (float)sg, jacobi / scale, nullptr);
+  if (!STS_CUDA_OK(cudaMemcpyAsync(z, nt->z, (size_t)n * n * 8, cudaMemcpyDeviceToDevice, nt->ctx->stream))) return -1;
+  return STS_CUDA_OK(cudaGetLastError()) ? 0 : -1;
+}
+
+// one sample: loss = 0.5 ||M r - e||^2 / ||e||^2 and dloss/dW (FP32, host) — scale = 1
+extern "C" int STS_NetLossGrad(STS_Net nt, int n, const double* r, const float* e, double sk, double sg, double jacobi,
+                               double* loss, float* grad)
+{
+  if (!net_size_ok(nt, n) || !r || !e) return -1;
+  ctx_activate(nt->ctx);
+  cudaStream_t st = nt->ctx->stream;
+  const long long np = (long long)n * n;
+  // ||e||^2 on the host (test-sized inputs)
+  std::vector<float> eh(np);
+  if (!STS_CUDA_OK(cudaMemcpy(eh.data(), e, np * 4, cudaMemcpyDeviceToHost))) return -1;
+  double e2 = 0.0;
+  for (float v : eh) e2 += (double)v * v;
+  net_forward<double>(nt, n, 1, r, 1.0, (float)sk, (float)sg, jacobi, nullptr);
+  cudaMemsetAsync(nt->dacc, 0, 8, st);
+  net::sq_diff_kernel<<<grid_for(np), 256, 0, st>>>(np, np, nt->z, e, nullptr, nt->dacc);
+  double d2 = 0.0;
+  cudaMemcpyAsync(&d2, nt->dacc, 8, cudaMemcpyDeviceToHost, st);
+  cudaMemsetAsync(nt->g, 0, NLAYER * WSZ * 4, st);
+  net_backward(nt, n, 1, e, jacobi / e2, nullptr);
+  if (!STS_CUDA_OK(cudaStreamSynchronize(st))) return -1;
+  if (loss) *loss = 0.5 * d2 / e2;
+  if (grad && !STS_CUDA_OK(cudaMemcpy(grad, nt->g, NLAYER * WSZ * 4, cudaMemcpyDeviceToHost))) return -1;
+  return 0;
+}
+
+// Adam training on nsamples pairs (r_k, e_k) of n x n fields stored as FP32 on the device;
+// meta[5k..5k+4] = {sk, sg, jacobi, scale, 1/||e_k||^2}. Each epoch visits the samples in a
+// fresh shuffled order in minibatches of `batch` images (gathered into a staging buffer and
+// run as one batched forward/backward); loss = mean over the minibatch of
+// 0.5 ||M r_k - e_k||^2 / ||e_k||^2. Returns the mean loss of the last epoch.
+extern "C" int STS_NetTrain(STS_Net nt, int n, int nsamples, const float* r, const float* e, const float* meta,
+                            int epochs, int batch, float lr, unsigned long long seed, double* last_loss)
+{
+  if (!net_size_ok(nt, n) || nsamples < 1 || batch < 1 || epochs < 0 || !r || !e || !meta)
+  {
+    sts_set_error("STS_NetTrain: invalid arguments");
+    return -1;
+  }
+  ctx_activate(nt->ctx);
+  cudaStream_t st = nt->ctx->stream;
+  const long long ip = (long long)n * n;
+  batch = std::min(batch, nsamples);
+  if (!ensure_capacity(nt, ip * batch)) return -1;
+  cudaFree(nt->mb);
+  cudaFree(nt->idx);
+  nt->mb  = nullptr;
+  nt->idx = nullptr;
+  bool ok = true;
+  nt->mb  = (float*)dalloc((size_t)META * batch * 4, &ok);
+  nt->idx = (int*)dalloc((size_t)nsamples * 4, &ok);
+  if (!ok) return -1;
+  std::vector<int> order(nsamples);
+  for (int k = 0; k < nsamples; ++k) order[k] = k;
+  std::mt19937_64 rng(seed);
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  double epoch_loss = 0.0;
+  for (int ep = 0; ep < epochs; ++ep)
+  {
+    std::shuffle(order.begin(), order.end(), rng);
+    cudaMemcpyAsync(nt->idx, order.data(), nsamples * 4, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(nt->dacc, 0, 8, st);
+    int nbatches = 0;
+    for (int s0 = 0; s0 + batch <= nsamples; s0 += batch) // whole minibatches only
+    {
+      const long long len = ip;
+      net::gather_kernel<<<grid_for(len * batch), 256, 0, st>>>(r, e, meta, nt->idx + s0, batch, len, nt->rb, nt->eb,
+                                                                nt->mb);
+      cudaMemsetAsync(nt->g, 0, NLAYER * WSZ * 4, st);
+      net_forward<float>(nt, n, batch, nt->rb, 1.0, 0.f, 0.f, 1.0, nt->mb);
+      net::sq_diff_kernel<<<grid_for(ip * batch), 256, 0, st>>>(ip * batch, ip, nt->z, nt->eb, nt->mb, nt->dacc);
+      net_backward(nt, n, batch, nt->eb, 1.0 / batch, nt->mb);
+      nt->adam_t++;
+      const float bc1 = 1.f - powf(b1, (float)nt->adam_t), bc2 = 1.f - powf(b2, (float)nt->adam_t);
+      net::adam_kernel<<<(NLAYER * WSZ + 255) / 256, 256, 0, st>>>(NLAYER * WSZ, nt->w, nt->m, nt->v, nt->g, nt->mask, lr,
+                                                                 b1, b2, eps, bc1, bc2, 1.f);
+      refresh_frags(nt);
+      ++nbatches;
+    }
+    double d2 = 0.0;
+    cudaMemcpyAsync(&d2, nt->dacc, 8, cudaMemcpyDeviceToHost, st);
+    if (!STS_CUDA_OK(cudaStreamSynchronize(st))) return -1;
+    epoch_loss = 0.5 * d2 / ((double)nbatches * batch);
+  }
+  if (last_loss) *last_loss = epoch_loss;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// training data from PCG solves, and flexible CG with the network
+// ---------------------------------------------------------------------------------------
+#include <functional>
+
+int sts_pcg_run(STS_Problem p, double gamma, N_Vector b, N_Vector x, double tol, int maxit, int jacobi, int* iters,
+                double* relres, const std::function<void(int, const double*, const double*)>& batch_cb);
+
+namespace net {
+// dst (crop x crop FP32) = src (n-wide FP64) window at (x0, y0)
+__global__ void crop_kernel(const double* __restrict__ src, long long nx, int x0, int y0, int crop,
+                            float* __restrict__ dst)
+{
+  const long long n = (long long)crop * crop;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+  {
+    const int i = (int)(k % crop), j = (int)(k / crop);
+    dst[k] = (float)src[(long long)(y0 + j) * nx + (x0 + i)];
+  }
+}
+
+// e = x*_crop - e (e holds x_k crops while the solve runs)
+__global__ void corr_kernel(const double* __restrict__ xs, long long nx, int x0, int y0, int crop, float* __restrict__ e)
+{
+  const long long n = (long long)crop * crop;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+  {
+    const int i = (int)(k % crop), j = (int)(k / crop);
+    e[k] = (float)(xs[(long long)(y0 + j) * nx + (x0 + i)] - (double)e[k]);
+  }
+}
+
+// q = p - gamma A p (Dirichlet 5-point operator)
+__global__ void shifted_apply_kernel(ProbDev P, double gamma, const double* __restrict__ p, double* __restrict__ q)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long j = (long long)blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= P.nx || j >= P.ny) return;
+  const long long k = j * P.nx + i;
+  const double pc = p[k];
+  const double pw = (i > 0) ? p[k - 1] : 0.0, pe = (i < P.nx - 1) ? p[k + 1] : 0.0;
+  const double ps = (j > 0) ? p[k - P.nx] : 0.0, pn = (j < P.ny - 1) ? p[k + P.nx] : 0.0;
+  const double sx = pw + pe, sy = ps + pn;
+  double acc = P.cc * pc;
+  acc        = __fma_rn(P.cx, sx, acc);
+  acc        = __fma_rn(P.cy, sy, acc);
+  q[k]       = __fma_rn(-gamma, acc, pc);
+}
+
+// p = z + beta p ; x += alpha p style updates
+__global__ void axpby_kernel(long long n, double a, const double* __restrict__ xv, double b, double* __restrict__ y)
+{
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    y[k] = __fma_rn(a, xv[k], b * y[k]);
+}
+} // namespace net
+
+extern "C" int STS_HarvestPCGPairs(STS_Problem p, double gamma, N_Vector b, int ncrops, int crop, int every,
+                                   int max_pairs, float* r_out, float* e_out, unsigned long long seed, int* npairs,
+                                   int* iters)
+{
+  if (!p || !b || crop < 16 || crop > p->nx || crop > p->ny || ncrops < 1 || every < 1 || max_pairs < 1)
+  {
+    sts_set_error("STS_HarvestPCGPairs: invalid arguments");
+    return -1;
+  }
+  STS_Context ctx = p->ctx;
+  ctx_activate(ctx);
+  cudaStream_t st = ctx->stream;
+  N_Vector x      = N_VNew_Sts(NVL(b), ctx);
+  std::mt19937_64 rng(seed);
+  std::vector<int> cx(ncrops), cy(ncrops);
+  for (int c = 0; c < ncrops; ++c)
+  {
+    cx[c] = (int)(rng() % (unsigned long long)(p->nx - crop + 1));
+    cy[c] = (int)(rng() % (unsigned long long)(p->ny - crop + 1));
+  }
+  std::vector<int> pair_crop;
+  int batch_no      = 0;
+  const long long cs = (long long)crop * crop;
+  auto cb = [&](int, const double* xk, const double* rk) {
+    if ((batch_no++ % every) != 0) return;
+    for (int c = 0; c < ncrops && (int)pair_crop.size() < max_pairs; ++c)
+    {
+      const long long slot = (long long)pair_crop.size();
+      net::crop_kernel<<<grid_for(cs), 256, 0, st>>>(rk, p->nx, cx[c], cy[c], crop, r_out + slot * cs);
+      net::crop_kernel<<<grid_for(cs), 256, 0, st>>>(xk, p->nx, cx[c], cy[c], crop, e_out + slot * cs);
+      pair_crop.push_back(c);
+    }
+  };
+  int it = 0;
+  double rel;
+  int rc = sts_pcg_run(p, gamma, b, x, 1e-10, 1000000, 1, &it, &rel, cb);
+  for (size_t k = 0; k < pair_crop.size(); ++k)
+  {
+    const int c = pair_crop[k];
+    net::corr_kernel<<<grid_for(cs), 256, 0, st>>>(NVD(x), p->nx, cx[c], cy[c], crop, e_out + (long long)k * cs);
+  }
+  STS_CUDA_OK(cudaStreamSynchronize(st));
+  N_VDestroy_Sts(x);
+  if (npairs) *npairs = (int)pair_crop.size();
+  if (iters) *iters = it;
+  return rc < 0 ? rc : 0;
+}
+
+// Flexible CG (one-term A-orthogonalisation of the preconditioned residual, Notay 2000):
+// z_k = M r_k, p_k = z_k - (z_k . q_{k-1})/(p_{k-1} . q_{k-1}) p_{k-1}, q_k = (I - gamma A) p_k,
+// alpha = (p_k . r_k)/(p_k . q_k). Dots use the exact reductions; the stopping test uses the
+// updated FP64 residual and the returned relres is the true residual of the final x.
+extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b, N_Vector x, double tol, int maxit,
+                            int* iters, double* relres)
+{
+  if (!p || !nt || !b || !x || p->nx != p->ny || NVL(b) != p->nx * p->ny)
+  {
+    sts_set_error("STS_FCGSolve: invalid arguments (square grids, sizes a multiple of 16)");
+    return -1;
+  }
+  const int n = (int)p->nx;
+  if (!net_size_ok(nt, n)) return -1;
+  STS_Context ctx = p->ctx;
+  ctx_activate(ctx);
+  cudaStream_t st   = ctx->stream;
+  const long long N = NVL(b);
+  double *r, *z, *pv, *q, *pp, *qp;
+  cudaMallocAsync(&r, N * 8, st);
+  cudaMallocAsync(&z, N * 8, st);
+  cudaMallocAsync(&pv, N * 8, st);
+  cudaMallocAsync(&q, N * 8, st);
+  cudaMallocAsync(&pp, N * 8, st);
+  cudaMallocAsync(&qp, N * 8, st);
+  cudaMemsetAsync(NVD(x), 0, N * 8, st);
+  cudaMemcpyAsync(r, NVD(b), N * 8, cudaMemcpyDeviceToDevice, st);
+  const double jac = 1.0 / (1.0 - gamma * p->cc);
+  const double dx  = p->dx;
+  const double sk  = (std::log10(p->ky / p->kx) + 1.5) / 1.5;
+  const double sg  = std::log10(gamma / (dx * dx)) - 3.6;
+  dim3 bb(64, 4), gg((unsigned)((p->nx + 63) / 64), (unsigned)((p->ny + 3) / 4));
+  const double bnorm = sqrt(sts_dot_exact(ctx, NVD(b), NVD(b), N, SLOT_PCG0));
+  double rr = bnorm * bnorm, pq_prev = 0.0;
+  int it = 0, ret = 1;
+  if (!(bnorm > 0.0)) ret = 0;
+  for (it = 1; ret == 1 && it <= maxit; ++it)
+  {
+    const double scale = std::sqrt((double)N / rr);
+    STS_NetApply(nt, n, r, z, sk, sg, jac, scale);
+    if (it > 1)
+    {
+      const double zq  = sts_dot_exact(ctx, z, qp, N, SLOT_PCG1);
+      const double beta = -zq / pq_prev;
+      cudaMemcpyAsync(pv, z, N * 8, cudaMemcpyDeviceToDevice, st);
+      net::axpby_kernel<<<grid_for(N), 256, 0, st>>>(N, beta, pp, 1.0, pv); // p = z + beta p_prev
+    }
+    else cudaMemcpyAsync(pv, z, N * 8, cudaMemcpyDeviceToDevice, st);
+    net::shifted_apply_kernel<<<gg, bb, 0, st>>>(p->dev, gamma, pv, q);
+    const double pr    = sts_dot_exact(ctx, pv, r, N, SLOT_PCG1);
+    const double pq    = sts_dot_exact(ctx, pv, q, N, SLOT_PCG2);
+    const double alpha = pr / pq;
+    net::axpby_kernel<<<grid_for(N), 256, 0, st>>>(N, alpha, pv, 1.0, NVD(x));
+    net::axpby_kernel<<<grid_for(N), 256, 0, st>>>(N, -alpha, q, 1.0, r);
+    rr = sts_dot_exact(ctx, r, r, N, SLOT_PCG3);
+    if (!(rr == rr))
+    {
+      ret = -3;
+      break;
+    }
+    if (std::sqrt(rr) <= tol * bnorm)
+    {
+      ret = 0;
+      break;
+    }
+    std::swap(pv, pp);
+    std::swap(q, qp);
+    pq_prev = pq;
+  }
+  if (it > maxit) it = maxit;
+  // true residual of the final iterate
+  net::shifted_apply_kernel<<<gg, bb, 0, st>>>(p->dev, gamma, NVD(x), q);
+  net::axpby_kernel<<<grid_for(N), 256, 0, st>>>(N, 1.0, NVD(b), -1.0, q); // q = b - M x
+  const double tr = bnorm > 0.0 ? sqrt(sts_dot_exact(ctx, q, q, N, SLOT_PCG3)) / bnorm : 0.0;
+  cudaFreeAsync(r, st);
+  cudaFreeAsync(z, st);
+  cudaFreeAsync(pv, st);
+  cudaFreeAsync(q, st);
+  cudaFreeAsync(pp, st);
+  cudaFreeAsync(qp, st);
+  STS_CUDA_OK(cudaStreamSynchronize(st));
+  if (iters) *iters = it;
+  if (relres) *relres = tr;
+  return ret;
+}

@@ -263,6 +263,66 @@ int STS_ImplicitSolvePCG(STS_Problem p, double gamma, N_Vector b, N_Vector x, do
 int STS_SDIRK2Evolve(STS_Problem p, N_Vector y, double t0, double h, int nsteps, double tol,
                      int maxit, long long* total_iters);
 
+/* ------------------------------------------------------------------------------------
+ * Batched STS (new; the reference integrates one problem per run): many independent
+ * homogeneous-Dirichlet unforced heat problems, each with its own n x n grid and kx, ky,
+ * integrated from t = 0 to tf in one persistent launch with per-instance step control on
+ * the device (same method, controller and step rules as the single-problem integrator).
+ * States are concatenated in instance order, each row-major n x n.
+ * ----------------------------------------------------------------------------------*/
+typedef struct STS_Batch_* STS_Batch;
+STS_Batch STS_BatchCreate(STS_Context ctx, int ninst, const int* n, const double* kx,
+                          const double* ky);
+int STS_BatchFree(STS_Batch* b);
+long long STS_BatchTotalDOF(STS_Batch b);
+int STS_BatchSetState(STS_Batch b, const double* host_y);
+int STS_BatchGetState(STS_Batch b, double* host_y);
+/* nmodes sine modes per instance: arrays of ninst*nmodes (p, q integers, a amplitudes) */
+int STS_BatchSetInitialModes(STS_Batch b, int nmodes, const int* p, const int* q,
+                             const double* a);
+int STS_BatchEvolve(STS_Batch b, double tf, int method, double rtol, double atol, int smax,
+                    int controller, long long maxsteps);
+double STS_BatchLastMilliseconds(STS_Batch b);
+int STS_BatchGetInstanceStats(STS_Batch b, int inst, STS_Stats* stats);
+/* launch shape: threads per CTA (256 or 512) and CTAs per SM */
+int STS_BatchSetLaunch(STS_Batch b, int threads, int ctas_per_sm);
+/* autotuner: time every launch shape on the probe horizon [0, tf_probe], keep the fastest */
+int STS_BatchAutotune(STS_Batch b, double tf_probe, int method, double rtol, double atol,
+                      int smax, int* threads, int* ctas_per_sm, double* ms_best);
+
+/* ------------------------------------------------------------------------------------
+ * Learned multilevel preconditioner (new; the reference's alternative to Jacobi is hypre
+ * PFMG, diffusion_2D/preconditioner_hypre.cpp). A linear 4-level convolutional network
+ * (16 channels, 3x3 kernels, BF16 weights, FP32 accumulation, tensor-core implicit GEMM)
+ * maps a residual r to a correction z ~ (I - gamma A)^{-1} r; sk = normalised log10(ky),
+ * sg = normalised log10(gamma/dx^2) enter as channels r*sk, r*sg. Sizes: multiples of 16.
+ * ----------------------------------------------------------------------------------*/
+typedef struct STS_Net_* STS_Net;
+STS_Net STS_NetCreate(STS_Context ctx, int nmax, unsigned long long seed);
+int STS_NetFree(STS_Net* net);
+/* weights: 9 layers (W_in, W_d1, W_d2, W_d3, W_c, W_u2, W_u1, W_u0, W_out) x [16][16][3][3] FP32 */
+int STS_NetSetWeights(STS_Net net, const float* w);
+int STS_NetGetWeights(STS_Net net, float* w);
+/* z = jacobi * net(scale * r) / scale on device arrays of n x n doubles */
+int STS_NetApply(STS_Net net, int n, const double* r, double* z, double sk, double sg, double jacobi,
+                 double scale);
+/* one sample: loss = 0.5 ||M r - e||^2 / ||e||^2 and its weight gradient (host FP32 array) */
+int STS_NetLossGrad(STS_Net net, int n, const double* r, const float* e, double sk, double sg,
+                    double jacobi, double* loss, float* grad);
+/* Adam over device samples r, e (nsamples x n x n FP32) with per-sample
+ * meta = {sk, sg, jacobi, scale, 1/||e||^2}, minibatches of `batch` samples run batched */
+int STS_NetTrain(STS_Net net, int n, int nsamples, const float* r, const float* e, const float* meta,
+                 int epochs, int batch, float lr, unsigned long long seed, double* last_loss);
+/* residual/correction pairs from a converged fused Jacobi-PCG solve of (I - gamma A) x = b:
+ * every `every` iterations, `ncrops` crops (crop x crop, fixed positions) of r_k and of
+ * e_k = x* - x_k are appended to r_out / e_out (device FP32, capacity max_pairs) */
+int STS_HarvestPCGPairs(STS_Problem p, double gamma, N_Vector b, int ncrops, int crop, int every,
+                        int max_pairs, float* r_out, float* e_out, unsigned long long seed,
+                        int* npairs, int* iters);
+/* flexible CG with the network as preconditioner, x0 = 0, stop at ||r|| <= tol ||b|| */
+int STS_FCGSolve(STS_Problem p, double gamma, STS_Net net, N_Vector b, N_Vector x, double tol,
+                 int maxit, int* iters, double* relres);
+
 #ifdef __cplusplus
 }
 #endif

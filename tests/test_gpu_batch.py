@@ -1,0 +1,55 @@
+"""Batched persistent STS launch against the CPU oracle, instance by instance.
+
+Each instance is integrated by the oracle's single-problem integrator with the same method,
+tolerances and step rules; the device controller uses CUDA's pow (the host uses the C
+library's), so the comparison allows last-bit differences in h to propagate (1e-9)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(stslib, count=20, seed=7):
+    return stslib.make_batch_instances(count=count, seed=seed, sizes=(16, 24, 32, 48, 40),
+                                       nmodes=4, pmax=6)
+
+
+def test_batch_matches_oracle_per_instance(ctx, stslib, oracle):
+    inst = small_batch(stslib)
+    B = stslib.Batch(ctx, inst)
+    B.evolve(0.01, method=stslib.RKL, rtol=1e-6, atol=1e-10)
+    y = B.state()
+    for i, (n, kx, ky, p, q, a) in enumerate(inst):
+        P = oracle.Problem(oracle.UNFORCED, n, n, kx=kx, ky=ky)
+        J = oracle.Integrator(P, P.initial_modes(p, q, a), method=oracle.RKL, rtol=1e-6, atol=1e-10)
+        assert J.evolve(0.01) == 0
+        yi = B.instance_state(y, i)
+        rel = np.linalg.norm(yi - J.y) / np.linalg.norm(J.y)
+        st, so = B.stats(i), J.stats()
+        assert st["t"] == 0.01
+        assert abs(st["nst"] - so["nst"]) <= max(1, so["nst"] // 100), (i, st["nst"], so["nst"])
+        assert rel < 1e-9, (i, rel)
+
+
+def test_batch_launch_shapes_agree_bitwise(ctx, stslib):
+    inst = small_batch(stslib, count=12, seed=3)
+    outs = []
+    for threads, cps in ((256, 1), (256, 2), (512, 1)):
+        B = stslib.Batch(ctx, inst)
+        assert B.set_launch(threads, cps) == 0
+        B.evolve(0.005, method=stslib.RKC, rtol=1e-6, atol=1e-10)
+        outs.append(B.state())
+    for o in outs[1:]:
+        assert np.array_equal(outs[0], o)
+
+
+def test_batch_autotune_keeps_results(ctx, stslib):
+    inst = small_batch(stslib, count=10, seed=5)
+    B = stslib.Batch(ctx, inst)
+    th, cp, ms = B.autotune(0.001)
+    assert th in (256, 512) and cp in (1, 2) and ms > 0
+    B.evolve(0.005)
+    C = stslib.Batch(ctx, inst)
+    C.set_launch(th, cp)
+    C.evolve(0.005)
+    assert np.array_equal(B.state(), C.state())

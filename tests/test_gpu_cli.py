@@ -1,0 +1,84 @@
+"""The command-line driver: reference flags (diffusion_2D/main.cpp:556-687,
+diffusion_2D.cpp:42-163) and the stdout labels diffusion_2D/runtests-diffusion2d.py:36-54
+parses, run on the GPU."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+EXE = os.path.join(ROOT, "ceda_demonstrations_gb300", "_build", "diffusion_2D_gpu")
+
+
+def parse_like_runtests(stdout):
+    """The parsing rules of runtests-diffusion2d.py:36-54, restated."""
+    stats = {"Steps": None, "Fails": None, "Accuracy": None, "FEvals": 0, "Runtime": None}
+    for line in stdout.split("\n"):
+        txt = line.split()
+        if "Steps" in txt:
+            stats["Steps"] = int(txt[2])
+        elif ("Error" in txt) and ("test" in txt):
+            stats["Fails"] = int(txt[4])
+        elif ("Maximum" in txt) and ("relative" in txt):
+            stats["Accuracy"] = float(txt[4])
+        elif ("RHS" in txt) and ("fn" in txt):
+            stats["FEvals"] += int(txt[4])
+        elif "simulation" in txt:
+            stats["Runtime"] = float(txt[4])
+    return stats
+
+
+def run(args, cwd=None):
+    r = subprocess.run([EXE] + args, capture_output=True, text=True, cwd=cwd, timeout=600)
+    return r.returncode, r.stdout, r.stderr
+
+
+def test_cli_manufactured_rkc_with_error_mode(stslib, oracle):
+    stslib.lib()
+    rc, out, err = run(["--problem", "manufactured", "--nx", "64", "--ny", "48", "--integrator", "rkc",
+                        "--rtol", "1e-6", "--atol", "1e-10", "--tf", "0.05", "--nout", "5", "--error",
+                        "--controller", "2", "--maxsteps", "10000"])
+    assert rc == 0, err
+    st = parse_like_runtests(out)
+    assert st["Steps"] > 0 and st["Fails"] >= 0 and st["FEvals"] > 0 and st["Runtime"] > 0
+    assert 0 < st["Accuracy"] < 1e-3
+    # the same run on the oracle (same outputs times, same controller)
+    P = oracle.Problem(oracle.MANUFACTURED, 64, 48)
+    J = oracle.Integrator(P, P.initial(), method=oracle.RKC, rtol=1e-6, atol=1e-10, controller=2)
+    for k in range(1, 6):
+        assert J.evolve(0.05 * k / 5) == 0
+    assert st["Steps"] == J.stats()["nst"]
+    ex = P.exact(0.05)
+    rel = np.linalg.norm(J.y - ex) / np.linalg.norm(ex)
+    line = [l for l in out.split("\n") if l.startswith("Relative L2 error vs exact")][0]
+    assert abs(float(line.split("=")[1]) - rel) <= 1e-12 * rel
+
+
+def test_cli_reference_mode_and_solution_file(stslib, tmp_path):
+    stslib.lib()
+    rc, out, err = run(["--nx", "40", "--ny", "32", "--integrator", "rkl", "--inhomogeneous",
+                        "--internaleig", "--tf", "0.2", "--nout", "4", "--output", "2"], cwd=str(tmp_path))
+    assert rc == 0, err
+    st = parse_like_runtests(out)
+    assert st["Steps"] > 0 and st["FEvals"] > 0
+    f = tmp_path / "diffusion_2d_solution.00000.txt"
+    lines = f.read_text().strip().split("\n")
+    header = [l for l in lines if l.startswith("#")]
+    rows = [l for l in lines if not l.startswith("#")]
+    assert header[0] == "# title Diffusion 2D" and "# nx  40" in header
+    assert len(rows) == 5 and all(len(r.split()) == 1 + 40 * 32 for r in rows)
+    assert np.isfinite(np.array(rows[-1].split(), dtype=float)).all()
+
+
+def test_cli_dirk_and_errors(stslib):
+    stslib.lib()
+    rc, out, err = run(["--problem", "manufactured", "--nx", "32", "--ny", "32", "--integrator", "dirk",
+                        "--fixedstep", "1e-3", "--tf", "0.01", "--nout", "2"])
+    assert rc == 0, err
+    assert parse_like_runtests(out)["Steps"] == 10
+    rc, out, err = run(["--bogus"])
+    assert rc == 1 and "Unknown inputs" in err
+    rc, out, err = run(["--integrator", "erk"])
+    assert rc == 1

@@ -1,0 +1,176 @@
+"""Learned multilevel preconditioner: GPU forward/backward kernels against the FP64 CPU
+reference (oracle/convnet.py), batched training, and flexible CG with the trained network
+against Jacobi-PCG on the same shifted systems (I - gamma A) x = b.
+
+Tolerances: the GPU keeps weights and activations in BF16 (8-bit mantissa, relative
+rounding 2^-9 per stored value) with FP32 accumulation, the reference computes in FP64 from
+the same BF16 weights; nine stored layers give a few 1e-3 relative error, so the forward
+output is held to 3e-2 relative L2 and each layer's weight gradient to 6e-2.
+"""
+import numpy as np
+import pytest
+
+import ceda_demonstrations_gb300 as sts
+from oracle import convnet
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+FWD_TOL = 3e-2
+GRAD_TOL = 6e-2
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
+
+
+def _f32_dev(a):
+    t = torch.as_tensor(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+    torch.cuda.synchronize()
+    return t
+
+
+def _smooth_field(n, rng, nbumps=24):
+    """A seeded random smooth field: Gaussian bumps with random centres, widths in
+    [0.03, 0.15] and N(0, 1) amplitudes on the interior grid x_i = (i + 1) / (n + 1)."""
+    x = (np.arange(n) + 1.0) / (n + 1)
+    X, Y = np.meshgrid(x, x)
+    f = np.zeros((n, n))
+    for _ in range(nbumps):
+        cx, cy = rng.uniform(0.1, 0.9, 2)
+        w = rng.uniform(0.03, 0.15)
+        f += rng.standard_normal() * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * w * w))
+    return f
+
+
+@pytest.fixture(scope="module")
+def weights():
+    return convnet.init_weights(seed=3)
+
+
+@pytest.mark.parametrize("n,sk,sg", [(64, 0.3, -0.5), (128, -1.0, 0.8)])
+def test_forward_matches_oracle(ctx, weights, n, sk, sg):
+    rng = np.random.default_rng(n)
+    r = rng.standard_normal((n, n))
+    jac = 0.37
+    net = sts.Net(ctx, 128, seed=0)
+    net.set_weights(weights)
+    rv = sts.NVector.from_numpy(ctx, r)
+    zv = sts.NVector(ctx, n * n)
+    net.apply(n, rv.ptr, zv.ptr, sk, sg, jac, 1.0)
+    z = zv.numpy().reshape(n, n)
+    zref, _ = convnet.forward(weights, r, sk, sg, jac)
+    assert _rel(z, zref) < FWD_TOL
+    # power-of-two input scaling commutes with every BF16 rounding: bitwise identical output
+    net.apply(n, rv.ptr, zv.ptr, sk, sg, jac, 4.0)
+    assert np.array_equal(zv.numpy().reshape(n, n), z)
+
+
+def test_weights_round_trip(ctx, weights):
+    net = sts.Net(ctx, 64, seed=1)
+    net.set_weights(weights)
+    got = net.weights()
+    for nm in convnet.NAMES:
+        co, ci = convnet.shape(nm)[:2]
+        assert np.array_equal(got[nm][:co, :ci], weights[nm])
+        assert not np.any(got[nm][co:]) and not np.any(got[nm][:, ci:])
+
+
+def test_gradients_match_oracle(ctx, weights):
+    n = 64
+    rng = np.random.default_rng(11)
+    r = rng.standard_normal((n, n))
+    e = rng.standard_normal((n, n)).astype(np.float32)
+    sk, sg, jac = 0.4, -0.2, 0.5
+    net = sts.Net(ctx, n, seed=0)
+    net.set_weights(weights)
+    rv = sts.NVector.from_numpy(ctx, r)
+    et = _f32_dev(e)
+    loss, grad = net.loss_grad(n, rv.ptr, et.data_ptr(), sk, sg, jac)
+    lref, gref = convnet.loss_and_grad(weights, r, e.astype(np.float64), sk, sg, jac)
+    assert abs(loss - lref) / lref < FWD_TOL
+    for nm in convnet.NAMES:
+        co, ci = convnet.shape(nm)[:2]
+        assert _rel(grad[nm][:co, :ci], gref[nm]) < GRAD_TOL, nm
+        # padded channels stay exactly zero
+        assert not np.any(grad[nm][co:]) and not np.any(grad[nm][:, ci:])
+
+
+def _harvest(ctx, n, ky, gam_rel, crop, ncrops, every, max_pairs, seed):
+    p = sts.Problem(ctx, sts.UNFORCED, n, n, 1.0, ky)
+    dx = 1.0 / (n + 1)
+    gamma = gam_rel * dx * dx
+    b = sts.NVector.from_numpy(ctx, _smooth_field(n, np.random.default_rng(seed)))
+    r_t = torch.empty(max_pairs * crop * crop, dtype=torch.float32, device="cuda")
+    e_t = torch.empty_like(r_t)
+    torch.cuda.synchronize()
+    npairs, iters = sts.harvest_pcg_pairs(p, gamma, b, ncrops, crop, every, max_pairs,
+                                          r_t.data_ptr(), e_t.data_ptr(), seed)
+    r_t = r_t[:npairs * crop * crop].view(npairs, -1)
+    e_t = e_t[:npairs * crop * crop].view(npairs, -1)
+    sk, sg, jac = sts.net_features(1.0, ky, gamma, dx)
+    meta = torch.empty(npairs, 5, dtype=torch.float32, device="cuda")
+    meta[:, 0] = sk
+    meta[:, 1] = sg
+    meta[:, 2] = jac
+    meta[:, 3] = torch.rsqrt((r_t.double() ** 2).mean(1)).float()
+    meta[:, 4] = (1.0 / (e_t.double() ** 2).sum(1)).float()
+    torch.cuda.synchronize()
+    return p, b, gamma, r_t, e_t, meta, iters
+
+
+def test_harvest_pairs_satisfy_the_system(ctx):
+    """Away from the crop edges, (I - gamma A) e_k = r_k holds for every harvested pair."""
+    n, crop = 128, 64
+    p, b, gamma, r_t, e_t, meta, iters = _harvest(ctx, n, 0.3, 300.0, crop, 2, 2, 16, 5)
+    assert r_t.shape[0] == 16 and iters > 16
+    dx = 1.0 / (n + 1)
+    cx, cy = 1.0 / dx ** 2, 0.3 / dx ** 2
+    for k in range(4):
+        e = e_t[k].double().cpu().numpy().reshape(crop, crop)
+        r = r_t[k].double().cpu().numpy().reshape(crop, crop)
+        lap = cx * (e[1:-1, :-2] + e[1:-1, 2:]) + cy * (e[:-2, 1:-1] + e[2:, 1:-1]) \
+            - 2 * (cx + cy) * e[1:-1, 1:-1]
+        res = e[1:-1, 1:-1] - gamma * lap
+        # e is stored in FP32: its rounding, amplified by gamma * 4 / dx^2, bounds the error
+        scale = np.abs(e).max() * (1 + 4 * gamma * (cx + cy))
+        assert np.abs(res - r[1:-1, 1:-1]).max() < 1e-5 * scale
+
+
+def test_trained_network_cuts_fcg_iterations(ctx):
+    """Train on pairs harvested from Jacobi-PCG solves of three systems, then solve a fourth
+    (unseen right-hand side) with FCG + network and with Jacobi-PCG to the same 1e-8 residual."""
+    n, crop = 256, 64
+    rs, es, ms = [], [], []
+    for k, (ky, grel) in enumerate([(1.0, 2000.0), (0.1, 800.0), (0.01, 3000.0)]):
+        _, _, _, r_t, e_t, meta, _ = _harvest(ctx, n, ky, grel, crop, 8, 4, 512, 100 + k)
+        rs.append(r_t)
+        es.append(e_t)
+        ms.append(meta)
+    r_all = torch.cat(rs).contiguous()
+    e_all = torch.cat(es).contiguous()
+    m_all = torch.cat(ms).contiguous()
+    torch.cuda.synchronize()
+    net = sts.Net(ctx, n, seed=7)
+    npairs = r_all.shape[0]
+    loss0 = net.train(crop, npairs, r_all.data_ptr(), e_all.data_ptr(), m_all.data_ptr(),
+                      epochs=1, batch=16, lr=0.0, seed=1)
+    loss = net.train(crop, npairs, r_all.data_ptr(), e_all.data_ptr(), m_all.data_ptr(),
+                     epochs=30, batch=16, lr=2e-3, seed=2)
+    assert loss < 0.5 * loss0
+
+    ky, grel = 0.3, 1500.0
+    p = sts.Problem(ctx, sts.UNFORCED, n, n, 1.0, ky)
+    dx = 1.0 / (n + 1)
+    gamma = grel * dx * dx
+    b = sts.NVector.from_numpy(ctx, _smooth_field(n, np.random.default_rng(999)))
+    x_pcg = p.vector()
+    it_pcg, rel_pcg, rc = sts.implicit_solve_pcg(p, gamma, b, x_pcg, tol=1e-8)
+    assert rc == 0 and rel_pcg <= 1e-8
+    x_fcg = p.vector()
+    it_fcg, rel_fcg, rc = sts.fcg_solve(p, gamma, net, b, x_fcg, tol=1e-8, maxit=2000)
+    assert rc == 0
+    assert rel_fcg <= 2e-8  # true FP64 residual of the returned iterate
+    assert _rel(x_fcg.numpy(), x_pcg.numpy()) < 1e-6
+    assert it_fcg < 0.5 * it_pcg, (it_fcg, it_pcg)
