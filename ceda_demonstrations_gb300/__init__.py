@@ -23,7 +23,7 @@ from . import build as _build
 
 __all__ = ["lib", "Context", "NVector", "Problem", "LSRKStep", "PCGSolver", "implicit_solve_pcg",
            "sdirk2_evolve", "RKC", "RKL", "PID", "PI", "I", "MANUFACTURED", "UNFORCED", "PERIODIC",
-           "Net", "fcg_solve", "harvest_pcg_pairs", "net_features", "STSError"]
+           "Net", "fcg_solve", "harvest_pcg_pairs", "net_features", "smooth_field", "STSError"]
 
 RKC, RKL = 0, 1
 PID, PI, I = 0, 1, 2
@@ -644,10 +644,29 @@ class Batch:
             _err("STS_BatchEvolve returned %d" % rc)
         return lib().STS_BatchLastMilliseconds(self.h)
 
-    def autotune(self, tf_probe, method=RKL, rtol=1e-6, atol=1e-10, smax=200):
+    def autotune(self, tf_probe, method=RKL, rtol=1e-6, atol=1e-10, smax=200, cache_file=None):
+        """Pick the launch shape (threads per instance CTA, CTAs per SM) by timing a short
+        probe evolve of each candidate; with `cache_file`, a JSON map from the workload
+        signature to the chosen shape is read first and updated after tuning."""
+        import json
+        key = "n%d_dof%d_m%d_rtol%g_atol%g_smax%d" % (len(self.instances), self.total, method, rtol,
+                                                     atol, smax)
+        cache = {}
+        if cache_file and os.path.exists(cache_file):
+            with open(cache_file) as f:
+                cache = json.load(f)
+            if key in cache:
+                th, cp = cache[key]["threads"], cache[key]["ctas_per_sm"]
+                self.set_launch(th, cp)
+                return th, cp, cache[key]["probe_ms"]
         th, cp, ms = C.c_int(), C.c_int(), C.c_double()
-        lib().STS_BatchAutotune(self.h, tf_probe, method, rtol, atol, smax, C.byref(th), C.byref(cp),
-                                C.byref(ms))
+        if lib().STS_BatchAutotune(self.h, tf_probe, method, rtol, atol, smax, C.byref(th),
+                                   C.byref(cp), C.byref(ms)) != 0:
+            _err("STS_BatchAutotune")
+        if cache_file:
+            cache[key] = {"threads": th.value, "ctas_per_sm": cp.value, "probe_ms": ms.value}
+            with open(cache_file, "w") as f:
+                json.dump(cache, f, indent=1, sort_keys=True)
         return th.value, cp.value, ms.value
 
     def set_launch(self, threads, ctas_per_sm):
@@ -691,6 +710,20 @@ class Batch:
 # ---------------------------------------------------------------------------------------
 NET_LAYERS = ["W_in", "W_d1", "W_d2", "W_d3", "W_c", "W_u2", "W_u1", "W_u0", "W_out"]
 NET_WSZ = 16 * 16 * 9
+
+
+def smooth_field(n, rng, nbumps=24):
+    """A seeded random smooth field on the interior grid x_i = (i + 1) / (n + 1): a sum of
+    Gaussian bumps with centres uniform in (0.1, 0.9)^2, widths uniform in [0.03, 0.15]
+    and N(0, 1) amplitudes (separable, built as outer products)."""
+    x = (np.arange(n) + 1.0) / (n + 1)
+    f = np.zeros((n, n))
+    for _ in range(nbumps):
+        cx, cy = rng.uniform(0.1, 0.9, 2)
+        w = rng.uniform(0.03, 0.15)
+        a = rng.standard_normal()
+        f += a * np.outer(np.exp(-(x - cy) ** 2 / (2 * w * w)), np.exp(-(x - cx) ** 2 / (2 * w * w)))
+    return f
 
 
 def net_features(kx, ky, gamma, dx):
@@ -781,7 +814,8 @@ def harvest_pcg_pairs(problem, gamma, b, ncrops, crop, every, max_pairs, r_ptr, 
 
 def fcg_solve(problem, gamma, net, b, x, tol=1e-8, maxit=10000):
     """Flexible CG on (I - gamma A) x = b with the network as preconditioner; returns
-    (iterations, true relative residual, status)."""
+    (iterations, true relative residual, status): status 0 converged, 2 converged through
+    the Jacobi-PCG fallback (after FCG stagnated or broke down), 1 not converged."""
     it, rel = C.c_int(), C.c_double()
     rc = lib().STS_FCGSolve(problem.h, gamma, net.h, b.h, x.h, tol, maxit, C.byref(it),
                             C.byref(rel))

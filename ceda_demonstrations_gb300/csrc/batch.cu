@@ -727,7 +727,7 @@ extern "C" int STS_BatchAutotune(STS_Batch b, double tf_probe, int method, doubl
   {
     b->block       = sh[0];
     b->ctas_per_sm = sh[1];
-    const int rc   = STS_BatchEvolve(b, tf_probe, method, rtol, atol, smax, 2, 0);
+    const int rc   = STS_BatchEvolve(b, tf_probe, method, rtol, atol, smax, 0, 0); // PID, as evolve
     cudaMemcpyAsync(b->y, save, b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->ctx->stream);
     if (rc == 0 && b->last_ms < best)
     {

@@ -19,6 +19,7 @@
 #include <functional>
 
 #include "kernels.cuh"
+#include "krylov.cuh"
 #include "sts_internal.cuh"
 
 struct PcgScal {
@@ -50,77 +51,6 @@ struct PcgWork {
 
 static constexpr int PCG_BATCH = 8; // iterations per graph launch (even: p ping-pong)
 
-// block combine of up to two exact accumulators into s->limbs, last block runs `fin`
-template <int NT, int NACC, typename Fin>
-__device__ __forceinline__ void pcg_block_finish(xsum::Limbs* a, unsigned* fl, PcgScal* s, Fin fin)
-{
-  __shared__ long long sm[NT / 32][NACC][xsum::NL];
-  __shared__ unsigned sflags[NACC];
-  __shared__ bool last;
-  const int tid  = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-  const int lane = tid & 31, warp = tid >> 5;
-  if (tid < NACC) sflags[tid] = 0;
-#pragma unroll
-  for (int c = 0; c < NACC; ++c)
-#pragma unroll
-    for (int k = 0; k < xsum::NL; ++k)
-    {
-      long long v = a[c].l[k];
-#pragma unroll
-      for (int m = 16; m >= 1; m >>= 1) v += shfl_xor_ll(v, m);
-      if (lane == 0) sm[warp][c][k] = v;
-    }
-  __syncthreads();
-#pragma unroll
-  for (int c = 0; c < NACC; ++c)
-    if (fl[c]) atomicOr(&sflags[c], fl[c]);
-  if (warp == 0)
-  {
-#pragma unroll
-    for (int c = 0; c < NACC; ++c)
-#pragma unroll
-      for (int k = 0; k < xsum::NL; ++k)
-      {
-        long long v = (lane < NT / 32) ? sm[lane][c][k] : 0LL;
-#pragma unroll
-        for (int m = 16; m >= 1; m >>= 1) v += shfl_xor_ll(v, m);
-        if (lane == 0 && v != 0) atomicAdd(&s->limbs[c][k], (unsigned long long)v);
-      }
-  }
-  __syncthreads();
-  if (tid == 0)
-  {
-#pragma unroll
-    for (int c = 0; c < NACC; ++c)
-      if (sflags[c]) atomicOr(&s->flags[c], sflags[c]);
-    __threadfence();
-    unsigned t = atomicAdd(&s->ticket, 1u);
-    last       = (t == gridDim.x * gridDim.y - 1);
-  }
-  __syncthreads();
-  if (last && tid == 0)
-  {
-    __threadfence();
-    double v[NACC];
-#pragma unroll
-    for (int c = 0; c < NACC; ++c)
-    {
-      long long tot[xsum::NL];
-#pragma unroll
-      for (int k = 0; k < xsum::NL; ++k)
-      {
-        tot[k]         = (long long)atomicAdd(&s->limbs[c][k], 0ULL);
-        s->limbs[c][k] = 0ULL;
-      }
-      v[c]        = xsum::finalize(tot, atomicOr(&s->flags[c], 0u));
-      s->flags[c] = 0u;
-    }
-    fin(v);
-    s->ticket = 0u;
-    __threadfence();
-  }
-}
-
 // initial scalars: rz = r.(D r) with r = b, bnorm via b.b
 __global__ void __launch_bounds__(256) pcg_init_kernel(long long n, const double* __restrict__ b,
                                                        PcgScal* s)
@@ -137,7 +67,7 @@ __global__ void __launch_bounds__(256) pcg_init_kernel(long long n, const double
     xsum::add(a[0], r * (D * r), fl[0]);
     xsum::add(a[1], r * r, fl[1]);
   }
-  pcg_block_finish<256, 2>(a, fl, s, [&](const double* v) {
+  krylov_block_finish<256, 2>(a, fl, s, [&](const double* v) {
     s->rz   = v[0];
     s->rr   = v[1];
     s->beta = 0.0;
@@ -183,7 +113,7 @@ __global__ void __launch_bounds__(256) pcg_q_kernel(ProbDev P, const double* __r
       q[k]            = qk;
       xsum::add(a[0], pc * qk, fl[0]);
     }
-  pcg_block_finish<256, 1>(a, fl, s, [&](const double* v) {
+  krylov_block_finish<256, 1>(a, fl, s, [&](const double* v) {
     s->pq    = v[0];
     s->alpha = s->rz / v[0];
   });
@@ -208,7 +138,7 @@ __global__ void __launch_bounds__(256) pcg_x_kernel(long long n, const double* _
     xsum::add(a[0], rk * rk, fl[0]);
     xsum::add(a[1], rk * (D * rk), fl[1]);
   }
-  pcg_block_finish<256, 2>(a, fl, s, [&](const double* v) {
+  krylov_block_finish<256, 2>(a, fl, s, [&](const double* v) {
     s->rr = v[0];
     s->iters += 1;
     if (sqrt(v[0]) <= s->tolb) s->state = 1;
@@ -336,8 +266,15 @@ int sts_pcg_run(STS_Problem p, double gamma, N_Vector b, N_Vector x, double tol,
     return -1;
   }
   cudaGraphDestroy(g);
-  for (;;)
+  // the device sets state 2 at maxit; the host bound on launches is a second guard
+  for (long long launches = 0;; ++launches)
   {
+    if (launches > maxit / PCG_BATCH + 2)
+    {
+      sts_set_error("STS_ImplicitSolvePCG: the device-side stop flag was not set");
+      ret = -1;
+      break;
+    }
     if (!STS_CUDA_OK(cudaGraphLaunch(w->graph[0], st)) || !STS_CUDA_OK(cudaStreamSynchronize(st)))
     {
       ret = -1;

@@ -31,17 +31,8 @@ def _f32_dev(a):
     return t
 
 
-def _smooth_field(n, rng, nbumps=24):
-    """A seeded random smooth field: Gaussian bumps with random centres, widths in
-    [0.03, 0.15] and N(0, 1) amplitudes on the interior grid x_i = (i + 1) / (n + 1)."""
-    x = (np.arange(n) + 1.0) / (n + 1)
-    X, Y = np.meshgrid(x, x)
-    f = np.zeros((n, n))
-    for _ in range(nbumps):
-        cx, cy = rng.uniform(0.1, 0.9, 2)
-        w = rng.uniform(0.03, 0.15)
-        f += rng.standard_normal() * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * w * w))
-    return f
+def _smooth_field(n, rng):
+    return sts.smooth_field(n, rng)
 
 
 @pytest.fixture(scope="module")
