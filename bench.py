@@ -181,7 +181,8 @@ def run_gpu(args):
     clock_samples = []
     for mixed in (True, False):
         I = sts.LSRKStep(ctx, G, 0.0, G.initial(), method=METHOD, rtol=RTOL, atol=ATOL,
-                         smax=SMAX, mixed=mixed, graphs=True, maxsteps=1000000)
+                         smax=SMAX, mixed=mixed, graphs=True, maxsteps=1000000,
+                         stage_kernel=args.stage_kernel if mixed else 0)
         y = G.vector()
         for _ in range(args.warmup):
             I.evolve(TF, y, sts.ONE_STEP)
@@ -559,6 +560,8 @@ def main():
     ap.add_argument("--both-methods", action="store_true")
     ap.add_argument("--both-rtols", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--stage-kernel", type=int, default=0,
+                    help="mixed stage kernel: 0 autotune, 1 register marching, 2+k TMA configuration k")
     ap.add_argument("--batch", action="store_true")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-tf", type=float, default=0.01)

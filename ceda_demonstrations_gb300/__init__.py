@@ -164,6 +164,8 @@ SIGNATURES = [
     ("STS_BatchSetLaunch", C.c_int, [_vp, C.c_int, C.c_int]),
     ("STS_BatchAutotune", C.c_int, [_vp, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int,
                                     _ip, _ip, _dp]),
+    ("STS_LSRKStepWriteCheckpoint", C.c_int, [_vp, C.c_char_p]),
+    ("STS_LSRKStepReadCheckpoint", C.c_int, [_vp, C.c_char_p]),
     ("STS_NetCreate", _vp, [_vp, C.c_int, C.c_ulonglong]),
     ("STS_NetFree", C.c_int, [C.POINTER(_vp)]),
     ("STS_NetSetWeights", C.c_int, [_vp, _fp]),
@@ -502,6 +504,14 @@ class LSRKStep:
         rc = lib().STS_ARKodeReset(self.mem, t, y.h)
         if rc != 0:
             _err("STS_ARKodeReset returned %d" % rc)
+
+    def write_checkpoint(self, path):
+        if lib().STS_LSRKStepWriteCheckpoint(self.mem, os.fsencode(path)) != 0:
+            _err("STS_LSRKStepWriteCheckpoint")
+
+    def read_checkpoint(self, path):
+        if lib().STS_LSRKStepReadCheckpoint(self.mem, os.fsencode(path)) != 0:
+            _err("STS_LSRKStepReadCheckpoint")
 
     def stage_kernel_info(self):
         v, ms = C.c_int(), C.c_double()

@@ -40,6 +40,8 @@ struct Opts {
   string ls = "cg";
   // output (UserOutput)
   int output = 1, nout = 20;
+  // binary checkpoint of the integrator state written at the end / read before the run
+  string checkpoint, restart;
 };
 
 static bool take(vector<string>& a, const string& key, string* val)
@@ -72,7 +74,9 @@ static void help()
           "\nDIRK solver command line options:\n"
           "  --order --nonlinear --ls <cg> --lsinfo --liniters --epslin --noprec --msbp\n"
           "\nOutput command line options:\n"
-          "  --output <level> (0 = none, 1 = stats, 2 = solution)  --nout <nout>\n";
+          "  --output <level> (0 = none, 1 = stats, 2 = solution)  --nout <nout>\n"
+          "  --checkpoint <file> : write the integrator state at the end of the run\n"
+          "  --restart <file>    : continue from a checkpoint written by --checkpoint\n";
 }
 
 static int parse(int argc, char** argv, Opts& o)
@@ -119,6 +123,8 @@ static int parse(int argc, char** argv, Opts& o)
   if (take(a, "--nographs", nullptr)) o.graphs = false;
   if (take(a, "--output", &v)) o.output = stoi(v);
   if (take(a, "--nout", &v)) o.nout = stoi(v);
+  if (take(a, "--checkpoint", &v)) o.checkpoint = v;
+  if (take(a, "--restart", &v)) o.restart = v;
   if (!a.empty())
   { // main.cpp:116-132
     cerr << "ERROR: Unknown inputs: ";
@@ -237,6 +243,28 @@ int main(int argc, char** argv)
     itask = STS_ONE_STEP;
   }
   double t = 0.0, dTout = o.tf / nout, tout = dTout, errtot = 0.0, simtime = 0.0;
+  if (!o.restart.empty())
+  {
+    if (!sts || STS_LSRKStepReadCheckpoint(mem, o.restart.c_str()) != 0)
+    {
+      cerr << "ERROR: cannot restart from " << o.restart << ": " << STS_GetLastError() << endl;
+      return 1;
+    }
+    STS_Stats st;
+    STS_ARKodeGetStats(mem, &st);
+    t = st.t;
+    while (tout <= t * (1.0 + 1e-14)) tout += dTout; // the next output time after the checkpoint
+    tout = (tout > o.tf) ? o.tf : tout;
+    if (o.error && ref)
+    { // the self-oracle restarts from the checkpointed state too
+      double t2 = 0.0;
+      STS_ARKodeSetStopTime(mem, t);
+      STS_ARKodeEvolve(mem, t, u, &t2, STS_NORMAL); // copies the restored y_n into u
+      STS_ARKodeSetStopTime(mem, o.tf);
+      N_VScale_Sts(1.0, u, uref);
+      STS_ARKodeReset(ref, t, uref);
+    }
+  }
   long long lin_iters = 0;
   FILE* sol = nullptr;
   cout << scientific << setprecision(numeric_limits<double>::digits10);
@@ -305,6 +333,11 @@ int main(int argc, char** argv)
     tout = (tout > o.tf) ? o.tf : tout;
   }
   if (sol) fclose(sol);
+  if (!o.checkpoint.empty() && sts && STS_LSRKStepWriteCheckpoint(mem, o.checkpoint.c_str()) != 0)
+  {
+    cerr << "ERROR: cannot write checkpoint " << o.checkpoint << ": " << STS_GetLastError() << endl;
+    return 1;
+  }
   if (o.output > 0) cout << " ----------------------------------------------\n\n";
   if (o.error) cout << "Maximum relative error = " << errtot << endl;
   cout << "Total simulation time = " << simtime << endl << endl;

@@ -1278,3 +1278,172 @@ void sts_f64_to_f32(STS_Context ctx, const double* a, float* b, long long n)
 {
   f64_to_f32_kernel<<<ew_blocks(ctx, n, 256 * 4), 256, 0, ctx->stream>>>(n, a, b);
 }
+
+// ---------------------------------------------------------------------------------------
+// checkpoint / restart: the complete integrator state (time, step-size history, controller
+// memory, eigenvalue refresh counter and estimate, statistics, y_n, the FSAL F_n and, for the
+// mixed path, its FP32 copy, and the power-iteration vector) in one binary file, so that a
+// restarted run continues with the same step sequence and the same bits.
+// Layout: CkptHeader, then y_n (n doubles), F_n (n doubles, if initialised), F_n FP32
+// (n floats, mixed fused path), eigenvector (n doubles, if has_evec). Native endianness.
+// ---------------------------------------------------------------------------------------
+struct CkptHeader {
+  char magic[8];
+  int version, method, mixed, fused_path;
+  long long n;
+  double t, hnext, hlast, rho, ep1, ep2;
+  long long ncf, nst, nst_att, netf, nfe, nfe_dee, ndee, nst_exp, stage_max, stages_total, nhist, steps_since_dee;
+  int initialized, after_fail, has_evec, last_s;
+};
+static const char CKPT_MAGIC[8] = {'S', 'T', 'S', 'C', 'K', 'P', 'T', '1'};
+
+static bool ckpt_io(FILE* f, void* host, const void* dev, void* dev_out, size_t bytes, bool write, cudaStream_t st)
+{
+  if (write)
+  {
+    if (!STS_CUDA_OK(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, st)) ||
+        !STS_CUDA_OK(cudaStreamSynchronize(st)))
+      return false;
+    return fwrite(host, 1, bytes, f) == bytes;
+  }
+  if (fread(host, 1, bytes, f) != bytes) return false;
+  return STS_CUDA_OK(cudaMemcpyAsync(dev_out, host, bytes, cudaMemcpyHostToDevice, st)) &&
+         STS_CUDA_OK(cudaStreamSynchronize(st));
+}
+
+extern "C" int STS_LSRKStepWriteCheckpoint(void* mem, const char* path)
+{
+  CHECK_MEM(mem);
+  LSRKMem* m = MEM(mem);
+  if (!path) return STS_ILL_INPUT;
+  ctx_activate(m->ctx);
+  cudaStream_t st = m->ctx->stream;
+  if (!STS_CUDA_OK(cudaStreamSynchronize(st))) return STS_ERR_FAILURE;
+  CkptHeader h;
+  memset(&h, 0, sizeof(h));
+  memcpy(h.magic, CKPT_MAGIC, 8);
+  h.version         = 1;
+  h.method          = m->method;
+  h.mixed           = m->mixed;
+  const bool fz     = fused(m) && m->yb[0] != nullptr;
+  h.fused_path      = fz;
+  h.n               = m->n;
+  h.t               = m->t;
+  h.hnext           = m->hnext;
+  h.hlast           = m->hlast;
+  h.rho             = m->rho;
+  h.ep1             = m->ep1;
+  h.ep2             = m->ep2;
+  h.ncf             = m->ncf;
+  h.nst             = m->nst;
+  h.nst_att         = m->nst_att;
+  h.netf            = m->netf;
+  h.nfe             = m->nfe;
+  h.nfe_dee         = m->nfe_dee;
+  h.ndee            = m->ndee;
+  h.nst_exp         = m->nst_exp;
+  h.stage_max       = m->stage_max;
+  h.stages_total    = m->stages_total;
+  h.nhist           = m->nhist;
+  h.steps_since_dee = m->steps_since_dee;
+  h.initialized     = m->initialized;
+  h.after_fail      = m->after_fail;
+  h.has_evec        = m->evec != nullptr;
+  h.last_s          = m->last_s;
+  FILE* f = fopen(path, "wb");
+  if (!f)
+  {
+    sts_set_error("STS_LSRKStepWriteCheckpoint: cannot open %s", path);
+    return STS_ILL_INPUT;
+  }
+  std::vector<char> host((size_t)m->n * sizeof(double));
+  bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
+  const double* y = fz ? m->yb[m->par] : NVD(m->g_y);
+  const double* F = fz ? m->Fb[m->par] : NVD(m->g_Fn);
+  ok = ok && ckpt_io(f, host.data(), y, nullptr, m->n * sizeof(double), true, st);
+  if (m->initialized) ok = ok && ckpt_io(f, host.data(), F, nullptr, m->n * sizeof(double), true, st);
+  if (m->initialized && fz && m->mixed)
+    ok = ok && ckpt_io(f, host.data(), m->Ffb[m->par], nullptr, m->n * sizeof(float), true, st);
+  if (h.has_evec) ok = ok && ckpt_io(f, host.data(), m->evec, nullptr, m->n * sizeof(double), true, st);
+  ok = (fclose(f) == 0) && ok;
+  if (!ok) sts_set_error("STS_LSRKStepWriteCheckpoint: write to %s failed", path);
+  return ok ? STS_SUCCESS : STS_ERR_FAILURE;
+}
+
+extern "C" int STS_LSRKStepReadCheckpoint(void* mem, const char* path)
+{
+  CHECK_MEM(mem);
+  LSRKMem* m = MEM(mem);
+  if (!path) return STS_ILL_INPUT;
+  ctx_activate(m->ctx);
+  cudaStream_t st = m->ctx->stream;
+  FILE* f         = fopen(path, "rb");
+  if (!f)
+  {
+    sts_set_error("STS_LSRKStepReadCheckpoint: cannot open %s", path);
+    return STS_ILL_INPUT;
+  }
+  CkptHeader h;
+  bool ok = fread(&h, sizeof(h), 1, f) == 1 && memcmp(h.magic, CKPT_MAGIC, 8) == 0 && h.version == 1;
+  if (!ok || h.n != m->n || h.method != m->method || h.mixed != (int)m->mixed)
+  {
+    fclose(f);
+    sts_set_error("STS_LSRKStepReadCheckpoint: %s is not a checkpoint of this problem size, method and "
+                  "precision",
+                  path);
+    return STS_ILL_INPUT;
+  }
+  const bool fz = fused(m);
+  if (h.fused_path != (int)fz)
+  {
+    fclose(f);
+    sts_set_error("STS_LSRKStepReadCheckpoint: checkpoint written by the %s path", h.fused_path ? "fused" : "generic");
+    return STS_ILL_INPUT;
+  }
+  if (fz && !m->yb[0] && alloc_fused(m, NVD(m->g_y)))
+  {
+    fclose(f);
+    return STS_ERR_FAILURE;
+  }
+  m->par       = 0;
+  double* y    = fz ? m->yb[0] : NVD(m->g_y);
+  double* F    = fz ? m->Fb[0] : NVD(m->g_Fn);
+  std::vector<char> host((size_t)m->n * sizeof(double));
+  ok = ckpt_io(f, host.data(), nullptr, y, m->n * sizeof(double), false, st);
+  if (h.initialized) ok = ok && ckpt_io(f, host.data(), nullptr, F, m->n * sizeof(double), false, st);
+  if (h.initialized && fz && h.mixed)
+    ok = ok && ckpt_io(f, host.data(), nullptr, m->Ffb[0], m->n * sizeof(float), false, st);
+  if (ok && h.has_evec)
+  {
+    if (!m->evec && !STS_CUDA_OK(cudaMalloc(&m->evec, m->n * sizeof(double)))) ok = false;
+    ok = ok && ckpt_io(f, host.data(), nullptr, m->evec, m->n * sizeof(double), false, st);
+  }
+  fclose(f);
+  if (!ok)
+  {
+    sts_set_error("STS_LSRKStepReadCheckpoint: %s is truncated or unreadable", path);
+    return STS_ERR_FAILURE;
+  }
+  m->t               = h.t;
+  m->hnext           = h.hnext;
+  m->hlast           = h.hlast;
+  m->rho             = h.rho;
+  m->ep1             = h.ep1;
+  m->ep2             = h.ep2;
+  m->ncf             = h.ncf;
+  m->nst             = h.nst;
+  m->nst_att         = h.nst_att;
+  m->netf            = h.netf;
+  m->nfe             = h.nfe;
+  m->nfe_dee         = h.nfe_dee;
+  m->ndee            = h.ndee;
+  m->nst_exp         = h.nst_exp;
+  m->stage_max       = h.stage_max;
+  m->stages_total    = h.stages_total;
+  m->nhist           = h.nhist;
+  m->steps_since_dee = h.steps_since_dee;
+  m->initialized     = h.initialized != 0;
+  m->after_fail      = h.after_fail != 0;
+  m->last_s          = h.last_s;
+  return STS_SUCCESS;
+}

@@ -221,6 +221,14 @@ int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* tret, int it
 /* ARKodeReset: restart from (t, y) keeping options, counters and the step size; F(t, y) is
  * re-evaluated on the next step */
 int STS_ARKodeReset(void* mem, double t, N_Vector y);
+/* Checkpoint / restart (new; the reference writes only text snapshots of u,
+ * diffusion_2D.cpp:729-842): the full integrator state (t, step-size and controller history,
+ * eigenvalue estimate and refresh counter, statistics, y_n, the FSAL F_n, the mixed path's
+ * FP32 copy of F_n and the power-iteration vector) to one binary file. Reading it into an
+ * integrator created for the same problem size, method and precision continues the run
+ * with the same step sequence and bits as the uninterrupted one. */
+int STS_LSRKStepWriteCheckpoint(void* arkode_mem, const char* path);
+int STS_LSRKStepReadCheckpoint(void* arkode_mem, const char* path);
 /* CUDA-event timing of the fused stage kernel on the integrator's current buffers (after at
  * least one evolve): average milliseconds per launch over nlaunch launches of stage j = s/2
  * of the last step, launched on the context stream exactly as the integrator does */

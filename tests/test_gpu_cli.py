@@ -82,3 +82,27 @@ def test_cli_dirk_and_errors(stslib):
     assert rc == 1 and "Unknown inputs" in err
     rc, out, err = run(["--integrator", "erk"])
     assert rc == 1
+
+
+def test_cli_checkpoint_restart_matches_uninterrupted_run(stslib, tmp_path):
+    stslib.lib()
+    common = ["--problem", "manufactured", "--nx", "64", "--ny", "64", "--integrator", "rkl",
+              "--rtol", "1e-6", "--maxsteps", "10000"]
+    ck = str(tmp_path / "half.ckpt")
+    rc, out1, err = run(common + ["--tf", "0.005", "--nout", "1", "--checkpoint", ck])
+    assert rc == 0, err
+    rc, out2, err = run(common + ["--tf", "0.01", "--nout", "2", "--restart", ck])
+    assert rc == 0, err
+    rc, full, err = run(common + ["--tf", "0.01", "--nout", "2"])
+    assert rc == 0, err
+
+    def last_rms(out):
+        rows = [l.split() for l in out.split("\n") if len(l.split()) == 2]
+        return rows[-1]
+
+    def l2(out):
+        return [l for l in out.split("\n") if l.startswith("Relative L2 error vs exact")][0]
+
+    assert last_rms(out2) == last_rms(full)
+    assert l2(out2) == l2(full)
+    assert parse_like_runtests(out2)["Steps"] == parse_like_runtests(full)["Steps"]
