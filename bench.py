@@ -462,7 +462,7 @@ def run_precond(args):
     cap = args.precond_pairs
     r_all = torch.empty(cap * crop * crop, dtype=torch.float32, device="cuda")
     e_all = torch.empty_like(r_all)
-    meta = torch.empty(cap, 5, dtype=torch.float32, device="cuda")
+    meta = torch.empty(cap * 7, dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     got, nsys, pcg_its = 0, 0, []
@@ -471,17 +471,10 @@ def run_precond(args):
         P = sts.Problem(ctx, sts.UNFORCED, n, n, 1.0, ky)
         b = sts.NVector.from_numpy(ctx, sts.smooth_field(n, rng))
         off = got * crop * crop
-        k, its = sts.harvest_pcg_pairs(P, gh, b, args.precond_crops, crop, 1, min(cap - got, 4000),
-                                       r_all.data_ptr() + 4 * off, e_all.data_ptr() + 4 * off,
+        k, its = sts.harvest_pcg_pairs(P, gh, b, args.precond_crops, crop, args.precond_every,
+                                       min(cap - got, 4000), r_all.data_ptr() + 4 * off,
+                                       e_all.data_ptr() + 4 * off, meta.data_ptr() + 4 * 7 * got,
                                        int(rng.integers(1 << 62)))
-        sk, sg, jac = sts.net_features(1.0, ky, gh, dx)
-        rr = r_all[off:off + k * crop * crop].view(k, -1).double()
-        ee = e_all[off:off + k * crop * crop].view(k, -1).double()
-        meta[got:got + k, 0] = sk
-        meta[got:got + k, 1] = sg
-        meta[got:got + k, 2] = jac
-        meta[got:got + k, 3] = torch.rsqrt((rr ** 2).mean(1)).float()
-        meta[got:got + k, 4] = (1.0 / (ee ** 2).sum(1)).float()
         got += k
         nsys += 1
         pcg_its.append(its)
@@ -519,7 +512,9 @@ def run_precond(args):
             it2, rel2, rc2 = sts.fcg_solve(P, gh, net, b, x2, tol=1e-8, maxit=20000)
             t_fcg = time.perf_counter() - t
             res = {"ky": ky, "gamma_h": gh, "pcg_iters": it1, "pcg_s": t_pcg, "pcg_relres": rel1,
-                   "fcg_iters": it2, "fcg_s": t_fcg, "fcg_true_relres": rel2, "fcg_status": rc2}
+                   "fcg_iters": it2, "fcg_s": t_fcg, "fcg_true_relres": rel2, "fcg_status": rc2,
+                   "pcg_ms_per_iter": 1e3 * t_pcg / max(1, it1),
+                   "fcg_ms_per_iter": 1e3 * t_fcg / max(1, it2)}
         xa, xb = x1.numpy(), x2.numpy()
         res["solution_rel_diff"] = float(np.linalg.norm(xa - xb) / np.linalg.norm(xa))
         rows.append(res)
@@ -569,6 +564,7 @@ def main():
     ap.add_argument("--precond-n", type=int, default=2048)
     ap.add_argument("--precond-crop", type=int, default=128)
     ap.add_argument("--precond-crops", type=int, default=4)
+    ap.add_argument("--precond-every", type=int, default=1)
     ap.add_argument("--precond-pairs", type=int, default=51200)
     ap.add_argument("--precond-epochs", type=int, default=8)
     ap.add_argument("--precond-batch", type=int, default=32)

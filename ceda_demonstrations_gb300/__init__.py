@@ -173,11 +173,11 @@ SIGNATURES = [
     ("STS_NetApply", C.c_int, [_vp, C.c_int, _vp, _vp, C.c_double, C.c_double, C.c_double,
                                C.c_double]),
     ("STS_NetLossGrad", C.c_int, [_vp, C.c_int, _vp, _vp, C.c_double, C.c_double, C.c_double,
-                                  _dp, _fp]),
+                                  C.c_double, C.c_double, _dp, _fp]),
     ("STS_NetTrain", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, C.c_int, C.c_float,
                                C.c_ulonglong, _dp]),
     ("STS_HarvestPCGPairs", C.c_int, [_vp, C.c_double, _NV, C.c_int, C.c_int, C.c_int, C.c_int,
-                                      _vp, _vp, C.c_ulonglong, _ip, _ip]),
+                                      _vp, _vp, _vp, C.c_ulonglong, _ip, _ip]),
     ("STS_FCGSolve", C.c_int, [_vp, C.c_double, _vp, _NV, _NV, C.c_double, C.c_int, _ip, _dp]),
 ]
 
@@ -737,12 +737,13 @@ def smooth_field(n, rng, nbumps=24):
 
 
 def net_features(kx, ky, gamma, dx):
-    """(sk, sg, jacobi) of the shifted system (I - gamma A): the normalised anisotropy
-    log10(ky/kx), the normalised log10(gamma/dx^2) and the Jacobi factor 1/(1 - gamma cc)."""
+    """(sk, sg, jacobi, gcx, gcy) of the shifted system (I - gamma A) on a square grid: the
+    normalised anisotropy log10(ky/kx), the normalised log10(gamma/dx^2), the Jacobi factor
+    1/(1 - gamma cc) and the scaled stencil weights gamma kx/dx^2, gamma ky/dx^2."""
     cc = -2.0 * (kx + ky) / (dx * dx)
     sk = (np.log10(ky / kx) + 1.5) / 1.5
     sg = np.log10(gamma / (dx * dx)) - 3.6
-    return sk, sg, 1.0 / (1.0 - gamma * cc)
+    return sk, sg, 1.0 / (1.0 - gamma * cc), gamma * kx / (dx * dx), gamma * ky / (dx * dx)
 
 
 class Net:
@@ -781,10 +782,10 @@ class Net:
         if lib().STS_NetApply(self.h, n, r_ptr, z_ptr, sk, sg, jacobi, scale) != 0:
             _err("STS_NetApply")
 
-    def loss_grad(self, n, r_ptr, e_ptr, sk, sg, jacobi):
+    def loss_grad(self, n, r_ptr, e_ptr, sk, sg, jacobi, gcx, gcy):
         loss = C.c_double()
         g = np.empty(len(NET_LAYERS) * NET_WSZ, dtype=np.float32)
-        if lib().STS_NetLossGrad(self.h, n, r_ptr, e_ptr, sk, sg, jacobi, C.byref(loss),
+        if lib().STS_NetLossGrad(self.h, n, r_ptr, e_ptr, sk, sg, jacobi, gcx, gcy, C.byref(loss),
                                  g.ctypes.data_as(_fp)) != 0:
             _err("STS_NetLossGrad")
         return loss.value, {nm: g[i * NET_WSZ:(i + 1) * NET_WSZ].reshape(16, 16, 3, 3).copy()
@@ -810,13 +811,15 @@ class Net:
             pass
 
 
-def harvest_pcg_pairs(problem, gamma, b, ncrops, crop, every, max_pairs, r_ptr, e_ptr, seed=0):
+def harvest_pcg_pairs(problem, gamma, b, ncrops, crop, every, max_pairs, r_ptr, e_ptr, meta_ptr,
+                      seed=0):
     """Run Jacobi-PCG to 1e-10 on (I - gamma A) x = b, recording crop x crop windows of r_k
     and e_k = x* - x_k every `every` batches of 8 iterations (device FP32 buffers of
-    max_pairs * crop^2). Returns (pairs recorded, PCG iterations)."""
+    max_pairs * crop^2) with their training metadata (7 floats per pair, may be 0).
+    Returns (pairs recorded, PCG iterations)."""
     npairs, iters = C.c_int(), C.c_int()
     rc = lib().STS_HarvestPCGPairs(problem.h, gamma, b.h, ncrops, crop, every, max_pairs, r_ptr,
-                                   e_ptr, seed, C.byref(npairs), C.byref(iters))
+                                   e_ptr, meta_ptr, seed, C.byref(npairs), C.byref(iters))
     if rc < 0:
         _err("STS_HarvestPCGPairs")
     return npairs.value, iters.value

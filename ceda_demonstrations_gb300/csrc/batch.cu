@@ -9,9 +9,10 @@
 // single-problem integrator (lsrk.cu). No host round trip happens per step; the host only
 // launches the batch and reads the per-instance statistics afterwards.
 //
-// Precision: FP64 throughout (the path is FP64-ALU-bound on GB300). The device controller
-// uses the CUDA math library's pow, so step sequences can differ from the CPU oracle's in the
-// last bit of h; the parity tests compare with a tolerance.
+// Precision: FP64 throughout (the path is FP64-ALU-bound on GB300). Every step decision uses
+// the arithmetic of the single-problem integrator and the CPU oracle: stage coefficients from
+// the host's table, IEEE sqrt/divide, and the deterministic pow of portable_math.cuh in the
+// controller, so each instance follows the oracle's step sequence and matches it bit for bit.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -21,6 +22,7 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "portable_math.cuh"
 #include "sts_internal.cuh"
 
 struct BatchInst {
@@ -38,9 +40,17 @@ struct BatchArrays {
   double* buf[5]; // F_n, F_{n+1} / Y work buffers (instance-local regions)
 };
 
+// Stage coefficients come from a table the host fills with STS_LSRKStageCoeffs for every
+// stage count 2..smax (the single-problem integrator's and the oracle's values, bit for bit):
+// entry (s, j) = {mu_j, nu_j, mus_j, a_{j-1}}.
+struct CoefT {
+  double mu, nu, mus, ajm1;
+};
+
 struct BatchParams {
   double tf, rtol, atol, eig_safety;
   int method, smax, controller, maxsteps;
+  const void* coef; // CoefT table [(smax + 1) x (smax + 1)]
 };
 
 struct STS_Batch_ {
@@ -56,6 +66,8 @@ struct STS_Batch_ {
   int block        = 512;
   int ctas_per_sm  = 2;
   double last_ms   = 0.0;
+  CoefT* dcoef     = nullptr; // stage-coefficient table of (coef_method, coef_smax)
+  int coef_method = -1, coef_smax = -1;
 };
 
 // ---------------------------------------------------------------------------------------
@@ -71,16 +83,16 @@ __device__ double d_controller(int controller, double h, double dsm, double ep1,
   double e1 = fmax(B_BIAS * dsm, B_TINY), e2 = fmax(B_BIAS * ep1, B_TINY), e3 = fmax(B_BIAS * ep2, B_TINY);
   if (controller == 0)
   {
-    if (nhist < 1) return h * pow(e1, -0.58 / B_ORD);
-    if (nhist < 2) return h * pow(e1, -0.58 / B_ORD) * pow(e2, 0.21 / B_ORD);
-    return h * pow(e1, -0.58 / B_ORD) * pow(e2, 0.21 / B_ORD) * pow(e3, -0.1 / B_ORD);
+    if (nhist < 1) return h * stsm::pow(e1, -0.58 / B_ORD);
+    if (nhist < 2) return h * stsm::pow(e1, -0.58 / B_ORD) * stsm::pow(e2, 0.21 / B_ORD);
+    return h * stsm::pow(e1, -0.58 / B_ORD) * stsm::pow(e2, 0.21 / B_ORD) * stsm::pow(e3, -0.1 / B_ORD);
   }
   if (controller == 1)
   {
-    if (nhist < 1) return h * pow(e1, -0.8 / B_ORD);
-    return h * pow(e1, -0.8 / B_ORD) * pow(e2, 0.31 / B_ORD);
+    if (nhist < 1) return h * stsm::pow(e1, -0.8 / B_ORD);
+    return h * stsm::pow(e1, -0.8 / B_ORD) * stsm::pow(e2, 0.31 / B_ORD);
   }
-  return h * pow(e1, -1.0 / B_ORD);
+  return h * stsm::pow(e1, -1.0 / B_ORD);
 }
 
 __device__ int d_stages(int method, double h, double rho, int smax, double* hmax)
@@ -100,100 +112,6 @@ __device__ int d_stages(int method, double h, double rho, int smax, double* hmax
   if (ss < 2.0) ss = 2.0;
   if (ss > 1e9) ss = 1e9;
   return (int)ss;
-}
-
-// Per-stage coefficients, generated on the fly (same recurrences as STS_LSRKStageCoeffs)
-struct Coef {
-  // RKC state
-  double w0, w1, bjm1, bjm2, zjm1, zjm2, dzjm1, dzjm2, d2zjm1, d2zjm2, thjm1, thjm2;
-  // RKL state
-  double cj1;
-  int method, s;
-  double mus1;
-};
-
-__device__ void coef_init(Coef& c, int method, int s)
-{
-  c.method = method;
-  c.s      = s;
-  const double sd = (double)s;
-  if (method == 0)
-  {
-    c.w0               = 1.0 + 2.0 / (13.0 * (sd * sd));
-    const double temp1 = c.w0 * c.w0 - 1.0;
-    const double temp2 = sqrt(temp1);
-    const double arg   = sd * log(c.w0 + temp2);
-    c.w1               = sinh(arg) * temp1 / (cosh(arg) * sd * temp2 - c.w0 * sinh(arg));
-    c.bjm1             = 1.0 / ((2.0 * c.w0) * (2.0 * c.w0));
-    c.bjm2             = c.bjm1;
-    c.mus1             = c.w1 * c.bjm1;
-    c.thjm2            = 0.0;
-    c.thjm1            = c.mus1;
-    c.zjm1 = c.w0;
-    c.zjm2 = 1.0;
-    c.dzjm1 = 1.0;
-    c.dzjm2 = 0.0;
-    c.d2zjm1 = 0.0;
-    c.d2zjm2 = 0.0;
-  }
-  else
-  {
-    c.w1   = 4.0 / ((sd + 2.0) * (sd - 1.0));
-    c.bjm2 = 1.0 / 3.0;
-    c.bjm1 = 1.0 / 3.0;
-    c.mus1 = c.w1 * c.bjm1;
-    c.cj1  = c.mus1;
-  }
-}
-
-// coefficients of stage j (2..s), advancing the recurrence
-__device__ void coef_next(Coef& c, int j, double* mu, double* nu, double* mus, double* ajm1, double* cjm1)
-{
-  if (c.method == 0)
-  {
-    const double zj   = 2.0 * c.w0 * c.zjm1 - c.zjm2;
-    const double dzj  = 2.0 * c.w0 * c.dzjm1 - c.dzjm2 + 2.0 * c.zjm1;
-    const double d2zj = 2.0 * c.w0 * c.d2zjm1 - c.d2zjm2 + 4.0 * c.dzjm1;
-    const double bj   = d2zj / (dzj * dzj);
-    const double a    = 1.0 - c.zjm1 * c.bjm1;
-    const double m    = 2.0 * c.w0 * bj / c.bjm1;
-    const double n    = -bj / c.bjm2;
-    const double ms   = m * c.w1 / c.w0;
-    *mu = m;
-    *nu = n;
-    *mus = ms;
-    *ajm1 = a;
-    *cjm1 = c.thjm1;
-    const double thj = m * c.thjm1 + n * c.thjm2 + ms * (1.0 - a);
-    c.thjm2 = c.thjm1;
-    c.thjm1 = thj;
-    c.bjm2 = c.bjm1;
-    c.bjm1 = bj;
-    c.zjm2 = c.zjm1;
-    c.zjm1 = zj;
-    c.dzjm2 = c.dzjm1;
-    c.dzjm1 = dzj;
-    c.d2zjm2 = c.d2zjm1;
-    c.d2zjm1 = d2zj;
-  }
-  else
-  {
-    const double jd   = (double)j;
-    const double temj = (jd + 2.0) * (jd - 1.0);
-    const double cj   = temj * c.w1 / 4.0;
-    const double bj   = temj / (2.0 * jd * (jd + 1.0));
-    const double a    = 1.0 - c.bjm1;
-    const double m    = (2.0 * jd - 1.0) / jd * (bj / c.bjm1);
-    const double n    = -(jd - 1.0) / jd * (bj / c.bjm2);
-    *mu = m;
-    *nu = n;
-    *mus = c.w1 * m;
-    *ajm1 = a;
-    *cjm1 = c.cj1;
-    c.cj1 = cj;
-    c.bjm2 = c.bjm1;
-    c.bjm1 = bj;
-  }
 }
 
 // CTA-wide exact sum of per-thread limbs; returns the rounded total to every thread
@@ -331,7 +249,7 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
       nfe++;
       const double d2 = sqrt(cta_exact_sum<NT>(a2, f2, sm, &sflags, &sres) / (double)N) / h0;
       const double dm = d1 > d2 ? d1 : d2;
-      double h1       = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : pow(0.01 / dm, 1.0 / B_ORD);
+      double h1       = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : stsm::pow(0.01 / dm, 1.0 / B_ORD);
       if (!(h1 > 0.0) || !(h1 < 1e300)) h1 = h0;
       double h = (100.0 * h0 < h1) ? 100.0 * h0 : h1;
       if (h > prm.tf) h = prm.tf;
@@ -363,13 +281,12 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
         }
         s = d_stages(prm.method, h, rho, prm.smax, &hmax);
         natt++;
-        Coef co;
-        coef_init(co, prm.method, s);
+        const CoefT* ct = reinterpret_cast<const CoefT*>(prm.coef) + (long long)s * (prm.smax + 1);
         const double* yc = P[iy];
         const double* F0 = P[iF];
         // stage 1 -> bufs[0]
         {
-          const double hm1 = h * co.mus1;
+          const double hm1 = h * ct[1].mus;
           double* y1       = P[bufs[0]];
           for (int j = warp; j < n; j += NW)
             for (int i = lane; i < n; i += 32)
@@ -383,8 +300,7 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
         int last          = 0; // index into bufs of Y_{j-1}
         for (int jst = 2; jst <= s; ++jst)
         {
-          double mu, nu, mus, ajm1, cjm1;
-          coef_next(co, jst, &mu, &nu, &mus, &ajm1, &cjm1);
+          const double mu = ct[jst].mu, nu = ct[jst].nu, mus = ct[jst].mus, ajm1 = ct[jst].ajm1;
           const double hm = h * mus;
           const double tm = hm * cc;
           const double gc = mu + tm, gx = hm * cx, gy = hm * cy, gn = nu, g0 = (1.0 - mu) - nu;
@@ -593,6 +509,7 @@ extern "C" int STS_BatchFree(STS_Batch* pb)
   cudaFree(b->dqueue);
   cudaFree(b->y);
   cudaFree(b->work);
+  cudaFree(b->dcoef);
   delete b;
   *pb = nullptr;
   return 0;
@@ -645,7 +562,7 @@ extern "C" int STS_BatchSetInitialModes(STS_Batch b, int nmodes, const int* p, c
 extern "C" int STS_BatchEvolve(STS_Batch b, double tf, int method, double rtol, double atol, int smax, int controller,
                                long long maxsteps)
 {
-  if (!b || !(tf > 0.0) || smax < 2) return STS_ILL_INPUT;
+  if (!b || !(tf > 0.0) || smax < 2 || smax > 10000) return STS_ILL_INPUT;
   ctx_activate(b->ctx);
   BatchParams prm;
   prm.tf         = tf;
@@ -656,6 +573,25 @@ extern "C" int STS_BatchEvolve(STS_Batch b, double tf, int method, double rtol, 
   prm.smax       = smax;
   prm.controller = controller;
   prm.maxsteps   = (int)(maxsteps > 0 ? std::min<long long>(maxsteps, 1LL << 30) : 1000000);
+  if (b->coef_method != method || b->coef_smax != smax)
+  {
+    const int S = smax + 1;
+    std::vector<CoefT> tab((size_t)S * S);
+    std::vector<double> mu(S), nu(S), mus(S), ajm1(S), cjm1(S);
+    for (int sc = 2; sc <= smax; ++sc)
+    {
+      STS_LSRKStageCoeffs(method, sc, mu.data(), nu.data(), mus.data(), ajm1.data(), cjm1.data());
+      for (int j = 1; j <= sc; ++j) tab[(size_t)sc * S + j] = CoefT{mu[j], nu[j], mus[j], ajm1[j]};
+    }
+    cudaFree(b->dcoef);
+    b->dcoef = nullptr;
+    if (!STS_CUDA_OK(cudaMalloc(&b->dcoef, tab.size() * sizeof(CoefT))) ||
+        !STS_CUDA_OK(cudaMemcpy(b->dcoef, tab.data(), tab.size() * sizeof(CoefT), cudaMemcpyHostToDevice)))
+      return -1;
+    b->coef_method = method;
+    b->coef_smax   = smax;
+  }
+  prm.coef = b->dcoef;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);

@@ -28,6 +28,7 @@
 
 #include "kernels.cuh"
 #include "stage_tma.cuh"
+#include "portable_math.cuh"
 #include "sts_internal.cuh"
 
 void sts_f64_to_f32(STS_Context ctx, const double* a, float* b, long long n);
@@ -149,16 +150,16 @@ extern "C" double STS_AdaptControllerEstimate(int controller, double h, double d
   if (e3 < TINYE) e3 = TINYE;
   if (controller == STS_ADAPT_PID)
   {
-    if (nhist < 1) return h * pow(e1, -0.58 / ORD);
-    if (nhist < 2) return h * pow(e1, -0.58 / ORD) * pow(e2, 0.21 / ORD);
-    return h * pow(e1, -0.58 / ORD) * pow(e2, 0.21 / ORD) * pow(e3, -0.1 / ORD);
+    if (nhist < 1) return h * stsm::pow(e1, -0.58 / ORD);
+    if (nhist < 2) return h * stsm::pow(e1, -0.58 / ORD) * stsm::pow(e2, 0.21 / ORD);
+    return h * stsm::pow(e1, -0.58 / ORD) * stsm::pow(e2, 0.21 / ORD) * stsm::pow(e3, -0.1 / ORD);
   }
   if (controller == STS_ADAPT_PI)
   {
-    if (nhist < 1) return h * pow(e1, -0.8 / ORD);
-    return h * pow(e1, -0.8 / ORD) * pow(e2, 0.31 / ORD);
+    if (nhist < 1) return h * stsm::pow(e1, -0.8 / ORD);
+    return h * stsm::pow(e1, -0.8 / ORD) * stsm::pow(e2, 0.31 / ORD);
   }
-  return h * pow(e1, -1.0 / ORD);
+  return h * stsm::pow(e1, -1.0 / ORD);
 }
 
 static constexpr double SAFETY = 0.96, GROWTH = 20.0, ETAMX1 = 10000.0, ETAMXF = 0.3, ETAMIN = 0.1;
@@ -670,7 +671,7 @@ static double initial_step(LSRKMem* m, const double* y0, const double* F0, doubl
   cudaFreeAsync(F1, ctx->stream);
   if (rc < 0) return -1.0;
   const double dm = d1 > d2 ? d1 : d2;
-  double h1       = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : pow(0.01 / dm, 1.0 / ORD);
+  double h1       = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : stsm::pow(0.01 / dm, 1.0 / ORD);
   if (!(h1 > 0.0) || !(h1 < INFINITY)) h1 = h0;
   double h = (100.0 * h0 < h1) ? 100.0 * h0 : h1;
   if (h > tdist) h = tdist;

@@ -48,8 +48,9 @@ __device__ __forceinline__ int swz(int p, int h) { return p * 32 + ((h ^ ((p >> 
 // Weight fragments: wf[(tap * 2 + nh) * 32 + lane] = {b0b1, b2b3} for n-half nh
 // (B[k = ci][n = co], b0b1 = ci (lane%4)*2..+1, b2b3 = ci (lane%4)*2+8..+9, co = nh*8 + lane/4)
 
-// Per-sample metadata of a training batch: {sk, sg, jacobi, scale, 1/||e||^2}
-constexpr int META = 5;
+// Per-sample metadata of a training pair: {sk, sg, jacobi, scale, 1/(e^T M e), gamma cx, gamma cy}
+// (M = I - gamma A on the crop; scale = 1/rms(r) normalises the network input)
+constexpr int META = 7;
 __device__ __forceinline__ double meta_out_scale(const float* meta, int img)
 {
   return (double)meta[META * img + 2] / (double)meta[META * img + 3];
@@ -63,7 +64,8 @@ __device__ __forceinline__ double meta_out_scale(const float* meta, int img)
 //             upadd_kernel), so the skip sum is never stored.
 enum { LD_PLAIN = 0, LD_R64 = 1, LD_UPADD = 2 };
 struct LoadArgs {
-  const double* r       = nullptr;
+  const double* r       = nullptr; // FP64 residual (network input / Jacobi skip)
+  const float* r32      = nullptr; // FP32 residual (training batches; Jacobi skip)
   double scale          = 1.0;
   float sk = 0.f, sg    = 0.f;
   const __nv_bfloat16* coarse = nullptr;
@@ -71,8 +73,9 @@ struct LoadArgs {
 
 // out[p][co] = sum_{tap, ci} w[co][ci][tap] * in[p + tap - 1][ci], for each image of a batch
 // (blockIdx.z; images of H x W pixels stored one after another, zero padding at every edge)
-// mode 0: BF16 NHWC output (16 channels); mode 1: FP64 output of channel 0 times the image's
-// output scale (meta, or out_scale when meta is null)
+// mode 0: BF16 NHWC output (16 channels); mode 1: FP64 output (channel 0 + the Jacobi skip
+// r * scale when la.r or la.r32 is set) times the image's output scale (meta, or out_scale
+// when meta is null)
 template <int MODE, int LOAD = LD_PLAIN>
 __global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __restrict__ in, int H, int W,
                                                        const uint2* __restrict__ wf, __nv_bfloat16* __restrict__ out,
@@ -88,7 +91,11 @@ __global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __re
   else
   {
     out64 += img_pix;
-    if (meta) out_scale = meta_out_scale(meta, blockIdx.z);
+    if (meta)
+    {
+      out_scale = meta_out_scale(meta, blockIdx.z);
+      la.scale  = (double)meta[META * blockIdx.z + 3];
+    }
   }
   // stage the input tile with a one-pixel halo (16-byte chunks, zero outside the image)
   for (int c = tid; c < (TR + 2) * (TC + 2) * 2; c += NTHR)
@@ -188,7 +195,12 @@ __global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __re
           }
         }
         else if ((lane & 3) == 0)
-          out64[p] = (double)acc[0][half * 2] * out_scale;
+        {
+          double v = (double)acc[0][half * 2];
+          if (la.r) v += la.r[img_pix + p] * la.scale;
+          else if (la.r32) v += (double)la.r32[img_pix + p] * la.scale;
+          out64[p] = v * out_scale;
+        }
       }
     }
   }
@@ -262,28 +274,88 @@ __global__ void poolT_add_kernel(const __nv_bfloat16* __restrict__ gcoarse, int 
   }
 }
 
-// dL/dz (FP64, one channel) -> BF16 NHWC gradient (channel 0) times scale; with meta, the
-// image's scale is out_scale * (1/||e||^2) * scale
-__global__ void gradz_kernel(long long npix, long long img_pix, const double* __restrict__ z,
-                             const float* __restrict__ e, double scale, const float* __restrict__ meta,
-                             __nv_bfloat16* __restrict__ g)
+// Energy-norm loss of each image (n x n): d = z - e, L_img = 0.5 d^T M d / (e^T M e) with
+// M = I - gamma A on the crop (zero outside). Writes dL/dy = (M d) * out_scale / (e^T M e) * gscale
+// as the BF16 channel-0 gradient of the network output y and adds gscale * sum L_img to *acc.
+__global__ void gradz_kernel(long long npix, int n, const double* __restrict__ z, const float* __restrict__ e,
+                             double gscale, const float* __restrict__ meta, __nv_bfloat16* __restrict__ g,
+                             double* __restrict__ acc)
 {
+  const long long ip = (long long)n * n;
+  double lsum        = 0.0;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x)
   {
-    double sc = scale;
-    if (meta)
-    {
-      const int img = (int)(p / img_pix);
-      sc *= meta_out_scale(meta, img) * (double)meta[META * img + 4];
-    }
-    const float d = (float)((z[p] - (double)e[p]) * sc);
+    const int img = (int)(p / ip);
+    const int q = (int)(p % ip), i = q % n, j = q / n;
+    const float* m = meta + META * img;
+    const double gcx = m[5], gcy = m[6];
+    auto dd = [&](long long k) { return z[k] - (double)e[k]; };
+    const double dc = dd(p);
+    const double dw = i > 0 ? dd(p - 1) : 0.0, de = i < n - 1 ? dd(p + 1) : 0.0;
+    const double ds = j > 0 ? dd(p - n) : 0.0, dn = j < n - 1 ? dd(p + n) : 0.0;
+    const double Md = (1.0 + 2.0 * (gcx + gcy)) * dc - gcx * (dw + de) - gcy * (ds + dn);
+    const double inv = (double)m[4];
+    lsum += 0.5 * dc * Md * inv;
+    const float gv = (float)(Md * inv * meta_out_scale(meta, img) * gscale);
     __align__(16) __nv_bfloat16 o[CH];
-    o[0] = __float2bfloat16_rn(d);
+    o[0] = __float2bfloat16_rn(gv);
 #pragma unroll
     for (int c = 1; c < CH; ++c) o[c] = __float2bfloat16_rn(0.f);
     uint4* dst = reinterpret_cast<uint4*>(g + p * CH);
     dst[0]     = reinterpret_cast<uint4*>(o)[0];
     dst[1]     = reinterpret_cast<uint4*>(o)[1];
+  }
+  for (int m = 16; m >= 1; m >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, m);
+  if ((threadIdx.x & 31) == 0 && lsum != 0.0) atomicAdd(acc, lsum * gscale);
+}
+
+// per-pair metadata from the harvested crops: scale = 1/rms(r), 1/(e^T M e); one block per pair
+__global__ void __launch_bounds__(256) pair_meta_kernel(const float* __restrict__ r, const float* __restrict__ e, int n,
+                                                        float sk, float sg, float jac, double gcx, double gcy,
+                                                        float* __restrict__ meta)
+{
+  __shared__ double s1[8], s2[8];
+  const long long ip = (long long)n * n;
+  const float* rp    = r + ip * blockIdx.x;
+  const float* ep    = e + ip * blockIdx.x;
+  double a = 0.0, b = 0.0;
+  for (long long q = threadIdx.x; q < ip; q += blockDim.x)
+  {
+    const int i = (int)(q % n), j = (int)(q / n);
+    const double rv = rp[q];
+    a += rv * rv;
+    const double ec = ep[q];
+    const double ew = i > 0 ? ep[q - 1] : 0.0, ee = i < n - 1 ? ep[q + 1] : 0.0;
+    const double es = j > 0 ? ep[q - n] : 0.0, en = j < n - 1 ? ep[q + n] : 0.0;
+    b += ec * ((1.0 + 2.0 * (gcx + gcy)) * ec - gcx * (ew + ee) - gcy * (es + en));
+  }
+  for (int m = 16; m >= 1; m >>= 1)
+  {
+    a += __shfl_xor_sync(0xffffffffu, a, m);
+    b += __shfl_xor_sync(0xffffffffu, b, m);
+  }
+  if ((threadIdx.x & 31) == 0)
+  {
+    s1[threadIdx.x >> 5] = a;
+    s2[threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    double A = 0.0, B = 0.0;
+    for (int w = 0; w < 8; ++w)
+    {
+      A += s1[w];
+      B += s2[w];
+    }
+    float* m = meta + META * blockIdx.x;
+    m[0]     = sk;
+    m[1]     = sg;
+    m[2]     = jac;
+    m[3]     = A > 0.0 ? (float)sqrt((double)ip / A) : 1.f;
+    m[4]     = B > 0.0 ? (float)(1.0 / B) : 0.f;
+    m[5]     = (float)gcx;
+    m[6]     = (float)gcy;
   }
 }
 
@@ -401,20 +473,6 @@ __global__ void input_kernel_t(long long npix, long long img_pix, const T* __res
     dst[0]     = reinterpret_cast<uint4*>(o)[0];
     dst[1]     = reinterpret_cast<uint4*>(o)[1];
   }
-}
-
-// acc += sum_p w_img (z_p - e_p)^2 with w_img = 1/||e||^2 of the image (meta) or 1
-__global__ void sq_diff_kernel(long long n, long long img_pix, const double* __restrict__ z,
-                               const float* __restrict__ e, const float* __restrict__ meta, double* acc)
-{
-  double s = 0.0;
-  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
-  {
-    const double d = z[p] - (double)e[p];
-    s += d * d * (meta ? (double)meta[META * (int)(p / img_pix) + 4] : 1.0);
-  }
-  for (int m = 16; m >= 1; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
-  if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
 }
 
 // dst[q] = src[idx[q]] for q < nb samples of `len` floats each (and their metadata)
@@ -569,7 +627,8 @@ extern "C" STS_Net STS_NetCreate(STS_Context ctx, int nmax, unsigned long long s
   for (int l = 0; l < NLAYER; ++l)
   {
     const int ci_n = (l == net::L_IN) ? 3 : CH, co_n = (l == net::L_OUT) ? 1 : CH;
-    const float sd = std::sqrt(1.0f / (ci_n * 9));
+    // the output layer starts small, so the untrained network is close to its Jacobi skip
+    const float sd = std::sqrt(1.0f / (ci_n * 9)) * (l == net::L_OUT ? 0.1f : 1.0f);
     for (int co = 0; co < co_n; ++co)
       for (int ci = 0; ci < ci_n; ++ci)
         for (int t = 0; t < 9; ++t)
@@ -668,8 +727,12 @@ static void net_forward(STS_Net nt, int n, int nimg, const T* r, double scale, f
   net::upadd_kernel<<<grid_for(np * CH), 256, 0, st>>>(L[1].b, L[0].a, n * nimg, n, L[0].s);      // s0
   conv(nt, L[0].s, n, nimg, net::L_U0, false, L[0].b);                                           // b0
   dim3 g((unsigned)((n + net::TC - 1) / net::TC), (unsigned)((n + net::TR - 1) / net::TR), (unsigned)nimg);
+  net::LoadArgs la; // Jacobi skip from the network input
+  if constexpr (sizeof(T) == 8) la.r = reinterpret_cast<const double*>(r);
+  else la.r32 = reinterpret_cast<const float*>(r);
+  la.scale = scale;
   net::conv3x3_kernel<1><<<g, net::NTHR, 0, st>>>(L[0].b, n, n, nt->wf + net::L_OUT * 576, nullptr,
-                                                  zout ? zout : nt->z, out_scale, meta);
+                                                  zout ? zout : nt->z, out_scale, meta, la);
 }
 
 // Inference forward pass of one n x n residual (FP64, device) into zout: the input channels
@@ -707,7 +770,7 @@ static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
   net::conv3x3_kernel<0, net::LD_UPADD><<<grid(n), net::NTHR, 0, st>>>(L[0].a, n, n, nt->wf + net::L_U0 * 576, L[0].b,
                                                                         nullptr, 0.0, nullptr, lu);  // b0
   net::conv3x3_kernel<1><<<grid(n), net::NTHR, 0, st>>>(L[0].b, n, n, nt->wf + net::L_OUT * 576, nullptr, zout,
-                                                        out_scale, nullptr);                        // z
+                                                        out_scale, nullptr, la);                    // z
 }
 
 static void wgrad(STS_Net nt, const __nv_bfloat16* x, const __nv_bfloat16* g, int n, int nimg, int layer)
@@ -717,16 +780,15 @@ static void wgrad(STS_Net nt, const __nv_bfloat16* x, const __nv_bfloat16* g, in
   net::wgrad_kernel<<<grid, 256, 0, nt->ctx->stream>>>(x, g, n, n, nimg, nt->g + layer * WSZ);
 }
 
-// gradient of the loss w.r.t. the weights, accumulated into nt->g; needs the preceding
-// forward; the output gradient is (z - e) * gscale (times the image's out_scale / ||e||^2
-// when meta is given)
+// gradient of the energy-norm loss w.r.t. the weights, accumulated into nt->g (and gscale
+// times the loss into nt->dacc); needs the preceding forward and the per-image meta
 static void net_backward(STS_Net nt, int n, int nimg, const float* e, double gscale, const float* meta)
 {
   cudaStream_t st = nt->ctx->stream;
   net::Level* L   = nt->L;
   const long long ip = (long long)n * n, np = ip * nimg;
   const int m = nimg;
-  net::gradz_kernel<<<grid_for(np), 256, 0, st>>>(np, ip, nt->z, e, gscale, meta, L[0].gt);     // g (channel 0)
+  net::gradz_kernel<<<grid_for(np), 256, 0, st>>>(np, n, nt->z, e, gscale, meta, L[0].gt, nt->dacc); // g (channel 0)
   wgrad(nt, L[0].b, L[0].gt, n, m, net::L_OUT);
   conv(nt, L[0].gt, n, m, net::L_OUT, true, L[0].gb);                                          // gb0
   wgrad(nt, L[0].s, L[0].gb, n, m, net::L_U0);
@@ -772,37 +834,52 @@ extern "C" int STS_NetApply(STS_Net nt, int n, const double* r, double* z, doubl
   return STS_CUDA_OK(cudaGetLastError()) ? 0 : -1;
 }
 
-// one sample: loss = 0.5 ||M r - e||^2 / ||e||^2 and dloss/dW (FP32, host) — scale = 1
+// one sample (scale 1): loss = 0.5 (z - e)^T M (z - e) / (e^T M e), M = I - gamma A on the
+// n x n field with gamma cx = gcx, gamma cy = gcy, and dloss/dW (FP32, host)
 extern "C" int STS_NetLossGrad(STS_Net nt, int n, const double* r, const float* e, double sk, double sg, double jacobi,
-                               double* loss, float* grad)
+                               double gcx, double gcy, double* loss, float* grad)
 {
   if (!net_size_ok(nt, n) || !r || !e) return -1;
   ctx_activate(nt->ctx);
   cudaStream_t st = nt->ctx->stream;
   const long long np = (long long)n * n;
-  // ||e||^2 on the host (test-sized inputs)
+  // e^T M e on the host (test-sized inputs)
   std::vector<float> eh(np);
   if (!STS_CUDA_OK(cudaMemcpy(eh.data(), e, np * 4, cudaMemcpyDeviceToHost))) return -1;
-  double e2 = 0.0;
-  for (float v : eh) e2 += (double)v * v;
-  net_forward<double>(nt, n, 1, r, 1.0, (float)sk, (float)sg, jacobi, nullptr);
+  double eMe = 0.0;
+  for (long long q = 0; q < np; ++q)
+  {
+    const int i = (int)(q % n), j = (int)(q / n);
+    const double c  = eh[q];
+    const double w  = i > 0 ? eh[q - 1] : 0.0, ea = i < n - 1 ? eh[q + 1] : 0.0;
+    const double so = j > 0 ? eh[q - n] : 0.0, no = j < n - 1 ? eh[q + n] : 0.0;
+    eMe += c * ((1.0 + 2.0 * (gcx + gcy)) * c - gcx * (w + ea) - gcy * (so + no));
+  }
+  if (!nt->mb)
+  {
+    bool ok = true;
+    nt->mb  = (float*)dalloc(META * 4, &ok);
+    if (!ok) return -1;
+  }
+  const float mh[META] = {(float)sk, (float)sg, (float)jacobi, 1.f, (float)(1.0 / eMe), (float)gcx, (float)gcy};
+  cudaMemcpyAsync(nt->mb, mh, sizeof(mh), cudaMemcpyHostToDevice, st);
+  net_forward<double>(nt, n, 1, r, 1.0, (float)sk, (float)sg, jacobi, nt->mb);
   cudaMemsetAsync(nt->dacc, 0, 8, st);
-  net::sq_diff_kernel<<<grid_for(np), 256, 0, st>>>(np, np, nt->z, e, nullptr, nt->dacc);
-  double d2 = 0.0;
-  cudaMemcpyAsync(&d2, nt->dacc, 8, cudaMemcpyDeviceToHost, st);
   cudaMemsetAsync(nt->g, 0, NLAYER * WSZ * 4, st);
-  net_backward(nt, n, 1, e, jacobi / e2, nullptr);
+  net_backward(nt, n, 1, e, 1.0, nt->mb);
+  double l = 0.0;
+  cudaMemcpyAsync(&l, nt->dacc, 8, cudaMemcpyDeviceToHost, st);
   if (!STS_CUDA_OK(cudaStreamSynchronize(st))) return -1;
-  if (loss) *loss = 0.5 * d2 / e2;
+  if (loss) *loss = l;
   if (grad && !STS_CUDA_OK(cudaMemcpy(grad, nt->g, NLAYER * WSZ * 4, cudaMemcpyDeviceToHost))) return -1;
   return 0;
 }
 
 // Adam training on nsamples pairs (r_k, e_k) of n x n fields stored as FP32 on the device;
-// meta[5k..5k+4] = {sk, sg, jacobi, scale, 1/||e_k||^2}. Each epoch visits the samples in a
-// fresh shuffled order in minibatches of `batch` images (gathered into a staging buffer and
-// run as one batched forward/backward); loss = mean over the minibatch of
-// 0.5 ||M r_k - e_k||^2 / ||e_k||^2. Returns the mean loss of the last epoch.
+// meta[7k..7k+6] = {sk, sg, jacobi, scale, 1/(e_k^T M e_k), gamma cx, gamma cy}. Each epoch
+// visits the samples in a fresh shuffled order in minibatches of `batch` images (gathered into
+// a staging buffer and run as one batched forward/backward); loss = mean over the minibatch of
+// 0.5 d^T M d / (e^T M e), d = z_k - e_k. Returns the mean loss of the last epoch.
 extern "C" int STS_NetTrain(STS_Net nt, int n, int nsamples, const float* r, const float* e, const float* meta,
                             int epochs, int batch, float lr, unsigned long long seed, double* last_loss)
 {
@@ -842,7 +919,6 @@ extern "C" int STS_NetTrain(STS_Net nt, int n, int nsamples, const float* r, con
                                                                 nt->mb);
       cudaMemsetAsync(nt->g, 0, NLAYER * WSZ * 4, st);
       net_forward<float>(nt, n, batch, nt->rb, 1.0, 0.f, 0.f, 1.0, nt->mb);
-      net::sq_diff_kernel<<<grid_for(ip * batch), 256, 0, st>>>(ip * batch, ip, nt->z, nt->eb, nt->mb, nt->dacc);
       net_backward(nt, n, batch, nt->eb, 1.0 / batch, nt->mb);
       nt->adam_t++;
       const float bc1 = 1.f - powf(b1, (float)nt->adam_t), bc2 = 1.f - powf(b2, (float)nt->adam_t);
@@ -854,7 +930,7 @@ extern "C" int STS_NetTrain(STS_Net nt, int n, int nsamples, const float* r, con
     double d2 = 0.0;
     cudaMemcpyAsync(&d2, nt->dacc, 8, cudaMemcpyDeviceToHost, st);
     if (!STS_CUDA_OK(cudaStreamSynchronize(st))) return -1;
-    epoch_loss = 0.5 * d2 / ((double)nbatches * batch);
+    epoch_loss = d2 / (double)nbatches;
   }
   if (last_loss) *last_loss = epoch_loss;
   return 0;
@@ -895,8 +971,8 @@ __global__ void corr_kernel(const double* __restrict__ xs, long long nx, int x0,
 } // namespace net
 
 extern "C" int STS_HarvestPCGPairs(STS_Problem p, double gamma, N_Vector b, int ncrops, int crop, int every,
-                                   int max_pairs, float* r_out, float* e_out, unsigned long long seed, int* npairs,
-                                   int* iters)
+                                   int max_pairs, float* r_out, float* e_out, float* meta_out,
+                                   unsigned long long seed, int* npairs, int* iters)
 {
   if (!p || !b || crop < 16 || crop > p->nx || crop > p->ny || ncrops < 1 || every < 1 || max_pairs < 1)
   {
@@ -934,6 +1010,14 @@ extern "C" int STS_HarvestPCGPairs(STS_Problem p, double gamma, N_Vector b, int 
   {
     const int c = pair_crop[k];
     net::corr_kernel<<<grid_for(cs), 256, 0, st>>>(NVD(x), p->nx, cx[c], cy[c], crop, e_out + (long long)k * cs);
+  }
+  if (meta_out && !pair_crop.empty())
+  {
+    const double sk  = (std::log10(p->ky / p->kx) + 1.5) / 1.5;
+    const double sg  = std::log10(gamma / (p->dx * p->dx)) - 3.6;
+    const double jac = 1.0 / (1.0 - gamma * p->cc);
+    net::pair_meta_kernel<<<(unsigned)pair_crop.size(), 256, 0, st>>>(r_out, e_out, crop, (float)sk, (float)sg, (float)jac,
+                                                                      gamma * p->cx, gamma * p->cy, meta_out);
   }
   STS_CUDA_OK(cudaStreamSynchronize(st));
   N_VDestroy_Sts(x);

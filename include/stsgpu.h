@@ -311,22 +311,28 @@ int STS_NetFree(STS_Net* net);
 /* weights: 9 layers (W_in, W_d1, W_d2, W_d3, W_c, W_u2, W_u1, W_u0, W_out) x [16][16][3][3] FP32 */
 int STS_NetSetWeights(STS_Net net, const float* w);
 int STS_NetGetWeights(STS_Net net, float* w);
-/* z = jacobi * net(scale * r) / scale on device arrays of n x n doubles */
+/* z = jacobi * (r + net(scale * r) / scale) on device arrays of n x n doubles (the Jacobi
+ * preconditioner plus the learned correction) */
 int STS_NetApply(STS_Net net, int n, const double* r, double* z, double sk, double sg, double jacobi,
                  double scale);
-/* one sample: loss = 0.5 ||M r - e||^2 / ||e||^2 and its weight gradient (host FP32 array) */
+/* one sample (scale 1): loss = 0.5 (z - e)^T M (z - e) / (e^T M e) with M = I - gamma A on the
+ * n x n field (zero outside; gcx = gamma kx/dx^2, gcy = gamma ky/dy^2) and its weight
+ * gradient (host FP32 array); z = jacobi (r + net(r)) */
 int STS_NetLossGrad(STS_Net net, int n, const double* r, const float* e, double sk, double sg,
-                    double jacobi, double* loss, float* grad);
+                    double jacobi, double gcx, double gcy, double* loss, float* grad);
 /* Adam over device samples r, e (nsamples x n x n FP32) with per-sample
- * meta = {sk, sg, jacobi, scale, 1/||e||^2}, minibatches of `batch` samples run batched */
+ * meta = {sk, sg, jacobi, scale, 1/(e^T M e), gcx, gcy} (7 floats, as STS_HarvestPCGPairs
+ * writes it), minibatches of `batch` samples run batched */
 int STS_NetTrain(STS_Net net, int n, int nsamples, const float* r, const float* e, const float* meta,
                  int epochs, int batch, float lr, unsigned long long seed, double* last_loss);
 /* residual/correction pairs from a converged fused Jacobi-PCG solve of (I - gamma A) x = b:
- * every `every` iterations, `ncrops` crops (crop x crop, fixed positions) of r_k and of
- * e_k = x* - x_k are appended to r_out / e_out (device FP32, capacity max_pairs) */
+ * after every `every`-th batch of 8 iterations, `ncrops` crops (crop x crop, seeded fixed
+ * positions) of r_k and of e_k = x* - x_k are appended to r_out / e_out (device FP32,
+ * capacity max_pairs), and their training metadata (7 floats each) to meta_out (device,
+ * may be NULL) */
 int STS_HarvestPCGPairs(STS_Problem p, double gamma, N_Vector b, int ncrops, int crop, int every,
-                        int max_pairs, float* r_out, float* e_out, unsigned long long seed,
-                        int* npairs, int* iters);
+                        int max_pairs, float* r_out, float* e_out, float* meta_out,
+                        unsigned long long seed, int* npairs, int* iters);
 /* flexible CG with the network as preconditioner, x0 = 0, stop at ||r|| <= tol ||b||; on
  * stagnation (maxit) or breakdown it falls back to Jacobi-PCG on the remaining correction.
  * Returns 0 converged, 2 converged through the fallback, 1 not converged, < 0 error; iters

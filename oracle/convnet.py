@@ -13,10 +13,17 @@ Architecture (4 levels, C = 16 channels, 3x3 convolutions with zero padding, no 
     b2 = conv(up(a3) + a2, W_u2)            C -> C   at n/4
     b1 = conv(up(b2) + a1, W_u1)            C -> C   at n/2
     b0 = conv(up(b1) + a0, W_u0)            C -> C   at n
-    z  = conv(b0, W_out) * jacobi           C -> 1   at n   (scaled by the Jacobi factor)
+    z  = (r + conv(b0, W_out)) * jacobi     C -> 1   at n   (Jacobi skip: z = D r + D N(r))
 pool = 2x2 mean; up = nearest-neighbour copy (its adjoint is the 2x2 sum). Weights are
-stored in BF16 (rounded to nearest even from FP32), activations in FP32 with FP32
-accumulation on the GPU; this reference computes in FP64 from the same BF16 weights.
+stored in BF16 (rounded to nearest even from FP32), activations in BF16 with FP32
+accumulation on the GPU; this reference computes in FP64 from the same BF16 weights. The
+skip term D r makes the untrained network (small W_out) the Jacobi preconditioner, and the
+network learns the correction beyond it.
+
+Loss (energy norm of the shifted operator M = I - gamma A, the norm CG minimises): with
+d = z - e, L = 0.5 d^T M d / (e^T M e), M applied on the crop with zero values outside it:
+(M d)_ij = (1 + 2 (gcx + gcy)) d_ij - gcx (d_i-1,j + d_i+1,j) - gcy (d_i,j-1 + d_i,j+1),
+gcx = gamma kx / dx^2, gcy = gamma ky / dy^2; dL/dz = M d / (e^T M e).
 
 forward() returns the output and a cache; backward() returns dL/dW for every weight given
 dL/dz, written out by hand (the GPU kernels are checked against it).
@@ -119,7 +126,7 @@ def forward(W, r, sk, sg, jacobi):
     b1 = conv(s1, Wd["W_u1"])
     s0 = up(b1) + a0
     b0 = conv(s0, Wd["W_u0"])
-    z = conv(b0, Wd["W_out"])[0] * jacobi
+    z = (conv(b0, Wd["W_out"])[0] + x[0]) * jacobi
     cache = dict(x=x, a0=a0, p0=p0, a1=a1, p1=p1, a2=a2, p2=p2, c3=c3, a3=a3, s2=s2, b2=b2, s1=s1,
                  b1=b1, s0=s0, b0=b0, Wd=Wd, jacobi=jacobi)
     return z, cache
@@ -151,10 +158,19 @@ def backward(cache, gz):
     return dW
 
 
-def loss_and_grad(W, r, e, sk, sg, jacobi):
-    """L = 0.5 ||M r - e||^2 / ||e||^2 and its weight gradients."""
+def apply_M(d, gcx, gcy):
+    """(I - gamma A) d on one crop, zero outside it (axis 0 = y rows, axis 1 = x columns)."""
+    p = np.zeros((d.shape[0] + 2, d.shape[1] + 2))
+    p[1:-1, 1:-1] = d
+    return (1.0 + 2.0 * (gcx + gcy)) * d - gcx * (p[1:-1, :-2] + p[1:-1, 2:]) \
+        - gcy * (p[:-2, 1:-1] + p[2:, 1:-1])
+
+
+def loss_and_grad(W, r, e, sk, sg, jacobi, gcx, gcy):
+    """L = 0.5 (z - e)^T M (z - e) / (e^T M e) and its weight gradients."""
     z, cache = forward(W, r, sk, sg, jacobi)
     d = z - e
-    den = float(np.sum(e * e))
-    L = 0.5 * float(np.sum(d * d)) / den
-    return L, backward(cache, d / den)
+    den = float(np.sum(e * apply_M(e, gcx, gcy)))
+    Md = apply_M(d, gcx, gcy)
+    L = 0.5 * float(np.sum(d * Md)) / den
+    return L, backward(cache, Md / den)

@@ -94,6 +94,8 @@ def lib():
         L.orc_stage_coeffs.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]
         L.orc_stages_needed.restype = C.c_int
         L.orc_stages_needed.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, _dp]
+        L.orc_pow.restype = C.c_double
+        L.orc_pow.argtypes = [C.c_double, C.c_double]
         L.orc_controller.restype = C.c_double
         L.orc_controller.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                      C.c_long]

@@ -648,6 +648,48 @@ int orc_stages_needed(int method, double h, double rho, int smax, double* hmax)
 #define ORD 3.0
 #define BIAS 1.5
 #define TINYE 1.0e-10
+/* Deterministic pow for the controllers, restated from the product's portable math (the
+ * same IEEE operation sequence runs in the device batch kernel): log x = k ln2 + 2 atanh(f),
+ * x = m 2^k, m in [sqrt(1/2), sqrt(2)), f = (m-1)/(m+1), series to f^25; exp y = 2^k e^r,
+ * k = rint(y / ln2), r = y - k ln2 (two-part ln2), Taylor series to r^17/17!. */
+static const double ORC_LN2_HI = 0.6931471805599453094, ORC_LN2_LO = 2.3190468138462996e-17,
+                    ORC_INV_LN2 = 1.4426950408889634074;
+
+static double orc_log(double x)
+{
+  if (!(x > 0.0)) return x == 0.0 ? -HUGE_VAL : NAN;
+  if (x == HUGE_VAL) return x;
+  int k    = 0;
+  double m = frexp(x, &k);
+  if (m < 0.70710678118654752440)
+  {
+    m = m * 2.0;
+    k = k - 1;
+  }
+  double f = (m - 1.0) / (m + 1.0), f2 = f * f, s = 1.0 / 25.0;
+  for (int i = 11; i >= 0; --i) s = fma(s, f2, 1.0 / (double)(2 * i + 1));
+  double lm = 2.0 * f * s, kd = (double)k;
+  return fma(kd, ORC_LN2_HI, fma(kd, ORC_LN2_LO, lm));
+}
+
+static double orc_exp(double y)
+{
+  if (y != y) return y;
+  if (y > 709.78) return HUGE_VAL;
+  if (y < -745.2) return 0.0;
+  double k = rint(y * ORC_INV_LN2);
+  double r = fma(-k, ORC_LN2_HI, y);
+  r        = fma(-k, ORC_LN2_LO, r);
+  double c[18];
+  c[0] = 1.0;
+  for (int i = 1; i < 18; ++i) c[i] = c[i - 1] / (double)i;
+  double s = c[17];
+  for (int i = 16; i >= 0; --i) s = fma(s, r, c[i]);
+  return ldexp(s, (int)k);
+}
+
+double orc_pow(double x, double y) { return orc_exp(y * orc_log(x)); }
+
 double orc_controller(int controller, double h, double dsm, double ep1, double ep2, long nhist)
 {
   double e1 = BIAS * dsm;
@@ -658,16 +700,16 @@ double orc_controller(int controller, double h, double dsm, double ep1, double e
   if (e3 < TINYE) e3 = TINYE;
   if (controller == 0)
   {
-    if (nhist < 1) return h * pow(e1, -0.58 / ORD);
-    if (nhist < 2) return h * pow(e1, -0.58 / ORD) * pow(e2, 0.21 / ORD);
-    return h * pow(e1, -0.58 / ORD) * pow(e2, 0.21 / ORD) * pow(e3, -0.1 / ORD);
+    if (nhist < 1) return h * orc_pow(e1, -0.58 / ORD);
+    if (nhist < 2) return h * orc_pow(e1, -0.58 / ORD) * orc_pow(e2, 0.21 / ORD);
+    return h * orc_pow(e1, -0.58 / ORD) * orc_pow(e2, 0.21 / ORD) * orc_pow(e3, -0.1 / ORD);
   }
   if (controller == 1)
   {
-    if (nhist < 1) return h * pow(e1, -0.8 / ORD);
-    return h * pow(e1, -0.8 / ORD) * pow(e2, 0.31 / ORD);
+    if (nhist < 1) return h * orc_pow(e1, -0.8 / ORD);
+    return h * orc_pow(e1, -0.8 / ORD) * orc_pow(e2, 0.31 / ORD);
   }
-  return h * pow(e1, -1.0 / ORD);
+  return h * orc_pow(e1, -1.0 / ORD);
 }
 
 #define SAFETY 0.96
@@ -867,7 +909,7 @@ static double initial_step(const orc_prob* p, const orc_opts* o, double t0, cons
   (*nfe)++;
   double d2  = wrms_diff_ewt(o, F1, F0, y0, n) / h0;
   double dm  = d1 > d2 ? d1 : d2;
-  double h1  = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : pow(0.01 / dm, 1.0 / ORD);
+  double h1  = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : orc_pow(0.01 / dm, 1.0 / ORD);
   if (!(h1 > 0.0) || !(h1 < INFINITY)) h1 = h0;
   double h   = (100.0 * h0 < h1) ? 100.0 * h0 : h1;
   if (h > tdist) h = tdist;

@@ -80,6 +80,7 @@ int orc_power_iteration(const orc_prob* p, double* v, int maxiters, double relto
 int orc_stage_coeffs(int method, int s, double* mu, double* nu, double* mus, double* ajm1,
                      double* cjm1);
 int orc_stages_needed(int method, double h, double rho, int smax, double* hmax);
+double orc_pow(double x, double y); /* deterministic pow of the controllers */
 double orc_controller(int controller, double h, double dsm, double ep1, double ep2, long nhist);
 
 void orc_state_init(orc_state* st, double t0);

@@ -30,21 +30,52 @@ def test_linear_in_the_residual():
     assert np.allclose(z12, 2.0 * z1 - 3.0 * z2, rtol=1e-12, atol=1e-12)
 
 
+def test_zero_network_is_jacobi():
+    W = {k: np.zeros_like(v) for k, v in convnet.init_weights(seed=2).items()}
+    r = np.random.default_rng(3).standard_normal((16, 16))
+    z, _ = convnet.forward(W, r, 0.1, 0.2, 0.25)
+    assert np.array_equal(z, 0.25 * r)
+
+
+def test_energy_operator_is_the_shifted_stencil():
+    rng = np.random.default_rng(4)
+    d = rng.standard_normal((8, 6))
+    gcx, gcy = 3.0, 0.5
+    Md = convnet.apply_M(d, gcx, gcy)
+    # dense (I - gamma A) with the Dirichlet 5-point stencil, x fastest
+    ny, nx = d.shape
+    M = np.zeros((ny * nx, ny * nx))
+    for j in range(ny):
+        for i in range(nx):
+            k = j * nx + i
+            M[k, k] = 1 + 2 * (gcx + gcy)
+            if i > 0:
+                M[k, k - 1] = -gcx
+            if i < nx - 1:
+                M[k, k + 1] = -gcx
+            if j > 0:
+                M[k, k - nx] = -gcy
+            if j < ny - 1:
+                M[k, k + nx] = -gcy
+    assert np.allclose(Md.ravel(), M @ d.ravel(), rtol=1e-14, atol=1e-14)
+    assert np.all(np.linalg.eigvalsh(M) > 0)
+
+
 def test_gradients_match_finite_differences():
     W = convnet.init_weights(seed=5)
     rng = np.random.default_rng(1)
     n = 16
     r = rng.standard_normal((n, n))
     e = rng.standard_normal((n, n))
-    sk, sg, jac = 0.2, -0.6, 0.9
-    _, g = convnet.loss_and_grad(W, r, e, sk, sg, jac)
+    sk, sg, jac, gcx, gcy = 0.2, -0.6, 0.9, 40.0, 4.0
+    _, g = convnet.loss_and_grad(W, r, e, sk, sg, jac, gcx, gcy)
     h = 1e-6
     for nm in convnet.NAMES:
         Wd = {k: v.astype(np.float64) for k, v in W.items()}
         idx = tuple(rng.integers(0, s) for s in convnet.shape(nm))
         Wd[nm][idx] += h
-        lp, _ = convnet.loss_and_grad(Wd, r, e, sk, sg, jac)
+        lp, _ = convnet.loss_and_grad(Wd, r, e, sk, sg, jac, gcx, gcy)
         Wd[nm][idx] -= 2 * h
-        lm, _ = convnet.loss_and_grad(Wd, r, e, sk, sg, jac)
+        lm, _ = convnet.loss_and_grad(Wd, r, e, sk, sg, jac, gcx, gcy)
         fd = (lp - lm) / (2 * h)
         assert abs(fd - g[nm][idx]) <= 1e-6 * max(1.0, abs(fd)), nm

@@ -47,8 +47,11 @@ def test_cli_manufactured_rkc_with_error_mode(stslib, oracle):
     # the same run on the oracle (same outputs times, same controller)
     P = oracle.Problem(oracle.MANUFACTURED, 64, 48)
     J = oracle.Integrator(P, P.initial(), method=oracle.RKC, rtol=1e-6, atol=1e-10, controller=2)
-    for k in range(1, 6):
-        assert J.evolve(0.05 * k / 5) == 0
+    # output times accumulate like the driver's (main.cpp: tout += dTout, capped at tf)
+    dt, tout = 0.05 / 5, 0.05 / 5
+    for k in range(5):
+        assert J.evolve(tout) == 0
+        tout = min(tout + dt, 0.05)
     assert st["Steps"] == J.stats()["nst"]
     ex = P.exact(0.05)
     rel = np.linalg.norm(J.y - ex) / np.linalg.norm(ex)

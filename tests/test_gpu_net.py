@@ -73,13 +73,13 @@ def test_gradients_match_oracle(ctx, weights):
     rng = np.random.default_rng(11)
     r = rng.standard_normal((n, n))
     e = rng.standard_normal((n, n)).astype(np.float32)
-    sk, sg, jac = 0.4, -0.2, 0.5
+    sk, sg, jac, gcx, gcy = 0.4, -0.2, 0.5, 24.0, 3.0
     net = sts.Net(ctx, n, seed=0)
     net.set_weights(weights)
     rv = sts.NVector.from_numpy(ctx, r)
     et = _f32_dev(e)
-    loss, grad = net.loss_grad(n, rv.ptr, et.data_ptr(), sk, sg, jac)
-    lref, gref = convnet.loss_and_grad(weights, r, e.astype(np.float64), sk, sg, jac)
+    loss, grad = net.loss_grad(n, rv.ptr, et.data_ptr(), sk, sg, jac, gcx, gcy)
+    lref, gref = convnet.loss_and_grad(weights, r, e.astype(np.float64), sk, sg, jac, gcx, gcy)
     assert abs(loss - lref) / lref < FWD_TOL
     for nm in convnet.NAMES:
         co, ci = convnet.shape(nm)[:2]
@@ -95,18 +95,13 @@ def _harvest(ctx, n, ky, gam_rel, crop, ncrops, every, max_pairs, seed):
     b = sts.NVector.from_numpy(ctx, _smooth_field(n, np.random.default_rng(seed)))
     r_t = torch.empty(max_pairs * crop * crop, dtype=torch.float32, device="cuda")
     e_t = torch.empty_like(r_t)
+    meta = torch.empty(max_pairs * 7, dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
     npairs, iters = sts.harvest_pcg_pairs(p, gamma, b, ncrops, crop, every, max_pairs,
-                                          r_t.data_ptr(), e_t.data_ptr(), seed)
+                                          r_t.data_ptr(), e_t.data_ptr(), meta.data_ptr(), seed)
     r_t = r_t[:npairs * crop * crop].view(npairs, -1)
     e_t = e_t[:npairs * crop * crop].view(npairs, -1)
-    sk, sg, jac = sts.net_features(1.0, ky, gamma, dx)
-    meta = torch.empty(npairs, 5, dtype=torch.float32, device="cuda")
-    meta[:, 0] = sk
-    meta[:, 1] = sg
-    meta[:, 2] = jac
-    meta[:, 3] = torch.rsqrt((r_t.double() ** 2).mean(1)).float()
-    meta[:, 4] = (1.0 / (e_t.double() ** 2).sum(1)).float()
+    meta = meta[:npairs * 7].view(npairs, 7)
     torch.cuda.synchronize()
     return p, b, gamma, r_t, e_t, meta, iters
 
@@ -117,6 +112,14 @@ def test_harvest_pairs_satisfy_the_system(ctx):
     p, b, gamma, r_t, e_t, meta, iters = _harvest(ctx, n, 0.3, 300.0, crop, 2, 2, 16, 5)
     assert r_t.shape[0] == 16 and iters > 16
     dx = 1.0 / (n + 1)
+    # metadata: features of the system, 1/rms(r) and 1/(e^T M e) of each crop
+    sk, sg, jac, gcx, gcy = sts.net_features(1.0, 0.3, gamma, dx)
+    m = meta.double().cpu().numpy()
+    assert np.allclose(m[:, [0, 1, 2, 5, 6]], [sk, sg, jac, gcx, gcy], rtol=1e-6)
+    r0 = r_t[0].double().cpu().numpy().reshape(crop, crop)
+    e0 = e_t[0].double().cpu().numpy().reshape(crop, crop)
+    assert np.isclose(m[0, 3], 1.0 / np.sqrt(np.mean(r0 ** 2)), rtol=1e-5)
+    assert np.isclose(m[0, 4], 1.0 / np.sum(e0 * convnet.apply_M(e0, gcx, gcy)), rtol=1e-5)
     cx, cy = 1.0 / dx ** 2, 0.3 / dx ** 2
     for k in range(4):
         e = e_t[k].double().cpu().numpy().reshape(crop, crop)

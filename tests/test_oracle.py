@@ -7,6 +7,15 @@ import os
 from fractions import Fraction
 
 import numpy as np
+
+
+def mpmath_pow(x, y):
+    """x**y to double precision through exact rational arithmetic on a 60-digit decimal
+    expansion (python's decimal module), independent of the C library."""
+    import decimal
+    with decimal.localcontext() as c:
+        c.prec = 60
+        return float((decimal.Decimal(x).ln() * decimal.Decimal(y)).exp())
 import pytest
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -262,3 +271,17 @@ def test_library_exports_every_declared_symbol(stslib):
         assert hasattr(L, n), n
     declared = {s[0] for s in stslib.SIGNATURES}
     assert set(names) == declared
+
+
+def test_deterministic_pow_accuracy(oracle):
+    """The controllers' pow (series log/exp built from exactly rounded operations) stays within
+    a few ulp of the exact value over the controllers' range."""
+    L = oracle.lib()
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([10.0 ** rng.uniform(-10, 10, 2000), [1.0, 0.5, 2.0, 1e-10, 1.5e-10, 7.3]])
+    for y in (-0.58 / 3, 0.21 / 3, -0.1 / 3, -0.8 / 3, 0.31 / 3, -1.0 / 3, 1.0 / 3, 2.5):
+        got = np.array([L.orc_pow(float(x), y) for x in xs])
+        want = np.array([float(mpmath_pow(x, y)) for x in xs])
+        # the rounding of y log x is amplified by |y log x| in exp: a few ulp times (1 + |y log x|)
+        bound = 4.5e-16 * (1.0 + np.abs(y * np.log(xs)))
+        assert np.all(np.abs(got - want) / want < bound)
