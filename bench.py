@@ -541,6 +541,32 @@ def run_precond(args):
     print(json.dumps(line), flush=True)
 
 
+def run_precond_profile(args):
+    """A short FCG + network solve and a short Jacobi-PCG solve on one 2048^2 system (16
+    iterations each, untrained network), for kernel launch lists."""
+    import numpy as np
+    import ceda_demonstrations_gb300 as sts
+    ctx = sts.Context(0)
+    n = args.precond_n
+    rng = np.random.default_rng(5)
+    P = sts.Problem(ctx, sts.UNFORCED, n, n, 1.0, 0.1)
+    b = sts.NVector.from_numpy(ctx, sts.smooth_field(n, rng))
+    x = P.vector()
+    net = sts.Net(ctx, n, seed=1)
+    gh = 1e-3
+    for _ in range(args.warmup):
+        sts.fcg_solve(P, gh, net, b, x, tol=1e-14, maxit=16)
+        sts.implicit_solve_pcg(P, gh, b, x, tol=1e-14, maxit=16)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    it1, _, _ = sts.fcg_solve(P, gh, net, b, x, tol=1e-14, maxit=16)
+    t1 = time.perf_counter()
+    it2, _, _ = sts.implicit_solve_pcg(P, gh, b, x, tol=1e-14, maxit=16)
+    t2 = time.perf_counter()
+    print(json.dumps({"fcg_iters": it1, "fcg_ms_per_iter": 1e3 * (t1 - t0) / max(1, it1),
+                      "pcg_iters": it2, "pcg_ms_per_iter": 1e3 * (t2 - t1) / max(1, it2)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -561,6 +587,7 @@ def main():
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-tf", type=float, default=0.01)
     ap.add_argument("--precond", action="store_true")
+    ap.add_argument("--precond-profile", action="store_true")
     ap.add_argument("--precond-n", type=int, default=2048)
     ap.add_argument("--precond-crop", type=int, default=128)
     ap.add_argument("--precond-crops", type=int, default=4)
@@ -580,6 +607,8 @@ def main():
         run_batch(args)
     elif args.precond:
         run_precond(args)
+    elif args.precond_profile:
+        run_precond_profile(args)
     else:
         run_gpu(args)
 

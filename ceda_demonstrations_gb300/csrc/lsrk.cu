@@ -399,18 +399,21 @@ static void autotune_stage32(LSRKMem* m, STS_Problem p)
   a->gnf = -0.9f;
   a->gFf = 1e-5f;
   cudaMemcpyAsync(m->d_par, m->h_par, m->par_bytes, cudaMemcpyHostToDevice, st);
+  // scratch only: the stage buffers and the FP32 F of the other parity (the current one may
+  // hold a restored or reset state)
+  const int fpar = 1 - m->par;
   cudaMemsetAsync(m->D[0], 0, m->n * sizeof(float), st);
   cudaMemsetAsync(m->D[1], 0, m->n * sizeof(float), st);
-  cudaMemsetAsync(m->Ffb[m->par], 0, m->n * sizeof(float), st);
+  cudaMemsetAsync(m->Ffb[fpar], 0, m->n * sizeof(float), st);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   double best = 1e30;
   for (int v = -1; v < TMA_STAGE32_NVARIANTS; ++v)
   {
-    for (int k = 0; k < 2; ++k) launch_stage32_idx(m, p, dstage(m) + 2, 0, 1, m->par, 2, v);
+    for (int k = 0; k < 2; ++k) launch_stage32_idx(m, p, dstage(m) + 2, 0, 1, fpar, 2, v);
     cudaEventRecord(e0, st);
-    for (int k = 0; k < 5; ++k) launch_stage32_idx(m, p, dstage(m) + 2, 0, 1, m->par, 2, v);
+    for (int k = 0; k < 5; ++k) launch_stage32_idx(m, p, dstage(m) + 2, 0, 1, fpar, 2, v);
     cudaEventRecord(e1, st);
     if (cudaEventSynchronize(e1) != cudaSuccess) break;
     float ms = 0.f;
