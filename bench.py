@@ -410,6 +410,7 @@ def run_batch(args):
     nfe = [B.stats(i)["nfe"] for i in range(len(inst))]
     nst = [B.stats(i)["nst"] for i in range(len(inst))]
     dof_stages = float(sum(inst[i][0] ** 2 * nfe[i] for i in range(len(inst))))
+    per_inst = sorted((inst[i][0] ** 2 * nfe[i] for i in range(len(inst))), reverse=True)
     # CPU oracle on a sample of instances (all host threads), and parity on that sample
     sample = list(range(0, len(inst), max(1, len(inst) // 16)))[:16]
     t0 = time.perf_counter()
@@ -429,6 +430,8 @@ def run_batch(args):
         "value": dof_stages / (ms / 1e3), "unit": "DOF-stages/s", "time_s": ms / 1e3,
         "total_dof": int(B.total), "dof_stages": dof_stages, "steps_total": int(sum(nst)),
         "steps_max": int(max(nst)), "launch": {"threads": th, "ctas_per_sm": cp, "probe_ms": tune_ms},
+        "largest_instance_dof_stages": float(per_inst[0]),
+        "largest_instance_share": float(per_inst[0]) / dof_stages,
         "dtype": "f64", "data": "synthetic (seeded sine-mode initial states, seed 20261203)",
         "parity_sample_max_rel_l2_vs_oracle": maxrel,
         "cpu_baseline": {"value": cpu_dof / cpu_s, "unit": "DOF-stages/s", "cores": po.lib().orc_nthreads(),

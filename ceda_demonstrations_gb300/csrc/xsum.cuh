@@ -1,7 +1,7 @@
 // Exact, order-independent accumulation of doubles (host + device).
 //
 // Every term x is truncated toward zero to a multiple of 2^-160 and added exactly into
-// eight signed 64-bit limbs, limb k carrying 32-bit digits of weight 2^(32k-160). A term
+// ten signed 64-bit limbs, limb k carrying 32-bit digits of weight 2^(32k-160). A term
 // touches at most three limbs and never propagates a carry, so per-thread accumulators,
 // warp shuffles, block trees and global atomics can combine partial sums in any order and
 // the total is the same integer. The result is that integer rounded once to the nearest
@@ -76,19 +76,40 @@ XS_HD void add(Limbs& a, double x, unsigned& flags)
     m  = (sh <= -64) ? 0ULL : (m >> (-sh));
     sh = 0;
   }
-  const int k  = sh >> 5;
+  const int k  = sh >> 5; // 0 .. 7 (sh <= 235)
   const int bs = sh & 31;
   // v = m << bs spans up to 85 bits: digits d0 | d1 | d2
   const unsigned long long lo = m << bs;
   const unsigned long long hi = bs ? (m >> (64 - bs)) : 0ULL;
-  const long long d0          = (long long)(lo & 0xffffffffULL);
-  const long long d1          = (long long)(lo >> 32);
-  const long long d2          = (long long)hi;
-#pragma unroll
-  for (int L = 0; L < NL; ++L)
+  long long d0                = (long long)(lo & 0xffffffffULL);
+  long long d1                = (long long)(lo >> 32);
+  long long d2                = (long long)hi;
+  if (neg)
   {
-    long long v = (L == k) ? d0 : (L == k + 1) ? d1 : (L == k + 2) ? d2 : 0LL;
-    a.l[L] += neg ? -v : v;
+    d0 = -d0;
+    d1 = -d1;
+    d2 = -d2;
+  }
+  // three adds into limbs k, k+1, k+2; one branch per term (the terms of one warp usually
+  // share k) instead of a select on every limb
+  switch (k)
+  {
+#define XS_CASE(K)                                                                                                   \
+  case K:                                                                                                            \
+    a.l[K] += d0;                                                                                                    \
+    a.l[K + 1] += d1;                                                                                                \
+    a.l[K + 2] += d2;                                                                                                \
+    break;
+    XS_CASE(0)
+    XS_CASE(1)
+    XS_CASE(2)
+    XS_CASE(3)
+    XS_CASE(4)
+    XS_CASE(5)
+    XS_CASE(6)
+    XS_CASE(7)
+#undef XS_CASE
+  default: break;
   }
 }
 
