@@ -164,6 +164,8 @@ SIGNATURES = [
     ("STS_BatchSetLaunch", C.c_int, [_vp, C.c_int, C.c_int]),
     ("STS_BatchAutotune", C.c_int, [_vp, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int,
                                     _ip, _ip, _dp]),
+    ("STS_BatchSetCluster", C.c_int, [_vp, C.c_int, C.c_int]),
+    ("STS_BatchGetLaunch", C.c_int, [_vp, _ip, _ip, _ip, _ip]),
     ("STS_LSRKStepWriteCheckpoint", C.c_int, [_vp, C.c_char_p]),
     ("STS_LSRKStepReadCheckpoint", C.c_int, [_vp, C.c_char_p]),
     ("STS_NetCreate", _vp, [_vp, C.c_int, C.c_ulonglong]),
@@ -667,20 +669,30 @@ class Batch:
                 cache = json.load(f)
             if key in cache:
                 th, cp = cache[key]["threads"], cache[key]["ctas_per_sm"]
-                self.set_launch(th, cp)
+                self.set_launch(th, cp, cache[key].get("cluster", 1))
                 return th, cp, cache[key]["probe_ms"]
         th, cp, ms = C.c_int(), C.c_int(), C.c_double()
         if lib().STS_BatchAutotune(self.h, tf_probe, method, rtol, atol, smax, C.byref(th),
                                    C.byref(cp), C.byref(ms)) != 0:
             _err("STS_BatchAutotune")
         if cache_file:
-            cache[key] = {"threads": th.value, "ctas_per_sm": cp.value, "probe_ms": ms.value}
+            cache[key] = {"threads": th.value, "ctas_per_sm": cp.value, "cluster": self.launch()[2],
+                          "probe_ms": ms.value}
             with open(cache_file, "w") as f:
                 json.dump(cache, f, indent=1, sort_keys=True)
         return th.value, cp.value, ms.value
 
-    def set_launch(self, threads, ctas_per_sm):
-        return lib().STS_BatchSetLaunch(self.h, threads, ctas_per_sm)
+    def set_launch(self, threads, ctas_per_sm, cluster=None, big_n=256):
+        rc = lib().STS_BatchSetLaunch(self.h, threads, ctas_per_sm)
+        if rc == 0 and cluster is not None:
+            rc = lib().STS_BatchSetCluster(self.h, cluster, big_n)
+        return rc
+
+    def launch(self):
+        """(threads per CTA, CTAs per SM, cluster size, smallest n on clusters)"""
+        v = [C.c_int() for _ in range(4)]
+        lib().STS_BatchGetLaunch(self.h, *[C.byref(x) for x in v])
+        return tuple(x.value for x in v)
 
     def state(self):
         out = np.empty(self.total)

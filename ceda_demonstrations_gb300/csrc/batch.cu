@@ -13,6 +13,7 @@
 // the arithmetic of the single-problem integrator and the CPU oracle: stage coefficients from
 // the host's table, IEEE sqrt/divide, and the deterministic pow of portable_math.cuh in the
 // controller, so each instance follows the oracle's step sequence and matches it bit for bit.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -68,6 +69,16 @@ struct STS_Batch_ {
   double last_ms   = 0.0;
   CoefT* dcoef     = nullptr; // stage-coefficient table of (coef_method, coef_smax)
   int coef_method = -1, coef_smax = -1;
+  // instances with n >= big_n run on clusters of `cluster` CTAs (1: all on single CTAs)
+  int cluster      = 1;
+  int big_n        = 256;
+  int nbig         = 0;
+  double big_share = 0.0;      // estimated cost share of the clustered group
+  int* dorder_big   = nullptr; // cost-ordered indices of each group
+  int* dorder_small = nullptr;
+  cudaStream_t side = nullptr; // second stream for the single-CTA group
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  std::vector<double> cost;
 };
 
 // ---------------------------------------------------------------------------------------
@@ -114,13 +125,26 @@ __device__ int d_stages(int method, double h, double rho, int smax, double* hmax
   return (int)ss;
 }
 
-// CTA-wide exact sum of per-thread limbs; returns the rounded total to every thread
-template <int NT>
-__device__ double cta_exact_sum(xsum::Limbs& a, unsigned flags, long long (*sm)[xsum::NL], unsigned* sflags,
-                                double* sres)
+// Barrier over the CTAs that share an instance: the whole thread-block cluster (barrier.cluster
+// with release/acquire semantics, so the other CTAs' global stores of the previous sweep are
+// visible), or the CTA when an instance has one CTA.
+template <int CL>
+__device__ __forceinline__ void inst_sync()
+{
+  if constexpr (CL > 1) cooperative_groups::this_cluster().sync();
+  else __syncthreads();
+}
+
+// Exact sum over all threads of the instance's CTAs, returned to every thread. Each CTA
+// combines its threads' limbs (warp shuffles + shared memory) into climb[]; with a cluster,
+// every CTA then reads all CTAs' climb[] through distributed shared memory and adds them in
+// rank order, so all CTAs obtain the same integer and the same rounded value.
+template <int NT, int CL>
+__device__ double inst_exact_sum(xsum::Limbs& a, unsigned flags, long long (*sm)[xsum::NL], long long* climb,
+                                 unsigned* cflags, double* sres)
 {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) *sflags = 0;
+  if (tid == 0) *cflags = 0;
 #pragma unroll
   for (int k = 0; k < xsum::NL; ++k)
   {
@@ -130,34 +154,53 @@ __device__ double cta_exact_sum(xsum::Limbs& a, unsigned flags, long long (*sm)[
     if (lane == 0) sm[warp][k] = v;
   }
   __syncthreads();
-  if (flags) atomicOr(sflags, flags);
-  __syncthreads();
+  if (flags) atomicOr(cflags, flags);
+  if (tid < xsum::NL)
+  {
+    long long v = 0;
+    for (int w = 0; w < NT / 32; ++w) v += sm[w][tid];
+    climb[tid] = v;
+  }
+  inst_sync<CL>(); // climb[] and cflags of every CTA complete
   if (tid == 0)
   {
     long long tot[xsum::NL];
-    for (int k = 0; k < xsum::NL; ++k)
+    unsigned fl = 0;
+    if constexpr (CL > 1)
     {
-      long long v = 0;
-      for (int w = 0; w < NT / 32; ++w) v += sm[w][k];
-      tot[k] = v;
+      cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+      for (int k = 0; k < xsum::NL; ++k) tot[k] = 0;
+      for (int r = 0; r < CL; ++r)
+      {
+        const long long* rl = cl.map_shared_rank(climb, r);
+        for (int k = 0; k < xsum::NL; ++k) tot[k] += rl[k];
+        fl |= *cl.map_shared_rank(cflags, r);
+      }
     }
-    *sres = xsum::finalize(tot, *sflags);
+    else
+    {
+      for (int k = 0; k < xsum::NL; ++k) tot[k] = climb[k];
+      fl = *cflags;
+    }
+    *sres = xsum::finalize(tot, fl);
   }
-  __syncthreads();
-  const double r = *sres;
-  __syncthreads();
-  return r;
+  inst_sync<CL>(); // every CTA has read the others' climb[] before they are reused
+  return *sres;
 }
 
-__device__ __forceinline__ double lap(const double* __restrict__ u, int n, int i, int j, double cx, double cy,
-                                      double cc)
+// Stencil-row load: rows owned by another CTA of the cluster are read through L2 (ld.cg),
+// so no stale L1 line of an earlier sweep is used.
+__device__ __forceinline__ double ldrow(const double* p, bool foreign) { return foreign ? __ldcg(p) : *p; }
+
+__device__ __forceinline__ double lap(const double* __restrict__ u, int n, int i, int j, int j0, int j1, double cx,
+                                      double cy, double cc)
 {
   const long long k = (long long)j * n + i;
   const double uc = u[k];
   const double uw = (i > 0) ? u[k - 1] : 0.0;
   const double ue = (i < n - 1) ? u[k + 1] : 0.0;
-  const double us = (j > 0) ? u[k - n] : 0.0;
-  const double un = (j < n - 1) ? u[k + n] : 0.0;
+  const double us = (j > 0) ? ldrow(&u[k - n], j - 1 < j0) : 0.0;
+  const double un = (j < n - 1) ? ldrow(&u[k + n], j + 1 >= j1) : 0.0;
   const double sx = uw + ue, sy = us + un;
   double acc      = cc * uc;
   acc             = __fma_rn(cx, sx, acc);
@@ -165,27 +208,36 @@ __device__ __forceinline__ double lap(const double* __restrict__ u, int n, int i
   return acc;
 }
 
-template <int NT>
-__global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts, const int* __restrict__ order,
+// CL CTAs (a thread-block cluster when CL > 1) integrate one instance together: CTA `rank`
+// owns rows [j0, j1) of every sweep; sweeps are separated by cluster barriers and the exact
+// reductions are combined through distributed shared memory. Every CTA of the cluster
+// evaluates the step control from the same reduced values, so all take the same decisions.
+template <int NT, int CL>
+__global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restrict__ insts, const int* __restrict__ order,
                                                    int ninst, int* queue, double* __restrict__ yall,
                                                    double* __restrict__ work, long long total, BatchParams prm)
 {
   __shared__ long long sm[NT / 32][xsum::NL];
+  __shared__ long long climb[xsum::NL];
   __shared__ unsigned sflags;
   __shared__ double sres;
   __shared__ int sidx;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = NT / 32;
+  int rank = 0;
+  if constexpr (CL > 1) rank = (int)cooperative_groups::this_cluster().block_rank();
 
   for (;;)
   {
-    if (tid == 0) sidx = atomicAdd(queue, 1);
-    __syncthreads();
-    const int idx = sidx;
-    __syncthreads();
+    if (rank == 0 && tid == 0) sidx = atomicAdd(queue, 1);
+    inst_sync<CL>();
+    int idx = sidx;
+    if constexpr (CL > 1) idx = *cooperative_groups::this_cluster().map_shared_rank(&sidx, 0);
+    inst_sync<CL>(); // every CTA has read the index before rank 0 fetches the next one
     if (idx >= ninst) break;
     BatchInst& I = insts[order[idx]];
     const int n = I.n;
+    const int j0 = (int)((long long)n * rank / CL), j1 = (int)((long long)n * (rank + 1) / CL);
     const long long N = (long long)n * n;
     const double cx = I.cx, cy = I.cy, cc = I.cc, rho = I.rho;
     // six instance-local regions: the y array and five work regions; roles are indices
@@ -196,9 +248,9 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
     int bufs[3] = {3, 4, 5}; // stage buffers (rotated like the single-problem integrator)
 
     // F_0 = A y_0
-    for (int j = warp; j < n; j += NW)
-      for (int i = lane; i < n; i += 32) P[iF][(long long)j * n + i] = lap(P[iy], n, i, j, cx, cy, cc);
-    __syncthreads();
+    for (int j = j0 + warp; j < j1; j += NW)
+      for (int i = lane; i < n; i += 32) P[iF][(long long)j * n + i] = lap(P[iy], n, i, j, j0, j1, cx, cy, cc);
+    inst_sync<CL>();
     long long nfe = 1, nst = 0, natt = 0, netf = 0, nexp = 0, stmax = 0, sttot = 0, nhist = 0;
     double t = 0.0, hnext = 0.0, hlast = 0.0, ep1 = 0.0, ep2 = 0.0;
     bool after_fail = false;
@@ -212,7 +264,7 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
       xsum::zero(a0);
       xsum::zero(a1);
       unsigned f0 = 0, f1 = 0;
-      for (int j = warp; j < n; j += NW)
+      for (int j = j0 + warp; j < j1; j += NW)
         for (int i = lane; i < n; i += 32)
         {
           const long long k = (long long)j * n + i;
@@ -221,33 +273,33 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
           xsum::add(a0, x0 * x0, f0);
           xsum::add(a1, x1 * x1, f1);
         }
-      const double d0 = sqrt(cta_exact_sum<NT>(a0, f0, sm, &sflags, &sres) / (double)N);
-      const double d1 = sqrt(cta_exact_sum<NT>(a1, f1, sm, &sflags, &sres) / (double)N);
+      const double d0 = sqrt(inst_exact_sum<NT, CL>(a0, f0, sm, climb, &sflags, &sres) / (double)N);
+      const double d1 = sqrt(inst_exact_sum<NT, CL>(a1, f1, sm, climb, &sflags, &sres) / (double)N);
       double h0       = (d0 < 1.0e-5 || d1 < 1.0e-5) ? 1.0e-6 : 0.01 * (d0 / d1);
       if (rho > 0.0 && h0 * rho > 1.0) h0 = 1.0 / rho;
       if (h0 > prm.tf) h0 = prm.tf;
       double* y1 = P[bufs[0]];
-      for (int j = warp; j < n; j += NW)
+      for (int j = j0 + warp; j < j1; j += NW)
         for (int i = lane; i < n; i += 32)
         {
           const long long k = (long long)j * n + i;
           y1[k]             = __fma_rn(h0, F0[k], yc[k]);
         }
-      __syncthreads();
+      inst_sync<CL>();
       xsum::Limbs a2;
       xsum::zero(a2);
       unsigned f2 = 0;
-      for (int j = warp; j < n; j += NW)
+      for (int j = j0 + warp; j < j1; j += NW)
         for (int i = lane; i < n; i += 32)
         {
           const long long k = (long long)j * n + i;
-          const double f1v  = lap(y1, n, i, j, cx, cy, cc);
+          const double f1v  = lap(y1, n, i, j, j0, j1, cx, cy, cc);
           const double wt   = 1.0 / (prm.rtol * fabs(yc[k]) + prm.atol);
           const double x    = (f1v - F0[k]) * wt;
           xsum::add(a2, x * x, f2);
         }
       nfe++;
-      const double d2 = sqrt(cta_exact_sum<NT>(a2, f2, sm, &sflags, &sres) / (double)N) / h0;
+      const double d2 = sqrt(inst_exact_sum<NT, CL>(a2, f2, sm, climb, &sflags, &sres) / (double)N) / h0;
       const double dm = d1 > d2 ? d1 : d2;
       double h1       = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : stsm::pow(0.01 / dm, 1.0 / B_ORD);
       if (!(h1 > 0.0) || !(h1 < 1e300)) h1 = h0;
@@ -288,13 +340,13 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
         {
           const double hm1 = h * ct[1].mus;
           double* y1       = P[bufs[0]];
-          for (int j = warp; j < n; j += NW)
+          for (int j = j0 + warp; j < j1; j += NW)
             for (int i = lane; i < n; i += 32)
             {
               const long long k = (long long)j * n + i;
               y1[k]             = __fma_rn(hm1, F0[k], yc[k]);
             }
-          __syncthreads();
+          inst_sync<CL>();
         }
         const double* ym2 = yc;
         int last          = 0; // index into bufs of Y_{j-1}
@@ -308,14 +360,14 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
           const double* ym1 = P[bufs[last]];
           const int nxt     = (last + 1) % 3;
           double* yj        = P[bufs[nxt]];
-          for (int j = warp; j < n; j += NW)
+          for (int j = j0 + warp; j < j1; j += NW)
             for (int i = lane; i < n; i += 32)
             {
               const long long k = (long long)j * n + i;
               const double uw = (i > 0) ? ym1[k - 1] : 0.0;
               const double ue = (i < n - 1) ? ym1[k + 1] : 0.0;
-              const double us = (j > 0) ? ym1[k - n] : 0.0;
-              const double un = (j < n - 1) ? ym1[k + n] : 0.0;
+              const double us = (j > 0) ? ldrow(&ym1[k - n], j - 1 < j0) : 0.0;
+              const double un = (j < n - 1) ? ldrow(&ym1[k + n], j + 1 >= j1) : 0.0;
               const double sx = uw + ue, sy = us + un;
               double acc      = gc * ym1[k];
               acc             = __fma_rn(gx, sx, acc);
@@ -325,7 +377,7 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
               acc             = __fma_rn(gf, F0[k], acc);
               yj[k]           = acc;
             }
-          __syncthreads();
+          inst_sync<CL>();
           ym2  = ym1;
           last = nxt;
         }
@@ -336,11 +388,11 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
         xsum::zero(ae);
         unsigned fe      = 0;
         const double p4h = 0.4 * h;
-        for (int j = warp; j < n; j += NW)
+        for (int j = j0 + warp; j < j1; j += NW)
           for (int i = lane; i < n; i += 32)
           {
             const long long k = (long long)j * n + i;
-            const double f    = lap(Ys, n, i, j, cx, cy, cc);
+            const double f    = lap(Ys, n, i, j, j0, j1, cx, cy, cc);
             Fnew[k]           = f;
             const double yv   = yc[k];
             const double d    = yv - Ys[k];
@@ -351,7 +403,7 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
             const double x    = e * wt;
             xsum::add(ae, x * x, fe);
           }
-        const double dsm = sqrt(cta_exact_sum<NT>(ae, fe, sm, &sflags, &sres) / (double)N);
+        const double dsm = sqrt(inst_exact_sum<NT, CL>(ae, fe, sm, climb, &sflags, &sres) / (double)N);
         nfe += s;
         sttot += s;
         if (s > stmax) stmax = s;
@@ -398,7 +450,7 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
     if (iy != 0)
     {
       const double* yc = P[iy];
-      for (int j = warp; j < n; j += NW)
+      for (int j = j0 + warp; j < j1; j += NW)
         for (int i = lane; i < n; i += 32)
         {
           const long long k = (long long)j * n + i;
@@ -406,7 +458,7 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
         }
     }
     __syncthreads();
-    if (tid == 0)
+    if (tid == 0 && rank == 0)
     {
       I.status       = status;
       I.nst          = nst;
@@ -428,17 +480,94 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchInst* __restrict__ insts
 // ---------------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------------
+template <int NT, int CL>
+static bool launch_group(const STS_Batch b, const BatchParams& prm, const int* order, int count, int* queue, int grid,
+                         cudaStream_t st)
+{
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim            = dim3((unsigned)grid, 1, 1);
+  cfg.blockDim           = dim3(NT, 1, 1);
+  cfg.dynamicSmemBytes   = 0;
+  cfg.stream             = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id               = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs                = attr;
+  cfg.numAttrs             = CL > 1 ? 1 : 0;
+  return STS_CUDA_OK(cudaLaunchKernelEx(&cfg, batch_kernel<NT, CL>, b->dinst, order, count, queue, b->y, b->work,
+                                        b->total, prm));
+}
+
+template <int NT>
+static bool launch_cl(const STS_Batch b, const BatchParams& prm, int cl, const int* order, int count, int* queue,
+                      int grid, cudaStream_t st)
+{
+  switch (cl)
+  {
+  case 2: return launch_group<NT, 2>(b, prm, order, count, queue, grid, st);
+  case 4: return launch_group<NT, 4>(b, prm, order, count, queue, grid, st);
+  case 8: return launch_group<NT, 8>(b, prm, order, count, queue, grid, st);
+  default: return launch_group<NT, 1>(b, prm, order, count, queue, grid, st);
+  }
+}
+
+// One launch (cluster size 1), or two concurrent launches: instances with n >= big_n on
+// clusters of `cluster` CTAs (launched first), the rest on single CTAs on a second stream.
+// The CTA slots (SMs x CTAs per SM) are split between the two in proportion to their
+// estimated cost.
 static bool batch_launch(STS_Batch b, const BatchParams& prm, int threads, int ctas_per_sm)
 {
   STS_Context ctx = b->ctx;
   cudaStream_t st = ctx->stream;
-  if (!STS_CUDA_OK(cudaMemsetAsync(b->dqueue, 0, sizeof(int), st))) return false;
-  const int grid = std::max(1, std::min(b->ninst, ctx->num_sms * ctas_per_sm));
-  if (threads == 256)
-    batch_kernel<256><<<grid, 256, 0, st>>>(b->dinst, b->dorder, b->ninst, b->dqueue, b->y, b->work, b->total, prm);
-  else
-    batch_kernel<512><<<grid, 512, 0, st>>>(b->dinst, b->dorder, b->ninst, b->dqueue, b->y, b->work, b->total, prm);
-  return STS_CUDA_OK(cudaGetLastError());
+  if (!STS_CUDA_OK(cudaMemsetAsync(b->dqueue, 0, 2 * sizeof(int), st))) return false;
+  const int slots = ctx->num_sms * ctas_per_sm;
+  auto go = [&](int cl, const int* order, int count, int* queue, int grid, cudaStream_t s) {
+    return threads == 256 ? launch_cl<256>(b, prm, cl, order, count, queue, grid, s)
+                          : launch_cl<512>(b, prm, cl, order, count, queue, grid, s);
+  };
+  const int CL = b->cluster;
+  if (CL <= 1 || b->nbig == 0)
+    return go(1, b->dorder, b->ninst, b->dqueue, std::max(1, std::min(b->ninst, slots)), st);
+  const int nsmall = b->ninst - b->nbig;
+  int gbig = (int)std::lround(b->big_share * slots / CL) * CL;
+  gbig     = std::max(CL, std::min(gbig, b->nbig * CL));
+  gbig     = std::min(gbig, (slots / CL) * CL);
+  int gsm  = std::max(1, std::min(nsmall, slots - gbig));
+  bool ok  = go(CL, b->dorder_big, b->nbig, b->dqueue, gbig, st);
+  if (ok && nsmall > 0)
+  {
+    ok = STS_CUDA_OK(cudaEventRecord(b->ev_fork, st)) && STS_CUDA_OK(cudaStreamWaitEvent(b->side, b->ev_fork, 0)) &&
+         go(1, b->dorder_small, nsmall, b->dqueue + 1, gsm, b->side) &&
+         STS_CUDA_OK(cudaEventRecord(b->ev_join, b->side)) && STS_CUDA_OK(cudaStreamWaitEvent(st, b->ev_join, 0));
+  }
+  return ok;
+}
+
+// split the cost-ordered instances into the clustered group (n >= big_n) and the rest
+static bool batch_regroup(STS_Batch b)
+{
+  std::vector<int> order(b->ninst), big, small;
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->cost[x] > b->cost[y]; });
+  double cb = 0.0, ct = 0.0;
+  for (int i : order)
+  {
+    ct += b->cost[i];
+    if (b->cluster > 1 && b->hinst[i].n >= b->big_n)
+    {
+      big.push_back(i);
+      cb += b->cost[i];
+    }
+    else small.push_back(i);
+  }
+  b->nbig      = (int)big.size();
+  b->big_share = ct > 0.0 ? cb / ct : 0.0;
+  return (big.empty() || STS_CUDA_OK(cudaMemcpy(b->dorder_big, big.data(), big.size() * sizeof(int),
+                                                 cudaMemcpyHostToDevice))) &&
+         (small.empty() || STS_CUDA_OK(cudaMemcpy(b->dorder_small, small.data(), small.size() * sizeof(int),
+                                                   cudaMemcpyHostToDevice)));
 }
 
 extern "C" STS_Batch STS_BatchCreate(STS_Context ctx, int ninst, const int* n, const double* kx, const double* ky)
@@ -480,17 +609,23 @@ extern "C" STS_Batch STS_BatchCreate(STS_Context ctx, int ninst, const int* n, c
     cost[i] = (double)n[i] * n[i] * sqrt(I.rho);
   }
   b->total = off;
+  b->cost  = cost;
   std::vector<int> order(ninst);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
   bool ok = STS_CUDA_OK(cudaMalloc(&b->dinst, ninst * sizeof(BatchInst))) &&
             STS_CUDA_OK(cudaMalloc(&b->dorder, ninst * sizeof(int))) &&
-            STS_CUDA_OK(cudaMalloc(&b->dqueue, sizeof(int))) &&
+            STS_CUDA_OK(cudaMalloc(&b->dorder_big, ninst * sizeof(int))) &&
+            STS_CUDA_OK(cudaMalloc(&b->dorder_small, ninst * sizeof(int))) &&
+            STS_CUDA_OK(cudaMalloc(&b->dqueue, 2 * sizeof(int))) &&
+            STS_CUDA_OK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking)) &&
+            STS_CUDA_OK(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming)) &&
+            STS_CUDA_OK(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming)) &&
             STS_CUDA_OK(cudaMalloc(&b->y, b->total * sizeof(double))) &&
             STS_CUDA_OK(cudaMalloc(&b->work, 5 * b->total * sizeof(double))) &&
             STS_CUDA_OK(cudaMemcpy(b->dinst, b->hinst.data(), ninst * sizeof(BatchInst), cudaMemcpyHostToDevice)) &&
             STS_CUDA_OK(cudaMemcpy(b->dorder, order.data(), ninst * sizeof(int), cudaMemcpyHostToDevice)) &&
-            STS_CUDA_OK(cudaMemset(b->y, 0, b->total * sizeof(double)));
+            STS_CUDA_OK(cudaMemset(b->y, 0, b->total * sizeof(double))) && batch_regroup(b);
   if (!ok)
   {
     STS_BatchFree(&b);
@@ -510,6 +645,11 @@ extern "C" int STS_BatchFree(STS_Batch* pb)
   cudaFree(b->y);
   cudaFree(b->work);
   cudaFree(b->dcoef);
+  cudaFree(b->dorder_big);
+  cudaFree(b->dorder_small);
+  if (b->side) cudaStreamDestroy(b->side);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
   delete b;
   *pb = nullptr;
   return 0;
@@ -646,8 +786,28 @@ extern "C" int STS_BatchSetLaunch(STS_Batch b, int threads, int ctas_per_sm)
   return 0;
 }
 
-// Autotuner: runs the batch from its current state to tf_probe with every launch shape,
-// restores the state after each probe, and keeps the fastest shape.
+extern "C" int STS_BatchSetCluster(STS_Batch b, int cluster, int big_n)
+{
+  if (!b || (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8) || big_n < 2) return STS_ILL_INPUT;
+  ctx_activate(b->ctx);
+  b->cluster = cluster;
+  b->big_n   = big_n;
+  return batch_regroup(b) ? 0 : STS_ERR_FAILURE;
+}
+
+extern "C" int STS_BatchGetLaunch(STS_Batch b, int* threads, int* ctas_per_sm, int* cluster, int* big_n)
+{
+  if (!b) return STS_ILL_INPUT;
+  if (threads) *threads = b->block;
+  if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm;
+  if (cluster) *cluster = b->cluster;
+  if (big_n) *big_n = b->big_n;
+  return 0;
+}
+
+// Autotuner: runs the batch from its current state to tf_probe with every launch shape
+// (threads per CTA, CTAs per SM, cluster size for the large instances), restores the state
+// after each probe, and keeps the fastest shape.
 extern "C" int STS_BatchAutotune(STS_Batch b, double tf_probe, int method, double rtol, double atol, int smax,
                                  int* threads, int* ctas_per_sm, double* ms_best)
 {
@@ -656,26 +816,34 @@ extern "C" int STS_BatchAutotune(STS_Batch b, double tf_probe, int method, doubl
   double* save = nullptr;
   if (!STS_CUDA_OK(cudaMalloc(&save, b->total * sizeof(double)))) return -1;
   cudaMemcpyAsync(save, b->y, b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->ctx->stream);
-  const int shapes[][2] = {{256, 1}, {256, 2}, {512, 1}, {512, 2}};
+  // {threads per CTA, CTAs per SM, cluster size of the large-instance group}
+  // (the kernel is compiled for 1024 resident threads per SM: 64 registers per thread)
+  const int shapes[][3] = {{256, 4, 1}, {512, 2, 1}, {256, 4, 4}, {512, 2, 4},
+                           {256, 4, 8}, {512, 2, 8}, {512, 1, 8}};
   double best           = 1e30;
-  int bt = b->block, bc = b->ctas_per_sm;
+  int bt = b->block, bc = b->ctas_per_sm, bcl = b->cluster;
   for (auto& sh : shapes)
   {
     b->block       = sh[0];
     b->ctas_per_sm = sh[1];
-    const int rc   = STS_BatchEvolve(b, tf_probe, method, rtol, atol, smax, 0, 0); // PID, as evolve
+    b->cluster     = sh[2];
+    if (!batch_regroup(b)) break;
+    const int rc = STS_BatchEvolve(b, tf_probe, method, rtol, atol, smax, 0, 0); // PID, as evolve
     cudaMemcpyAsync(b->y, save, b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->ctx->stream);
     if (rc == 0 && b->last_ms < best)
     {
       best = b->last_ms;
       bt   = sh[0];
       bc   = sh[1];
+      bcl  = sh[2];
     }
   }
   cudaStreamSynchronize(b->ctx->stream);
   cudaFree(save);
   b->block       = bt;
   b->ctas_per_sm = bc;
+  b->cluster     = bcl;
+  batch_regroup(b);
   if (threads) *threads = bt;
   if (ctas_per_sm) *ctas_per_sm = bc;
   if (ms_best) *ms_best = best;

@@ -297,6 +297,11 @@ int STS_BatchSetLaunch(STS_Batch b, int threads, int ctas_per_sm);
 /* autotuner: time every launch shape on the probe horizon [0, tf_probe], keep the fastest */
 int STS_BatchAutotune(STS_Batch b, double tf_probe, int method, double rtol, double atol,
                       int smax, int* threads, int* ctas_per_sm, double* ms_best);
+/* instances with n >= big_n are integrated by thread-block clusters of `cluster` CTAs (1, 2,
+ * 4 or 8; rows split between the CTAs, cluster barriers between sweeps, the exact reductions
+ * combined through distributed shared memory), concurrently with the single-CTA group */
+int STS_BatchSetCluster(STS_Batch b, int cluster, int big_n);
+int STS_BatchGetLaunch(STS_Batch b, int* threads, int* ctas_per_sm, int* cluster, int* big_n);
 
 /* ------------------------------------------------------------------------------------
  * Learned multilevel preconditioner (new; the reference's alternative to Jacobi is hypre

@@ -35,15 +35,33 @@ def test_batch_matches_oracle_per_instance(ctx, stslib, oracle, method, controll
 
 
 def test_batch_launch_shapes_agree_bitwise(ctx, stslib):
+    """Launch shape and thread-block clusters (instances with n >= 32 split over 2, 4 or 8
+    CTAs, exact reductions combined through distributed shared memory) change nothing."""
     inst = small_batch(stslib, count=12, seed=3)
     outs = []
-    for threads, cps in ((256, 1), (256, 2), (512, 1)):
+    for threads, cps, cluster in ((256, 1, 1), (256, 2, 1), (512, 1, 1), (256, 2, 2), (512, 2, 4),
+                                  (256, 4, 8)):
         B = stslib.Batch(ctx, inst)
-        assert B.set_launch(threads, cps) == 0
+        assert B.set_launch(threads, cps, cluster, big_n=32) == 0
         B.evolve(0.005, method=stslib.RKC, rtol=1e-6, atol=1e-10)
         outs.append(B.state())
+        assert B.launch() == (threads, cps, cluster, 32)
     for o in outs[1:]:
         assert np.array_equal(outs[0], o)
+
+
+def test_batch_clusters_match_oracle(ctx, stslib, oracle):
+    inst = small_batch(stslib, count=10, seed=11)
+    B = stslib.Batch(ctx, inst)
+    assert B.set_launch(256, 2, 4, big_n=16) == 0  # every instance on a 4-CTA cluster
+    B.evolve(0.01, method=stslib.RKL, rtol=1e-6, atol=1e-10)
+    y = B.state()
+    for i, (n, kx, ky, p, q, a) in enumerate(inst):
+        P = oracle.Problem(oracle.UNFORCED, n, n, kx=kx, ky=ky)
+        J = oracle.Integrator(P, P.initial_modes(p, q, a), method=oracle.RKL, rtol=1e-6, atol=1e-10)
+        assert J.evolve(0.01) == 0
+        assert np.array_equal(B.instance_state(y, i), J.y), i
+        assert B.stats(i)["nst"] == J.stats()["nst"]
 
 
 def test_batch_autotune_keeps_results(ctx, stslib):
