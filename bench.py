@@ -429,7 +429,9 @@ def run_batch(args):
         "metric": "batched STS: DOF-stages/s and time for %d independent problems in one launch" % len(inst),
         "value": dof_stages / (ms / 1e3), "unit": "DOF-stages/s", "time_s": ms / 1e3,
         "total_dof": int(B.total), "dof_stages": dof_stages, "steps_total": int(sum(nst)),
-        "steps_max": int(max(nst)), "launch": {"threads": th, "ctas_per_sm": cp, "probe_ms": tune_ms},
+        "steps_max": int(max(nst)),
+        "launch": {"threads": th, "ctas_per_sm": cp, "cluster_large": B.launch()[2],
+                   "cluster_min_n": B.launch()[3], "probe_ms": tune_ms},
         "largest_instance_dof_stages": float(per_inst[0]),
         "largest_instance_share": float(per_inst[0]) / dof_stages,
         "dtype": "f64", "data": "synthetic (seeded sine-mode initial states, seed 20261203)",

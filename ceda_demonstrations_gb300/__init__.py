@@ -730,7 +730,7 @@ class Batch:
 # ---------------------------------------------------------------------------------------
 # learned multilevel preconditioner
 # ---------------------------------------------------------------------------------------
-NET_LAYERS = ["W_in", "W_d1", "W_d2", "W_d3", "W_c", "W_u2", "W_u1", "W_u0", "W_out"]
+NET_LAYERS = ["W_in", "W_1", "W_2", "W_3"]
 NET_WSZ = 16 * 16 * 9
 
 
@@ -759,7 +759,8 @@ def net_features(kx, ky, gamma, dx):
 
 
 class Net:
-    """STS_Net: the linear multilevel convolutional preconditioner (BF16 tensor-core kernels).
+    """STS_Net: the learned SPD multilevel preconditioner z = D (r + E^T E r) (BF16
+    tensor-core kernels).
 
     Device arrays are passed as raw device pointers (ints), e.g. ``NVector.ptr`` or a
     ``torch`` CUDA tensor's ``data_ptr()``; the caller orders work on other streams."""

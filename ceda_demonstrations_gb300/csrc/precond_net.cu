@@ -1,20 +1,21 @@
-// Learned multilevel preconditioner: a small linear convolutional network (4 levels, 16
-// channels, 3x3 kernels, BF16 weights, FP32 accumulation) with hand-written training and
-// inference kernels. The architecture and the gradient formulas follow the CPU reference
-// oracle/convnet.py, against which the tests check the forward output and the gradients.
+// Learned multilevel preconditioner with hand-written training and inference kernels. The
+// architecture and the gradient formulas follow the CPU reference oracle/convnet.py, against
+// which the tests check the output and the gradients:
 //
-//   a0 = conv(x, W_in)            x = [r, r s_k, r s_g] * scale      (3 -> 16, n)
-//   a1 = conv(pool(a0), W_d1)     a2 = conv(pool(a1), W_d2)           (n/2, n/4)
-//   a3 = conv(conv(pool(a2), W_d3), W_c)                               (n/8)
-//   b2 = conv(up(a3) + a2, W_u2)  b1 = conv(up(b2) + a1, W_u1)  b0 = conv(up(b1) + a0, W_u0)
-//   z  = conv(b0, W_out) * jacobi / scale                              (16 -> 1, n)
+//   z = D (r + E^T E r)        D: Jacobi diagonal, E: 4-level linear encoder, E^T its adjoint
+//   x  = [r, r s_k, r s_g] * scale                    h0 = conv(x, W_in)       (3 -> 16, n)
+//   h1 = conv(pool(h0), W_1)   h2 = conv(pool(h1), W_2)   h3 = conv(pool(h2), W_3)
+//   g3 = h3,  g_l = h_l + poolT(convT(g_{l+1}, W_{l+1})),  u = [1, s_k, s_g] . convT(g0, W_in)
+//   z  = D (r + u / scale)
+// E^T E is symmetric positive semi-definite, so the preconditioner is SPD for every system
+// (an additive multilevel preconditioner with learned level operators), linear in r.
 //
 // Activations are NHWC BF16 with 16 channels (32 bytes per pixel). The 3x3 convolutions are
 // implicit GEMMs on the tensor cores (mma.sync m16n8k16 BF16 -> FP32): a CTA stages a
 // (rows+2) x (64+2) pixel tile in shared memory (16-byte halves XOR-swizzled by pixel so
 // ldmatrix is conflict-free), each warp computes 16-pixel x 16-channel tiles over the nine
-// taps with the weights held in registers as MMA fragments. The input gradient is the same
-// kernel with the flipped, transposed weights; the weight gradient is a per-tile FP32
+// taps with the weights held in registers as MMA fragments. A transposed convolution is the
+// same kernel with the flipped, transposed weights; the weight gradient is a per-tile FP32
 // reduction added to global memory with atomics.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -31,9 +32,9 @@
 namespace net {
 
 constexpr int CH = 16;
-constexpr int NLAYER = 9; // W_in, W_d1, W_d2, W_d3, W_c, W_u2, W_u1, W_u0, W_out
+constexpr int NLAYER = 4; // W_in, W_1, W_2, W_3
 constexpr int WSZ = CH * CH * 9; // every layer stored as 16 x 16 x 3 x 3 (zero padded)
-enum { L_IN = 0, L_D1, L_D2, L_D3, L_C, L_U2, L_U1, L_U0, L_OUT };
+enum { L_IN = 0, L_1, L_2, L_3 };
 
 // conv tile: CTA = 4 warps, tile = TR rows x 64 columns, each warp one row at a time
 constexpr int TC = 64;
@@ -69,13 +70,15 @@ struct LoadArgs {
   double scale          = 1.0;
   float sk = 0.f, sg    = 0.f;
   const __nv_bfloat16* coarse = nullptr;
+  float cscale          = 1.f; // LD_UPADD: in + cscale * up(coarse)
 };
 
 // out[p][co] = sum_{tap, ci} w[co][ci][tap] * in[p + tap - 1][ci], for each image of a batch
 // (blockIdx.z; images of H x W pixels stored one after another, zero padding at every edge)
-// mode 0: BF16 NHWC output (16 channels); mode 1: FP64 output (channel 0 + the Jacobi skip
-// r * scale when la.r or la.r32 is set) times the image's output scale (meta, or out_scale
-// when meta is null)
+// mode 0: BF16 NHWC output (16 channels); mode 2: FP64 output u = c0 + sk c1 + sg c2 of the
+// first three output channels (only the first 8 output channels are computed) plus the
+// Jacobi skip r * scale (la.r or la.r32), times the image's output scale (meta, or out_scale
+// when meta is null); sk, sg from meta or la
 template <int MODE, int LOAD = LD_PLAIN>
 __global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __restrict__ in, int H, int W,
                                                        const uint2* __restrict__ wf, __nv_bfloat16* __restrict__ out,
@@ -95,6 +98,8 @@ __global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __re
     {
       out_scale = meta_out_scale(meta, blockIdx.z);
       la.scale  = (double)meta[META * blockIdx.z + 3];
+      la.sk     = meta[META * blockIdx.z];
+      la.sg     = meta[META * blockIdx.z + 1];
     }
   }
   // stage the input tile with a one-pixel halo (16-byte chunks, zero outside the image)
@@ -130,7 +135,7 @@ __global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __re
         for (int q = 0; q < 4; ++q)
         {
           const float2 a = __bfloat1622float2(fb[q]), b = __bfloat1622float2(cb[q]);
-          __nv_bfloat162 t = __floats2bfloat162_rn(b.x + a.x, b.y + a.y);
+          __nv_bfloat162 t = __floats2bfloat162_rn(la.cscale * b.x + a.x, la.cscale * b.y + a.y);
           o[q] = *reinterpret_cast<uint32_t*>(&t);
         }
         v = make_uint4(o[0], o[1], o[2], o[3]);
@@ -143,7 +148,7 @@ __global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __re
 #pragma unroll
   for (int t = 0; t < 9; ++t)
 #pragma unroll
-    for (int nh = 0; nh < 2; ++nh) wr[t][nh] = wf[(t * 2 + nh) * 32 + lane];
+    for (int nh = 0; nh < 2; ++nh) wr[t][nh] = (MODE == 0 || nh == 0) ? wf[(t * 2 + nh) * 32 + lane] : make_uint2(0, 0);
   __syncthreads();
   const int row = warp; // one tile row per warp (TR == 4 warps)
   const int gy  = y0 + row;
@@ -166,7 +171,7 @@ __global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __re
                    : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3)
                    : "r"(smem_u32(rp)));
 #pragma unroll
-      for (int nh = 0; nh < 2; ++nh)
+      for (int nh = 0; nh < (MODE == 0 ? 2 : 1); ++nh)
       {
         asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
                      "{%0,%1,%2,%3};"
@@ -175,9 +180,16 @@ __global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __re
       }
     }
     // accumulator layout: c0,c1 -> pixel lane/4, channels (lane%4)*2..+1; c2,c3 -> pixel lane/4+8
-    if (gy < H)
+    if (gy < H) // uniform across the warp
     {
       const int pr0 = lane >> 2;
+      // mode 2: channel 2 sits in the next lane (all lanes take part in the shuffle)
+      float c2h[2] = {0.f, 0.f};
+      if (MODE != 0)
+      {
+        c2h[0] = __shfl_down_sync(0xffffffffu, acc[0][0], 1);
+        c2h[1] = __shfl_down_sync(0xffffffffu, acc[0][2], 1);
+      }
 #pragma unroll
       for (int half = 0; half < 2; ++half)
       {
@@ -194,12 +206,18 @@ __global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __re
             *reinterpret_cast<__nv_bfloat162*>(out + p * CH + co) = v;
           }
         }
-        else if ((lane & 3) == 0)
+        else
         {
-          double v = (double)acc[0][half * 2];
-          if (la.r) v += la.r[img_pix + p] * la.scale;
-          else if (la.r32) v += (double)la.r32[img_pix + p] * la.scale;
-          out64[p] = v * out_scale;
+          // channels 0, 1 in this lane (lane % 4 == 0), channel 2 in the next lane
+          const float c2 = c2h[half];
+          if ((lane & 3) == 0)
+          {
+            double v = (double)acc[0][half * 2] + (double)la.sk * (double)acc[0][half * 2 + 1] +
+                       (double)la.sg * (double)c2;
+            if (la.r) v += la.r[img_pix + p] * la.scale;
+            else if (la.r32) v += (double)la.r32[img_pix + p] * la.scale;
+            out64[p] = v * out_scale;
+          }
         }
       }
     }
@@ -223,9 +241,10 @@ __global__ void pool_kernel(const __nv_bfloat16* __restrict__ in, int H, int W, 
   }
 }
 
-// s = up(coarse) + fine (nearest-neighbour upsampling)
+// s = cscale * up(coarse) + fine (nearest-neighbour upsampling; cscale 0.25 is the adjoint
+// of the 2x2 mean)
 __global__ void upadd_kernel(const __nv_bfloat16* __restrict__ coarse, const __nv_bfloat16* __restrict__ fine, int H,
-                             int W, __nv_bfloat16* __restrict__ out)
+                             int W, float cscale, __nv_bfloat16* __restrict__ out)
 {
   const long long n = (long long)H * W * CH;
   const int Wc      = W / 2;
@@ -234,7 +253,8 @@ __global__ void upadd_kernel(const __nv_bfloat16* __restrict__ coarse, const __n
     const int c = (int)(k % CH);
     const long long p = k / CH;
     const int x = (int)(p % W), y = (int)(p / W);
-    const float v = __bfloat162float(coarse[((long long)(y / 2) * Wc + x / 2) * CH + c]) + __bfloat162float(fine[k]);
+    const float v = cscale * __bfloat162float(coarse[((long long)(y / 2) * Wc + x / 2) * CH + c]) +
+                    __bfloat162float(fine[k]);
     out[k] = __float2bfloat16_rn(v);
   }
 }
@@ -275,8 +295,9 @@ __global__ void poolT_add_kernel(const __nv_bfloat16* __restrict__ gcoarse, int 
 }
 
 // Energy-norm loss of each image (n x n): d = z - e, L_img = 0.5 d^T M d / (e^T M e) with
-// M = I - gamma A on the crop (zero outside). Writes dL/dy = (M d) * out_scale / (e^T M e) * gscale
-// as the BF16 channel-0 gradient of the network output y and adds gscale * sum L_img to *acc.
+// M = I - gamma A on the crop (zero outside). With g = (M d) * out_scale / (e^T M e) * gscale
+// the gradient of the last transposed convolution's output channels is [g, sk g, sg g] (BF16);
+// adds gscale * sum L_img to *acc.
 __global__ void gradz_kernel(long long npix, int n, const double* __restrict__ z, const float* __restrict__ e,
                              double gscale, const float* __restrict__ meta, __nv_bfloat16* __restrict__ g,
                              double* __restrict__ acc)
@@ -298,9 +319,11 @@ __global__ void gradz_kernel(long long npix, int n, const double* __restrict__ z
     lsum += 0.5 * dc * Md * inv;
     const float gv = (float)(Md * inv * meta_out_scale(meta, img) * gscale);
     __align__(16) __nv_bfloat16 o[CH];
-    o[0] = __float2bfloat16_rn(gv);
+    o[0] = __float2bfloat16_rn(gv); // dL/du expanded over the input channels [1, sk, sg]
+    o[1] = __float2bfloat16_rn(gv * m[0]);
+    o[2] = __float2bfloat16_rn(gv * m[1]);
 #pragma unroll
-    for (int c = 1; c < CH; ++c) o[c] = __float2bfloat16_rn(0.f);
+    for (int c = 3; c < CH; ++c) o[c] = __float2bfloat16_rn(0.f);
     uint4* dst = reinterpret_cast<uint4*>(g + p * CH);
     dst[0]     = reinterpret_cast<uint4*>(o)[0];
     dst[1]     = reinterpret_cast<uint4*>(o)[1];
@@ -492,9 +515,10 @@ __global__ void gather_kernel(const float* __restrict__ r, const float* __restri
 }
 
 struct Level {
-  int n = 0;
-  __nv_bfloat16 *x = nullptr, *a = nullptr, *p = nullptr, *c = nullptr, *s = nullptr, *b = nullptr;
-  __nv_bfloat16 *ga = nullptr, *gb = nullptr, *gt = nullptr; // gradient buffers
+  __nv_bfloat16 *x = nullptr;                     // level 0: network input channels
+  __nv_bfloat16 *h = nullptr, *p = nullptr;       // encoder output, pooled input (l >= 1)
+  __nv_bfloat16 *g = nullptr, *y = nullptr;       // adjoint-pass sum g_l, convT output y_l (l >= 1)
+  __nv_bfloat16 *dg = nullptr, *dy = nullptr, *t = nullptr; // gradients and scratch
 };
 
 } // namespace net
@@ -535,14 +559,13 @@ static void free_levels(STS_Net nt)
   for (auto& L : nt->L)
   {
     cudaFree(L.x);
-    cudaFree(L.a);
+    cudaFree(L.h);
     cudaFree(L.p);
-    cudaFree(L.c);
-    cudaFree(L.s);
-    cudaFree(L.b);
-    cudaFree(L.ga);
-    cudaFree(L.gb);
-    cudaFree(L.gt);
+    cudaFree(L.g);
+    cudaFree(L.y);
+    cudaFree(L.dg);
+    cudaFree(L.dy);
+    cudaFree(L.t);
     L = net::Level();
   }
   cudaFree(nt->z);
@@ -563,15 +586,14 @@ static bool ensure_capacity(STS_Net nt, long long pix)
   for (int l = 0; l < 4 && ok; ++l)
   {
     const long long np = (pix >> (2 * l)) * CH * 2;
-    nt->L[l].x  = (__nv_bfloat16*)dalloc(np, &ok);
-    nt->L[l].a  = (__nv_bfloat16*)dalloc(np, &ok);
+    if (l == 0) nt->L[l].x = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].h  = (__nv_bfloat16*)dalloc(np, &ok);
     nt->L[l].p  = (__nv_bfloat16*)dalloc(np, &ok);
-    nt->L[l].c  = (__nv_bfloat16*)dalloc(np, &ok);
-    nt->L[l].s  = (__nv_bfloat16*)dalloc(np, &ok);
-    nt->L[l].b  = (__nv_bfloat16*)dalloc(np, &ok);
-    nt->L[l].ga = (__nv_bfloat16*)dalloc(np, &ok);
-    nt->L[l].gb = (__nv_bfloat16*)dalloc(np, &ok);
-    nt->L[l].gt = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].g  = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].y  = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].dg = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].dy = (__nv_bfloat16*)dalloc(np, &ok);
+    nt->L[l].t  = (__nv_bfloat16*)dalloc(np, &ok);
   }
   nt->z  = (double*)dalloc((size_t)pix * 8, &ok);
   nt->rb = (float*)dalloc((size_t)pix * 4, &ok);
@@ -626,9 +648,9 @@ extern "C" STS_Net STS_NetCreate(STS_Context ctx, int nmax, unsigned long long s
   std::normal_distribution<float> nd(0.f, 1.f);
   for (int l = 0; l < NLAYER; ++l)
   {
-    const int ci_n = (l == net::L_IN) ? 3 : CH, co_n = (l == net::L_OUT) ? 1 : CH;
-    // the output layer starts small, so the untrained network is close to its Jacobi skip
-    const float sd = std::sqrt(1.0f / (ci_n * 9)) * (l == net::L_OUT ? 0.1f : 1.0f);
+    const int ci_n = (l == net::L_IN) ? 3 : CH, co_n = CH;
+    // small initial weights: the untrained preconditioner is close to Jacobi (E^T E ~ 0.1^4)
+    const float sd = std::sqrt(1.0f / (ci_n * 9)) * 0.3f;
     for (int co = 0; co < co_n; ++co)
       for (int ci = 0; ci < ci_n; ++ci)
         for (int t = 0; t < 9; ++t)
@@ -703,7 +725,22 @@ static void conv(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, int layer
                                                                out, nullptr, 0.0, nullptr);
 }
 
-// forward pass over nimg images of n x n; meta (device, per image) or the scalars
+static void pool(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, __nv_bfloat16* out)
+{
+  const long long cnt = (long long)n * n * nimg / 4 * CH;
+  net::pool_kernel<<<grid_for(cnt), 256, 0, nt->ctx->stream>>>(in, n * nimg, n, out);
+}
+
+// out = fine + 0.25 up(coarse) (fine at n x n)
+static void upadd(STS_Net nt, const __nv_bfloat16* coarse, const __nv_bfloat16* fine, int n, int nimg,
+                  __nv_bfloat16* out)
+{
+  const long long cnt = (long long)n * n * nimg * CH;
+  net::upadd_kernel<<<grid_for(cnt), 256, 0, nt->ctx->stream>>>(coarse, fine, n * nimg, n, 0.25f, out);
+}
+
+// Training forward over nimg images of n x n (per-image meta), every intermediate stored:
+// encoder h_l, p_l; adjoint pass y_l, g_l; output z = D (r + u / scale) into nt->z
 template <typename T>
 static void net_forward(STS_Net nt, int n, int nimg, const T* r, double scale, float sk, float sg, double out_scale,
                         const float* meta, double* zout = nullptr)
@@ -712,65 +749,68 @@ static void net_forward(STS_Net nt, int n, int nimg, const T* r, double scale, f
   net::Level* L   = nt->L;
   const long long ip = (long long)n * n, np = ip * nimg;
   net::input_kernel_t<T><<<grid_for(np), 256, 0, st>>>(np, ip, r, scale, sk, sg, meta, L[0].x);
-  conv(nt, L[0].x, n, nimg, net::L_IN, false, L[0].a);                                           // a0
-  net::pool_kernel<<<grid_for(np / 4 * CH), 256, 0, st>>>(L[0].a, n * nimg, n, L[1].p);          // p0
-  conv(nt, L[1].p, n / 2, nimg, net::L_D1, false, L[1].a);                                       // a1
-  net::pool_kernel<<<grid_for(np / 16 * CH), 256, 0, st>>>(L[1].a, n / 2 * nimg, n / 2, L[2].p); // p1
-  conv(nt, L[2].p, n / 4, nimg, net::L_D2, false, L[2].a);                                       // a2
-  net::pool_kernel<<<grid_for(np / 64 * CH), 256, 0, st>>>(L[2].a, n / 4 * nimg, n / 4, L[3].p); // p2
-  conv(nt, L[3].p, n / 8, nimg, net::L_D3, false, L[3].c);                                       // c3
-  conv(nt, L[3].c, n / 8, nimg, net::L_C, false, L[3].a);                                        // a3
-  net::upadd_kernel<<<grid_for(np / 16 * CH), 256, 0, st>>>(L[3].a, L[2].a, n / 4 * nimg, n / 4, L[2].s); // s2
-  conv(nt, L[2].s, n / 4, nimg, net::L_U2, false, L[2].b);                                       // b2
-  net::upadd_kernel<<<grid_for(np / 4 * CH), 256, 0, st>>>(L[2].b, L[1].a, n / 2 * nimg, n / 2, L[1].s); // s1
-  conv(nt, L[1].s, n / 2, nimg, net::L_U1, false, L[1].b);                                       // b1
-  net::upadd_kernel<<<grid_for(np * CH), 256, 0, st>>>(L[1].b, L[0].a, n * nimg, n, L[0].s);      // s0
-  conv(nt, L[0].s, n, nimg, net::L_U0, false, L[0].b);                                           // b0
+  conv(nt, L[0].x, n, nimg, net::L_IN, false, L[0].h);          // h0
+  pool(nt, L[0].h, n, nimg, L[1].p);                            // p0 (level 1)
+  conv(nt, L[1].p, n / 2, nimg, net::L_1, false, L[1].h);       // h1
+  pool(nt, L[1].h, n / 2, nimg, L[2].p);                        // p1
+  conv(nt, L[2].p, n / 4, nimg, net::L_2, false, L[2].h);       // h2
+  pool(nt, L[2].h, n / 4, nimg, L[3].p);                        // p2
+  conv(nt, L[3].p, n / 8, nimg, net::L_3, false, L[3].h);       // h3 = g3
+  conv(nt, L[3].h, n / 8, nimg, net::L_3, true, L[3].y);        // y3 = convT(g3, W_3)
+  upadd(nt, L[3].y, L[2].h, n / 4, nimg, L[2].g);               // g2 = h2 + poolT(y3)
+  conv(nt, L[2].g, n / 4, nimg, net::L_2, true, L[2].y);        // y2
+  upadd(nt, L[2].y, L[1].h, n / 2, nimg, L[1].g);               // g1
+  conv(nt, L[1].g, n / 2, nimg, net::L_1, true, L[1].y);        // y1
+  upadd(nt, L[1].y, L[0].h, n, nimg, L[0].g);                   // g0
   dim3 g((unsigned)((n + net::TC - 1) / net::TC), (unsigned)((n + net::TR - 1) / net::TR), (unsigned)nimg);
-  net::LoadArgs la; // Jacobi skip from the network input
+  net::LoadArgs la; // Jacobi skip from the network input; sk, sg for the output combination
   if constexpr (sizeof(T) == 8) la.r = reinterpret_cast<const double*>(r);
   else la.r32 = reinterpret_cast<const float*>(r);
   la.scale = scale;
-  net::conv3x3_kernel<1><<<g, net::NTHR, 0, st>>>(L[0].b, n, n, nt->wf + net::L_OUT * 576, nullptr,
-                                                  zout ? zout : nt->z, out_scale, meta, la);
+  la.sk    = sk;
+  la.sg    = sg;
+  net::conv3x3_kernel<2><<<g, net::NTHR, 0, st>>>(L[0].g, n, n, nt->wt + net::L_IN * 576, nullptr,
+                                                  zout ? zout : nt->z, out_scale, meta, la); // z
 }
 
-// Inference forward pass of one n x n residual (FP64, device) into zout: the input channels
-// are built inside the first convolution and the skip sums inside the up-path convolutions,
-// so neither x nor s_l is stored. Produces bitwise the output of net_forward.
+// Inference of one n x n residual (FP64, device) into zout: the input channels are built in the
+// first convolution's tile loader and the sums g_l = h_l + poolT(y_{l+1}) in the transposed
+// convolutions' loaders, so only h_l, p_l and y_l are stored. Bitwise the output of net_forward.
 static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, float sk, float sg, double out_scale,
                               double* zout)
 {
   cudaStream_t st = nt->ctx->stream;
   net::Level* L   = nt->L;
-  const long long np = (long long)n * n;
   auto grid = [](int m) { return dim3((unsigned)((m + net::TC - 1) / net::TC), (unsigned)((m + net::TR - 1) / net::TR), 1u); };
   net::LoadArgs la;
   la.r     = r;
   la.scale = scale;
   la.sk    = sk;
   la.sg    = sg;
-  net::conv3x3_kernel<0, net::LD_R64><<<grid(n), net::NTHR, 0, st>>>(nullptr, n, n, nt->wf + net::L_IN * 576, L[0].a,
-                                                                      nullptr, 0.0, nullptr, la);     // a0
-  net::pool_kernel<<<grid_for(np / 4 * CH), 256, 0, st>>>(L[0].a, n, n, L[1].p);                   // p0
-  conv(nt, L[1].p, n / 2, 1, net::L_D1, false, L[1].a);                                           // a1
-  net::pool_kernel<<<grid_for(np / 16 * CH), 256, 0, st>>>(L[1].a, n / 2, n / 2, L[2].p);          // p1
-  conv(nt, L[2].p, n / 4, 1, net::L_D2, false, L[2].a);                                           // a2
-  net::pool_kernel<<<grid_for(np / 64 * CH), 256, 0, st>>>(L[2].a, n / 4, n / 4, L[3].p);          // p2
-  conv(nt, L[3].p, n / 8, 1, net::L_D3, false, L[3].c);                                           // c3
-  conv(nt, L[3].c, n / 8, 1, net::L_C, false, L[3].a);                                            // a3
+  net::conv3x3_kernel<0, net::LD_R64><<<grid(n), net::NTHR, 0, st>>>(nullptr, n, n, nt->wf + net::L_IN * 576, L[0].h,
+                                                                      nullptr, 0.0, nullptr, la);     // h0
+  pool(nt, L[0].h, n, 1, L[1].p);
+  conv(nt, L[1].p, n / 2, 1, net::L_1, false, L[1].h);                                                // h1
+  pool(nt, L[1].h, n / 2, 1, L[2].p);
+  conv(nt, L[2].p, n / 4, 1, net::L_2, false, L[2].h);                                                // h2
+  pool(nt, L[2].h, n / 4, 1, L[3].p);
+  conv(nt, L[3].p, n / 8, 1, net::L_3, false, L[3].h);                                                // h3
+  conv(nt, L[3].h, n / 8, 1, net::L_3, true, L[3].y);                                                 // y3
   net::LoadArgs lu;
-  lu.coarse = L[3].a;
-  net::conv3x3_kernel<0, net::LD_UPADD><<<grid(n / 4), net::NTHR, 0, st>>>(L[2].a, n / 4, n / 4, nt->wf + net::L_U2 * 576,
-                                                                            L[2].b, nullptr, 0.0, nullptr, lu); // b2
-  lu.coarse = L[2].b;
-  net::conv3x3_kernel<0, net::LD_UPADD><<<grid(n / 2), net::NTHR, 0, st>>>(L[1].a, n / 2, n / 2, nt->wf + net::L_U1 * 576,
-                                                                            L[1].b, nullptr, 0.0, nullptr, lu); // b1
-  lu.coarse = L[1].b;
-  net::conv3x3_kernel<0, net::LD_UPADD><<<grid(n), net::NTHR, 0, st>>>(L[0].a, n, n, nt->wf + net::L_U0 * 576, L[0].b,
-                                                                        nullptr, 0.0, nullptr, lu);  // b0
-  net::conv3x3_kernel<1><<<grid(n), net::NTHR, 0, st>>>(L[0].b, n, n, nt->wf + net::L_OUT * 576, nullptr, zout,
-                                                        out_scale, nullptr, la);                    // z
+  lu.cscale = 0.25f;
+  lu.coarse = L[3].y;
+  net::conv3x3_kernel<0, net::LD_UPADD><<<grid(n / 4), net::NTHR, 0, st>>>(L[2].h, n / 4, n / 4, nt->wt + net::L_2 * 576,
+                                                                            L[2].y, nullptr, 0.0, nullptr, lu); // y2
+  lu.coarse = L[2].y;
+  net::conv3x3_kernel<0, net::LD_UPADD><<<grid(n / 2), net::NTHR, 0, st>>>(L[1].h, n / 2, n / 2, nt->wt + net::L_1 * 576,
+                                                                            L[1].y, nullptr, 0.0, nullptr, lu); // y1
+  lu.coarse = L[1].y;
+  lu.r      = r;
+  lu.scale  = scale;
+  lu.sk     = sk;
+  lu.sg     = sg;
+  net::conv3x3_kernel<2, net::LD_UPADD><<<grid(n), net::NTHR, 0, st>>>(L[0].h, n, n, nt->wt + net::L_IN * 576, nullptr,
+                                                                        zout, out_scale, nullptr, lu);  // z
 }
 
 static void wgrad(STS_Net nt, const __nv_bfloat16* x, const __nv_bfloat16* g, int n, int nimg, int layer)
@@ -780,38 +820,48 @@ static void wgrad(STS_Net nt, const __nv_bfloat16* x, const __nv_bfloat16* g, in
   net::wgrad_kernel<<<grid, 256, 0, nt->ctx->stream>>>(x, g, n, n, nimg, nt->g + layer * WSZ);
 }
 
-// gradient of the energy-norm loss w.r.t. the weights, accumulated into nt->g (and gscale
-// times the loss into nt->dacc); needs the preceding forward and the per-image meta
+// out_fine += 0.25 up(coarse) (adjoint of the 2x2 mean), fine at n x n
+static void poolT_add(STS_Net nt, const __nv_bfloat16* coarse, int n, int nimg, __nv_bfloat16* fine)
+{
+  const long long cnt = (long long)n * n * nimg * CH;
+  net::poolT_add_kernel<<<grid_for(cnt), 256, 0, nt->ctx->stream>>>(coarse, n * nimg, n, fine);
+}
+
+// Gradient of the energy-norm loss w.r.t. the weights, accumulated into nt->g (and gscale times
+// the loss into nt->dacc); needs the preceding net_forward and the per-image meta. Each weight
+// is used twice (encoder conv and adjoint-pass convT): a convT(a, W) layer with output
+// gradient dy contributes wgrad(x = dy, g = a) and passes conv(dy, W) down; a conv(a, W) layer
+// contributes wgrad(x = a, g = dh) and passes convT(dh, W) down.
 static void net_backward(STS_Net nt, int n, int nimg, const float* e, double gscale, const float* meta)
 {
   cudaStream_t st = nt->ctx->stream;
   net::Level* L   = nt->L;
   const long long ip = (long long)n * n, np = ip * nimg;
   const int m = nimg;
-  net::gradz_kernel<<<grid_for(np), 256, 0, st>>>(np, n, nt->z, e, gscale, meta, L[0].gt, nt->dacc); // g (channel 0)
-  wgrad(nt, L[0].b, L[0].gt, n, m, net::L_OUT);
-  conv(nt, L[0].gt, n, m, net::L_OUT, true, L[0].gb);                                          // gb0
-  wgrad(nt, L[0].s, L[0].gb, n, m, net::L_U0);
-  conv(nt, L[0].gb, n, m, net::L_U0, true, L[0].ga);                                           // gs0 = ga0
-  net::upT_kernel<<<grid_for(np / 4 * CH), 256, 0, st>>>(L[0].ga, n * m, n, L[1].gb, 0);        // gb1
-  wgrad(nt, L[1].s, L[1].gb, n / 2, m, net::L_U1);
-  conv(nt, L[1].gb, n / 2, m, net::L_U1, true, L[1].ga);                                       // gs1 = ga1
-  net::upT_kernel<<<grid_for(np / 16 * CH), 256, 0, st>>>(L[1].ga, n / 2 * m, n / 2, L[2].gb, 0); // gb2
-  wgrad(nt, L[2].s, L[2].gb, n / 4, m, net::L_U2);
-  conv(nt, L[2].gb, n / 4, m, net::L_U2, true, L[2].ga);                                       // gs2 = ga2
-  net::upT_kernel<<<grid_for(np / 64 * CH), 256, 0, st>>>(L[2].ga, n / 4 * m, n / 4, L[3].gb, 0); // ga3
-  wgrad(nt, L[3].c, L[3].gb, n / 8, m, net::L_C);
-  conv(nt, L[3].gb, n / 8, m, net::L_C, true, L[3].ga);                                        // gc3
-  wgrad(nt, L[3].p, L[3].ga, n / 8, m, net::L_D3);
-  conv(nt, L[3].ga, n / 8, m, net::L_D3, true, L[3].gt);                                       // gp2
-  net::poolT_add_kernel<<<grid_for(np / 16 * CH), 256, 0, st>>>(L[3].gt, n / 4 * m, n / 4, L[2].ga); // ga2 += pool^T
-  wgrad(nt, L[2].p, L[2].ga, n / 4, m, net::L_D2);
-  conv(nt, L[2].ga, n / 4, m, net::L_D2, true, L[2].gt);                                       // gp1
-  net::poolT_add_kernel<<<grid_for(np / 4 * CH), 256, 0, st>>>(L[2].gt, n / 2 * m, n / 2, L[1].ga); // ga1 += pool^T
-  wgrad(nt, L[1].p, L[1].ga, n / 2, m, net::L_D1);
-  conv(nt, L[1].ga, n / 2, m, net::L_D1, true, L[1].gt);                                       // gp0
-  net::poolT_add_kernel<<<grid_for(np * CH), 256, 0, st>>>(L[1].gt, n * m, n, L[0].ga);         // ga0 += pool^T
-  wgrad(nt, L[0].x, L[0].ga, n, m, net::L_IN);
+  net::gradz_kernel<<<grid_for(np), 256, 0, st>>>(np, n, nt->z, e, gscale, meta, L[0].dy, nt->dacc); // d gx (3 ch)
+  // adjoint pass, top (level 0) to bottom (level 3)
+  wgrad(nt, L[0].dy, L[0].g, n, m, net::L_IN);                 // W_in via convT(g0)
+  conv(nt, L[0].dy, n, m, net::L_IN, false, L[0].dg);          // d g0 (= d h0 so far)
+  pool(nt, L[0].dg, n, m, L[1].dy);                            // d y1
+  wgrad(nt, L[1].dy, L[1].g, n / 2, m, net::L_1);
+  conv(nt, L[1].dy, n / 2, m, net::L_1, false, L[1].dg);       // d g1 (= d h1 so far)
+  pool(nt, L[1].dg, n / 2, m, L[2].dy);                        // d y2
+  wgrad(nt, L[2].dy, L[2].g, n / 4, m, net::L_2);
+  conv(nt, L[2].dy, n / 4, m, net::L_2, false, L[2].dg);       // d g2 (= d h2 so far)
+  pool(nt, L[2].dg, n / 4, m, L[3].dy);                        // d y3
+  wgrad(nt, L[3].dy, L[3].h, n / 8, m, net::L_3);              // g3 = h3
+  conv(nt, L[3].dy, n / 8, m, net::L_3, false, L[3].dg);       // d h3
+  // encoder, bottom to top
+  wgrad(nt, L[3].p, L[3].dg, n / 8, m, net::L_3);
+  conv(nt, L[3].dg, n / 8, m, net::L_3, true, L[3].t);
+  poolT_add(nt, L[3].t, n / 4, m, L[2].dg);                    // d h2 += poolT(convT(d h3))
+  wgrad(nt, L[2].p, L[2].dg, n / 4, m, net::L_2);
+  conv(nt, L[2].dg, n / 4, m, net::L_2, true, L[2].t);
+  poolT_add(nt, L[2].t, n / 2, m, L[1].dg);                    // d h1
+  wgrad(nt, L[1].p, L[1].dg, n / 2, m, net::L_1);
+  conv(nt, L[1].dg, n / 2, m, net::L_1, true, L[1].t);
+  poolT_add(nt, L[1].t, n, m, L[0].dg);                        // d h0
+  wgrad(nt, L[0].x, L[0].dg, n, m, net::L_IN);
 }
 
 static bool net_size_ok(STS_Net nt, int n)

@@ -304,25 +304,26 @@ int STS_BatchSetCluster(STS_Batch b, int cluster, int big_n);
 int STS_BatchGetLaunch(STS_Batch b, int* threads, int* ctas_per_sm, int* cluster, int* big_n);
 
 /* ------------------------------------------------------------------------------------
- * Learned multilevel preconditioner (new; the reference's alternative to Jacobi is hypre
- * PFMG, diffusion_2D/preconditioner_hypre.cpp). A linear 4-level convolutional network
- * (16 channels, 3x3 kernels, BF16 weights, FP32 accumulation, tensor-core implicit GEMM)
- * maps a residual r to a correction z ~ (I - gamma A)^{-1} r; sk = normalised log10(ky),
- * sg = normalised log10(gamma/dx^2) enter as channels r*sk, r*sg. Sizes: multiples of 16.
+ * Learned multilevel preconditioner (new; the reference's multilevel alternative to Jacobi
+ * is hypre PFMG, diffusion_2D/preconditioner_hypre.cpp). z = D (r + E^T E r): D the Jacobi
+ * diagonal, E a 4-level linear convolutional encoder (16 channels, 3x3 kernels, 2x2 mean
+ * pooling, BF16 weights, FP32 accumulation, tensor-core implicit GEMM) on the input channels
+ * [r, r sk, r sg] (sk = normalised log10(ky/kx), sg = normalised log10(gamma/dx^2)), E^T its
+ * exact adjoint: an SPD additive multilevel preconditioner with learned level operators.
+ * Sizes: multiples of 16.
  * ----------------------------------------------------------------------------------*/
 typedef struct STS_Net_* STS_Net;
 STS_Net STS_NetCreate(STS_Context ctx, int nmax, unsigned long long seed);
 int STS_NetFree(STS_Net* net);
-/* weights: 9 layers (W_in, W_d1, W_d2, W_d3, W_c, W_u2, W_u1, W_u0, W_out) x [16][16][3][3] FP32 */
+/* weights: 4 layers (W_in, W_1, W_2, W_3) x [16][16][3][3] FP32 (W_in: 3 input channels) */
 int STS_NetSetWeights(STS_Net net, const float* w);
 int STS_NetGetWeights(STS_Net net, float* w);
-/* z = jacobi * (r + net(scale * r) / scale) on device arrays of n x n doubles (the Jacobi
- * preconditioner plus the learned correction) */
+/* z = jacobi * (r + E^T E (scale r) / scale) on device arrays of n x n doubles */
 int STS_NetApply(STS_Net net, int n, const double* r, double* z, double sk, double sg, double jacobi,
                  double scale);
 /* one sample (scale 1): loss = 0.5 (z - e)^T M (z - e) / (e^T M e) with M = I - gamma A on the
  * n x n field (zero outside; gcx = gamma kx/dx^2, gcy = gamma ky/dy^2) and its weight
- * gradient (host FP32 array); z = jacobi (r + net(r)) */
+ * gradient (host FP32 array); z = jacobi (r + E^T E r) */
 int STS_NetLossGrad(STS_Net net, int n, const double* r, const float* e, double sk, double sg,
                     double jacobi, double gcx, double gcy, double* loss, float* grad);
 /* Adam over device samples r, e (nsamples x n x n FP32) with per-sample

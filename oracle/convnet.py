@@ -1,38 +1,45 @@
 """CPU reference (test infrastructure only) of the learned multilevel preconditioner.
 
-The network maps a residual r (one n x n field) to a correction z ~ (I - gamma A)^{-1} r. It is
-linear in r: the input channels are r, r*s_k and r*s_g, where s_k and s_g are the normalised
-log10(ky) and log10(gamma*h / dx^2) of the system, so the parameters modulate the operator
-while M(a r) = a M(r) holds exactly (as a Krylov preconditioner needs).
+The preconditioner maps a residual r (one n x n field) to a correction
+    z = D (r + E^T E r)
+with the Jacobi diagonal D and a 4-level linear convolutional encoder E. E^T is the exact
+adjoint of E (the same weights, transposed and flipped), so E^T E is symmetric positive
+semi-definite and z = P r with an SPD operator P: an additive multilevel (BPX-like)
+preconditioner whose level operators are learned. The system parameters enter as input
+channels: E acts on x = [r, r*s_k, r*s_g] (s_k, s_g: normalised log10(ky/kx) and
+log10(gamma/dx^2)), which keeps P linear in r and symmetric for every system.
 
-Architecture (4 levels, C = 16 channels, 3x3 convolutions with zero padding, no bias):
-    a0 = conv(x, W_in)                      3 -> C   at n
-    a1 = conv(pool(a0), W_d1)               C -> C   at n/2
-    a2 = conv(pool(a1), W_d2)               C -> C   at n/4
-    a3 = conv(conv(pool(a2), W_d3), W_c)    C -> C   at n/8 (two convolutions)
-    b2 = conv(up(a3) + a2, W_u2)            C -> C   at n/4
-    b1 = conv(up(b2) + a1, W_u1)            C -> C   at n/2
-    b0 = conv(up(b1) + a0, W_u0)            C -> C   at n
-    z  = (r + conv(b0, W_out)) * jacobi     C -> 1   at n   (Jacobi skip: z = D r + D N(r))
-pool = 2x2 mean; up = nearest-neighbour copy (its adjoint is the 2x2 sum). Weights are
-stored in BF16 (rounded to nearest even from FP32), activations in BF16 with FP32
-accumulation on the GPU; this reference computes in FP64 from the same BF16 weights. The
-skip term D r makes the untrained network (small W_out) the Jacobi preconditioner, and the
-network learns the correction beyond it.
+Encoder (16 channels, 3x3 convolutions with zero padding, no bias; pool = 2x2 mean):
+    h0 = conv(x, W_in)                 3 -> C   at n
+    h1 = conv(pool(h0), W_1)           C -> C   at n/2
+    h2 = conv(pool(h1), W_2)           C -> C   at n/4
+    h3 = conv(pool(h2), W_3)           C -> C   at n/8
+Adjoint pass with the features as its input (convT = transposed, flipped convolution,
+poolT = 0.25 * nearest upsampling, the adjoint of the 2x2 mean):
+    g3 = h3
+    g2 = h2 + poolT(convT(g3, W_3))
+    g1 = h1 + poolT(convT(g2, W_2))
+    g0 = h0 + poolT(convT(g1, W_1))
+    gx = convT(g0, W_in)               C -> 3   at n
+    u  = gx[0] + s_k gx[1] + s_g gx[2]
+    z  = jacobi * (r + u)
+Weights are stored in BF16 (rounded to nearest even from FP32); the GPU keeps activations in
+BF16 with FP32 accumulation, this reference computes in FP64 from the same BF16 weights.
 
 Loss (energy norm of the shifted operator M = I - gamma A, the norm CG minimises): with
 d = z - e, L = 0.5 d^T M d / (e^T M e), M applied on the crop with zero values outside it:
 (M d)_ij = (1 + 2 (gcx + gcy)) d_ij - gcx (d_i-1,j + d_i+1,j) - gcy (d_i,j-1 + d_i,j+1),
 gcx = gamma kx / dx^2, gcy = gamma ky / dy^2; dL/dz = M d / (e^T M e).
 
-forward() returns the output and a cache; backward() returns dL/dW for every weight given
-dL/dz, written out by hand (the GPU kernels are checked against it).
+forward() returns z and a cache; backward() returns dL/dW for every weight given dL/dz,
+written out by hand through both uses of each weight (encoder and adjoint pass); the GPU
+kernels are checked against it.
 """
 import numpy as np
 
 C = 16
-NAMES = ["W_in", "W_d1", "W_d2", "W_d3", "W_c", "W_u2", "W_u1", "W_u0", "W_out"]
-SHAPES = {"W_in": (C, 3, 3, 3), "W_out": (1, C, 3, 3)}
+NAMES = ["W_in", "W_1", "W_2", "W_3"]
+SHAPES = {"W_in": (C, 3, 3, 3)}
 
 
 def shape(name):
@@ -71,19 +78,26 @@ def conv(x, w):
     return out
 
 
-def conv_backward(x, w, g):
-    """Gradients of conv: returns (dx, dw) for upstream gradient g (Co, n, m)."""
+def convT(g, w):
+    """Adjoint of conv(., w): g (Co, n, m) -> (Ci, n, m)."""
+    co, n, m = g.shape
+    out = np.zeros((w.shape[1], n + 2, m + 2))
+    for dy in range(3):
+        for dx in range(3):
+            out[:, dy:dy + n, dx:dx + m] += np.einsum("oc,onm->cnm", w[:, :, dy, dx], g)
+    return out[:, 1:-1, 1:-1]
+
+
+def wgrad(g, x):
+    """dW of conv(x, W) for output gradient g: dW[o, c, dy, dx] = sum g[o] * shifted x[c]."""
     ci, n, m = x.shape
     xp = np.zeros((ci, n + 2, m + 2))
     xp[:, 1:-1, 1:-1] = x
-    dw = np.zeros_like(w, dtype=np.float64)
-    dxp = np.zeros((ci, n + 2, m + 2))
+    dw = np.zeros((g.shape[0], ci, 3, 3))
     for dy in range(3):
         for dx in range(3):
-            patch = xp[:, dy:dy + n, dx:dx + m]
-            dw[:, :, dy, dx] = np.einsum("onm,cnm->oc", g, patch)
-            dxp[:, dy:dy + n, dx:dx + m] += np.einsum("oc,onm->cnm", w[:, :, dy, dx], g)
-    return dxp[:, 1:-1, 1:-1], dw
+            dw[:, :, dy, dx] = np.einsum("onm,cnm->oc", g, xp[:, dy:dy + n, dx:dx + m])
+    return dw
 
 
 def pool(x):
@@ -91,17 +105,9 @@ def pool(x):
     return x.reshape(c, n // 2, 2, m // 2, 2).mean(axis=(2, 4))
 
 
-def pool_backward(g):
-    return np.repeat(np.repeat(g, 2, axis=1), 2, axis=2) * 0.25
-
-
-def up(x):
-    return np.repeat(np.repeat(x, 2, axis=1), 2, axis=2)
-
-
-def up_backward(g):
-    c, n, m = g.shape
-    return g.reshape(c, n // 2, 2, m // 2, 2).sum(axis=(2, 4))
+def poolT(y):
+    """Adjoint of the 2x2 mean: 0.25 * nearest upsampling."""
+    return np.repeat(np.repeat(y, 2, axis=1), 2, axis=2) * 0.25
 
 
 def inputs(r, sk, sg):
@@ -111,50 +117,56 @@ def inputs(r, sk, sg):
 def forward(W, r, sk, sg, jacobi):
     """r: (n, n) residual; returns z (n, n) and a cache for backward."""
     Wd = {k: v.astype(np.float64) for k, v in W.items()}
-    x = inputs(np.asarray(r, dtype=np.float64), sk, sg)
-    a0 = conv(x, Wd["W_in"])
-    p0 = pool(a0)
-    a1 = conv(p0, Wd["W_d1"])
-    p1 = pool(a1)
-    a2 = conv(p1, Wd["W_d2"])
-    p2 = pool(a2)
-    c3 = conv(p2, Wd["W_d3"])
-    a3 = conv(c3, Wd["W_c"])
-    s2 = up(a3) + a2
-    b2 = conv(s2, Wd["W_u2"])
-    s1 = up(b2) + a1
-    b1 = conv(s1, Wd["W_u1"])
-    s0 = up(b1) + a0
-    b0 = conv(s0, Wd["W_u0"])
-    z = (conv(b0, Wd["W_out"])[0] + x[0]) * jacobi
-    cache = dict(x=x, a0=a0, p0=p0, a1=a1, p1=p1, a2=a2, p2=p2, c3=c3, a3=a3, s2=s2, b2=b2, s1=s1,
-                 b1=b1, s0=s0, b0=b0, Wd=Wd, jacobi=jacobi)
+    r = np.asarray(r, dtype=np.float64)
+    x = inputs(r, sk, sg)
+    h0 = conv(x, Wd["W_in"])
+    p0 = pool(h0)
+    h1 = conv(p0, Wd["W_1"])
+    p1 = pool(h1)
+    h2 = conv(p1, Wd["W_2"])
+    p2 = pool(h2)
+    h3 = conv(p2, Wd["W_3"])
+    g3 = h3
+    g2 = h2 + poolT(convT(g3, Wd["W_3"]))
+    g1 = h1 + poolT(convT(g2, Wd["W_2"]))
+    g0 = h0 + poolT(convT(g1, Wd["W_1"]))
+    gx = convT(g0, Wd["W_in"])
+    u = gx[0] + sk * gx[1] + sg * gx[2]
+    z = (r + u) * jacobi
+    cache = dict(x=x, p0=p0, p1=p1, p2=p2, g3=g3, g2=g2, g1=g1, g0=g0, Wd=Wd, jacobi=jacobi, sk=sk,
+                 sg=sg)
     return z, cache
 
 
 def backward(cache, gz):
     """dL/dW for all weights given dL/dz (n, n)."""
-    Wd = cache["Wd"]
-    dW = {}
-    g = (np.asarray(gz, dtype=np.float64) * cache["jacobi"])[None]
-    gb0, dW["W_out"] = conv_backward(cache["b0"], Wd["W_out"], g)
-    gs0, dW["W_u0"] = conv_backward(cache["s0"], Wd["W_u0"], gb0)
-    ga0 = gs0.copy()
-    gb1 = up_backward(gs0)
-    gs1, dW["W_u1"] = conv_backward(cache["s1"], Wd["W_u1"], gb1)
-    ga1 = gs1.copy()
-    gb2 = up_backward(gs1)
-    gs2, dW["W_u2"] = conv_backward(cache["s2"], Wd["W_u2"], gb2)
-    ga2 = gs2.copy()
-    ga3 = up_backward(gs2)
-    gc3, dW["W_c"] = conv_backward(cache["c3"], Wd["W_c"], ga3)
-    gp2, dW["W_d3"] = conv_backward(cache["p2"], Wd["W_d3"], gc3)
-    ga2 += pool_backward(gp2)
-    gp1, dW["W_d2"] = conv_backward(cache["p1"], Wd["W_d2"], ga2)
-    ga1 += pool_backward(gp1)
-    gp0, dW["W_d1"] = conv_backward(cache["p0"], Wd["W_d1"], ga1)
-    ga0 += pool_backward(gp0)
-    _, dW["W_in"] = conv_backward(cache["x"], Wd["W_in"], ga0)
+    c = cache
+    Wd = c["Wd"]
+    gu = np.asarray(gz, dtype=np.float64) * c["jacobi"]
+    dgx = np.stack([gu, c["sk"] * gu, c["sg"] * gu])
+    # adjoint pass: each convT(a, W) contributes dW = wgrad(a, dy) and passes conv(dy, W) down
+    dW = {"W_in": wgrad(c["g0"], dgx)}
+    dg0 = conv(dgx, Wd["W_in"])
+    dh0 = dg0.copy()
+    dy1 = pool(dg0)
+    dW["W_1"] = wgrad(c["g1"], dy1)
+    dg1 = conv(dy1, Wd["W_1"])
+    dh1 = dg1.copy()
+    dy2 = pool(dg1)
+    dW["W_2"] = wgrad(c["g2"], dy2)
+    dg2 = conv(dy2, Wd["W_2"])
+    dh2 = dg2.copy()
+    dy3 = pool(dg2)
+    dW["W_3"] = wgrad(c["g3"], dy3)
+    dh3 = conv(dy3, Wd["W_3"])
+    # encoder
+    dW["W_3"] += wgrad(dh3, c["p2"])
+    dh2 += poolT(convT(dh3, Wd["W_3"]))
+    dW["W_2"] += wgrad(dh2, c["p1"])
+    dh1 += poolT(convT(dh2, Wd["W_2"]))
+    dW["W_1"] += wgrad(dh1, c["p0"])
+    dh0 += poolT(convT(dh1, Wd["W_1"]))
+    dW["W_in"] += wgrad(dh0, c["x"])
     return dW
 
 

@@ -1,6 +1,7 @@
 """The CPU reference of the learned preconditioner (oracle/convnet.py) checked by itself:
-hand-written gradients against central finite differences, linearity in the residual, and
-BF16 rounding against numpy's float32 bit patterns."""
+hand-written gradients against central finite differences, linearity in the residual,
+symmetry and positive definiteness of the preconditioner, and BF16 rounding against numpy's
+float32 bit patterns."""
 import numpy as np
 
 from oracle import convnet
@@ -28,6 +29,20 @@ def test_linear_in_the_residual():
     z2, _ = convnet.forward(W, r2, 0.3, -0.4, 0.7)
     z12, _ = convnet.forward(W, 2.0 * r1 - 3.0 * r2, 0.3, -0.4, 0.7)
     assert np.allclose(z12, 2.0 * z1 - 3.0 * z2, rtol=1e-12, atol=1e-12)
+
+
+def test_preconditioner_is_symmetric_positive_definite():
+    """P r = D (r + E^T E r): <P a, b> = <a, P b> and <P a, a> > 0, checked on the dense
+    matrix of P for a 16 x 16 grid."""
+    W = convnet.init_weights(seed=7)
+    n = 16
+    P = np.zeros((n * n, n * n))
+    for k in range(n * n):
+        e = np.zeros(n * n)
+        e[k] = 1.0
+        P[:, k] = convnet.forward(W, e.reshape(n, n), 0.4, -0.3, 0.2)[0].ravel()
+    assert np.allclose(P, P.T, rtol=1e-12, atol=1e-12 * np.abs(P).max())
+    assert np.linalg.eigvalsh(0.5 * (P + P.T)).min() >= 0.2 * (1 - 1e-12)
 
 
 def test_zero_network_is_jacobi():
