@@ -559,12 +559,13 @@ def run_precond_profile(args):
     x = P.vector()
     net = sts.Net(ctx, n, seed=1)
     gh = 1e-3
+    # tolerances no solve reaches in 16 iterations; FCG without its fallback (negative maxit)
     for _ in range(args.warmup):
-        sts.fcg_solve(P, gh, net, b, x, tol=1e-14, maxit=16)
+        sts.fcg_solve(P, gh, net, b, x, tol=1e-14, maxit=-16)
         sts.implicit_solve_pcg(P, gh, b, x, tol=1e-14, maxit=16)
     ctx.synchronize()
     t0 = time.perf_counter()
-    it1, _, _ = sts.fcg_solve(P, gh, net, b, x, tol=1e-14, maxit=16)
+    it1, _, _ = sts.fcg_solve(P, gh, net, b, x, tol=1e-14, maxit=-16)
     t1 = time.perf_counter()
     it2, _, _ = sts.implicit_solve_pcg(P, gh, b, x, tol=1e-14, maxit=16)
     t2 = time.perf_counter()

@@ -224,6 +224,237 @@ __global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __re
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Row-marching convolution: a CTA owns a 64-column strip of one image and marches down a
+// segment of rows, keeping a ring of 4 input rows (66 pixels with the halo, swizzled) in
+// shared memory. Row y+2 is fetched while row y is computed (cp.async for plain BF16 input;
+// register prefetch and conversion for the FP64-residual and skip-sum loaders), so the halo
+// overhead is 2 rows per segment instead of 2 per 4-row tile and the loads overlap the MMAs.
+// Same arithmetic, fragment layout and output modes as conv3x3_kernel (bitwise identical).
+// ---------------------------------------------------------------------------------------
+constexpr int MRING = 4;
+constexpr int ROWB  = (TC + 2) * 32; // bytes of one staged row
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid)
+{
+  const int n = valid ? 16 : 0; // zero-fill when the pixel lies outside the image
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// raw data of the (up to two) 16-byte chunks a thread stages for one row
+struct RowRaw {
+  uint4 f[2], c[2];
+  double r[2];
+};
+
+template <int LOAD>
+__device__ __forceinline__ void fetch_row(RowRaw& raw, const __nv_bfloat16* in, int H, int W, int x0, int row,
+                                          long long img_pix, const LoadArgs& la, int tid)
+{
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+  {
+    const int c = tid + q * NTHR;
+    raw.f[q] = raw.c[q] = make_uint4(0, 0, 0, 0);
+    raw.r[q] = 0.0;
+    if (c >= (TC + 2) * 2) continue;
+    const int h = c & 1, tx = c >> 1, gx = x0 + tx - 1;
+    if (row < 0 || row >= H || gx < 0 || gx >= W) continue;
+    if (LOAD == LD_R64)
+    {
+      if (h == 0) raw.r[q] = la.r[img_pix + (long long)row * W + gx];
+    }
+    else
+    {
+      raw.f[q] = *reinterpret_cast<const uint4*>(in + ((long long)row * W + gx) * CH + h * 8);
+      raw.c[q] = *reinterpret_cast<const uint4*>(la.coarse + (img_pix / 4 + (long long)(row / 2) * (W / 2) + gx / 2) * CH +
+                                                 h * 8);
+    }
+  }
+}
+
+template <int LOAD>
+__device__ __forceinline__ void store_row(const RowRaw& raw, unsigned char* slot, int H, int W, int x0, int row,
+                                          const LoadArgs& la, int tid)
+{
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+  {
+    const int c = tid + q * NTHR;
+    if (c >= (TC + 2) * 2) continue;
+    const int h = c & 1, tx = c >> 1, gx = x0 + tx - 1;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (row >= 0 && row < H && gx >= 0 && gx < W)
+    {
+      if (LOAD == LD_R64)
+      {
+        if (h == 0)
+        {
+          const float xv = (float)(raw.r[q] * la.scale);
+          __nv_bfloat162 c01 = __halves2bfloat162(__float2bfloat16_rn(xv), __float2bfloat16_rn(xv * la.sk));
+          __nv_bfloat162 c23 = __halves2bfloat162(__float2bfloat16_rn(xv * la.sg), __float2bfloat16_rn(0.f));
+          v.x = *reinterpret_cast<uint32_t*>(&c01);
+          v.y = *reinterpret_cast<uint32_t*>(&c23);
+        }
+      }
+      else
+      {
+        const __nv_bfloat162* fb = reinterpret_cast<const __nv_bfloat162*>(&raw.f[q]);
+        const __nv_bfloat162* cb = reinterpret_cast<const __nv_bfloat162*>(&raw.c[q]);
+        uint32_t o[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+          const float2 a = __bfloat1622float2(fb[k]), b = __bfloat1622float2(cb[k]);
+          __nv_bfloat162 t = __floats2bfloat162_rn(la.cscale * b.x + a.x, la.cscale * b.y + a.y);
+          o[k] = *reinterpret_cast<uint32_t*>(&t);
+        }
+        v = make_uint4(o[0], o[1], o[2], o[3]);
+      }
+    }
+    *reinterpret_cast<uint4*>(slot + swz(tx, h)) = v;
+  }
+}
+
+template <int MODE, int LOAD = LD_PLAIN>
+__global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16* __restrict__ in, int H, int W,
+                                                             const uint2* __restrict__ wf,
+                                                             __nv_bfloat16* __restrict__ out,
+                                                             double* __restrict__ out64, double out_scale,
+                                                             const float* __restrict__ meta, LoadArgs la, int rows)
+{
+  __shared__ __align__(128) unsigned char ring[MRING][ROWB];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int x0 = blockIdx.x * TC;
+  const int ys = blockIdx.y * rows, ye = min(H, ys + rows);
+  const long long img_pix = (long long)H * W * blockIdx.z;
+  if (LOAD != LD_R64) in += img_pix * CH;
+  if (MODE == 0) out += img_pix * CH;
+  else
+  {
+    out64 += img_pix;
+    if (meta)
+    {
+      out_scale = meta_out_scale(meta, blockIdx.z);
+      la.scale  = (double)meta[META * blockIdx.z + 3];
+      la.sk     = meta[META * blockIdx.z];
+      la.sg     = meta[META * blockIdx.z + 1];
+    }
+  }
+  if (ys >= H) return;
+  auto slot = [&](int r) { return &ring[(r - ys + 1) & (MRING - 1)][0]; };
+  auto issue_plain = [&](int r) { // cp.async of row r (zero rows and columns outside the image)
+    unsigned char* sl = slot(r);
+    for (int c = tid; c < (TC + 2) * 2; c += NTHR)
+    {
+      const int h = c & 1, tx = c >> 1, gx = x0 + tx - 1;
+      const bool valid = r >= 0 && r < H && gx >= 0 && gx < W;
+      const __nv_bfloat16* src = valid ? in + ((long long)r * W + gx) * CH + h * 8 : in;
+      cp_async16(smem_u32(sl + swz(tx, h)), src, valid);
+    }
+    cp_async_commit();
+  };
+  // weights into registers
+  uint2 wr[9][2];
+#pragma unroll
+  for (int t = 0; t < 9; ++t)
+#pragma unroll
+    for (int nh = 0; nh < 2; ++nh) wr[t][nh] = (MODE == 0 || nh == 0) ? wf[(t * 2 + nh) * 32 + lane] : make_uint2(0, 0);
+  // prologue: rows ys-1, ys, ys+1
+  RowRaw raw;
+  if (LOAD == LD_PLAIN)
+  {
+    issue_plain(ys - 1);
+    issue_plain(ys);
+    issue_plain(ys + 1);
+  }
+  else
+    for (int r = ys - 1; r <= ys + 1; ++r)
+    {
+      fetch_row<LOAD>(raw, in, H, W, x0, r, img_pix, la, tid);
+      store_row<LOAD>(raw, slot(r), H, W, x0, r, la, tid);
+    }
+  for (int y = ys; y < ye; ++y)
+  {
+    // A: fetch row y+2 (needed by output row y+1)
+    const bool more = y + 2 <= ye;
+    if (LOAD == LD_PLAIN)
+    {
+      if (more) issue_plain(y + 2);
+      else cp_async_commit(); // empty group keeps the wait count uniform
+      cp_async_wait1();       // rows up to y+1 have landed
+    }
+    else if (more)
+      fetch_row<LOAD>(raw, in, H, W, x0, y + 2, img_pix, la, tid);
+    __syncthreads();
+    // B: output row y, one 16-pixel m-tile per warp
+    {
+      const int mt = warp;
+      float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+      for (int t = 0; t < 9; ++t)
+      {
+        const int dy = t / 3, dx = t % 3;
+        const int pi = (lane & 7) + ((lane >> 3) & 1) * 8;
+        const int hh = lane >> 4;
+        const int px = mt * 16 + pi + dx;
+        const unsigned char* rp = slot(y - 1 + dy) + swz(px, hh);
+        uint32_t a0, a1, a2, a3;
+        asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                     : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3)
+                     : "r"(smem_u32(rp)));
+#pragma unroll
+        for (int nh = 0; nh < (MODE == 0 ? 2 : 1); ++nh)
+        {
+          asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                       "{%0,%1,%2,%3};"
+                       : "+f"(acc[nh][0]), "+f"(acc[nh][1]), "+f"(acc[nh][2]), "+f"(acc[nh][3])
+                       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(wr[t][nh].x), "r"(wr[t][nh].y));
+        }
+      }
+      const int pr0 = lane >> 2;
+      float c2h[2] = {0.f, 0.f};
+      if (MODE != 0)
+      {
+        c2h[0] = __shfl_down_sync(0xffffffffu, acc[0][0], 1);
+        c2h[1] = __shfl_down_sync(0xffffffffu, acc[0][2], 1);
+      }
+#pragma unroll
+      for (int half = 0; half < 2; ++half)
+      {
+        const int gx = x0 + mt * 16 + pr0 + half * 8;
+        if (gx >= W) continue;
+        const long long p = (long long)y * W + gx;
+        if (MODE == 0)
+        {
+#pragma unroll
+          for (int nh = 0; nh < 2; ++nh)
+          {
+            const int co = nh * 8 + (lane & 3) * 2;
+            __nv_bfloat162 v = __floats2bfloat162_rn(acc[nh][half * 2], acc[nh][half * 2 + 1]);
+            *reinterpret_cast<__nv_bfloat162*>(out + p * CH + co) = v;
+          }
+        }
+        else if ((lane & 3) == 0)
+        {
+          double v = (double)acc[0][half * 2] + (double)la.sk * (double)acc[0][half * 2 + 1] +
+                     (double)la.sg * (double)c2h[half];
+          if (la.r) v += la.r[img_pix + p] * la.scale;
+          else if (la.r32) v += (double)la.r32[img_pix + p] * la.scale;
+          out64[p] = v * out_scale;
+        }
+      }
+    }
+    // C: stage the prefetched row (its slot held row y-2, last read before the previous barrier)
+    if (LOAD != LD_PLAIN && more) store_row<LOAD>(raw, slot(y + 2), H, W, x0, y + 2, la, tid);
+    __syncthreads(); // D: row y's slots free for reuse, row y+2 visible
+  }
+  if (LOAD == LD_PLAIN) cp_async_wait0();
+}
+
 // 2x2 mean pooling (FP32 arithmetic, BF16 storage); W, H of the fine level
 __global__ void pool_kernel(const __nv_bfloat16* __restrict__ in, int H, int W, __nv_bfloat16* __restrict__ out)
 {
@@ -718,11 +949,39 @@ extern "C" int STS_NetGetWeights(STS_Net nt, float* w)
   return STS_CUDA_OK(cudaMemcpy(w, nt->w, NLAYER * WSZ * 4, cudaMemcpyDeviceToHost)) ? 0 : -1;
 }
 
+// launch shape of the row-marching convolution: 64-column strips, row segments sized so that
+// the grid holds at least 4 CTAs per SM (each CTA keeps 8.4 KB of rows in flight)
+struct MarchGrid {
+  dim3 grid;
+  int rows;
+};
+static MarchGrid march_grid(STS_Net nt, int n, int nimg)
+{
+  const int strips = (n + net::TC - 1) / net::TC;
+  const long long want = 4LL * nt->ctx->num_sms;
+  long long segs = (want + (long long)strips * nimg - 1) / ((long long)strips * nimg);
+  if (segs < 1) segs = 1;
+  int rows = (int)((n + segs - 1) / segs);
+  if (rows < 4) rows = 4;
+  MarchGrid m;
+  m.rows = rows;
+  m.grid = dim3((unsigned)strips, (unsigned)((n + rows - 1) / rows), (unsigned)nimg);
+  return m;
+}
+
+template <int MODE, int LOAD = net::LD_PLAIN>
+static void conv_launch(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, const uint2* frags, __nv_bfloat16* out,
+                        double* out64, double out_scale, const float* meta, const net::LoadArgs& la)
+{
+  const MarchGrid m = march_grid(nt, n, nimg);
+  net::conv3x3_march_kernel<MODE, LOAD><<<m.grid, net::NTHR, 0, nt->ctx->stream>>>(in, n, n, frags, out, out64,
+                                                                                 out_scale, meta, la, m.rows);
+}
+
 static void conv(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, int layer, bool transposed, __nv_bfloat16* out)
 {
-  dim3 g((unsigned)((n + net::TC - 1) / net::TC), (unsigned)((n + net::TR - 1) / net::TR), (unsigned)nimg);
-  net::conv3x3_kernel<0><<<g, net::NTHR, 0, nt->ctx->stream>>>(in, n, n, (transposed ? nt->wt : nt->wf) + layer * 576,
-                                                               out, nullptr, 0.0, nullptr);
+  conv_launch<0>(nt, in, n, nimg, (transposed ? nt->wt : nt->wf) + layer * 576, out, nullptr, 0.0, nullptr,
+                 net::LoadArgs());
 }
 
 static void pool(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, __nv_bfloat16* out)
@@ -762,15 +1021,13 @@ static void net_forward(STS_Net nt, int n, int nimg, const T* r, double scale, f
   upadd(nt, L[2].y, L[1].h, n / 2, nimg, L[1].g);               // g1
   conv(nt, L[1].g, n / 2, nimg, net::L_1, true, L[1].y);        // y1
   upadd(nt, L[1].y, L[0].h, n, nimg, L[0].g);                   // g0
-  dim3 g((unsigned)((n + net::TC - 1) / net::TC), (unsigned)((n + net::TR - 1) / net::TR), (unsigned)nimg);
   net::LoadArgs la; // Jacobi skip from the network input; sk, sg for the output combination
   if constexpr (sizeof(T) == 8) la.r = reinterpret_cast<const double*>(r);
   else la.r32 = reinterpret_cast<const float*>(r);
   la.scale = scale;
   la.sk    = sk;
   la.sg    = sg;
-  net::conv3x3_kernel<2><<<g, net::NTHR, 0, st>>>(L[0].g, n, n, nt->wt + net::L_IN * 576, nullptr,
-                                                  zout ? zout : nt->z, out_scale, meta, la); // z
+  conv_launch<2>(nt, L[0].g, n, nimg, nt->wt + net::L_IN * 576, nullptr, zout ? zout : nt->z, out_scale, meta, la); // z
 }
 
 // Inference of one n x n residual (FP64, device) into zout: the input channels are built in the
@@ -781,14 +1038,12 @@ static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
 {
   cudaStream_t st = nt->ctx->stream;
   net::Level* L   = nt->L;
-  auto grid = [](int m) { return dim3((unsigned)((m + net::TC - 1) / net::TC), (unsigned)((m + net::TR - 1) / net::TR), 1u); };
   net::LoadArgs la;
   la.r     = r;
   la.scale = scale;
   la.sk    = sk;
   la.sg    = sg;
-  net::conv3x3_kernel<0, net::LD_R64><<<grid(n), net::NTHR, 0, st>>>(nullptr, n, n, nt->wf + net::L_IN * 576, L[0].h,
-                                                                      nullptr, 0.0, nullptr, la);     // h0
+  conv_launch<0, net::LD_R64>(nt, nullptr, n, 1, nt->wf + net::L_IN * 576, L[0].h, nullptr, 0.0, nullptr, la); // h0
   pool(nt, L[0].h, n, 1, L[1].p);
   conv(nt, L[1].p, n / 2, 1, net::L_1, false, L[1].h);                                                // h1
   pool(nt, L[1].h, n / 2, 1, L[2].p);
@@ -799,18 +1054,15 @@ static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
   net::LoadArgs lu;
   lu.cscale = 0.25f;
   lu.coarse = L[3].y;
-  net::conv3x3_kernel<0, net::LD_UPADD><<<grid(n / 4), net::NTHR, 0, st>>>(L[2].h, n / 4, n / 4, nt->wt + net::L_2 * 576,
-                                                                            L[2].y, nullptr, 0.0, nullptr, lu); // y2
+  conv_launch<0, net::LD_UPADD>(nt, L[2].h, n / 4, 1, nt->wt + net::L_2 * 576, L[2].y, nullptr, 0.0, nullptr, lu); // y2
   lu.coarse = L[2].y;
-  net::conv3x3_kernel<0, net::LD_UPADD><<<grid(n / 2), net::NTHR, 0, st>>>(L[1].h, n / 2, n / 2, nt->wt + net::L_1 * 576,
-                                                                            L[1].y, nullptr, 0.0, nullptr, lu); // y1
+  conv_launch<0, net::LD_UPADD>(nt, L[1].h, n / 2, 1, nt->wt + net::L_1 * 576, L[1].y, nullptr, 0.0, nullptr, lu); // y1
   lu.coarse = L[1].y;
   lu.r      = r;
   lu.scale  = scale;
   lu.sk     = sk;
   lu.sg     = sg;
-  net::conv3x3_kernel<2, net::LD_UPADD><<<grid(n), net::NTHR, 0, st>>>(L[0].h, n, n, nt->wt + net::L_IN * 576, nullptr,
-                                                                        zout, out_scale, nullptr, lu);  // z
+  conv_launch<2, net::LD_UPADD>(nt, L[0].h, n, 1, nt->wt + net::L_IN * 576, nullptr, zout, out_scale, nullptr, lu); // z
 }
 
 static void wgrad(STS_Net nt, const __nv_bfloat16* x, const __nv_bfloat16* g, int n, int nimg, int layer)
@@ -1230,6 +1482,8 @@ __global__ void true_residual_kernel(ProbDev P, double gamma, const double* __re
 extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b, N_Vector x, double tol, int maxit,
                             int* iters, double* relres)
 {
+  const bool fallback = maxit > 0; // maxit < 0: at most -maxit iterations, no fallback
+  if (maxit < 0) maxit = -maxit;
   if (!p || !nt || !b || !x || p->nx != p->ny || NVL(b) != p->nx * p->ny || NVL(x) != NVL(b) || maxit < 1 ||
       p->kind == STS_PROBLEM_PERIODIC)
   {
@@ -1338,7 +1592,7 @@ extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b,
     dim3 bb(64, 4), gg((unsigned)((p->nx + 63) / 64), (unsigned)((p->ny + 3) / 4));
     net::true_residual_kernel<<<gg, bb, 0, st>>>(p->dev, gamma, NVD(x), NVD(b), Q2[0]);
     tr = sqrt(sts_dot_exact(ctx, Q2[0], Q2[0], N, SLOT_PCG3)) / bnorm;
-    if ((ret == 1 || ret == -3) && tr == tr && tr > tol)
+    if (fallback && (ret == 1 || ret == -3) && tr == tr && tr > tol)
     {
       // Jacobi-PCG fallback on the correction: (I - gamma A) d = b - (I - gamma A) x, x += d
       N_Vector qv = N_VMake_Sts(N, Q2[0], ctx);

@@ -342,7 +342,8 @@ int STS_HarvestPCGPairs(STS_Problem p, double gamma, N_Vector b, int ncrops, int
 /* flexible CG with the network as preconditioner, x0 = 0, stop at ||r|| <= tol ||b||; on
  * stagnation (maxit) or breakdown it falls back to Jacobi-PCG on the remaining correction.
  * Returns 0 converged, 2 converged through the fallback, 1 not converged, < 0 error; iters
- * counts FCG plus fallback iterations; relres is the true FP64 residual of the returned x. */
+ * counts FCG plus fallback iterations; relres is the true FP64 residual of the returned x.
+ * maxit < 0 runs at most -maxit FCG iterations without the fallback. */
 int STS_FCGSolve(STS_Problem p, double gamma, STS_Net net, N_Vector b, N_Vector x, double tol,
                  int maxit, int* iters, double* relres);
 
