@@ -390,10 +390,12 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
     else if (more)
       fetch_row<LOAD>(raw, in, H, W, x0, y + 2, img_pix, la, tid);
     __syncthreads();
-    // B: output row y, one 16-pixel m-tile per warp
+    // B: output row y, one 16-pixel m-tile per warp; taps in two independent accumulator
+    // chains (rows y-1, y | row y+1) that are added at the end, to overlap MMA latencies
     {
       const int mt = warp;
       float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+      float acd[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
       for (int t = 0; t < 9; ++t)
       {
@@ -406,15 +408,20 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
         asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
                      : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3)
                      : "r"(smem_u32(rp)));
+        float(&A)[2][4] = (t < 6) ? acc : acd;
 #pragma unroll
         for (int nh = 0; nh < (MODE == 0 ? 2 : 1); ++nh)
         {
           asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
                        "{%0,%1,%2,%3};"
-                       : "+f"(acc[nh][0]), "+f"(acc[nh][1]), "+f"(acc[nh][2]), "+f"(acc[nh][3])
+                       : "+f"(A[nh][0]), "+f"(A[nh][1]), "+f"(A[nh][2]), "+f"(A[nh][3])
                        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(wr[t][nh].x), "r"(wr[t][nh].y));
         }
       }
+#pragma unroll
+      for (int nh = 0; nh < 2; ++nh)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[nh][q] += acd[nh][q];
       const int pr0 = lane >> 2;
       float c2h[2] = {0.f, 0.f};
       if (MODE != 0)
@@ -958,11 +965,11 @@ struct MarchGrid {
 static MarchGrid march_grid(STS_Net nt, int n, int nimg)
 {
   const int strips = (n + net::TC - 1) / net::TC;
-  const long long want = 4LL * nt->ctx->num_sms;
+  const long long want = 16LL * nt->ctx->num_sms; // several waves of up to 7 resident CTAs per SM
   long long segs = (want + (long long)strips * nimg - 1) / ((long long)strips * nimg);
   if (segs < 1) segs = 1;
   int rows = (int)((n + segs - 1) / segs);
-  if (rows < 4) rows = 4;
+  if (rows < 8) rows = 8;
   MarchGrid m;
   m.rows = rows;
   m.grid = dim3((unsigned)strips, (unsigned)((n + rows - 1) / rows), (unsigned)nimg);
@@ -1376,15 +1383,15 @@ __global__ void __launch_bounds__(256) fcg_beta_kernel(long long n, const double
   });
 }
 
-__device__ __forceinline__ double fcg_p(const double* z, const double* pp, double beta, long long k)
-{
-  return __fma_rn(beta, pp[k], z[k]);
-}
-
-__global__ void __launch_bounds__(256) fcg_pq_kernel(ProbDev P, const double* __restrict__ z,
-                                                     const double* __restrict__ pp, const double* __restrict__ r,
-                                                     double* __restrict__ p, double* __restrict__ q, FcgScal* s,
-                                                     FcgOut* out)
+// KP: p = z + beta p_prev, q = (I - gamma A) p, p.r and p.q -> alpha. A thread owns one column of a segment of FCG_ROWS rows
+// and forms p = z + beta p_prev once per point (rows j-1, j, j+1 in registers, west/east
+// neighbours by warp shuffles; the two warp-edge lanes form their outside neighbours from
+// z and p_prev directly), so p is formed once per point.
+constexpr int FCG_ROWS = 64;
+__global__ void __launch_bounds__(256) fcg_pq_march_kernel(ProbDev P, const double* __restrict__ z,
+                                                           const double* __restrict__ pp,
+                                                           const double* __restrict__ r, double* __restrict__ p,
+                                                           double* __restrict__ q, FcgScal* s, FcgOut* out)
 {
   if (s->state != 0) return;
   const double gamma = s->gamma, beta = s->beta;
@@ -1393,17 +1400,31 @@ __global__ void __launch_bounds__(256) fcg_pq_kernel(ProbDev P, const double* __
   xsum::zero(a[0]);
   xsum::zero(a[1]);
   const long long nx = P.nx, ny = P.ny;
+  const int lane     = threadIdx.x & 31;
   const long long i  = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < nx)
-    for (long long j = blockIdx.y; j < ny; j += gridDim.y)
+  const bool col     = i < nx;
+  const long long ic = col ? i : nx - 1; // inactive lanes shadow the last column (no stores)
+  const long long j0 = (long long)blockIdx.y * FCG_ROWS;
+  const long long j1 = j0 + FCG_ROWS < ny ? j0 + FCG_ROWS : ny;
+  auto pval = [&](long long ii, long long jj) -> double {
+    if (ii < 0 || ii >= nx || jj < 0 || jj >= ny) return 0.0;
+    const long long k = jj * nx + ii;
+    return __fma_rn(beta, pp[k], z[k]);
+  };
+  double pm = pval(ic, j0 - 1), pc = pval(ic, j0);
+  for (long long j = j0; j < j1; ++j)
+  {
+    const double pn = pval(ic, j + 1);
+    double pw = __shfl_up_sync(0xffffffffu, pc, 1);
+    double pe = __shfl_down_sync(0xffffffffu, pc, 1);
+    if (lane == 0) pw = pval(ic - 1, j);
+    if (lane == 31) pe = pval(ic + 1, j);
+    if (ic == 0) pw = 0.0;
+    if (ic == nx - 1) pe = 0.0;
+    if (col)
     {
-      const long long k = j * nx + i;
-      const double pc   = fcg_p(z, pp, beta, k);
-      const double pw   = (i > 0) ? fcg_p(z, pp, beta, k - 1) : 0.0;
-      const double pe   = (i < nx - 1) ? fcg_p(z, pp, beta, k + 1) : 0.0;
-      const double ps   = (j > 0) ? fcg_p(z, pp, beta, k - nx) : 0.0;
-      const double pn   = (j < ny - 1) ? fcg_p(z, pp, beta, k + nx) : 0.0;
-      const double sx = pw + pe, sy = ps + pn;
+      const long long k = j * nx + ic;
+      const double sx = pw + pe, sy = pm + pn;
       double acc = P.cc * pc;
       acc        = __fma_rn(P.cx, sx, acc);
       acc        = __fma_rn(P.cy, sy, acc);
@@ -1413,6 +1434,9 @@ __global__ void __launch_bounds__(256) fcg_pq_kernel(ProbDev P, const double* __
       xsum::add(a[0], pc * r[k], fl[0]);
       xsum::add(a[1], pc * qk, fl[1]);
     }
+    pm = pc;
+    pc = pn;
+  }
   krylov_block_finish<256, 2>(a, fl, s, [&](const double* v) {
     s->alpha   = v[0] / v[1];
     s->pq_prev = v[1];
@@ -1541,9 +1565,7 @@ extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b,
     const int eb = ew_blocks(ctx, N, 256 * 2);
     dim3 bq(256, 1);
     const unsigned gx = (unsigned)((p->nx + 255) / 256);
-    long long gy_cap  = (long long)ctx->num_sms * 8 / gx;
-    if (gy_cap < 1) gy_cap = 1;
-    dim3 gq(gx, (unsigned)(p->ny < gy_cap ? p->ny : gy_cap));
+    dim3 gm(gx, (unsigned)((p->ny + net::FCG_ROWS - 1) / net::FCG_ROWS));
     cudaGraph_t g;
     cudaGraphExec_t ge = nullptr;
     bool ok = STS_CUDA_OK(cudaStreamSynchronize(st)) &&
@@ -1556,7 +1578,7 @@ extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b,
         double *qp = Q2[k & 1], *qn = Q2[(k + 1) & 1];
         net_forward_infer(nt, n, r, scale, (float)sk, (float)sg, jac / scale, z);
         net::fcg_beta_kernel<<<eb, 256, 0, st>>>(N, z, qp, d_s);
-        net::fcg_pq_kernel<<<gq, bq, 0, st>>>(p->dev, z, pp, r, pn, qn, d_s, d_out);
+        net::fcg_pq_march_kernel<<<gm, bq, 0, st>>>(p->dev, z, pp, r, pn, qn, d_s, d_out);
         net::fcg_x_kernel<<<eb, 256, 0, st>>>(N, pn, qn, NVD(x), r, d_s, d_out);
       }
       ok = STS_CUDA_OK(cudaStreamEndCapture(st, &g));
