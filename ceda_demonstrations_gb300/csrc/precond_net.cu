@@ -36,14 +36,14 @@ constexpr int NLAYER = 4; // W_in, W_1, W_2, W_3
 constexpr int WSZ = CH * CH * 9; // every layer stored as 16 x 16 x 3 x 3 (zero padded)
 enum { L_IN = 0, L_1, L_2, L_3 };
 
-// conv tile: CTA = 4 warps, tile = TR rows x 64 columns, each warp one row at a time
+// convolution strip: CTA = 4 warps, 64 columns (one 16-pixel m-tile per warp)
 constexpr int TC = 64;
-constexpr int TR = 4;
 constexpr int NTHR = 128;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// swizzled byte offset of (pixel p of the tile row, channel half h) within a tile row
+// swizzled byte offset of (pixel p of a staged row, channel half h): the 16-byte halves are
+// XOR-swizzled by pixel so the eight row addresses of an ldmatrix phase hit distinct banks
 __device__ __forceinline__ int swz(int p, int h) { return p * 32 + ((h ^ ((p >> 2) & 1)) << 4); }
 
 // Weight fragments: wf[(tap * 2 + nh) * 32 + lane] = {b0b1, b2b3} for n-half nh
@@ -73,164 +73,15 @@ struct LoadArgs {
   float cscale          = 1.f; // LD_UPADD: in + cscale * up(coarse)
 };
 
-// out[p][co] = sum_{tap, ci} w[co][ci][tap] * in[p + tap - 1][ci], for each image of a batch
-// (blockIdx.z; images of H x W pixels stored one after another, zero padding at every edge)
-// mode 0: BF16 NHWC output (16 channels); mode 2: FP64 output u = c0 + sk c1 + sg c2 of the
-// first three output channels (only the first 8 output channels are computed) plus the
-// Jacobi skip r * scale (la.r or la.r32), times the image's output scale (meta, or out_scale
-// when meta is null); sk, sg from meta or la
-template <int MODE, int LOAD = LD_PLAIN>
-__global__ void __launch_bounds__(NTHR) conv3x3_kernel(const __nv_bfloat16* __restrict__ in, int H, int W,
-                                                       const uint2* __restrict__ wf, __nv_bfloat16* __restrict__ out,
-                                                       double* __restrict__ out64, double out_scale,
-                                                       const float* __restrict__ meta, LoadArgs la = LoadArgs())
-{
-  __shared__ __align__(128) unsigned char tile[(TR + 2) * (TC + 2) * 32];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int x0 = blockIdx.x * TC, y0 = blockIdx.y * TR;
-  const long long img_pix = (long long)H * W * blockIdx.z;
-  if (LOAD != LD_R64) in += img_pix * CH;
-  if (MODE == 0) out += img_pix * CH;
-  else
-  {
-    out64 += img_pix;
-    if (meta)
-    {
-      out_scale = meta_out_scale(meta, blockIdx.z);
-      la.scale  = (double)meta[META * blockIdx.z + 3];
-      la.sk     = meta[META * blockIdx.z];
-      la.sg     = meta[META * blockIdx.z + 1];
-    }
-  }
-  // stage the input tile with a one-pixel halo (16-byte chunks, zero outside the image)
-  for (int c = tid; c < (TR + 2) * (TC + 2) * 2; c += NTHR)
-  {
-    const int h = c & 1, pix = c >> 1;
-    const int ty = pix / (TC + 2), tx = pix % (TC + 2);
-    const int gy = y0 + ty - 1, gx = x0 + tx - 1;
-    uint4 v = make_uint4(0, 0, 0, 0);
-    if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-    {
-      if (LOAD == LD_PLAIN) v = *reinterpret_cast<const uint4*>(in + ((long long)gy * W + gx) * CH + h * 8);
-      else if (LOAD == LD_R64)
-      {
-        if (h == 0)
-        {
-          const float xv = (float)(la.r[img_pix + (long long)gy * W + gx] * la.scale);
-          __nv_bfloat162 c01 = __halves2bfloat162(__float2bfloat16_rn(xv), __float2bfloat16_rn(xv * la.sk));
-          __nv_bfloat162 c23 = __halves2bfloat162(__float2bfloat16_rn(xv * la.sg), __float2bfloat16_rn(0.f));
-          v.x = *reinterpret_cast<uint32_t*>(&c01);
-          v.y = *reinterpret_cast<uint32_t*>(&c23);
-        }
-      }
-      else
-      {
-        const uint4 f = *reinterpret_cast<const uint4*>(in + ((long long)gy * W + gx) * CH + h * 8);
-        const uint4 c = *reinterpret_cast<const uint4*>(
-            la.coarse + (img_pix / 4 + (long long)(gy / 2) * (W / 2) + gx / 2) * CH + h * 8);
-        const __nv_bfloat162* fb = reinterpret_cast<const __nv_bfloat162*>(&f);
-        const __nv_bfloat162* cb = reinterpret_cast<const __nv_bfloat162*>(&c);
-        uint32_t o[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-        {
-          const float2 a = __bfloat1622float2(fb[q]), b = __bfloat1622float2(cb[q]);
-          __nv_bfloat162 t = __floats2bfloat162_rn(la.cscale * b.x + a.x, la.cscale * b.y + a.y);
-          o[q] = *reinterpret_cast<uint32_t*>(&t);
-        }
-        v = make_uint4(o[0], o[1], o[2], o[3]);
-      }
-    }
-    *reinterpret_cast<uint4*>(tile + ty * (TC + 2) * 32 + swz(tx, h)) = v;
-  }
-  // weights into registers
-  uint2 wr[9][2];
-#pragma unroll
-  for (int t = 0; t < 9; ++t)
-#pragma unroll
-    for (int nh = 0; nh < 2; ++nh) wr[t][nh] = (MODE == 0 || nh == 0) ? wf[(t * 2 + nh) * 32 + lane] : make_uint2(0, 0);
-  __syncthreads();
-  const int row = warp; // one tile row per warp (TR == 4 warps)
-  const int gy  = y0 + row;
-#pragma unroll 1
-  for (int mt = 0; mt < TC / 16; ++mt)
-  {
-    float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-#pragma unroll
-    for (int t = 0; t < 9; ++t)
-    {
-      const int dy = t / 3, dx = t % 3;
-      // ldmatrix.x4 row addresses: lanes 0-7 pixels 0-7 half 0, 8-15 pixels 8-15 half 0,
-      // 16-23 pixels 0-7 half 1, 24-31 pixels 8-15 half 1
-      const int pi = (lane & 7) + ((lane >> 3) & 1) * 8;
-      const int hh = lane >> 4;
-      const int px = mt * 16 + pi + dx; // tile column (halo offset included via dx)
-      const unsigned char* rp = tile + (row + dy) * (TC + 2) * 32 + swz(px, hh);
-      uint32_t a0, a1, a2, a3;
-      asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-                   : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3)
-                   : "r"(smem_u32(rp)));
-#pragma unroll
-      for (int nh = 0; nh < (MODE == 0 ? 2 : 1); ++nh)
-      {
-        asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                     "{%0,%1,%2,%3};"
-                     : "+f"(acc[nh][0]), "+f"(acc[nh][1]), "+f"(acc[nh][2]), "+f"(acc[nh][3])
-                     : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(wr[t][nh].x), "r"(wr[t][nh].y));
-      }
-    }
-    // accumulator layout: c0,c1 -> pixel lane/4, channels (lane%4)*2..+1; c2,c3 -> pixel lane/4+8
-    if (gy < H) // uniform across the warp
-    {
-      const int pr0 = lane >> 2;
-      // mode 2: channel 2 sits in the next lane (all lanes take part in the shuffle)
-      float c2h[2] = {0.f, 0.f};
-      if (MODE != 0)
-      {
-        c2h[0] = __shfl_down_sync(0xffffffffu, acc[0][0], 1);
-        c2h[1] = __shfl_down_sync(0xffffffffu, acc[0][2], 1);
-      }
-#pragma unroll
-      for (int half = 0; half < 2; ++half)
-      {
-        const int gx = x0 + mt * 16 + pr0 + half * 8;
-        if (gx >= W) continue;
-        const long long p = (long long)gy * W + gx;
-        if (MODE == 0)
-        {
-#pragma unroll
-          for (int nh = 0; nh < 2; ++nh)
-          {
-            const int co = nh * 8 + (lane & 3) * 2;
-            __nv_bfloat162 v = __floats2bfloat162_rn(acc[nh][half * 2], acc[nh][half * 2 + 1]);
-            *reinterpret_cast<__nv_bfloat162*>(out + p * CH + co) = v;
-          }
-        }
-        else
-        {
-          // channels 0, 1 in this lane (lane % 4 == 0), channel 2 in the next lane
-          const float c2 = c2h[half];
-          if ((lane & 3) == 0)
-          {
-            double v = (double)acc[0][half * 2] + (double)la.sk * (double)acc[0][half * 2 + 1] +
-                       (double)la.sg * (double)c2;
-            if (la.r) v += la.r[img_pix + p] * la.scale;
-            else if (la.r32) v += (double)la.r32[img_pix + p] * la.scale;
-            out64[p] = v * out_scale;
-          }
-        }
-      }
-    }
-  }
-}
-
 // ---------------------------------------------------------------------------------------
 // Row-marching convolution: a CTA owns a 64-column strip of one image and marches down a
 // segment of rows, keeping a ring of 4 input rows (66 pixels with the halo, swizzled) in
 // shared memory. Row y+2 is fetched while row y is computed (cp.async for plain BF16 input;
 // register prefetch and conversion for the FP64-residual and skip-sum loaders), so the halo
 // overhead is 2 rows per segment instead of 2 per 4-row tile and the loads overlap the MMAs.
-// Same arithmetic, fragment layout and output modes as conv3x3_kernel (bitwise identical).
+// Implicit GEMM per row: each warp computes one 16-pixel x 16-channel tile over the nine taps
+// (mma.sync m16n8k16 BF16 -> FP32, A by ldmatrix.x4 from the swizzled ring, weights in
+// registers as B fragments).
 // ---------------------------------------------------------------------------------------
 constexpr int MRING = 4;
 constexpr int ROWB  = (TC + 2) * 32; // bytes of one staged row
@@ -293,7 +144,7 @@ __device__ __forceinline__ void store_row(const RowRaw& raw, unsigned char* slot
       {
         if (h == 0)
         {
-          const float xv = (float)(raw.r[q] * la.scale);
+          const float xv = (float)raw.r[q] * (float)la.scale; // one FP64 instruction (the conversion)
           __nv_bfloat162 c01 = __halves2bfloat162(__float2bfloat16_rn(xv), __float2bfloat16_rn(xv * la.sk));
           __nv_bfloat162 c23 = __halves2bfloat162(__float2bfloat16_rn(xv * la.sg), __float2bfloat16_rn(0.f));
           v.x = *reinterpret_cast<uint32_t*>(&c01);
@@ -316,6 +167,55 @@ __device__ __forceinline__ void store_row(const RowRaw& raw, unsigned char* slot
       }
     }
     *reinterpret_cast<uint4*>(slot + swz(tx, h)) = v;
+  }
+}
+
+// Epilogue of one 16-pixel m-tile of output row y starting at column xb.
+// mode 0: BF16 NHWC, 16 channels. Accumulator layout: c0,c1 -> pixel lane/4, channels
+// (lane%4)*2..+1; c2,c3 -> pixel lane/4 + 8.
+// mode 2: u = c0 + sk c1 + sg c2 (FP32; channel 2 sits in the next lane), redistributed so
+// that lanes 0..15 own pixels 0..15, then z = (out_scale u) + (out_scale scale) r in FP64: two
+// FP64 instructions per 16 pixels (GB300's FP64 issue rate is 1/64 of FP32).
+template <int MODE>
+__device__ __forceinline__ void conv_epilogue(const float (&acc)[2][4], int lane, int xb, int y, int W,
+                                              long long img_pix, __nv_bfloat16* out, double* out64, double out_scale,
+                                              const LoadArgs& la)
+{
+  const int pr0 = lane >> 2;
+  if (MODE == 0)
+  {
+#pragma unroll
+    for (int half = 0; half < 2; ++half)
+    {
+      const int gx = xb + pr0 + half * 8;
+      if (gx >= W) continue;
+      const long long p = (long long)y * W + gx;
+#pragma unroll
+      for (int nh = 0; nh < 2; ++nh)
+      {
+        const int co = nh * 8 + (lane & 3) * 2;
+        __nv_bfloat162 v = __floats2bfloat162_rn(acc[nh][half * 2], acc[nh][half * 2 + 1]);
+        *reinterpret_cast<__nv_bfloat162*>(out + p * CH + co) = v;
+      }
+    }
+  }
+  else
+  {
+    const float c2a = __shfl_down_sync(0xffffffffu, acc[0][0], 1);
+    const float c2b = __shfl_down_sync(0xffffffffu, acc[0][2], 1);
+    const float u0  = acc[0][0] + la.sk * acc[0][1] + la.sg * c2a; // pixel lane/4      (lane%4 == 0)
+    const float u1  = acc[0][2] + la.sk * acc[0][3] + la.sg * c2b; // pixel lane/4 + 8
+    const int src   = 4 * (lane & 7);
+    const float a   = __shfl_sync(0xffffffffu, u0, src);
+    const float b   = __shfl_sync(0xffffffffu, u1, src);
+    const int gx    = xb + lane;
+    if (lane < 16 && gx < W)
+    {
+      const float u       = lane < 8 ? a : b;
+      const long long p   = (long long)y * W + gx;
+      const double rv     = la.r ? la.r[img_pix + p] : (la.r32 ? (double)la.r32[img_pix + p] : 0.0);
+      out64[p]            = __fma_rn(out_scale * la.scale, rv, (double)((float)out_scale * u));
+    }
   }
 }
 
@@ -422,38 +322,7 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
       for (int nh = 0; nh < 2; ++nh)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[nh][q] += acd[nh][q];
-      const int pr0 = lane >> 2;
-      float c2h[2] = {0.f, 0.f};
-      if (MODE != 0)
-      {
-        c2h[0] = __shfl_down_sync(0xffffffffu, acc[0][0], 1);
-        c2h[1] = __shfl_down_sync(0xffffffffu, acc[0][2], 1);
-      }
-#pragma unroll
-      for (int half = 0; half < 2; ++half)
-      {
-        const int gx = x0 + mt * 16 + pr0 + half * 8;
-        if (gx >= W) continue;
-        const long long p = (long long)y * W + gx;
-        if (MODE == 0)
-        {
-#pragma unroll
-          for (int nh = 0; nh < 2; ++nh)
-          {
-            const int co = nh * 8 + (lane & 3) * 2;
-            __nv_bfloat162 v = __floats2bfloat162_rn(acc[nh][half * 2], acc[nh][half * 2 + 1]);
-            *reinterpret_cast<__nv_bfloat162*>(out + p * CH + co) = v;
-          }
-        }
-        else if ((lane & 3) == 0)
-        {
-          double v = (double)acc[0][half * 2] + (double)la.sk * (double)acc[0][half * 2 + 1] +
-                     (double)la.sg * (double)c2h[half];
-          if (la.r) v += la.r[img_pix + p] * la.scale;
-          else if (la.r32) v += (double)la.r32[img_pix + p] * la.scale;
-          out64[p] = v * out_scale;
-        }
-      }
+      conv_epilogue<MODE>(acc, lane, x0 + mt * 16, y, W, img_pix, out, out64, out_scale, la);
     }
     // C: stage the prefetched row (its slot held row y-2, last read before the previous barrier)
     if (LOAD != LD_PLAIN && more) store_row<LOAD>(raw, slot(y + 2), H, W, x0, y + 2, la, tid);
@@ -462,73 +331,90 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
   if (LOAD == LD_PLAIN) cp_async_wait0();
 }
 
-// 2x2 mean pooling (FP32 arithmetic, BF16 storage); W, H of the fine level
+// Level transfers, one thread per coarse (pool) or fine (upsampling) pixel and all 16 channels
+// as two 16-byte vectors; H, W are the fine level's (H counts the rows of all stacked images).
+// Index arithmetic in 32 bits (at most 2^31 pixels per level).
+struct V16 {
+  float v[CH];
+};
+__device__ __forceinline__ void ld16(const __nv_bfloat16* p, V16& o)
+{
+  const uint4 a = *reinterpret_cast<const uint4*>(p), b = *reinterpret_cast<const uint4*>(p + 8);
+  const __nv_bfloat162* x = reinterpret_cast<const __nv_bfloat162*>(&a);
+  const __nv_bfloat162* y = reinterpret_cast<const __nv_bfloat162*>(&b);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+  {
+    const float2 f = __bfloat1622float2(x[k]), g = __bfloat1622float2(y[k]);
+    o.v[2 * k]         = f.x;
+    o.v[2 * k + 1]     = f.y;
+    o.v[8 + 2 * k]     = g.x;
+    o.v[8 + 2 * k + 1] = g.y;
+  }
+}
+__device__ __forceinline__ void st16(__nv_bfloat16* p, const V16& o)
+{
+  uint32_t w[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+  {
+    __nv_bfloat162 t = __floats2bfloat162_rn(o.v[2 * k], o.v[2 * k + 1]);
+    w[k]             = *reinterpret_cast<uint32_t*>(&t);
+  }
+  *reinterpret_cast<uint4*>(p)     = make_uint4(w[0], w[1], w[2], w[3]);
+  *reinterpret_cast<uint4*>(p + 8) = make_uint4(w[4], w[5], w[6], w[7]);
+}
+
+// 2x2 mean pooling (FP32 arithmetic, BF16 storage)
 __global__ void pool_kernel(const __nv_bfloat16* __restrict__ in, int H, int W, __nv_bfloat16* __restrict__ out)
 {
-  const int Wc = W / 2, Hc = H / 2;
-  const long long n = (long long)Hc * Wc * CH;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+  const unsigned Wc = (unsigned)W / 2, n = (unsigned)(H / 2) * Wc;
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
   {
-    const int c = (int)(k % CH);
-    const long long p = k / CH;
-    const int x = (int)(p % Wc), y = (int)(p / Wc);
-    const long long f = ((long long)(2 * y) * W + 2 * x) * CH + c;
-    const float s = __bfloat162float(in[f]) + __bfloat162float(in[f + CH]) + __bfloat162float(in[f + (long long)W * CH]) +
-                    __bfloat162float(in[f + (long long)W * CH + CH]);
-    out[k] = __float2bfloat16_rn(0.25f * s);
+    const unsigned x = q % Wc, y = q / Wc;
+    const size_t f = ((size_t)(2 * y) * W + 2 * x) * CH;
+    V16 a, b, c, d;
+    ld16(in + f, a);
+    ld16(in + f + CH, b);
+    ld16(in + f + (size_t)W * CH, c);
+    ld16(in + f + (size_t)W * CH + CH, d);
+#pragma unroll
+    for (int k = 0; k < CH; ++k) a.v[k] = 0.25f * (a.v[k] + b.v[k] + c.v[k] + d.v[k]);
+    st16(out + (size_t)q * CH, a);
   }
 }
 
-// s = cscale * up(coarse) + fine (nearest-neighbour upsampling; cscale 0.25 is the adjoint
+// out = cscale * up(coarse) + fine (nearest-neighbour upsampling; cscale 0.25 is the adjoint
 // of the 2x2 mean)
 __global__ void upadd_kernel(const __nv_bfloat16* __restrict__ coarse, const __nv_bfloat16* __restrict__ fine, int H,
                              int W, float cscale, __nv_bfloat16* __restrict__ out)
 {
-  const long long n = (long long)H * W * CH;
-  const int Wc      = W / 2;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+  const unsigned n = (unsigned)H * (unsigned)W, Wc = (unsigned)W / 2;
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
   {
-    const int c = (int)(k % CH);
-    const long long p = k / CH;
-    const int x = (int)(p % W), y = (int)(p / W);
-    const float v = cscale * __bfloat162float(coarse[((long long)(y / 2) * Wc + x / 2) * CH + c]) +
-                    __bfloat162float(fine[k]);
-    out[k] = __float2bfloat16_rn(v);
+    const unsigned x = q % (unsigned)W, y = q / (unsigned)W;
+    V16 c, f;
+    ld16(coarse + ((size_t)(y / 2) * Wc + x / 2) * CH, c);
+    ld16(fine + (size_t)q * CH, f);
+#pragma unroll
+    for (int k = 0; k < CH; ++k) f.v[k] = cscale * c.v[k] + f.v[k];
+    st16(out + (size_t)q * CH, f);
   }
 }
 
-// backward helpers (FP32 gradients stored as BF16 activations-gradients for the conv kernel)
-// g_coarse = up^T(g) (2x2 sum); g_coarse += pool^T adds 0.25 g to each fine pixel
-__global__ void upT_kernel(const __nv_bfloat16* __restrict__ g, int H, int W, __nv_bfloat16* __restrict__ gc,
-                           int accumulate)
-{
-  const int Wc = W / 2, Hc = H / 2;
-  const long long n = (long long)Hc * Wc * CH;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-  {
-    const int c = (int)(k % CH);
-    const long long p = k / CH;
-    const int x = (int)(p % Wc), y = (int)(p / Wc);
-    const long long f = ((long long)(2 * y) * W + 2 * x) * CH + c;
-    float s = __bfloat162float(g[f]) + __bfloat162float(g[f + CH]) + __bfloat162float(g[f + (long long)W * CH]) +
-              __bfloat162float(g[f + (long long)W * CH + CH]);
-    if (accumulate) s += __bfloat162float(gc[k]);
-    gc[k] = __float2bfloat16_rn(s);
-  }
-}
-
-// g_fine += 0.25 * repeat(g_coarse)   (adjoint of the 2x2 mean pooling)
+// g_fine += 0.25 * up(g_coarse)   (adjoint of the 2x2 mean pooling)
 __global__ void poolT_add_kernel(const __nv_bfloat16* __restrict__ gcoarse, int H, int W, __nv_bfloat16* __restrict__ gf)
 {
-  const long long n = (long long)H * W * CH;
-  const int Wc      = W / 2;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+  const unsigned n = (unsigned)H * (unsigned)W, Wc = (unsigned)W / 2;
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
   {
-    const int c = (int)(k % CH);
-    const long long p = k / CH;
-    const int x = (int)(p % W), y = (int)(p / W);
-    const float v = __bfloat162float(gf[k]) + 0.25f * __bfloat162float(gcoarse[((long long)(y / 2) * Wc + x / 2) * CH + c]);
-    gf[k] = __float2bfloat16_rn(v);
+    const unsigned x = q % (unsigned)W, y = q / (unsigned)W;
+    V16 c, f;
+    ld16(gcoarse + ((size_t)(y / 2) * Wc + x / 2) * CH, c);
+    ld16(gf + (size_t)q * CH, f);
+#pragma unroll
+    for (int k = 0; k < CH; ++k) f.v[k] = f.v[k] + 0.25f * c.v[k];
+    st16(gf + (size_t)q * CH, f);
   }
 }
 
@@ -689,7 +575,7 @@ __global__ void adam_kernel(int n, float* __restrict__ w, float* __restrict__ m,
 // ---------------------------------------------------------------------------------------
 namespace net {
 
-// fragment layout of one layer's weights (BF16, see conv3x3_kernel); transpose = 1 builds
+// fragment layout of one layer's weights (BF16, see conv3x3_march_kernel); transpose = 1 builds
 // the input-gradient weights W'[ci][co][8 - t] = W[co][ci][t]
 __global__ void frag_kernel(const float* __restrict__ W, uint2* __restrict__ wf, int transpose)
 {
@@ -723,7 +609,7 @@ __global__ void input_kernel_t(long long npix, long long img_pix, const T* __res
       sg            = meta[META * img + 1];
       scale         = (double)meta[META * img + 3];
     }
-    const float v = (float)((double)r[p] * scale);
+    const float v = (float)r[p] * (float)scale; // as the first convolution's tile loader
     __align__(16) __nv_bfloat16 o[CH];
     o[0] = __float2bfloat16_rn(v);
     o[1] = __float2bfloat16_rn(v * sk);
@@ -993,7 +879,7 @@ static void conv(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, int layer
 
 static void pool(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, __nv_bfloat16* out)
 {
-  const long long cnt = (long long)n * n * nimg / 4 * CH;
+  const long long cnt = (long long)n * n * nimg / 4;
   net::pool_kernel<<<grid_for(cnt), 256, 0, nt->ctx->stream>>>(in, n * nimg, n, out);
 }
 
@@ -1001,7 +887,7 @@ static void pool(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, __nv_bflo
 static void upadd(STS_Net nt, const __nv_bfloat16* coarse, const __nv_bfloat16* fine, int n, int nimg,
                   __nv_bfloat16* out)
 {
-  const long long cnt = (long long)n * n * nimg * CH;
+  const long long cnt = (long long)n * n * nimg;
   net::upadd_kernel<<<grid_for(cnt), 256, 0, nt->ctx->stream>>>(coarse, fine, n * nimg, n, 0.25f, out);
 }
 
@@ -1082,7 +968,7 @@ static void wgrad(STS_Net nt, const __nv_bfloat16* x, const __nv_bfloat16* g, in
 // out_fine += 0.25 up(coarse) (adjoint of the 2x2 mean), fine at n x n
 static void poolT_add(STS_Net nt, const __nv_bfloat16* coarse, int n, int nimg, __nv_bfloat16* fine)
 {
-  const long long cnt = (long long)n * n * nimg * CH;
+  const long long cnt = (long long)n * n * nimg;
   net::poolT_add_kernel<<<grid_for(cnt), 256, 0, nt->ctx->stream>>>(coarse, n * nimg, n, fine);
 }
 
@@ -1387,7 +1273,7 @@ __global__ void __launch_bounds__(256) fcg_beta_kernel(long long n, const double
 // and forms p = z + beta p_prev once per point (rows j-1, j, j+1 in registers, west/east
 // neighbours by warp shuffles; the two warp-edge lanes form their outside neighbours from
 // z and p_prev directly), so p is formed once per point.
-constexpr int FCG_ROWS = 64;
+constexpr int FCG_ROWS = 16;
 __global__ void __launch_bounds__(256) fcg_pq_march_kernel(ProbDev P, const double* __restrict__ z,
                                                            const double* __restrict__ pp,
                                                            const double* __restrict__ r, double* __restrict__ p,
@@ -1411,10 +1297,24 @@ __global__ void __launch_bounds__(256) fcg_pq_march_kernel(ProbDev P, const doub
     const long long k = jj * nx + ii;
     return __fma_rn(beta, pp[k], z[k]);
   };
+  // raw z, p_prev of row jj at this column (0 outside the grid), loaded one row ahead
+  auto raw = [&](long long jj, double& zz, double& qq) {
+    zz = qq = 0.0;
+    if (jj >= 0 && jj < ny)
+    {
+      const long long k = jj * nx + ic;
+      zz = z[k];
+      qq = pp[k];
+    }
+  };
+  double zn, qn, zn2, qn2;
   double pm = pval(ic, j0 - 1), pc = pval(ic, j0);
+  raw(j0 + 1, zn, qn);
   for (long long j = j0; j < j1; ++j)
   {
-    const double pn = pval(ic, j + 1);
+    raw(j + 2, zn2, qn2); // prefetch
+    const double rk = col ? r[j * nx + ic] : 0.0;
+    const double pn = (j + 1 < ny) ? __fma_rn(beta, qn, zn) : 0.0;
     double pw = __shfl_up_sync(0xffffffffu, pc, 1);
     double pe = __shfl_down_sync(0xffffffffu, pc, 1);
     if (lane == 0) pw = pval(ic - 1, j);
@@ -1431,11 +1331,13 @@ __global__ void __launch_bounds__(256) fcg_pq_march_kernel(ProbDev P, const doub
       const double qk = __fma_rn(-gamma, acc, pc);
       p[k]            = pc;
       q[k]            = qk;
-      xsum::add(a[0], pc * r[k], fl[0]);
+      xsum::add(a[0], pc * rk, fl[0]);
       xsum::add(a[1], pc * qk, fl[1]);
     }
     pm = pc;
     pc = pn;
+    zn = zn2;
+    qn = qn2;
   }
   krylov_block_finish<256, 2>(a, fl, s, [&](const double* v) {
     s->alpha   = v[0] / v[1];
