@@ -179,25 +179,27 @@ __device__ __forceinline__ void store_row(const RowRaw& raw, unsigned char* slot
 template <int MODE>
 __device__ __forceinline__ void conv_epilogue(const float (&acc)[2][4], int lane, int xb, int y, int W,
                                               long long img_pix, __nv_bfloat16* out, double* out64, double out_scale,
-                                              const LoadArgs& la)
+                                              const LoadArgs& la, unsigned char* stage)
 {
   const int pr0 = lane >> 2;
   if (MODE == 0)
   {
+    // through the warp's 512-byte staging buffer, so each lane stores one full 16-byte half
+    // pixel and the warp writes its 16 pixels x 32 bytes with one coalesced instruction
 #pragma unroll
     for (int half = 0; half < 2; ++half)
-    {
-      const int gx = xb + pr0 + half * 8;
-      if (gx >= W) continue;
-      const long long p = (long long)y * W + gx;
 #pragma unroll
       for (int nh = 0; nh < 2; ++nh)
       {
         const int co = nh * 8 + (lane & 3) * 2;
         __nv_bfloat162 v = __floats2bfloat162_rn(acc[nh][half * 2], acc[nh][half * 2 + 1]);
-        *reinterpret_cast<__nv_bfloat162*>(out + p * CH + co) = v;
+        *reinterpret_cast<__nv_bfloat162*>(stage + (pr0 + half * 8) * 32 + co * 2) = v;
       }
-    }
+    __syncwarp();
+    const int px = lane >> 1, gx = xb + px;
+    const uint4 v = *reinterpret_cast<const uint4*>(stage + lane * 16);
+    if (gx < W) *reinterpret_cast<uint4*>(out + ((long long)y * W + gx) * CH + (lane & 1) * 8) = v;
+    __syncwarp();
   }
   else
   {
@@ -227,6 +229,7 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
                                                              const float* __restrict__ meta, LoadArgs la, int rows)
 {
   __shared__ __align__(128) unsigned char ring[MRING][ROWB];
+  __shared__ __align__(16) unsigned char stage[NTHR / 32][16 * 32]; // per-warp output staging
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int x0 = blockIdx.x * TC;
   const int ys = blockIdx.y * rows, ye = min(H, ys + rows);
@@ -322,7 +325,7 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
       for (int nh = 0; nh < 2; ++nh)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[nh][q] += acd[nh][q];
-      conv_epilogue<MODE>(acc, lane, x0 + mt * 16, y, W, img_pix, out, out64, out_scale, la);
+      conv_epilogue<MODE>(acc, lane, x0 + mt * 16, y, W, img_pix, out, out64, out_scale, la, stage[warp]);
     }
     // C: stage the prefetched row (its slot held row y-2, last read before the previous barrier)
     if (LOAD != LD_PLAIN && more) store_row<LOAD>(raw, slot(y + 2), H, W, x0, y + 2, la, tid);
