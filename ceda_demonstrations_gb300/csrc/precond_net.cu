@@ -76,9 +76,10 @@ struct LoadArgs {
 // ---------------------------------------------------------------------------------------
 // Row-marching convolution: a CTA owns a 64-column strip of one image and marches down a
 // segment of rows, keeping a ring of 4 input rows (66 pixels with the halo, swizzled) in
-// shared memory. Row y+2 is fetched while row y is computed (cp.async for plain BF16 input;
-// register prefetch and conversion for the FP64-residual and skip-sum loaders), so the halo
-// overhead is 2 rows per segment instead of 2 per 4-row tile and the loads overlap the MMAs.
+// shared memory. Row y+2 is fetched while row y is computed (cp.async straight into the ring
+// for plain BF16 input; for the FP64-residual and skip-sum loaders cp.async of the raw bytes
+// three rows ahead into a raw ring, converted one iteration later), so the halo overhead is
+// 2 rows per segment and the loads overlap the MMAs.
 // Implicit GEMM per row: each warp computes one 16-pixel x 16-channel tile over the nine taps
 // (mma.sync m16n8k16 BF16 -> FP32, A by ldmatrix.x4 from the swizzled ring, weights in
 // registers as B fragments).
@@ -95,76 +96,77 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// raw data of the (up to two) 16-byte chunks a thread stages for one row
-struct RowRaw {
-  uint4 f[2], c[2];
-  double r[2];
-};
+// Raw staging for the converting loaders (LD_R64, LD_UPADD): the source bytes of a row are
+// copied by cp.async into a 4-row raw ring two rows ahead of use; each thread later converts
+// exactly the chunks it copied (its own cp.async data needs no barrier), writing the BF16 row
+// into the convolution ring. Per 16-byte chunk c of a staged row: 32 raw bytes, the fine chunk
+// and the coarse chunk above it (LD_UPADD), or the residual value (LD_R64, chunks of half 0).
+constexpr int RAWB = (TC + 2) * 2 * 32;
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src, bool valid)
+{
+  const int n = valid ? 8 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(n) : "memory");
+}
 
 template <int LOAD>
-__device__ __forceinline__ void fetch_row(RowRaw& raw, const __nv_bfloat16* in, int H, int W, int x0, int row,
+__device__ __forceinline__ void issue_raw(unsigned char* rs, const __nv_bfloat16* in, int H, int W, int x0, int row,
                                           long long img_pix, const LoadArgs& la, int tid)
 {
-#pragma unroll
-  for (int q = 0; q < 2; ++q)
+  for (int c = tid; c < (TC + 2) * 2; c += NTHR)
   {
-    const int c = tid + q * NTHR;
-    raw.f[q] = raw.c[q] = make_uint4(0, 0, 0, 0);
-    raw.r[q] = 0.0;
-    if (c >= (TC + 2) * 2) continue;
     const int h = c & 1, tx = c >> 1, gx = x0 + tx - 1;
-    if (row < 0 || row >= H || gx < 0 || gx >= W) continue;
+    const bool valid = row >= 0 && row < H && gx >= 0 && gx < W;
+    unsigned char* d = rs + c * 32;
     if (LOAD == LD_R64)
     {
-      if (h == 0) raw.r[q] = la.r[img_pix + (long long)row * W + gx];
+      if (h == 0) cp_async8(smem_u32(d), valid ? (const void*)(la.r + img_pix + (long long)row * W + gx) : (const void*)la.r,
+                            valid);
     }
     else
     {
-      raw.f[q] = *reinterpret_cast<const uint4*>(in + ((long long)row * W + gx) * CH + h * 8);
-      raw.c[q] = *reinterpret_cast<const uint4*>(la.coarse + (img_pix / 4 + (long long)(row / 2) * (W / 2) + gx / 2) * CH +
-                                                 h * 8);
+      cp_async16(smem_u32(d), valid ? (const void*)(in + ((long long)row * W + gx) * CH + h * 8) : (const void*)in, valid);
+      cp_async16(smem_u32(d + 16),
+                 valid ? (const void*)(la.coarse + (img_pix / 4 + (long long)(row / 2) * (W / 2) + gx / 2) * CH + h * 8)
+                       : (const void*)la.coarse,
+                 valid);
     }
   }
 }
 
 template <int LOAD>
-__device__ __forceinline__ void store_row(const RowRaw& raw, unsigned char* slot, int H, int W, int x0, int row,
-                                          const LoadArgs& la, int tid)
+__device__ __forceinline__ void convert_raw(const unsigned char* rs, unsigned char* slot, const LoadArgs& la, int tid)
 {
-#pragma unroll
-  for (int q = 0; q < 2; ++q)
+  for (int c = tid; c < (TC + 2) * 2; c += NTHR)
   {
-    const int c = tid + q * NTHR;
-    if (c >= (TC + 2) * 2) continue;
-    const int h = c & 1, tx = c >> 1, gx = x0 + tx - 1;
+    const int h = c & 1, tx = c >> 1;
+    const unsigned char* d = rs + c * 32;
     uint4 v = make_uint4(0, 0, 0, 0);
-    if (row >= 0 && row < H && gx >= 0 && gx < W)
+    if (LOAD == LD_R64)
     {
-      if (LOAD == LD_R64)
+      if (h == 0)
       {
-        if (h == 0)
-        {
-          const float xv = (float)raw.r[q] * (float)la.scale; // one FP64 instruction (the conversion)
-          __nv_bfloat162 c01 = __halves2bfloat162(__float2bfloat16_rn(xv), __float2bfloat16_rn(xv * la.sk));
-          __nv_bfloat162 c23 = __halves2bfloat162(__float2bfloat16_rn(xv * la.sg), __float2bfloat16_rn(0.f));
-          v.x = *reinterpret_cast<uint32_t*>(&c01);
-          v.y = *reinterpret_cast<uint32_t*>(&c23);
-        }
+        const double rv = *reinterpret_cast<const double*>(d);
+        const float xv  = (float)rv * (float)la.scale;
+        __nv_bfloat162 c01 = __halves2bfloat162(__float2bfloat16_rn(xv), __float2bfloat16_rn(xv * la.sk));
+        __nv_bfloat162 c23 = __halves2bfloat162(__float2bfloat16_rn(xv * la.sg), __float2bfloat16_rn(0.f));
+        v.x = *reinterpret_cast<uint32_t*>(&c01);
+        v.y = *reinterpret_cast<uint32_t*>(&c23);
       }
-      else
-      {
-        const __nv_bfloat162* fb = reinterpret_cast<const __nv_bfloat162*>(&raw.f[q]);
-        const __nv_bfloat162* cb = reinterpret_cast<const __nv_bfloat162*>(&raw.c[q]);
-        uint32_t o[4];
+    }
+    else
+    {
+      const uint4 f = *reinterpret_cast<const uint4*>(d), cc = *reinterpret_cast<const uint4*>(d + 16);
+      const __nv_bfloat162* fb = reinterpret_cast<const __nv_bfloat162*>(&f);
+      const __nv_bfloat162* cb = reinterpret_cast<const __nv_bfloat162*>(&cc);
+      uint32_t o[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-        {
-          const float2 a = __bfloat1622float2(fb[k]), b = __bfloat1622float2(cb[k]);
-          __nv_bfloat162 t = __floats2bfloat162_rn(la.cscale * b.x + a.x, la.cscale * b.y + a.y);
-          o[k] = *reinterpret_cast<uint32_t*>(&t);
-        }
-        v = make_uint4(o[0], o[1], o[2], o[3]);
+      for (int k = 0; k < 4; ++k)
+      {
+        const float2 a = __bfloat1622float2(fb[k]), b = __bfloat1622float2(cb[k]);
+        __nv_bfloat162 t = __floats2bfloat162_rn(la.cscale * b.x + a.x, la.cscale * b.y + a.y);
+        o[k] = *reinterpret_cast<uint32_t*>(&t);
       }
+      v = make_uint4(o[0], o[1], o[2], o[3]);
     }
     *reinterpret_cast<uint4*>(slot + swz(tx, h)) = v;
   }
@@ -230,6 +232,7 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
 {
   __shared__ __align__(128) unsigned char ring[MRING][ROWB];
   __shared__ __align__(16) unsigned char stage[NTHR / 32][16 * 32]; // per-warp output staging
+  __shared__ __align__(16) unsigned char rawring[LOAD == LD_PLAIN ? 1 : MRING][LOAD == LD_PLAIN ? 16 : RAWB];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int x0 = blockIdx.x * TC;
   const int ys = blockIdx.y * rows, ye = min(H, ys + rows);
@@ -266,8 +269,12 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
   for (int t = 0; t < 9; ++t)
 #pragma unroll
     for (int nh = 0; nh < 2; ++nh) wr[t][nh] = (MODE == 0 || nh == 0) ? wf[(t * 2 + nh) * 32 + lane] : make_uint2(0, 0);
-  // prologue: rows ys-1, ys, ys+1
-  RowRaw raw;
+  auto rawslot = [&](int r) { return &rawring[(r - ys + 1) & (MRING - 1)][0]; };
+  auto issue_conv = [&](int r) { // raw copy of row r (rows past ye are not needed: empty group)
+    if (r <= ye) issue_raw<LOAD>(rawslot(r), in, H, W, x0, r, img_pix, la, tid);
+    cp_async_commit();
+  };
+  // prologue: rows ys-1, ys, ys+1 staged (and, for the converting loaders, row ys+2 in flight)
   if (LOAD == LD_PLAIN)
   {
     issue_plain(ys - 1);
@@ -275,14 +282,18 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
     issue_plain(ys + 1);
   }
   else
-    for (int r = ys - 1; r <= ys + 1; ++r)
-    {
-      fetch_row<LOAD>(raw, in, H, W, x0, r, img_pix, la, tid);
-      store_row<LOAD>(raw, slot(r), H, W, x0, r, la, tid);
-    }
+  {
+    issue_conv(ys - 1);
+    issue_conv(ys);
+    issue_conv(ys + 1);
+    issue_conv(ys + 2);
+    cp_async_wait1(); // all but the row ys+2 group
+    for (int r = ys - 1; r <= ys + 1; ++r) convert_raw<LOAD>(rawslot(r), slot(r), la, tid);
+  }
   for (int y = ys; y < ye; ++y)
   {
-    // A: fetch row y+2 (needed by output row y+1)
+    // A: fetch ahead: plain rows land directly in the ring (row y+2); the converting loaders
+    // copy raw row y+3 and convert raw row y+2 below
     const bool more = y + 2 <= ye;
     if (LOAD == LD_PLAIN)
     {
@@ -290,8 +301,11 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
       else cp_async_commit(); // empty group keeps the wait count uniform
       cp_async_wait1();       // rows up to y+1 have landed
     }
-    else if (more)
-      fetch_row<LOAD>(raw, in, H, W, x0, y + 2, img_pix, la, tid);
+    else
+    {
+      issue_conv(y + 3);
+      cp_async_wait1(); // raw row y+2 (this thread's copies) has landed
+    }
     __syncthreads();
     // B: output row y, one 16-pixel m-tile per warp; taps in two independent accumulator
     // chains (rows y-1, y | row y+1) that are added at the end, to overlap MMA latencies
@@ -327,11 +341,13 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
         for (int q = 0; q < 4; ++q) acc[nh][q] += acd[nh][q];
       conv_epilogue<MODE>(acc, lane, x0 + mt * 16, y, W, img_pix, out, out64, out_scale, la, stage[warp]);
     }
-    // C: stage the prefetched row (its slot held row y-2, last read before the previous barrier)
-    if (LOAD != LD_PLAIN && more) store_row<LOAD>(raw, slot(y + 2), H, W, x0, y + 2, la, tid);
+    // C: convert raw row y+2 into its ring slot (held row y-2, last read before the previous
+    // barrier); its raw slot is reused by the copy of row y+6, issued after the barriers of
+    // iterations y, y+1 and y+2
+    if (LOAD != LD_PLAIN && more) convert_raw<LOAD>(rawslot(y + 2), slot(y + 2), la, tid);
     __syncthreads(); // D: row y's slots free for reuse, row y+2 visible
   }
-  if (LOAD == LD_PLAIN) cp_async_wait0();
+  cp_async_wait0();
 }
 
 // Level transfers, one thread per coarse (pool) or fine (upsampling) pixel and all 16 channels
