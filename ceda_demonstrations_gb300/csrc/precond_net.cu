@@ -1288,27 +1288,31 @@ __global__ void __launch_bounds__(256) fcg_beta_kernel(long long n, const double
   });
 }
 
-// KP: p = z + beta p_prev, q = (I - gamma A) p, p.r and p.q -> alpha. A thread owns one column of a segment of FCG_ROWS rows
-// and forms p = z + beta p_prev once per point (rows j-1, j, j+1 in registers, west/east
-// neighbours by warp shuffles; the two warp-edge lanes form their outside neighbours from
-// z and p_prev directly), so p is formed once per point.
+// KP: p = z + beta p_prev, q = (I - gamma A) p, p.r and p.q -> alpha. A block owns 256
+// columns of a segment of FCG_ROWS rows and marches down it: each row of p (with one halo
+// column on each side) is formed once into a 3-row shared ring, and q is taken from the ring
+// as q = (1 - gamma cc) p_C - gamma cx (p_W + p_E) - gamma cy (p_S + p_N). Eight FP64
+// instructions per point (p, stencil, the two dot products): GB300 issues FP64 at 1/64 of
+// the FP32 rate, so these kernels are bounded by the FP64 pipe rather than by HBM.
 constexpr int FCG_ROWS = 16;
 __global__ void __launch_bounds__(256) fcg_pq_march_kernel(ProbDev P, const double* __restrict__ z,
                                                            const double* __restrict__ pp,
                                                            const double* __restrict__ r, double* __restrict__ p,
                                                            double* __restrict__ q, FcgScal* s, FcgOut* out)
 {
+  __shared__ double ring[3][256 + 2];
   if (s->state != 0) return;
   const double gamma = s->gamma, beta = s->beta;
+  const double c0 = 1.0 - gamma * P.cc, c1 = -gamma * P.cx, c2 = -gamma * P.cy;
   xsum::Limbs a[2];
   unsigned fl[2] = {0, 0};
   xsum::zero(a[0]);
   xsum::zero(a[1]);
   const long long nx = P.nx, ny = P.ny;
-  const int lane     = threadIdx.x & 31;
-  const long long i  = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid      = threadIdx.x;
+  const long long x0 = (long long)blockIdx.x * 256;
+  const long long i  = x0 + tid;
   const bool col     = i < nx;
-  const long long ic = col ? i : nx - 1; // inactive lanes shadow the last column (no stores)
   const long long j0 = (long long)blockIdx.y * FCG_ROWS;
   const long long j1 = j0 + FCG_ROWS < ny ? j0 + FCG_ROWS : ny;
   auto pval = [&](long long ii, long long jj) -> double {
@@ -1316,47 +1320,35 @@ __global__ void __launch_bounds__(256) fcg_pq_march_kernel(ProbDev P, const doub
     const long long k = jj * nx + ii;
     return __fma_rn(beta, pp[k], z[k]);
   };
-  // raw z, p_prev of row jj at this column (0 outside the grid), loaded one row ahead
-  auto raw = [&](long long jj, double& zz, double& qq) {
-    zz = qq = 0.0;
-    if (jj >= 0 && jj < ny)
-    {
-      const long long k = jj * nx + ic;
-      zz = z[k];
-      qq = pp[k];
-    }
+  // row jj of p into ring slot (jj - j0 + 1) % 3: own column, threads 0 / 255 also the halo
+  auto stage_row = [&](long long jj) {
+    double* rw = ring[(int)((jj - j0 + 1) % 3)];
+    rw[tid + 1] = pval(i, jj);
+    if (tid == 0) rw[0] = pval(x0 - 1, jj);
+    if (tid == 255) rw[257] = pval(x0 + 256, jj);
   };
-  double zn, qn, zn2, qn2;
-  double pm = pval(ic, j0 - 1), pc = pval(ic, j0);
-  raw(j0 + 1, zn, qn);
+  stage_row(j0 - 1);
+  stage_row(j0);
   for (long long j = j0; j < j1; ++j)
   {
-    raw(j + 2, zn2, qn2); // prefetch
-    const double rk = col ? r[j * nx + ic] : 0.0;
-    const double pn = (j + 1 < ny) ? __fma_rn(beta, qn, zn) : 0.0;
-    double pw = __shfl_up_sync(0xffffffffu, pc, 1);
-    double pe = __shfl_down_sync(0xffffffffu, pc, 1);
-    if (lane == 0) pw = pval(ic - 1, j);
-    if (lane == 31) pe = pval(ic + 1, j);
-    if (ic == 0) pw = 0.0;
-    if (ic == nx - 1) pe = 0.0;
+    stage_row(j + 1);
+    const double rk = col ? r[j * nx + i] : 0.0;
+    __syncthreads();
     if (col)
     {
-      const long long k = j * nx + ic;
-      const double sx = pw + pe, sy = pm + pn;
-      double acc = P.cc * pc;
-      acc        = __fma_rn(P.cx, sx, acc);
-      acc        = __fma_rn(P.cy, sy, acc);
-      const double qk = __fma_rn(-gamma, acc, pc);
-      p[k]            = pc;
-      q[k]            = qk;
+      const double* rm = ring[(int)((j - j0) % 3)];
+      const double* rc = ring[(int)((j - j0 + 1) % 3)];
+      const double* rn = ring[(int)((j - j0 + 2) % 3)];
+      const double pc = rc[tid + 1];
+      const double sx = rc[tid] + rc[tid + 2], sy = rm[tid + 1] + rn[tid + 1];
+      const double qk = __fma_rn(c1, sx, __fma_rn(c2, sy, c0 * pc));
+      const long long k = j * nx + i;
+      p[k]              = pc;
+      q[k]              = qk;
       xsum::add(a[0], pc * rk, fl[0]);
       xsum::add(a[1], pc * qk, fl[1]);
     }
-    pm = pc;
-    pc = pn;
-    zn = zn2;
-    qn = qn2;
+    __syncthreads(); // row j-1's slot is overwritten by row j+2 in the next iteration
   }
   krylov_block_finish<256, 2>(a, fl, s, [&](const double* v) {
     s->alpha   = v[0] / v[1];
