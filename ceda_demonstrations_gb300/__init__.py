@@ -23,7 +23,7 @@ from . import build as _build
 
 __all__ = ["lib", "Context", "NVector", "Problem", "LSRKStep", "PCGSolver", "implicit_solve_pcg",
            "sdirk2_evolve", "RKC", "RKL", "PID", "PI", "I", "MANUFACTURED", "UNFORCED", "PERIODIC",
-           "Net", "fcg_solve", "harvest_pcg_pairs", "net_features", "smooth_field", "STSError"]
+           "Net", "fcg_solve", "implicit_solve_learned", "harvest_pcg_pairs", "net_features", "smooth_field", "STSError"]
 
 RKC, RKL = 0, 1
 PID, PI, I = 0, 1, 2
@@ -181,6 +181,8 @@ SIGNATURES = [
     ("STS_HarvestPCGPairs", C.c_int, [_vp, C.c_double, _NV, C.c_int, C.c_int, C.c_int, C.c_int,
                                       _vp, _vp, _vp, C.c_ulonglong, _ip, _ip]),
     ("STS_FCGSolve", C.c_int, [_vp, C.c_double, _vp, _NV, _NV, C.c_double, C.c_int, _ip, _dp]),
+    ("STS_ImplicitSolveLearned", C.c_int, [_vp, C.c_double, _vp, _NV, _NV, C.c_double, C.c_int,
+                                           C.c_double, _ip, _dp, _ip]),
 ]
 
 _lib = None
@@ -848,3 +850,14 @@ def fcg_solve(problem, gamma, net, b, x, tol=1e-8, maxit=10000):
     if rc < 0:
         _err("STS_FCGSolve")
     return it.value, rel.value, rc
+
+
+def implicit_solve_learned(problem, gamma, net, b, x, tol=1e-8, maxit=20000, kappa_min=0.0):
+    """Shifted solve choosing FCG + network (kappa = 1 + 4 gamma (cx + cy) >= kappa_min) or
+    Jacobi-PCG; returns (iterations, relative residual, status, used_net)."""
+    it, rel, used = C.c_int(), C.c_double(), C.c_int()
+    rc = lib().STS_ImplicitSolveLearned(problem.h, gamma, net.h if net else None, b.h, x.h, tol,
+                                        maxit, kappa_min, C.byref(it), C.byref(rel), C.byref(used))
+    if rc < 0:
+        _err("STS_ImplicitSolveLearned")
+    return it.value, rel.value, rc, bool(used.value)

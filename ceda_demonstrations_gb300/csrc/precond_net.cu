@@ -99,9 +99,11 @@ __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_g
 // Raw staging for the converting loaders (LD_R64, LD_UPADD): the source bytes of a row are
 // copied by cp.async into a 4-row raw ring two rows ahead of use; each thread later converts
 // exactly the chunks it copied (its own cp.async data needs no barrier), writing the BF16 row
-// into the convolution ring. Per 16-byte chunk c of a staged row: 32 raw bytes, the fine chunk
-// and the coarse chunk above it (LD_UPADD), or the residual value (LD_R64, chunks of half 0).
-constexpr int RAWB = (TC + 2) * 2 * 32;
+// into the convolution ring. Raw row layout (contiguous, so the 16- and 8-byte accesses of a
+// warp are bank-conflict free): LD_UPADD the 132 fine chunks, then the 132 coarse chunks
+// above them; LD_R64 the 66 residual values.
+constexpr int RAWC = (TC + 2) * 2;  // chunks per staged row
+constexpr int RAWB = RAWC * 2 * 16;
 __device__ __forceinline__ void cp_async8(uint32_t dst, const void* src, bool valid)
 {
   const int n = valid ? 8 : 0;
@@ -116,16 +118,17 @@ __device__ __forceinline__ void issue_raw(unsigned char* rs, const __nv_bfloat16
   {
     const int h = c & 1, tx = c >> 1, gx = x0 + tx - 1;
     const bool valid = row >= 0 && row < H && gx >= 0 && gx < W;
-    unsigned char* d = rs + c * 32;
     if (LOAD == LD_R64)
     {
-      if (h == 0) cp_async8(smem_u32(d), valid ? (const void*)(la.r + img_pix + (long long)row * W + gx) : (const void*)la.r,
-                            valid);
+      if (h == 0)
+        cp_async8(smem_u32(rs + tx * 8), valid ? (const void*)(la.r + img_pix + (long long)row * W + gx) : (const void*)la.r,
+                  valid);
     }
     else
     {
-      cp_async16(smem_u32(d), valid ? (const void*)(in + ((long long)row * W + gx) * CH + h * 8) : (const void*)in, valid);
-      cp_async16(smem_u32(d + 16),
+      cp_async16(smem_u32(rs + c * 16), valid ? (const void*)(in + ((long long)row * W + gx) * CH + h * 8) : (const void*)in,
+                 valid);
+      cp_async16(smem_u32(rs + (RAWC + c) * 16),
                  valid ? (const void*)(la.coarse + (img_pix / 4 + (long long)(row / 2) * (W / 2) + gx / 2) * CH + h * 8)
                        : (const void*)la.coarse,
                  valid);
@@ -139,13 +142,12 @@ __device__ __forceinline__ void convert_raw(const unsigned char* rs, unsigned ch
   for (int c = tid; c < (TC + 2) * 2; c += NTHR)
   {
     const int h = c & 1, tx = c >> 1;
-    const unsigned char* d = rs + c * 32;
     uint4 v = make_uint4(0, 0, 0, 0);
     if (LOAD == LD_R64)
     {
       if (h == 0)
       {
-        const double rv = *reinterpret_cast<const double*>(d);
+        const double rv = *reinterpret_cast<const double*>(rs + tx * 8);
         const float xv  = (float)rv * (float)la.scale;
         __nv_bfloat162 c01 = __halves2bfloat162(__float2bfloat16_rn(xv), __float2bfloat16_rn(xv * la.sk));
         __nv_bfloat162 c23 = __halves2bfloat162(__float2bfloat16_rn(xv * la.sg), __float2bfloat16_rn(0.f));
@@ -155,7 +157,8 @@ __device__ __forceinline__ void convert_raw(const unsigned char* rs, unsigned ch
     }
     else
     {
-      const uint4 f = *reinterpret_cast<const uint4*>(d), cc = *reinterpret_cast<const uint4*>(d + 16);
+      const uint4 f  = *reinterpret_cast<const uint4*>(rs + c * 16);
+      const uint4 cc = *reinterpret_cast<const uint4*>(rs + (RAWC + c) * 16);
       const __nv_bfloat162* fb = reinterpret_cast<const __nv_bfloat162*>(&f);
       const __nv_bfloat162* cb = reinterpret_cast<const __nv_bfloat162*>(&cc);
       uint32_t o[4];
@@ -173,6 +176,7 @@ __device__ __forceinline__ void convert_raw(const unsigned char* rs, unsigned ch
 }
 
 // Epilogue of one 16-pixel m-tile of output row y starting at column xb.
+constexpr int STG = 48; // staging bytes per pixel (32 + 16 of padding: conflict-free fragment stores)
 // mode 0: BF16 NHWC, 16 channels. Accumulator layout: c0,c1 -> pixel lane/4, channels
 // (lane%4)*2..+1; c2,c3 -> pixel lane/4 + 8.
 // mode 2: u = c0 + sk c1 + sg c2 (FP32; channel 2 sits in the next lane), redistributed so
@@ -195,11 +199,11 @@ __device__ __forceinline__ void conv_epilogue(const float (&acc)[2][4], int lane
       {
         const int co = nh * 8 + (lane & 3) * 2;
         __nv_bfloat162 v = __floats2bfloat162_rn(acc[nh][half * 2], acc[nh][half * 2 + 1]);
-        *reinterpret_cast<__nv_bfloat162*>(stage + (pr0 + half * 8) * 32 + co * 2) = v;
+        *reinterpret_cast<__nv_bfloat162*>(stage + (pr0 + half * 8) * STG + co * 2) = v;
       }
     __syncwarp();
     const int px = lane >> 1, gx = xb + px;
-    const uint4 v = *reinterpret_cast<const uint4*>(stage + lane * 16);
+    const uint4 v = *reinterpret_cast<const uint4*>(stage + px * STG + (lane & 1) * 16);
     if (gx < W) *reinterpret_cast<uint4*>(out + ((long long)y * W + gx) * CH + (lane & 1) * 8) = v;
     __syncwarp();
   }
@@ -223,7 +227,9 @@ __device__ __forceinline__ void conv_epilogue(const float (&acc)[2][4], int lane
   }
 }
 
-template <int MODE, int LOAD = LD_PLAIN>
+// NARROW: the input has channels 0..7 only (the network input [r, r sk, r sg], or its
+// gradient): the MMAs run with K = 8 (m16n8k8, A by ldmatrix.x2), half the tensor work.
+template <int MODE, int LOAD = LD_PLAIN, bool NARROW = false>
 __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16* __restrict__ in, int H, int W,
                                                              const uint2* __restrict__ wf,
                                                              __nv_bfloat16* __restrict__ out,
@@ -231,7 +237,7 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
                                                              const float* __restrict__ meta, LoadArgs la, int rows)
 {
   __shared__ __align__(128) unsigned char ring[MRING][ROWB];
-  __shared__ __align__(16) unsigned char stage[NTHR / 32][16 * 32]; // per-warp output staging
+  __shared__ __align__(16) unsigned char stage[NTHR / 32][16 * STG]; // per-warp output staging
   __shared__ __align__(16) unsigned char rawring[LOAD == LD_PLAIN ? 1 : MRING][LOAD == LD_PLAIN ? 16 : RAWB];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int x0 = blockIdx.x * TC;
@@ -320,19 +326,39 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
         const int pi = (lane & 7) + ((lane >> 3) & 1) * 8;
         const int hh = lane >> 4;
         const int px = mt * 16 + pi + dx;
-        const unsigned char* rp = slot(y - 1 + dy) + swz(px, hh);
-        uint32_t a0, a1, a2, a3;
-        asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-                     : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3)
-                     : "r"(smem_u32(rp)));
         float(&A)[2][4] = (t < 6) ? acc : acd;
-#pragma unroll
-        for (int nh = 0; nh < (MODE == 0 ? 2 : 1); ++nh)
+        if constexpr (NARROW)
         {
-          asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                       "{%0,%1,%2,%3};"
-                       : "+f"(A[nh][0]), "+f"(A[nh][1]), "+f"(A[nh][2]), "+f"(A[nh][3])
-                       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(wr[t][nh].x), "r"(wr[t][nh].y));
+          // lanes 0-7: pixels 0-7, lanes 8-15: pixels 8-15, channels 0-7 (half 0)
+          const unsigned char* rp = slot(y - 1 + dy) + swz(mt * 16 + (lane & 15) + dx, 0);
+          uint32_t a0, a1;
+          asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];"
+                       : "=r"(a0), "=r"(a1)
+                       : "r"(smem_u32(rp)));
+#pragma unroll
+          for (int nh = 0; nh < (MODE == 0 ? 2 : 1); ++nh)
+          {
+            asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, "
+                         "{%0,%1,%2,%3};"
+                         : "+f"(A[nh][0]), "+f"(A[nh][1]), "+f"(A[nh][2]), "+f"(A[nh][3])
+                         : "r"(a0), "r"(a1), "r"(wr[t][nh].x));
+          }
+        }
+        else
+        {
+          const unsigned char* rp = slot(y - 1 + dy) + swz(px, hh);
+          uint32_t a0, a1, a2, a3;
+          asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                       : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3)
+                       : "r"(smem_u32(rp)));
+#pragma unroll
+          for (int nh = 0; nh < (MODE == 0 ? 2 : 1); ++nh)
+          {
+            asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                         "{%0,%1,%2,%3};"
+                         : "+f"(A[nh][0]), "+f"(A[nh][1]), "+f"(A[nh][2]), "+f"(A[nh][3])
+                         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(wr[t][nh].x), "r"(wr[t][nh].y));
+          }
         }
       }
 #pragma unroll
@@ -881,19 +907,23 @@ static MarchGrid march_grid(STS_Net nt, int n, int nimg)
   return m;
 }
 
-template <int MODE, int LOAD = net::LD_PLAIN>
+template <int MODE, int LOAD = net::LD_PLAIN, bool NARROW = false>
 static void conv_launch(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, const uint2* frags, __nv_bfloat16* out,
                         double* out64, double out_scale, const float* meta, const net::LoadArgs& la)
 {
   const MarchGrid m = march_grid(nt, n, nimg);
-  net::conv3x3_march_kernel<MODE, LOAD><<<m.grid, net::NTHR, 0, nt->ctx->stream>>>(in, n, n, frags, out, out64,
-                                                                                 out_scale, meta, la, m.rows);
+  net::conv3x3_march_kernel<MODE, LOAD, NARROW><<<m.grid, net::NTHR, 0, nt->ctx->stream>>>(
+      in, n, n, frags, out, out64, out_scale, meta, la, m.rows);
 }
 
+// convolution (or transposed convolution) with one layer's weights; W_in forward reads the
+// 3-channel network input (or its gradient) and runs narrow
 static void conv(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, int layer, bool transposed, __nv_bfloat16* out)
 {
-  conv_launch<0>(nt, in, n, nimg, (transposed ? nt->wt : nt->wf) + layer * 576, out, nullptr, 0.0, nullptr,
-                 net::LoadArgs());
+  const uint2* frags = (transposed ? nt->wt : nt->wf) + layer * 576;
+  if (layer == net::L_IN && !transposed)
+    conv_launch<0, net::LD_PLAIN, true>(nt, in, n, nimg, frags, out, nullptr, 0.0, nullptr, net::LoadArgs());
+  else conv_launch<0>(nt, in, n, nimg, frags, out, nullptr, 0.0, nullptr, net::LoadArgs());
 }
 
 static void pool(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, __nv_bfloat16* out)
@@ -955,7 +985,7 @@ static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
   la.scale = scale;
   la.sk    = sk;
   la.sg    = sg;
-  conv_launch<0, net::LD_R64>(nt, nullptr, n, 1, nt->wf + net::L_IN * 576, L[0].h, nullptr, 0.0, nullptr, la); // h0
+  conv_launch<0, net::LD_R64, true>(nt, nullptr, n, 1, nt->wf + net::L_IN * 576, L[0].h, nullptr, 0.0, nullptr, la); // h0
   pool(nt, L[0].h, n, 1, L[1].p);
   conv(nt, L[1].p, n / 2, 1, net::L_1, false, L[1].h);                                                // h1
   pool(nt, L[1].h, n / 2, 1, L[2].p);
@@ -1556,4 +1586,28 @@ extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b,
   if (iters) *iters = it;
   if (relres) *relres = tr;
   return ret;
+}
+
+// Shifted solve with a choice of method: the condition-number estimate of the Jacobi-scaled
+// operator, kappa = 1 + 4 gamma (cx + cy), predicts Jacobi-PCG's iteration count (~sqrt(kappa));
+// below kappa_min the network's per-iteration cost is not repaid and Jacobi-PCG runs directly,
+// above it flexible CG with the network (falling back to Jacobi-PCG itself if needed).
+extern "C" int STS_ImplicitSolveLearned(STS_Problem p, double gamma, STS_Net nt, N_Vector b, N_Vector x, double tol,
+                                        int maxit, double kappa_min, int* iters, double* relres, int* used_net)
+{
+  if (!p || !b || !x)
+  {
+    sts_set_error("STS_ImplicitSolveLearned: invalid arguments");
+    return -1;
+  }
+  if (!(kappa_min > 0.0)) kappa_min = 6000.0;
+  const double kappa = 1.0 + 4.0 * gamma * (p->cx + p->cy);
+  const bool net_ok  = nt && p->nx == p->ny && p->kind != STS_PROBLEM_PERIODIC && p->nx % 16 == 0 && p->nx <= nt->nmax;
+  if (used_net) *used_net = 0;
+  if (net_ok && kappa >= kappa_min)
+  {
+    if (used_net) *used_net = 1;
+    return STS_FCGSolve(p, gamma, nt, b, x, tol, maxit, iters, relres);
+  }
+  return STS_ImplicitSolvePCG(p, gamma, b, x, tol, maxit, 1, iters, relres);
 }
