@@ -182,16 +182,19 @@ constexpr int STG = 48; // staging bytes per pixel (32 + 16 of padding: conflict
 // mode 2: u = c0 + sk c1 + sg c2 (FP32; channel 2 sits in the next lane), redistributed so
 // that lanes 0..15 own pixels 0..15, then z = (out_scale u) + (out_scale scale) r in FP64: two
 // FP64 instructions per 16 pixels (GB300's FP64 issue rate is 1/64 of FP32).
-template <int MODE>
+// POOL: the output rows also go through 2x2 mean pooling (the next level's input, pout): the
+// staged BF16 row of an even y is kept and combined with row y+1, in the order of pool_kernel.
+template <int MODE, bool POOL = false>
 __device__ __forceinline__ void conv_epilogue(const float (&acc)[2][4], int lane, int xb, int y, int W,
                                               long long img_pix, __nv_bfloat16* out, double* out64, double out_scale,
-                                              const LoadArgs& la, unsigned char* stage)
+                                              const LoadArgs& la, unsigned char* stage, __nv_bfloat16* pout = nullptr)
 {
   const int pr0 = lane >> 2;
   if (MODE == 0)
   {
-    // through the warp's 512-byte staging buffer, so each lane stores one full 16-byte half
-    // pixel and the warp writes its 16 pixels x 32 bytes with one coalesced instruction
+    // through the warp's staging buffer, so each lane stores one full 16-byte half pixel and
+    // the warp writes its 16 pixels x 32 bytes with one coalesced instruction
+    unsigned char* st = stage + (POOL ? (y & 1) * 16 * STG : 0);
 #pragma unroll
     for (int half = 0; half < 2; ++half)
 #pragma unroll
@@ -199,12 +202,41 @@ __device__ __forceinline__ void conv_epilogue(const float (&acc)[2][4], int lane
       {
         const int co = nh * 8 + (lane & 3) * 2;
         __nv_bfloat162 v = __floats2bfloat162_rn(acc[nh][half * 2], acc[nh][half * 2 + 1]);
-        *reinterpret_cast<__nv_bfloat162*>(stage + (pr0 + half * 8) * STG + co * 2) = v;
+        *reinterpret_cast<__nv_bfloat162*>(st + (pr0 + half * 8) * STG + co * 2) = v;
       }
     __syncwarp();
     const int px = lane >> 1, gx = xb + px;
-    const uint4 v = *reinterpret_cast<const uint4*>(stage + px * STG + (lane & 1) * 16);
+    const uint4 v = *reinterpret_cast<const uint4*>(st + px * STG + (lane & 1) * 16);
     if (gx < W) *reinterpret_cast<uint4*>(out + ((long long)y * W + gx) * CH + (lane & 1) * 8) = v;
+    if (POOL && (y & 1) && lane < 16)
+    {
+      // pooled pixel k = lane / 2 of this warp's 8, channel half lane % 2
+      const int k = lane >> 1, hb = (lane & 1) * 16, gxc = xb / 2 + k;
+      if (2 * gxc < W)
+      {
+        const unsigned char* r0 = stage;            // row y - 1
+        const unsigned char* r1 = stage + 16 * STG; // row y
+        const uint4 a = *reinterpret_cast<const uint4*>(r0 + (2 * k) * STG + hb);
+        const uint4 b = *reinterpret_cast<const uint4*>(r0 + (2 * k + 1) * STG + hb);
+        const uint4 c = *reinterpret_cast<const uint4*>(r1 + (2 * k) * STG + hb);
+        const uint4 d = *reinterpret_cast<const uint4*>(r1 + (2 * k + 1) * STG + hb);
+        const __nv_bfloat162* A = reinterpret_cast<const __nv_bfloat162*>(&a);
+        const __nv_bfloat162* B = reinterpret_cast<const __nv_bfloat162*>(&b);
+        const __nv_bfloat162* Cc = reinterpret_cast<const __nv_bfloat162*>(&c);
+        const __nv_bfloat162* D = reinterpret_cast<const __nv_bfloat162*>(&d);
+        uint32_t o[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+        {
+          const float2 fa = __bfloat1622float2(A[m]), fb = __bfloat1622float2(B[m]), fc = __bfloat1622float2(Cc[m]),
+                       fd = __bfloat1622float2(D[m]);
+          __nv_bfloat162 t = __floats2bfloat162_rn(0.25f * (fa.x + fb.x + fc.x + fd.x), 0.25f * (fa.y + fb.y + fc.y + fd.y));
+          o[m] = *reinterpret_cast<uint32_t*>(&t);
+        }
+        *reinterpret_cast<uint4*>(pout + ((long long)(y / 2) * (W / 2) + gxc) * CH + (lane & 1) * 8) =
+            make_uint4(o[0], o[1], o[2], o[3]);
+      }
+    }
     __syncwarp();
   }
   else
@@ -229,22 +261,27 @@ __device__ __forceinline__ void conv_epilogue(const float (&acc)[2][4], int lane
 
 // NARROW: the input has channels 0..7 only (the network input [r, r sk, r sg], or its
 // gradient): the MMAs run with K = 8 (m16n8k8, A by ldmatrix.x2), half the tensor work.
-template <int MODE, int LOAD = LD_PLAIN, bool NARROW = false>
+template <int MODE, int LOAD = LD_PLAIN, bool NARROW = false, bool POOL = false>
 __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16* __restrict__ in, int H, int W,
                                                              const uint2* __restrict__ wf,
                                                              __nv_bfloat16* __restrict__ out,
                                                              double* __restrict__ out64, double out_scale,
-                                                             const float* __restrict__ meta, LoadArgs la, int rows)
+                                                             const float* __restrict__ meta, LoadArgs la, int rows,
+                                                             __nv_bfloat16* __restrict__ pout)
 {
   __shared__ __align__(128) unsigned char ring[MRING][ROWB];
-  __shared__ __align__(16) unsigned char stage[NTHR / 32][16 * STG]; // per-warp output staging
+  __shared__ __align__(16) unsigned char stage[NTHR / 32][(POOL ? 2 : 1) * 16 * STG]; // per-warp output staging
   __shared__ __align__(16) unsigned char rawring[LOAD == LD_PLAIN ? 1 : MRING][LOAD == LD_PLAIN ? 16 : RAWB];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int x0 = blockIdx.x * TC;
   const int ys = blockIdx.y * rows, ye = min(H, ys + rows);
   const long long img_pix = (long long)H * W * blockIdx.z;
   if (LOAD != LD_R64) in += img_pix * CH;
-  if (MODE == 0) out += img_pix * CH;
+  if (MODE == 0)
+  {
+    out += img_pix * CH;
+    if (POOL) pout += img_pix / 4 * CH;
+  }
   else
   {
     out64 += img_pix;
@@ -365,7 +402,7 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
       for (int nh = 0; nh < 2; ++nh)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[nh][q] += acd[nh][q];
-      conv_epilogue<MODE>(acc, lane, x0 + mt * 16, y, W, img_pix, out, out64, out_scale, la, stage[warp]);
+      conv_epilogue<MODE, POOL>(acc, lane, x0 + mt * 16, y, W, img_pix, out, out64, out_scale, la, stage[warp], pout);
     }
     // C: convert raw row y+2 into its ring slot (held row y-2, last read before the previous
     // barrier); its raw slot is reused by the copy of row y+6, issued after the barriers of
@@ -901,29 +938,37 @@ static MarchGrid march_grid(STS_Net nt, int n, int nimg)
   if (segs < 1) segs = 1;
   int rows = (int)((n + segs - 1) / segs);
   if (rows < 8) rows = 8;
+  rows += rows & 1; // even: row pairs stay in one CTA (fused pooling)
   MarchGrid m;
   m.rows = rows;
   m.grid = dim3((unsigned)strips, (unsigned)((n + rows - 1) / rows), (unsigned)nimg);
   return m;
 }
 
-template <int MODE, int LOAD = net::LD_PLAIN, bool NARROW = false>
+template <int MODE, int LOAD = net::LD_PLAIN, bool NARROW = false, bool POOL = false>
 static void conv_launch(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, const uint2* frags, __nv_bfloat16* out,
-                        double* out64, double out_scale, const float* meta, const net::LoadArgs& la)
+                        double* out64, double out_scale, const float* meta, const net::LoadArgs& la,
+                        __nv_bfloat16* pout = nullptr)
 {
   const MarchGrid m = march_grid(nt, n, nimg);
-  net::conv3x3_march_kernel<MODE, LOAD, NARROW><<<m.grid, net::NTHR, 0, nt->ctx->stream>>>(
-      in, n, n, frags, out, out64, out_scale, meta, la, m.rows);
+  net::conv3x3_march_kernel<MODE, LOAD, NARROW, POOL><<<m.grid, net::NTHR, 0, nt->ctx->stream>>>(
+      in, n, n, frags, out, out64, out_scale, meta, la, m.rows, pout);
 }
 
 // convolution (or transposed convolution) with one layer's weights; W_in forward reads the
 // 3-channel network input (or its gradient) and runs narrow
-static void conv(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, int layer, bool transposed, __nv_bfloat16* out)
+static void conv(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, int layer, bool transposed, __nv_bfloat16* out,
+                 __nv_bfloat16* pooled = nullptr)
 {
   const uint2* frags = (transposed ? nt->wt : nt->wf) + layer * 576;
+  const net::LoadArgs la;
   if (layer == net::L_IN && !transposed)
-    conv_launch<0, net::LD_PLAIN, true>(nt, in, n, nimg, frags, out, nullptr, 0.0, nullptr, net::LoadArgs());
-  else conv_launch<0>(nt, in, n, nimg, frags, out, nullptr, 0.0, nullptr, net::LoadArgs());
+  {
+    if (pooled) conv_launch<0, net::LD_PLAIN, true, true>(nt, in, n, nimg, frags, out, nullptr, 0.0, nullptr, la, pooled);
+    else conv_launch<0, net::LD_PLAIN, true>(nt, in, n, nimg, frags, out, nullptr, 0.0, nullptr, la);
+  }
+  else if (pooled) conv_launch<0, net::LD_PLAIN, false, true>(nt, in, n, nimg, frags, out, nullptr, 0.0, nullptr, la, pooled);
+  else conv_launch<0>(nt, in, n, nimg, frags, out, nullptr, 0.0, nullptr, la);
 }
 
 static void pool(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, __nv_bfloat16* out)
@@ -950,12 +995,9 @@ static void net_forward(STS_Net nt, int n, int nimg, const T* r, double scale, f
   net::Level* L   = nt->L;
   const long long ip = (long long)n * n, np = ip * nimg;
   net::input_kernel_t<T><<<grid_for(np), 256, 0, st>>>(np, ip, r, scale, sk, sg, meta, L[0].x);
-  conv(nt, L[0].x, n, nimg, net::L_IN, false, L[0].h);          // h0
-  pool(nt, L[0].h, n, nimg, L[1].p);                            // p0 (level 1)
-  conv(nt, L[1].p, n / 2, nimg, net::L_1, false, L[1].h);       // h1
-  pool(nt, L[1].h, n / 2, nimg, L[2].p);                        // p1
-  conv(nt, L[2].p, n / 4, nimg, net::L_2, false, L[2].h);       // h2
-  pool(nt, L[2].h, n / 4, nimg, L[3].p);                        // p2
+  conv(nt, L[0].x, n, nimg, net::L_IN, false, L[0].h, L[1].p);     // h0, p0 (level 1)
+  conv(nt, L[1].p, n / 2, nimg, net::L_1, false, L[1].h, L[2].p);  // h1, p1
+  conv(nt, L[2].p, n / 4, nimg, net::L_2, false, L[2].h, L[3].p);  // h2, p2
   conv(nt, L[3].p, n / 8, nimg, net::L_3, false, L[3].h);       // h3 = g3
   conv(nt, L[3].h, n / 8, nimg, net::L_3, true, L[3].y);        // y3 = convT(g3, W_3)
   upadd(nt, L[3].y, L[2].h, n / 4, nimg, L[2].g);               // g2 = h2 + poolT(y3)
@@ -985,12 +1027,10 @@ static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
   la.scale = scale;
   la.sk    = sk;
   la.sg    = sg;
-  conv_launch<0, net::LD_R64, true>(nt, nullptr, n, 1, nt->wf + net::L_IN * 576, L[0].h, nullptr, 0.0, nullptr, la); // h0
-  pool(nt, L[0].h, n, 1, L[1].p);
-  conv(nt, L[1].p, n / 2, 1, net::L_1, false, L[1].h);                                                // h1
-  pool(nt, L[1].h, n / 2, 1, L[2].p);
-  conv(nt, L[2].p, n / 4, 1, net::L_2, false, L[2].h);                                                // h2
-  pool(nt, L[2].h, n / 4, 1, L[3].p);
+  conv_launch<0, net::LD_R64, true, true>(nt, nullptr, n, 1, nt->wf + net::L_IN * 576, L[0].h, nullptr, 0.0, nullptr, la,
+                                          L[1].p);                                     // h0, p0
+  conv(nt, L[1].p, n / 2, 1, net::L_1, false, L[1].h, L[2].p);                         // h1, p1
+  conv(nt, L[2].p, n / 4, 1, net::L_2, false, L[2].h, L[3].p);                         // h2, p2
   conv(nt, L[3].p, n / 8, 1, net::L_3, false, L[3].h);                                                // h3
   conv(nt, L[3].h, n / 8, 1, net::L_3, true, L[3].y);                                                 // y3
   net::LoadArgs lu;
@@ -1350,25 +1390,26 @@ __global__ void __launch_bounds__(256) fcg_pq_march_kernel(ProbDev P, const doub
     const long long k = jj * nx + ii;
     return __fma_rn(beta, pp[k], z[k]);
   };
-  // row jj of p into ring slot (jj - j0 + 1) % 3: own column, threads 0 / 255 also the halo
-  auto stage_row = [&](long long jj) {
-    double* rw = ring[(int)((jj - j0 + 1) % 3)];
+  // row jj of p into ring slot sl: own column, threads 0 / 255 also the halo columns
+  auto stage_row = [&](long long jj, int sl) {
+    double* rw  = ring[sl];
     rw[tid + 1] = pval(i, jj);
     if (tid == 0) rw[0] = pval(x0 - 1, jj);
     if (tid == 255) rw[257] = pval(x0 + 256, jj);
   };
-  stage_row(j0 - 1);
-  stage_row(j0);
+  int sm = 0, sc = 1, sn = 2; // ring slots of rows j-1, j, j+1 (rotated, no modulo)
+  stage_row(j0 - 1, sm);
+  stage_row(j0, sc);
   for (long long j = j0; j < j1; ++j)
   {
-    stage_row(j + 1);
+    stage_row(j + 1, sn);
     const double rk = col ? r[j * nx + i] : 0.0;
     __syncthreads();
     if (col)
     {
-      const double* rm = ring[(int)((j - j0) % 3)];
-      const double* rc = ring[(int)((j - j0 + 1) % 3)];
-      const double* rn = ring[(int)((j - j0 + 2) % 3)];
+      const double* rm = ring[sm];
+      const double* rc = ring[sc];
+      const double* rn = ring[sn];
       const double pc = rc[tid + 1];
       const double sx = rc[tid] + rc[tid + 2], sy = rm[tid + 1] + rn[tid + 1];
       const double qk = __fma_rn(c1, sx, __fma_rn(c2, sy, c0 * pc));
@@ -1378,7 +1419,11 @@ __global__ void __launch_bounds__(256) fcg_pq_march_kernel(ProbDev P, const doub
       xsum::add(a[0], pc * rk, fl[0]);
       xsum::add(a[1], pc * qk, fl[1]);
     }
-    __syncthreads(); // row j-1's slot is overwritten by row j+2 in the next iteration
+    __syncthreads(); // row j-1's slot receives row j+2 in the next iteration
+    const int t = sm;
+    sm          = sc;
+    sc          = sn;
+    sn          = t;
   }
   krylov_block_finish<256, 2>(a, fl, s, [&](const double* v) {
     s->alpha   = v[0] / v[1];
