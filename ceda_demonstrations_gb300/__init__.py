@@ -151,6 +151,8 @@ SIGNATURES = [
                                        _ip, _dp]),
     ("STS_SDIRK2Evolve", C.c_int, [_vp, _NV, C.c_double, C.c_double, C.c_int, C.c_double,
                                    C.c_int, C.POINTER(_ll)]),
+    ("STS_SDIRK2EvolveLearned", C.c_int, [_vp, _vp, _NV, C.c_double, C.c_double, C.c_int,
+                                          C.c_double, C.c_int, C.POINTER(_ll)]),
     ("STS_BatchCreate", _vp, [_vp, C.c_int, _ip, _dp, _dp]),
     ("STS_BatchFree", C.c_int, [C.POINTER(_vp)]),
     ("STS_BatchTotalDOF", _ll, [_vp]),
@@ -606,6 +608,15 @@ def sdirk2_evolve(problem, y, t0, h, nsteps, tol=1e-10, maxit=100000):
     rc = lib().STS_SDIRK2Evolve(problem.h, y.h, t0, h, nsteps, tol, maxit, C.byref(it))
     if rc < 0:
         _err("STS_SDIRK2Evolve")
+    return it.value
+
+
+def sdirk2_evolve_learned(problem, net, y, t0, h, nsteps, tol=1e-10, maxit=100000):
+    """SDIRK2 steps with the stage solves by the learned-or-Jacobi shifted solve."""
+    it = _ll()
+    rc = lib().STS_SDIRK2EvolveLearned(problem.h, net.h, y.h, t0, h, nsteps, tol, maxit, C.byref(it))
+    if rc < 0:
+        _err("STS_SDIRK2EvolveLearned")
     return it.value
 
 

@@ -410,8 +410,9 @@ extern "C" int STS_SUNLinSolFree(void* LS)
 // SDIRK2 (Alexander, gamma = 1 - 1/sqrt(2)), each stage's linear Newton correction solved
 // by the fused Jacobi-PCG; same arithmetic order as the oracle's orc_sdirk2.
 // ---------------------------------------------------------------------------------------
-extern "C" int STS_SDIRK2Evolve(STS_Problem p, N_Vector y, double t0, double h, int nsteps, double tol, int maxit,
-                                long long* total_iters)
+// stage solves through `solve(gamma, rhs, d, &iters)`; returns < 0 on failure
+template <typename Solve>
+static int sdirk2_run(STS_Problem p, N_Vector y, double t0, double h, int nsteps, long long* total_iters, Solve solve)
 {
   if (!p || !y || NVL(y) != p->nx * p->ny) return -1;
   const double g = 1.0 - sqrt(0.5);
@@ -424,17 +425,16 @@ extern "C" int STS_SDIRK2Evolve(STS_Problem p, N_Vector y, double t0, double h, 
   {
     const double hg = h * g;
     int it          = 0;
-    double rel;
     STS_Diffusion(t + g * h, y, f, p);
     N_VScale_Sts(hg, f, rhs);
-    if (STS_ImplicitSolvePCG(p, hg, rhs, d, tol, maxit, 1, &it, &rel) < 0) ret = -1;
+    if (solve(hg, rhs, d, &it) < 0) ret = -1;
     iters += it;
     N_VLinearSum_Sts(1.0, y, 1.0, d, Y1);
     STS_Diffusion(t + g * h, Y1, f1, p);
     STS_Diffusion(t + h, y, f, p);
     const double h1g = h * (1.0 - g);
     N_VLinearSum_Sts(h1g, f1, hg, f, rhs);
-    if (STS_ImplicitSolvePCG(p, hg, rhs, d, tol, maxit, 1, &it, &rel) < 0) ret = -1;
+    if (solve(hg, rhs, d, &it) < 0) ret = -1;
     iters += it;
     N_VLinearSum_Sts(1.0, y, 1.0, d, y);
     t = t0 + (s + 1) * h;
@@ -447,4 +447,25 @@ extern "C" int STS_SDIRK2Evolve(STS_Problem p, N_Vector y, double t0, double h, 
   N_VDestroy_Sts(Y1);
   if (total_iters) *total_iters = iters;
   return ret;
+}
+
+extern "C" int STS_SDIRK2Evolve(STS_Problem p, N_Vector y, double t0, double h, int nsteps, double tol, int maxit,
+                                long long* total_iters)
+{
+  return sdirk2_run(p, y, t0, h, nsteps, total_iters, [&](double hg, N_Vector rhs, N_Vector d, int* it) {
+    double rel;
+    return STS_ImplicitSolvePCG(p, hg, rhs, d, tol, maxit, 1, it, &rel);
+  });
+}
+
+// The same SDIRK2 driver with each stage solved by STS_ImplicitSolveLearned (FCG with the
+// learned preconditioner where the condition estimate favours it, Jacobi-PCG elsewhere).
+extern "C" int STS_SDIRK2EvolveLearned(STS_Problem p, STS_Net net, N_Vector y, double t0, double h, int nsteps,
+                                       double tol, int maxit, long long* total_iters)
+{
+  return sdirk2_run(p, y, t0, h, nsteps, total_iters, [&](double hg, N_Vector rhs, N_Vector d, int* it) {
+    double rel;
+    int used;
+    return STS_ImplicitSolveLearned(p, hg, net, rhs, d, tol, maxit, 0.0, it, &rel, &used);
+  });
 }

@@ -270,6 +270,11 @@ int STS_ImplicitSolvePCG(STS_Problem p, double gamma, N_Vector b, N_Vector x, do
 /* fixed-step SDIRK2 with fused Jacobi-PCG stage solves (ARKStep DIRK, main.cpp:242,272) */
 int STS_SDIRK2Evolve(STS_Problem p, N_Vector y, double t0, double h, int nsteps, double tol,
                      int maxit, long long* total_iters);
+/* SDIRK2 with each stage solved by STS_ImplicitSolveLearned (declared below); STS_Net is the
+ * learned preconditioner's handle */
+typedef struct STS_Net_* STS_Net;
+int STS_SDIRK2EvolveLearned(STS_Problem p, STS_Net net, N_Vector y, double t0, double h, int nsteps,
+                            double tol, int maxit, long long* total_iters);
 
 /* ------------------------------------------------------------------------------------
  * Batched STS (new; the reference integrates one problem per run): many independent
@@ -312,7 +317,6 @@ int STS_BatchGetLaunch(STS_Batch b, int* threads, int* ctas_per_sm, int* cluster
  * exact adjoint: an SPD additive multilevel preconditioner with learned level operators.
  * Sizes: multiples of 16.
  * ----------------------------------------------------------------------------------*/
-typedef struct STS_Net_* STS_Net;
 STS_Net STS_NetCreate(STS_Context ctx, int nmax, unsigned long long seed);
 int STS_NetFree(STS_Net* net);
 /* weights: 4 layers (W_in, W_1, W_2, W_3) x [16][16][3][3] FP32 (W_in: 3 input channels) */

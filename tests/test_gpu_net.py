@@ -168,3 +168,17 @@ def test_trained_network_cuts_fcg_iterations(ctx):
     assert rel_fcg <= 2e-8  # true FP64 residual of the returned iterate
     assert _rel(x_fcg.numpy(), x_pcg.numpy()) < 1e-6
     assert it_fcg < 0.5 * it_pcg, (it_fcg, it_pcg)
+
+
+def test_sdirk2_with_learned_solves_matches_jacobi(ctx):
+    """SDIRK2 on the manufactured problem with its stage systems solved by the learned-or-Jacobi
+    solve (kappa ~ 7.7e3 here: the network path) agrees with the Jacobi-PCG driver to the
+    solver tolerance."""
+    n = 256
+    P = sts.Problem(ctx, sts.MANUFACTURED, n, n, 1.0, 1.0)
+    net = sts.Net(ctx, n, seed=3)
+    ya, yb = P.initial(), P.initial()
+    ia = sts.sdirk2_evolve(P, ya, 0.0, 0.05, 3, tol=1e-10)
+    ib = sts.sdirk2_evolve_learned(P, net, yb, 0.0, 0.05, 3, tol=1e-10)
+    assert ia > 0 and ib > 0
+    assert _rel(yb.numpy(), ya.numpy()) < 1e-8
