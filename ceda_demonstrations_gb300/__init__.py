@@ -168,6 +168,8 @@ SIGNATURES = [
                                     _ip, _ip, _dp]),
     ("STS_BatchSetCluster", C.c_int, [_vp, C.c_int, C.c_int]),
     ("STS_BatchGetLaunch", C.c_int, [_vp, _ip, _ip, _ip, _ip]),
+    ("STS_LSRKStepSetNumDomEigEstInitPreprocessIters", C.c_int, [_vp, C.c_int]),
+    ("STS_LSRKStepSetNumDomEigEstPreprocessIters", C.c_int, [_vp, C.c_int]),
     ("STS_LSRKStepWriteCheckpoint", C.c_int, [_vp, C.c_char_p]),
     ("STS_LSRKStepReadCheckpoint", C.c_int, [_vp, C.c_char_p]),
     ("STS_NetCreate", _vp, [_vp, C.c_int, C.c_ulonglong]),
@@ -451,7 +453,7 @@ class LSRKStep:
 
     def __init__(self, ctx, rhs, t0, y0, method=RKC, rtol=1e-6, atol=1e-10, controller=PID,
                  smax=200, mixed=False, graphs=True, dom_eig=None, power=None, maxsteps=100000,
-                 hfixed=0.0, stage_kernel=0):
+                 hfixed=0.0, stage_kernel=0, dee_warmups=(0, 0)):
         self.ctx = ctx
         L = lib()
         self._keep = []
@@ -481,6 +483,8 @@ class LSRKStep:
         L.STS_LSRKStepSetUseGraphs(self.mem, int(graphs))
         L.STS_LSRKStepSetStageKernel(self.mem, int(stage_kernel))
         L.STS_ARKodeSetMaxNumSteps(self.mem, maxsteps)
+        L.STS_LSRKStepSetNumDomEigEstInitPreprocessIters(self.mem, int(dee_warmups[0]))
+        L.STS_LSRKStepSetNumDomEigEstPreprocessIters(self.mem, int(dee_warmups[1]))
         if hfixed > 0:
             L.STS_ARKodeSetFixedStep(self.mem, hfixed)
         if power is not None:

@@ -181,6 +181,8 @@ struct LSRKMem {
   STS_ARKDomEigFn domeig = nullptr;
   bool power            = false;
   int dee_maxiters      = 100;
+  int dee_init_warmups  = 0; // power iterations before the first estimate
+  int dee_succ_warmups  = 0; // power iterations before each later estimate
   double dee_reltol     = 0.01;
   int method            = STS_LSRK_RKC_2;
   int controller        = STS_ADAPT_PID;
@@ -623,8 +625,15 @@ static int dee_update(LSRKMem* m, N_Vector ycur, N_Vector fcur)
                       m->ctx->stream);
     }
     N_Vector ev = N_VMake_Sts(m->n, m->evec, m->ctx);
-    int it      = 0;
-    int rc      = STS_PowerIteration(p, ev, m->dee_maxiters, m->dee_reltol, &lam, &it);
+    int it      = 0, rc = 0;
+    // warm-up ("preprocessing") iterations: v <- A v / |A v| without a convergence test
+    const int warm = (m->ndee == 0) ? m->dee_init_warmups : m->dee_succ_warmups;
+    if (warm > 0)
+    {
+      rc = STS_PowerIteration(p, ev, warm, 0.0, &lam, &it);
+      m->nfe_dee += it;
+    }
+    if (rc == 0) rc = STS_PowerIteration(p, ev, m->dee_maxiters, m->dee_reltol, &lam, &it);
     N_VDestroy_Sts(ev);
     if (rc) return -1;
     m->nfe_dee += it;
@@ -1449,5 +1458,22 @@ extern "C" int STS_LSRKStepReadCheckpoint(void* mem, const char* path)
   m->initialized     = h.initialized != 0;
   m->after_fail      = h.after_fail != 0;
   m->last_s          = h.last_s;
+  return STS_SUCCESS;
+}
+
+// LSRKStepSetNumDomEigEstInitPreprocessIters / LSRKStepSetNumDomEigEstPreprocessIters
+// (gkeyll_diffusion/gk_diffusion_1x1v_p1.c:873-885): power iterations run before the first
+// and before every later dominant-eigenvalue estimate
+extern "C" int STS_LSRKStepSetNumDomEigEstInitPreprocessIters(void* mem, int iters)
+{
+  CHECK_MEM(mem);
+  MEM(mem)->dee_init_warmups = iters > 0 ? iters : 0;
+  return STS_SUCCESS;
+}
+
+extern "C" int STS_LSRKStepSetNumDomEigEstPreprocessIters(void* mem, int iters)
+{
+  CHECK_MEM(mem);
+  MEM(mem)->dee_succ_warmups = iters > 0 ? iters : 0;
   return STS_SUCCESS;
 }

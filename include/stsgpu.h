@@ -197,7 +197,12 @@ int STS_LSRKStepSetSTSMethod(void* mem, int method);                 /* main.cpp
 int STS_ARKodeSStolerances(void* mem, double rtol, double atol);      /* main.cpp:262 */
 int STS_ARKodeSetUserData(void* mem, void* user_data);                /* main.cpp:266 */
 int STS_LSRKStepSetDomEigFn(void* mem, STS_ARKDomEigFn fn);           /* main.cpp:352 */
-int STS_LSRKStepSetDomEigEstimatorPower(void* mem, int maxiters, double reltol); /* main.cpp:344-348 */
+int STS_LSRKStepSetDomEigEstimatorPower(void* mem, int maxiters, double reltol);
+/* LSRKStepSetNumDomEigEstInitPreprocessIters / ...PreprocessIters
+ * (gkeyll_diffusion/gk_diffusion_1x1v_p1.c:873-885): warm-up power iterations before the
+ * first / every later estimate of the power-iteration estimator */
+int STS_LSRKStepSetNumDomEigEstInitPreprocessIters(void* arkode_mem, int iters);
+int STS_LSRKStepSetNumDomEigEstPreprocessIters(void* arkode_mem, int iters); /* main.cpp:344-348 */
 int STS_LSRKStepSetDomEigFrequency(void* mem, long long nsteps);      /* gk_diffusion_1x1v_p1.c / analytic_CR_test.c:320 */
 int STS_LSRKStepSetMaxNumStages(void* mem, int smax);                 /* analytic_CR_test.c:324 */
 int STS_LSRKStepSetDomEigSafetyFactor(void* mem, double safety);      /* analytic_CR_test.c:332 */

@@ -34,7 +34,8 @@ class Opts(C.Structure):
                 ("smax", C.c_int), ("internaleig", C.c_int), ("dee_maxiters", C.c_int),
                 ("dom_eig_freq", C.c_int), ("pad_", C.c_int), ("maxsteps", C.c_long),
                 ("rtol", C.c_double), ("atol", C.c_double), ("hfixed", C.c_double),
-                ("eig_safety", C.c_double), ("dee_reltol", C.c_double)]
+                ("eig_safety", C.c_double), ("dee_reltol", C.c_double),
+                ("dee_init_warmups", C.c_int), ("dee_succ_warmups", C.c_int)]
 
 
 class State(C.Structure):
@@ -244,11 +245,12 @@ class Problem:
 
 def make_opts(method=RKC, mixed=False, controller=0, smax=200, rtol=1e-6, atol=1e-10,
               hfixed=0.0, internaleig=False, maxsteps=100000, eig_safety=1.01, dee_maxiters=100,
-              dee_reltol=0.01, dom_eig_freq=25):
+              dee_reltol=0.01, dom_eig_freq=25, dee_warmups=(0, 0)):
     return Opts(method=method, mixed=int(mixed), controller=controller, smax=smax,
                 internaleig=int(internaleig), dee_maxiters=dee_maxiters, dom_eig_freq=dom_eig_freq,
                 maxsteps=maxsteps, rtol=rtol, atol=atol, hfixed=hfixed, eig_safety=eig_safety,
-                dee_reltol=dee_reltol)
+                dee_reltol=dee_reltol, dee_init_warmups=dee_warmups[0],
+                dee_succ_warmups=dee_warmups[1])
 
 
 class Integrator:

@@ -995,6 +995,9 @@ int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double 
           st->evec = (double*)malloc(n * sizeof(double));
           memcpy(st->evec, y, n * sizeof(double));
         }
+        /* warm-up iterations (LSRKStepSetNumDomEigEst[Init]PreprocessIters): no convergence test */
+        int warm = (st->ndee == 0) ? o->dee_init_warmups : o->dee_succ_warmups;
+        if (warm > 0) st->nfe_dee += orc_power_iteration(p, st->evec, warm, 0.0, &lam);
         int it = orc_power_iteration(p, st->evec, o->dee_maxiters > 0 ? o->dee_maxiters : 100,
                                      o->dee_reltol > 0.0 ? o->dee_reltol : 0.01, &lam);
         st->nfe_dee += it;

@@ -44,6 +44,7 @@ typedef struct orc_opts {
   int pad_;
   long maxsteps;   /* per evolve call; <= 0 means 500 */
   double rtol, atol, hfixed, eig_safety, dee_reltol;
+  int dee_init_warmups, dee_succ_warmups; /* power iterations before the first / later estimates */
 } orc_opts;
 
 typedef struct orc_state {

@@ -113,6 +113,25 @@ def test_power_iteration_estimator_bitwise(ctx, stslib, oracle):
     assert np.array_equal(yout.numpy(), J.y)
 
 
+def test_power_iteration_warmups_bitwise(ctx, stslib, oracle):
+    """Warm-up ("preprocessing") power iterations before the first and the later estimates
+    (LSRKStepSetNumDomEigEst[Init]PreprocessIters) against the oracle, bit for bit."""
+    pk = dict(kind=0, nx=40, ny=32, kx=1.0, ky=0.5)
+    G = stslib.Problem(ctx, **pk)
+    O = oracle.Problem(**pk)
+    I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), method=1, rtol=1e-6, atol=1e-10,
+                        power=(100, 0.01), dee_warmups=(7, 2))
+    J = oracle.Integrator(O, O.initial(), method=1, rtol=1e-6, atol=1e-10, internaleig=True,
+                          dee_warmups=(7, 2))
+    yout = G.vector()
+    I.evolve(0.05, yout)
+    assert J.evolve(0.05) == 0
+    si, sj = I.stats(), J.stats()
+    assert si["ndee"] >= 2 and si["nfe_dee"] == sj["nfe_dee"]
+    assert si["spectral_radius"] == sj["spectral_radius"]
+    assert np.array_equal(yout.numpy(), J.y)
+
+
 def test_graphs_do_not_change_results(ctx, stslib, oracle):
     pk = dict(kind=0, nx=64, ny=32, kx=1.0, ky=1.0)
     ok = dict(method=1, rtol=1e-6, atol=1e-10)
