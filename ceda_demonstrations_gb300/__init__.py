@@ -26,6 +26,7 @@ __all__ = ["lib", "Context", "NVector", "Problem", "LSRKStep", "PCGSolver", "imp
            "Net", "fcg_solve", "implicit_solve_learned", "harvest_pcg_pairs", "net_features", "smooth_field", "STSError"]
 
 RKC, RKL = 0, 1
+SSP_S_2, SSP_S_3, SSP_10_4 = 2, 3, 4
 PID, PI, I = 0, 1, 2
 MANUFACTURED, UNFORCED, PERIODIC = 0, 1, 2
 NORMAL, ONE_STEP = 1, 2
@@ -168,6 +169,10 @@ SIGNATURES = [
                                     _ip, _ip, _dp]),
     ("STS_BatchSetCluster", C.c_int, [_vp, C.c_int, C.c_int]),
     ("STS_BatchGetLaunch", C.c_int, [_vp, _ip, _ip, _ip, _ip]),
+    ("STS_LSRKStepCreateSSP", _vp, [_vp, C.c_double, _NV, _vp]),
+    ("STS_LSRKStepSetSSPMethod", C.c_int, [_vp, C.c_int]),
+    ("STS_LSRKStepSetNumSSPStages", C.c_int, [_vp, C.c_int]),
+    ("STS_LSRKSSPWeights", C.c_int, [C.c_int, C.c_int, _dp, _dp, _dp]),
     ("STS_LSRKStepSetNumDomEigEstInitPreprocessIters", C.c_int, [_vp, C.c_int]),
     ("STS_LSRKStepSetNumDomEigEstPreprocessIters", C.c_int, [_vp, C.c_int]),
     ("STS_LSRKStepWriteCheckpoint", C.c_int, [_vp, C.c_char_p]),
@@ -453,7 +458,7 @@ class LSRKStep:
 
     def __init__(self, ctx, rhs, t0, y0, method=RKC, rtol=1e-6, atol=1e-10, controller=PID,
                  smax=200, mixed=False, graphs=True, dom_eig=None, power=None, maxsteps=100000,
-                 hfixed=0.0, stage_kernel=0, dee_warmups=(0, 0)):
+                 hfixed=0.0, stage_kernel=0, dee_warmups=(0, 0), ssp=None):
         self.ctx = ctx
         L = lib()
         self._keep = []
@@ -469,13 +474,21 @@ class LSRKStep:
             fn = C.cast(cb, _vp)
             ud = None
             self.problem = None
-        self.mem = L.STS_LSRKStepCreateSTS(fn, t0, y0.h, ctx.h)
+        if ssp is None:
+            self.mem = L.STS_LSRKStepCreateSTS(fn, t0, y0.h, ctx.h)
+        else:  # ssp = (type, stages)
+            self.mem = L.STS_LSRKStepCreateSSP(fn, t0, y0.h, ctx.h)
         if not self.mem:
-            _err("STS_LSRKStepCreateSTS")
+            _err("STS_LSRKStepCreate")
         ctx.live += 1
         self.n = len(y0)
         L.STS_ARKodeSetUserData(self.mem, ud)
-        L.STS_LSRKStepSetSTSMethod(self.mem, method)
+        if ssp is None:
+            L.STS_LSRKStepSetSTSMethod(self.mem, method)
+        else:
+            if L.STS_LSRKStepSetSSPMethod(self.mem, ssp[0]) != 0 or \
+                    L.STS_LSRKStepSetNumSSPStages(self.mem, ssp[1]) != 0:
+                _err("STS_LSRKStepSetSSPMethod")
         L.STS_ARKodeSStolerances(self.mem, rtol, atol)
         L.STS_ARKodeSetAdaptController(self.mem, controller)
         L.STS_LSRKStepSetMaxNumStages(self.mem, smax)
@@ -876,3 +889,11 @@ def implicit_solve_learned(problem, gamma, net, b, x, tol=1e-8, maxit=20000, kap
     if rc < 0:
         _err("STS_ImplicitSolveLearned")
     return it.value, rel.value, rc, bool(used.value)
+
+
+def ssp_weights(type_, s):
+    """(b, c, w = b - bhat) of an SSP method, as the integrator uses them."""
+    b, c, w = np.empty(s), np.empty(s), np.empty(s)
+    if lib().STS_LSRKSSPWeights(type_, s, _dptr(b), _dptr(c), _dptr(w)) != 0:
+        _err("STS_LSRKSSPWeights")
+    return b, c, w

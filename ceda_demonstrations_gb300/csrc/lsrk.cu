@@ -139,8 +139,17 @@ extern "C" int STS_LSRKStagesNeeded(int method, double h, double rho, int smax, 
 }
 
 static constexpr double ORD = 3.0, BIAS = 1.5, TINYE = 1.0e-10;
+static double controller_estimate(int controller, double h, double dsm, double ep1, double ep2, long long nhist,
+                                  double ORD);
 extern "C" double STS_AdaptControllerEstimate(int controller, double h, double dsm, double ep1, double ep2,
                                               long long nhist)
+{
+  return controller_estimate(controller, h, dsm, ep1, ep2, nhist, ORD);
+}
+
+// the controllers for an error estimate of order ORD (3 for the STS methods' embedding)
+static double controller_estimate(int controller, double h, double dsm, double ep1, double ep2, long long nhist,
+                                  double ORD)
 {
   double e1 = BIAS * dsm;
   if (e1 < TINYE) e1 = TINYE;
@@ -185,6 +194,11 @@ struct LSRKMem {
   int dee_succ_warmups  = 0; // power iterations before each later estimate
   double dee_reltol     = 0.01;
   int method            = STS_LSRK_RKC_2;
+  double ord            = 3.0; // order of the error estimate seen by the controller
+  // SSP methods (LSRKStepCreateSSP): stage count and the error weights h (b_j - bhat_j)
+  bool ssp              = false;
+  int ssp_stages        = 10;
+  std::vector<double> ssp_w, ssp_c; // error weights b - bhat, stage times
   int controller        = STS_ADAPT_PID;
   int smax              = 200;
   double rtol = 1e-4, atol = 1e-9; // ARKODE defaults until SStolerances is called
@@ -233,8 +247,181 @@ struct LSRKMem {
 
 static bool fused(const LSRKMem* m)
 {
-  return m->rhs == STS_Diffusion && m->user_data != nullptr &&
+  return !m->ssp && m->rhs == STS_Diffusion && m->user_data != nullptr &&
          ((STS_Problem)m->user_data)->kind != STS_PROBLEM_PERIODIC;
+}
+
+// ---------------------------------------------------------------------------------------
+// SSP methods of LSRKStepCreateSSP (diffusion_2D/main.cpp:250-294), restated from Ketcheson,
+// "Highly efficient strong stability-preserving Runge-Kutta methods with low-storage
+// implementations", SIAM J. Sci. Comput. 30 (2008):
+//   SSP(s,2), s >= 2:       s-1 forward-Euler substeps of h/(s-1), then
+//                           y+ = y/s + (s-1)/s (Y + h/(s-1) F(Y));
+//   SSP(s,3), s = n^2 >= 4: Euler substeps of h/(n^2-n) with one convex combination
+//                           (n/(2n-1)) q2 + ((n-1)/(2n-1)) (q1 + h/r F(q1)) at substep n(n+1)/2;
+//   SSP(10,4):              5 substeps of h/6, q2 = q2/25 + 9 q1/25, q1 = 15 q2 - 5 q1,
+//                           4 substeps, y+ = q2 + 3/5 q1 + h/10 F(q1).
+// Embedded estimates (this implementation's choice; the SUNDIALS embeddings are not available
+// here): SSP(s,2) the internal stage Y_s (first order: weights 1/(s-1) on the first s-1
+// stage derivatives); SSP(s,3) and SSP(10,4) the weights nearest to a reference (uniform 1/s;
+// for SSP(10,4), whose b is uniform, alternating 0.15 / 0.05) that satisfy the order
+// conditions of order 2 (resp. 3) on the method's own stages. The error estimate is
+// h sum_j (b_j - bhat_j) F_j; the controller uses order (embedding order + 1).
+// ---------------------------------------------------------------------------------------
+enum { SSP_S_2 = STS_LSRK_SSP_S_2, SSP_S_3 = STS_LSRK_SSP_S_3, SSP_10_4 = STS_LSRK_SSP_10_4 };
+
+static bool ssp_stages_valid(int type, int s)
+{
+  if (type == SSP_S_2) return s >= 2 && s <= 1024;
+  if (type == SSP_S_3)
+  {
+    const int n = (int)std::lround(std::sqrt((double)s));
+    return n >= 2 && n * n == s && s <= 1024;
+  }
+  return type == SSP_10_4 && s == 10;
+}
+
+// Butcher weights of the SSP method (registers tracked as y coefficient + multiples of h F_j):
+// A (s x s, row-major), b, c; and the error weights w = b - bhat
+static void ssp_tableau(int type, int s, std::vector<double>& A, std::vector<double>& b, std::vector<double>& c,
+                        std::vector<double>& w)
+{
+  struct Reg {
+    double cy;
+    std::vector<double> f;
+  };
+  // the stage matrix is only needed for the third-order conditions of SSP(10,4)
+  A.assign(type == SSP_10_4 ? (size_t)s * s : 0, 0.0);
+  c.assign(s, 0.0);
+  int j = 0;
+  auto stage = [&](const Reg& q) {
+    double cj = 0.0;
+    for (int k = 0; k < s; ++k)
+    {
+      if (type == SSP_10_4) A[(size_t)j * s + k] = q.f[k];
+      cj += q.f[k];
+    }
+    c[j] = cj;
+    return j++;
+  };
+  auto comb = [&](double a, const Reg& x, double bb, const Reg& y) {
+    Reg r{a * x.cy + bb * y.cy, std::vector<double>(s)};
+    for (int k = 0; k < s; ++k) r.f[k] = a * x.f[k] + bb * y.f[k];
+    return r;
+  };
+  Reg q1{1.0, std::vector<double>(s, 0.0)}, q2 = q1, fin = q1;
+  if (type == SSP_S_2)
+  {
+    const double r = s - 1.0;
+    for (int i = 0; i < s - 1; ++i) q1.f[stage(q1)] += 1.0 / r;
+    const int js = stage(q1);
+    Reg t        = q1;
+    t.f[js] += 1.0 / r;
+    fin = comb(1.0 / s, Reg{1.0, std::vector<double>(s, 0.0)}, (s - 1.0) / s, t);
+  }
+  else if (type == SSP_S_3)
+  {
+    const int n    = (int)std::lround(std::sqrt((double)s));
+    const double r = (double)(n * n - n);
+    const int e1 = (n - 1) * (n - 2) / 2, e2 = n * (n + 1) / 2;
+    for (int i = 1; i <= e1; ++i) q1.f[stage(q1)] += 1.0 / r;
+    q2 = q1;
+    for (int i = e1 + 1; i <= e2 - 1; ++i) q1.f[stage(q1)] += 1.0 / r;
+    const int jc = stage(q1);
+    Reg t        = q1;
+    t.f[jc] += 1.0 / r;
+    q1 = comb((double)n / (2 * n - 1), q2, (n - 1.0) / (2 * n - 1), t);
+    for (int i = e2 + 1; i <= n * n; ++i) q1.f[stage(q1)] += 1.0 / r;
+    fin = q1;
+  }
+  else
+  {
+    for (int i = 1; i <= 5; ++i) q1.f[stage(q1)] += 1.0 / 6.0;
+    q2 = comb(1.0 / 25.0, q2, 9.0 / 25.0, q1);
+    q1 = comb(15.0, q2, -5.0, q1);
+    for (int i = 6; i <= 9; ++i) q1.f[stage(q1)] += 1.0 / 6.0;
+    const int jl = stage(q1);
+    Reg t        = q1;
+    fin          = comb(1.0, q2, 3.0 / 5.0, t);
+    fin.f[jl] += 1.0 / 10.0;
+  }
+  b = fin.f;
+  std::vector<double> bh(s);
+  if (type == SSP_S_2)
+    for (int k = 0; k < s; ++k) bh[k] = (k < s - 1) ? 1.0 / (s - 1.0) : 0.0;
+  else
+  {
+    // bhat = u - C^T (C C^T)^-1 (C u - d): nearest to uniform u under the order conditions
+    std::vector<std::vector<double>> C;
+    std::vector<double> d;
+    C.push_back(std::vector<double>(s, 1.0));
+    d.push_back(1.0);
+    C.push_back(c);
+    d.push_back(0.5);
+    if (type == SSP_10_4)
+    {
+      std::vector<double> c2(s), Ac(s, 0.0);
+      for (int k = 0; k < s; ++k)
+      {
+        c2[k] = c[k] * c[k];
+        for (int l = 0; l < s; ++l) Ac[k] += A[(size_t)k * s + l] * c[l];
+      }
+      C.push_back(c2);
+      d.push_back(1.0 / 3.0);
+      C.push_back(Ac);
+      d.push_back(1.0 / 6.0);
+    }
+    const int m = (int)C.size();
+    // reference: uniform weights, except SSP(10,4) whose b is itself uniform: there
+    // alternating 0.15 / 0.05 (its projection violates the fourth-order conditions)
+    std::vector<double> u(s, 1.0 / s), res(m), G((size_t)m * m);
+    if (type == SSP_10_4)
+      for (int k = 0; k < s; ++k) u[k] = (k & 1) ? 0.05 : 0.15;
+    for (int a = 0; a < m; ++a)
+    {
+      double v = 0.0;
+      for (int k = 0; k < s; ++k) v += C[a][k] * u[k];
+      res[a] = v - d[a];
+      for (int e = 0; e < m; ++e)
+      {
+        double g = 0.0;
+        for (int k = 0; k < s; ++k) g += C[a][k] * C[e][k];
+        G[(size_t)a * m + e] = g;
+      }
+    }
+    // solve G lam = res (Gaussian elimination with partial pivoting, m <= 4)
+    std::vector<double> lam = res;
+    for (int col = 0; col < m; ++col)
+    {
+      int pr = col;
+      for (int rr = col + 1; rr < m; ++rr)
+        if (std::fabs(G[(size_t)rr * m + col]) > std::fabs(G[(size_t)pr * m + col])) pr = rr;
+      if (pr != col)
+      {
+        for (int e = 0; e < m; ++e) std::swap(G[(size_t)col * m + e], G[(size_t)pr * m + e]);
+        std::swap(lam[col], lam[pr]);
+      }
+      for (int rr = col + 1; rr < m; ++rr)
+      {
+        const double f = G[(size_t)rr * m + col] / G[(size_t)col * m + col];
+        for (int e = col; e < m; ++e) G[(size_t)rr * m + e] -= f * G[(size_t)col * m + e];
+        lam[rr] -= f * lam[col];
+      }
+    }
+    for (int col = m - 1; col >= 0; --col)
+    {
+      for (int e = col + 1; e < m; ++e) lam[col] -= G[(size_t)col * m + e] * lam[e];
+      lam[col] /= G[(size_t)col * m + col];
+    }
+    for (int k = 0; k < s; ++k)
+    {
+      double v = u[k];
+      for (int a = 0; a < m; ++a) v -= C[a][k] * lam[a];
+      bh[k] = v;
+    }
+  }
+  w.assign(s, 0.0);
+  for (int k = 0; k < s; ++k) w[k] = b[k] - bh[k];
 }
 
 static void free_device(LSRKMem* m)
@@ -683,7 +870,7 @@ static double initial_step(LSRKMem* m, const double* y0, const double* F0, doubl
   cudaFreeAsync(F1, ctx->stream);
   if (rc < 0) return -1.0;
   const double dm = d1 > d2 ? d1 : d2;
-  double h1       = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : stsm::pow(0.01 / dm, 1.0 / ORD);
+  double h1       = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : stsm::pow(0.01 / dm, 1.0 / m->ord);
   if (!(h1 > 0.0) || !(h1 < INFINITY)) h1 = h0;
   double h = (100.0 * h0 < h1) ? 100.0 * h0 : h1;
   if (h > tdist) h = tdist;
@@ -710,7 +897,7 @@ static void accept_control(LSRKMem* m, double h, double dsm)
   }
   else
   {
-    double hn  = STS_AdaptControllerEstimate(m->controller, h, dsm, m->ep1, m->ep2, m->nhist);
+    double hn  = controller_estimate(m->controller, h, dsm, m->ep1, m->ep2, m->nhist, m->ord);
     double eta = SAFETY * hn / h;
     double emx = (m->nst == 0) ? ETAMX1 : (m->after_fail ? 1.0 : GROWTH);
     if (eta > emx) eta = emx;
@@ -725,7 +912,7 @@ static void accept_control(LSRKMem* m, double h, double dsm)
 
 static void reject_control(LSRKMem* m, double h, double dsm, int nef)
 {
-  double hn  = STS_AdaptControllerEstimate(m->controller, h, dsm, m->ep1, m->ep2, m->nhist);
+  double hn  = controller_estimate(m->controller, h, dsm, m->ep1, m->ep2, m->nhist, m->ord);
   double eta = SAFETY * hn / h;
   if (eta > 1.0) eta = 1.0;
   if (nef >= SMALL_NEF && eta > ETAMXF) eta = ETAMXF;
@@ -853,6 +1040,95 @@ static int evolve_fused(LSRKMem* m, double target, int itask)
 // ---------------------------------------------------------------------------------------
 // generic evolve (user RHS through N_Vector ops)
 // ---------------------------------------------------------------------------------------
+// One SSP step attempt of size h from (t, y, F = F(t, y)) with N_Vector operations: the new
+// state into `yout`, the error estimate h sum_j w_j F_j into m->g_err. Registers: q1 = g_Y[0],
+// q2 = g_Y[1], stage derivative G = g_F. Returns the RHS status (0 ok).
+static int ssp_attempt(LSRKMem* m, double h, N_Vector y, N_Vector F, N_Vector yout)
+{
+  const int type = m->method, s = m->ssp_stages;
+  const std::vector<double>& w = m->ssp_w;
+  N_Vector q1 = m->g_Y[0], q2 = m->g_Y[1], G = m->g_F, E = m->g_err;
+  const std::vector<double>& c = m->ssp_c;
+  int j = 0;
+  // stage j: G = F(t + c_j h, q) (stage 0 reuses F), E += h w_j G; returns the derivative
+  auto stage = [&](N_Vector q) -> N_Vector {
+    N_Vector g = F;
+    if (j > 0)
+    {
+      const int rc = m->rhs(m->t + c[j] * h, q, G, m->user_data);
+      if (rc != 0) return nullptr;
+      g = G;
+    }
+    if (j == 0) N_VScale_Sts(h * w[0], g, E);
+    else N_VLinearSum_Sts(h * w[j], g, 1.0, E, E);
+    ++j;
+    return g;
+  };
+  int frc = 0;
+  auto euler = [&](double hr) { // q1 = q1 + hr F(q1)
+    N_Vector g = stage(q1);
+    if (!g) return false;
+    N_VLinearSum_Sts(hr, g, 1.0, q1, q1);
+    return true;
+  };
+  N_VScale_Sts(1.0, y, q1);
+  if (type == SSP_S_2)
+  {
+    const double hr = h / (s - 1.0);
+    for (int i = 0; i < s - 1; ++i)
+      if (!euler(hr)) return 1;
+    N_Vector g = stage(q1);
+    if (!g) return 1;
+    double cf[3]  = {1.0 / s, (s - 1.0) / s, (s - 1.0) / s * hr};
+    N_Vector X[3] = {y, q1, g};
+    N_VLinearCombination_Sts(3, cf, X, yout);
+  }
+  else if (type == SSP_S_3)
+  {
+    const int n     = (int)std::lround(std::sqrt((double)s));
+    const double hr = h / (double)(n * n - n);
+    const int e1 = (n - 1) * (n - 2) / 2, e2 = n * (n + 1) / 2;
+    for (int i = 1; i <= e1; ++i)
+      if (!euler(hr)) return 1;
+    N_VScale_Sts(1.0, q1, q2);
+    for (int i = e1 + 1; i <= e2 - 1; ++i)
+      if (!euler(hr)) return 1;
+    N_Vector g = stage(q1);
+    if (!g) return 1;
+    double cf[3]  = {(double)n / (2 * n - 1), (n - 1.0) / (2 * n - 1), (n - 1.0) / (2 * n - 1) * hr};
+    N_Vector X[3] = {q2, q1, g};
+    N_VLinearCombination_Sts(3, cf, X, q1);
+    for (int i = e2 + 1; i <= n * n; ++i)
+      if (!euler(hr)) return 1;
+    N_VScale_Sts(1.0, q1, yout);
+  }
+  else
+  {
+    N_VScale_Sts(1.0, y, q2);
+    for (int i = 1; i <= 5; ++i)
+      if (!euler(h / 6.0)) return 1;
+    {
+      double cf[2]  = {1.0 / 25.0, 9.0 / 25.0};
+      N_Vector X[2] = {q2, q1};
+      N_VLinearCombination_Sts(2, cf, X, q2);
+    }
+    {
+      double cf[2]  = {15.0, -5.0};
+      N_Vector X[2] = {q2, q1};
+      N_VLinearCombination_Sts(2, cf, X, q1);
+    }
+    for (int i = 6; i <= 9; ++i)
+      if (!euler(h / 6.0)) return 1;
+    N_Vector g = stage(q1);
+    if (!g) return 1;
+    double cf[3]  = {1.0, 3.0 / 5.0, h / 10.0};
+    N_Vector X[3] = {q2, q1, g};
+    N_VLinearCombination_Sts(3, cf, X, yout);
+  }
+  (void)frc;
+  return 0;
+}
+
 static int evolve_generic(LSRKMem* m, double target, int itask)
 {
   N_Vector y = m->g_y, F = m->g_Fn;
@@ -883,7 +1159,7 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
       break;
     }
     const long long freq = m->dom_eig_freq; // <= 0: computed once
-    if (m->steps_since_dee < 0 || (freq > 0 && m->steps_since_dee >= freq))
+    if (!m->ssp && (m->steps_since_dee < 0 || (freq > 0 && m->steps_since_dee >= freq)))
       if (dee_update(m, y, F)) return STS_ERR_FAILURE;
     if (!(m->hnext > 0.0))
     {
@@ -897,6 +1173,52 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
       double h;
       int s;
       bool clipped;
+      if (m->ssp)
+      { // fixed stage count; the step only clipped at the target
+        h       = m->hnext;
+        clipped = false;
+        if (m->t + h >= target)
+        {
+          h       = target - m->t;
+          clipped = true;
+        }
+        s = m->ssp_stages;
+        m->nst_att++;
+        const int frc = ssp_attempt(m, h, y, F, m->g_Fnew); // new state into g_Fnew (scratch)
+        m->nfe += s - 1;
+        if (frc != 0)
+        { // recoverable RHS failure: retry with h/4
+          m->ncf++;
+          if (++ncf_step > 10) return STS_RHSFUNC_FAIL;
+          m->hnext      = 0.25 * h;
+          m->after_fail = true;
+          continue;
+        }
+        N_VAbs_Sts(y, m->g_ewt);
+        N_VScale_Sts(m->rtol, m->g_ewt, m->g_ewt);
+        N_VAddConst_Sts(m->g_ewt, m->atol, m->g_ewt);
+        N_VInv_Sts(m->g_ewt, m->g_ewt);
+        const double dsm = N_VWrmsNorm_Sts(m->g_err, m->g_ewt);
+        m->stages_total += s;
+        if (s > m->stage_max) m->stage_max = s;
+        if (m->hfixed > 0.0 || dsm <= 1.0)
+        {
+          m->t = clipped ? target : m->t + h;
+          cudaMemcpyAsync(NVD(y), NVD(m->g_Fnew), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
+          if (m->rhs(m->t, y, F, m->user_data) != 0) return STS_RHSFUNC_FAIL; // F(y_{n+1}) for the next step
+          m->nfe++;
+          m->hlast = h;
+          accept_control(m, h, dsm);
+          m->nst++;
+          nsteps_call++;
+          break;
+        }
+        m->netf++;
+        nef++;
+        if (!(dsm == dsm) || nef > 20) return STS_ERR_FAILURE;
+        reject_control(m, h, dsm, nef);
+        continue;
+      }
       if (choose_step(m, target, &h, &s, &clipped)) return STS_ILL_INPUT;
       STS_LSRKStageCoeffs(m->method, s, mu.data(), nu.data(), mus.data(), ajm1.data(), cjm1.data());
       m->nst_att++;
@@ -1005,8 +1327,55 @@ extern "C" void* STS_LSRKStepCreateSTS(STS_ARKRhsFn rhs, double t0, N_Vector y0,
 extern "C" int STS_LSRKStepSetSTSMethod(void* mem, int method)
 {
   CHECK_MEM(mem);
-  if (method != STS_LSRK_RKC_2 && method != STS_LSRK_RKL_2) return STS_ILL_INPUT;
+  if (MEM(mem)->ssp || (method != STS_LSRK_RKC_2 && method != STS_LSRK_RKL_2)) return STS_ILL_INPUT;
   MEM(mem)->method = method;
+  return 0;
+}
+
+static void ssp_configure(LSRKMem* m)
+{
+  std::vector<double> A, b;
+  ssp_tableau(m->method, m->ssp_stages, A, b, m->ssp_c, m->ssp_w);
+  m->ord = (m->method == SSP_S_2) ? 2.0 : (m->method == SSP_S_3 ? 3.0 : 4.0); // embedding order + 1
+}
+
+// LSRKStepCreateSSP (diffusion_2D/main.cpp:251): SSP(s,2) with 10 stages until set otherwise
+extern "C" void* STS_LSRKStepCreateSSP(STS_ARKRhsFn rhs, double t0, N_Vector y0, STS_Context ctx)
+{
+  void* mem = STS_LSRKStepCreateSTS(rhs, t0, y0, ctx);
+  if (!mem) return nullptr;
+  LSRKMem* m    = MEM(mem);
+  m->ssp        = true;
+  m->method     = SSP_S_2;
+  m->ssp_stages = 10;
+  ssp_configure(m);
+  return mem;
+}
+
+// LSRKStepSetSSPMethod (main.cpp:289): ARKODE_LSRK_SSP_S_2 (10 stages), _S_3 (9), _10_4 (10)
+extern "C" int STS_LSRKStepSetSSPMethod(void* mem, int type)
+{
+  CHECK_MEM(mem);
+  LSRKMem* m = MEM(mem);
+  if (!m->ssp || (type != SSP_S_2 && type != SSP_S_3 && type != SSP_10_4)) return STS_ILL_INPUT;
+  m->method     = type;
+  m->ssp_stages = (type == SSP_S_3) ? 9 : 10;
+  ssp_configure(m);
+  return 0;
+}
+
+// LSRKStepSetNumSSPStages (main.cpp:291): s >= 2 (S_2), s = n^2 >= 4 (S_3), s = 10 (10_4)
+extern "C" int STS_LSRKStepSetNumSSPStages(void* mem, int s)
+{
+  CHECK_MEM(mem);
+  LSRKMem* m = MEM(mem);
+  if (!m->ssp || !ssp_stages_valid(m->method, s))
+  {
+    sts_set_error("LSRKStepSetNumSSPStages: %d stages are not valid for this SSP method", s);
+    return STS_ILL_INPUT;
+  }
+  m->ssp_stages = s;
+  ssp_configure(m);
   return 0;
 }
 extern "C" int STS_ARKodeSStolerances(void* mem, double rtol, double atol)
@@ -1476,4 +1845,20 @@ extern "C" int STS_LSRKStepSetNumDomEigEstPreprocessIters(void* mem, int iters)
   CHECK_MEM(mem);
   MEM(mem)->dee_succ_warmups = iters > 0 ? iters : 0;
   return STS_SUCCESS;
+}
+
+// host helper: the SSP method's weights b, stage times c and error weights w = b - bhat
+extern "C" int STS_LSRKSSPWeights(int type, int s, double* b, double* c, double* w)
+{
+  if ((type != SSP_S_2 && type != SSP_S_3 && type != SSP_10_4) || !ssp_stages_valid(type, s) || !b || !c || !w)
+    return STS_ILL_INPUT;
+  std::vector<double> A, bb, cc, ww;
+  ssp_tableau(type, s, A, bb, cc, ww);
+  for (int k = 0; k < s; ++k)
+  {
+    b[k] = bb[k];
+    c[k] = cc[k];
+    w[k] = ww[k];
+  }
+  return 0;
 }

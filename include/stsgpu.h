@@ -174,6 +174,9 @@ typedef int (*STS_ARKDomEigFn)(double t, N_Vector y, N_Vector fn, double* lambda
 
 #define STS_LSRK_RKC_2 0 /* ARKODE_LSRK_RKC_2 */
 #define STS_LSRK_RKL_2 1 /* ARKODE_LSRK_RKL_2 */
+#define STS_LSRK_SSP_S_2 2  /* ARKODE_LSRK_SSP_S_2 */
+#define STS_LSRK_SSP_S_3 3  /* ARKODE_LSRK_SSP_S_3 */
+#define STS_LSRK_SSP_10_4 4 /* ARKODE_LSRK_SSP_10_4 */
 #define STS_ADAPT_PID 0  /* ARK_ADAPT_PID */
 #define STS_ADAPT_PI 1   /* ARK_ADAPT_PI */
 #define STS_ADAPT_I 2    /* ARK_ADAPT_I */
@@ -193,7 +196,16 @@ typedef struct STS_Stats {
 } STS_Stats;
 
 void* STS_LSRKStepCreateSTS(STS_ARKRhsFn rhs, double t0, N_Vector y0, STS_Context ctx); /* main.cpp:257 */
-int STS_LSRKStepSetSTSMethod(void* mem, int method);                 /* main.cpp:336-338 */
+int STS_LSRKStepSetSTSMethod(void* mem, int method);
+/* LSRKStepCreateSSP / LSRKStepSetSSPMethod / LSRKStepSetNumSSPStages (diffusion_2D/main.cpp:
+ * 250-294): SSP(s,2) (s >= 2, default 10), SSP(s,3) (s = n^2 >= 4, default 9), SSP(10,4);
+ * integrated through the N_Vector ops with an embedded error estimate (first / second / third
+ * order) and the same step-size controllers */
+void* STS_LSRKStepCreateSSP(STS_ARKRhsFn rhs, double t0, N_Vector y0, STS_Context ctx);
+int STS_LSRKStepSetSSPMethod(void* arkode_mem, int type);
+int STS_LSRKStepSetNumSSPStages(void* arkode_mem, int num_stages);
+/* host helper: weights b, stage times c, error weights w = b - bhat of an SSP method */
+int STS_LSRKSSPWeights(int type, int s, double* b, double* c, double* w);                 /* main.cpp:336-338 */
 int STS_ARKodeSStolerances(void* mem, double rtol, double atol);      /* main.cpp:262 */
 int STS_ARKodeSetUserData(void* mem, void* user_data);                /* main.cpp:266 */
 int STS_LSRKStepSetDomEigFn(void* mem, STS_ARKDomEigFn fn);           /* main.cpp:352 */

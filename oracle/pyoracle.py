@@ -95,6 +95,9 @@ def lib():
         L.orc_stage_coeffs.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]
         L.orc_stages_needed.restype = C.c_int
         L.orc_stages_needed.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, _dp]
+        L.orc_ssp_weights.restype = C.c_int
+        L.orc_ssp_weights.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp]
+        L.orc_ssp_evolve.restype = C.c_int
         L.orc_pow.restype = C.c_double
         L.orc_pow.argtypes = [C.c_double, C.c_double]
         L.orc_controller.restype = C.c_double
@@ -256,14 +259,18 @@ def make_opts(method=RKC, mixed=False, controller=0, smax=200, rtol=1e-6, atol=1
 class Integrator:
     """The oracle's LSRK integrator (state persists across evolve calls)."""
 
-    def __init__(self, prob, y0, t0=0.0, **opts):
+    def __init__(self, prob, y0, t0=0.0, ssp=None, **opts):
         self.prob = prob
+        self.ssp = ssp  # (type, stages) for the SSP methods
         self.opts = make_opts(**opts)
         self.st = State()
         lib().orc_state_init(C.byref(self.st), t0)
         self.y = np.array(y0, dtype=np.float64)
 
     def evolve(self, tout):
+        if self.ssp is not None:
+            return lib().orc_ssp_evolve(self.prob.p, C.byref(self.opts), self.ssp[0], self.ssp[1],
+                                        C.byref(self.st), C.c_double(tout), dptr(self.y))
         rc = lib().orc_lsrk_evolve(self.prob.p, C.byref(self.opts), C.byref(self.st), tout,
                                    dptr(self.y))
         return rc
@@ -279,3 +286,10 @@ class Integrator:
             lib().orc_state_free(C.byref(self.st))
         except Exception:
             pass
+
+
+def ssp_weights(type_, s):
+    b, c, w = np.empty(s), np.empty(s), np.empty(s)
+    if lib().orc_ssp_weights(type_, s, dptr(b), dptr(c), dptr(w)) != 0:
+        raise ValueError("invalid SSP method / stage count")
+    return b, c, w

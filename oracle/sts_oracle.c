@@ -690,8 +690,18 @@ static double orc_exp(double y)
 
 double orc_pow(double x, double y) { return orc_exp(y * orc_log(x)); }
 
+static double controller_ord(int controller, double h, double dsm, double ep1, double ep2, long nhist, double ORDV);
+
 double orc_controller(int controller, double h, double dsm, double ep1, double ep2, long nhist)
 {
+  return controller_ord(controller, h, dsm, ep1, ep2, nhist, ORD);
+}
+
+/* the controllers for an error estimate of order ORDV (3 for the STS embedding) */
+static double controller_ord(int controller, double h, double dsm, double ep1, double ep2, long nhist, double ORDV)
+{
+#undef ORD
+#define ORD ORDV
   double e1 = BIAS * dsm;
   if (e1 < TINYE) e1 = TINYE;
   double e2 = BIAS * ep1;
@@ -710,6 +720,8 @@ double orc_controller(int controller, double h, double dsm, double ep1, double e
     return h * orc_pow(e1, -0.8 / ORD) * orc_pow(e2, 0.31 / ORD);
   }
   return h * orc_pow(e1, -1.0 / ORD);
+#undef ORD
+#define ORD 3.0
 }
 
 #define SAFETY 0.96
@@ -893,8 +905,16 @@ static double wrms_diff_ewt(const orc_opts* o, const double* a, const double* b,
  * order ORD; the explicit-Euler probe step is capped at 1/rho so that it stays stable, a
  * non-finite second-derivative estimate falls back to the probe step, and the result is
  * capped at tdist. */
+static double initial_step_ord(const orc_prob* p, const orc_opts* o, double t0, const double* y0,
+                               const double* F0, double tdist, double rho, long* nfe, double ordv);
 static double initial_step(const orc_prob* p, const orc_opts* o, double t0, const double* y0,
                            const double* F0, double tdist, double rho, long* nfe)
+{
+  return initial_step_ord(p, o, t0, y0, F0, tdist, rho, nfe, ORD);
+}
+
+static double initial_step_ord(const orc_prob* p, const orc_opts* o, double t0, const double* y0,
+                               const double* F0, double tdist, double rho, long* nfe, double ordv)
 {
   long n = (long)p->nx * p->ny;
   double d0 = wrms_ewt(o, y0, y0, n);
@@ -909,7 +929,7 @@ static double initial_step(const orc_prob* p, const orc_opts* o, double t0, cons
   (*nfe)++;
   double d2  = wrms_diff_ewt(o, F1, F0, y0, n) / h0;
   double dm  = d1 > d2 ? d1 : d2;
-  double h1  = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : orc_pow(0.01 / dm, 1.0 / ORD);
+  double h1  = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : orc_pow(0.01 / dm, 1.0 / ordv);
   if (!(h1 > 0.0) || !(h1 < INFINITY)) h1 = h0;
   double h   = (100.0 * h0 < h1) ? 100.0 * h0 : h1;
   if (h > tdist) h = tdist;
@@ -1271,4 +1291,401 @@ int orc_sdirk2(const orc_prob* p, double t0, double h, int nsteps, double tol, i
   free(d);
   free(Y1);
   return 0;
+}
+
+/* ------------------------------------------------------------------------------------
+ * SSP methods of LSRKStepCreateSSP (diffusion_2D/main.cpp:250-294), restated from Ketcheson
+ * (SIAM J. Sci. Comput. 30, 2008) with this project's embedded estimates, in the exact
+ * operation sequence of the product's generic path (N_Vector ops: LinearSum z = fma(a, x, b y),
+ * Scale z = c x, LinearCombination acc = c0 x0 then fma(c_k, x_k, acc)).
+ * ----------------------------------------------------------------------------------*/
+static int ssp_valid(int type, int s)
+{
+  if (type == 2) return s >= 2 && s <= 1024;
+  if (type == 3)
+  {
+    int n = (int)lround(sqrt((double)s));
+    return n >= 2 && n * n == s && s <= 1024;
+  }
+  return type == 4 && s == 10;
+}
+
+/* b, c and the error weights w = b - bhat of the SSP method (as the product computes them) */
+int orc_ssp_weights(int type, int s, double* b, double* c, double* w)
+{
+  if (!ssp_valid(type, s)) return -1;
+  /* registers: y coefficient + multiples of h F_j */
+  double* q1 = (double*)calloc(s, sizeof(double));
+  double* q2 = (double*)calloc(s, sizeof(double));
+  double* fin = (double*)calloc(s, sizeof(double));
+  double* A = (type == 4) ? (double*)calloc((size_t)s * s, sizeof(double)) : NULL;
+  double q1y = 1.0, q2y = 1.0, finy = 1.0;
+  int j = 0;
+#define STAGE(q)                                                                                        \
+  do                                                                                                    \
+  {                                                                                                     \
+    double cj = 0.0;                                                                                    \
+    for (int k = 0; k < s; ++k)                                                                         \
+    {                                                                                                   \
+      if (A) A[(size_t)j * s + k] = (q)[k];                                                             \
+      cj += (q)[k];                                                                                     \
+    }                                                                                                   \
+    c[j] = cj;                                                                                          \
+    ++j;                                                                                                \
+  } while (0)
+  if (type == 2)
+  {
+    double r = s - 1.0;
+    for (int i = 0; i < s - 1; ++i)
+    {
+      STAGE(q1);
+      q1[j - 1] += 1.0 / r;
+    }
+    STAGE(q1);
+    q1[j - 1] += 1.0 / r; /* t = q1 + (1/r) e_{s-1} (q1 is not used again) */
+    for (int k = 0; k < s; ++k) fin[k] = (1.0 / s) * 0.0 + ((s - 1.0) / s) * q1[k];
+    finy = (1.0 / s) * 1.0 + ((s - 1.0) / s) * q1y;
+  }
+  else if (type == 3)
+  {
+    int n = (int)lround(sqrt((double)s));
+    double r = (double)(n * n - n);
+    int e1 = (n - 1) * (n - 2) / 2, e2 = n * (n + 1) / 2;
+    for (int i = 1; i <= e1; ++i)
+    {
+      STAGE(q1);
+      q1[j - 1] += 1.0 / r;
+    }
+    memcpy(q2, q1, s * sizeof(double));
+    q2y = q1y;
+    for (int i = e1 + 1; i <= e2 - 1; ++i)
+    {
+      STAGE(q1);
+      q1[j - 1] += 1.0 / r;
+    }
+    STAGE(q1);
+    q1[j - 1] += 1.0 / r;
+    double a = (double)n / (2 * n - 1), bb = (n - 1.0) / (2 * n - 1);
+    for (int k = 0; k < s; ++k) q1[k] = a * q2[k] + bb * q1[k];
+    q1y = a * q2y + bb * q1y;
+    for (int i = e2 + 1; i <= n * n; ++i)
+    {
+      STAGE(q1);
+      q1[j - 1] += 1.0 / r;
+    }
+    memcpy(fin, q1, s * sizeof(double));
+    finy = q1y;
+  }
+  else
+  {
+    for (int i = 1; i <= 5; ++i)
+    {
+      STAGE(q1);
+      q1[j - 1] += 1.0 / 6.0;
+    }
+    for (int k = 0; k < s; ++k) q2[k] = (1.0 / 25.0) * q2[k] + (9.0 / 25.0) * q1[k];
+    q2y = (1.0 / 25.0) * q2y + (9.0 / 25.0) * q1y;
+    for (int k = 0; k < s; ++k) q1[k] = 15.0 * q2[k] + -5.0 * q1[k];
+    q1y = 15.0 * q2y + -5.0 * q1y;
+    for (int i = 6; i <= 9; ++i)
+    {
+      STAGE(q1);
+      q1[j - 1] += 1.0 / 6.0;
+    }
+    STAGE(q1);
+    for (int k = 0; k < s; ++k) fin[k] = 1.0 * q2[k] + (3.0 / 5.0) * q1[k];
+    fin[j - 1] += 1.0 / 10.0;
+    finy = 1.0 * q2y + (3.0 / 5.0) * q1y;
+  }
+#undef STAGE
+  (void)finy;
+  memcpy(b, fin, s * sizeof(double));
+  double* bh = (double*)calloc(s, sizeof(double));
+  if (type == 2)
+    for (int k = 0; k < s; ++k) bh[k] = (k < s - 1) ? 1.0 / (s - 1.0) : 0.0;
+  else
+  {
+    int m = (type == 4) ? 4 : 2;
+    double* Cm = (double*)calloc((size_t)m * s, sizeof(double));
+    double d[4] = {1.0, 0.5, 1.0 / 3.0, 1.0 / 6.0};
+    for (int k = 0; k < s; ++k)
+    {
+      Cm[k]     = 1.0;
+      Cm[s + k] = c[k];
+      if (m == 4)
+      {
+        Cm[2 * s + k] = c[k] * c[k];
+        double ac     = 0.0;
+        for (int l = 0; l < s; ++l) ac += A[(size_t)k * s + l] * c[l];
+        Cm[3 * s + k] = ac;
+      }
+    }
+    double G[16], lam[4];
+    /* reference weights: uniform; SSP(10,4) (uniform b) alternating 0.15 / 0.05 */
+#define UREF(k) ((type == 4) ? (((k) & 1) ? 0.05 : 0.15) : 1.0 / s)
+    for (int a = 0; a < m; ++a)
+    {
+      double v = 0.0;
+      for (int k = 0; k < s; ++k) v += Cm[a * s + k] * UREF(k);
+      lam[a] = v - d[a];
+      for (int e = 0; e < m; ++e)
+      {
+        double g = 0.0;
+        for (int k = 0; k < s; ++k) g += Cm[a * s + k] * Cm[e * s + k];
+        G[a * m + e] = g;
+      }
+    }
+    for (int col = 0; col < m; ++col)
+    {
+      int pr = col;
+      for (int rr = col + 1; rr < m; ++rr)
+        if (fabs(G[rr * m + col]) > fabs(G[pr * m + col])) pr = rr;
+      if (pr != col)
+      {
+        for (int e = 0; e < m; ++e)
+        {
+          double t = G[col * m + e];
+          G[col * m + e] = G[pr * m + e];
+          G[pr * m + e]  = t;
+        }
+        double t = lam[col];
+        lam[col] = lam[pr];
+        lam[pr]  = t;
+      }
+      for (int rr = col + 1; rr < m; ++rr)
+      {
+        double f = G[rr * m + col] / G[col * m + col];
+        for (int e = col; e < m; ++e) G[rr * m + e] -= f * G[col * m + e];
+        lam[rr] -= f * lam[col];
+      }
+    }
+    for (int col = m - 1; col >= 0; --col)
+    {
+      for (int e = col + 1; e < m; ++e) lam[col] -= G[col * m + e] * lam[e];
+      lam[col] /= G[col * m + col];
+    }
+    for (int k = 0; k < s; ++k)
+    {
+      double v = UREF(k);
+      for (int a = 0; a < m; ++a) v -= Cm[a * s + k] * lam[a];
+      bh[k] = v;
+    }
+#undef UREF
+    free(Cm);
+  }
+  for (int k = 0; k < s; ++k) w[k] = b[k] - bh[k];
+  free(bh);
+  free(q1);
+  free(q2);
+  free(fin);
+  free(A);
+  return 0;
+}
+
+/* N_Vector operation restatements (the product's arithmetic) */
+static void v_linsum(long n, double a, const double* x, double b, const double* y, double* z)
+{
+  for (long k = 0; k < n; ++k) z[k] = fma(a, x[k], b * y[k]);
+}
+static void v_scale(long n, double c, const double* x, double* z)
+{
+  for (long k = 0; k < n; ++k) z[k] = c * x[k];
+}
+static void v_lincomb(long n, int nv, const double* cf, const double** X, double* z)
+{
+  for (long k = 0; k < n; ++k)
+  {
+    double acc = cf[0] * X[0][k];
+    for (int v = 1; v < nv; ++v) acc = fma(cf[v], X[v][k], acc);
+    z[k] = acc;
+  }
+}
+
+/* Adaptive SSP integration (type 2 = SSP(s,2), 3 = SSP(s,3), 4 = SSP(10,4)); state in st as
+ * for orc_lsrk_evolve. The controller order is the embedding order + 1. */
+int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_state* st, double tout, double* y)
+{
+  if (!ssp_valid(type, s)) return -4;
+  long n    = (long)p->nx * p->ny;
+  long maxs = o->maxsteps > 0 ? o->maxsteps : 500;
+  double ordv = (type == 2) ? 2.0 : (type == 3 ? 3.0 : 4.0);
+  double *b = (double*)malloc(s * sizeof(double)), *c = (double*)malloc(s * sizeof(double)),
+         *w = (double*)malloc(s * sizeof(double));
+  orc_ssp_weights(type, s, b, c, w);
+  double *q1 = (double*)malloc(n * sizeof(double)), *q2 = (double*)malloc(n * sizeof(double)),
+         *G = (double*)malloc(n * sizeof(double)), *E = (double*)malloc(n * sizeof(double)),
+         *ynew = (double*)malloc(n * sizeof(double));
+  int ret = 0;
+  if (!st->initialized)
+  {
+    st->F = (double*)malloc(n * sizeof(double));
+    st->Ff = NULL;
+    orc_rhs(p, st->t, y, st->F);
+    st->nfe++;
+    st->hnext       = (o->hfixed > 0.0) ? o->hfixed : 0.0;
+    st->initialized = 1;
+  }
+  long nsteps_call = 0;
+  while (st->t < tout)
+  {
+    if (nsteps_call >= maxs)
+    {
+      ret = -1;
+      break;
+    }
+    if (!(st->hnext > 0.0)) st->hnext = initial_step_ord(p, o, st->t, y, st->F, tout - st->t, 0.0, &st->nfe, ordv);
+    int nef = 0;
+    for (;;)
+    {
+      double h = st->hnext;
+      int clipped = 0;
+      if (st->t + h >= tout)
+      {
+        h       = tout - st->t;
+        clipped = 1;
+      }
+      st->nst_attempts++;
+      int j = 0;
+      /* stage: derivative of register q (stage 0 reuses F), E += h w_j G */
+#define SSP_STAGE(q, g)                                                                                 \
+  do                                                                                                    \
+  {                                                                                                     \
+    if (j == 0) g = st->F;                                                                              \
+    else                                                                                                \
+    {                                                                                                   \
+      orc_rhs(p, st->t + c[j] * h, q, G);                                                               \
+      g = G;                                                                                            \
+    }                                                                                                   \
+    if (j == 0) v_scale(n, h * w[0], g, E);                                                             \
+    else v_linsum(n, h * w[j], g, 1.0, E, E);                                                           \
+    ++j;                                                                                                \
+  } while (0)
+      const double* g;
+      v_scale(n, 1.0, y, q1);
+      if (type == 2)
+      {
+        double hr = h / (s - 1.0);
+        for (int i = 0; i < s - 1; ++i)
+        {
+          SSP_STAGE(q1, g);
+          v_linsum(n, hr, g, 1.0, q1, q1);
+        }
+        SSP_STAGE(q1, g);
+        double cf[3] = {1.0 / s, (s - 1.0) / s, (s - 1.0) / s * hr};
+        const double* X[3] = {y, q1, g};
+        v_lincomb(n, 3, cf, X, ynew);
+      }
+      else if (type == 3)
+      {
+        int nn = (int)lround(sqrt((double)s));
+        double hr = h / (double)(nn * nn - nn);
+        int e1 = (nn - 1) * (nn - 2) / 2, e2 = nn * (nn + 1) / 2;
+        for (int i = 1; i <= e1; ++i)
+        {
+          SSP_STAGE(q1, g);
+          v_linsum(n, hr, g, 1.0, q1, q1);
+        }
+        v_scale(n, 1.0, q1, q2);
+        for (int i = e1 + 1; i <= e2 - 1; ++i)
+        {
+          SSP_STAGE(q1, g);
+          v_linsum(n, hr, g, 1.0, q1, q1);
+        }
+        SSP_STAGE(q1, g);
+        {
+          double cf[3] = {(double)nn / (2 * nn - 1), (nn - 1.0) / (2 * nn - 1), (nn - 1.0) / (2 * nn - 1) * hr};
+          const double* X[3] = {q2, q1, g};
+          v_lincomb(n, 3, cf, X, q1);
+        }
+        for (int i = e2 + 1; i <= nn * nn; ++i)
+        {
+          SSP_STAGE(q1, g);
+          v_linsum(n, hr, g, 1.0, q1, q1);
+        }
+        v_scale(n, 1.0, q1, ynew);
+      }
+      else
+      {
+        v_scale(n, 1.0, y, q2);
+        for (int i = 1; i <= 5; ++i)
+        {
+          SSP_STAGE(q1, g);
+          v_linsum(n, h / 6.0, g, 1.0, q1, q1);
+        }
+        {
+          double cf[2] = {1.0 / 25.0, 9.0 / 25.0};
+          const double* X[2] = {q2, q1};
+          v_lincomb(n, 2, cf, X, q2);
+        }
+        {
+          double cf[2] = {15.0, -5.0};
+          const double* X[2] = {q2, q1};
+          v_lincomb(n, 2, cf, X, q1);
+        }
+        for (int i = 6; i <= 9; ++i)
+        {
+          SSP_STAGE(q1, g);
+          v_linsum(n, h / 6.0, g, 1.0, q1, q1);
+        }
+        SSP_STAGE(q1, g);
+        double cf[3] = {1.0, 3.0 / 5.0, h / 10.0};
+        const double* X[3] = {q2, q1, g};
+        v_lincomb(n, 3, cf, X, ynew);
+      }
+#undef SSP_STAGE
+      st->nfe += s - 1;
+      double dsm = wrms_ewt(o, E, y, n);
+      st->stages_total += s;
+      if (s > st->stage_max) st->stage_max = s;
+      if (o->hfixed > 0.0 || dsm <= 1.0)
+      {
+        st->t = clipped ? tout : st->t + h;
+        memcpy(y, ynew, n * sizeof(double));
+        orc_rhs(p, st->t, y, st->F);
+        st->nfe++;
+        st->hlast = h;
+        if (o->hfixed > 0.0) st->hnext = o->hfixed;
+        else
+        {
+          double hn  = controller_ord(o->controller, h, dsm, st->ep1, st->ep2, st->nhist, ordv);
+          double eta = SAFETY * hn / h;
+          double emx = (st->nst == 0) ? ETAMX1 : (st->after_fail ? 1.0 : GROWTH);
+          if (eta > emx) eta = emx;
+          if (eta >= LBOUND && eta <= UBOUND) eta = 1.0;
+          st->hnext = h * eta;
+          st->ep2   = st->ep1;
+          st->ep1   = dsm;
+          st->nhist++;
+        }
+        st->after_fail = 0;
+        st->nst++;
+        nsteps_call++;
+        break;
+      }
+      st->netf++;
+      nef++;
+      if (!(dsm == dsm) || nef > 20)
+      {
+        ret = -3;
+        goto done;
+      }
+      double hn  = controller_ord(o->controller, h, dsm, st->ep1, st->ep2, st->nhist, ordv);
+      double eta = SAFETY * hn / h;
+      if (eta > 1.0) eta = 1.0;
+      if (nef >= SMALL_NEF && eta > ETAMXF) eta = ETAMXF;
+      if (eta < ETAMIN) eta = ETAMIN;
+      st->hnext      = h * eta;
+      st->after_fail = 1;
+    }
+  }
+done:
+  free(b);
+  free(c);
+  free(w);
+  free(q1);
+  free(q2);
+  free(G);
+  free(E);
+  free(ynew);
+  return ret;
 }

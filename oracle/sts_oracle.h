@@ -82,6 +82,9 @@ int orc_stage_coeffs(int method, int s, double* mu, double* nu, double* mus, dou
                      double* cjm1);
 int orc_stages_needed(int method, double h, double rho, int smax, double* hmax);
 double orc_pow(double x, double y); /* deterministic pow of the controllers */
+/* SSP methods (type 2 = SSP(s,2), 3 = SSP(s,3), 4 = SSP(10,4)) */
+int orc_ssp_weights(int type, int s, double* b, double* c, double* w);
+int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_state* st, double tout, double* y);
 double orc_controller(int controller, double h, double dsm, double ep1, double ep2, long nhist);
 
 void orc_state_init(orc_state* st, double t0);

@@ -285,3 +285,22 @@ def test_deterministic_pow_accuracy(oracle):
         # the rounding of y log x is amplified by |y log x| in exp: a few ulp times (1 + |y log x|)
         bound = 4.5e-16 * (1.0 + np.abs(y * np.log(xs)))
         assert np.all(np.abs(got - want) / want < bound)
+
+
+@pytest.mark.parametrize("type_,s,order", [(2, 2, 2), (2, 10, 2), (2, 37, 2), (3, 4, 3), (3, 9, 3),
+                                           (3, 16, 3), (3, 25, 3), (4, 10, 4)])
+def test_ssp_weights_order_and_parity(oracle, stslib, type_, s, order):
+    """SSP(s,2) / SSP(n^2,3) / SSP(10,4) (Ketcheson 2008) as the integrator builds them: the
+    product's host weights equal the oracle's bit for bit; the method meets its order
+    conditions on b, the embedded weights bhat = b - w exactly one order less."""
+    b, c, w = stslib.ssp_weights(type_, s)
+    ob, oc, ow = oracle.ssp_weights(type_, s)
+    assert np.array_equal(b, ob) and np.array_equal(c, oc) and np.array_equal(w, ow)
+    bh = b - w
+    # quadrature conditions sum b c^(k-1) = 1/k (sufficient to tell the orders apart here)
+    for k in range(1, order + 1):
+        assert abs(np.dot(b, c ** (k - 1)) - 1.0 / k) < 1e-12, ("main", k)
+    for k in range(1, order):
+        assert abs(np.dot(bh, c ** (k - 1)) - 1.0 / k) < 1e-12, ("embedded", k)
+    assert abs(np.dot(bh, c ** (order - 1)) - 1.0 / order) > 1e-6  # embedding exactly one order less
+    assert np.abs(w).max() > 1e-6
