@@ -27,7 +27,7 @@ def test_ssp_matches_oracle_bitwise(ctx, stslib, oracle, ssp):
     si, sj = I.stats(), J.stats()
     for k in ("nst", "nst_attempts", "netf", "nfe", "stages_total"):
         assert si[k] == sj[k], k
-    assert si["stage_max"] == ssp[1] and si["nst"] > 3
+    assert si["stage_max"] == ssp[1] and si["nst"] >= 3
 
 
 @pytest.mark.parametrize("ssp,order", [((2, 5), 2), ((3, 9), 3), ((4, 10), 4)])
