@@ -27,7 +27,7 @@ __all__ = ["lib", "Context", "NVector", "Problem", "LSRKStep", "PCGSolver", "imp
 
 RKC, RKL = 0, 1
 SSP_S_2, SSP_S_3, SSP_10_4 = 2, 3, 4
-PID, PI, I = 0, 1, 2
+PID, PI, I, EXP_GUS, IMP_GUS, IMEX_GUS = 0, 1, 2, 3, 4, 5
 MANUFACTURED, UNFORCED, PERIODIC = 0, 1, 2
 NORMAL, ONE_STEP = 1, 2
 TOO_MUCH_WORK = -1
@@ -138,7 +138,7 @@ SIGNATURES = [
     ("STS_LSRKStageCoeffs", C.c_int, [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]),
     ("STS_LSRKStagesNeeded", C.c_int, [C.c_int, C.c_double, C.c_double, C.c_int, _dp]),
     ("STS_AdaptControllerEstimate", C.c_double, [C.c_int, C.c_double, C.c_double, C.c_double,
-                                                 C.c_double, _ll]),
+                                                 C.c_double, C.c_double, _ll]),
     ("STS_ManufacturedTables", C.c_int, [_ll, C.c_double, _dp, _dp]),
     ("STS_ExactSumHost", C.c_double, [_dp, _ll]),
     ("STS_SUNLinSol_PCG", _vp, [_NV, C.c_int, C.c_int, _vp]),

@@ -69,7 +69,7 @@ static void help()
           "  --inhomogeneous : use spatially-varying diffusion coefficients\n"
           "  --tf <time>     : final time\n"
           "\nIntegrator command line options:\n"
-          "  --integrator <dirk|rkc|rkl> --rtol --atol --fixedstep --controller <0|1|2>\n"
+          "  --integrator <dirk|rkc|rkl> --rtol --atol --fixedstep --controller <0..5: PID PI I ExpGus ImpGus ImExGus>\n"
           "  --maxsteps --onestep <n> --error --internaleig --smax <stages> --mixed --nographs\n"
           "\nDIRK solver command line options:\n"
           "  --order --nonlinear --ls <cg> --lsinfo --liniters --epslin --noprec --msbp\n"
@@ -170,6 +170,11 @@ int main(int argc, char** argv)
   if (impl && (kind == STS_PROBLEM_PERIODIC || !(o.hfixed > 0.0)))
   {
     cerr << "ERROR: dirk runs fixed steps (--fixedstep) on the Dirichlet problems" << endl;
+    return 1;
+  }
+  if (o.controller < STS_ADAPT_PID || o.controller > STS_ADAPT_IMEX_GUS)
+  {
+    cerr << "ERROR: illegal controller (0 PID, 1 PI, 2 I, 3 ExpGus, 4 ImpGus, 5 ImExGus)" << endl;
     return 1;
   }
   STS_Context ctx;

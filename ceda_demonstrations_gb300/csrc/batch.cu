@@ -89,7 +89,9 @@ namespace {
 constexpr double B_ORD = 3.0, B_BIAS = 1.5, B_TINY = 1.0e-10;
 constexpr double B_SAFETY = 0.96, B_GROWTH = 20.0, B_ETAMX1 = 10000.0, B_ETAMXF = 0.3, B_ETAMIN = 0.1;
 
-__device__ double d_controller(int controller, double h, double dsm, double ep1, double ep2, long long nhist)
+// hp: previous accepted step size (implicit Gustafsson controller); the host integrator's rules
+__device__ double d_controller(int controller, double h, double dsm, double ep1, double ep2, double hp,
+                               long long nhist)
 {
   double e1 = fmax(B_BIAS * dsm, B_TINY), e2 = fmax(B_BIAS * ep1, B_TINY), e3 = fmax(B_BIAS * ep2, B_TINY);
   if (controller == 0)
@@ -102,6 +104,15 @@ __device__ double d_controller(int controller, double h, double dsm, double ep1,
   {
     if (nhist < 1) return h * stsm::pow(e1, -0.8 / B_ORD);
     return h * stsm::pow(e1, -0.8 / B_ORD) * stsm::pow(e2, 0.31 / B_ORD);
+  }
+  if (controller >= 3 && controller <= 5 && nhist >= 1 && hp > 0.0)
+  { // Gustafsson: explicit (3), implicit (4), the smaller of the two (5)
+    const double r    = e1 / e2;
+    const double hexp = h * stsm::pow(e1, -0.367 / B_ORD) * stsm::pow(r, -0.268 / B_ORD);
+    if (controller == 3) return hexp;
+    const double himp = h * (h / hp) * stsm::pow(e1, -0.98 / B_ORD) * stsm::pow(r, -0.95 / B_ORD);
+    if (controller == 4) return himp;
+    return hexp < himp ? hexp : himp;
   }
   return h * stsm::pow(e1, -1.0 / B_ORD);
 }
@@ -416,8 +427,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
           const int tf_ = iF;
           iF           = iFn;
           iFn          = tf_;
+          const double hprev = hlast;
           hlast        = h;
-          double hn    = d_controller(prm.controller, h, dsm, ep1, ep2, nhist);
+          double hn    = d_controller(prm.controller, h, dsm, ep1, ep2, hprev, nhist);
           double eta   = B_SAFETY * hn / h;
           const double emx = (nst == 0) ? B_ETAMX1 : (after_fail ? 1.0 : B_GROWTH);
           if (eta > emx) eta = emx;
@@ -437,7 +449,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
           status = -3;
           break;
         }
-        double hn  = d_controller(prm.controller, h, dsm, ep1, ep2, nhist);
+        double hn  = d_controller(prm.controller, h, dsm, ep1, ep2, hlast, nhist);
         double eta = B_SAFETY * hn / h;
         if (eta > 1.0) eta = 1.0;
         if (nef >= 2 && eta > B_ETAMXF) eta = B_ETAMXF;
@@ -703,6 +715,8 @@ extern "C" int STS_BatchEvolve(STS_Batch b, double tf, int method, double rtol, 
                                long long maxsteps)
 {
   if (!b || !(tf > 0.0) || smax < 2 || smax > 10000) return STS_ILL_INPUT;
+  if (controller < STS_ADAPT_PID || controller > STS_ADAPT_IMEX_GUS) return STS_ILL_INPUT;
+  if (method != STS_LSRK_RKC_2 && method != STS_LSRK_RKL_2) return STS_ILL_INPUT;
   ctx_activate(b->ctx);
   BatchParams prm;
   prm.tf         = tf;

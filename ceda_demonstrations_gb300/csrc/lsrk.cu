@@ -139,17 +139,22 @@ extern "C" int STS_LSRKStagesNeeded(int method, double h, double rho, int smax, 
 }
 
 static constexpr double ORD = 3.0, BIAS = 1.5, TINYE = 1.0e-10;
-static double controller_estimate(int controller, double h, double dsm, double ep1, double ep2, long long nhist,
-                                  double ORD);
+static double controller_estimate(int controller, double h, double dsm, double ep1, double ep2, double hp,
+                                  long long nhist, double ORD);
 extern "C" double STS_AdaptControllerEstimate(int controller, double h, double dsm, double ep1, double ep2,
-                                              long long nhist)
+                                              double hp, long long nhist)
 {
-  return controller_estimate(controller, h, dsm, ep1, ep2, nhist, ORD);
+  return controller_estimate(controller, h, dsm, ep1, ep2, hp, nhist, ORD);
 }
 
-// the controllers for an error estimate of order ORD (3 for the STS methods' embedding)
-static double controller_estimate(int controller, double h, double dsm, double ep1, double ep2, long long nhist,
-                                  double ORD)
+// The controllers of diffusion_2D/main.cpp:366-376 for an error estimate of order ORD (3 for
+// the STS methods' embedding); e = bias * dsm floored at 1e-10, hp = previous accepted step.
+//   PID / PI / I: Soderlind-form exponents, leading terms only until enough history exists
+//   ExpGus  (Gustafsson 1991): h e_n^(-k1/p) (e_n/e_{n-1})^(-k2/p), k1 0.367, k2 0.268
+//   ImpGus  (Gustafsson 1994): h (h/h_{n-1}) e_n^(-k1/p) (e_n/e_{n-1})^(-k2/p), k1 0.98, k2 0.95
+//   ImExGus: the smaller of the two; all three use h e_n^(-1/p) on the first step.
+static double controller_estimate(int controller, double h, double dsm, double ep1, double ep2, double hp,
+                                  long long nhist, double ORD)
 {
   double e1 = BIAS * dsm;
   if (e1 < TINYE) e1 = TINYE;
@@ -167,6 +172,15 @@ static double controller_estimate(int controller, double h, double dsm, double e
   {
     if (nhist < 1) return h * stsm::pow(e1, -0.8 / ORD);
     return h * stsm::pow(e1, -0.8 / ORD) * stsm::pow(e2, 0.31 / ORD);
+  }
+  if (controller >= STS_ADAPT_EXP_GUS && controller <= STS_ADAPT_IMEX_GUS && nhist >= 1 && hp > 0.0)
+  {
+    const double r    = e1 / e2;
+    const double hexp = h * stsm::pow(e1, -0.367 / ORD) * stsm::pow(r, -0.268 / ORD);
+    if (controller == STS_ADAPT_EXP_GUS) return hexp;
+    const double himp = h * (h / hp) * stsm::pow(e1, -0.98 / ORD) * stsm::pow(r, -0.95 / ORD);
+    if (controller == STS_ADAPT_IMP_GUS) return himp;
+    return hexp < himp ? hexp : himp;
   }
   return h * stsm::pow(e1, -1.0 / ORD);
 }
@@ -891,13 +905,15 @@ double sts_wrms_ewt(STS_Context ctx, const double* a, const double* b, const dou
 // controller update after an accepted step of size h with error dsm
 static void accept_control(LSRKMem* m, double h, double dsm)
 {
+  const double hprev = m->hlast; // previous accepted step (implicit Gustafsson controller)
+  m->hlast           = h;
   if (m->hfixed > 0.0)
   {
     m->hnext = m->hfixed;
   }
   else
   {
-    double hn  = controller_estimate(m->controller, h, dsm, m->ep1, m->ep2, m->nhist, m->ord);
+    double hn  = controller_estimate(m->controller, h, dsm, m->ep1, m->ep2, hprev, m->nhist, m->ord);
     double eta = SAFETY * hn / h;
     double emx = (m->nst == 0) ? ETAMX1 : (m->after_fail ? 1.0 : GROWTH);
     if (eta > emx) eta = emx;
@@ -912,7 +928,7 @@ static void accept_control(LSRKMem* m, double h, double dsm)
 
 static void reject_control(LSRKMem* m, double h, double dsm, int nef)
 {
-  double hn  = controller_estimate(m->controller, h, dsm, m->ep1, m->ep2, m->nhist, m->ord);
+  double hn  = controller_estimate(m->controller, h, dsm, m->ep1, m->ep2, m->hlast, m->nhist, m->ord);
   double eta = SAFETY * hn / h;
   if (eta > 1.0) eta = 1.0;
   if (nef >= SMALL_NEF && eta > ETAMXF) eta = ETAMXF;
@@ -1020,7 +1036,6 @@ static int evolve_fused(LSRKMem* m, double target, int itask)
       {
         m->t     = clipped ? target : m->t + h;
         m->par   = 1 - m->par;
-        m->hlast = h;
         accept_control(m, h, dsm);
         m->nst++;
         m->steps_since_dee++;
@@ -1207,7 +1222,6 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
           cudaMemcpyAsync(NVD(y), NVD(m->g_Fnew), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
           if (m->rhs(m->t, y, F, m->user_data) != 0) return STS_RHSFUNC_FAIL; // F(y_{n+1}) for the next step
           m->nfe++;
-          m->hlast = h;
           accept_control(m, h, dsm);
           m->nst++;
           nsteps_call++;
@@ -1268,7 +1282,6 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
         m->t = clipped ? target : m->t + h;
         cudaMemcpyAsync(NVD(y), NVD(yj), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
         cudaMemcpyAsync(NVD(F), NVD(m->g_Fnew), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
-        m->hlast = h;
         accept_control(m, h, dsm);
         m->nst++;
         m->steps_since_dee++;
@@ -1430,7 +1443,7 @@ extern "C" int STS_LSRKStepSetDomEigSafetyFactor(void* mem, double safety)
 extern "C" int STS_ARKodeSetAdaptController(void* mem, int controller)
 {
   CHECK_MEM(mem);
-  if (controller < 0 || controller > 2) return STS_ILL_INPUT;
+  if (controller < STS_ADAPT_PID || controller > STS_ADAPT_IMEX_GUS) return STS_ILL_INPUT;
   MEM(mem)->controller = controller;
   return 0;
 }

@@ -180,6 +180,9 @@ typedef int (*STS_ARKDomEigFn)(double t, N_Vector y, N_Vector fn, double* lambda
 #define STS_ADAPT_PID 0  /* ARK_ADAPT_PID */
 #define STS_ADAPT_PI 1   /* ARK_ADAPT_PI */
 #define STS_ADAPT_I 2    /* ARK_ADAPT_I */
+#define STS_ADAPT_EXP_GUS 3  /* ARK_ADAPT_EXP_GUS */
+#define STS_ADAPT_IMP_GUS 4  /* ARK_ADAPT_IMP_GUS */
+#define STS_ADAPT_IMEX_GUS 5 /* ARK_ADAPT_IMEX_GUS */
 #define STS_NORMAL 1     /* ARK_NORMAL */
 #define STS_ONE_STEP 2   /* ARK_ONE_STEP */
 #define STS_SUCCESS 0
@@ -259,7 +262,7 @@ int STS_LSRKStageCoeffs(int method, int s, double* mu, double* nu, double* mus, 
                         double* cjm1);
 int STS_LSRKStagesNeeded(int method, double h, double rho, int smax, double* hmax);
 double STS_AdaptControllerEstimate(int controller, double h, double dsm, double ep1, double ep2,
-                                   long long nhist);
+                                   double hp, long long nhist);
 int STS_ManufacturedTables(sts_index n, double d, double* S, double* Sdd);
 double STS_ExactSumHost(const double* x, sts_index n);
 

@@ -102,7 +102,7 @@ def lib():
         L.orc_pow.argtypes = [C.c_double, C.c_double]
         L.orc_controller.restype = C.c_double
         L.orc_controller.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
-                                     C.c_long]
+                                     C.c_double, C.c_long]
         L.orc_state_init.argtypes = [C.POINTER(State), C.c_double]
         L.orc_state_free.argtypes = [C.POINTER(State)]
         L.orc_lsrk_evolve.restype = C.c_int
@@ -159,8 +159,8 @@ def stages_needed(method, h, rho, smax):
     return s, hmax.value
 
 
-def controller(kind, h, dsm, ep1, ep2, nhist):
-    return lib().orc_controller(kind, h, dsm, ep1, ep2, nhist)
+def controller(kind, h, dsm, ep1, ep2, hp, nhist):
+    return lib().orc_controller(kind, h, dsm, ep1, ep2, hp, nhist)
 
 
 class Problem:

@@ -690,15 +690,25 @@ static double orc_exp(double y)
 
 double orc_pow(double x, double y) { return orc_exp(y * orc_log(x)); }
 
-static double controller_ord(int controller, double h, double dsm, double ep1, double ep2, long nhist, double ORDV);
+static double controller_ord(int controller, double h, double dsm, double ep1, double ep2, double hp, long nhist,
+                             double ORDV);
 
-double orc_controller(int controller, double h, double dsm, double ep1, double ep2, long nhist)
+double orc_controller(int controller, double h, double dsm, double ep1, double ep2, double hp, long nhist)
 {
-  return controller_ord(controller, h, dsm, ep1, ep2, nhist, ORD);
+  return controller_ord(controller, h, dsm, ep1, ep2, hp, nhist, ORD);
 }
 
-/* the controllers for an error estimate of order ORDV (3 for the STS embedding) */
-static double controller_ord(int controller, double h, double dsm, double ep1, double ep2, long nhist, double ORDV)
+/* the controllers for an error estimate of order ORDV (3 for the STS embedding); hp is the
+ * previous accepted step size (used by the implicit Gustafsson controller). ARKODE's
+ * controller set, diffusion_2D/main.cpp:366-376: PID, PI, I (Soderlind-form exponents, the
+ * leading terms only until enough history exists) and Gustafsson's explicit (1991), implicit
+ * (1994) and combined controllers:
+ *   ExpGus  h' = h e_n^(-k1/p) (e_n/e_{n-1})^(-k2/p),               k1 0.367, k2 0.268
+ *   ImpGus  h' = h (h/h_{n-1}) e_n^(-k1/p) (e_n/e_{n-1})^(-k2/p),   k1 0.98,  k2 0.95
+ *   ImExGus h' = min(ExpGus, ImpGus) with those two parameter pairs
+ * with h' = h e_n^(-1/p) on the first step; e = bias * dsm, floored at 1e-10. */
+static double controller_ord(int controller, double h, double dsm, double ep1, double ep2, double hp, long nhist,
+                             double ORDV)
 {
 #undef ORD
 #define ORD ORDV
@@ -718,6 +728,15 @@ static double controller_ord(int controller, double h, double dsm, double ep1, d
   {
     if (nhist < 1) return h * orc_pow(e1, -0.8 / ORD);
     return h * orc_pow(e1, -0.8 / ORD) * orc_pow(e2, 0.31 / ORD);
+  }
+  if (controller >= 3 && controller <= 5 && nhist >= 1 && hp > 0.0)
+  {
+    const double r    = e1 / e2;
+    const double hexp = h * orc_pow(e1, -0.367 / ORD) * orc_pow(r, -0.268 / ORD);
+    if (controller == 3) return hexp;
+    const double himp = h * (h / hp) * orc_pow(e1, -0.98 / ORD) * orc_pow(r, -0.95 / ORD);
+    if (controller == 4) return himp;
+    return hexp < himp ? hexp : himp;
   }
   return h * orc_pow(e1, -1.0 / ORD);
 #undef ORD
@@ -1112,11 +1131,12 @@ int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double 
         if (o->mixed) memcpy(st->Ff, Fnewf, n * sizeof(float));
         else
           for (long k = 0; k < n; ++k) st->Ff[k] = (float)Fnew[k];
-        st->hlast = h;
+        const double hprev = st->hlast;
+        st->hlast          = h;
         if (o->hfixed > 0.0) st->hnext = o->hfixed;
         else
         {
-          double hn  = orc_controller(o->controller, h, dsm, st->ep1, st->ep2, st->nhist);
+          double hn  = orc_controller(o->controller, h, dsm, st->ep1, st->ep2, hprev, st->nhist);
           double eta = SAFETY * hn / h;
           double emx = (st->nst == 0) ? ETAMX1 : (st->after_fail ? 1.0 : GROWTH);
           if (eta > emx) eta = emx;
@@ -1140,7 +1160,7 @@ int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double 
         ret = -3; /* ARK_ERR_FAILURE */
         goto done;
       }
-      double hn  = orc_controller(o->controller, h, dsm, st->ep1, st->ep2, st->nhist);
+      double hn  = orc_controller(o->controller, h, dsm, st->ep1, st->ep2, st->hlast, st->nhist);
       double eta = SAFETY * hn / h;
       if (eta > 1.0) eta = 1.0;
       if (nef >= SMALL_NEF && eta > ETAMXF) eta = ETAMXF;
@@ -1643,11 +1663,12 @@ int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_st
         memcpy(y, ynew, n * sizeof(double));
         orc_rhs(p, st->t, y, st->F);
         st->nfe++;
-        st->hlast = h;
+        const double hprev = st->hlast;
+        st->hlast          = h;
         if (o->hfixed > 0.0) st->hnext = o->hfixed;
         else
         {
-          double hn  = controller_ord(o->controller, h, dsm, st->ep1, st->ep2, st->nhist, ordv);
+          double hn  = controller_ord(o->controller, h, dsm, st->ep1, st->ep2, hprev, st->nhist, ordv);
           double eta = SAFETY * hn / h;
           double emx = (st->nst == 0) ? ETAMX1 : (st->after_fail ? 1.0 : GROWTH);
           if (eta > emx) eta = emx;
@@ -1669,7 +1690,7 @@ int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_st
         ret = -3;
         goto done;
       }
-      double hn  = controller_ord(o->controller, h, dsm, st->ep1, st->ep2, st->nhist, ordv);
+      double hn  = controller_ord(o->controller, h, dsm, st->ep1, st->ep2, st->hlast, st->nhist, ordv);
       double eta = SAFETY * hn / h;
       if (eta > 1.0) eta = 1.0;
       if (nef >= SMALL_NEF && eta > ETAMXF) eta = ETAMXF;

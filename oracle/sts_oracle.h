@@ -85,7 +85,7 @@ double orc_pow(double x, double y); /* deterministic pow of the controllers */
 /* SSP methods (type 2 = SSP(s,2), 3 = SSP(s,3), 4 = SSP(10,4)) */
 int orc_ssp_weights(int type, int s, double* b, double* c, double* w);
 int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_state* st, double tout, double* y);
-double orc_controller(int controller, double h, double dsm, double ep1, double ep2, long nhist);
+double orc_controller(int controller, double h, double dsm, double ep1, double ep2, double hp, long nhist);
 
 void orc_state_init(orc_state* st, double t0);
 void orc_state_free(orc_state* st);

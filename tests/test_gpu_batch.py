@@ -15,7 +15,7 @@ def small_batch(stslib, count=20, seed=7):
                                        nmodes=4, pmax=6)
 
 
-@pytest.mark.parametrize("method,controller", [(1, 0), (0, 0), (1, 1), (0, 2)])
+@pytest.mark.parametrize("method,controller", [(1, 0), (0, 0), (1, 1), (0, 2), (1, 3), (0, 4), (1, 5)])
 def test_batch_matches_oracle_per_instance(ctx, stslib, oracle, method, controller):
     inst = small_batch(stslib)
     B = stslib.Batch(ctx, inst)

@@ -13,15 +13,18 @@ CASES = [
     dict(kind=sts.MANUFACTURED, n=96, mixed=True, method=sts.RKC, power=None),
     dict(kind=sts.MANUFACTURED, n=64, mixed=False, method=sts.RKC, power=(100, 0.01)),
     dict(kind=sts.PERIODIC, n=48, mixed=False, method=sts.RKL, power=None),  # generic path
+    # the implicit Gustafsson controller reads the previous step size from the checkpoint
+    dict(kind=sts.MANUFACTURED, n=64, mixed=False, method=sts.RKL, power=None, controller=sts.IMP_GUS),
 ]
 
 
 def _integrator(ctx, P, case):
     return sts.LSRKStep(ctx, P, 0.0, P.initial(), method=case["method"], rtol=1e-6, atol=1e-10,
-                        mixed=case["mixed"], power=case["power"], maxsteps=100000)
+                        mixed=case["mixed"], power=case["power"], maxsteps=100000,
+                        controller=case.get("controller", sts.PID))
 
 
-@pytest.mark.parametrize("case", CASES, ids=["rkl_fp64", "rkc_mixed", "rkc_power", "periodic"])
+@pytest.mark.parametrize("case", CASES, ids=["rkl_fp64", "rkc_mixed", "rkc_power", "periodic", "rkl_impgus"])
 def test_restart_continues_bitwise(ctx, tmp_path, case):
     P = sts.Problem(ctx, case["kind"], case["n"], case["n"], 1.0, 0.5)
     t1, t2 = 0.003, 0.007

@@ -35,18 +35,20 @@ def run(args, cwd=None):
     return r.returncode, r.stdout, r.stderr
 
 
-def test_cli_manufactured_rkc_with_error_mode(stslib, oracle):
+@pytest.mark.parametrize("controller", [2, 5])
+def test_cli_manufactured_rkc_with_error_mode(stslib, oracle, controller):
     stslib.lib()
     rc, out, err = run(["--problem", "manufactured", "--nx", "64", "--ny", "48", "--integrator", "rkc",
                         "--rtol", "1e-6", "--atol", "1e-10", "--tf", "0.05", "--nout", "5", "--error",
-                        "--controller", "2", "--maxsteps", "10000"])
+                        "--controller", str(controller), "--maxsteps", "10000"])
     assert rc == 0, err
     st = parse_like_runtests(out)
     assert st["Steps"] > 0 and st["Fails"] >= 0 and st["FEvals"] > 0 and st["Runtime"] > 0
     assert 0 < st["Accuracy"] < 1e-3
     # the same run on the oracle (same outputs times, same controller)
     P = oracle.Problem(oracle.MANUFACTURED, 64, 48)
-    J = oracle.Integrator(P, P.initial(), method=oracle.RKC, rtol=1e-6, atol=1e-10, controller=2)
+    J = oracle.Integrator(P, P.initial(), method=oracle.RKC, rtol=1e-6, atol=1e-10,
+                          controller=controller)
     # output times accumulate like the driver's (main.cpp: tout += dTout, capped at tf)
     dt, tout = 0.05 / 5, 0.05 / 5
     for k in range(5):
@@ -85,6 +87,8 @@ def test_cli_dirk_and_errors(stslib):
     assert rc == 1 and "Unknown inputs" in err
     rc, out, err = run(["--integrator", "erk"])
     assert rc == 1
+    rc, out, err = run(["--controller", "6"])
+    assert rc == 1 and "controller" in err
 
 
 def test_cli_checkpoint_restart_matches_uninterrupted_run(stslib, tmp_path):

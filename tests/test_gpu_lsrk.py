@@ -46,7 +46,7 @@ def test_fused_fp64_bitwise(ctx, stslib, oracle, nx, ny, method):
     run_pair(ctx, stslib, oracle, pk, ok, [0.02, 0.05])
 
 
-@pytest.mark.parametrize("controller", [0, 1, 2])
+@pytest.mark.parametrize("controller", [0, 1, 2, 3, 4, 5])
 def test_controllers_bitwise(ctx, stslib, oracle, controller):
     pk = dict(kind=0, nx=48, ny=40, kx=1.0, ky=0.01)
     ok = dict(method=1, rtol=1e-5, atol=1e-9, controller=controller)

@@ -134,11 +134,32 @@ def test_product_step_rules_equal_oracle(oracle, stslib):
         s = L.STS_LSRKStagesNeeded(method, h, rho, smax, C.byref(hm))
         so, hmo = oracle.stages_needed(method, h, rho, smax)
         assert s == so and hm.value == hmo
-        ctrl = int(rng.integers(0, 3))
+        ctrl = int(rng.integers(0, 6))
         dsm, ep1, ep2 = (float(10 ** rng.uniform(-4, 1)) for _ in range(3))
+        hp = h * float(10 ** rng.uniform(-1, 1))
         nh = int(rng.integers(0, 4))
-        assert L.STS_AdaptControllerEstimate(ctrl, h, dsm, ep1, ep2, nh) == \
-            oracle.controller(ctrl, h, dsm, ep1, ep2, nh)
+        assert L.STS_AdaptControllerEstimate(ctrl, h, dsm, ep1, ep2, hp, nh) == \
+            oracle.controller(ctrl, h, dsm, ep1, ep2, hp, nh)
+
+
+def test_gustafsson_controllers(oracle):
+    """ExpGus / ImpGus / ImExGus (diffusion_2D/main.cpp:366-376): the published formulas,
+    evaluated here with numpy's pow, agree with the oracle to a few ulp; the first step is the
+    I controller; ImExGus is the smaller of the two."""
+    rng = np.random.default_rng(11)
+    p = 3.0
+    for _ in range(300):
+        h = float(10 ** rng.uniform(-8, -1))
+        hp = h * float(10 ** rng.uniform(-1, 1))
+        dsm, ep1 = (float(10 ** rng.uniform(-4, 1)) for _ in range(2))
+        e1, e2 = max(1.5 * dsm, 1e-10), max(1.5 * ep1, 1e-10)
+        exp_ = h * e1 ** (-0.367 / p) * (e1 / e2) ** (-0.268 / p)
+        imp_ = h * (h / hp) * e1 ** (-0.98 / p) * (e1 / e2) ** (-0.95 / p)
+        for ctrl, want in ((3, exp_), (4, imp_), (5, min(exp_, imp_))):
+            got = oracle.controller(ctrl, h, dsm, ep1, 0.5, hp, 1)
+            assert abs(got - want) <= 1e-13 * want
+            first = oracle.controller(ctrl, h, dsm, ep1, 0.5, hp, 0)
+            assert abs(first - h * e1 ** (-1 / p)) <= 1e-13 * first
 
 
 def test_product_tables_equal_oracle(oracle, stslib):
