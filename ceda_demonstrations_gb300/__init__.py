@@ -28,6 +28,7 @@ __all__ = ["lib", "Context", "NVector", "Problem", "LSRKStep", "PCGSolver", "imp
 RKC, RKL = 0, 1
 SSP_S_2, SSP_S_3, SSP_10_4 = 2, 3, 4
 PID, PI, I, EXP_GUS, IMP_GUS, IMEX_GUS = 0, 1, 2, 3, 4, 5
+MODIFIED_GS, CLASSICAL_GS = 1, 2
 MANUFACTURED, UNFORCED, PERIODIC = 0, 1, 2
 NORMAL, ONE_STEP = 1, 2
 TOO_MUCH_WORK = -1
@@ -97,6 +98,7 @@ SIGNATURES = [
     ("N_VMaxNorm_Sts", C.c_double, [_NV]),
     ("N_VWrmsNorm_Sts", C.c_double, [_NV, _NV]),
     ("N_VLinearCombination_Sts", C.c_int, [C.c_int, _dp, C.POINTER(_NV), _NV]),
+    ("N_VDotProdMulti_Sts", C.c_int, [C.c_int, _NV, C.POINTER(_NV), _dp]),
     ("STS_WrmsNormNoAlloc", C.c_int, [_vp, _vp, _ll, _vp, _vp]),
     ("STS_ProblemCreate", _vp, [_vp, C.c_int, _ll, _ll, C.c_double, C.c_double, C.c_int,
                                 C.c_double, C.c_double, C.c_double, C.c_double]),
@@ -148,6 +150,11 @@ SIGNATURES = [
     ("STS_SUNLinSolNumIters", C.c_int, [_vp]),
     ("STS_SUNLinSolResNorm", C.c_double, [_vp]),
     ("STS_SUNLinSolFree", C.c_int, [_vp]),
+    ("STS_SUNLinSol_SPGMR", _vp, [_NV, C.c_int, C.c_int, _vp]),
+    ("STS_SUNLinSol_SPGMRSetMaxRestarts", C.c_int, [_vp, C.c_int]),
+    ("STS_SUNLinSol_SPGMRSetGSType", C.c_int, [_vp, C.c_int]),
+    ("STS_SDIRK2EvolveLS", C.c_int, [_vp, _vp, C.c_int, _NV, C.c_double, C.c_double, C.c_int,
+                                     C.c_double, C.POINTER(_ll)]),
     ("STS_ImplicitSolvePCG", C.c_int, [_vp, C.c_double, _NV, _NV, C.c_double, C.c_int, C.c_int,
                                        _ip, _dp]),
     ("STS_SDIRK2Evolve", C.c_int, [_vp, _NV, C.c_double, C.c_double, C.c_int, C.c_double,
@@ -354,6 +361,15 @@ class NVector:
 
     def dot(self, y):
         return lib().N_VDotProd_Sts(self.h, y.h)
+
+    def dot_multi(self, vecs):
+        """N_VDotProdMulti: exact dot products with each vector of ``vecs``."""
+        n = len(vecs)
+        out = (C.c_double * n)()
+        X = (_NV * n)(*[v.h for v in vecs])
+        if lib().N_VDotProdMulti_Sts(n, self.h, X, out) != 0:
+            _err("N_VDotProdMulti_Sts")
+        return list(out)
 
     def max_norm(self):
         return lib().N_VMaxNorm_Sts(self.h)
@@ -576,14 +592,23 @@ class LSRKStep:
 
 
 class PCGSolver:
-    """SUNLinSol_PCG through ATimes / PSolve callbacks (generic path)."""
+    """SUNLinSol_PCG through ATimes / PSolve callbacks (generic path). With ``atimes=None``
+    the object is a bare solver for :func:`sdirk2_evolve_ls`, which attaches its own
+    callbacks; ``precond`` then selects SUN_PREC_RIGHT."""
 
-    def __init__(self, ctx, y, atimes, psolve=None, maxl=100):
+    _create = "STS_SUNLinSol_PCG"
+
+    def __init__(self, ctx, y, atimes=None, psolve=None, maxl=100, precond=None):
         L = lib()
         self.ctx = ctx
-        self.LS = L.STS_SUNLinSol_PCG(y.h, 2 if psolve else 0, maxl, ctx.h)
+        pre = bool(psolve) if precond is None else bool(precond)
+        self.LS = getattr(L, self._create)(y.h, 2 if pre else 0, maxl, ctx.h)
+        if not self.LS:
+            _err(self._create)
         ctx.live += 1
         self._keep = []
+        if atimes is None:
+            return
 
         def at(_d, v, z):
             return int(atimes(NVector.wrap(ctx, v), NVector.wrap(ctx, z)) or 0)
@@ -618,6 +643,32 @@ def implicit_solve_pcg(problem, gamma, b, x, tol=1e-8, maxit=100000, jacobi=True
     if rc < 0:
         _err("STS_ImplicitSolvePCG")
     return it.value, rel.value, rc
+
+
+class SPGMRSolver(PCGSolver):
+    """SUNLinSol_SPGMR (restarted GMRES, right preconditioning) through ATimes / PSolve
+    callbacks; ``gstype`` 1 = modified, 2 = classical Gram-Schmidt."""
+
+    _create = "STS_SUNLinSol_SPGMR"
+
+    def __init__(self, ctx, y, atimes=None, psolve=None, maxl=20, max_restarts=0, gstype=MODIFIED_GS,
+                 precond=None):
+        super().__init__(ctx, y, atimes, psolve, maxl, precond)
+        L = lib()
+        if L.STS_SUNLinSol_SPGMRSetMaxRestarts(self.LS, max_restarts) != 0 or \
+                L.STS_SUNLinSol_SPGMRSetGSType(self.LS, gstype) != 0:
+            _err("SPGMR options")
+
+
+def sdirk2_evolve_ls(problem, solver, y, t0, h, nsteps, tol=1e-10, precond=True):
+    """Fixed-step SDIRK2 with the stage systems solved by a generic SUNLinearSolver
+    (:class:`PCGSolver` or :class:`SPGMRSolver`); returns the total Krylov iterations."""
+    it = _ll()
+    rc = lib().STS_SDIRK2EvolveLS(problem.h, solver.LS, int(precond), y.h, t0, h, nsteps, tol,
+                                  C.byref(it))
+    if rc < 0:
+        _err("STS_SDIRK2EvolveLS")
+    return it.value
 
 
 def sdirk2_evolve(problem, y, t0, h, nsteps, tol=1e-10, maxit=100000):

@@ -8,6 +8,7 @@
 // --problem manufactured (BASELINE manufactured Dirichlet problem on [0,1]^2) or unforced.
 // Integrators: rkc, rkl (LSRKStep STS, fused kernels for the Dirichlet problems) and dirk
 // (fixed-step SDIRK2 with the fused Jacobi-PCG, Dirichlet problems, --fixedstep required).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -72,7 +73,7 @@ static void help()
           "  --integrator <dirk|rkc|rkl> --rtol --atol --fixedstep --controller <0..5: PID PI I ExpGus ImpGus ImExGus>\n"
           "  --maxsteps --onestep <n> --error --internaleig --smax <stages> --mixed --nographs\n"
           "\nDIRK solver command line options:\n"
-          "  --order --nonlinear --ls <cg> --lsinfo --liniters --epslin --noprec --msbp\n"
+          "  --order --nonlinear --ls <cg|gmres> --lsinfo --liniters --epslin --noprec --msbp\n"
           "\nOutput command line options:\n"
           "  --output <level> (0 = none, 1 = stats, 2 = solution)  --nout <nout>\n"
           "  --checkpoint <file> : write the integrator state at the end of the run\n"
@@ -172,6 +173,11 @@ int main(int argc, char** argv)
     cerr << "ERROR: dirk runs fixed steps (--fixedstep) on the Dirichlet problems" << endl;
     return 1;
   }
+  if (impl && o.ls != "cg" && o.ls != "gmres")
+  {
+    cerr << "ERROR: illegal linear solver (cg or gmres)" << endl;
+    return 1;
+  }
   if (o.controller < STS_ADAPT_PID || o.controller > STS_ADAPT_IMEX_GUS)
   {
     cerr << "ERROR: illegal controller (0 PID, 1 PI, 2 I, 3 ExpGus, 4 ImpGus, 5 ImExGus)" << endl;
@@ -216,6 +222,7 @@ int main(int argc, char** argv)
   }
   void* mem = nullptr;
   void* ref = nullptr;
+  void* LS  = nullptr; // generic linear solver of the dirk path (--ls gmres, or cg with --noprec)
   if (sts)
   {
     mem = STS_LSRKStepCreateSTS(STS_Diffusion, 0.0, u, ctx);
@@ -306,7 +313,23 @@ int main(int argc, char** argv)
       const double h    = o.hfixed;
       const int nsteps  = (int)llround((tout - t) / h);
       long long its     = 0;
-      flag              = STS_SDIRK2Evolve(P, u, t, h, nsteps, o.epslin > 0 ? o.epslin : 1e-10, 100000, &its);
+      const double tol  = o.epslin > 0 ? o.epslin : 1e-10;
+      if (o.ls == "cg" && o.prec) flag = STS_SDIRK2Evolve(P, u, t, h, nsteps, tol, 100000, &its);
+      else
+      { // generic solver object (main.cpp:209-218): PCG without preconditioner, or SPGMR with
+        // maxl = --liniters, restarted up to 10^5 iterations in total
+        if (!LS)
+        {
+          if (o.ls == "cg") LS = STS_SUNLinSol_PCG(u, STS_PREC_NONE, 100000, ctx);
+          else
+          {
+            const int maxl = o.liniters > 0 ? o.liniters : 20;
+            LS = STS_SUNLinSol_SPGMR(u, o.prec ? STS_PREC_RIGHT : STS_PREC_NONE, maxl, ctx);
+            if (LS) STS_SUNLinSol_SPGMRSetMaxRestarts(LS, std::max(0, 100000 / maxl - 1));
+          }
+        }
+        flag = LS ? STS_SDIRK2EvolveLS(P, LS, o.prec ? 1 : 0, u, t, h, nsteps, tol, &its) : -1;
+      }
       lin_iters += its;
       t += nsteps * h;
     }
@@ -372,6 +395,7 @@ int main(int argc, char** argv)
   }
   if (mem) STS_ARKodeFree(&mem);
   if (ref) STS_ARKodeFree(&ref);
+  if (LS) STS_SUNLinSolFree(LS);
   N_VDestroy_Sts(u);
   if (uref) N_VDestroy_Sts(uref);
   if (uerr) N_VDestroy_Sts(uerr);

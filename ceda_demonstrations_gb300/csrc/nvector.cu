@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -258,6 +259,7 @@ static N_Vector_Ops make_ops()
   o->nvmaxnorm            = N_VMaxNorm_Sts;
   o->nvwrmsnorm           = N_VWrmsNorm_Sts;
   o->nvlinearcombination  = N_VLinearCombination_Sts;
+  o->nvdotprodmulti       = N_VDotProdMulti_Sts;
   return o;
 }
 
@@ -452,6 +454,30 @@ extern "C" double N_VMaxNorm_Sts(N_Vector x)
   maxnorm_kernel<<<ew_blocks(ctx, n, 256 * 4), 256, 0, ctx->stream>>>(n, NVD(x), ctx->d_work,
                                                                        ctx->d_slots + SLOT_GENERIC);
   return read_slot(ctx, SLOT_GENERIC);
+}
+
+// N_VDotProdMulti: the exact dot products of x with Y[0..nvec-1], each written to its own
+// result slot; one stream synchronisation per STS_NSLOTS - SLOT_MULTI products
+extern "C" int N_VDotProdMulti_Sts(int nvec, N_Vector x, N_Vector* Y, double* dots)
+{
+  if (nvec < 1 || !x || !Y || !dots) return -1;
+  STS_Context ctx = x->sunctx;
+  long long n     = NVL(x);
+  ctx_activate(ctx);
+  constexpr int CH = STS_NSLOTS - SLOT_MULTI;
+  for (int c0 = 0; c0 < nvec; c0 += CH)
+  {
+    const int cnt = std::min(CH, nvec - c0);
+    for (int k = 0; k < cnt; ++k)
+    {
+      if (NVL(Y[c0 + k]) != n) return -1;
+      xred_kernel<0><<<ew_blocks(ctx, n, 256 * 4), 256, 0, ctx->stream>>>(n, NVD(x), NVD(Y[c0 + k]), ctx->d_work,
+                                                                           ctx->d_slots + SLOT_MULTI + k);
+    }
+    if (!STS_CUDA_OK(cudaStreamSynchronize(ctx->stream))) return -1;
+    for (int k = 0; k < cnt; ++k) dots[c0 + k] = ((volatile double*)ctx->h_slots)[SLOT_MULTI + k];
+  }
+  return 0;
 }
 
 extern "C" int N_VLinearCombination_Sts(int nvec, double* c, N_Vector* X, N_Vector z)

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <vector>
 
 #include "kernels.cuh"
 #include "krylov.cuh"
@@ -299,9 +300,13 @@ extern "C" int STS_ImplicitSolvePCG(STS_Problem p, double gamma, N_Vector b, N_V
 }
 
 // ---------------------------------------------------------------------------------------
-// generic PCG through ATimes / PSolve callbacks (SUNLinSol_PCG interface)
+// Generic Krylov solvers through ATimes / PSolve callbacks: SUNLinSol_PCG and SUNLinSol_SPGMR
+// (diffusion_2D/main.cpp:209-218). One object type; the solve dispatches on the kind.
 // ---------------------------------------------------------------------------------------
-struct LinSolPCG {
+enum { LS_PCG = 0, LS_SPGMR = 1 };
+
+struct LinSol {
+  int kind          = LS_PCG;
   STS_Context ctx   = nullptr;
   int pretype       = STS_PREC_NONE;
   int maxl          = 5;
@@ -310,55 +315,89 @@ struct LinSolPCG {
   void* P_data      = nullptr;
   STS_PSolveFn psolve = nullptr;
   N_Vector r = nullptr, pv = nullptr, z = nullptr, Ap = nullptr;
+  // SPGMR: Krylov basis V[0..maxl], restarts, Gram-Schmidt variant, Hessenberg + Givens
+  std::vector<N_Vector> V;
+  int max_restarts  = 0;
+  int gstype        = STS_MODIFIED_GS;
   int last_iters    = 0;
   double last_res   = 0.0;
 };
 
-extern "C" void* STS_SUNLinSol_PCG(N_Vector y, int pretype, int maxl, STS_Context ctx)
+static LinSol* linsol_new(int kind, N_Vector y, int pretype, int maxl, STS_Context ctx)
 {
   if (!y || !ctx)
   {
-    sts_set_error("SUNLinSol_PCG: NULL argument");
+    sts_set_error("SUNLinSol: NULL argument");
     return nullptr;
   }
-  LinSolPCG* L = new LinSolPCG();
-  L->ctx       = ctx;
-  L->pretype   = pretype;
-  L->maxl      = maxl > 0 ? maxl : 5;
-  L->r         = N_VClone_Sts(y);
-  L->pv        = N_VClone_Sts(y);
-  L->z         = N_VClone_Sts(y);
-  L->Ap        = N_VClone_Sts(y);
+  LinSol* L  = new LinSol();
+  L->kind    = kind;
+  L->ctx     = ctx;
+  L->pretype = pretype;
+  L->maxl    = maxl > 0 ? maxl : 5;
+  L->r       = N_VClone_Sts(y);
+  L->z       = N_VClone_Sts(y);
+  L->Ap      = N_VClone_Sts(y);
+  if (kind == LS_PCG) L->pv = N_VClone_Sts(y);
+  else
+    for (int k = 0; k <= L->maxl; ++k) L->V.push_back(N_VClone_Sts(y));
   return L;
+}
+
+extern "C" void* STS_SUNLinSol_PCG(N_Vector y, int pretype, int maxl, STS_Context ctx)
+{
+  return linsol_new(LS_PCG, y, pretype, maxl, ctx);
+}
+
+extern "C" void* STS_SUNLinSol_SPGMR(N_Vector y, int pretype, int maxl, STS_Context ctx)
+{
+  if (maxl > 1000)
+  {
+    sts_set_error("SUNLinSol_SPGMR: maxl %d > 1000", maxl);
+    return nullptr;
+  }
+  return linsol_new(LS_SPGMR, y, pretype, maxl, ctx);
+}
+
+extern "C" int STS_SUNLinSol_SPGMRSetMaxRestarts(void* LS, int maxrs)
+{
+  LinSol* L = (LinSol*)LS;
+  if (!L || L->kind != LS_SPGMR || maxrs < 0) return -1;
+  L->max_restarts = maxrs;
+  return 0;
+}
+
+extern "C" int STS_SUNLinSol_SPGMRSetGSType(void* LS, int gstype)
+{
+  LinSol* L = (LinSol*)LS;
+  if (!L || L->kind != LS_SPGMR || (gstype != STS_MODIFIED_GS && gstype != STS_CLASSICAL_GS)) return -1;
+  L->gstype = gstype;
+  return 0;
 }
 
 extern "C" int STS_SUNLinSolSetATimes(void* LS, void* A_data, STS_ATimesFn atimes)
 {
   if (!LS) return -1;
-  ((LinSolPCG*)LS)->A_data = A_data;
-  ((LinSolPCG*)LS)->atimes = atimes;
+  ((LinSol*)LS)->A_data = A_data;
+  ((LinSol*)LS)->atimes = atimes;
   return 0;
 }
 
 extern "C" int STS_SUNLinSolSetPreconditioner(void* LS, void* P_data, STS_PSolveFn psolve)
 {
   if (!LS) return -1;
-  ((LinSolPCG*)LS)->P_data = P_data;
-  ((LinSolPCG*)LS)->psolve = psolve;
+  ((LinSol*)LS)->P_data = P_data;
+  ((LinSol*)LS)->psolve = psolve;
   return 0;
 }
 
 // standard PCG, x0 = 0, stop when ||r||_2 <= delta ||b||_2
-extern "C" int STS_SUNLinSolSolve(void* LS, N_Vector x, N_Vector b, double delta)
+static int pcg_solve(LinSol* L, N_Vector x, N_Vector b, double delta)
 {
-  LinSolPCG* L = (LinSolPCG*)LS;
-  if (!L || !L->atimes) return -1;
   const bool prec = L->pretype != STS_PREC_NONE && L->psolve;
   N_VConst_Sts(0.0, x);
   N_VLinearSum_Sts(1.0, b, 0.0, b, L->r);
   const double bnorm = sqrt(N_VDotProd_Sts(b, b));
-  L->last_iters      = 0;
-  L->last_res        = 0.0;
   if (!(bnorm > 0.0)) return 0;
   if (prec)
   {
@@ -391,17 +430,160 @@ extern "C" int STS_SUNLinSolSolve(void* LS, N_Vector x, N_Vector b, double delta
   return 1; // SUNLS_CONV_FAIL (recoverable)
 }
 
-extern "C" int STS_SUNLinSolNumIters(void* LS) { return LS ? ((LinSolPCG*)LS)->last_iters : 0; }
-extern "C" double STS_SUNLinSolResNorm(void* LS) { return LS ? ((LinSolPCG*)LS)->last_res : 0.0; }
+// Givens rotation (c, s) with [c s; -s c] [a; b] = [r; 0], scaled to avoid overflow
+static void givens(double a, double b, double* c, double* s)
+{
+  if (b == 0.0)
+  {
+    *c = 1.0;
+    *s = 0.0;
+  }
+  else if (fabs(b) > fabs(a))
+  {
+    const double t = a / b;
+    *s             = 1.0 / sqrt(1.0 + t * t);
+    *c             = *s * t;
+  }
+  else
+  {
+    const double t = b / a;
+    *c             = 1.0 / sqrt(1.0 + t * t);
+    *s             = *c * t;
+  }
+}
+
+// Restarted GMRES(maxl) with right preconditioning (Saad & Schultz 1986), x0 = 0: minimise
+// ||b - A P^-1 u|| over the Krylov space of the current residual, x += P^-1 u at the end of
+// each cycle; Arnoldi by modified Gram-Schmidt (one exact dot and one LinearSum per basis
+// vector) or classical Gram-Schmidt with one re-orthogonalisation pass (two N_VDotProdMulti +
+// N_VLinearCombination); the Hessenberg matrix is reduced by Givens rotations on the host, so
+// the residual estimate |g_{j+1}| is known after every iteration. Stop when it is at most
+// delta ||b||_2; after max_restarts restarts without convergence return 1 (recoverable).
+static int spgmr_solve(LinSol* L, N_Vector x, N_Vector b, double delta)
+{
+  const bool prec = L->pretype != STS_PREC_NONE && L->psolve;
+  const int m     = L->maxl;
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m), h(m + 1), h2(m + 1);
+  std::vector<double> cf(m + 2);
+  std::vector<N_Vector> X(m + 2);
+  auto Hij = [&](int i, int j) -> double& { return H[(size_t)i * m + j]; };
+  N_VConst_Sts(0.0, x);
+  N_VLinearSum_Sts(1.0, b, 0.0, b, L->r);
+  const double bnorm = sqrt(N_VDotProd_Sts(b, b));
+  if (!(bnorm > 0.0)) return 0;
+  double beta = bnorm;
+  for (int cycle = 0; cycle <= L->max_restarts; ++cycle)
+  {
+    N_VScale_Sts(1.0 / beta, L->r, L->V[0]);
+    for (int k = 0; k <= m; ++k) g[k] = 0.0;
+    g[0]          = beta;
+    int k         = 0; // columns built in this cycle
+    bool converged = false;
+    for (int j = 0; j < m; ++j)
+    {
+      N_Vector w = L->V[j + 1];
+      if (prec)
+      {
+        if (L->psolve(L->P_data, L->V[j], L->z, delta, L->pretype)) return 1;
+        if (L->atimes(L->A_data, L->z, w)) return 1;
+      }
+      else if (L->atimes(L->A_data, L->V[j], w)) return 1;
+      if (L->gstype == STS_MODIFIED_GS)
+      {
+        for (int i = 0; i <= j; ++i)
+        {
+          Hij(i, j) = N_VDotProd_Sts(w, L->V[i]);
+          N_VLinearSum_Sts(-Hij(i, j), L->V[i], 1.0, w, w);
+        }
+      }
+      else
+      {
+        for (int pass = 0; pass < 2; ++pass)
+        {
+          double* hp = pass ? h2.data() : h.data();
+          if (N_VDotProdMulti_Sts(j + 1, w, L->V.data(), hp)) return -1;
+          cf[0] = 1.0;
+          X[0]  = w;
+          for (int i = 0; i <= j; ++i)
+          {
+            cf[i + 1] = -hp[i];
+            X[i + 1]  = L->V[i];
+          }
+          N_VLinearCombination_Sts(j + 2, cf.data(), X.data(), w);
+        }
+        for (int i = 0; i <= j; ++i) Hij(i, j) = h[i] + h2[i];
+      }
+      const double hn = sqrt(N_VDotProd_Sts(w, w));
+      Hij(j + 1, j)   = hn;
+      // apply the previous rotations to column j, then the new one
+      for (int i = 0; i < j; ++i)
+      {
+        const double a = Hij(i, j), bb = Hij(i + 1, j);
+        Hij(i, j)     = cs[i] * a + sn[i] * bb;
+        Hij(i + 1, j) = cs[i] * bb - sn[i] * a;
+      }
+      givens(Hij(j, j), Hij(j + 1, j), &cs[j], &sn[j]);
+      Hij(j, j)     = cs[j] * Hij(j, j) + sn[j] * Hij(j + 1, j);
+      Hij(j + 1, j) = 0.0;
+      g[j + 1]      = -sn[j] * g[j];
+      g[j]          = cs[j] * g[j];
+      k             = j + 1;
+      L->last_iters++;
+      L->last_res = fabs(g[j + 1]) / bnorm;
+      if (hn > 0.0) N_VScale_Sts(1.0 / hn, w, w);
+      if (fabs(g[j + 1]) <= delta * bnorm || !(hn > 0.0))
+      {
+        converged = fabs(g[j + 1]) <= delta * bnorm;
+        break;
+      }
+    }
+    // y = H^-1 g (upper triangular, k columns); u = V y; x += P^-1 u
+    for (int i = k - 1; i >= 0; --i)
+    {
+      double sacc = g[i];
+      for (int q = i + 1; q < k; ++q) sacc = sacc - Hij(i, q) * y[q];
+      y[i] = sacc / Hij(i, i);
+    }
+    N_VLinearCombination_Sts(k, y.data(), L->V.data(), L->Ap);
+    if (prec)
+    {
+      if (L->psolve(L->P_data, L->Ap, L->z, delta, L->pretype)) return 1;
+      N_VLinearSum_Sts(1.0, x, 1.0, L->z, x);
+    }
+    else N_VLinearSum_Sts(1.0, x, 1.0, L->Ap, x);
+    if (converged) return 0;
+    if (cycle == L->max_restarts) break;
+    // restart from the true residual r = b - A x
+    if (L->atimes(L->A_data, x, L->Ap)) return 1;
+    N_VLinearSum_Sts(1.0, b, -1.0, L->Ap, L->r);
+    beta = sqrt(N_VDotProd_Sts(L->r, L->r));
+    L->last_res = beta / bnorm;
+    if (beta <= delta * bnorm) return 0;
+  }
+  return 1; // SUNLS_CONV_FAIL / SUNLS_RES_REDUCED (recoverable)
+}
+
+extern "C" int STS_SUNLinSolSolve(void* LS, N_Vector x, N_Vector b, double delta)
+{
+  LinSol* L = (LinSol*)LS;
+  if (!L || !L->atimes || !x || !b) return -1;
+  L->last_iters = 0;
+  L->last_res   = 0.0;
+  return L->kind == LS_PCG ? pcg_solve(L, x, b, delta) : spgmr_solve(L, x, b, delta);
+}
+
+extern "C" int STS_SUNLinSolNumIters(void* LS) { return LS ? ((LinSol*)LS)->last_iters : 0; }
+extern "C" double STS_SUNLinSolResNorm(void* LS) { return LS ? ((LinSol*)LS)->last_res : 0.0; }
 
 extern "C" int STS_SUNLinSolFree(void* LS)
 {
-  LinSolPCG* L = (LinSolPCG*)LS;
+  LinSol* L = (LinSol*)LS;
   if (!L) return 0;
   N_VDestroy_Sts(L->r);
-  N_VDestroy_Sts(L->pv);
   N_VDestroy_Sts(L->z);
   N_VDestroy_Sts(L->Ap);
+  if (L->pv) N_VDestroy_Sts(L->pv);
+  for (N_Vector v : L->V) N_VDestroy_Sts(v);
   delete L;
   return 0;
 }
@@ -456,6 +638,49 @@ extern "C" int STS_SDIRK2Evolve(STS_Problem p, N_Vector y, double t0, double h, 
     double rel;
     return STS_ImplicitSolvePCG(p, hg, rhs, d, tol, maxit, 1, it, &rel);
   });
+}
+
+// The SDIRK2 driver with a generic SUNLinearSolver: ATimes v -> v - gamma A v through the
+// problem's J*v, PSolve the Jacobi STS_PSolve (ARKODE's linear-solver interface attaches its
+// own ATimes and the user's preconditioner in the same way, main.cpp:302-316).
+namespace {
+struct ShiftedOp {
+  STS_Problem p;
+  double gamma;
+  N_Vector tmp;
+};
+int shifted_atimes(void* d, N_Vector v, N_Vector z)
+{
+  ShiftedOp* a = (ShiftedOp*)d;
+  if (STS_JacTimes(v, a->tmp, 0.0, nullptr, nullptr, a->p, nullptr)) return -1;
+  N_VLinearSum_Sts(1.0, v, -a->gamma, a->tmp, z);
+  return 0;
+}
+int jacobi_psolve(void* d, N_Vector r, N_Vector z, double tol, int lr)
+{
+  ShiftedOp* a = (ShiftedOp*)d;
+  return STS_PSolve(0.0, nullptr, nullptr, r, z, a->gamma, tol, lr, a->p);
+}
+} // namespace
+
+extern "C" int STS_SDIRK2EvolveLS(STS_Problem p, void* LS, int precond, N_Vector y, double t0, double h,
+                                  int nsteps, double tol, long long* total_iters)
+{
+  LinSol* L = (LinSol*)LS;
+  if (!p || !L || !y) return -1;
+  ShiftedOp op{p, 0.0, N_VClone_Sts(y)};
+  STS_SUNLinSolSetATimes(L, &op, shifted_atimes);
+  STS_SUNLinSolSetPreconditioner(L, precond ? &op : nullptr, precond ? jacobi_psolve : nullptr);
+  const int rc = sdirk2_run(p, y, t0, h, nsteps, total_iters, [&](double hg, N_Vector rhs, N_Vector d, int* it) {
+    op.gamma     = hg;
+    const int sr = STS_SUNLinSolSolve(L, d, rhs, tol);
+    *it          = STS_SUNLinSolNumIters(L);
+    return sr < 0 ? -1 : 0;
+  });
+  STS_SUNLinSolSetATimes(L, nullptr, nullptr);
+  STS_SUNLinSolSetPreconditioner(L, nullptr, nullptr);
+  N_VDestroy_Sts(op.tmp);
+  return rc;
 }
 
 // The same SDIRK2 driver with each stage solved by STS_ImplicitSolveLearned (FCG with the

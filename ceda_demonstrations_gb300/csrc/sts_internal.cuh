@@ -31,7 +31,7 @@ void sts_set_error(const char* fmt, ...);
 // total into a double written to a result slot (mapped pinned host memory) and clears the
 // workspace for the next reduction on the stream.
 // ---------------------------------------------------------------------------------------
-constexpr int STS_NSLOTS = 16;
+constexpr int STS_NSLOTS = 64;
 enum ResultSlot {
   SLOT_GENERIC = 0,
   SLOT_DSM     = 1,
@@ -44,6 +44,7 @@ enum ResultSlot {
   SLOT_PCG1    = 9,
   SLOT_PCG2    = 10,
   SLOT_PCG3    = 11,
+  SLOT_MULTI   = 16, // N_VDotProdMulti: slots 16 .. 63
 };
 
 struct RedWork {

@@ -40,7 +40,7 @@ int STS_DeviceCount(void);
  * N_Vector (device). Layout {content, ops, sunctx} as SUNDIALS' generic N_Vector; the ops
  * table holds the subset LSRKStep, the PCG solver and the Jacobi PSolve use
  * (gkeyll_diffusion/src/nvector_gkylzero.c:45-60, + nvprod for
- * diffusion_2D/preconditioner_jacobi.cpp:58, + nvlinearcombination).
+ * diffusion_2D/preconditioner_jacobi.cpp:58, + nvlinearcombination and nvdotprodmulti).
  * ----------------------------------------------------------------------------------*/
 typedef struct _generic_N_Vector* N_Vector;
 typedef struct _generic_N_Vector_Ops* N_Vector_Ops;
@@ -64,6 +64,7 @@ struct _generic_N_Vector_Ops {
   double (*nvmaxnorm)(N_Vector);
   double (*nvwrmsnorm)(N_Vector, N_Vector);
   int (*nvlinearcombination)(int, double*, N_Vector*, N_Vector);
+  int (*nvdotprodmulti)(int, N_Vector, N_Vector*, double*);
 };
 
 struct _generic_N_Vector {
@@ -108,6 +109,9 @@ double N_VDotProd_Sts(N_Vector x, N_Vector y);
 double N_VMaxNorm_Sts(N_Vector x);
 double N_VWrmsNorm_Sts(N_Vector x, N_Vector w);
 int N_VLinearCombination_Sts(int nvec, double* c, N_Vector* X, N_Vector z);
+/* N_VDotProdMulti (SUNDIALS fused op, used by SPGMR's classical Gram-Schmidt): dots[k] =
+ * exact x . Y[k]; returns 0, or -1 on a length mismatch or a CUDA error */
+int N_VDotProdMulti_Sts(int nvec, N_Vector x, N_Vector* Y, double* dots);
 
 /* Allocation-free WRMS norm. No counterpart in the reference: it exists for callers that
  * cannot allocate device or pinned memory when they need a norm (work recorded into another
@@ -277,9 +281,19 @@ typedef int (*STS_ATimesFn)(void* A_data, N_Vector v, N_Vector z);
 typedef int (*STS_PSolveFn)(void* P_data, N_Vector r, N_Vector z, double tol, int lr);
 
 void* STS_SUNLinSol_PCG(N_Vector y, int pretype, int maxl, STS_Context ctx); /* main.cpp:211 */
+/* SUNLinSol_SPGMR (main.cpp:216, --ls gmres): restarted GMRES(maxl), right preconditioning,
+ * maxl <= 1000; SUNLinSol_SPGMRSetMaxRestarts (default 0) / SetGSType (default modified) */
+#define STS_MODIFIED_GS 1  /* SUN_MODIFIED_GS */
+#define STS_CLASSICAL_GS 2 /* SUN_CLASSICAL_GS (with one re-orthogonalisation pass) */
+void* STS_SUNLinSol_SPGMR(N_Vector y, int pretype, int maxl, STS_Context ctx);
+int STS_SUNLinSol_SPGMRSetMaxRestarts(void* LS, int maxrs);
+int STS_SUNLinSol_SPGMRSetGSType(void* LS, int gstype);
 int STS_SUNLinSolSetATimes(void* LS, void* A_data, STS_ATimesFn atimes);
 int STS_SUNLinSolSetPreconditioner(void* LS, void* P_data, STS_PSolveFn psolve);
-/* generic PCG through the callbacks; stop when ||r||_2 <= delta ||b||_2 */
+/* solve A x = b from x0 = 0 through the callbacks; stop when ||r||_2 <= delta ||b||_2 (PCG:
+ * the recurrence residual; SPGMR: the Givens residual estimate). Returns 0 converged, 1 not
+ * converged within maxl iterations (SPGMR: maxl (max_restarts + 1)) or a callback failed,
+ * -1 illegal input */
 int STS_SUNLinSolSolve(void* LS, N_Vector x, N_Vector b, double delta);
 int STS_SUNLinSolNumIters(void* LS);
 double STS_SUNLinSolResNorm(void* LS);
@@ -290,6 +304,14 @@ int STS_ImplicitSolvePCG(STS_Problem p, double gamma, N_Vector b, N_Vector x, do
 /* fixed-step SDIRK2 with fused Jacobi-PCG stage solves (ARKStep DIRK, main.cpp:242,272) */
 int STS_SDIRK2Evolve(STS_Problem p, N_Vector y, double t0, double h, int nsteps, double tol,
                      int maxit, long long* total_iters);
+/* fixed-step SDIRK2 whose stage systems (I - gamma h A) d = rhs are solved by a generic
+ * SUNLinearSolver (STS_SUNLinSol_PCG or STS_SUNLinSol_SPGMR), as ARKodeSetLinearSolver +
+ * ARKodeSetPreconditioner attach one (main.cpp:302-316): the driver sets the solver's ATimes
+ * to v - gamma h A v (STS_JacTimes) and, when `precond` is 1, its PSolve to the Jacobi
+ * STS_PSolve (used when the solver was created with STS_PREC_RIGHT). The solver's own
+ * callbacks are replaced. Returns 0, or -1 on illegal input or a failed solve (rc < 0). */
+int STS_SDIRK2EvolveLS(STS_Problem p, void* LS, int precond, N_Vector y, double t0, double h,
+                       int nsteps, double tol, long long* total_iters);
 /* SDIRK2 with each stage solved by STS_ImplicitSolveLearned (declared below); STS_Net is the
  * learned preconditioner's handle */
 typedef struct STS_Net_* STS_Net;

@@ -114,6 +114,16 @@ def lib():
         L.orc_sdirk2.restype = C.c_int
         L.orc_sdirk2.argtypes = [C.POINTER(Prob), C.c_double, C.c_double, C.c_int, C.c_double,
                                  C.c_int, _dp, C.POINTER(C.c_long)]
+        L.orc_pcg_generic.restype = C.c_int
+        L.orc_pcg_generic.argtypes = [C.POINTER(Prob), C.c_double, C.c_int, _dp, _dp, C.c_double,
+                                      C.c_int, C.POINTER(C.c_int), _dp]
+        L.orc_spgmr.restype = C.c_int
+        L.orc_spgmr.argtypes = [C.POINTER(Prob), C.c_double, C.c_int, _dp, _dp, C.c_double, C.c_int,
+                                C.c_int, C.c_int, C.POINTER(C.c_int), _dp]
+        L.orc_sdirk2_ls.restype = C.c_int
+        L.orc_sdirk2_ls.argtypes = [C.POINTER(Prob), C.c_double, C.c_double, C.c_int, C.c_double,
+                                    C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp,
+                                    C.POINTER(C.c_long)]
         L.orc_nthreads.restype = C.c_int
         _lib = L
     return _lib
@@ -238,6 +248,32 @@ class Problem:
         rel = C.c_double()
         it = lib().orc_pcg(self.p, gamma, int(jacobi), dptr(b), dptr(x), tol, maxit, C.byref(rel))
         return x, it, rel.value
+
+    def pcg_generic(self, gamma, b, tol=1e-8, maxl=10000, jacobi=True):
+        """SUNLinSol_PCG through callbacks: (x, status, iterations, relative residual)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = self.field()
+        it, rel = C.c_int(), C.c_double()
+        rc = lib().orc_pcg_generic(self.p, gamma, int(jacobi), dptr(b), dptr(x), tol, maxl,
+                                   C.byref(it), C.byref(rel))
+        return x, rc, it.value, rel.value
+
+    def spgmr(self, gamma, b, tol=1e-8, maxl=20, max_restarts=0, gstype=1, jacobi=True):
+        """SUNLinSol_SPGMR: (x, status, iterations, relative residual estimate)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = self.field()
+        it, rel = C.c_int(), C.c_double()
+        rc = lib().orc_spgmr(self.p, gamma, int(jacobi), dptr(b), dptr(x), tol, maxl, max_restarts,
+                             gstype, C.byref(it), C.byref(rel))
+        return x, rc, it.value, rel.value
+
+    def sdirk2_ls(self, y0, t0, h, nsteps, tol=1e-10, ls=1, maxl=20, max_restarts=0, gstype=1,
+                  jacobi=True):
+        y = np.array(y0, dtype=np.float64)
+        it = C.c_long()
+        lib().orc_sdirk2_ls(self.p, t0, h, nsteps, tol, ls, maxl, max_restarts, gstype, int(jacobi),
+                            dptr(y), C.byref(it))
+        return y, it.value
 
     def sdirk2(self, y0, t0, h, nsteps, tol=1e-10, maxit=10000):
         y = np.array(y0, dtype=np.float64)

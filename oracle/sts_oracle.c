@@ -1313,6 +1313,324 @@ int orc_sdirk2(const orc_prob* p, double t0, double h, int nsteps, double tol, i
   return 0;
 }
 
+static void v_linsum(long n, double a, const double* x, double b, const double* y, double* z)
+{
+  for (long k = 0; k < n; ++k) z[k] = fma(a, x[k], b * y[k]);
+}
+static void v_scale(long n, double c, const double* x, double* z)
+{
+  for (long k = 0; k < n; ++k) z[k] = c * x[k];
+}
+static void v_lincomb(long n, int nv, const double* cf, const double** X, double* z)
+{
+  for (long k = 0; k < n; ++k)
+  {
+    double acc = cf[0] * X[0][k];
+    for (int v = 1; v < nv; ++v) acc = fma(cf[v], X[v][k], acc);
+    z[k] = acc;
+  }
+}
+
+/* ------------------------------------------------------------------------------------
+ * Generic Krylov solvers of the SUNLinSol_PCG / SUNLinSol_SPGMR interface
+ * (diffusion_2D/main.cpp:209-218) on (I - gamma A) x = b with the Jacobi preconditioner,
+ * restated in the exact operation sequence of the product's callback path: ATimes
+ * z = fma(1, v, (-gamma) (A v)) (N_VLinearSum after J*v), PSolve z = D r, LinearSum
+ * z = fma(a, x, b y), Scale z = c x, LinearCombination acc = c0 x0 then fma(c_k, x_k, acc),
+ * exact dot products; small dense algebra in plain double arithmetic. Dirichlet kinds only.
+ * ----------------------------------------------------------------------------------*/
+typedef struct {
+  const orc_prob* p;
+  double gamma, D;
+  int jacobi;
+  double* tmp;
+} gen_op;
+
+static void gen_atimes(const gen_op* o, const double* v, double* z)
+{
+  long n = (long)o->p->nx * o->p->ny;
+  orc_apply_A(o->p, v, o->tmp);
+  v_linsum(n, 1.0, v, -o->gamma, o->tmp, z);
+}
+
+/* z = P^-1 r (Jacobi) or z = r when unpreconditioned (PCG copies with LinearSum(1, r, 0, r)) */
+static void gen_psolve(const gen_op* o, const double* r, double* z, int copy_form)
+{
+  long n = (long)o->p->nx * o->p->ny;
+  if (o->jacobi)
+    for (long k = 0; k < n; ++k) z[k] = o->D * r[k];
+  else if (copy_form) v_linsum(n, 1.0, r, 0.0, r, z);
+  else memcpy(z, r, n * sizeof(double));
+}
+
+/* SUNLinSol_PCG through callbacks, x0 = 0, stop when ||r|| <= tol ||b|| (0 / 1 = converged /
+ * not within maxl iterations) */
+int orc_pcg_generic(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol,
+                    int maxl, int* iters, double* relres)
+{
+  long n = (long)p->nx * p->ny;
+  gen_op o = {p, gamma, 1.0 / (1.0 - gamma * p->cc), jacobi, (double*)malloc(n * sizeof(double))};
+  double* r  = (double*)malloc(n * sizeof(double));
+  double* z  = (double*)malloc(n * sizeof(double));
+  double* pv = (double*)malloc(n * sizeof(double));
+  double* Ap = (double*)malloc(n * sizeof(double));
+  int ret = 1;
+  *iters = 0;
+  *relres = 0.0;
+  for (long k = 0; k < n; ++k) x[k] = 0.0;
+  v_linsum(n, 1.0, b, 0.0, b, r);
+  double bnorm = sqrt(orc_xdot(b, b, n));
+  if (!(bnorm > 0.0))
+  {
+    ret = 0;
+    goto out;
+  }
+  gen_psolve(&o, r, z, 1);
+  double rz = orc_xdot(r, z, n);
+  v_linsum(n, 1.0, z, 0.0, z, pv);
+  for (int it = 1; it <= maxl; ++it)
+  {
+    gen_atimes(&o, pv, Ap);
+    double pq    = orc_xdot(pv, Ap, n);
+    double alpha = rz / pq;
+    v_linsum(n, alpha, pv, 1.0, x, x);
+    v_linsum(n, -alpha, Ap, 1.0, r, r);
+    double rr = orc_xdot(r, r, n);
+    *iters    = it;
+    *relres   = sqrt(rr) / bnorm;
+    if (sqrt(rr) <= tol * bnorm)
+    {
+      ret = 0;
+      goto out;
+    }
+    gen_psolve(&o, r, z, 1);
+    double rzn  = orc_xdot(r, z, n);
+    double beta = rzn / rz;
+    rz          = rzn;
+    v_linsum(n, 1.0, z, beta, pv, pv);
+  }
+out:
+  free(o.tmp);
+  free(r);
+  free(z);
+  free(pv);
+  free(Ap);
+  return ret;
+}
+
+static void orc_givens(double a, double b, double* c, double* s)
+{
+  if (b == 0.0)
+  {
+    *c = 1.0;
+    *s = 0.0;
+  }
+  else if (fabs(b) > fabs(a))
+  {
+    double t = a / b;
+    *s       = 1.0 / sqrt(1.0 + t * t);
+    *c       = *s * t;
+  }
+  else
+  {
+    double t = b / a;
+    *c       = 1.0 / sqrt(1.0 + t * t);
+    *s       = *c * t;
+  }
+}
+
+/* SUNLinSol_SPGMR: restarted GMRES(maxl) with right preconditioning (Saad & Schultz 1986),
+ * x0 = 0, Arnoldi by modified Gram-Schmidt (gstype 1) or classical Gram-Schmidt with one
+ * re-orthogonalisation pass (gstype 2), Givens rotations; stop when the residual estimate
+ * |g_{j+1}| <= tol ||b||; restart from the true residual. Returns 0 / 1 as orc_pcg_generic. */
+int orc_spgmr(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol, int maxl,
+              int max_restarts, int gstype, int* iters, double* relres)
+{
+  long n  = (long)p->nx * p->ny;
+  int m   = maxl;
+  gen_op o = {p, gamma, 1.0 / (1.0 - gamma * p->cc), jacobi, (double*)malloc(n * sizeof(double))};
+  double** V = (double**)malloc((m + 1) * sizeof(double*));
+  for (int k = 0; k <= m; ++k) V[k] = (double*)malloc(n * sizeof(double));
+  double* r  = (double*)malloc(n * sizeof(double));
+  double* z  = (double*)malloc(n * sizeof(double));
+  double* u  = (double*)malloc(n * sizeof(double));
+  double* H  = (double*)calloc((size_t)(m + 1) * m, sizeof(double));
+  double* cs = (double*)malloc(m * sizeof(double));
+  double* sn = (double*)malloc(m * sizeof(double));
+  double* g  = (double*)malloc((m + 1) * sizeof(double));
+  double* y  = (double*)malloc(m * sizeof(double));
+  double* h1 = (double*)malloc((m + 1) * sizeof(double));
+  double* h2 = (double*)malloc((m + 1) * sizeof(double));
+  double* cf = (double*)malloc((m + 2) * sizeof(double));
+  const double** X = (const double**)malloc((m + 2) * sizeof(double*));
+#define HH(i, j) H[(size_t)(i) * m + (j)]
+  int ret = 1;
+  *iters  = 0;
+  *relres = 0.0;
+  for (long k = 0; k < n; ++k) x[k] = 0.0;
+  v_linsum(n, 1.0, b, 0.0, b, r);
+  double bnorm = sqrt(orc_xdot(b, b, n));
+  if (!(bnorm > 0.0))
+  {
+    ret = 0;
+    goto out;
+  }
+  double beta = bnorm;
+  for (int cycle = 0; cycle <= max_restarts; ++cycle)
+  {
+    v_scale(n, 1.0 / beta, r, V[0]);
+    for (int k = 0; k <= m; ++k) g[k] = 0.0;
+    g[0]          = beta;
+    int kc        = 0;
+    int converged = 0;
+    for (int j = 0; j < m; ++j)
+    {
+      double* w = V[j + 1];
+      if (jacobi)
+      {
+        gen_psolve(&o, V[j], z, 0);
+        gen_atimes(&o, z, w);
+      }
+      else gen_atimes(&o, V[j], w);
+      if (gstype == 1)
+        for (int i = 0; i <= j; ++i)
+        {
+          HH(i, j) = orc_xdot(w, V[i], n);
+          v_linsum(n, -HH(i, j), V[i], 1.0, w, w);
+        }
+      else
+      {
+        for (int pass = 0; pass < 2; ++pass)
+        {
+          double* hp = pass ? h2 : h1;
+          for (int i = 0; i <= j; ++i) hp[i] = orc_xdot(w, V[i], n);
+          cf[0] = 1.0;
+          X[0]  = w;
+          for (int i = 0; i <= j; ++i)
+          {
+            cf[i + 1] = -hp[i];
+            X[i + 1]  = V[i];
+          }
+          v_lincomb(n, j + 2, cf, X, w);
+        }
+        for (int i = 0; i <= j; ++i) HH(i, j) = h1[i] + h2[i];
+      }
+      double hn    = sqrt(orc_xdot(w, w, n));
+      HH(j + 1, j) = hn;
+      for (int i = 0; i < j; ++i)
+      {
+        double a = HH(i, j), bb = HH(i + 1, j);
+        HH(i, j)     = cs[i] * a + sn[i] * bb;
+        HH(i + 1, j) = cs[i] * bb - sn[i] * a;
+      }
+      orc_givens(HH(j, j), HH(j + 1, j), &cs[j], &sn[j]);
+      HH(j, j)     = cs[j] * HH(j, j) + sn[j] * HH(j + 1, j);
+      HH(j + 1, j) = 0.0;
+      g[j + 1]     = -sn[j] * g[j];
+      g[j]         = cs[j] * g[j];
+      kc           = j + 1;
+      (*iters)++;
+      *relres = fabs(g[j + 1]) / bnorm;
+      if (hn > 0.0) v_scale(n, 1.0 / hn, w, w);
+      if (fabs(g[j + 1]) <= tol * bnorm || !(hn > 0.0))
+      {
+        converged = fabs(g[j + 1]) <= tol * bnorm;
+        break;
+      }
+    }
+    for (int i = kc - 1; i >= 0; --i)
+    {
+      double sacc = g[i];
+      for (int q = i + 1; q < kc; ++q) sacc = sacc - HH(i, q) * y[q];
+      y[i] = sacc / HH(i, i);
+    }
+    for (int i = 0; i < kc; ++i) X[i] = V[i];
+    v_lincomb(n, kc, y, X, u);
+    if (jacobi)
+    {
+      gen_psolve(&o, u, z, 0);
+      v_linsum(n, 1.0, x, 1.0, z, x);
+    }
+    else v_linsum(n, 1.0, x, 1.0, u, x);
+    if (converged)
+    {
+      ret = 0;
+      goto out;
+    }
+    if (cycle == max_restarts) break;
+    gen_atimes(&o, x, u);
+    v_linsum(n, 1.0, b, -1.0, u, r);
+    beta    = sqrt(orc_xdot(r, r, n));
+    *relres = beta / bnorm;
+    if (beta <= tol * bnorm)
+    {
+      ret = 0;
+      goto out;
+    }
+  }
+#undef HH
+out:
+  free(o.tmp);
+  for (int k = 0; k <= m; ++k) free(V[k]);
+  free(V);
+  free(r);
+  free(z);
+  free(u);
+  free(H);
+  free(cs);
+  free(sn);
+  free(g);
+  free(y);
+  free(h1);
+  free(h2);
+  free(cf);
+  free(X);
+  return ret;
+}
+
+/* SDIRK2 (orc_sdirk2's stages) with a generic solver: ls 0 = PCG, 1 = SPGMR */
+int orc_sdirk2_ls(const orc_prob* p, double t0, double h, int nsteps, double tol, int ls, int maxl,
+                  int max_restarts, int gstype, int jacobi, double* y, long* total_iters)
+{
+  long n     = (long)p->nx * p->ny;
+  double g   = 1.0 - sqrt(0.5);
+  double* f  = (double*)malloc(n * sizeof(double));
+  double* f1 = (double*)malloc(n * sizeof(double));
+  double* rhs = (double*)malloc(n * sizeof(double));
+  double* d   = (double*)malloc(n * sizeof(double));
+  double* Y1  = (double*)malloc(n * sizeof(double));
+  double relres;
+  long iters = 0;
+  double t   = t0;
+  int it;
+  for (int s = 0; s < nsteps; ++s)
+  {
+    double hg = h * g;
+    orc_rhs(p, t + g * h, y, f);
+    v_scale(n, hg, f, rhs);
+    if (ls == 0) orc_pcg_generic(p, hg, jacobi, rhs, d, tol, maxl, &it, &relres);
+    else orc_spgmr(p, hg, jacobi, rhs, d, tol, maxl, max_restarts, gstype, &it, &relres);
+    iters += it;
+    v_linsum(n, 1.0, y, 1.0, d, Y1);
+    orc_rhs(p, t + g * h, Y1, f1);
+    orc_rhs(p, t + h, y, f);
+    double h1g = h * (1.0 - g);
+    v_linsum(n, h1g, f1, hg, f, rhs);
+    if (ls == 0) orc_pcg_generic(p, hg, jacobi, rhs, d, tol, maxl, &it, &relres);
+    else orc_spgmr(p, hg, jacobi, rhs, d, tol, maxl, max_restarts, gstype, &it, &relres);
+    iters += it;
+    v_linsum(n, 1.0, y, 1.0, d, y);
+    t = t0 + (s + 1) * h;
+  }
+  *total_iters = iters;
+  free(f);
+  free(f1);
+  free(rhs);
+  free(d);
+  free(Y1);
+  return 0;
+}
+
 /* ------------------------------------------------------------------------------------
  * SSP methods of LSRKStepCreateSSP (diffusion_2D/main.cpp:250-294), restated from Ketcheson
  * (SIAM J. Sci. Comput. 30, 2008) with this project's embedded estimates, in the exact
@@ -1503,24 +1821,6 @@ int orc_ssp_weights(int type, int s, double* b, double* c, double* w)
 }
 
 /* N_Vector operation restatements (the product's arithmetic) */
-static void v_linsum(long n, double a, const double* x, double b, const double* y, double* z)
-{
-  for (long k = 0; k < n; ++k) z[k] = fma(a, x[k], b * y[k]);
-}
-static void v_scale(long n, double c, const double* x, double* z)
-{
-  for (long k = 0; k < n; ++k) z[k] = c * x[k];
-}
-static void v_lincomb(long n, int nv, const double* cf, const double** X, double* z)
-{
-  for (long k = 0; k < n; ++k)
-  {
-    double acc = cf[0] * X[0][k];
-    for (int v = 1; v < nv; ++v) acc = fma(cf[v], X[v][k], acc);
-    z[k] = acc;
-  }
-}
-
 /* Adaptive SSP integration (type 2 = SSP(s,2), 3 = SSP(s,3), 4 = SSP(10,4)); state in st as
  * for orc_lsrk_evolve. The controller order is the embedding order + 1. */
 int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_state* st, double tout, double* y)

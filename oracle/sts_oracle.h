@@ -96,6 +96,13 @@ int orc_pcg(const orc_prob* p, double gamma, int jacobi, const double* b, double
 int orc_sdirk2(const orc_prob* p, double t0, double h, int nsteps, double tol, int maxit,
                double* y, long* total_iters);
 
+/* generic SUNLinSol_PCG / SUNLinSol_SPGMR on (I - gamma A) x = b, Jacobi or none; SDIRK2 with them */
+int orc_pcg_generic(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol,
+                    int maxl, int* iters, double* relres);
+int orc_spgmr(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol, int maxl,
+              int max_restarts, int gstype, int* iters, double* relres);
+int orc_sdirk2_ls(const orc_prob* p, double t0, double h, int nsteps, double tol, int ls, int maxl,
+                  int max_restarts, int gstype, int jacobi, double* y, long* total_iters);
 int orc_nthreads(void);
 
 #ifdef __cplusplus

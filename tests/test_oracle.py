@@ -325,3 +325,29 @@ def test_ssp_weights_order_and_parity(oracle, stslib, type_, s, order):
         assert abs(np.dot(bh, c ** (k - 1)) - 1.0 / k) < 1e-12, ("embedded", k)
     assert abs(np.dot(bh, c ** (order - 1)) - 1.0 / order) > 1e-6  # embedding exactly one order less
     assert np.abs(w).max() > 1e-6
+
+
+def test_oracle_krylov_solvers_against_dense_solve(oracle):
+    """The oracle's SUNLinSol_SPGMR / generic PCG restatements solve (I - gamma A) x = b to the
+    requested tolerance (checked against a dense solve); GMRES residual estimates equal the
+    true residuals; restarting and both Gram-Schmidt variants converge."""
+    nx, ny, gamma = 20, 16, 2e-3
+    P = oracle.Problem(oracle.MANUFACTURED, nx, ny, kx=1.0, ky=0.2)
+    n = nx * ny
+    M = np.zeros((n, n))
+    for k in range(n):
+        e = np.zeros(n)
+        e[k] = 1.0
+        M[:, k] = e - gamma * P.apply_A(e)
+    b = np.random.default_rng(2).standard_normal(n)
+    xt = np.linalg.solve(M, b)
+    for gs in (1, 2):
+        for maxl, rs in ((60, 0), (7, 40)):
+            x, rc, it, rel = P.spgmr(gamma, b, tol=1e-10, maxl=maxl, max_restarts=rs, gstype=gs)
+            true = np.linalg.norm(b - M @ x) / np.linalg.norm(b)
+            assert rc == 0 and rel <= 1e-10 and abs(true - rel) < 1e-12
+            assert np.linalg.norm(x - xt) / np.linalg.norm(xt) < 1e-8
+    x, rc, it, rel = P.spgmr(gamma, b, tol=1e-14, maxl=3, max_restarts=0)
+    assert rc == 1 and it == 3
+    x, rc, it, rel = P.pcg_generic(gamma, b, tol=1e-10)
+    assert rc == 0 and np.linalg.norm(x - xt) / np.linalg.norm(xt) < 1e-8
