@@ -188,6 +188,7 @@ SIGNATURES = [
     ("STS_NetFree", C.c_int, [C.POINTER(_vp)]),
     ("STS_NetSetWeights", C.c_int, [_vp, _fp]),
     ("STS_NetGetWeights", C.c_int, [_vp, _fp]),
+    ("STS_NetSetTensorPath", C.c_int, [_vp, C.c_int]),
     ("STS_NetApply", C.c_int, [_vp, C.c_int, _vp, _vp, C.c_double, C.c_double, C.c_double,
                                C.c_double]),
     ("STS_NetLossGrad", C.c_int, [_vp, C.c_int, _vp, _vp, C.c_double, C.c_double, C.c_double,
@@ -871,6 +872,11 @@ class Net:
         w = np.ascontiguousarray(w.ravel())
         if lib().STS_NetSetWeights(self.h, w.ctypes.data_as(_fp)) != 0:
             _err("STS_NetSetWeights")
+
+    def set_tensor_path(self, path):
+        """Inference convolutions: 0 = mma.sync (default), 1 = tcgen05 + TMEM + TMA."""
+        if lib().STS_NetSetTensorPath(self.h, int(path)) != 0:
+            _err("STS_NetSetTensorPath")
 
     def apply(self, n, r_ptr, z_ptr, sk, sg, jacobi, scale=1.0):
         if lib().STS_NetApply(self.h, n, r_ptr, z_ptr, sk, sg, jacobi, scale) != 0:

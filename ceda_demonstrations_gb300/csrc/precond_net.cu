@@ -413,6 +413,462 @@ __global__ void __launch_bounds__(NTHR) conv3x3_march_kernel(const __nv_bfloat16
   cp_async_wait0();
 }
 
+// ---------------------------------------------------------------------------------------
+// Inference convolution on the 5th-generation tensor cores (tcgen05 + tensor memory).
+// A CTA of 128 threads owns a 128-column strip and marches down a segment of rows, two output
+// rows per round. Output row y is one UMMA tile D[128 pixels][16 channels] (FP32 in TMEM, 16
+// columns; the round's two rows use columns 0-15 and 16-31) accumulated by nine
+// tcgen05.mma (M 128, N 16, K 16, BF16) over the 3x3 taps, issued by one thread and
+// committed to an mbarrier.
+//   Input: each needed input row (130 pixels with the halo; for the skip-sum loader also the
+// 66 coarse pixels under it; for the residual loader 132 FP64 values) arrives by a 1-D TMA
+// bulk copy into a raw ring, four rows ahead of use, completing on the slot's mbarrier.
+// Threads then convert it into the operand ring: canonical K-major layout without swizzle
+// (core matrices of 8 rows x 8 channels = 128 bytes, the two channel halves 128 bytes apart,
+// 8-row groups 256 bytes apart). UMMA row m stands for output pixel 16 (m % 8) + m / 8, so
+// group g + 1 is group g shifted by one pixel: a staged row keeps 18 groups (pixel q = 16 r + g
+// at row r of group g; the pixels that also fit as group g + 16 of row r - 1 stored twice) and
+// the operand of tap dx is one descriptor moved by dx groups. The conversion's thread-to-
+// (pixel, half) map keeps both the raw reads and the operand writes free of bank conflicts.
+//   Output: each warp reads its 32 TMEM lanes (tcgen05.ld), the epilogue writes the rows (and
+// the pooled row, or the FP64 output) into a staging buffer, and one thread stores it with
+// 1-D TMA bulk stores.
+// Every wait is bounded: a timeout sets the context's error flag, and the CTA waits (bounded)
+// for its copies in flight, frees its tensor memory and returns.
+// ---------------------------------------------------------------------------------------
+namespace tc {
+constexpr int COLS   = 128;            // output pixels per row tile (UMMA M)
+constexpr int GROUPS = COLS / 8 + 2;   // 8-row groups of a staged row (shifts 0, 1, 2)
+constexpr int SLOTB  = GROUPS * 256;   // operand ring slot: one staged row
+constexpr int RING   = 6;              // operand rows: y-1 .. y+2 in use, y+3, y+4 being staged
+constexpr int NRAW   = 6;              // raw rows: two being converted, four in flight
+constexpr int RAWF   = (COLS + 2) * 32; // raw fine row: pixels x0-1 .. x0+128
+constexpr int RAWC   = (COLS / 2 + 2) * 32; // raw coarse row: coarse pixels x0/2-1 .. x0/2+64
+constexpr int RAWR   = (COLS + 4) * 8; // raw FP64 row: columns x0-2 .. x0+129
+constexpr int WB     = 9 * 512;        // B operands of the nine taps (16 x 16 bf16 each)
+constexpr int STAGE  = 2 * COLS * 32 + COLS * 16; // two output rows + one pooled row
+template <int LOAD>
+struct Cfg {
+  static constexpr int RAWB = LOAD == LD_R64 ? RAWR : (LOAD == LD_UPADD ? RAWF + RAWC : RAWF);
+  static constexpr int SMEM = RING * SLOTB + NRAW * RAWB + WB + STAGE;
+};
+// instruction descriptor, kind::f16: D F32, A and B BF16, both K-major, N 16, M 128
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr long long WAIT_LIMIT = 1LL << 26;
+
+// shared-memory matrix descriptor, K-major without swizzle: leading (channel-half) offset 128 B,
+// stride (8-row group) offset 256 B, descriptor version 1 (bit 46)
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr)
+{
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) | (1ull << 46);
+}
+// the output pixel (column offset in the strip) of UMMA row / TMEM lane m
+__device__ __forceinline__ int xpix(int m) { return 16 * (m & 7) + (m >> 3); }
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+               : "=r"(ok)
+               : "r"(bar), "r"(parity)
+               : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+  for (long long i = 0; i < WAIT_LIMIT; ++i)
+    if (mbar_try(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar) { asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// 1-D TMA: global -> shared (completes on bar), shared -> global (bulk group)
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_store(void* dst, uint32_t src, uint32_t bytes)
+{
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate)
+{
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+               "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+               "l"(a), "l"(b), "r"(IDESC), "r"(accumulate)
+               : "memory");
+}
+__device__ __forceinline__ void commit(uint32_t bar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16])
+{
+  uint32_t r[16];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                 "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// TMA of the in-image part of input row `row` into raw slot `raw` (thread 0); bytes issued
+template <int LOAD>
+__device__ __forceinline__ void issue_row(unsigned char* raw, uint32_t bar, const __nv_bfloat16* in, const LoadArgs& la,
+                                          long long img_pix, int H, int W, int row, int x0)
+{
+  if (row < 0 || row >= H)
+  {
+    mbar_arrive(bar); // nothing to copy: the phase completes at once
+    return;
+  }
+  if (LOAD == LD_R64)
+  {
+    const int c0 = max(x0 - 2, 0), c1 = min(x0 + COLS + 2, W); // even bounds: 16-byte aligned
+    const uint32_t bytes = (uint32_t)(c1 - c0) * 8;
+    mbar_expect(bar, bytes);
+    bulk_load(smem_u32(raw + (c0 - (x0 - 2)) * 8), la.r + img_pix + (long long)row * W + c0, bytes, bar);
+  }
+  else
+  {
+    const int c0 = max(x0 - 1, 0), c1 = min(x0 + COLS + 1, W);
+    const uint32_t fb = (uint32_t)(c1 - c0) * 32;
+    uint32_t cb = 0;
+    int k0 = 0, k1 = 0;
+    if (LOAD == LD_UPADD)
+    {
+      k0 = max(x0 / 2 - 1, 0);
+      k1 = min(x0 / 2 + COLS / 2 + 1, W / 2);
+      cb = (uint32_t)(k1 - k0) * 32;
+    }
+    mbar_expect(bar, fb + cb);
+    bulk_load(smem_u32(raw + (c0 - (x0 - 1)) * 32), in + ((long long)row * W + c0) * CH, fb, bar);
+    if (LOAD == LD_UPADD)
+      bulk_load(smem_u32(raw + RAWF + (k0 - (x0 / 2 - 1)) * 32),
+                la.coarse + (img_pix / 4 + (long long)(row / 2) * (W / 2) + k0) * CH, cb, bar);
+  }
+}
+
+// one 16-byte channel half h of staged pixel q of input row `row` from the raw slot, with the
+// roundings of convert_raw (zero outside the image)
+template <int LOAD>
+__device__ __forceinline__ uint4 make_half(const unsigned char* raw, const LoadArgs& la, int H, int W, int row, int x0,
+                                           int q, int h)
+{
+  const int c = x0 - 1 + q;
+  if (row < 0 || row >= H || c < 0 || c >= W) return make_uint4(0, 0, 0, 0);
+  if (LOAD == LD_PLAIN) return *reinterpret_cast<const uint4*>(raw + q * 32 + h * 16);
+  if (LOAD == LD_R64)
+  {
+    if (h) return make_uint4(0, 0, 0, 0);
+    const double rv = *reinterpret_cast<const double*>(raw + (q + 1) * 8);
+    const float xv  = (float)rv * (float)la.scale;
+    __nv_bfloat162 c01 = __halves2bfloat162(__float2bfloat16_rn(xv), __float2bfloat16_rn(xv * la.sk));
+    __nv_bfloat162 c23 = __halves2bfloat162(__float2bfloat16_rn(xv * la.sg), __float2bfloat16_rn(0.f));
+    return make_uint4(*reinterpret_cast<uint32_t*>(&c01), *reinterpret_cast<uint32_t*>(&c23), 0u, 0u);
+  }
+  const uint4 f  = *reinterpret_cast<const uint4*>(raw + q * 32 + h * 16);
+  const uint4 cc = *reinterpret_cast<const uint4*>(raw + RAWF + (c / 2 - (x0 / 2 - 1)) * 32 + h * 16);
+  const __nv_bfloat162* fb = reinterpret_cast<const __nv_bfloat162*>(&f);
+  const __nv_bfloat162* cb = reinterpret_cast<const __nv_bfloat162*>(&cc);
+  uint32_t w[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+  {
+    const float2 a = __bfloat1622float2(fb[k]), b = __bfloat1622float2(cb[k]);
+    __nv_bfloat162 t = __floats2bfloat162_rn(la.cscale * b.x + a.x, la.cscale * b.y + a.y);
+    w[k] = *reinterpret_cast<uint32_t*>(&t);
+  }
+  return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// raw row -> operand slot. Item i = tid + 128 j (j = 0, 1) is (pixel q = 16 r + g, half h) with
+// l = i % 8, p = (i / 8) % 8, g = 4 (i / 64) + l / 2, h = l % 2, r = (l + p) % 8: the eight
+// lanes of a 128-byte phase read 16-byte pieces 16 l bytes apart (mod 128) and write operand
+// rows r that differ, so neither side has bank conflicts. Threads 0-3 also stage pixels 128
+// and 129 (r = 7, g = 16, 17).
+template <int LOAD>
+__device__ __forceinline__ void convert_row(const unsigned char* raw, unsigned char* slot, const LoadArgs& la, int H,
+                                            int W, int row, int x0, int tid)
+{
+#pragma unroll
+  for (int j = 0; j < 2; ++j)
+  {
+    const int i = tid + COLS * j;
+    const int l = i & 7, p = (i >> 3) & 7;
+    const int g = 4 * (i >> 6) + (l >> 1), h = l & 1, r = (l + p) & 7;
+    const int q = 16 * r + g;
+    const uint4 v = make_half<LOAD>(raw, la, H, W, row, x0, q, h);
+    *reinterpret_cast<uint4*>(slot + g * 256 + h * 128 + r * 16) = v;
+    if (g < 2 && r >= 1) *reinterpret_cast<uint4*>(slot + (g + 16) * 256 + h * 128 + (r - 1) * 16) = v;
+  }
+  if (tid < 4)
+  {
+    const int q = COLS + (tid >> 1), h = tid & 1;
+    *reinterpret_cast<uint4*>(slot + (q - 112) * 256 + h * 128 + 7 * 16) = make_half<LOAD>(raw, la, H, W, row, x0, q, h);
+  }
+}
+} // namespace tc
+
+// MODE 0: BF16 NHWC output (POOL: also the 2x2 means of the round's row pair into pout, in the
+// order of pool_kernel); MODE 2: z = (out_scale scale) r + (double)((float)out_scale u),
+// u = c0 + sk c1 + sg c2, as conv_epilogue. wu: the nine taps' B operands (tc_weight_kernel).
+// Segments start on even rows and H is even, so every round has two rows.
+template <int MODE, int LOAD, bool POOL>
+__global__ void __launch_bounds__(tc::COLS) conv3x3_tc_kernel(const __nv_bfloat16* __restrict__ in, int H, int W,
+                                                              const uint4* __restrict__ wu,
+                                                              __nv_bfloat16* __restrict__ out,
+                                                              double* __restrict__ out64, double out_scale, LoadArgs la,
+                                                              int rows, __nv_bfloat16* __restrict__ pout, int* err)
+{
+  using C = tc::Cfg<LOAD>;
+  extern __shared__ __align__(128) unsigned char dsm[];
+  __shared__ uint32_t tbase;
+  __shared__ __align__(8) uint64_t bars[1 + tc::NRAW]; // MMA completion, raw slots
+  unsigned char* ring  = dsm;
+  unsigned char* rawr  = ring + tc::RING * tc::SLOTB;
+  unsigned char* wsm   = rawr + tc::NRAW * C::RAWB;
+  unsigned char* stage = wsm + tc::WB;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int x0 = blockIdx.x * tc::COLS;
+  const int ys = blockIdx.y * rows, ye = min(H, ys + rows);
+  const long long img_pix = (long long)H * W * blockIdx.z;
+  if (LOAD != LD_R64) in += img_pix * CH;
+  if (MODE == 0)
+  {
+    out += img_pix * CH;
+    if (POOL) pout += img_pix / 4 * CH;
+  }
+  else out64 += img_pix;
+  if (ys >= H) return;
+  const int cnt = min(tc::COLS, W - x0); // output pixels of this strip (even)
+  const uint32_t mbar = smem_u32(&bars[0]);
+  auto rawbar  = [&](int r) { return smem_u32(&bars[1 + (r - ys + 1) % tc::NRAW]); };
+  auto rawslot = [&](int r) { return rawr + ((r - ys + 1) % tc::NRAW) * C::RAWB; };
+  auto rawpar  = [&](int r) { return (uint32_t)(((r - ys + 1) / tc::NRAW) & 1); };
+  auto slot    = [&](int r) { return ring + ((r - ys + 1) % tc::RING) * tc::SLOTB; };
+  if (tid == 0)
+  {
+    for (int k = 0; k <= tc::NRAW; ++k) tc::mbar_init(smem_u32(&bars[k]));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // raw rows ys-1 .. ys+4 in flight (rows past ye are never needed)
+  int issued = ys - 2; // last input row whose copy was issued
+  if (tid == 0)
+    for (int r = ys - 1; r <= min(ys + 4, ye); ++r) tc::issue_row<LOAD>(rawslot(r), rawbar(r), in, la, img_pix, H, W, r, x0);
+  issued = min(ys + 4, ye);
+  for (int c = tid; c < 9 * 32; c += tc::COLS) reinterpret_cast<uint4*>(wsm)[c] = wu[c];
+  if (warp == 0)
+  {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tbase)), "r"(32)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  // operand rows ys-1 .. ys+2
+  bool ok = true;
+  int converted = ys - 2; // last input row converted into the operand ring
+  for (int r = ys - 1; r <= min(ys + 2, ye) && ok; ++r)
+  {
+    ok = tc::mbar_wait(rawbar(r), rawpar(r));
+    if (ok)
+    {
+      tc::convert_row<LOAD>(rawslot(r), slot(r), la, H, W, r, x0, tid);
+      converted = r;
+    }
+  }
+  tc::fence_async_smem();
+  tc::fence_before();
+  const bool bad0 = __syncthreads_or(!ok);
+  tc::fence_after();
+  const uint32_t tm    = tbase;
+  const uint32_t taddr = tm + ((uint32_t)(warp * 32) << 16);
+  const int px         = tc::xpix(tid); // this thread's output pixel offset (TMEM lane tid)
+  const int gx         = x0 + px;
+  bool failed          = bad0;
+  int round            = 0;
+  for (int y = ys; y < ye && !failed; y += 2, ++round)
+  {
+    const bool two = y + 1 < ye;
+    // 1. MMAs of rows y, y+1 (operand rows y-1 .. y+2); the previous round's bulk stores
+    //    have read the staging buffer before it is rewritten below
+    if (tid == 0)
+    {
+#pragma unroll
+      for (int t = 0; t < 9; ++t)
+      {
+        const int dy = t / 3, dx = t % 3;
+        tc::mma(tm, tc::sdesc(smem_u32(slot(y - 1 + dy) + dx * 256)), tc::sdesc(smem_u32(wsm + t * 512)),
+                t > 0 ? 1u : 0u);
+      }
+      if (two)
+#pragma unroll
+        for (int t = 0; t < 9; ++t)
+        {
+          const int dy = t / 3, dx = t % 3;
+          tc::mma(tm + 16, tc::sdesc(smem_u32(slot(y + dy) + dx * 256)), tc::sdesc(smem_u32(wsm + t * 512)),
+                  t > 0 ? 1u : 0u);
+        }
+      tc::commit(mbar);
+      tc::bulk_wait_read();
+    }
+    // 2. stage operand rows y+3, y+4 (their slots held rows y-3, y-2: read by the last round)
+    for (int r = y + 3; r <= min(y + 4, ye) && ok; ++r)
+    {
+      ok = tc::mbar_wait(rawbar(r), rawpar(r));
+      if (ok)
+      {
+        tc::convert_row<LOAD>(rawslot(r), slot(r), la, H, W, r, x0, tid);
+        converted = r;
+      }
+    }
+    tc::fence_async_smem();
+    if (__syncthreads_or(!ok))
+    {
+      failed = true;
+      break;
+    }
+    // 3. raw rows y+5, y+6 into the slots of the rows just converted
+    if (tid == 0)
+      for (int r = issued + 1; r <= min(y + 6, ye); ++r)
+        tc::issue_row<LOAD>(rawslot(r), rawbar(r), in, la, img_pix, H, W, r, x0);
+    issued = max(issued, min(y + 6, ye));
+    // 4. results of rows y, y+1 into the staging buffer
+    ok = tc::mbar_wait(mbar, (uint32_t)(round & 1));
+    tc::fence_after();
+    float a0[16], a1[16];
+    tc::ld16(taddr, a0);
+    if (two) tc::ld16(taddr + 16, a1);
+    if (MODE == 0)
+    {
+      uint32_t o0[8], o1[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+      {
+        __nv_bfloat162 v0 = __floats2bfloat162_rn(a0[2 * k], a0[2 * k + 1]);
+        __nv_bfloat162 v1 = __floats2bfloat162_rn(a1[2 * k], a1[2 * k + 1]);
+        o0[k] = *reinterpret_cast<uint32_t*>(&v0);
+        o1[k] = *reinterpret_cast<uint32_t*>(&v1);
+      }
+      uint4* s0 = reinterpret_cast<uint4*>(stage + px * 32);
+      uint4* s1 = reinterpret_cast<uint4*>(stage + tc::COLS * 32 + px * 32);
+      s0[0] = make_uint4(o0[0], o0[1], o0[2], o0[3]);
+      s0[1] = make_uint4(o0[4], o0[5], o0[6], o0[7]);
+      s1[0] = make_uint4(o1[0], o1[1], o1[2], o1[3]);
+      s1[1] = make_uint4(o1[4], o1[5], o1[6], o1[7]);
+      if (POOL)
+      {
+        // pixel px + 1 is lane tid + 8 (the next group), in the same warp for even px
+        uint32_t n0[8], n1[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+        {
+          n0[k] = __shfl_down_sync(0xffffffffu, o0[k], 8);
+          n1[k] = __shfl_down_sync(0xffffffffu, o1[k], 8);
+        }
+        if (!(px & 1))
+        {
+          uint32_t q[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+          {
+            const float2 fa = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&o0[k]));
+            const float2 fb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&n0[k]));
+            const float2 fc = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&o1[k]));
+            const float2 fd = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&n1[k]));
+            __nv_bfloat162 t = __floats2bfloat162_rn(0.25f * (fa.x + fb.x + fc.x + fd.x),
+                                                     0.25f * (fa.y + fb.y + fc.y + fd.y));
+            q[k] = *reinterpret_cast<uint32_t*>(&t);
+          }
+          uint4* sp = reinterpret_cast<uint4*>(stage + 2 * tc::COLS * 32 + (px / 2) * 32);
+          sp[0]     = make_uint4(q[0], q[1], q[2], q[3]);
+          sp[1]     = make_uint4(q[4], q[5], q[6], q[7]);
+        }
+      }
+    }
+    else if (gx < W)
+    {
+      double* s64 = reinterpret_cast<double*>(stage);
+      const float u0 = a0[0] + la.sk * a0[1] + la.sg * a0[2];
+      s64[px]        = __fma_rn(out_scale * la.scale, la.r[img_pix + (long long)y * W + gx], (double)((float)out_scale * u0));
+      if (two)
+      {
+        const float u1     = a1[0] + la.sk * a1[1] + la.sg * a1[2];
+        s64[tc::COLS + px] = __fma_rn(out_scale * la.scale, la.r[img_pix + (long long)(y + 1) * W + gx],
+                                      (double)((float)out_scale * u1));
+      }
+    }
+    tc::fence_async_smem();
+    tc::fence_before();
+    if (__syncthreads_or(!ok))
+    {
+      failed = true;
+      break;
+    }
+    tc::fence_after();
+    // 5. bulk stores of the staged rows
+    if (tid == 0)
+    {
+      if (MODE == 0)
+      {
+        tc::bulk_store(out + ((long long)y * W + x0) * CH, smem_u32(stage), (uint32_t)cnt * 32);
+        if (two) tc::bulk_store(out + ((long long)(y + 1) * W + x0) * CH, smem_u32(stage + tc::COLS * 32), (uint32_t)cnt * 32);
+        if (POOL)
+          tc::bulk_store(pout + ((long long)(y / 2) * (W / 2) + x0 / 2) * CH, smem_u32(stage + 2 * tc::COLS * 32),
+                         (uint32_t)cnt * 16);
+      }
+      else
+      {
+        tc::bulk_store(out64 + (long long)y * W + x0, smem_u32(stage), (uint32_t)cnt * 8);
+        if (two) tc::bulk_store(out64 + (long long)(y + 1) * W + x0, smem_u32(stage + tc::COLS * 8), (uint32_t)cnt * 8);
+      }
+      tc::bulk_commit();
+    }
+  }
+  if (failed)
+  {
+    if (tid == 0) atomicExch(err, 2);
+    // bounded waits for the copies and MMAs still in flight before the memory is released
+    for (int r = converted + 1; r <= issued; ++r) tc::mbar_wait(rawbar(r), rawpar(r));
+    tc::mbar_wait(mbar, (uint32_t)(round & 1));
+  }
+  if (tid == 0) tc::bulk_wait_all();
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(32) : "memory");
+}
+
+// The nine taps' B operands (B[n = output channel][k = input channel], K-major without
+// swizzle: byte t*512 + (n/8)*256 + (k/8)*128 + (n%8)*16 + (k%8)*2) of a layer, forward or
+// transposed (swapped channels, flipped taps), as frag_kernel's weights
+__global__ void tc_weight_kernel(const float* __restrict__ W, __nv_bfloat16* __restrict__ wu, int transpose)
+{
+  const int e = blockIdx.x * blockDim.x + threadIdx.x; // 0 .. 9*256
+  if (e >= 9 * 256) return;
+  const int t = e >> 8, n = (e >> 4) & 15, k = e & 15;
+  const float v = transpose ? W[(k * CH + n) * 9 + (8 - t)] : W[(n * CH + k) * 9 + t];
+  wu[t * 256 + (n >> 3) * 128 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7)] = __float2bfloat16_rn(v);
+}
+
 // Level transfers, one thread per coarse (pool) or fine (upsampling) pixel and all 16 channels
 // as two 16-byte vectors; H, W are the fine level's (H counts the rows of all stacked images).
 // Index arithmetic in 32 bits (at most 2^31 pixels per level).
@@ -738,6 +1194,9 @@ struct STS_Net_ {
   float *m = nullptr, *v = nullptr, *g = nullptr;
   uint2* wf       = nullptr; // forward fragments, 9 x 576
   uint2* wt       = nullptr; // input-gradient fragments
+  __nv_bfloat16* wu  = nullptr; // forward UMMA B operands (tcgen05 inference), 9 x 256 per layer
+  __nv_bfloat16* wut = nullptr; // transposed UMMA B operands
+  int tensor_path    = 0;       // inference convolutions: 0 mma.sync (faster here), 1 tcgen05 + TMEM
   net::Level L[4];
   double* z       = nullptr; // FP64 output at the finest level
   double* dacc    = nullptr;
@@ -820,6 +1279,8 @@ static void refresh_frags(STS_Net nt)
   {
     net::frag_kernel<<<3, 256, 0, st>>>(nt->w + l * WSZ, nt->wf + l * 576, 0);
     net::frag_kernel<<<3, 256, 0, st>>>(nt->w + l * WSZ, nt->wt + l * 576, 1);
+    net::tc_weight_kernel<<<9, 256, 0, st>>>(nt->w + l * WSZ, nt->wu + l * 9 * 256, 0);
+    net::tc_weight_kernel<<<9, 256, 0, st>>>(nt->w + l * WSZ, nt->wut + l * 9 * 256, 1);
   }
 }
 
@@ -841,6 +1302,8 @@ extern "C" STS_Net STS_NetCreate(STS_Context ctx, int nmax, unsigned long long s
   nt->v    = (float*)dalloc(NLAYER * WSZ * 4, &ok);
   nt->g    = (float*)dalloc(NLAYER * WSZ * 4, &ok);
   nt->wf   = (uint2*)dalloc(NLAYER * 576 * 8, &ok);
+  nt->wu   = (__nv_bfloat16*)dalloc(NLAYER * 9 * 256 * 2, &ok);
+  nt->wut  = (__nv_bfloat16*)dalloc(NLAYER * 9 * 256 * 2, &ok);
   nt->wt   = (uint2*)dalloc(NLAYER * 576 * 8, &ok);
   nt->dacc = (double*)dalloc(8, &ok);
   if (!ok || !ensure_capacity(nt, (long long)nmax * nmax))
@@ -891,6 +1354,8 @@ extern "C" int STS_NetFree(STS_Net* pn)
   cudaFree(nt->v);
   cudaFree(nt->g);
   cudaFree(nt->wf);
+  cudaFree(nt->wu);
+  cudaFree(nt->wut);
   cudaFree(nt->wt);
   cudaFree(nt->dacc);
   cudaFree(nt->mb);
@@ -953,6 +1418,40 @@ static void conv_launch(STS_Net nt, const __nv_bfloat16* in, int n, int nimg, co
   const MarchGrid m = march_grid(nt, n, nimg);
   net::conv3x3_march_kernel<MODE, LOAD, NARROW, POOL><<<m.grid, net::NTHR, 0, nt->ctx->stream>>>(
       in, n, n, frags, out, out64, out_scale, meta, la, m.rows, pout);
+}
+
+// tcgen05 inference convolution: 128-column strips, row segments sized so that the grid is one
+// full wave of resident CTAs (even, so the fused pooling's row pairs stay in one CTA)
+template <int MODE, int LOAD = net::LD_PLAIN, bool POOL = false>
+static void conv_tc(STS_Net nt, const __nv_bfloat16* in, int n, const __nv_bfloat16* wu, __nv_bfloat16* out,
+                    double* out64, double out_scale, const net::LoadArgs& la, __nv_bfloat16* pout = nullptr)
+{
+  static int occ = 0; // resident CTAs per SM
+  if (!occ)
+  {
+    cudaFuncSetAttribute(net::conv3x3_tc_kernel<MODE, LOAD, POOL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         net::tc::Cfg<LOAD>::SMEM);
+    // from the kernel's registers and shared memory (the runtime's occupancy query reports one
+    // CTA per SM for kernels that allocate tensor memory; 32 TMEM columns per CTA allow 16)
+    cudaFuncAttributes fa;
+    occ = 4;
+    if (cudaFuncGetAttributes(&fa, net::conv3x3_tc_kernel<MODE, LOAD, POOL>) == cudaSuccess)
+    {
+      const int regs = (fa.numRegs + 7) / 8 * 8;
+      const int by_regs = regs > 0 ? 65536 / (regs * net::tc::COLS) : 16;
+      const int by_smem = (227 * 1024) / (net::tc::Cfg<LOAD>::SMEM + (int)fa.sharedSizeBytes + 1024);
+      occ               = std::max(1, std::min(std::min(by_regs, by_smem), 16));
+    }
+  }
+  const int strips     = (n + net::tc::COLS - 1) / net::tc::COLS;
+  const long long want = (long long)occ * nt->ctx->num_sms; // one full wave
+  long long segs       = (want + strips - 1) / strips;
+  int rows             = (int)((n + segs - 1) / segs);
+  if (rows < 8) rows = 8;
+  rows += rows & 1;
+  const dim3 grid((unsigned)strips, (unsigned)((n + rows - 1) / rows), 1);
+  net::conv3x3_tc_kernel<MODE, LOAD, POOL><<<grid, net::tc::COLS, net::tc::Cfg<LOAD>::SMEM, nt->ctx->stream>>>(
+      in, n, n, reinterpret_cast<const uint4*>(wu), out, out64, out_scale, la, rows, pout, nt->ctx->d_err);
 }
 
 // convolution (or transposed convolution) with one layer's weights; W_in forward reads the
@@ -1020,21 +1519,42 @@ static void net_forward(STS_Net nt, int n, int nimg, const T* r, double scale, f
 static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, float sk, float sg, double out_scale,
                               double* zout)
 {
-  cudaStream_t st = nt->ctx->stream;
-  net::Level* L   = nt->L;
+  net::Level* L = nt->L;
   net::LoadArgs la;
   la.r     = r;
   la.scale = scale;
   la.sk    = sk;
   la.sg    = sg;
+  net::LoadArgs lu;
+  lu.cscale = 0.25f;
+  if (nt->tensor_path == 1)
+  { // tcgen05 + TMEM
+    const net::LoadArgs lp;
+    const int WL = 9 * 256;
+    conv_tc<0, net::LD_R64, true>(nt, nullptr, n, nt->wu + net::L_IN * WL, L[0].h, nullptr, 0.0, la, L[1].p); // h0, p0
+    conv_tc<0, net::LD_PLAIN, true>(nt, L[1].p, n / 2, nt->wu + net::L_1 * WL, L[1].h, nullptr, 0.0, lp, L[2].p); // h1, p1
+    conv_tc<0, net::LD_PLAIN, true>(nt, L[2].p, n / 4, nt->wu + net::L_2 * WL, L[2].h, nullptr, 0.0, lp, L[3].p); // h2, p2
+    conv_tc<0>(nt, L[3].p, n / 8, nt->wu + net::L_3 * WL, L[3].h, nullptr, 0.0, lp);                             // h3
+    conv_tc<0>(nt, L[3].h, n / 8, nt->wut + net::L_3 * WL, L[3].y, nullptr, 0.0, lp);                            // y3
+    lu.coarse = L[3].y;
+    conv_tc<0, net::LD_UPADD>(nt, L[2].h, n / 4, nt->wut + net::L_2 * WL, L[2].y, nullptr, 0.0, lu); // y2
+    lu.coarse = L[2].y;
+    conv_tc<0, net::LD_UPADD>(nt, L[1].h, n / 2, nt->wut + net::L_1 * WL, L[1].y, nullptr, 0.0, lu); // y1
+    lu.coarse = L[1].y;
+    lu.r      = r;
+    lu.scale  = scale;
+    lu.sk     = sk;
+    lu.sg     = sg;
+    conv_tc<2, net::LD_UPADD>(nt, L[0].h, n, nt->wut + net::L_IN * WL, nullptr, zout, out_scale, lu); // z
+    return;
+  }
+  // mma.sync path (the training kernels)
   conv_launch<0, net::LD_R64, true, true>(nt, nullptr, n, 1, nt->wf + net::L_IN * 576, L[0].h, nullptr, 0.0, nullptr, la,
                                           L[1].p);                                     // h0, p0
   conv(nt, L[1].p, n / 2, 1, net::L_1, false, L[1].h, L[2].p);                         // h1, p1
   conv(nt, L[2].p, n / 4, 1, net::L_2, false, L[2].h, L[3].p);                         // h2, p2
   conv(nt, L[3].p, n / 8, 1, net::L_3, false, L[3].h);                                                // h3
   conv(nt, L[3].h, n / 8, 1, net::L_3, true, L[3].y);                                                 // y3
-  net::LoadArgs lu;
-  lu.cscale = 0.25f;
   lu.coarse = L[3].y;
   conv_launch<0, net::LD_UPADD>(nt, L[2].h, n / 4, 1, nt->wt + net::L_2 * 576, L[2].y, nullptr, 0.0, nullptr, lu); // y2
   lu.coarse = L[2].y;
@@ -1109,6 +1629,13 @@ static bool net_size_ok(STS_Net nt, int n)
 }
 
 // z = M r for one n x n residual (device pointers): z = jacobi * net(scale r) / scale
+extern "C" int STS_NetSetTensorPath(STS_Net nt, int path)
+{
+  if (!nt || (path != 0 && path != 1)) return -1;
+  nt->tensor_path = path;
+  return 0;
+}
+
 extern "C" int STS_NetApply(STS_Net nt, int n, const double* r, double* z, double sk, double sg, double jacobi,
                             double scale)
 {
@@ -1588,6 +2115,13 @@ extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b,
       }
       if (!STS_CUDA_OK(cudaGraphLaunch(ge, st)) || !STS_CUDA_OK(cudaStreamSynchronize(st)))
       {
+        ret = -1;
+        break;
+      }
+      if (*(volatile int*)ctx->h_err)
+      { // a tensor-core convolution's bounded wait timed out
+        *ctx->h_err = 0;
+        sts_set_error("STS_FCGSolve: a tensor-core wait timed out");
         ret = -1;
         break;
       }

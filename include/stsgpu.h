@@ -365,6 +365,10 @@ int STS_NetFree(STS_Net* net);
 int STS_NetSetWeights(STS_Net net, const float* w);
 int STS_NetGetWeights(STS_Net net, float* w);
 /* z = jacobi * (r + E^T E (scale r) / scale) on device arrays of n x n doubles */
+/* inference convolutions: 0 = the row-marching mma.sync kernels the training uses (default,
+ * the faster of the two at 2048^2), 1 = tcgen05 tensor cores with TMEM accumulators, 1-D TMA
+ * bulk loads and stores; both compute the same network */
+int STS_NetSetTensorPath(STS_Net net, int path);
 int STS_NetApply(STS_Net net, int n, const double* r, double* z, double sk, double sg, double jacobi,
                  double scale);
 /* one sample (scale 1): loss = 0.5 (z - e)^T M (z - e) / (e^T M e) with M = I - gamma A on the

@@ -58,6 +58,27 @@ def test_forward_matches_oracle(ctx, weights, n, sk, sg):
     assert np.array_equal(zv.numpy().reshape(n, n), z)
 
 
+@pytest.mark.parametrize("n", [128, 384])
+def test_tcgen05_and_mma_sync_paths_agree(ctx, weights, n):
+    """The inference convolutions on tcgen05 (TMEM accumulators, 128-pixel UMMA tiles) and
+    on mma.sync compute the same network: both within the oracle tolerance, and within BF16
+    rounding of each other (the accumulation order inside the tensor cores differs)."""
+    rng = np.random.default_rng(n + 1)
+    r = rng.standard_normal((n, n))
+    net = sts.Net(ctx, 384, seed=0)
+    net.set_weights(weights)
+    rv = sts.NVector.from_numpy(ctx, r)
+    zv = sts.NVector(ctx, n * n)
+    out = []
+    for path in (1, 0):
+        net.set_tensor_path(path)
+        net.apply(n, rv.ptr, zv.ptr, 0.4, -0.2, 0.5, 1.0)
+        out.append(zv.numpy().reshape(n, n))
+    zref, _ = convnet.forward(weights, r, 0.4, -0.2, 0.5)
+    assert _rel(out[0], zref) < FWD_TOL and _rel(out[1], zref) < FWD_TOL
+    assert _rel(out[0], out[1]) < 1e-2
+
+
 def test_weights_round_trip(ctx, weights):
     net = sts.Net(ctx, 64, seed=1)
     net.set_weights(weights)
