@@ -496,6 +496,35 @@ template <int NT, int CL>
 static bool launch_group(const STS_Batch b, const BatchParams& prm, const int* order, int count, int* queue, int grid,
                          cudaStream_t st)
 {
+  if constexpr (CL > 8)
+  { // 16-CTA clusters are a non-portable size: opt in, and launch only if one fits
+    static int fits = -1;
+    if (fits < 0)
+    {
+      fits = 0;
+      if (cudaFuncSetAttribute(batch_kernel<NT, CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
+      {
+        cudaLaunchConfig_t q = {};
+        q.gridDim            = dim3(CL, 1, 1);
+        q.blockDim           = dim3(NT, 1, 1);
+        cudaLaunchAttribute qa[1];
+        qa[0].id               = cudaLaunchAttributeClusterDimension;
+        qa[0].val.clusterDim.x = CL;
+        qa[0].val.clusterDim.y = 1;
+        qa[0].val.clusterDim.z = 1;
+        q.attrs                = qa;
+        q.numAttrs             = 1;
+        int nc                 = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, batch_kernel<NT, CL>, &q) == cudaSuccess && nc > 0) fits = 1;
+      }
+      cudaGetLastError();
+    }
+    if (!fits)
+    {
+      sts_set_error("STS_Batch: %d-CTA clusters of %d threads cannot be scheduled", CL, NT);
+      return false;
+    }
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim            = dim3((unsigned)grid, 1, 1);
   cfg.blockDim           = dim3(NT, 1, 1);
@@ -521,6 +550,7 @@ static bool launch_cl(const STS_Batch b, const BatchParams& prm, int cl, const i
   case 2: return launch_group<NT, 2>(b, prm, order, count, queue, grid, st);
   case 4: return launch_group<NT, 4>(b, prm, order, count, queue, grid, st);
   case 8: return launch_group<NT, 8>(b, prm, order, count, queue, grid, st);
+  case 16: return launch_group<NT, 16>(b, prm, order, count, queue, grid, st);
   default: return launch_group<NT, 1>(b, prm, order, count, queue, grid, st);
   }
 }
@@ -802,7 +832,8 @@ extern "C" int STS_BatchSetLaunch(STS_Batch b, int threads, int ctas_per_sm)
 
 extern "C" int STS_BatchSetCluster(STS_Batch b, int cluster, int big_n)
 {
-  if (!b || (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8) || big_n < 2) return STS_ILL_INPUT;
+  if (!b || (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16) || big_n < 2)
+    return STS_ILL_INPUT;
   ctx_activate(b->ctx);
   b->cluster = cluster;
   b->big_n   = big_n;
@@ -832,8 +863,8 @@ extern "C" int STS_BatchAutotune(STS_Batch b, double tf_probe, int method, doubl
   cudaMemcpyAsync(save, b->y, b->total * sizeof(double), cudaMemcpyDeviceToDevice, b->ctx->stream);
   // {threads per CTA, CTAs per SM, cluster size of the large-instance group}
   // (the kernel is compiled for 1024 resident threads per SM: 64 registers per thread)
-  const int shapes[][3] = {{256, 4, 1}, {512, 2, 1}, {256, 4, 4}, {512, 2, 4},
-                           {256, 4, 8}, {512, 2, 8}, {512, 1, 8}};
+  const int shapes[][3] = {{256, 4, 1}, {512, 2, 1}, {256, 4, 4}, {512, 2, 4}, {256, 4, 8},
+                           {512, 2, 8}, {512, 1, 8}, {256, 4, 16}, {512, 2, 16}};
   double best           = 1e30;
   int bt = b->block, bc = b->ctas_per_sm, bcl = b->cluster;
   for (auto& sh : shapes)

@@ -345,8 +345,9 @@ int STS_BatchSetLaunch(STS_Batch b, int threads, int ctas_per_sm);
 int STS_BatchAutotune(STS_Batch b, double tf_probe, int method, double rtol, double atol,
                       int smax, int* threads, int* ctas_per_sm, double* ms_best);
 /* instances with n >= big_n are integrated by thread-block clusters of `cluster` CTAs (1, 2,
- * 4 or 8; rows split between the CTAs, cluster barriers between sweeps, the exact reductions
- * combined through distributed shared memory), concurrently with the single-CTA group */
+ * 4, 8, or 16 where the device schedules that non-portable size; rows split between the
+ * CTAs, cluster barriers between sweeps, the exact reductions combined through distributed
+ * shared memory), concurrently with the single-CTA group */
 int STS_BatchSetCluster(STS_Batch b, int cluster, int big_n);
 int STS_BatchGetLaunch(STS_Batch b, int* threads, int* ctas_per_sm, int* cluster, int* big_n);
 

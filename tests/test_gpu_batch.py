@@ -40,10 +40,16 @@ def test_batch_launch_shapes_agree_bitwise(ctx, stslib):
     inst = small_batch(stslib, count=12, seed=3)
     outs = []
     for threads, cps, cluster in ((256, 1, 1), (256, 2, 1), (512, 1, 1), (256, 2, 2), (512, 2, 4),
-                                  (256, 4, 8)):
+                                  (256, 4, 8), (256, 4, 16)):
         B = stslib.Batch(ctx, inst)
         assert B.set_launch(threads, cps, cluster, big_n=32) == 0
-        B.evolve(0.005, method=stslib.RKC, rtol=1e-6, atol=1e-10)
+        try:
+            B.evolve(0.005, method=stslib.RKC, rtol=1e-6, atol=1e-10)
+        except stslib.STSError as e:
+            # a 16-CTA cluster is a non-portable size: the library refuses it where the device
+            # cannot schedule one
+            assert cluster == 16 and "cannot be scheduled" in str(e)
+            continue
         outs.append(B.state())
         assert B.launch() == (threads, cps, cluster, 32)
     for o in outs[1:]:
@@ -68,7 +74,7 @@ def test_batch_autotune_keeps_results(ctx, stslib):
     inst = small_batch(stslib, count=10, seed=5)
     B = stslib.Batch(ctx, inst)
     th, cp, ms = B.autotune(0.001)
-    assert th in (256, 512) and cp in (1, 2, 4) and ms > 0 and B.launch()[2] in (1, 4, 8)
+    assert th in (256, 512) and cp in (1, 2, 4) and ms > 0 and B.launch()[2] in (1, 4, 8, 16)
     B.evolve(0.005)
     C = stslib.Batch(ctx, inst)
     C.set_launch(th, cp)
