@@ -609,8 +609,8 @@ def main():
     ap.add_argument("--precond-crop", type=int, default=128)
     ap.add_argument("--precond-crops", type=int, default=4)
     ap.add_argument("--precond-every", type=int, default=1)
-    ap.add_argument("--precond-pairs", type=int, default=51200)
-    ap.add_argument("--precond-epochs", type=int, default=8)
+    ap.add_argument("--precond-pairs", type=int, default=102400)
+    ap.add_argument("--precond-epochs", type=int, default=24)
     ap.add_argument("--precond-batch", type=int, default=32)
     ap.add_argument("--precond-eval", type=int, default=8)
     args = ap.parse_args()
