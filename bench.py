@@ -208,29 +208,30 @@ def run_gpu(args):
     # end to end (mixed): state in from pinned host memory, one step, state back out
     import torch
     I = res[True]["I"]
-    host_in = torch.empty(N2, dtype=torch.float64, pin_memory=True)
-    host_out = torch.empty(N2, dtype=torch.float64, pin_memory=True)
-    host_in.numpy()[:] = res[True]["y"]
+    # two pinned host buffers in turn: step k reads buffer k % 2 and writes the other, which
+    # is the next step's input
+    host = [torch.empty(N2, dtype=torch.float64, pin_memory=True) for _ in range(2)]
+    host[0].numpy()[:] = res[True]["y"]
     yv = G.vector()
     L = sts.lib()
-    pin = C.cast(host_in.data_ptr(), sts._dp)
-    pout = C.cast(host_out.data_ptr(), sts._dp)
+    hp = [C.cast(h.data_ptr(), sts._dp) for h in host]
     t_cur = res[True]["t"]
+    k = 0
     for _ in range(2):
-        L.N_VCopyFromHost_Sts(yv.h, pin)
+        L.N_VCopyFromHost_Sts(yv.h, hp[k])
         I.reset(t_cur, yv)
         t_cur, _ = I.evolve(TF, yv, sts.ONE_STEP)
-        L.N_VCopyToHost_Sts(yv.h, pout)
-        host_in.copy_(host_out)
+        L.N_VCopyToHost_Sts(yv.h, hp[1 - k])
+        k = 1 - k
     barrier()
     s0 = I.stats()
     with timer() as tm:
         for _ in range(args.steps):
-            L.N_VCopyFromHost_Sts(yv.h, pin)
+            L.N_VCopyFromHost_Sts(yv.h, hp[k])
             I.reset(t_cur, yv)
             t_cur, _ = I.evolve(TF, yv, sts.ONE_STEP)
-            L.N_VCopyToHost_Sts(yv.h, pout)
-            host_in.copy_(host_out)
+            L.N_VCopyToHost_Sts(yv.h, hp[1 - k])
+            k = 1 - k
     s1 = I.stats()
     e2e_ms = max_over_ranks(tm.ms)
     e2e_dof = N2 * (s1["nfe"] - s0["nfe"])
