@@ -506,7 +506,8 @@ def run_precond(args):
         ky, gh = system(erng)
         P = sts.Problem(ctx, sts.UNFORCED, n, n, 1.0, ky)
         b = sts.NVector.from_numpy(ctx, sts.smooth_field(n, erng))
-        x1, x2 = P.vector(), P.vector()
+        x1, x2, x3 = P.vector(), P.vector(), P.vector()
+        mg = sts.PFMG(P, relax=2, nrelax=2)  # the reference's multilevel comparator (PFMG role)
         res = {}
         for rep in range(2):  # the first solve of each kind warms up (graph instantiation)
             ctx.synchronize()
@@ -521,7 +522,12 @@ def run_precond(args):
             t = time.perf_counter()
             it3, rel3, rc3, used = sts.implicit_solve_learned(P, gh, net, b, x2, tol=1e-8, maxit=20000)
             t_auto = time.perf_counter() - t
+            ctx.synchronize()
+            t = time.perf_counter()
+            it4, rel4, rc4 = sts.implicit_solve_pfmg(P, gh, mg, b, x3, tol=1e-8, maxit=10000)
+            t_mg = time.perf_counter() - t
             res = {"ky": ky, "gamma_h": gh, "pcg_iters": it1, "pcg_s": t_pcg, "pcg_relres": rel1,
+                   "pfmg_iters": it4, "pfmg_s": t_mg, "pfmg_relres": rel4, "pfmg_levels": mg.levels(),
                    "fcg_iters": it2, "fcg_s": t_fcg, "fcg_true_relres": rel2, "fcg_status": rc2,
                    "pcg_ms_per_iter": 1e3 * t_pcg / max(1, it1),
                    "fcg_ms_per_iter": 1e3 * t_fcg / max(1, it2),
@@ -529,8 +535,10 @@ def run_precond(args):
                    "learned_relres": rel3}
         xa, xb = x1.numpy(), x2.numpy()
         res["solution_rel_diff"] = float(np.linalg.norm(xa - xb) / np.linalg.norm(xa))
+        res["pfmg_solution_rel_diff"] = float(np.linalg.norm(xa - x3.numpy()) / np.linalg.norm(xa))
         rows.append(res)
         print(json.dumps(res), flush=True)
+        del mg
         P.free()
     t_pcg = sum(r["pcg_s"] for r in rows)
     t_fcg = sum(r["fcg_s"] for r in rows)
@@ -541,6 +549,8 @@ def run_precond(args):
         "value": t_pcg / t_auto, "unit": "x", "higher_is_better": True, "n_gpus": 1,
         "pcg_total_s": t_pcg, "learned_total_s": t_auto, "fcg_total_s": t_fcg,
         "fcg_only_speedup": t_pcg / t_fcg,
+        "pfmg_total_s": sum(r["pfmg_s"] for r in rows),
+        "pfmg_speedup_vs_jacobi_pcg": t_pcg / max(1e-12, sum(r["pfmg_s"] for r in rows)),
         "systems_on_net": sum(1 for r in rows if r["learned_used_net"]),
         "max_learned_relres": max(r["learned_relres"] for r in rows),
         "iters_ratio": sum(r["pcg_iters"] for r in rows) / max(1, sum(r["fcg_iters"] for r in rows)),

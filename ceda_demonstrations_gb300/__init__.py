@@ -153,6 +153,15 @@ SIGNATURES = [
     ("STS_SUNLinSol_SPGMR", _vp, [_NV, C.c_int, C.c_int, _vp]),
     ("STS_SUNLinSol_SPGMRSetMaxRestarts", C.c_int, [_vp, C.c_int]),
     ("STS_SUNLinSol_SPGMRSetGSType", C.c_int, [_vp, C.c_int]),
+    ("STS_PFMGCreate", _vp, [_vp, C.c_int, C.c_int]),
+    ("STS_PFMGFree", None, [C.POINTER(_vp)]),
+    ("STS_PFMGPSetup", C.c_int, [C.c_double, _NV, _NV, C.c_int, C.POINTER(C.c_int), C.c_double, _vp]),
+    ("STS_PFMGPSolve", C.c_int, [C.c_double, _NV, _NV, _NV, _NV, C.c_double, C.c_double, C.c_int, _vp]),
+    ("STS_PFMGPrecSolve", C.c_int, [_vp, _NV, _NV, C.c_double, C.c_int]),
+    ("STS_PFMGNumLevels", C.c_int, [_vp]),
+    ("STS_PFMGNumVCycles", _ll, [_vp]),
+    ("STS_ImplicitSolvePFMG", C.c_int, [_vp, C.c_double, _vp, _NV, _NV, C.c_double, C.c_int,
+                                        C.POINTER(C.c_int), _dp]),
     ("STS_SDIRK2EvolveLS", C.c_int, [_vp, _vp, C.c_int, _NV, C.c_double, C.c_double, C.c_int,
                                      C.c_double, C.POINTER(_ll)]),
     ("STS_ImplicitSolvePCG", C.c_int, [_vp, C.c_double, _NV, _NV, C.c_double, C.c_int, C.c_int,
@@ -643,6 +652,51 @@ def implicit_solve_pcg(problem, gamma, b, x, tol=1e-8, maxit=100000, jacobi=True
                                     C.byref(it), C.byref(rel))
     if rc < 0:
         _err("STS_ImplicitSolvePCG")
+    return it.value, rel.value, rc
+
+
+class PFMG:
+    """Structured multigrid preconditioner in hypre PFMG's role (preconditioner_hypre.cpp):
+    relax 1 = weighted Jacobi, 2 = symmetric red/black Gauss-Seidel; nrelax pre/post sweeps."""
+
+    def __init__(self, problem, relax=2, nrelax=2):
+        self.problem = problem
+        self.h = lib().STS_PFMGCreate(problem.h, relax, nrelax)
+        if not self.h:
+            _err("STS_PFMGCreate")
+
+    def setup(self, gamma):
+        cur = C.c_int()
+        if lib().STS_PFMGPSetup(0.0, None, None, 0, C.byref(cur), gamma, self.h) != 0:
+            _err("STS_PFMGPSetup")
+
+    def psolve(self, r, z, gamma):
+        if lib().STS_PFMGPSolve(0.0, None, None, r.h, z.h, gamma, 0.0, 2, self.h) != 0:
+            _err("STS_PFMGPSolve")
+
+    def levels(self):
+        return lib().STS_PFMGNumLevels(self.h)
+
+    def vcycles(self):
+        return lib().STS_PFMGNumVCycles(self.h)
+
+    def __del__(self):
+        try:
+            if not _exiting and self.h:
+                h = _vp(self.h)
+                lib().STS_PFMGFree(C.byref(h))
+                self.h = None
+        except Exception:
+            pass
+
+
+def implicit_solve_pfmg(problem, gamma, mg, b, x, tol=1e-8, maxit=100000):
+    """(I - gamma A) x = b by CG with the PFMG preconditioner: (iterations, rel. residual, rc)."""
+    it, rel = C.c_int(), C.c_double()
+    rc = lib().STS_ImplicitSolvePFMG(problem.h, gamma, mg.h, b.h, x.h, tol, maxit, C.byref(it),
+                                     C.byref(rel))
+    if rc < 0:
+        _err("STS_ImplicitSolvePFMG")
     return it.value, rel.value, rc
 
 

@@ -319,6 +319,31 @@ int STS_SDIRK2EvolveLearned(STS_Problem p, STS_Net net, N_Vector y, double t0, d
                             double tol, int maxit, long long* total_iters);
 
 /* ------------------------------------------------------------------------------------
+ * Structured multigrid preconditioner in the role of hypre PFMG
+ * (diffusion_2D/preconditioner_hypre.cpp; --pfmg_relax, --pfmg_nrelax of
+ * diffusion_2D.cpp:138-150): one V-cycle per PSolve, semicoarsening in the direction of the
+ * stronger coupling, non-Galerkin coarse operators, weighted Jacobi (relax_type 1) or
+ * symmetric red/black Gauss-Seidel (2, the reference's default) with nrelax pre and post
+ * sweeps. Dirichlet problems.
+ * ----------------------------------------------------------------------------------*/
+typedef struct STS_PFMG_* STS_PFMG;
+STS_PFMG STS_PFMGCreate(STS_Problem p, int relax_type, int nrelax);
+void STS_PFMGFree(STS_PFMG* mg);
+/* PSetup / PSolve (preconditioner_hypre.cpp:13-180), user_data = the STS_PFMG */
+int STS_PFMGPSetup(double t, N_Vector u, N_Vector f, int jok, int* jcurPtr, double gamma,
+                   void* user_data);
+int STS_PFMGPSolve(double t, N_Vector u, N_Vector f, N_Vector r, N_Vector z, double gamma,
+                   double delta, int lr, void* user_data);
+/* the SUNLinSol PSolve callback form, for a PFMG set up with STS_PFMGPSetup */
+int STS_PFMGPrecSolve(void* P_data, N_Vector r, N_Vector z, double tol, int lr);
+int STS_PFMGNumLevels(STS_PFMG mg);
+long long STS_PFMGNumVCycles(STS_PFMG mg);
+/* (I - gamma A) x = b by CG (SUNLinSol_PCG through the callbacks) with the PFMG
+ * preconditioner, x0 = 0, stop at ||r||_2 <= tol ||b||_2; returns as STS_SUNLinSolSolve */
+int STS_ImplicitSolvePFMG(STS_Problem p, double gamma, STS_PFMG mg, N_Vector b, N_Vector x,
+                          double tol, int maxit, int* iters, double* relres);
+
+/* ------------------------------------------------------------------------------------
  * Batched STS (new; the reference integrates one problem per run): many independent
  * homogeneous-Dirichlet unforced heat problems, each with its own n x n grid and kx, ky,
  * integrated from t = 0 to tf in one persistent launch with per-instance step control on

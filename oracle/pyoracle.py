@@ -124,6 +124,12 @@ def lib():
         L.orc_sdirk2_ls.argtypes = [C.POINTER(Prob), C.c_double, C.c_double, C.c_int, C.c_double,
                                     C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp,
                                     C.POINTER(C.c_long)]
+        L.orc_pfmg_vcycle.restype = C.c_int
+        L.orc_pfmg_vcycle.argtypes = [C.POINTER(Prob), C.c_double, C.c_int, C.c_int, _dp, _dp,
+                                      C.POINTER(C.c_int)]
+        L.orc_pcg_pfmg.restype = C.c_int
+        L.orc_pcg_pfmg.argtypes = [C.POINTER(Prob), C.c_double, C.c_int, C.c_int, _dp, _dp, C.c_double,
+                                   C.c_int, C.POINTER(C.c_int), _dp]
         L.orc_nthreads.restype = C.c_int
         _lib = L
     return _lib
@@ -265,6 +271,23 @@ class Problem:
         it, rel = C.c_int(), C.c_double()
         rc = lib().orc_spgmr(self.p, gamma, int(jacobi), dptr(b), dptr(x), tol, maxl, max_restarts,
                              gstype, C.byref(it), C.byref(rel))
+        return x, rc, it.value, rel.value
+
+    def pfmg_vcycle(self, gamma, r, relax=2, nrelax=2):
+        """One PFMG-role V-cycle z = B r: (z, number of levels)."""
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = self.field()
+        nl = C.c_int()
+        lib().orc_pfmg_vcycle(self.p, gamma, relax, nrelax, dptr(r), dptr(z), C.byref(nl))
+        return z, nl.value
+
+    def pcg_pfmg(self, gamma, b, tol=1e-8, maxl=10000, relax=2, nrelax=2):
+        """CG with the PFMG-role preconditioner: (x, status, iterations, relative residual)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = self.field()
+        it, rel = C.c_int(), C.c_double()
+        rc = lib().orc_pcg_pfmg(self.p, gamma, relax, nrelax, dptr(b), dptr(x), tol, maxl, C.byref(it),
+                                C.byref(rel))
         return x, rc, it.value, rel.value
 
     def sdirk2_ls(self, y0, t0, h, nsteps, tol=1e-10, ls=1, maxl=20, max_restarts=0, gstype=1,

@@ -1339,11 +1339,15 @@ static void v_lincomb(long n, int nv, const double* cf, const double** X, double
  * z = fma(a, x, b y), Scale z = c x, LinearCombination acc = c0 x0 then fma(c_k, x_k, acc),
  * exact dot products; small dense algebra in plain double arithmetic. Dirichlet kinds only.
  * ----------------------------------------------------------------------------------*/
+typedef struct orc_pfmg orc_pfmg;
+static void pfmg_apply(orc_pfmg* mg, const double* r, double* z);
+
 typedef struct {
   const orc_prob* p;
   double gamma, D;
-  int jacobi;
+  int jacobi;     /* 1: Jacobi PSolve, 2: the PFMG V-cycle below */
   double* tmp;
+  orc_pfmg* mg;
 } gen_op;
 
 static void gen_atimes(const gen_op* o, const double* v, double* z)
@@ -1357,7 +1361,8 @@ static void gen_atimes(const gen_op* o, const double* v, double* z)
 static void gen_psolve(const gen_op* o, const double* r, double* z, int copy_form)
 {
   long n = (long)o->p->nx * o->p->ny;
-  if (o->jacobi)
+  if (o->jacobi == 2) pfmg_apply(o->mg, r, z);
+  else if (o->jacobi)
     for (long k = 0; k < n; ++k) z[k] = o->D * r[k];
   else if (copy_form) v_linsum(n, 1.0, r, 0.0, r, z);
   else memcpy(z, r, n * sizeof(double));
@@ -1369,7 +1374,7 @@ int orc_pcg_generic(const orc_prob* p, double gamma, int jacobi, const double* b
                     int maxl, int* iters, double* relres)
 {
   long n = (long)p->nx * p->ny;
-  gen_op o = {p, gamma, 1.0 / (1.0 - gamma * p->cc), jacobi, (double*)malloc(n * sizeof(double))};
+  gen_op o = {p, gamma, 1.0 / (1.0 - gamma * p->cc), jacobi, (double*)malloc(n * sizeof(double)), NULL};
   double* r  = (double*)malloc(n * sizeof(double));
   double* z  = (double*)malloc(n * sizeof(double));
   double* pv = (double*)malloc(n * sizeof(double));
@@ -1448,7 +1453,7 @@ int orc_spgmr(const orc_prob* p, double gamma, int jacobi, const double* b, doub
 {
   long n  = (long)p->nx * p->ny;
   int m   = maxl;
-  gen_op o = {p, gamma, 1.0 / (1.0 - gamma * p->cc), jacobi, (double*)malloc(n * sizeof(double))};
+  gen_op o = {p, gamma, 1.0 / (1.0 - gamma * p->cc), jacobi, (double*)malloc(n * sizeof(double)), NULL};
   double** V = (double**)malloc((m + 1) * sizeof(double*));
   for (int k = 0; k <= m; ++k) V[k] = (double*)malloc(n * sizeof(double));
   double* r  = (double*)malloc(n * sizeof(double));
@@ -1585,6 +1590,261 @@ out:
   free(h2);
   free(cf);
   free(X);
+  return ret;
+}
+
+/* ------------------------------------------------------------------------------------
+ * Structured multigrid V-cycle in the role of hypre PFMG (diffusion_2D/preconditioner_hypre.cpp
+ * :13-180): semicoarsening in the direction of the larger coupling (coarse point I = fine
+ * 2I + 1, coupling / 4), non-Galerkin coarse operators d = 1 + 2 (a_x + a_y), linear
+ * interpolation, full-weighting restriction, weighted Jacobi (omega 0.8) or symmetric red/black
+ * Gauss-Seidel relaxation, 8 sweeps on the coarsest level (at most 2 x 2); the product's
+ * operation order (csrc/pfmg.cu).
+ * ----------------------------------------------------------------------------------*/
+typedef struct {
+  long nx, ny;
+  double ax, ay, d, dinv, wd;
+  int dir;
+  double *f, *u, *t;
+} pfmg_level;
+
+struct orc_pfmg {
+  int relax, nrelax, nl;
+  pfmg_level L[64];
+};
+
+static double pat(const double* u, long nx, long ny, long i, long j)
+{
+  return (i >= 0 && i < nx && j >= 0 && j < ny) ? u[j * nx + i] : 0.0;
+}
+
+static double pfmg_m(const double* u, const pfmg_level* l, long i, long j)
+{
+  double sx = pat(u, l->nx, l->ny, i - 1, j) + pat(u, l->nx, l->ny, i + 1, j);
+  double sy = pat(u, l->nx, l->ny, i, j - 1) + pat(u, l->nx, l->ny, i, j + 1);
+  double m  = l->d * u[j * l->nx + i];
+  m         = fma(-l->ax, sx, m);
+  m         = fma(-l->ay, sy, m);
+  return m;
+}
+
+static void pfmg_smooth(orc_pfmg* mg, pfmg_level* l, int sweeps, int post)
+{
+  long n = l->nx * l->ny;
+  if (mg->relax == 1)
+  {
+    for (int s = 0; s < sweeps; ++s)
+    {
+      const double* in = (s & 1) ? l->t : l->u;
+      double* out      = (s & 1) ? l->u : l->t;
+      for (long j = 0; j < l->ny; ++j)
+        for (long i = 0; i < l->nx; ++i)
+        {
+          long k = j * l->nx + i;
+          out[k] = fma(l->wd, l->f[k] - pfmg_m(in, l, i, j), in[k]);
+        }
+    }
+    if (sweeps & 1) memcpy(l->u, l->t, n * sizeof(double));
+  }
+  else
+  {
+    for (int s = 0; s < sweeps; ++s)
+      for (int h = 0; h < 2; ++h)
+      {
+        int color = post ? 1 - h : h;
+        for (long j = 0; j < l->ny; ++j)
+          for (long i = (j + color) & 1; i < l->nx; i += 2)
+          {
+            double sx = pat(l->u, l->nx, l->ny, i - 1, j) + pat(l->u, l->nx, l->ny, i + 1, j);
+            double sy = pat(l->u, l->nx, l->ny, i, j - 1) + pat(l->u, l->nx, l->ny, i, j + 1);
+            double v  = fma(l->ax, sx, l->f[j * l->nx + i]);
+            v         = fma(l->ay, sy, v);
+            l->u[j * l->nx + i] = l->dinv * v;
+          }
+      }
+  }
+}
+
+static orc_pfmg* pfmg_create(const orc_prob* p, double gamma, int relax, int nrelax)
+{
+  orc_pfmg* mg = (orc_pfmg*)calloc(1, sizeof(orc_pfmg));
+  mg->relax    = relax;
+  mg->nrelax   = nrelax;
+  for (int lev = 0; lev < 64; ++lev)
+  {
+    pfmg_level l;
+    if (lev == 0)
+    {
+      l.nx = p->nx;
+      l.ny = p->ny;
+      l.ax = gamma * p->cx;
+      l.ay = gamma * p->cy;
+      l.d  = 1.0 - gamma * p->cc;
+    }
+    else
+    {
+      l = mg->L[lev - 1];
+      if (l.dir == 0)
+      {
+        l.nx = l.nx / 2;
+        l.ax = l.ax * 0.25;
+      }
+      else
+      {
+        l.ny = l.ny / 2;
+        l.ay = l.ay * 0.25;
+      }
+      l.d = 1.0 + 2.0 * (l.ax + l.ay);
+    }
+    l.dinv = 1.0 / l.d;
+    l.wd   = 0.8 * l.dinv;
+    if (l.nx > 2 && (l.ax >= l.ay || l.ny <= 2)) l.dir = 0;
+    else if (l.ny > 2) l.dir = 1;
+    else l.dir = -1;
+    long n = l.nx * l.ny;
+    l.f    = (double*)calloc(n, sizeof(double));
+    l.u    = (double*)calloc(n, sizeof(double));
+    l.t    = (double*)calloc(n, sizeof(double));
+    mg->L[lev] = l;
+    mg->nl     = lev + 1;
+    if (l.dir < 0) break;
+  }
+  return mg;
+}
+
+static void pfmg_destroy(orc_pfmg* mg)
+{
+  for (int k = 0; k < mg->nl; ++k)
+  {
+    free(mg->L[k].f);
+    free(mg->L[k].u);
+    free(mg->L[k].t);
+  }
+  free(mg);
+}
+
+static void pfmg_apply(orc_pfmg* mg, const double* r, double* z)
+{
+  pfmg_level* L = mg->L;
+  memcpy(L[0].f, r, (size_t)(L[0].nx * L[0].ny) * sizeof(double));
+  for (int lev = 0; lev < mg->nl; ++lev)
+  {
+    pfmg_level* l = &L[lev];
+    memset(l->u, 0, (size_t)(l->nx * l->ny) * sizeof(double));
+    if (l->dir < 0)
+    {
+      pfmg_smooth(mg, l, 8, 0);
+      break;
+    }
+    pfmg_smooth(mg, l, mg->nrelax, 0);
+    for (long j = 0; j < l->ny; ++j)
+      for (long i = 0; i < l->nx; ++i) l->t[j * l->nx + i] = l->f[j * l->nx + i] - pfmg_m(l->u, l, i, j);
+    pfmg_level* c = &L[lev + 1];
+    for (long J = 0; J < c->ny; ++J)
+      for (long I = 0; I < c->nx; ++I)
+      {
+        double a, b, cc;
+        if (l->dir == 0)
+        {
+          a  = pat(l->t, l->nx, l->ny, 2 * I, J);
+          b  = pat(l->t, l->nx, l->ny, 2 * I + 1, J);
+          cc = pat(l->t, l->nx, l->ny, 2 * I + 2, J);
+        }
+        else
+        {
+          a  = pat(l->t, l->nx, l->ny, I, 2 * J);
+          b  = pat(l->t, l->nx, l->ny, I, 2 * J + 1);
+          cc = pat(l->t, l->nx, l->ny, I, 2 * J + 2);
+        }
+        c->f[J * c->nx + I] = fma(0.5, b, 0.25 * (a + cc));
+      }
+  }
+  for (int lev = mg->nl - 2; lev >= 0; --lev)
+  {
+    pfmg_level* l = &L[lev];
+    pfmg_level* c = &L[lev + 1];
+    for (long j = 0; j < l->ny; ++j)
+      for (long i = 0; i < l->nx; ++i)
+      {
+        long q = l->dir == 0 ? i : j;
+        double e;
+        if (q & 1)
+          e = l->dir == 0 ? pat(c->u, c->nx, c->ny, q >> 1, j) : pat(c->u, c->nx, c->ny, i, q >> 1);
+        else
+        {
+          long Q    = q >> 1;
+          double lo = l->dir == 0 ? pat(c->u, c->nx, c->ny, Q - 1, j) : pat(c->u, c->nx, c->ny, i, Q - 1);
+          double hi = l->dir == 0 ? pat(c->u, c->nx, c->ny, Q, j) : pat(c->u, c->nx, c->ny, i, Q);
+          e         = 0.5 * (lo + hi);
+        }
+        l->u[j * l->nx + i] += e;
+      }
+    pfmg_smooth(mg, l, mg->nrelax, 1);
+  }
+  memcpy(z, L[0].u, (size_t)(L[0].nx * L[0].ny) * sizeof(double));
+}
+
+int orc_pfmg_vcycle(const orc_prob* p, double gamma, int relax, int nrelax, const double* r, double* z, int* nlevels)
+{
+  orc_pfmg* mg = pfmg_create(p, gamma, relax, nrelax);
+  pfmg_apply(mg, r, z);
+  if (nlevels) *nlevels = mg->nl;
+  pfmg_destroy(mg);
+  return 0;
+}
+
+/* CG with the PFMG preconditioner, the operation sequence of orc_pcg_generic */
+int orc_pcg_pfmg(const orc_prob* p, double gamma, int relax, int nrelax, const double* b, double* x, double tol,
+                 int maxl, int* iters, double* relres)
+{
+  long n = (long)p->nx * p->ny;
+  gen_op o = {p, gamma, 0.0, 2, (double*)malloc(n * sizeof(double)), pfmg_create(p, gamma, relax, nrelax)};
+  double* r  = (double*)malloc(n * sizeof(double));
+  double* z  = (double*)malloc(n * sizeof(double));
+  double* pv = (double*)malloc(n * sizeof(double));
+  double* Ap = (double*)malloc(n * sizeof(double));
+  int ret = 1;
+  *iters  = 0;
+  *relres = 0.0;
+  for (long k = 0; k < n; ++k) x[k] = 0.0;
+  v_linsum(n, 1.0, b, 0.0, b, r);
+  double bnorm = sqrt(orc_xdot(b, b, n));
+  if (!(bnorm > 0.0))
+  {
+    ret = 0;
+    goto out;
+  }
+  gen_psolve(&o, r, z, 1);
+  double rz = orc_xdot(r, z, n);
+  v_linsum(n, 1.0, z, 0.0, z, pv);
+  for (int it = 1; it <= maxl; ++it)
+  {
+    gen_atimes(&o, pv, Ap);
+    double pq    = orc_xdot(pv, Ap, n);
+    double alpha = rz / pq;
+    v_linsum(n, alpha, pv, 1.0, x, x);
+    v_linsum(n, -alpha, Ap, 1.0, r, r);
+    double rr = orc_xdot(r, r, n);
+    *iters    = it;
+    *relres   = sqrt(rr) / bnorm;
+    if (sqrt(rr) <= tol * bnorm)
+    {
+      ret = 0;
+      goto out;
+    }
+    gen_psolve(&o, r, z, 1);
+    double rzn  = orc_xdot(r, z, n);
+    double beta = rzn / rz;
+    rz          = rzn;
+    v_linsum(n, 1.0, z, beta, pv, pv);
+  }
+out:
+  pfmg_destroy(o.mg);
+  free(o.tmp);
+  free(r);
+  free(z);
+  free(pv);
+  free(Ap);
   return ret;
 }
 

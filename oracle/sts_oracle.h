@@ -103,6 +103,10 @@ int orc_spgmr(const orc_prob* p, double gamma, int jacobi, const double* b, doub
               int max_restarts, int gstype, int* iters, double* relres);
 int orc_sdirk2_ls(const orc_prob* p, double t0, double h, int nsteps, double tol, int ls, int maxl,
                   int max_restarts, int gstype, int jacobi, double* y, long* total_iters);
+/* PFMG-role V-cycle (relax 1 weighted Jacobi, 2 symmetric red/black Gauss-Seidel) and CG with it */
+int orc_pfmg_vcycle(const orc_prob* p, double gamma, int relax, int nrelax, const double* r, double* z, int* nlevels);
+int orc_pcg_pfmg(const orc_prob* p, double gamma, int relax, int nrelax, const double* b, double* x, double tol,
+                 int maxl, int* iters, double* relres);
 int orc_nthreads(void);
 
 #ifdef __cplusplus

@@ -1,0 +1,63 @@
+"""The structured multigrid preconditioner in hypre PFMG's role (diffusion_2D/
+preconditioner_hypre.cpp: one V-cycle per PSolve, semicoarsening, non-Galerkin coarse
+operators, weighted Jacobi or symmetric red/black Gauss-Seidel relaxation) on the GPU against
+the oracle's restatement, bit for bit: the V-cycle itself and CG with it."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def smooth_rhs(nx, ny, seed):
+    rng = np.random.default_rng(seed)
+    x = (np.arange(nx) + 1.0) / (nx + 1)
+    y = (np.arange(ny) + 1.0) / (ny + 1)
+    b = np.zeros((ny, nx))
+    for _ in range(6):
+        p, q = rng.integers(1, 8, size=2)
+        b += rng.standard_normal() * np.outer(np.sin(q * np.pi * y), np.sin(p * np.pi * x))
+    return b.ravel()
+
+
+CASES = [(32, 24, 0.3, 1e-2), (64, 64, 1e-3, 1e-2), (130, 66, 0.05, 5e-3), (257, 129, 1.0, 1e-3)]
+
+
+@pytest.mark.parametrize("relax", [1, 2], ids=["jacobi", "rbgs"])
+@pytest.mark.parametrize("nx,ny,ky,gamma", CASES)
+def test_vcycle_bitwise(ctx, stslib, oracle, relax, nx, ny, ky, gamma):
+    pk = dict(kind=0, nx=nx, ny=ny, kx=1.0, ky=ky)
+    G, O = stslib.Problem(ctx, **pk), oracle.Problem(**pk)
+    r = np.random.default_rng(nx + ny).standard_normal(nx * ny)
+    mg = stslib.PFMG(G, relax=relax, nrelax=2)
+    R = stslib.NVector.from_numpy(ctx, r)
+    Z = G.vector()
+    mg.psolve(R, Z, gamma)
+    z_o, nl = oracle.Problem(**pk).pfmg_vcycle(gamma, r, relax=relax, nrelax=2)
+    assert mg.levels() == nl
+    assert np.array_equal(Z.numpy(), z_o)
+
+
+@pytest.mark.parametrize("relax", [1, 2], ids=["jacobi", "rbgs"])
+def test_pcg_pfmg_bitwise_and_fast(ctx, stslib, oracle, relax):
+    nx, ny, ky, gamma = 128, 96, 0.02, 0.1  # kappa ~ 7000
+    pk = dict(kind=0, nx=nx, ny=ny, kx=1.0, ky=ky)
+    G, O = stslib.Problem(ctx, **pk), oracle.Problem(**pk)
+    b = np.random.default_rng(5).standard_normal(nx * ny)  # broadband: all modes present
+    mg = stslib.PFMG(G, relax=relax)
+    B = stslib.NVector.from_numpy(ctx, b)
+    X = G.vector()
+    it, rel, rc = stslib.implicit_solve_pfmg(G, gamma, mg, B, X, tol=1e-10)
+    x_o, rc_o, it_o, rel_o = O.pcg_pfmg(gamma, b, tol=1e-10, relax=relax)
+    assert rc == rc_o == 0 and it == it_o and rel == rel_o <= 1e-10
+    assert np.array_equal(X.numpy(), x_o)
+    _, it_j, _ = O.pcg(gamma, b, tol=1e-10)
+    assert it * 10 < it_j  # multigrid against the Jacobi-preconditioned iteration count
+
+
+def test_pfmg_rejects_periodic_and_bad_options(ctx, stslib):
+    P = stslib.Problem(ctx, stslib.PERIODIC, 32, 32, 1.0, 1.0)
+    with pytest.raises(stslib.STSError):
+        stslib.PFMG(P)
+    D = stslib.Problem(ctx, kind=0, nx=32, ny=32)
+    with pytest.raises(stslib.STSError):
+        stslib.PFMG(D, relax=3)

@@ -351,3 +351,24 @@ def test_oracle_krylov_solvers_against_dense_solve(oracle):
     assert rc == 1 and it == 3
     x, rc, it, rel = P.pcg_generic(gamma, b, tol=1e-10)
     assert rc == 0 and np.linalg.norm(x - xt) / np.linalg.norm(xt) < 1e-8
+
+
+def test_oracle_pfmg_vcycle_is_spd_and_converges(oracle):
+    """The PFMG-role V-cycle is a symmetric positive definite operator (so it preconditions
+    CG), and CG with it needs a handful of iterations where Jacobi-PCG needs hundreds."""
+    nx, ny, gamma = 24, 20, 1e-2
+    for relax in (1, 2):
+        for ky in (1.0, 1e-3):
+            P = oracle.Problem(oracle.MANUFACTURED, nx, ny, kx=1.0, ky=ky)
+            n = nx * ny
+            B = np.zeros((n, n))
+            for k in range(n):
+                e = np.zeros(n)
+                e[k] = 1.0
+                B[:, k] = P.pfmg_vcycle(gamma, e, relax=relax)[0]
+            assert np.abs(B - B.T).max() <= 1e-12 * np.abs(B).max()
+            assert np.linalg.eigvalsh(0.5 * (B + B.T)).min() > 0
+            b = np.random.default_rng(3).standard_normal(n)
+            x, rc, it, rel = P.pcg_pfmg(gamma, b, tol=1e-10, relax=relax)
+            _, it_j, _ = P.pcg(gamma, b, tol=1e-10)
+            assert rc == 0 and rel <= 1e-10 and it <= 12 and it_j > 3 * it
