@@ -162,6 +162,8 @@ SIGNATURES = [
     ("STS_PFMGNumVCycles", _ll, [_vp]),
     ("STS_ImplicitSolvePFMG", C.c_int, [_vp, C.c_double, _vp, _NV, _NV, C.c_double, C.c_int,
                                         C.POINTER(C.c_int), _dp]),
+    ("STS_SDIRK2EvolvePFMG", C.c_int, [_vp, _vp, _NV, C.c_double, C.c_double, C.c_int, C.c_double,
+                                       C.c_int, C.POINTER(_ll)]),
     ("STS_SDIRK2EvolveLS", C.c_int, [_vp, _vp, C.c_int, _NV, C.c_double, C.c_double, C.c_int,
                                      C.c_double, C.POINTER(_ll)]),
     ("STS_ImplicitSolvePCG", C.c_int, [_vp, C.c_double, _NV, _NV, C.c_double, C.c_int, C.c_int,
@@ -723,6 +725,15 @@ def sdirk2_evolve_ls(problem, solver, y, t0, h, nsteps, tol=1e-10, precond=True)
                                   C.byref(it))
     if rc < 0:
         _err("STS_SDIRK2EvolveLS")
+    return it.value
+
+
+def sdirk2_evolve_pfmg(problem, mg, y, t0, h, nsteps, tol=1e-10, maxit=100000):
+    """SDIRK2 steps with CG + the PFMG-role multigrid in every stage solve."""
+    it = _ll()
+    rc = lib().STS_SDIRK2EvolvePFMG(problem.h, mg.h, y.h, t0, h, nsteps, tol, maxit, C.byref(it))
+    if rc < 0:
+        _err("STS_SDIRK2EvolvePFMG")
     return it.value
 
 

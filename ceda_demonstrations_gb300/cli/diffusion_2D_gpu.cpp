@@ -39,6 +39,9 @@ struct Opts {
   bool error = false, linear = true, lsinfo = false, prec = true, internaleig = false;
   bool mixed = false, graphs = true;
   string ls = "cg";
+  // multigrid preconditioner in hypre PFMG's role (diffusion_2D.cpp:138-150, USE_HYPRE builds)
+  bool pfmg = false;
+  int pfmg_relax = 2, pfmg_nrelax = 2;
   // output (UserOutput)
   int output = 1, nout = 20;
   // binary checkpoint of the integrator state written at the end / read before the run
@@ -74,6 +77,9 @@ static void help()
           "  --maxsteps --onestep <n> --error --internaleig --smax <stages> --mixed --nographs\n"
           "\nDIRK solver command line options:\n"
           "  --order --nonlinear --ls <cg|gmres> --lsinfo --liniters --epslin --noprec --msbp\n"
+          "  --pfmg : CG stage solves preconditioned by the structured multigrid (PFMG role)\n"
+          "  --pfmg_relax <type> : 1 = weighted Jacobi, 2 = symmetric red/black Gauss-Seidel\n"
+          "  --pfmg_nrelax <num> : pre and post relaxation sweeps\n"
           "\nOutput command line options:\n"
           "  --output <level> (0 = none, 1 = stats, 2 = solution)  --nout <nout>\n"
           "  --checkpoint <file> : write the integrator state at the end of the run\n"
@@ -118,6 +124,17 @@ static int parse(int argc, char** argv, Opts& o)
   if (take(a, "--msbp", &v)) o.msbp = stoi(v);
   if (take(a, "--epslin", &v)) o.epslin = stod(v);
   if (take(a, "--noprec", nullptr)) o.prec = false;
+  if (take(a, "--pfmg", nullptr)) o.pfmg = true;
+  if (take(a, "--pfmg_relax", &v))
+  {
+    o.pfmg_relax = stoi(v);
+    o.pfmg       = true;
+  }
+  if (take(a, "--pfmg_nrelax", &v))
+  {
+    o.pfmg_nrelax = stoi(v);
+    o.pfmg        = true;
+  }
   if (take(a, "--internaleig", nullptr)) o.internaleig = true;
   if (take(a, "--smax", &v)) o.smax = stoi(v);
   if (take(a, "--mixed", nullptr)) o.mixed = true;
@@ -209,6 +226,8 @@ int main(int argc, char** argv)
          << "\n atol        = " << o.atol << "\n controller  = " << o.controller << "\n hfixed      = " << o.hfixed
          << "\n max steps   = " << o.maxsteps << "\n";
     if (sts) cout << (o.internaleig ? " internal eigenvalue estimation\n" : " user-provided dominant eigenvalue\n");
+    if (impl && o.pfmg) // diffusion_2D.cpp:217-218
+      cout << "  pfmg relaxtype = " << o.pfmg_relax << "\n  pfmg num relax = " << o.pfmg_nrelax << "\n";
     cout << " --------------------------------- \n";
   }
   N_Vector u = N_VNew_Sts(N, ctx);
@@ -223,6 +242,7 @@ int main(int argc, char** argv)
   void* mem = nullptr;
   void* ref = nullptr;
   void* LS  = nullptr; // generic linear solver of the dirk path (--ls gmres, or cg with --noprec)
+  STS_PFMG mg = nullptr; // multigrid preconditioner of the dirk path (--pfmg)
   if (sts)
   {
     mem = STS_LSRKStepCreateSTS(STS_Diffusion, 0.0, u, ctx);
@@ -314,7 +334,12 @@ int main(int argc, char** argv)
       const int nsteps  = (int)llround((tout - t) / h);
       long long its     = 0;
       const double tol  = o.epslin > 0 ? o.epslin : 1e-10;
-      if (o.ls == "cg" && o.prec) flag = STS_SDIRK2Evolve(P, u, t, h, nsteps, tol, 100000, &its);
+      if (o.pfmg && o.prec)
+      { // CG + the PFMG-role multigrid (preconditioner_hypre.cpp in a hypre build)
+        if (!mg) mg = STS_PFMGCreate(P, o.pfmg_relax, o.pfmg_nrelax);
+        flag = mg ? STS_SDIRK2EvolvePFMG(P, mg, u, t, h, nsteps, tol, 100000, &its) : -1;
+      }
+      else if (o.ls == "cg" && o.prec) flag = STS_SDIRK2Evolve(P, u, t, h, nsteps, tol, 100000, &its);
       else
       { // generic solver object (main.cpp:209-218): PCG without preconditioner, or SPGMR with
         // maxl = --liniters, restarted up to 10^5 iterations in total
@@ -396,6 +421,7 @@ int main(int argc, char** argv)
   if (mem) STS_ARKodeFree(&mem);
   if (ref) STS_ARKodeFree(&ref);
   if (LS) STS_SUNLinSolFree(LS);
+  if (mg) STS_PFMGFree(&mg);
   N_VDestroy_Sts(u);
   if (uref) N_VDestroy_Sts(uref);
   if (uerr) N_VDestroy_Sts(uerr);

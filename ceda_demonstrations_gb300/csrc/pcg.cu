@@ -683,6 +683,18 @@ extern "C" int STS_SDIRK2EvolveLS(STS_Problem p, void* LS, int precond, N_Vector
   return rc;
 }
 
+// The SDIRK2 driver with each stage solved by CG with the PFMG-role multigrid preconditioner
+// (the reference built with hypre: preconditioner_hypre.cpp attached by main.cpp:311)
+extern "C" int STS_SDIRK2EvolvePFMG(STS_Problem p, STS_PFMG mg, N_Vector y, double t0, double h, int nsteps,
+                                    double tol, int maxit, long long* total_iters)
+{
+  if (!mg) return -1;
+  return sdirk2_run(p, y, t0, h, nsteps, total_iters, [&](double hg, N_Vector rhs, N_Vector d, int* it) {
+    double rel;
+    return STS_ImplicitSolvePFMG(p, hg, mg, rhs, d, tol, maxit, it, &rel) < 0 ? -1 : 0;
+  });
+}
+
 // The same SDIRK2 driver with each stage solved by STS_ImplicitSolveLearned (FCG with the
 // learned preconditioner where the condition estimate favours it, Jacobi-PCG elsewhere).
 extern "C" int STS_SDIRK2EvolveLearned(STS_Problem p, STS_Net net, N_Vector y, double t0, double h, int nsteps,

@@ -342,6 +342,9 @@ long long STS_PFMGNumVCycles(STS_PFMG mg);
  * preconditioner, x0 = 0, stop at ||r||_2 <= tol ||b||_2; returns as STS_SUNLinSolSolve */
 int STS_ImplicitSolvePFMG(STS_Problem p, double gamma, STS_PFMG mg, N_Vector b, N_Vector x,
                           double tol, int maxit, int* iters, double* relres);
+/* fixed-step SDIRK2 with each stage solved by CG + PFMG (the DIRK runs of a hypre build) */
+int STS_SDIRK2EvolvePFMG(STS_Problem p, STS_PFMG mg, N_Vector y, double t0, double h, int nsteps,
+                         double tol, int maxit, long long* total_iters);
 
 /* ------------------------------------------------------------------------------------
  * Batched STS (new; the reference integrates one problem per run): many independent

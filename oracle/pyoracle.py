@@ -130,6 +130,9 @@ def lib():
         L.orc_pcg_pfmg.restype = C.c_int
         L.orc_pcg_pfmg.argtypes = [C.POINTER(Prob), C.c_double, C.c_int, C.c_int, _dp, _dp, C.c_double,
                                    C.c_int, C.POINTER(C.c_int), _dp]
+        L.orc_sdirk2_pfmg.restype = C.c_int
+        L.orc_sdirk2_pfmg.argtypes = [C.POINTER(Prob), C.c_double, C.c_double, C.c_int, C.c_double, C.c_int,
+                                      C.c_int, C.c_int, _dp, C.POINTER(C.c_long)]
         L.orc_nthreads.restype = C.c_int
         _lib = L
     return _lib
@@ -289,6 +292,12 @@ class Problem:
         rc = lib().orc_pcg_pfmg(self.p, gamma, relax, nrelax, dptr(b), dptr(x), tol, maxl, C.byref(it),
                                 C.byref(rel))
         return x, rc, it.value, rel.value
+
+    def sdirk2_pfmg(self, y0, t0, h, nsteps, tol=1e-10, maxl=100000, relax=2, nrelax=2):
+        y = np.array(y0, dtype=np.float64)
+        it = C.c_long()
+        lib().orc_sdirk2_pfmg(self.p, t0, h, nsteps, tol, maxl, relax, nrelax, dptr(y), C.byref(it))
+        return y, it.value
 
     def sdirk2_ls(self, y0, t0, h, nsteps, tol=1e-10, ls=1, maxl=20, max_restarts=0, gstype=1,
                   jacobi=True):

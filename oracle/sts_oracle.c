@@ -1848,6 +1848,47 @@ out:
   return ret;
 }
 
+/* SDIRK2 (orc_sdirk2's stages) with CG + the PFMG-role V-cycle (STS_SDIRK2EvolvePFMG) */
+int orc_sdirk2_pfmg(const orc_prob* p, double t0, double h, int nsteps, double tol, int maxl, int relax, int nrelax,
+                    double* y, long* total_iters)
+{
+  long n      = (long)p->nx * p->ny;
+  double g    = 1.0 - sqrt(0.5);
+  double* f   = (double*)malloc(n * sizeof(double));
+  double* f1  = (double*)malloc(n * sizeof(double));
+  double* rhs = (double*)malloc(n * sizeof(double));
+  double* d   = (double*)malloc(n * sizeof(double));
+  double* Y1  = (double*)malloc(n * sizeof(double));
+  double relres;
+  long iters = 0;
+  double t   = t0;
+  int it;
+  for (int s = 0; s < nsteps; ++s)
+  {
+    double hg = h * g;
+    orc_rhs(p, t + g * h, y, f);
+    v_scale(n, hg, f, rhs);
+    orc_pcg_pfmg(p, hg, relax, nrelax, rhs, d, tol, maxl, &it, &relres);
+    iters += it;
+    v_linsum(n, 1.0, y, 1.0, d, Y1);
+    orc_rhs(p, t + g * h, Y1, f1);
+    orc_rhs(p, t + h, y, f);
+    double h1g = h * (1.0 - g);
+    v_linsum(n, h1g, f1, hg, f, rhs);
+    orc_pcg_pfmg(p, hg, relax, nrelax, rhs, d, tol, maxl, &it, &relres);
+    iters += it;
+    v_linsum(n, 1.0, y, 1.0, d, y);
+    t = t0 + (s + 1) * h;
+  }
+  *total_iters = iters;
+  free(f);
+  free(f1);
+  free(rhs);
+  free(d);
+  free(Y1);
+  return 0;
+}
+
 /* SDIRK2 (orc_sdirk2's stages) with a generic solver: ls 0 = PCG, 1 = SPGMR */
 int orc_sdirk2_ls(const orc_prob* p, double t0, double h, int nsteps, double tol, int ls, int maxl,
                   int max_restarts, int gstype, int jacobi, double* y, long* total_iters)

@@ -107,6 +107,8 @@ int orc_sdirk2_ls(const orc_prob* p, double t0, double h, int nsteps, double tol
 int orc_pfmg_vcycle(const orc_prob* p, double gamma, int relax, int nrelax, const double* r, double* z, int* nlevels);
 int orc_pcg_pfmg(const orc_prob* p, double gamma, int relax, int nrelax, const double* b, double* x, double tol,
                  int maxl, int* iters, double* relres);
+int orc_sdirk2_pfmg(const orc_prob* p, double t0, double h, int nsteps, double tol, int maxl, int relax, int nrelax,
+                    double* y, long* total_iters);
 int orc_nthreads(void);
 
 #ifdef __cplusplus

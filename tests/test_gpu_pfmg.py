@@ -61,3 +61,39 @@ def test_pfmg_rejects_periodic_and_bad_options(ctx, stslib):
     D = stslib.Problem(ctx, kind=0, nx=32, ny=32)
     with pytest.raises(stslib.STSError):
         stslib.PFMG(D, relax=3)
+
+
+def test_sdirk2_pfmg_bitwise(ctx, stslib, oracle):
+    pk = dict(kind=0, nx=40, ny=32, kx=1.0, ky=0.3)
+    G, O = stslib.Problem(ctx, **pk), oracle.Problem(**pk)
+    mg = stslib.PFMG(G, relax=2, nrelax=2)
+    y = G.initial()
+    its = stslib.sdirk2_evolve_pfmg(G, mg, y, 0.0, 0.01, 4, tol=1e-10)
+    y_o, it_o = O.sdirk2_pfmg(O.initial(), 0.0, 0.01, 4, tol=1e-10)
+    assert its == it_o > 0
+    assert np.array_equal(y.numpy(), y_o)
+    y_f, it_j = O.sdirk2(O.initial(), 0.0, 0.01, 4, tol=1e-10)
+    assert np.linalg.norm(y_o - y_f) / np.linalg.norm(y_f) < 1e-8 and its < it_j
+
+
+def test_cli_dirk_pfmg(stslib):
+    import os
+    import subprocess
+    stslib.lib()
+    exe = os.path.join(os.path.dirname(stslib.__file__), "_build", "diffusion_2D_gpu")
+    out = {}
+    for extra in ([], ["--pfmg_relax", "1", "--pfmg_nrelax", "3"], ["--pfmg"]):
+        r = subprocess.run([exe, "--problem", "manufactured", "--nx", "48", "--ny", "48", "--integrator", "dirk",
+                            "--fixedstep", "1e-3", "--tf", "0.01", "--nout", "2"] + extra,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        line = [l for l in r.stdout.split("\n") if l.startswith("Relative L2 error vs exact")][0]
+        its = [l for l in r.stdout.split("\n") if l.startswith("Linear solver iterations")][0]
+        out[" ".join(extra)] = (float(line.split("=")[1]), int(its.split("=")[1]))
+        if extra:
+            assert "pfmg relaxtype" in r.stdout
+    base = out[""]
+    for k, (err, its) in out.items():
+        assert abs(err - base[0]) <= 1e-6 * base[0]
+        if k:
+            assert its < base[1]
