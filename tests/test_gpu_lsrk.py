@@ -46,6 +46,17 @@ def test_fused_fp64_bitwise(ctx, stslib, oracle, nx, ny, method):
     run_pair(ctx, stslib, oracle, pk, ok, [0.02, 0.05])
 
 
+@pytest.mark.parametrize("method", [0, 1])
+@pytest.mark.parametrize("inhomogeneous", [False, True])
+def test_reference_mode_periodic_bitwise(ctx, stslib, oracle, method, inhomogeneous):
+    """The reference's own problem (periodic wrap, Gaussian x sine initial state,
+    initial.cpp:42-43; optional inhomogeneous faces, diffusion.cpp:36-46) through the
+    generic integrator path, bit for bit against the oracle."""
+    pk = dict(kind=2, nx=48, ny=40, kx=1.0, ky=0.5, inhomogeneous=inhomogeneous)
+    ok = dict(method=method, rtol=1e-5, atol=1e-9)
+    run_pair(ctx, stslib, oracle, pk, ok, [0.002, 0.01])
+
+
 @pytest.mark.parametrize("controller", [0, 1, 2, 3, 4, 5])
 def test_controllers_bitwise(ctx, stslib, oracle, controller):
     pk = dict(kind=0, nx=48, ny=40, kx=1.0, ky=0.01)
