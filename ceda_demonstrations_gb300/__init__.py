@@ -131,6 +131,7 @@ SIGNATURES = [
     ("STS_LSRKStepSetStageKernel", C.c_int, [_vp, C.c_int]),
     ("STS_LSRKStepGetStageKernelInfo", C.c_int, [_vp, _ip, _dp, C.c_char_p, C.c_int]),
     ("STS_LSRKStepSetUseGraphs", C.c_int, [_vp, C.c_int]),
+    ("STS_LSRKStepSetFusedPeriodic", C.c_int, [_vp, C.c_int]),
     ("STS_ARKodeEvolve", C.c_int, [_vp, C.c_double, _NV, _dp, C.c_int]),
     ("STS_ARKodeReset", C.c_int, [_vp, C.c_double, _NV]),
     ("STS_LSRKStepTimeStageKernel", C.c_int, [_vp, C.c_int, _dp]),
@@ -486,7 +487,7 @@ class LSRKStep:
 
     def __init__(self, ctx, rhs, t0, y0, method=RKC, rtol=1e-6, atol=1e-10, controller=PID,
                  smax=200, mixed=False, graphs=True, dom_eig=None, power=None, maxsteps=100000,
-                 hfixed=0.0, stage_kernel=0, dee_warmups=(0, 0), ssp=None):
+                 hfixed=0.0, stage_kernel=0, dee_warmups=(0, 0), ssp=None, fused_periodic=True):
         self.ctx = ctx
         L = lib()
         self._keep = []
@@ -522,6 +523,7 @@ class LSRKStep:
         L.STS_LSRKStepSetMaxNumStages(self.mem, smax)
         L.STS_LSRKStepSetMixedPrecision(self.mem, int(mixed))
         L.STS_LSRKStepSetUseGraphs(self.mem, int(graphs))
+        L.STS_LSRKStepSetFusedPeriodic(self.mem, int(fused_periodic))
         L.STS_LSRKStepSetStageKernel(self.mem, int(stage_kernel))
         L.STS_ARKodeSetMaxNumSteps(self.mem, maxsteps)
         L.STS_LSRKStepSetNumDomEigEstInitPreprocessIters(self.mem, int(dee_warmups[0]))

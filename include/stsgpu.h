@@ -241,6 +241,9 @@ int STS_LSRKStepGetStageKernelInfo(void* mem, int* variant, double* ms_per_launc
                                    int namelen);
 /* new: capture the fixed-s stage loop of the fused path in CUDA graphs (default on) */
 int STS_LSRKStepSetUseGraphs(void* mem, int on);
+/* new: reference mode (STS_PROBLEM_PERIODIC with STS_Diffusion): fused stage and step-end
+ * kernels (default on) or the plain RHS + N_Vector sequence; both give identical bits */
+int STS_LSRKStepSetFusedPeriodic(void* mem, int on);
 int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* tret, int itask); /* main.cpp:442 */
 /* ARKodeReset: restart from (t, y) keeping options, counters and the step size; F(t, y) is
  * re-evaluated on the next step */
