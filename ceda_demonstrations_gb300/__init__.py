@@ -201,6 +201,7 @@ SIGNATURES = [
     ("STS_NetSetWeights", C.c_int, [_vp, _fp]),
     ("STS_NetGetWeights", C.c_int, [_vp, _fp]),
     ("STS_NetSetTensorPath", C.c_int, [_vp, C.c_int]),
+    ("STS_NetSetCollapsedLevel0", C.c_int, [_vp, C.c_int]),
     ("STS_NetApply", C.c_int, [_vp, C.c_int, _vp, _vp, C.c_double, C.c_double, C.c_double,
                                C.c_double]),
     ("STS_NetLossGrad", C.c_int, [_vp, C.c_int, _vp, _vp, C.c_double, C.c_double, C.c_double,
@@ -939,6 +940,11 @@ class Net:
         w = np.ascontiguousarray(w.ravel())
         if lib().STS_NetSetWeights(self.h, w.ctypes.data_as(_fp)) != 0:
             _err("STS_NetSetWeights")
+
+    def set_collapsed_level0(self, on):
+        """Inference level 0 collapsed into two kernels (default) or layer by layer."""
+        if lib().STS_NetSetCollapsedLevel0(self.h, int(on)) != 0:
+            _err("STS_NetSetCollapsedLevel0")
 
     def set_tensor_path(self, path):
         """Inference convolutions: 0 = mma.sync (default), 1 = tcgen05 + TMEM + TMA."""

@@ -857,6 +857,205 @@ __global__ void __launch_bounds__(tc::COLS) conv3x3_tc_kernel(const __nv_bfloat1
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(32) : "memory");
 }
 
+// ---------------------------------------------------------------------------------------
+// Level 0 collapsed (inference). The input layer sees x = [v, v s_k, v s_g], so
+// h0 = conv(x, W_in) = conv(v, F) with F[o][t] = sum_c s_c W_in[o][c][t], and the last adjoint
+// layer combined with the output weights is u = conv(g0, G), G[o][t] = F[o][8 - t], with
+// g0 = h0 + 0.25 up(y1). Nothing at level 0 needs the 16-channel fine tensors:
+//   p0 = pool(h0) is a stride-2 4x4 convolution of v (kernel Kp = the pooled F);
+//   conv(h0, G) = conv(v, K), K = sum_o G_o * F_o the 5x5 composition, exact away from the
+//     image edges; on the edge rows and columns the part through h0 outside the image is
+//     removed by 5-tap 1-D corrections along the edge (and added back once at the corners);
+//   conv(0.25 up(y1), G) takes, per fine pixel parity, a 2x2 coarse kernel per channel.
+// So the fine level reads v (the FP64 residual) twice and y1 once and writes p0 and z: about
+// 32 bytes per fine pixel instead of ~100, with 64 + 25 + 64 FP32 FMAs per pixel on the CUDA
+// cores. The folded kernels are formed on the host from the BF16 weights and passed as kernel
+// parameters (constant bank, uniform reads).
+// ---------------------------------------------------------------------------------------
+namespace l0 {
+struct FoldA {
+  float Kp[CH][16]; // [o][qy*4 + qx], offsets -1 .. 2 from (2I, 2J)
+};
+struct FoldB {
+  float K[25];            // [sy*5 + sx], offsets -2 .. 2
+  float Gc[2][2][CH][4];  // [b][a][o][cy*2 + cx]: fine parity (a, b), coarse offset (cx + a - 1, cy + b - 1)
+  float CL[5], CR[5], CT[5], CB[5]; // edge corrections along the edge, offsets -2 .. 2
+  float corner[4];        // (0,0), (n-1,0), (0,n-1), (n-1,n-1) add-backs
+};
+// Both kernels work on 2-D tiles of the coarse grid: the CTA loads its input window (with the
+// halo) into shared memory, computes, stores; many small CTAs per SM hide the memory latency.
+// The folded weights are kernel parameters indexed with compile-time offsets, so they are read
+// from the constant bank as FMA operands and take no registers.
+constexpr int PTX = 64, PTY = 4; // p0 tile: coarse columns x rows (256 threads, one coarse pixel each)
+constexpr int ZTX = 32, ZTY = 4; // z tile: coarse cells (128 threads, one 2 x 2 fine cell each)
+
+// p0 = pool(conv(v, F)): stride-2 4x4 convolution, all 16 channels per thread
+__global__ void __launch_bounds__(PTX * PTY) p0_kernel(const double* __restrict__ r, double scale, int n, FoldA fa,
+                                                       __nv_bfloat16* __restrict__ p0)
+{
+  constexpr int WR = 2 * PTY + 2, WC = 2 * PTX + 2; // fine window: rows 2J0-1 .., columns 2I0-1 ..
+  __shared__ float vw[WR][WC + 2];
+  const int tid = threadIdx.x, tx = tid % PTX, ty = tid / PTX;
+  const int nc = n / 2;
+  const int I0 = blockIdx.x * PTX, J0 = blockIdx.y * PTY;
+  const float fs = (float)scale;
+  for (int e = tid; e < WR * WC; e += PTX * PTY)
+  {
+    const int wr = e / WC, wc = e % WC;
+    const int y = 2 * J0 - 1 + wr, x = 2 * I0 - 1 + wc;
+    vw[wr][wc] = (y >= 0 && y < n && x >= 0 && x < n) ? (float)__ldg(r + (long long)y * n + x) * fs : 0.f;
+  }
+  __syncthreads();
+  const int I = I0 + tx, J = J0 + ty;
+  if (I >= nc || J >= nc) return;
+  float win[16];
+#pragma unroll
+  for (int qy = 0; qy < 4; ++qy)
+#pragma unroll
+    for (int qx = 0; qx < 4; ++qx) win[qy * 4 + qx] = vw[2 * ty + qy][2 * tx + qx];
+  uint32_t o[8];
+#pragma unroll
+  for (int c = 0; c < CH; c += 2)
+  {
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+    {
+      a0 = fmaf(fa.Kp[c][k], win[k], a0);
+      a1 = fmaf(fa.Kp[c + 1][k], win[k], a1);
+    }
+    __nv_bfloat162 h = __floats2bfloat162_rn(a0, a1);
+    o[c / 2]         = *reinterpret_cast<uint32_t*>(&h);
+  }
+  uint4* dst = reinterpret_cast<uint4*>(p0 + ((long long)J * nc + I) * CH);
+  dst[0]     = make_uint4(o[0], o[1], o[2], o[3]);
+  dst[1]     = make_uint4(o[4], o[5], o[6], o[7]);
+}
+
+// z = (out_scale scale) r + (double)((float)out_scale u), u = conv(v, K) (+ edge corrections)
+// + conv(0.25 up(y1), G); thread = one coarse cell, its 2 x 2 fine pixels
+__global__ void __launch_bounds__(ZTX * ZTY) z_kernel(const double* __restrict__ r, double scale, double out_scale,
+                                                      int n, const __nv_bfloat16* __restrict__ y1, FoldB fb,
+                                                      double* __restrict__ z)
+{
+  constexpr int VR = 2 * ZTY + 4, VC = 2 * ZTX + 4; // fine window: rows 2J0-2 .., columns 2I0-2 ..
+  constexpr int YR = ZTY + 2, YC = ZTX + 2;         // coarse window: rows J0-1 .., columns I0-1 ..
+  __shared__ float vw[VR][VC + 1];
+  __shared__ float4 yw[YR][4][YC];
+  const int tid = threadIdx.x, tx = tid % ZTX, ty = tid / ZTX;
+  const int nc = n / 2;
+  const int I0 = blockIdx.x * ZTX, J0 = blockIdx.y * ZTY;
+  const float fs = (float)scale;
+  for (int e = tid; e < VR * VC; e += ZTX * ZTY)
+  {
+    const int wr = e / VC, wc = e % VC;
+    const int y = 2 * J0 - 2 + wr, x = 2 * I0 - 2 + wc;
+    vw[wr][wc] = (y >= 0 && y < n && x >= 0 && x < n) ? (float)__ldg(r + (long long)y * n + x) * fs : 0.f;
+  }
+  for (int e = tid; e < YR * YC * 2; e += ZTX * ZTY)
+  {
+    const int h = e & 1, k = (e >> 1) % YC, wr = (e >> 1) / YC;
+    const int cy = J0 - 1 + wr, cx = I0 - 1 + k;
+    uint4 q = make_uint4(0, 0, 0, 0);
+    if (cy >= 0 && cy < nc && cx >= 0 && cx < nc)
+      q = __ldg(reinterpret_cast<const uint4*>(y1 + ((long long)cy * nc + cx) * CH) + h);
+    const __nv_bfloat162* bq = reinterpret_cast<const __nv_bfloat162*>(&q);
+    const float2 a0 = __bfloat1622float2(bq[0]), a1 = __bfloat1622float2(bq[1]), a2 = __bfloat1622float2(bq[2]),
+                 a3 = __bfloat1622float2(bq[3]);
+    yw[wr][2 * h][k]     = make_float4(a0.x, a0.y, a1.x, a1.y);
+    yw[wr][2 * h + 1][k] = make_float4(a2.x, a2.y, a3.x, a3.y);
+  }
+  __syncthreads();
+  const int I = I0 + tx, J = J0 + ty;
+  if (I >= nc || J >= nc) return;
+  const long long row0 = (long long)(2 * J) * n;
+  const double2 r0 = __ldg(reinterpret_cast<const double2*>(r + row0 + 2 * I));
+  const double2 r1 = __ldg(reinterpret_cast<const double2*>(r + row0 + n + 2 * I));
+  // conv(v, K): window rows 2ty .. 2ty+5, columns 2tx .. 2tx+5
+  float u[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+  for (int wy = 0; wy < 6; ++wy)
+  {
+    float wv[6];
+#pragma unroll
+    for (int wx = 0; wx < 6; ++wx) wv[wx] = vw[2 * ty + wy][2 * tx + wx];
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+    {
+      const int sy = wy - b;
+      if (sy < 0 || sy > 4) continue;
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int sx = 0; sx < 5; ++sx) u[b][a] = fmaf(fb.K[sy * 5 + sx], wv[a + sx], u[b][a]);
+    }
+  }
+  // edge corrections (image columns / rows 0 and n-1); image column 0 is window column 2 when
+  // I0 = 0, image row 0 window row 2 when J0 = 0
+  if (I == 0)
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int d = 0; d < 5; ++d) u[b][0] = fmaf(-fb.CL[d], vw[2 * ty + b + d][2], u[b][0]);
+  if (I == nc - 1)
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int d = 0; d < 5; ++d) u[b][1] = fmaf(-fb.CR[d], vw[2 * ty + b + d][2 * tx + 3], u[b][1]);
+  if (J == 0)
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int d = 0; d < 5; ++d) u[0][a] = fmaf(-fb.CT[d], vw[2][2 * tx + a + d], u[0][a]);
+  if (J == nc - 1)
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int d = 0; d < 5; ++d) u[1][a] = fmaf(-fb.CB[d], vw[2 * ty + 3][2 * tx + a + d], u[1][a]);
+  if (I == 0 && J == 0) u[0][0] = fmaf(fb.corner[0], vw[2][2], u[0][0]);
+  if (I == nc - 1 && J == 0) u[0][1] = fmaf(fb.corner[1], vw[2][2 * tx + 3], u[0][1]);
+  if (I == 0 && J == nc - 1) u[1][0] = fmaf(fb.corner[2], vw[2 * ty + 3][2], u[1][0]);
+  if (I == nc - 1 && J == nc - 1) u[1][1] = fmaf(fb.corner[3], vw[2 * ty + 3][2 * tx + 3], u[1][1]);
+  // conv(0.25 up(y1), G): coarse rows J-1 .. J+1, columns I-1 .. I+1 (window rows ty .., columns tx ..)
+#pragma unroll
+  for (int dJ = 0; dJ < 3; ++dJ)
+#pragma unroll
+    for (int dI = 0; dI < 3; ++dI)
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+      {
+        const float4 yv = yw[ty + dJ][m][tx + dI];
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+        {
+          const int cy = dJ - b;
+          if (cy < 0 || cy > 1) continue;
+#pragma unroll
+          for (int a = 0; a < 2; ++a)
+          {
+            const int cx = dI - a;
+            if (cx < 0 || cx > 1) continue;
+            float acc = u[b][a];
+            acc       = fmaf(fb.Gc[b][a][4 * m + 0][cy * 2 + cx], yv.x, acc);
+            acc       = fmaf(fb.Gc[b][a][4 * m + 1][cy * 2 + cx], yv.y, acc);
+            acc       = fmaf(fb.Gc[b][a][4 * m + 2][cy * 2 + cx], yv.z, acc);
+            acc       = fmaf(fb.Gc[b][a][4 * m + 3][cy * 2 + cx], yv.w, acc);
+            u[b][a]   = acc;
+          }
+        }
+      }
+  const double osc = out_scale * scale;
+  const float fo   = (float)out_scale;
+  double2 z0, z1;
+  z0.x = __fma_rn(osc, r0.x, (double)(fo * u[0][0]));
+  z0.y = __fma_rn(osc, r0.y, (double)(fo * u[0][1]));
+  z1.x = __fma_rn(osc, r1.x, (double)(fo * u[1][0]));
+  z1.y = __fma_rn(osc, r1.y, (double)(fo * u[1][1]));
+  *reinterpret_cast<double2*>(z + row0 + 2 * I)     = z0;
+  *reinterpret_cast<double2*>(z + row0 + n + 2 * I) = z1;
+}
+} // namespace l0
+
 // The nine taps' B operands (B[n = output channel][k = input channel], K-major without
 // swizzle: byte t*512 + (n/8)*256 + (k/8)*128 + (n%8)*16 + (k%8)*2) of a layer, forward or
 // transposed (swapped channels, flipped taps), as frag_kernel's weights
@@ -1197,6 +1396,9 @@ struct STS_Net_ {
   __nv_bfloat16* wu  = nullptr; // forward UMMA B operands (tcgen05 inference), 9 x 256 per layer
   __nv_bfloat16* wut = nullptr; // transposed UMMA B operands
   int tensor_path    = 0;       // inference convolutions: 0 mma.sync (faster here), 1 tcgen05 + TMEM
+  std::vector<float> win_host;  // W_in (FP32 master) on the host, for the folded level-0 kernels
+  bool win_stale     = true;
+  bool collapse_l0   = true;    // inference level 0 by the collapsed kernels (l0::p0_kernel, z_kernel)
   net::Level L[4];
   double* z       = nullptr; // FP64 output at the finest level
   double* dacc    = nullptr;
@@ -1282,6 +1484,93 @@ static void refresh_frags(STS_Net nt)
     net::tc_weight_kernel<<<9, 256, 0, st>>>(nt->w + l * WSZ, nt->wu + l * 9 * 256, 0);
     net::tc_weight_kernel<<<9, 256, 0, st>>>(nt->w + l * WSZ, nt->wut + l * 9 * 256, 1);
   }
+  nt->win_stale = true;
+}
+
+static float bf16_round_host(float x)
+{
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  u = (u + 0x7FFFu + ((u >> 16) & 1u)) & 0xFFFF0000u;
+  float y;
+  std::memcpy(&y, &u, 4);
+  return y;
+}
+
+static int floor_half(int x) { return x >= 0 ? x / 2 : -((1 - x) / 2); }
+
+// the folded level-0 kernels of a system (features s_k, s_g) from the BF16 input-layer weights;
+// host work, outside any graph capture (it may copy the weights back once after an update)
+static bool l0_prepare(STS_Net nt, float sk, float sg, net::l0::FoldA* fa, net::l0::FoldB* fb)
+{
+  if (nt->win_stale)
+  {
+    nt->win_host.resize(WSZ);
+    if (!STS_CUDA_OK(cudaMemcpyAsync(nt->win_host.data(), nt->w + net::L_IN * WSZ, WSZ * sizeof(float),
+                                     cudaMemcpyDeviceToHost, nt->ctx->stream)) ||
+        !STS_CUDA_OK(cudaStreamSynchronize(nt->ctx->stream)))
+      return false;
+    nt->win_stale = false;
+  }
+  const float* W = nt->win_host.data();
+  double F[CH][9], G[CH][9];
+  const double s[3] = {1.0, (double)sk, (double)sg};
+  for (int o = 0; o < CH; ++o)
+    for (int t = 0; t < 9; ++t)
+    {
+      double f = 0.0;
+      for (int c = 0; c < 3; ++c) f += s[c] * (double)bf16_round_host(W[(o * CH + c) * 9 + t]);
+      F[o][t] = f;
+    }
+  for (int o = 0; o < CH; ++o)
+    for (int t = 0; t < 9; ++t) G[o][t] = F[o][8 - t];
+  double Kp[CH][16] = {}, K[25] = {}, Gc[2][2][CH][4] = {}, C[4][5] = {}, corner[4] = {};
+  for (int o = 0; o < CH; ++o)
+    for (int dy = 0; dy < 3; ++dy)
+      for (int dx = 0; dx < 3; ++dx)
+      {
+        const double f = F[o][dy * 3 + dx], g = G[o][dy * 3 + dx];
+        for (int b = 0; b < 2; ++b)
+          for (int a = 0; a < 2; ++a)
+          {
+            Kp[o][(b + dy) * 4 + (a + dx)] += 0.25 * f;
+            const int cx = floor_half(a + dx - 1) - (a - 1), cy = floor_half(b + dy - 1) - (b - 1);
+            Gc[b][a][o][cy * 2 + cx] += 0.25 * g;
+          }
+        for (int ey = 0; ey < 3; ++ey)
+          for (int ex = 0; ex < 3; ++ex) K[(dy + ey) * 5 + (dx + ex)] += g * F[o][ey * 3 + ex];
+      }
+  for (int o = 0; o < CH; ++o)
+  {
+    for (int d = 0; d < 3; ++d)
+      for (int e = 0; e < 3; ++e)
+      {
+        C[0][d + e] += G[o][d * 3 + 0] * F[o][e * 3 + 2]; // left edge (column 0)
+        C[1][d + e] += G[o][d * 3 + 2] * F[o][e * 3 + 0]; // right edge
+        C[2][d + e] += G[o][0 * 3 + d] * F[o][2 * 3 + e]; // top edge (row 0)
+        C[3][d + e] += G[o][2 * 3 + d] * F[o][0 * 3 + e]; // bottom edge
+      }
+    corner[0] += G[o][0] * F[o][8];
+    corner[1] += G[o][2] * F[o][6];
+    corner[2] += G[o][6] * F[o][2];
+    corner[3] += G[o][8] * F[o][0];
+  }
+  for (int o = 0; o < CH; ++o)
+    for (int k = 0; k < 16; ++k) fa->Kp[o][k] = (float)Kp[o][k];
+  for (int k = 0; k < 25; ++k) fb->K[k] = (float)K[k];
+  for (int b = 0; b < 2; ++b)
+    for (int a = 0; a < 2; ++a)
+      for (int o = 0; o < CH; ++o)
+        for (int k = 0; k < 4; ++k) fb->Gc[b][a][o][k] = (float)Gc[b][a][o][k];
+  for (int d = 0; d < 5; ++d)
+  {
+    fb->CL[d] = (float)C[0][d];
+    fb->CR[d] = (float)C[1][d];
+    fb->CT[d] = (float)C[2][d];
+    fb->CB[d] = (float)C[3][d];
+  }
+  for (int k = 0; k < 4; ++k) fb->corner[k] = (float)corner[k];
+  return true;
 }
 
 extern "C" STS_Net STS_NetCreate(STS_Context ctx, int nmax, unsigned long long seed)
@@ -1517,7 +1806,7 @@ static void net_forward(STS_Net nt, int n, int nimg, const T* r, double scale, f
 // first convolution's tile loader and the sums g_l = h_l + poolT(y_{l+1}) in the transposed
 // convolutions' loaders, so only h_l, p_l and y_l are stored. Bitwise the output of net_forward.
 static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, float sk, float sg, double out_scale,
-                              double* zout)
+                              double* zout, const net::l0::FoldA* fa = nullptr, const net::l0::FoldB* fb = nullptr)
 {
   net::Level* L = nt->L;
   net::LoadArgs la;
@@ -1548,9 +1837,18 @@ static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
     conv_tc<2, net::LD_UPADD>(nt, L[0].h, n, nt->wut + net::L_IN * WL, nullptr, zout, out_scale, lu); // z
     return;
   }
-  // mma.sync path (the training kernels)
-  conv_launch<0, net::LD_R64, true, true>(nt, nullptr, n, 1, nt->wf + net::L_IN * 576, L[0].h, nullptr, 0.0, nullptr, la,
-                                          L[1].p);                                     // h0, p0
+  const bool collapsed = nt->collapse_l0 && fa && fb && n % 2 == 0;
+  cudaStream_t st      = nt->ctx->stream;
+  // level 0 collapsed (p0 straight from r, z straight from r and y1), or the mma.sync path
+  if (collapsed)
+  {
+    const int nc = n / 2;
+    dim3 g((unsigned)((nc + net::l0::PTX - 1) / net::l0::PTX), (unsigned)((nc + net::l0::PTY - 1) / net::l0::PTY));
+    net::l0::p0_kernel<<<g, net::l0::PTX * net::l0::PTY, 0, st>>>(r, scale, n, *fa, L[1].p); // p0
+  }
+  else
+    conv_launch<0, net::LD_R64, true, true>(nt, nullptr, n, 1, nt->wf + net::L_IN * 576, L[0].h, nullptr, 0.0, nullptr,
+                                            la, L[1].p); // h0, p0
   conv(nt, L[1].p, n / 2, 1, net::L_1, false, L[1].h, L[2].p);                         // h1, p1
   conv(nt, L[2].p, n / 4, 1, net::L_2, false, L[2].h, L[3].p);                         // h2, p2
   conv(nt, L[3].p, n / 8, 1, net::L_3, false, L[3].h);                                                // h3
@@ -1559,6 +1857,13 @@ static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
   conv_launch<0, net::LD_UPADD>(nt, L[2].h, n / 4, 1, nt->wt + net::L_2 * 576, L[2].y, nullptr, 0.0, nullptr, lu); // y2
   lu.coarse = L[2].y;
   conv_launch<0, net::LD_UPADD>(nt, L[1].h, n / 2, 1, nt->wt + net::L_1 * 576, L[1].y, nullptr, 0.0, nullptr, lu); // y1
+  if (collapsed)
+  {
+    const int nc = n / 2;
+    dim3 g((unsigned)((nc + net::l0::ZTX - 1) / net::l0::ZTX), (unsigned)((nc + net::l0::ZTY - 1) / net::l0::ZTY));
+    net::l0::z_kernel<<<g, net::l0::ZTX * net::l0::ZTY, 0, st>>>(r, scale, out_scale, n, L[1].y, *fb, zout); // z
+    return;
+  }
   lu.coarse = L[1].y;
   lu.r      = r;
   lu.scale  = scale;
@@ -1629,6 +1934,13 @@ static bool net_size_ok(STS_Net nt, int n)
 }
 
 // z = M r for one n x n residual (device pointers): z = jacobi * net(scale r) / scale
+extern "C" int STS_NetSetCollapsedLevel0(STS_Net nt, int on)
+{
+  if (!nt) return -1;
+  nt->collapse_l0 = on != 0;
+  return 0;
+}
+
 extern "C" int STS_NetSetTensorPath(STS_Net nt, int path)
 {
   if (!nt || (path != 0 && path != 1)) return -1;
@@ -1641,7 +1953,10 @@ extern "C" int STS_NetApply(STS_Net nt, int n, const double* r, double* z, doubl
 {
   if (!net_size_ok(nt, n) || !r || !z || !(scale > 0.0)) return -1;
   ctx_activate(nt->ctx);
-  net_forward_infer(nt, n, r, scale, (float)sk, (float)sg, jacobi / scale, z);
+  net::l0::FoldA fa;
+  net::l0::FoldB fb;
+  if (!l0_prepare(nt, (float)sk, (float)sg, &fa, &fb)) return -1;
+  net_forward_infer(nt, n, r, scale, (float)sk, (float)sg, jacobi / scale, z, &fa, &fb);
   return STS_CUDA_OK(cudaGetLastError()) ? 0 : -1;
 }
 
@@ -2083,7 +2398,9 @@ extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b,
     dim3 gm(gx, (unsigned)((p->ny + net::FCG_ROWS - 1) / net::FCG_ROWS));
     cudaGraph_t g;
     cudaGraphExec_t ge = nullptr;
-    bool ok = STS_CUDA_OK(cudaStreamSynchronize(st)) &&
+    net::l0::FoldA fa;
+    net::l0::FoldB fb;
+    bool ok = l0_prepare(nt, (float)sk, (float)sg, &fa, &fb) && STS_CUDA_OK(cudaStreamSynchronize(st)) &&
               STS_CUDA_OK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     if (ok)
     {
@@ -2091,7 +2408,7 @@ extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b,
       {
         double *pp = P2[k & 1], *pn = P2[(k + 1) & 1];
         double *qp = Q2[k & 1], *qn = Q2[(k + 1) & 1];
-        net_forward_infer(nt, n, r, scale, (float)sk, (float)sg, jac / scale, z);
+        net_forward_infer(nt, n, r, scale, (float)sk, (float)sg, jac / scale, z, &fa, &fb);
         net::fcg_beta_kernel<<<eb, 256, 0, st>>>(N, z, qp, d_s);
         net::fcg_pq_march_kernel<<<gm, bq, 0, st>>>(p->dev, z, pp, r, pn, qn, d_s, d_out);
         net::fcg_x_kernel<<<eb, 256, 0, st>>>(N, pn, qn, NVD(x), r, d_s, d_out);

@@ -401,6 +401,11 @@ int STS_NetGetWeights(STS_Net net, float* w);
  * the faster of the two at 2048^2), 1 = tcgen05 tensor cores with TMEM accumulators, 1-D TMA
  * bulk loads and stores; both compute the same network */
 int STS_NetSetTensorPath(STS_Net net, int path);
+/* inference level 0 collapsed (default 1): p0 as a stride-2 4x4 convolution of the input and
+ * z from a 5x5 convolution of the input plus a coarse-parity convolution of y1, with the
+ * system features folded into the weights, so no 16-channel fine-level tensor is formed;
+ * 0 = the layer-by-layer kernels. The same network either way. */
+int STS_NetSetCollapsedLevel0(STS_Net net, int on);
 int STS_NetApply(STS_Net net, int n, const double* r, double* z, double sk, double sg, double jacobi,
                  double scale);
 /* one sample (scale 1): loss = 0.5 (z - e)^T M (z - e) / (e^T M e) with M = I - gamma A on the

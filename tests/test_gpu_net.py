@@ -79,6 +79,30 @@ def test_tcgen05_and_mma_sync_paths_agree(ctx, weights, n):
     assert _rel(out[0], out[1]) < 1e-2
 
 
+@pytest.mark.parametrize("n", [64, 128, 384])
+def test_collapsed_level0_matches_layers(ctx, weights, n):
+    """Level 0 collapsed into two kernels (stride-2 4x4 convolution for p0; 5x5 convolution
+    with edge corrections plus coarse-parity kernels for z) is the same network as the
+    layer-by-layer kernels: both within the oracle tolerance, within BF16 rounding of each
+    other, and the collapsed form (no BF16 rounding of the fine-level tensors) closer to the
+    FP64 reference."""
+    rng = np.random.default_rng(n + 7)
+    r = rng.standard_normal((n, n))
+    net = sts.Net(ctx, 384, seed=0)
+    net.set_weights(weights)
+    rv = sts.NVector.from_numpy(ctx, r)
+    zv = sts.NVector(ctx, n * n)
+    out = []
+    for on in (True, False):
+        net.set_collapsed_level0(on)
+        net.apply(n, rv.ptr, zv.ptr, -0.4, 0.7, 0.6, 1.0)
+        out.append(zv.numpy().reshape(n, n))
+    zref, _ = convnet.forward(weights, r, -0.4, 0.7, 0.6)
+    e_col, e_lay = _rel(out[0], zref), _rel(out[1], zref)
+    assert e_col < FWD_TOL and e_lay < FWD_TOL and e_col <= e_lay
+    assert _rel(out[0], out[1]) < 1e-2
+
+
 def test_weights_round_trip(ctx, weights):
     net = sts.Net(ctx, 64, seed=1)
     net.set_weights(weights)
