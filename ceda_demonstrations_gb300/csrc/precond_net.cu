@@ -2496,7 +2496,7 @@ extern "C" int STS_ImplicitSolveLearned(STS_Problem p, double gamma, STS_Net nt,
     sts_set_error("STS_ImplicitSolveLearned: invalid arguments");
     return -1;
   }
-  if (!(kappa_min > 0.0)) kappa_min = 6000.0;
+  if (!(kappa_min > 0.0)) kappa_min = 1500.0;
   const double kappa = 1.0 + 4.0 * gamma * (p->cx + p->cy);
   const bool net_ok  = nt && p->nx == p->ny && p->kind != STS_PROBLEM_PERIODIC && p->nx % 16 == 0 && p->nx <= nt->nmax;
   if (used_net) *used_net = 0;

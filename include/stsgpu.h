@@ -434,7 +434,7 @@ int STS_HarvestPCGPairs(STS_Problem p, double gamma, N_Vector b, int ncrops, int
 int STS_FCGSolve(STS_Problem p, double gamma, STS_Net net, N_Vector b, N_Vector x, double tol,
                  int maxit, int* iters, double* relres);
 /* Learned-or-Jacobi shifted solve: FCG with the network when kappa = 1 + 4 gamma (cx + cy)
- * >= kappa_min (<= 0: 6000, the measured break-even of the network's per-iteration cost on
+ * >= kappa_min (<= 0: 1500, the measured break-even of the network's per-iteration cost on
  * GB300), otherwise the fused Jacobi-PCG; used_net reports the choice. Same return codes. */
 int STS_ImplicitSolveLearned(STS_Problem p, double gamma, STS_Net net, N_Vector b, N_Vector x,
                              double tol, int maxit, double kappa_min, int* iters, double* relres,
