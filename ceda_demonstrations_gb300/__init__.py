@@ -74,6 +74,7 @@ SIGNATURES = [
     ("STS_ContextGetStream", _vp, [_vp]),
     ("STS_GetLastError", C.c_char_p, []),
     ("STS_DeviceCount", C.c_int, []),
+    ("STS_WaitSelfTest", C.c_int, [_vp, C.c_int, C.c_longlong]),
     ("N_VNew_Sts", _NV, [_ll, _vp]),
     ("N_VNewEmpty_Sts", _NV, [_vp]),
     ("N_VMake_Sts", _NV, [_ll, _vp, _vp]),
@@ -272,6 +273,12 @@ class Context:
     @property
     def stream(self):
         return lib().STS_ContextGetStream(self.h)
+
+    def wait_self_test(self, arrive, limit=1000):
+        """Run the bounded-wait failure path on one pipeline barrier: returns the status
+        (0 when the barrier completed, STS_ERR_FAILURE when the wait ran out after `limit`
+        polls and the context's error word was read and cleared)."""
+        return lib().STS_WaitSelfTest(self.h, int(bool(arrive)), limit)
 
     def free(self):
         # Garbage collection of reference cycles (for example frames kept by a traceback)

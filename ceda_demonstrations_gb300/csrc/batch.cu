@@ -131,7 +131,8 @@ __device__ int d_stages(int method, double h, double rho, int smax, double* hmax
     ss    = ceil((sqrt(9.0 + 8.0 * h * rho) - 1.0) / 2.0);
     *hmax = (rho > 0.0) ? 0.96 * (sm * sm + sm - 2.0) / (2.0 * rho) : 1e300;
   }
-  if (ss < 2.0) ss = 2.0;
+  // a non-finite step (NaN state) gives the 2-stage minimum, as max(ss, 2) does
+  if (!(ss >= 2.0)) ss = 2.0;
   if (ss > 1e9) ss = 1e9;
   return (int)ss;
 }
@@ -317,6 +318,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
       double h = (100.0 * h0 < h1) ? 100.0 * h0 : h1;
       if (h > prm.tf) h = prm.tf;
       hnext = h;
+      if (!(h > 0.0)) status = -3; // a non-finite state gives no usable step
     }
 
     while (t < prm.tf && status == 0)

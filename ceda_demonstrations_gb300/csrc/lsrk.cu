@@ -133,7 +133,8 @@ extern "C" int STS_LSRKStagesNeeded(int method, double h, double rho, int smax, 
     ss    = ceil((sqrt(9.0 + 8.0 * h * rho) - 1.0) / 2.0);
     *hmax = (rho > 0.0) ? 0.96 * (sm * sm + sm - 2.0) / (2.0 * rho) : INFINITY;
   }
-  if (ss < 2.0) ss = 2.0;
+  // a non-finite step (NaN state) gives the 2-stage minimum, as max(ss, 2) does
+  if (!(ss >= 2.0)) ss = 2.0;
   if (ss > 1e9) ss = 1e9;
   return (int)ss;
 }
@@ -1006,7 +1007,11 @@ static int evolve_fused(LSRKMem* m, double target, int itask)
     if (!(m->hnext > 0.0))
     {
       double h0 = initial_step(m, m->yb[m->par], m->Fb[m->par], target - m->t);
-      if (!(h0 > 0.0)) return STS_ERR_FAILURE;
+      if (!(h0 > 0.0))
+      {
+        sts_set_error("LSRKStep: no usable initial step (RHS failure or non-finite state)");
+        return STS_ERR_FAILURE;
+      }
       m->hnext = h0;
     }
     int nef = 0;
@@ -1237,7 +1242,11 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
     if (!(m->hnext > 0.0))
     {
       double h0 = initial_step(m, NVD(y), NVD(F), target - m->t);
-      if (!(h0 > 0.0)) return STS_ERR_FAILURE;
+      if (!(h0 > 0.0))
+      {
+        sts_set_error("LSRKStep: no usable initial step (RHS failure or non-finite state)");
+        return STS_ERR_FAILURE;
+      }
       m->hnext = h0;
     }
     int nef = 0, ncf_step = 0;

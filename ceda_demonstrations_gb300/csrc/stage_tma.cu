@@ -77,9 +77,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
   return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit = WAIT_LIMIT)
 {
-  for (long long i = 0; i < WAIT_LIMIT; ++i)
+  for (long long i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -364,4 +364,45 @@ bool tma_stage32_launch(const TmaStage32* t, int variant, int num_sms, const Pro
   case 5: return launch_any<C5>(t, num_sms, P, A, im1, im2, if0, out, err, st);
   default: return false;
   }
+}
+
+// Bounded-wait self-test. One warp arms a pipeline barrier (arrival count 1) and waits on its
+// first phase with the stage kernel's try_wait loop, `limit` polls at most. With `arrive` set,
+// lane 0 arrives before the wait and the phase completes; without it nothing arrives, the wait
+// runs out and the kernel writes the context's error word exactly as a stalled tile pipeline
+// does, then returns. No copy is in flight, so nothing is left to drain.
+static __global__ void wait_selftest_kernel(int arrive, long long limit, int* err)
+{
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (threadIdx.x == 0 && arrive)
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bar)) : "memory");
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(&bar, 0u, limit);
+  if (!ok && threadIdx.x == 0) *(volatile int*)err = 1;
+}
+
+extern "C" int STS_WaitSelfTest(STS_Context ctx, int arrive, long long limit)
+{
+  if (!ctx || limit < 1 || limit > (1LL << 20))
+  {
+    sts_set_error("WaitSelfTest: limit must be in [1, 2^20] polls");
+    return STS_ILL_INPUT;
+  }
+  if (!ctx_activate(ctx)) return STS_ERR_FAILURE;
+  if (*(volatile int*)ctx->h_err)
+  {
+    sts_set_error("WaitSelfTest: the context's error word is already set");
+    return STS_ERR_FAILURE;
+  }
+  wait_selftest_kernel<<<1, 32, 0, ctx->stream>>>(arrive ? 1 : 0, limit, ctx->d_err);
+  if (!STS_CUDA_OK(cudaGetLastError()) || !STS_CUDA_OK(cudaStreamSynchronize(ctx->stream))) return STS_ERR_FAILURE;
+  if (*(volatile int*)ctx->h_err)
+  {
+    *ctx->h_err = 0;
+    sts_set_error("WaitSelfTest: the barrier wait timed out after %lld polls", limit);
+    return STS_ERR_FAILURE;
+  }
+  return STS_SUCCESS;
 }

@@ -35,6 +35,14 @@ int STS_ContextSynchronize(STS_Context ctx);
 void* STS_ContextGetStream(STS_Context ctx); /* cudaStream_t */
 const char* STS_GetLastError(void);
 int STS_DeviceCount(void);
+/* Failure-detection self-test (no reference counterpart; the reference has no device-side
+ * waits). Every spin on a pipeline barrier in this library is bounded: a wait that runs out
+ * sets the context's error word, the kernel drains what it has in flight and returns, and the
+ * host turns the word into STS_ERR_FAILURE with the context still usable. This entry point
+ * runs that path on one barrier: with `arrive` nonzero the barrier completes and the call
+ * returns STS_SUCCESS; with `arrive` 0 nothing arrives, the wait gives up after `limit` polls
+ * (1 .. 2^20) and the call returns STS_ERR_FAILURE and clears the word. */
+int STS_WaitSelfTest(STS_Context ctx, int arrive, long long limit);
 
 /* ------------------------------------------------------------------------------------
  * N_Vector (device). Layout {content, ops, sunctx} as SUNDIALS' generic N_Vector; the ops

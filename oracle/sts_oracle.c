@@ -637,7 +637,8 @@ int orc_stages_needed(int method, double h, double rho, int smax, double* hmax)
     ss    = ceil((sqrt(9.0 + 8.0 * h * rho) - 1.0) / 2.0);
     *hmax = (rho > 0.0) ? 0.96 * (sm * sm + sm - 2.0) / (2.0 * rho) : INFINITY;
   }
-  if (ss < 2.0) ss = 2.0;
+  /* a non-finite step (NaN state) gives the 2-stage minimum, as max(ss, 2) does */
+  if (!(ss >= 2.0)) ss = 2.0;
   if (ss > 1e9) ss = 1e9;
   return (int)ss;
 }
@@ -1048,7 +1049,16 @@ int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double 
       st->steps_since_dee = 0;
     }
     if (!(st->hnext > 0.0))
+    {
       st->hnext = initial_step(p, o, st->t, y, st->F, tout - st->t, st->spectral_radius, &st->nfe);
+      if (!(st->hnext > 0.0))
+      {
+        /* a non-finite state (NaN / Inf) gives no usable step: the call fails before any
+         * attempt, as an unrecoverable failure */
+        ret = -3;
+        goto done;
+      }
+    }
 
     int nef = 0;
     for (;;)
@@ -2201,7 +2211,15 @@ int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_st
       ret = -1;
       break;
     }
-    if (!(st->hnext > 0.0)) st->hnext = initial_step_ord(p, o, st->t, y, st->F, tout - st->t, 0.0, &st->nfe, ordv);
+    if (!(st->hnext > 0.0))
+    {
+      st->hnext = initial_step_ord(p, o, st->t, y, st->F, tout - st->t, 0.0, &st->nfe, ordv);
+      if (!(st->hnext > 0.0))
+      {
+        ret = -3; /* non-finite state: no usable step */
+        goto done;
+      }
+    }
     int nef = 0;
     for (;;)
     {

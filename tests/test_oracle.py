@@ -140,6 +140,12 @@ def test_product_step_rules_equal_oracle(oracle, stslib):
         nh = int(rng.integers(0, 4))
         assert L.STS_AdaptControllerEstimate(ctrl, h, dsm, ep1, ep2, hp, nh) == \
             oracle.controller(ctrl, h, dsm, ep1, ep2, hp, nh)
+    # a non-finite step (from a NaN state) takes the 2-stage minimum on both sides, the
+    # semantics of max(ss, 2) with an unordered comparison, not an undefined integer conversion
+    for method in (0, 1):
+        for h in (float("nan"), float("-inf")):
+            s = L.STS_LSRKStagesNeeded(method, h, 1e4, 200, C.byref(hm))
+            assert s == 2 and oracle.stages_needed(method, h, 1e4, 200)[0] == 2
 
 
 def test_gustafsson_controllers(oracle):
@@ -372,3 +378,20 @@ def test_oracle_pfmg_vcycle_is_spd_and_converges(oracle):
             x, rc, it, rel = P.pcg_pfmg(gamma, b, tol=1e-10, relax=relax)
             _, it_j, _ = P.pcg(gamma, b, tol=1e-10)
             assert rc == 0 and rel <= 1e-10 and it <= 12 and it_j > 3 * it
+
+
+def test_oracle_nonfinite_state_fails_cleanly(oracle):
+    """A NaN or Inf in the initial state: the initial step estimate is not finite, so the call
+    ends with ARK_ERR_FAILURE (-3) before any step attempt, with the counters consistent."""
+    for kind in (0, 2):
+        for mixed in ((False, True) if kind == 0 else (False,)):
+            for val in (np.nan, np.inf, -np.inf):
+                P = oracle.Problem(kind=kind, nx=16, ny=12)
+                y = P.initial()
+                y[37] = val
+                J = oracle.Integrator(P, y, method=1, mixed=mixed)
+                assert J.evolve(0.01) == -3
+                s = J.stats()
+                assert s["t"] == 0.0 and s["nst"] == 0
+                assert s["nst_attempts"] == 0 and s["netf"] == 0
+                assert s["stages_total"] == 0 and s["nfe"] == 2
