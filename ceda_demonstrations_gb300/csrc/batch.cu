@@ -746,6 +746,7 @@ extern "C" int STS_BatchSetInitialModes(STS_Batch b, int nmodes, const int* p, c
 extern "C" int STS_BatchEvolve(STS_Batch b, double tf, int method, double rtol, double atol, int smax, int controller,
                                long long maxsteps)
 {
+  STS_MARK_FUNCTION;
   if (!b || !(tf > 0.0) || smax < 2 || smax > 10000) return STS_ILL_INPUT;
   if (controller < STS_ADAPT_PID || controller > STS_ADAPT_IMEX_GUS) return STS_ILL_INPUT;
   if (method != STS_LSRK_RKC_2 && method != STS_LSRK_RKL_2) return STS_ILL_INPUT;

@@ -295,6 +295,7 @@ int sts_rhs_launch(STS_Problem p, double t, const double* u, double* f, bool for
 
 extern "C" int STS_Diffusion(double t, N_Vector u, N_Vector f, void* user_data)
 {
+  STS_MARK_FUNCTION;
   STS_Problem p = (STS_Problem)user_data;
   if (!check_vec(p, u, "STS_Diffusion") || !check_vec(p, f, "STS_Diffusion")) return -1;
   ctx_activate(p->ctx);
@@ -390,6 +391,7 @@ __global__ void jacobi_kernel(ProbDev P, double gamma, const double* __restrict_
 extern "C" int STS_PSetup(double t, N_Vector u, N_Vector f, int jok, int* jcurPtr, double gamma,
                           void* user_data)
 {
+  STS_MARK_FUNCTION;
   (void)t;
   (void)u;
   (void)f;
@@ -404,6 +406,7 @@ extern "C" int STS_PSetup(double t, N_Vector u, N_Vector f, int jok, int* jcurPt
 extern "C" int STS_PSolve(double t, N_Vector u, N_Vector f, N_Vector r, N_Vector z, double gamma,
                           double delta, int lr, void* user_data)
 {
+  STS_MARK_FUNCTION;
   (void)t;
   (void)u;
   (void)f;

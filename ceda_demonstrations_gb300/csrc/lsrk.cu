@@ -817,6 +817,7 @@ static void fill_params(LSRKMem* m, STS_Problem p, double t, double h, int s, co
 // ---------------------------------------------------------------------------------------
 static int dee_update(LSRKMem* m, N_Vector ycur, N_Vector fcur)
 {
+  STS_MARK_REGION("DomEig");
   double lam = 0.0, lami = 0.0;
   if (m->power)
   {
@@ -1612,6 +1613,7 @@ extern "C" int STS_LSRKStepSetFusedPeriodic(void* mem, int on)
 
 extern "C" int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* tret, int itask)
 {
+  STS_MARK_REGION("Evolve");
   CHECK_MEM(mem);
   LSRKMem* m = MEM(mem);
   if (!yout || NVL(yout) != m->n)

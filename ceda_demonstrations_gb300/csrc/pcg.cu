@@ -296,6 +296,7 @@ int sts_pcg_run(STS_Problem p, double gamma, N_Vector b, N_Vector x, double tol,
 extern "C" int STS_ImplicitSolvePCG(STS_Problem p, double gamma, N_Vector b, N_Vector x, double tol, int maxit,
                                     int jacobi, int* iters, double* relres)
 {
+  STS_MARK_FUNCTION;
   return sts_pcg_run(p, gamma, b, x, tol, maxit, jacobi, iters, relres, nullptr);
 }
 
@@ -565,6 +566,7 @@ static int spgmr_solve(LinSol* L, N_Vector x, N_Vector b, double delta)
 
 extern "C" int STS_SUNLinSolSolve(void* LS, N_Vector x, N_Vector b, double delta)
 {
+  STS_MARK_FUNCTION;
   LinSol* L = (LinSol*)LS;
   if (!L || !L->atimes || !x || !b) return -1;
   L->last_iters = 0;
@@ -634,6 +636,7 @@ static int sdirk2_run(STS_Problem p, N_Vector y, double t0, double h, int nsteps
 extern "C" int STS_SDIRK2Evolve(STS_Problem p, N_Vector y, double t0, double h, int nsteps, double tol, int maxit,
                                 long long* total_iters)
 {
+  STS_MARK_FUNCTION;
   return sdirk2_run(p, y, t0, h, nsteps, total_iters, [&](double hg, N_Vector rhs, N_Vector d, int* it) {
     double rel;
     return STS_ImplicitSolvePCG(p, hg, rhs, d, tol, maxit, 1, it, &rel);
@@ -666,6 +669,7 @@ int jacobi_psolve(void* d, N_Vector r, N_Vector z, double tol, int lr)
 extern "C" int STS_SDIRK2EvolveLS(STS_Problem p, void* LS, int precond, N_Vector y, double t0, double h,
                                   int nsteps, double tol, long long* total_iters)
 {
+  STS_MARK_FUNCTION;
   LinSol* L = (LinSol*)LS;
   if (!p || !L || !y) return -1;
   ShiftedOp op{p, 0.0, N_VClone_Sts(y)};
@@ -688,6 +692,7 @@ extern "C" int STS_SDIRK2EvolveLS(STS_Problem p, void* LS, int precond, N_Vector
 extern "C" int STS_SDIRK2EvolvePFMG(STS_Problem p, STS_PFMG mg, N_Vector y, double t0, double h, int nsteps,
                                     double tol, int maxit, long long* total_iters)
 {
+  STS_MARK_FUNCTION;
   if (!mg) return -1;
   return sdirk2_run(p, y, t0, h, nsteps, total_iters, [&](double hg, N_Vector rhs, N_Vector d, int* it) {
     double rel;
@@ -700,6 +705,7 @@ extern "C" int STS_SDIRK2EvolvePFMG(STS_Problem p, STS_PFMG mg, N_Vector y, doub
 extern "C" int STS_SDIRK2EvolveLearned(STS_Problem p, STS_Net net, N_Vector y, double t0, double h, int nsteps,
                                        double tol, int maxit, long long* total_iters)
 {
+  STS_MARK_FUNCTION;
   return sdirk2_run(p, y, t0, h, nsteps, total_iters, [&](double hg, N_Vector rhs, N_Vector d, int* it) {
     double rel;
     int used;

@@ -298,6 +298,7 @@ extern "C" long long STS_PFMGNumVCycles(STS_PFMG mg) { return mg ? mg->vcycles :
 // PSetup (preconditioner_hypre.cpp:13-108): the hierarchy and the captured V-cycle for gamma
 extern "C" int STS_PFMGPSetup(double t, N_Vector u, N_Vector f, int jok, int* jcurPtr, double gamma, void* user_data)
 {
+  STS_MARK_FUNCTION;
   (void)t;
   (void)u;
   (void)f;
@@ -328,6 +329,7 @@ extern "C" int STS_PFMGPSetup(double t, N_Vector u, N_Vector f, int jok, int* jc
 extern "C" int STS_PFMGPSolve(double t, N_Vector u, N_Vector f, N_Vector r, N_Vector z, double gamma, double delta,
                               int lr, void* user_data)
 {
+  STS_MARK_FUNCTION;
   (void)t;
   (void)u;
   (void)f;
@@ -353,6 +355,7 @@ extern "C" int STS_PFMGPSolve(double t, N_Vector u, N_Vector f, N_Vector r, N_Ve
 // the SUNLinSol PSolve callback form (P_data = the STS_PFMG, set up for the system's gamma)
 extern "C" int STS_PFMGPrecSolve(void* P_data, N_Vector r, N_Vector z, double tol, int lr)
 {
+  STS_MARK_FUNCTION;
   STS_PFMG mg = (STS_PFMG)P_data;
   return mg ? STS_PFMGPSolve(0.0, nullptr, nullptr, r, z, mg->gamma, tol, lr, mg) : -1;
 }
@@ -377,6 +380,7 @@ int shift_atimes(void* d, N_Vector v, N_Vector z)
 extern "C" int STS_ImplicitSolvePFMG(STS_Problem p, double gamma, STS_PFMG mg, N_Vector b, N_Vector x, double tol,
                                      int maxit, int* iters, double* relres)
 {
+  STS_MARK_FUNCTION;
   if (!p || !mg || mg->p != p || !b || !x || maxit < 1) return -1;
   if (STS_PFMGPSetup(0.0, nullptr, nullptr, 0, nullptr, gamma, mg) != 0) return -1;
   void* LS = STS_SUNLinSol_PCG(b, STS_PREC_RIGHT, maxit, p->ctx);

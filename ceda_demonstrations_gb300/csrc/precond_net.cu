@@ -1951,6 +1951,7 @@ extern "C" int STS_NetSetTensorPath(STS_Net nt, int path)
 extern "C" int STS_NetApply(STS_Net nt, int n, const double* r, double* z, double sk, double sg, double jacobi,
                             double scale)
 {
+  STS_MARK_FUNCTION;
   if (!net_size_ok(nt, n) || !r || !z || !(scale > 0.0)) return -1;
   ctx_activate(nt->ctx);
   net::l0::FoldA fa;
@@ -2336,6 +2337,7 @@ __global__ void true_residual_kernel(ProbDev P, double gamma, const double* __re
 extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b, N_Vector x, double tol, int maxit,
                             int* iters, double* relres)
 {
+  STS_MARK_FUNCTION;
   const bool fallback = maxit > 0; // maxit < 0: at most -maxit iterations, no fallback
   if (maxit < 0) maxit = -maxit;
   if (!p || !nt || !b || !x || p->nx != p->ny || NVL(b) != p->nx * p->ny || NVL(x) != NVL(b) || maxit < 1 ||
@@ -2491,6 +2493,7 @@ extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b,
 extern "C" int STS_ImplicitSolveLearned(STS_Problem p, double gamma, STS_Net nt, N_Vector b, N_Vector x, double tol,
                                         int maxit, double kappa_min, int* iters, double* relres, int* used_net)
 {
+  STS_MARK_FUNCTION;
   if (!p || !b || !x)
   {
     sts_set_error("STS_ImplicitSolveLearned: invalid arguments");

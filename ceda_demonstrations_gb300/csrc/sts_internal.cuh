@@ -9,6 +9,20 @@
 #include "../../include/stsgpu.h"
 #include "xsum.cuh"
 
+#include <nvtx3/nvToolsExt.h>
+
+// NVTX range over one API call: the regions the reference marks for its profiler (the RHS,
+// the preconditioner, Evolve) plus the solvers. Without an attached tool a push / pop costs a
+// test of a null function pointer.
+struct StsRange {
+  explicit StsRange(const char* name) { nvtxRangePushA(name); }
+  ~StsRange() { nvtxRangePop(); }
+  StsRange(const StsRange&)            = delete;
+  StsRange& operator=(const StsRange&) = delete;
+};
+#define STS_MARK_FUNCTION StsRange sts_range_(__func__)
+#define STS_MARK_REGION(name) StsRange sts_range_(name)
+
 // ---------------------------------------------------------------------------------------
 // errors
 // ---------------------------------------------------------------------------------------

@@ -395,3 +395,19 @@ def test_oracle_nonfinite_state_fails_cleanly(oracle):
                 assert s["t"] == 0.0 and s["nst"] == 0
                 assert s["nst_attempts"] == 0 and s["netf"] == 0
                 assert s["stages_total"] == 0 and s["nfe"] == 2
+
+
+def test_oracle_under_address_and_ub_sanitizers():
+    """The oracle built with AddressSanitizer and UndefinedBehaviorSanitizer (float-to-int
+    overflow included, every report fatal) walks every entry point on tiny and ragged grids."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None or shutil.which("make") is None:
+        pytest.skip("no gcc / make")
+    d = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle")
+    r = subprocess.run(["make", "-s", "-C", d, "sanitize", "CC=gcc"], capture_output=True,
+                       text=True, timeout=600)
+    if r.returncode != 0 and "cannot find" in r.stderr and "asan" in r.stderr:
+        pytest.skip("no sanitizer runtime for this compiler")
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "sanitize_check: ok" in r.stdout
