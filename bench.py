@@ -235,6 +235,15 @@ def run_gpu(args):
     s1 = I.stats()
     e2e_ms = max_over_ranks(tm.ms)
     e2e_dof = N2 * (s1["nfe"] - s0["nfe"])
+    # the host link alone (copy engine, pinned buffers, same calls): the part of the e2e step
+    # that the data dependence between steps keeps from overlapping the device work
+    with timer() as th:
+        for _ in range(3):
+            L.N_VCopyFromHost_Sts(yv.h, hp[k])
+    with timer() as td:
+        for _ in range(3):
+            L.N_VCopyToHost_Sts(yv.h, hp[1 - k])
+    h2d_ms, d2h_ms = th.ms / 3, td.ms / 3
 
     # accuracy on the timed step sequence
     ex = G.exact(res[True]["t"]).numpy()
@@ -275,7 +284,9 @@ def run_gpu(args):
                    "nx": n, "ny": n, "method": "RKL2", "stages_per_step": m["s"],
                    "inputs_exceed_l2": True, "parallelism": "replicas" if ws > 1 else "single GPU"},
         "e2e": {"value": ws * e2e_dof / (e2e_ms / 1e3), "unit": "DOF-stages/s",
-                "h2d_bytes_per_step": 8 * N2, "d2h_bytes_per_step": 8 * N2},
+                "h2d_bytes_per_step": 8 * N2, "d2h_bytes_per_step": 8 * N2,
+                "ms_per_step": e2e_ms / args.steps, "h2d_ms": h2d_ms, "d2h_ms": d2h_ms,
+                "h2d_gbs": 8 * N2 / (h2d_ms / 1e3) / 1e9, "d2h_gbs": 8 * N2 / (d2h_ms / 1e3) / 1e9},
         "gpu_launches": m["launches"],
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": ach / peak, "traffic": traffic,

@@ -155,6 +155,16 @@ SIGNATURES = [
     ("STS_SUNLinSol_SPGMR", _vp, [_NV, C.c_int, C.c_int, _vp]),
     ("STS_SUNLinSol_SPGMRSetMaxRestarts", C.c_int, [_vp, C.c_int]),
     ("STS_SUNLinSol_SPGMRSetGSType", C.c_int, [_vp, C.c_int]),
+    ("STS_SUNLinSol_SPFGMR", _vp, [_NV, C.c_int, C.c_int, _vp]),
+    ("STS_SUNLinSol_SPFGMRSetMaxRestarts", C.c_int, [_vp, C.c_int]),
+    ("STS_SUNLinSol_SPFGMRSetGSType", C.c_int, [_vp, C.c_int]),
+    ("STS_ImplicitSolveLS", C.c_int, [_vp, C.c_double, _vp, C.c_int, _vp, _vp, _NV, _NV,
+                                      C.c_double, C.POINTER(C.c_int), _dp]),
+    ("STS_NetPrecCreate", C.c_int, [_vp, _vp, C.POINTER(_vp)]),
+    ("STS_NetPrecFree", C.c_int, [C.POINTER(_vp)]),
+    ("STS_NetPSetup", C.c_int, [C.c_double, _NV, _NV, C.c_int, C.POINTER(C.c_int), C.c_double, _vp]),
+    ("STS_NetPSolve", C.c_int, [C.c_double, _NV, _NV, _NV, _NV, C.c_double, C.c_double, C.c_int, _vp]),
+    ("STS_NetPrecSolve", C.c_int, [_vp, _NV, _NV, C.c_double, C.c_int]),
     ("STS_PFMGCreate", _vp, [_vp, C.c_int, C.c_int]),
     ("STS_PFMGFree", None, [C.POINTER(_vp)]),
     ("STS_PFMGPSetup", C.c_int, [C.c_double, _NV, _NV, C.c_int, C.POINTER(C.c_int), C.c_double, _vp]),
@@ -725,6 +735,67 @@ class SPGMRSolver(PCGSolver):
         if L.STS_SUNLinSol_SPGMRSetMaxRestarts(self.LS, max_restarts) != 0 or \
                 L.STS_SUNLinSol_SPGMRSetGSType(self.LS, gstype) != 0:
             _err("SPGMR options")
+
+
+class SPFGMRSolver(PCGSolver):
+    """SUNLinSol_SPFGMR (flexible restarted GMRES, right preconditioning): the solver for a
+    preconditioner that may differ between applications, such as :class:`NetPrec`."""
+
+    _create = "STS_SUNLinSol_SPFGMR"
+
+    def __init__(self, ctx, y, atimes=None, psolve=None, maxl=20, max_restarts=0, gstype=MODIFIED_GS,
+                 precond=None):
+        super().__init__(ctx, y, atimes, psolve, maxl, precond)
+        L = lib()
+        if L.STS_SUNLinSol_SPFGMRSetMaxRestarts(self.LS, max_restarts) != 0 or \
+                L.STS_SUNLinSol_SPFGMRSetGSType(self.LS, gstype) != 0:
+            _err("SPFGMR options")
+
+
+PREC_NONE, PREC_JACOBI, PREC_USER = 0, 1, 2
+
+
+def implicit_solve_ls(problem, gamma, solver, b, x, tol=1e-8, prec=PREC_JACOBI, pdata=None,
+                      psolve=None):
+    """(I - gamma A) x = b with a generic solver object (:class:`PCGSolver`,
+    :class:`SPGMRSolver`, :class:`SPFGMRSolver`); ``prec`` PREC_NONE, PREC_JACOBI or PREC_USER
+    with ``pdata`` (a handle) and ``psolve`` (a C function pointer, e.g. ``NetPrec.psolve_fn``).
+    Returns (status, iterations, residual estimate)."""
+    it, rel = C.c_int(), C.c_double()
+    rc = lib().STS_ImplicitSolveLS(problem.h, gamma, solver.LS, prec, pdata, psolve, b.h, x.h, tol,
+                                   C.byref(it), C.byref(rel))
+    if rc < 0:
+        _err("STS_ImplicitSolveLS")
+    return rc, it.value, rel.value
+
+
+class NetPrec:
+    """The learned network behind the PSetup / PSolve interface (STS_NetPrec) for the generic
+    solvers; call :meth:`setup` with gamma before solving."""
+
+    def __init__(self, net, problem):
+        self.net, self.problem = net, problem
+        self.h = _vp()
+        if lib().STS_NetPrecCreate(net.h, problem.h, C.byref(self.h)) != 0:
+            _err("STS_NetPrecCreate")
+        self.psolve_fn = C.cast(lib().STS_NetPrecSolve, _vp)
+
+    def setup(self, gamma):
+        cur = C.c_int()
+        if lib().STS_NetPSetup(0.0, None, None, 0, C.byref(cur), gamma, self.h) != 0:
+            _err("STS_NetPSetup")
+
+    def psolve(self, r, z, gamma):
+        if lib().STS_NetPSolve(0.0, None, None, r.h, z.h, gamma, 0.0, 2, self.h) != 0:
+            _err("STS_NetPSolve")
+
+    def __del__(self):
+        try:
+            if not _exiting and self.h:
+                lib().STS_NetPrecFree(C.byref(self.h))
+                self.h = None
+        except Exception:
+            pass
 
 
 def sdirk2_evolve_ls(problem, solver, y, t0, h, nsteps, tol=1e-10, precond=True):

@@ -302,9 +302,11 @@ extern "C" int STS_ImplicitSolvePCG(STS_Problem p, double gamma, N_Vector b, N_V
 
 // ---------------------------------------------------------------------------------------
 // Generic Krylov solvers through ATimes / PSolve callbacks: SUNLinSol_PCG and SUNLinSol_SPGMR
-// (diffusion_2D/main.cpp:209-218). One object type; the solve dispatches on the kind.
+// (diffusion_2D/main.cpp:209-218), and SUNLinSol_SPFGMR, the flexible GMRES SUNDIALS offers for
+// preconditioners that change from one application to the next. One object type; the solve
+// dispatches on the kind.
 // ---------------------------------------------------------------------------------------
-enum { LS_PCG = 0, LS_SPGMR = 1 };
+enum { LS_PCG = 0, LS_SPGMR = 1, LS_SPFGMR = 2 };
 
 struct LinSol {
   int kind          = LS_PCG;
@@ -316,8 +318,9 @@ struct LinSol {
   void* P_data      = nullptr;
   STS_PSolveFn psolve = nullptr;
   N_Vector r = nullptr, pv = nullptr, z = nullptr, Ap = nullptr;
-  // SPGMR: Krylov basis V[0..maxl], restarts, Gram-Schmidt variant, Hessenberg + Givens
-  std::vector<N_Vector> V;
+  // SPGMR: Krylov basis V[0..maxl], restarts, Gram-Schmidt variant, Hessenberg + Givens;
+  // SPFGMR also keeps the preconditioned basis Z[0..maxl-1]
+  std::vector<N_Vector> V, Z;
   int max_restarts  = 0;
   int gstype        = STS_MODIFIED_GS;
   int last_iters    = 0;
@@ -342,6 +345,8 @@ static LinSol* linsol_new(int kind, N_Vector y, int pretype, int maxl, STS_Conte
   if (kind == LS_PCG) L->pv = N_VClone_Sts(y);
   else
     for (int k = 0; k <= L->maxl; ++k) L->V.push_back(N_VClone_Sts(y));
+  if (kind == LS_SPFGMR)
+    for (int k = 0; k < L->maxl; ++k) L->Z.push_back(N_VClone_Sts(y));
   return L;
 }
 
@@ -360,10 +365,21 @@ extern "C" void* STS_SUNLinSol_SPGMR(N_Vector y, int pretype, int maxl, STS_Cont
   return linsol_new(LS_SPGMR, y, pretype, maxl, ctx);
 }
 
+// SUNLinSol_SPFGMR: right preconditioning only (a left type is taken as right, as SUNDIALS does)
+extern "C" void* STS_SUNLinSol_SPFGMR(N_Vector y, int pretype, int maxl, STS_Context ctx)
+{
+  if (maxl > 1000)
+  {
+    sts_set_error("SUNLinSol_SPFGMR: maxl %d > 1000", maxl);
+    return nullptr;
+  }
+  return linsol_new(LS_SPFGMR, y, pretype == STS_PREC_NONE ? STS_PREC_NONE : STS_PREC_RIGHT, maxl, ctx);
+}
+
 extern "C" int STS_SUNLinSol_SPGMRSetMaxRestarts(void* LS, int maxrs)
 {
   LinSol* L = (LinSol*)LS;
-  if (!L || L->kind != LS_SPGMR || maxrs < 0) return -1;
+  if (!L || L->kind == LS_PCG || maxrs < 0) return -1;
   L->max_restarts = maxrs;
   return 0;
 }
@@ -371,9 +387,21 @@ extern "C" int STS_SUNLinSol_SPGMRSetMaxRestarts(void* LS, int maxrs)
 extern "C" int STS_SUNLinSol_SPGMRSetGSType(void* LS, int gstype)
 {
   LinSol* L = (LinSol*)LS;
-  if (!L || L->kind != LS_SPGMR || (gstype != STS_MODIFIED_GS && gstype != STS_CLASSICAL_GS)) return -1;
+  if (!L || L->kind == LS_PCG || (gstype != STS_MODIFIED_GS && gstype != STS_CLASSICAL_GS)) return -1;
   L->gstype = gstype;
   return 0;
+}
+
+extern "C" int STS_SUNLinSol_SPFGMRSetMaxRestarts(void* LS, int maxrs)
+{
+  LinSol* L = (LinSol*)LS;
+  return (L && L->kind == LS_SPFGMR) ? STS_SUNLinSol_SPGMRSetMaxRestarts(LS, maxrs) : -1;
+}
+
+extern "C" int STS_SUNLinSol_SPFGMRSetGSType(void* LS, int gstype)
+{
+  LinSol* L = (LinSol*)LS;
+  return (L && L->kind == LS_SPFGMR) ? STS_SUNLinSol_SPGMRSetGSType(LS, gstype) : -1;
 }
 
 extern "C" int STS_SUNLinSolSetATimes(void* LS, void* A_data, STS_ATimesFn atimes)
@@ -460,9 +488,12 @@ static void givens(double a, double b, double* c, double* s)
 // N_VLinearCombination); the Hessenberg matrix is reduced by Givens rotations on the host, so
 // the residual estimate |g_{j+1}| is known after every iteration. Stop when it is at most
 // delta ||b||_2; after max_restarts restarts without convergence return 1 (recoverable).
+// Flexible variant (SPFGMR, Saad 1993): the preconditioned vectors z_j = P_j^-1 v_j are kept,
+// w = A z_j, and the cycle ends with x += Z y, so P may differ between applications.
 static int spgmr_solve(LinSol* L, N_Vector x, N_Vector b, double delta)
 {
   const bool prec = L->pretype != STS_PREC_NONE && L->psolve;
+  const bool flex = L->kind == LS_SPFGMR && prec;
   const int m     = L->maxl;
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m), h(m + 1), h2(m + 1);
   std::vector<double> cf(m + 2);
@@ -485,8 +516,9 @@ static int spgmr_solve(LinSol* L, N_Vector x, N_Vector b, double delta)
       N_Vector w = L->V[j + 1];
       if (prec)
       {
-        if (L->psolve(L->P_data, L->V[j], L->z, delta, L->pretype)) return 1;
-        if (L->atimes(L->A_data, L->z, w)) return 1;
+        N_Vector zj = flex ? L->Z[j] : L->z;
+        if (L->psolve(L->P_data, L->V[j], zj, delta, L->pretype)) return 1;
+        if (L->atimes(L->A_data, zj, w)) return 1;
       }
       else if (L->atimes(L->A_data, L->V[j], w)) return 1;
       if (L->gstype == STS_MODIFIED_GS)
@@ -538,20 +570,28 @@ static int spgmr_solve(LinSol* L, N_Vector x, N_Vector b, double delta)
         break;
       }
     }
-    // y = H^-1 g (upper triangular, k columns); u = V y; x += P^-1 u
+    // y = H^-1 g (upper triangular, k columns); u = V y; x += P^-1 u (flexible: x += Z y)
     for (int i = k - 1; i >= 0; --i)
     {
       double sacc = g[i];
       for (int q = i + 1; q < k; ++q) sacc = sacc - Hij(i, q) * y[q];
       y[i] = sacc / Hij(i, i);
     }
-    N_VLinearCombination_Sts(k, y.data(), L->V.data(), L->Ap);
-    if (prec)
+    if (flex)
     {
-      if (L->psolve(L->P_data, L->Ap, L->z, delta, L->pretype)) return 1;
-      N_VLinearSum_Sts(1.0, x, 1.0, L->z, x);
+      N_VLinearCombination_Sts(k, y.data(), L->Z.data(), L->Ap);
+      N_VLinearSum_Sts(1.0, x, 1.0, L->Ap, x);
     }
-    else N_VLinearSum_Sts(1.0, x, 1.0, L->Ap, x);
+    else
+    {
+      N_VLinearCombination_Sts(k, y.data(), L->V.data(), L->Ap);
+      if (prec)
+      {
+        if (L->psolve(L->P_data, L->Ap, L->z, delta, L->pretype)) return 1;
+        N_VLinearSum_Sts(1.0, x, 1.0, L->z, x);
+      }
+      else N_VLinearSum_Sts(1.0, x, 1.0, L->Ap, x);
+    }
     if (converged) return 0;
     if (cycle == L->max_restarts) break;
     // restart from the true residual r = b - A x
@@ -586,6 +626,7 @@ extern "C" int STS_SUNLinSolFree(void* LS)
   N_VDestroy_Sts(L->Ap);
   if (L->pv) N_VDestroy_Sts(L->pv);
   for (N_Vector v : L->V) N_VDestroy_Sts(v);
+  for (N_Vector v : L->Z) N_VDestroy_Sts(v);
   delete L;
   return 0;
 }
@@ -681,6 +722,37 @@ extern "C" int STS_SDIRK2EvolveLS(STS_Problem p, void* LS, int precond, N_Vector
     *it          = STS_SUNLinSolNumIters(L);
     return sr < 0 ? -1 : 0;
   });
+  STS_SUNLinSolSetATimes(L, nullptr, nullptr);
+  STS_SUNLinSolSetPreconditioner(L, nullptr, nullptr);
+  N_VDestroy_Sts(op.tmp);
+  return rc;
+}
+
+// One shifted system (I - gamma A) x = b through a generic solver object (PCG, SPGMR or
+// SPFGMR): ATimes is the shifted operator, the preconditioner none (prec 0), the Jacobi PSolve
+// (1) or the caller's (2: P_data and psolve, e.g. STS_PFMGPrecSolve or STS_NetPrecSolve after
+// their PSetup). The solver keeps no reference to the callbacks after the call.
+extern "C" int STS_ImplicitSolveLS(STS_Problem p, double gamma, void* LS, int prec, void* P_data,
+                                   STS_PSolveFn psolve, N_Vector b, N_Vector x, double tol, int* iters,
+                                   double* relres)
+{
+  STS_MARK_FUNCTION;
+  LinSol* L = (LinSol*)LS;
+  if (!p || !L || !b || !x || prec < 0 || prec > 2 || (prec == 2 && !psolve) ||
+      (prec != 0 && L->pretype == STS_PREC_NONE))
+  {
+    sts_set_error("ImplicitSolveLS: invalid arguments (a preconditioner needs a solver made with a "
+                  "preconditioning type)");
+    return -1;
+  }
+  ShiftedOp op{p, gamma, N_VClone_Sts(b)};
+  STS_SUNLinSolSetATimes(L, &op, shifted_atimes);
+  if (prec == 1) STS_SUNLinSolSetPreconditioner(L, &op, jacobi_psolve);
+  else if (prec == 2) STS_SUNLinSolSetPreconditioner(L, P_data, psolve);
+  else STS_SUNLinSolSetPreconditioner(L, nullptr, nullptr);
+  const int rc = STS_SUNLinSolSolve(L, x, b, tol);
+  if (iters) *iters = STS_SUNLinSolNumIters(L);
+  if (relres) *relres = STS_SUNLinSolResNorm(L);
   STS_SUNLinSolSetATimes(L, nullptr, nullptr);
   STS_SUNLinSolSetPreconditioner(L, nullptr, nullptr);
   N_VDestroy_Sts(op.tmp);

@@ -2510,3 +2510,104 @@ extern "C" int STS_ImplicitSolveLearned(STS_Problem p, double gamma, STS_Net nt,
   }
   return STS_ImplicitSolvePCG(p, gamma, b, x, tol, maxit, 1, iters, relres);
 }
+
+// ---------------------------------------------------------------------------------------
+// The network as a preconditioner object behind the reference's PSetup / PSolve interface
+// (diffusion_2D/preconditioner_jacobi.cpp:9-61 signatures), for the generic Krylov solvers:
+// PSetup takes gamma and folds the system features into the level-0 weights, PSolve applies
+// z = M r with the input scaled by 1/rms(r) (the network is linear in r, the scale only keeps
+// the BF16 / FP32 activations in range). Flexible GMRES (SUNLinSol_SPFGMR) is the safe outer
+// method: the BF16 network is linear in exact arithmetic but its rounding is not.
+// ---------------------------------------------------------------------------------------
+struct STS_NetPrec_ {
+  STS_Net net       = nullptr;
+  STS_Problem p     = nullptr;
+  double gamma      = -1.0;
+  double sk = 0.0, sg = 0.0, jac = 1.0;
+  net::l0::FoldA fa;
+  net::l0::FoldB fb;
+  bool ready        = false;
+};
+
+extern "C" int STS_NetPrecCreate(STS_Net nt, STS_Problem p, STS_NetPrec* out)
+{
+  if (!out) return -1;
+  *out = nullptr;
+  if (!nt || !p || p->nx != p->ny || p->kind == STS_PROBLEM_PERIODIC || nt->ctx != p->ctx)
+  {
+    sts_set_error("STS_NetPrecCreate: square Dirichlet grid on the network's context required");
+    return -1;
+  }
+  if (!net_size_ok(nt, (int)p->nx)) return -1;
+  STS_NetPrec P = new STS_NetPrec_();
+  P->net        = nt;
+  P->p          = p;
+  *out          = P;
+  return 0;
+}
+
+extern "C" int STS_NetPrecFree(STS_NetPrec* P)
+{
+  if (!P || !*P) return 0;
+  delete *P;
+  *P = nullptr;
+  return 0;
+}
+
+extern "C" int STS_NetPSetup(double t, N_Vector u, N_Vector f, int jok, int* jcurPtr, double gamma, void* user_data)
+{
+  STS_MARK_FUNCTION;
+  (void)t;
+  (void)u;
+  (void)f;
+  (void)jok;
+  STS_NetPrec P = (STS_NetPrec)user_data;
+  if (!P || !(gamma > 0.0)) return -1;
+  STS_Problem p = P->p;
+  ctx_activate(p->ctx);
+  P->gamma = gamma;
+  P->jac   = 1.0 / (1.0 - gamma * p->cc);
+  P->sk    = (std::log10(p->ky / p->kx) + 1.5) / 1.5;
+  P->sg    = std::log10(gamma / (p->dx * p->dx)) - 3.6;
+  P->ready = l0_prepare(P->net, (float)P->sk, (float)P->sg, &P->fa, &P->fb);
+  if (jcurPtr) *jcurPtr = 1;
+  return P->ready ? 0 : -1;
+}
+
+extern "C" int STS_NetPrecSolve(void* P_data, N_Vector r, N_Vector z, double tol, int lr)
+{
+  STS_MARK_FUNCTION;
+  (void)tol;
+  (void)lr;
+  STS_NetPrec P = (STS_NetPrec)P_data;
+  if (!P || !P->ready || !r || !z || NVL(r) != P->p->nx * P->p->ny || NVL(z) != NVL(r))
+  {
+    sts_set_error("STS_NetPrecSolve: call STS_NetPSetup first; vectors of the problem's size");
+    return -1;
+  }
+  STS_Context ctx = P->p->ctx;
+  const long long N = NVL(r);
+  const double rn   = sqrt(sts_dot_exact(ctx, NVD(r), NVD(r), N, SLOT_PCG3));
+  if (!(rn > 0.0) || !(rn < INFINITY))
+  {
+    if (!(rn == 0.0)) return -1; // non-finite input
+    return STS_CUDA_OK(cudaMemsetAsync(NVD(z), 0, N * sizeof(double), ctx->stream)) ? 0 : -1;
+  }
+  const double scale = std::sqrt((double)N) / rn;
+  net_forward_infer(P->net, (int)P->p->nx, NVD(r), scale, (float)P->sk, (float)P->sg, P->jac / scale, NVD(z), &P->fa,
+                    &P->fb);
+  return STS_CUDA_OK(cudaGetLastError()) ? 0 : -1;
+}
+
+extern "C" int STS_NetPSolve(double t, N_Vector u, N_Vector f, N_Vector r, N_Vector z, double gamma, double delta,
+                             int lr, void* user_data)
+{
+  (void)t;
+  (void)u;
+  (void)f;
+  STS_NetPrec P = (STS_NetPrec)user_data;
+  if (!P) return -1;
+  if (!P->ready || P->gamma != gamma)
+    if (STS_NetPSetup(0.0, nullptr, nullptr, 0, nullptr, gamma, P) != 0) return -1;
+  return STS_NetPrecSolve(P, r, z, delta, lr);
+}

@@ -299,6 +299,13 @@ void* STS_SUNLinSol_PCG(N_Vector y, int pretype, int maxl, STS_Context ctx); /* 
 void* STS_SUNLinSol_SPGMR(N_Vector y, int pretype, int maxl, STS_Context ctx);
 int STS_SUNLinSol_SPGMRSetMaxRestarts(void* LS, int maxrs);
 int STS_SUNLinSol_SPGMRSetGSType(void* LS, int gstype);
+/* SUNLinSol_SPFGMR (SUNDIALS' flexible GMRES, the Krylov method for a preconditioner that may
+ * change between applications, e.g. the learned network below): restarted FGMRES(maxl), right
+ * preconditioning only (any other nonzero pretype is taken as right), maxl <= 1000; it keeps
+ * the preconditioned basis and updates x += Z y. SetMaxRestarts / SetGSType as for SPGMR. */
+void* STS_SUNLinSol_SPFGMR(N_Vector y, int pretype, int maxl, STS_Context ctx);
+int STS_SUNLinSol_SPFGMRSetMaxRestarts(void* LS, int maxrs);
+int STS_SUNLinSol_SPFGMRSetGSType(void* LS, int gstype);
 int STS_SUNLinSolSetATimes(void* LS, void* A_data, STS_ATimesFn atimes);
 int STS_SUNLinSolSetPreconditioner(void* LS, void* P_data, STS_PSolveFn psolve);
 /* solve A x = b from x0 = 0 through the callbacks; stop when ||r||_2 <= delta ||b||_2 (PCG:
@@ -323,6 +330,14 @@ int STS_SDIRK2Evolve(STS_Problem p, N_Vector y, double t0, double h, int nsteps,
  * callbacks are replaced. Returns 0, or -1 on illegal input or a failed solve (rc < 0). */
 int STS_SDIRK2EvolveLS(STS_Problem p, void* LS, int precond, N_Vector y, double t0, double h,
                        int nsteps, double tol, long long* total_iters);
+/* One shifted system (I - gamma A) x = b with a generic solver object (PCG, SPGMR or SPFGMR):
+ * the driver sets ATimes to the shifted operator and the preconditioner to none (prec 0), the
+ * Jacobi STS_PSolve (1) or the caller's (2: P_data + psolve, e.g. STS_PFMGPrecSolve or
+ * STS_NetPrecSolve after their PSetup); a preconditioner needs a solver made with
+ * STS_PREC_RIGHT. Returns the solver's code (0 converged, 1 not converged) or -1. */
+int STS_ImplicitSolveLS(STS_Problem p, double gamma, void* LS, int prec, void* P_data,
+                        STS_PSolveFn psolve, N_Vector b, N_Vector x, double tol, int* iters,
+                        double* relres);
 /* SDIRK2 with each stage solved by STS_ImplicitSolveLearned (declared below); STS_Net is the
  * learned preconditioner's handle */
 typedef struct STS_Net_* STS_Net;
@@ -447,6 +462,20 @@ int STS_FCGSolve(STS_Problem p, double gamma, STS_Net net, N_Vector b, N_Vector 
 int STS_ImplicitSolveLearned(STS_Problem p, double gamma, STS_Net net, N_Vector b, N_Vector x,
                              double tol, int maxit, double kappa_min, int* iters, double* relres,
                              int* used_net);
+/* The network as a preconditioner object with the reference's PSetup / PSolve signatures
+ * (diffusion_2D/preconditioner_jacobi.cpp:9-10,49-50) for the generic solvers: PSetup takes
+ * gamma and folds the system features (ky/kx, gamma/dx^2) into the level-0 weights; PSolve
+ * applies z = M r (input scaled by 1/rms(r)); STS_NetPrecSolve is the SUNLinSol PSolve form.
+ * Square Dirichlet grids with n a multiple of 16, on the network's context. Use with
+ * STS_SUNLinSol_SPFGMR (the BF16 network is linear only up to rounding). */
+typedef struct STS_NetPrec_* STS_NetPrec;
+int STS_NetPrecCreate(STS_Net net, STS_Problem p, STS_NetPrec* P);
+int STS_NetPrecFree(STS_NetPrec* P);
+int STS_NetPSetup(double t, N_Vector u, N_Vector f, int jok, int* jcurPtr, double gamma,
+                  void* user_data);
+int STS_NetPSolve(double t, N_Vector u, N_Vector f, N_Vector r, N_Vector z, double gamma,
+                  double delta, int lr, void* user_data);
+int STS_NetPrecSolve(void* P_data, N_Vector r, N_Vector z, double tol, int lr);
 
 #ifdef __cplusplus
 }

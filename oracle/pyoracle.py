@@ -120,6 +120,8 @@ def lib():
         L.orc_spgmr.restype = C.c_int
         L.orc_spgmr.argtypes = [C.POINTER(Prob), C.c_double, C.c_int, _dp, _dp, C.c_double, C.c_int,
                                 C.c_int, C.c_int, C.POINTER(C.c_int), _dp]
+        L.orc_spfgmr.restype = C.c_int
+        L.orc_spfgmr.argtypes = L.orc_spgmr.argtypes
         L.orc_sdirk2_ls.restype = C.c_int
         L.orc_sdirk2_ls.argtypes = [C.POINTER(Prob), C.c_double, C.c_double, C.c_int, C.c_double,
                                     C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp,
@@ -267,13 +269,16 @@ class Problem:
                                    C.byref(it), C.byref(rel))
         return x, rc, it.value, rel.value
 
-    def spgmr(self, gamma, b, tol=1e-8, maxl=20, max_restarts=0, gstype=1, jacobi=True):
-        """SUNLinSol_SPGMR: (x, status, iterations, relative residual estimate)."""
+    def spgmr(self, gamma, b, tol=1e-8, maxl=20, max_restarts=0, gstype=1, jacobi=True,
+              flexible=False):
+        """SUNLinSol_SPGMR (flexible: SUNLinSol_SPFGMR): (x, status, iterations, relative
+        residual estimate)."""
         b = np.ascontiguousarray(b, dtype=np.float64)
         x = self.field()
         it, rel = C.c_int(), C.c_double()
-        rc = lib().orc_spgmr(self.p, gamma, int(jacobi), dptr(b), dptr(x), tol, maxl, max_restarts,
-                             gstype, C.byref(it), C.byref(rel))
+        fn = lib().orc_spfgmr if flexible else lib().orc_spgmr
+        rc = fn(self.p, gamma, int(jacobi), dptr(b), dptr(x), tol, maxl, max_restarts, gstype,
+                C.byref(it), C.byref(rel))
         return x, rc, it.value, rel.value
 
     def pfmg_vcycle(self, gamma, r, relax=2, nrelax=2):

@@ -135,7 +135,11 @@ int main(void)
       int it = 0, nl = 0;
       (void)orc_pcg(p, gamma, 1, b, x, 1e-10, 1000, &rel);
       (void)orc_pcg_generic(p, gamma, 1, b, x, 1e-10, 1000, &it, &rel);
-      for (int gs = 0; gs < 2; ++gs) (void)orc_spgmr(p, gamma, 1, b, x, 1e-10, 5, 20, gs, &it, &rel);
+      for (int gs = 0; gs < 2; ++gs)
+      {
+        (void)orc_spgmr(p, gamma, 1, b, x, 1e-10, 5, 20, gs, &it, &rel);
+        (void)orc_spfgmr(p, gamma, 1, b, x, 1e-10, 5, 20, gs, &it, &rel);
+      }
       for (int relax = 1; relax <= 2; ++relax)
       {
         (void)orc_pfmg_vcycle(p, gamma, relax, 2, b, z, &nl);

@@ -1505,14 +1505,18 @@ static void orc_givens(double a, double b, double* c, double* s)
  * x0 = 0, Arnoldi by modified Gram-Schmidt (gstype 1) or classical Gram-Schmidt with one
  * re-orthogonalisation pass (gstype 2), Givens rotations; stop when the residual estimate
  * |g_{j+1}| <= tol ||b||; restart from the true residual. Returns 0 / 1 as orc_pcg_generic. */
-int orc_spgmr(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol, int maxl,
-              int max_restarts, int gstype, int* iters, double* relres)
+static int spgmr_impl(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol, int maxl,
+                      int max_restarts, int gstype, int flexible, int* iters, double* relres)
 {
   long n  = (long)p->nx * p->ny;
   int m   = maxl;
   gen_op o = {p, gamma, 1.0 / (1.0 - gamma * p->cc), jacobi, (double*)malloc(n * sizeof(double)), NULL};
   double** V = (double**)malloc((m + 1) * sizeof(double*));
   for (int k = 0; k <= m; ++k) V[k] = (double*)malloc(n * sizeof(double));
+  /* flexible GMRES keeps the preconditioned basis Z (Saad 1993) */
+  const int flex = flexible && jacobi;
+  double** Z     = (double**)malloc((m > 0 ? m : 1) * sizeof(double*));
+  for (int k = 0; k < m; ++k) Z[k] = flex ? (double*)malloc(n * sizeof(double)) : NULL;
   double* r  = (double*)malloc(n * sizeof(double));
   double* z  = (double*)malloc(n * sizeof(double));
   double* u  = (double*)malloc(n * sizeof(double));
@@ -1550,8 +1554,9 @@ int orc_spgmr(const orc_prob* p, double gamma, int jacobi, const double* b, doub
       double* w = V[j + 1];
       if (jacobi)
       {
-        gen_psolve(&o, V[j], z, 0);
-        gen_atimes(&o, z, w);
+        double* zj = flex ? Z[j] : z;
+        gen_psolve(&o, V[j], zj, 0);
+        gen_atimes(&o, zj, w);
       }
       else gen_atimes(&o, V[j], w);
       if (gstype == 1)
@@ -1606,14 +1611,23 @@ int orc_spgmr(const orc_prob* p, double gamma, int jacobi, const double* b, doub
       for (int q = i + 1; q < kc; ++q) sacc = sacc - HH(i, q) * y[q];
       y[i] = sacc / HH(i, i);
     }
-    for (int i = 0; i < kc; ++i) X[i] = V[i];
-    v_lincomb(n, kc, y, X, u);
-    if (jacobi)
+    if (flex)
     {
-      gen_psolve(&o, u, z, 0);
-      v_linsum(n, 1.0, x, 1.0, z, x);
+      for (int i = 0; i < kc; ++i) X[i] = Z[i];
+      v_lincomb(n, kc, y, X, u);
+      v_linsum(n, 1.0, x, 1.0, u, x);
     }
-    else v_linsum(n, 1.0, x, 1.0, u, x);
+    else
+    {
+      for (int i = 0; i < kc; ++i) X[i] = V[i];
+      v_lincomb(n, kc, y, X, u);
+      if (jacobi)
+      {
+        gen_psolve(&o, u, z, 0);
+        v_linsum(n, 1.0, x, 1.0, z, x);
+      }
+      else v_linsum(n, 1.0, x, 1.0, u, x);
+    }
     if (converged)
     {
       ret = 0;
@@ -1635,6 +1649,8 @@ out:
   free(o.tmp);
   for (int k = 0; k <= m; ++k) free(V[k]);
   free(V);
+  for (int k = 0; k < m; ++k) free(Z[k]);
+  free(Z);
   free(r);
   free(z);
   free(u);
@@ -1648,6 +1664,20 @@ out:
   free(cf);
   free(X);
   return ret;
+}
+
+int orc_spgmr(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol, int maxl,
+              int max_restarts, int gstype, int* iters, double* relres)
+{
+  return spgmr_impl(p, gamma, jacobi, b, x, tol, maxl, max_restarts, gstype, 0, iters, relres);
+}
+
+/* SUNLinSol_SPFGMR restated: the preconditioned vectors z_j = P^-1 v_j are kept and the cycle
+ * ends with x += Z y; without a preconditioner it is GMRES itself. */
+int orc_spfgmr(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol, int maxl,
+               int max_restarts, int gstype, int* iters, double* relres)
+{
+  return spgmr_impl(p, gamma, jacobi, b, x, tol, maxl, max_restarts, gstype, 1, iters, relres);
 }
 
 /* ------------------------------------------------------------------------------------

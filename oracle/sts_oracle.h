@@ -101,6 +101,8 @@ int orc_pcg_generic(const orc_prob* p, double gamma, int jacobi, const double* b
                     int maxl, int* iters, double* relres);
 int orc_spgmr(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol, int maxl,
               int max_restarts, int gstype, int* iters, double* relres);
+int orc_spfgmr(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol, int maxl,
+               int max_restarts, int gstype, int* iters, double* relres);
 int orc_sdirk2_ls(const orc_prob* p, double t0, double h, int nsteps, double tol, int ls, int maxl,
                   int max_restarts, int gstype, int jacobi, double* y, long* total_iters);
 /* PFMG-role V-cycle (relax 1 weighted Jacobi, 2 symmetric red/black Gauss-Seidel) and CG with it */

@@ -177,9 +177,10 @@ def test_harvest_pairs_satisfy_the_system(ctx):
         assert np.abs(res - r[1:-1, 1:-1]).max() < 1e-5 * scale
 
 
-def test_trained_network_cuts_fcg_iterations(ctx):
-    """Train on pairs harvested from Jacobi-PCG solves of three systems, then solve a fourth
-    (unseen right-hand side) with FCG + network and with Jacobi-PCG to the same 1e-8 residual."""
+@pytest.fixture(scope="module")
+def trained(ctx):
+    """A network trained on pairs harvested from Jacobi-PCG solves of three 256^2 systems:
+    (net, loss before, loss after)."""
     n, crop = 256, 64
     rs, es, ms = [], [], []
     for k, (ky, grel) in enumerate([(1.0, 2000.0), (0.1, 800.0), (0.01, 3000.0)]):
@@ -197,6 +198,14 @@ def test_trained_network_cuts_fcg_iterations(ctx):
                       epochs=1, batch=16, lr=0.0, seed=1)
     loss = net.train(crop, npairs, r_all.data_ptr(), e_all.data_ptr(), m_all.data_ptr(),
                      epochs=30, batch=16, lr=2e-3, seed=2)
+    return net, loss0, loss
+
+
+def test_trained_network_cuts_fcg_iterations(ctx, trained):
+    """Train on pairs harvested from Jacobi-PCG solves of three systems, then solve a fourth
+    (unseen right-hand side) with FCG + network and with Jacobi-PCG to the same 1e-8 residual."""
+    net, loss0, loss = trained
+    n = 256
     assert loss < loss0  # the training loop lowers the energy-norm loss
 
     ky, grel = 0.3, 1500.0
@@ -213,6 +222,45 @@ def test_trained_network_cuts_fcg_iterations(ctx):
     assert rel_fcg <= 2e-8  # true FP64 residual of the returned iterate
     assert _rel(x_fcg.numpy(), x_pcg.numpy()) < 1e-6
     assert it_fcg < 0.5 * it_pcg, (it_fcg, it_pcg)
+
+
+def test_network_as_psolve_in_flexible_gmres(ctx, trained):
+    """The trained network behind the PSetup / PSolve interface (STS_NetPrec) inside
+    SUNLinSol_SPFGMR, against the same solver with the Jacobi PSolve: both reach the 1e-8
+    residual on an unseen system (checked on the true FP64 residual), the network in far
+    fewer iterations."""
+    net = trained[0]
+    n, ky, grel = 256, 0.3, 1500.0
+    p = sts.Problem(ctx, sts.UNFORCED, n, n, 1.0, ky)
+    dx = 1.0 / (n + 1)
+    gamma = grel * dx * dx
+    bh = np.ascontiguousarray(_smooth_field(n, np.random.default_rng(4242)), dtype=np.float64).ravel()
+    b = sts.NVector.from_numpy(ctx, bh)
+    P = sts.NetPrec(net, p)
+    P.setup(gamma)
+    its = {}
+    for name in ("net", "jacobi"):
+        S = sts.SPFGMRSolver(ctx, b, maxl=40, max_restarts=300, gstype=sts.CLASSICAL_GS,
+                             precond=True)
+        x = p.vector()
+        if name == "net":
+            rc, it, res = sts.implicit_solve_ls(p, gamma, S, b, x, tol=1e-8, prec=sts.PREC_USER,
+                                                pdata=P.h, psolve=P.psolve_fn)
+        else:
+            rc, it, res = sts.implicit_solve_ls(p, gamma, S, b, x, tol=1e-8, prec=sts.PREC_JACOBI)
+        assert rc == 0 and res <= 1e-8, (name, rc, res)
+        ax = p.vector()
+        p.jac_times(x, ax)
+        true = np.linalg.norm(bh - (x.numpy() - gamma * ax.numpy())) / np.linalg.norm(bh)
+        assert true <= 2e-8, (name, true)
+        its[name] = it
+    assert its["net"] < 0.5 * its["jacobi"], its
+    # the ARKLsPrecSolveFn form applies the same operator
+    r = sts.NVector.from_numpy(ctx, bh)
+    z1, z2 = p.vector(), p.vector()
+    P.psolve(r, z1, gamma)
+    P.psolve(r, z2, gamma)
+    assert np.array_equal(z1.numpy(), z2.numpy()) and np.all(np.isfinite(z1.numpy()))
 
 
 def test_sdirk2_with_learned_solves_matches_jacobi(ctx):

@@ -1,5 +1,6 @@
 """Generic Krylov solvers of the SUNLinearSolver interface on the GPU (diffusion_2D/main.cpp:
-209-218: SUNLinSol_PCG and SUNLinSol_SPGMR with the Jacobi PSolve of preconditioner_jacobi.cpp)
+209-218: SUNLinSol_PCG and SUNLinSol_SPGMR with the Jacobi PSolve of preconditioner_jacobi.cpp;
+SUNLinSol_SPFGMR, SUNDIALS' flexible GMRES)
 against the oracle's restatement of the same operation sequence, bit for bit: ATimes
 v - gamma A v through J*v and N_VLinearSum, exact dot products (N_VDotProd, N_VDotProdMulti),
 N_VLinearCombination; SDIRK2 with a generic solver object attached by the driver; the
@@ -67,6 +68,60 @@ def test_spgmr_bitwise(ctx, stslib, oracle, gstype, jacobi, maxl, restarts):
     assert np.array_equal(X.numpy(), x_o)
     true = np.linalg.norm(b - (x_o - gamma * O.apply_A(x_o))) / np.linalg.norm(b)
     assert true < 1e-8
+
+
+@pytest.mark.parametrize("gstype", [1, 2], ids=["mgs", "cgs2"])
+@pytest.mark.parametrize("jacobi", [True, False], ids=["jacobi", "noprec"])
+@pytest.mark.parametrize("maxl,restarts", [(40, 0), (8, 50)], ids=["fgmres40", "fgmres8_restarted"])
+def test_spfgmr_bitwise(ctx, stslib, oracle, gstype, jacobi, maxl, restarts):
+    """SUNLinSol_SPFGMR through the native driver (shifted ATimes, the Jacobi PSolve) against
+    the oracle's flexible GMRES, bit for bit."""
+    nx, ny, gamma = 48, 40, 2e-4
+    pk = dict(kind=0, nx=nx, ny=ny, kx=1.0, ky=0.1)
+    G, O = stslib.Problem(ctx, **pk), oracle.Problem(**pk)
+    b = smooth_rhs(nx, ny, 3)
+    B = stslib.NVector.from_numpy(ctx, b)
+    S = stslib.SPFGMRSolver(ctx, B, maxl=maxl, max_restarts=restarts, gstype=gstype, precond=jacobi)
+    X = G.vector()
+    rc, it, res = stslib.implicit_solve_ls(G, gamma, S, B, X, tol=1e-9,
+                                           prec=stslib.PREC_JACOBI if jacobi else stslib.PREC_NONE)
+    x_o, rc_o, it_o, res_o = O.spgmr(gamma, b, tol=1e-9, maxl=maxl, max_restarts=restarts,
+                                     gstype=gstype, jacobi=jacobi, flexible=True)
+    assert rc == rc_o == 0 and it == it_o and res == res_o <= 1e-9
+    assert np.array_equal(X.numpy(), x_o)
+    true = np.linalg.norm(b - (x_o - gamma * O.apply_A(x_o))) / np.linalg.norm(b)
+    assert true < 1e-8
+    if not jacobi:
+        # without a preconditioner the flexible method is GMRES itself
+        x_g = O.spgmr(gamma, b, tol=1e-9, maxl=maxl, max_restarts=restarts, gstype=gstype,
+                      jacobi=False)[0]
+        assert np.array_equal(x_g, x_o)
+
+
+def test_generic_driver_with_pfmg_and_rejects(ctx, stslib):
+    """The generic driver with a caller's native PSolve (the PFMG-role cycle) in CG, GMRES and
+    flexible GMRES; a preconditioner on a solver made without one is refused."""
+    import ctypes as C
+    n, gamma = 96, 1e-3
+    G = stslib.Problem(ctx, stslib.UNFORCED, n, n, 1.0, 0.05)
+    b = smooth_rhs(n, n, 12)
+    B = stslib.NVector.from_numpy(ctx, b)
+    mg = stslib.PFMG(G)
+    mg.setup(gamma)
+    fn = C.cast(stslib.lib().STS_PFMGPrecSolve, C.c_void_p)
+    its = {}
+    for name, S in (("pcg", stslib.PCGSolver(ctx, B, maxl=500, precond=True)),
+                    ("gmres", stslib.SPGMRSolver(ctx, B, maxl=30, max_restarts=10, precond=True)),
+                    ("fgmres", stslib.SPFGMRSolver(ctx, B, maxl=30, max_restarts=10, precond=True))):
+        X = G.vector()
+        rc, it, res = stslib.implicit_solve_ls(G, gamma, S, B, X, tol=1e-9, prec=stslib.PREC_USER,
+                                               pdata=mg.h, psolve=fn)
+        assert rc == 0 and res <= 1e-9, (name, rc, res)
+        its[name] = it
+    assert max(its.values()) < 40, its
+    S = stslib.SPFGMRSolver(ctx, B, maxl=10, precond=False)
+    with pytest.raises(stslib.STSError):
+        stslib.implicit_solve_ls(G, gamma, S, B, G.vector(), prec=stslib.PREC_JACOBI)
 
 
 def test_spgmr_not_converged_is_recoverable(ctx, stslib, oracle):
