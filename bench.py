@@ -517,8 +517,11 @@ def run_precond(args):
         ky, gh = system(erng)
         P = sts.Problem(ctx, sts.UNFORCED, n, n, 1.0, ky)
         b = sts.NVector.from_numpy(ctx, sts.smooth_field(n, erng))
-        x1, x2, x3 = P.vector(), P.vector(), P.vector()
+        x1, x2, x3, x4 = P.vector(), P.vector(), P.vector(), P.vector()
         mg = sts.PFMG(P, relax=2, nrelax=2)  # the reference's multilevel comparator (PFMG role)
+        # the network behind PSetup / PSolve inside flexible GMRES(30), classical Gram-Schmidt
+        NP = sts.NetPrec(net, P)
+        FG = sts.SPFGMRSolver(ctx, b, maxl=30, max_restarts=2000, gstype=sts.CLASSICAL_GS, precond=True)
         res = {}
         for rep in range(2):  # the first solve of each kind warms up (graph instantiation)
             ctx.synchronize()
@@ -537,7 +540,15 @@ def run_precond(args):
             t = time.perf_counter()
             it4, rel4, rc4 = sts.implicit_solve_pfmg(P, gh, mg, b, x3, tol=1e-8, maxit=10000)
             t_mg = time.perf_counter() - t
+            ctx.synchronize()
+            t = time.perf_counter()
+            NP.setup(gh)
+            rc5, it5, rel5 = sts.implicit_solve_ls(P, gh, FG, b, x4, tol=1e-8, prec=sts.PREC_USER,
+                                                   pdata=NP.h, psolve=NP.psolve_fn)
+            t_fg = time.perf_counter() - t
             res = {"ky": ky, "gamma_h": gh, "pcg_iters": it1, "pcg_s": t_pcg, "pcg_relres": rel1,
+                   "fgmres_net_iters": it5, "fgmres_net_s": t_fg, "fgmres_net_relres": rel5,
+                   "fgmres_net_status": rc5,
                    "pfmg_iters": it4, "pfmg_s": t_mg, "pfmg_relres": rel4, "pfmg_levels": mg.levels(),
                    "fcg_iters": it2, "fcg_s": t_fcg, "fcg_true_relres": rel2, "fcg_status": rc2,
                    "pcg_ms_per_iter": 1e3 * t_pcg / max(1, it1),
@@ -547,9 +558,10 @@ def run_precond(args):
         xa, xb = x1.numpy(), x2.numpy()
         res["solution_rel_diff"] = float(np.linalg.norm(xa - xb) / np.linalg.norm(xa))
         res["pfmg_solution_rel_diff"] = float(np.linalg.norm(xa - x3.numpy()) / np.linalg.norm(xa))
+        res["fgmres_net_solution_rel_diff"] = float(np.linalg.norm(xa - x4.numpy()) / np.linalg.norm(xa))
         rows.append(res)
         print(json.dumps(res), flush=True)
-        del mg
+        del mg, FG, NP
         P.free()
     t_pcg = sum(r["pcg_s"] for r in rows)
     t_fcg = sum(r["fcg_s"] for r in rows)
@@ -562,6 +574,8 @@ def run_precond(args):
         "fcg_only_speedup": t_pcg / t_fcg,
         "pfmg_total_s": sum(r["pfmg_s"] for r in rows),
         "pfmg_speedup_vs_jacobi_pcg": t_pcg / max(1e-12, sum(r["pfmg_s"] for r in rows)),
+        "fgmres_net_total_s": sum(r["fgmres_net_s"] for r in rows),
+        "fgmres_net_speedup_vs_jacobi_pcg": t_pcg / max(1e-12, sum(r["fgmres_net_s"] for r in rows)),
         "systems_on_net": sum(1 for r in rows if r["learned_used_net"]),
         "max_learned_relres": max(r["learned_relres"] for r in rows),
         "iters_ratio": sum(r["pcg_iters"] for r in rows) / max(1, sum(r["fcg_iters"] for r in rows)),
