@@ -243,10 +243,12 @@ atexit.register(_at_exit)
 
 
 def lib(build=True):
-    """Load libstsgpu.so (building it first if needed)."""
+    """Load libstsgpu.so (building it first if needed). The environment variable
+    STS_LIBRARY_VARIANT=bounds selects the debug-bounds build instead."""
     global _lib
     if _lib is None:
-        path = _build.build() if build else _build.LIB
+        variant = os.environ.get("STS_LIBRARY_VARIANT", "")
+        path = _build.build(variant=variant) if build else _build.lib_path(variant)
         if not os.path.exists(path):
             raise STSError("libstsgpu.so is not built: run __graft_entry__.build()")
         L = C.CDLL(path)

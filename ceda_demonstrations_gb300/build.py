@@ -38,25 +38,41 @@ def _deps():
         [os.path.join(HERE, "..", "include", "stsgpu.h"), os.path.abspath(__file__), CLI_SRC]
 
 
-def up_to_date():
-    if not os.path.exists(LIB) or not os.path.exists(CLI):
+# Build variants: "" is the product; "bounds" adds -DSTS_DEBUG_BOUNDS (kernels check the index
+# range each thread touches and report a violation through the context's error word) into
+# _build/bounds/, without the command-line driver.
+VARIANTS = {"": [], "bounds": ["-DSTS_DEBUG_BOUNDS"]}
+
+
+def lib_path(variant=""):
+    return LIB if not variant else os.path.join(OUT_DIR, variant, "libstsgpu.so")
+
+
+def up_to_date(variant=""):
+    lib = lib_path(variant)
+    if not os.path.exists(lib) or (not variant and not os.path.exists(CLI)):
         return False
-    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
+    t = os.path.getmtime(lib) if variant else min(os.path.getmtime(lib), os.path.getmtime(CLI))
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
-def build(force=False, verbose=False, extra=()):
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(OUT_DIR, exist_ok=True)
+def build(force=False, verbose=False, extra=(), variant=""):
+    if variant not in VARIANTS:
+        raise ValueError("unknown build variant %r" % variant)
+    lib = lib_path(variant)
+    if not force and up_to_date(variant):
+        return lib
+    out_dir = os.path.dirname(lib)
+    os.makedirs(out_dir, exist_ok=True)
     nvcc = _nvcc()
     common = [ARCH, "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler",
-              "-fPIC,-ffp-contract=off,-O2", "-I" + os.path.join(HERE, "..", "include")] + list(extra)
+              "-fPIC,-ffp-contract=off,-O2", "-I" + os.path.join(HERE, "..", "include")] + \
+        VARIANTS[variant] + list(extra)
     if verbose:
         common += ["-Xptxas", "-v"]
 
     def compile_one(src):
-        obj = os.path.join(OUT_DIR, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(out_dir, os.path.basename(src)[:-3] + ".o")
         cmd = [nvcc, "-c", src, "-o", obj] + common
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -69,12 +85,14 @@ def build(force=False, verbose=False, extra=()):
         for _, err in results:
             sys.stderr.write(err)
     objs = [o for o, _ in results]
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc, ARCH, "-shared", "-cudart", "shared", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
+    if variant:
+        return lib
     # command-line driver (reference flags and output format), linked against the library
     cmd = [nvcc, "-O2", "-std=c++17", "-x", "c++", CLI_SRC, "-o", CLI + ".tmp",
            "-I" + os.path.join(HERE, "..", "include"), "-L" + OUT_DIR, "-lstsgpu",
@@ -87,5 +105,5 @@ def build(force=False, verbose=False, extra=()):
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose="-v" in sys.argv)
-    print(LIB)
+    v = "bounds" if "--bounds" in sys.argv else ""
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, variant=v))

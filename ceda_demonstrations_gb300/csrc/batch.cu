@@ -251,6 +251,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
     const int n = I.n;
     const int j0 = (int)((long long)n * rank / CL), j1 = (int)((long long)n * (rank + 1) / CL);
     const long long N = (long long)n * n;
+#ifdef STS_DEBUG_BOUNDS
+    // the instance's region lies inside the state arrays and every CTA of the cluster owns rows
+    if (I.off < 0 || I.off + N > total || n < CL)
+    {
+      if (rank == 0 && tid == 0) I.status = -5;
+      continue;
+    }
+#endif
     const double cx = I.cx, cy = I.cy, cc = I.cc, rho = I.rho;
     // six instance-local regions: the y array and five work regions; roles are indices
     double* P[6];

@@ -110,6 +110,7 @@ extern "C" STS_Problem STS_ProblemCreate(STS_Context ctx, int kind, sts_index nx
     return nullptr;
   }
   ProbDev& d = p->dev;
+  d.err      = ctx->d_err;
   d.nx       = nx;
   d.ny       = ny;
   d.kind     = kind;

@@ -136,6 +136,8 @@ __global__ void __launch_bounds__(256) stage64_kernel(ProbDev P, const StageArgs
   const long long jb = ((long long)blockIdx.y * blockDim.y + threadIdx.y) * RY;
   if (i0 >= nx || jb >= ny) return;
   const long long je = (jb + RY < ny) ? jb + RY : ny;
+  // the thread's VEC-wide loads and stores stay inside the row
+  if (!STS_IN_BOUNDS(i0 + VEC <= nx && i0 % VEC == 0, P.err)) return;
   const double gc = A->gc, gx = A->gx, gy = A->gy, gn = A->gn, g0 = A->g0, gf = A->gf;
   double Pi[VEC], Qi[VEC];
   if (FORCED)
@@ -216,6 +218,7 @@ __global__ void __launch_bounds__(256) stage32_kernel(ProbDev P, const StageArgs
   const long long jb = ((long long)blockIdx.y * blockDim.y + threadIdx.y) * RY;
   if (i0 >= nx || jb >= ny) return;
   const long long je = (jb + RY < ny) ? jb + RY : ny;
+  if (!STS_IN_BOUNDS(i0 + VEC <= nx && i0 % VEC == 0, P.err)) return;
   const float gc = A->gcf, gx = A->gxf, gy = A->gyf, gn = A->gnf, gF = A->gFf;
   float Pi[VEC], Qi[VEC];
   if (FORCED)
@@ -408,7 +411,8 @@ __global__ void __launch_bounds__(256) stepend_march_kernel(ProbDev P, const Ste
   xsum::zero(acc);
   unsigned flags   = 0;
   const bool colok = i0 < nx; // nx even: both columns valid
-  const bool active = colok && jb < ny;
+  // no early return here: the block reduction below has barriers
+  const bool active = colok && jb < ny && STS_IN_BOUNDS(i0 + 2 <= nx, P.err);
   // y_{n+1} at (row, i0..i0+1); zero outside the domain
   auto row2 = [&](long long j, double (&v)[2]) {
     if (!active || j < 0 || j >= ny)

@@ -1028,10 +1028,10 @@ static int evolve_fused(LSRKMem* m, double target, int itask)
       fill_params(m, p, m->t, h, s, mu, nu, mus, ajm1, cjm1);
       if (run_step_fused(m, p, s)) return STS_ERR_FAILURE;
       if (!STS_CUDA_OK(cudaStreamSynchronize(st))) return STS_ERR_FAILURE;
-      if (*(volatile int*)m->ctx->h_err)
+      if (const int ew = *(volatile int*)m->ctx->h_err)
       {
         *m->ctx->h_err = 0;
-        sts_set_error("LSRKStep: a stage kernel's pipeline wait timed out");
+        sts_set_error("LSRKStep: %s in a stage kernel", sts_err_word_text(ew));
         return STS_ERR_FAILURE;
       }
       const double dsm = ((volatile double*)m->ctx->h_slots)[SLOT_DSM];

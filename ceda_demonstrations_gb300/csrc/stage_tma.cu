@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(256, K::MINB)
         }
         o[v] = acc;
       }
-      if (y < ny && x < nx)
+      if (y < ny && x < nx && STS_IN_BOUNDS(x + 4 <= nx, err))
         *reinterpret_cast<float4*>(out + (long long)y * nx + x) = make_float4(o[0], o[1], o[2], o[3]);
       up  = cur;
       cur = dn;

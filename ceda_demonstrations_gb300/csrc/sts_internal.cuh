@@ -175,7 +175,31 @@ struct ProbDev {
   const double *Sx, *Sxx, *Sy, *Syy;
   const float *Sxf, *Sxxf, *Syf, *Syyf;
   const double *Dxw, *Dxe, *Dys, *Dyn;
+  int* err; // the context's error word (bounded waits, debug-bounds checks)
 };
+
+// Debug-bounds build (-DSTS_DEBUG_BOUNDS): before touching memory a kernel checks the index
+// range the thread (or the CTA) is about to use; a violation stores STS_ERR_WORD_BOUNDS in the
+// context's error word and the work is skipped, never trapped. The product build compiles the
+// checks to `true`.
+constexpr int STS_ERR_WORD_WAIT = 1, STS_ERR_WORD_TC_WAIT = 2, STS_ERR_WORD_BOUNDS = 3;
+inline const char* sts_err_word_text(int w)
+{
+  return w == STS_ERR_WORD_BOUNDS ? "an index range check failed (debug-bounds build)"
+                                  : "a pipeline wait timed out";
+}
+#ifdef STS_DEBUG_BOUNDS
+#ifdef __CUDACC__
+__device__ __forceinline__ bool sts_in_bounds(bool ok, int* err)
+{
+  if (!ok && err) atomicExch(err, STS_ERR_WORD_BOUNDS);
+  return ok;
+}
+#endif
+#define STS_IN_BOUNDS(cond, err) sts_in_bounds((cond), (err))
+#else
+#define STS_IN_BOUNDS(cond, err) true
+#endif
 
 struct STS_Problem_ {
   STS_Context ctx = nullptr;
