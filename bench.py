@@ -416,7 +416,7 @@ def run_batch(args):
     ctx = sts.Context(0)
     inst = sts.make_batch_instances(count=args.batch_count, seed=20261203)
     B = sts.Batch(ctx, inst)
-    th, cp, tune_ms = B.autotune(0.1 * args.batch_tf)
+    th, cp, tune_ms = B.autotune(0.25 * args.batch_tf)
     ms = B.evolve(args.batch_tf, method=sts.RKL, rtol=1e-6, atol=1e-10, smax=SMAX)
     y = B.state()
     nfe = [B.stats(i)["nfe"] for i in range(len(inst))]
@@ -437,6 +437,27 @@ def run_batch(args):
         yi = B.instance_state(y, i)
         maxrel = max(maxrel, float(np.linalg.norm(yi - J.y) / np.linalg.norm(J.y)))
     cpu_s = time.perf_counter() - t0
+    # the same batch with FP32 stage increments (own autotune), parity against the oracle's
+    # mixed integrator on the sample and accuracy against the FP64 batch
+    M = sts.Batch(ctx, inst)
+    M.set_mixed(True)
+    mth, mcp, mtune = M.autotune(0.25 * args.batch_tf)
+    mms = M.evolve(args.batch_tf, method=sts.RKL, rtol=1e-6, atol=1e-10, smax=SMAX)
+    ym = M.state()
+    mnfe = [M.stats(i)["nfe"] for i in range(len(inst))]
+    mdof = float(sum(inst[i][0] ** 2 * mnfe[i] for i in range(len(inst))))
+    mmax_or, mmax_64 = 0.0, 0.0
+    for i in sample:
+        n, kx, ky, p, q, a = inst[i]
+        P = po.Problem(po.UNFORCED, n, n, kx=kx, ky=ky)
+        J = po.Integrator(P, P.initial_modes(p, q, a), method=po.RKL, rtol=1e-6, atol=1e-10,
+                          mixed=True)
+        J.evolve(args.batch_tf)
+        yi = M.instance_state(ym, i)
+        mmax_or = max(mmax_or, float(np.linalg.norm(yi - J.y) / np.linalg.norm(J.y)))
+    for i in range(len(inst)):
+        ref = B.instance_state(y, i)
+        mmax_64 = max(mmax_64, float(np.linalg.norm(M.instance_state(ym, i) - ref) / np.linalg.norm(ref)))
     line = {
         "metric": "batched STS: DOF-stages/s and time for %d independent problems in one launch" % len(inst),
         "value": dof_stages / (ms / 1e3), "unit": "DOF-stages/s", "time_s": ms / 1e3,
@@ -448,6 +469,13 @@ def run_batch(args):
         "largest_instance_share": float(per_inst[0]) / dof_stages,
         "dtype": "f64", "data": "synthetic (seeded sine-mode initial states, seed 20261203)",
         "parity_sample_max_rel_l2_vs_oracle": maxrel,
+        "mixed": {"value": mdof / (mms / 1e3), "unit": "DOF-stages/s", "time_s": mms / 1e3,
+                  "dof_stages": mdof, "speedup_vs_f64": (mdof / (mms / 1e3)) / (dof_stages / (ms / 1e3)),
+                  "launch": {"threads": mth, "ctas_per_sm": mcp, "cluster_large": M.launch()[2],
+                             "probe_ms": mtune},
+                  "parity_sample_max_rel_l2_vs_mixed_oracle": mmax_or,
+                  "max_rel_l2_vs_f64_batch": mmax_64,
+                  "dtype": "f32 stage increments + f64 step update"},
         "cpu_baseline": {"value": cpu_dof / cpu_s, "unit": "DOF-stages/s", "cores": po.lib().orc_nthreads(),
                          "kind": "port", "sample": "%d of the %d instances, integrated one after another"
                                                    % (len(sample), len(inst))},

@@ -195,6 +195,7 @@ SIGNATURES = [
     ("STS_BatchLastMilliseconds", C.c_double, [_vp]),
     ("STS_BatchGetInstanceStats", C.c_int, [_vp, C.c_int, C.POINTER(Stats)]),
     ("STS_BatchSetLaunch", C.c_int, [_vp, C.c_int, C.c_int]),
+    ("STS_BatchSetMixed", C.c_int, [_vp, C.c_int]),
     ("STS_BatchAutotune", C.c_int, [_vp, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int,
                                     _ip, _ip, _dp]),
     ("STS_BatchSetCluster", C.c_int, [_vp, C.c_int, C.c_int]),
@@ -879,6 +880,11 @@ class Batch:
             _err("STS_BatchSetInitialModes")
         self.total = L.STS_BatchTotalDOF(self.h)
         self.offsets = np.concatenate([[0], np.cumsum([i[0] ** 2 for i in instances])])
+
+    def set_mixed(self, mixed):
+        """FP32 stage increments (True) or FP64 stages (False, the default)."""
+        if lib().STS_BatchSetMixed(self.h, int(bool(mixed))) != 0:
+            _err("STS_BatchSetMixed")
 
     def evolve(self, tf, method=RKL, rtol=1e-6, atol=1e-10, smax=200, controller=PID, maxsteps=0):
         rc = lib().STS_BatchEvolve(self.h, tf, method, rtol, atol, smax, controller, maxsteps)

@@ -52,6 +52,8 @@ struct BatchParams {
   double tf, rtol, atol, eig_safety;
   int method, smax, controller, maxsteps;
   const void* coef; // CoefT table [(smax + 1) x (smax + 1)]
+  int mixed;        // 1: FP32 stage increments relative to the FP64 step start
+  int pad_;
 };
 
 struct STS_Batch_ {
@@ -63,12 +65,13 @@ struct STS_Batch_ {
   int* dorder      = nullptr;
   int* dqueue      = nullptr;
   double* y        = nullptr;
-  double* work     = nullptr; // 5 x total
+  double* work     = nullptr; // 6 x total
   int block        = 512;
   int ctas_per_sm  = 2;
   double last_ms   = 0.0;
   CoefT* dcoef     = nullptr; // stage-coefficient table of (coef_method, coef_smax)
   int coef_method = -1, coef_smax = -1;
+  int mixed        = 0; // FP32 stage increments (STS_BatchSetMixed)
   // instances with n >= big_n run on clusters of `cluster` CTAs (1: all on single CTAs)
   int cluster      = 1;
   int big_n        = 256;
@@ -203,6 +206,7 @@ __device__ double inst_exact_sum(xsum::Limbs& a, unsigned flags, long long (*sm)
 // Stencil-row load: rows owned by another CTA of the cluster are read through L2 (ld.cg),
 // so no stale L1 line of an earlier sweep is used.
 __device__ __forceinline__ double ldrow(const double* p, bool foreign) { return foreign ? __ldcg(p) : *p; }
+__device__ __forceinline__ float ldrowf(const float* p, bool foreign) { return foreign ? __ldcg(p) : *p; }
 
 __device__ __forceinline__ double lap(const double* __restrict__ u, int n, int i, int j, int j0, int j1, double cx,
                                       double cy, double cc)
@@ -260,16 +264,29 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
     }
 #endif
     const double cx = I.cx, cy = I.cy, cc = I.cc, rho = I.rho;
-    // six instance-local regions: the y array and five work regions; roles are indices
-    double* P[6];
+    // seven instance-local regions: the y array and six work regions; roles are indices.
+    // FP64 stages: y, F, F_new and three Y stage buffers (regions 3-5). Mixed stages: y, F,
+    // F_new, y_new (region 3) and, as FP32 arrays of N values, three increments d (regions 4
+    // and 5) and the FP32 copies of F and F_new (region 5, second half, and region 6).
+    double* P[7];
     P[0] = yall + I.off;
-    for (int q = 0; q < 5; ++q) P[q + 1] = work + (long long)q * total + I.off;
+    for (int q = 0; q < 6; ++q) P[q + 1] = work + (long long)q * total + I.off;
     int iy = 0, iF = 1, iFn = 2;
     int bufs[3] = {3, 4, 5}; // stage buffers (rotated like the single-problem integrator)
+    int iyn = 3, iff = 0;    // mixed: y_new region, which FP32 F copy is current
+    float* D[3]  = {reinterpret_cast<float*>(P[4]), reinterpret_cast<float*>(P[4]) + N,
+                    reinterpret_cast<float*>(P[5])};
+    float* Ff[2] = {reinterpret_cast<float*>(P[5]) + N, reinterpret_cast<float*>(P[6])};
 
-    // F_0 = A y_0
+    // F_0 = A y_0 (and its FP32 copy for the mixed stages)
     for (int j = j0 + warp; j < j1; j += NW)
-      for (int i = lane; i < n; i += 32) P[iF][(long long)j * n + i] = lap(P[iy], n, i, j, j0, j1, cx, cy, cc);
+      for (int i = lane; i < n; i += 32)
+      {
+        const long long k = (long long)j * n + i;
+        const double f    = lap(P[iy], n, i, j, j0, j1, cx, cy, cc);
+        P[iF][k]          = f;
+        if (prm.mixed) Ff[0][k] = (float)f;
+      }
     inst_sync<CL>();
     long long nfe = 1, nst = 0, natt = 0, netf = 0, nexp = 0, stmax = 0, sttot = 0, nhist = 0;
     double t = 0.0, hnext = 0.0, hlast = 0.0, ep1 = 0.0, ep2 = 0.0;
@@ -357,83 +374,173 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
         const CoefT* ct = reinterpret_cast<const CoefT*>(prm.coef) + (long long)s * (prm.smax + 1);
         const double* yc = P[iy];
         const double* F0 = P[iF];
-        // stage 1 -> bufs[0]
-        {
-          const double hm1 = h * ct[1].mus;
-          double* y1       = P[bufs[0]];
-          for (int j = j0 + warp; j < j1; j += NW)
-            for (int i = lane; i < n; i += 32)
-            {
-              const long long k = (long long)j * n + i;
-              y1[k]             = __fma_rn(hm1, F0[k], yc[k]);
-            }
-          inst_sync<CL>();
-        }
-        const double* ym2 = yc;
-        int last          = 0; // index into bufs of Y_{j-1}
-        for (int jst = 2; jst <= s; ++jst)
-        {
-          const double mu = ct[jst].mu, nu = ct[jst].nu, mus = ct[jst].mus, ajm1 = ct[jst].ajm1;
-          const double hm = h * mus;
-          const double tm = hm * cc;
-          const double gc = mu + tm, gx = hm * cx, gy = hm * cy, gn = nu, g0 = (1.0 - mu) - nu;
-          const double gf = -(hm * ajm1);
-          const double* ym1 = P[bufs[last]];
-          const int nxt     = (last + 1) % 3;
-          double* yj        = P[bufs[nxt]];
-          for (int j = j0 + warp; j < j1; j += NW)
-            for (int i = lane; i < n; i += 32)
-            {
-              const long long k = (long long)j * n + i;
-              const double uw = (i > 0) ? ym1[k - 1] : 0.0;
-              const double ue = (i < n - 1) ? ym1[k + 1] : 0.0;
-              const double us = (j > 0) ? ldrow(&ym1[k - n], j - 1 < j0) : 0.0;
-              const double un = (j < n - 1) ? ldrow(&ym1[k + n], j + 1 >= j1) : 0.0;
-              const double sx = uw + ue, sy = us + un;
-              double acc      = gc * ym1[k];
-              acc             = __fma_rn(gx, sx, acc);
-              acc             = __fma_rn(gy, sy, acc);
-              acc             = __fma_rn(gn, ym2[k], acc);
-              acc             = __fma_rn(g0, yc[k], acc);
-              acc             = __fma_rn(gf, F0[k], acc);
-              yj[k]           = acc;
-            }
-          inst_sync<CL>();
-          ym2  = ym1;
-          last = nxt;
-        }
-        const double* Ys = P[bufs[last]];
-        double* Fnew     = P[iFn];
-        // step end: Fnew = A Ys, err = 0.8 (y - Ys) + 0.4 h (F + Fnew), exact WRMS
         xsum::Limbs ae;
         xsum::zero(ae);
         unsigned fe      = 0;
         const double p4h = 0.4 * h;
-        for (int j = j0 + warp; j < j1; j += NW)
-          for (int i = lane; i < n; i += 32)
+        int last         = 0; // FP64 stages: index into bufs of Y_{j-1}
+        if (prm.mixed)
+        {
+          // stage 1: d_1 = (h mus_1) F_0 in FP32
           {
-            const long long k = (long long)j * n + i;
-            const double f    = lap(Ys, n, i, j, j0, j1, cx, cy, cc);
-            Fnew[k]           = f;
-            const double yv   = yc[k];
-            const double d    = yv - Ys[k];
-            double e          = 0.8 * d;
-            e                 = __fma_rn(p4h, F0[k], e);
-            e                 = __fma_rn(p4h, f, e);
-            const double wt   = 1.0 / (prm.rtol * fabs(yv) + prm.atol);
-            const double x    = e * wt;
-            xsum::add(ae, x * x, fe);
+            const float hm1  = (float)(h * ct[1].mus);
+            const float* ff  = Ff[iff];
+            float* d1        = D[0];
+            for (int j = j0 + warp; j < j1; j += NW)
+              for (int i = lane; i < n; i += 32)
+              {
+                const long long k = (long long)j * n + i;
+                d1[k]             = hm1 * ff[k];
+              }
+            inst_sync<CL>();
           }
+          const float* dm2 = nullptr; // d_{j-2}; none at stage 2
+          int lastd        = 0;
+          for (int jst = 2; jst <= s; ++jst)
+          {
+            const double mu = ct[jst].mu, nu = ct[jst].nu, mus = ct[jst].mus, ajm1 = ct[jst].ajm1;
+            const double hm = h * mus;
+            const double tm = hm * cc;
+            const float gc = (float)(mu + tm), gx = (float)(hm * cx), gy = (float)(hm * cy), gn = (float)nu;
+            const float gF   = (float)(hm * (1.0 - ajm1));
+            const float* dm1 = D[lastd];
+            const float* ff  = Ff[iff];
+            const int nxt    = (lastd + 1) % 3;
+            float* dj        = D[nxt];
+            for (int j = j0 + warp; j < j1; j += NW)
+              for (int i = lane; i < n; i += 32)
+              {
+                const long long k = (long long)j * n + i;
+                const float dw = (i > 0) ? dm1[k - 1] : 0.0f;
+                const float de = (i < n - 1) ? dm1[k + 1] : 0.0f;
+                const float ds = (j > 0) ? ldrowf(&dm1[k - n], j - 1 < j0) : 0.0f;
+                const float dn = (j < n - 1) ? ldrowf(&dm1[k + n], j + 1 >= j1) : 0.0f;
+                const float sx = dw + de, sy = ds + dn;
+                float acc      = gc * dm1[k];
+                acc            = __fmaf_rn(gx, sx, acc);
+                acc            = __fmaf_rn(gy, sy, acc);
+                if (dm2) acc = __fmaf_rn(gn, dm2[k], acc);
+                acc   = __fmaf_rn(gF, ff[k], acc);
+                dj[k] = acc;
+              }
+            inst_sync<CL>();
+            dm2   = dm1;
+            lastd = nxt;
+          }
+          // step end: y_new = y + d_s (FP64), then F_new = A y_new, its FP32 copy and the error
+          const float* dsv = D[lastd];
+          double* yn       = P[iyn];
+          for (int j = j0 + warp; j < j1; j += NW)
+            for (int i = lane; i < n; i += 32)
+            {
+              const long long k = (long long)j * n + i;
+              yn[k]             = yc[k] + (double)dsv[k];
+            }
+          inst_sync<CL>();
+          double* Fnew = P[iFn];
+          float* Ffn   = Ff[1 - iff];
+          for (int j = j0 + warp; j < j1; j += NW)
+            for (int i = lane; i < n; i += 32)
+            {
+              const long long k = (long long)j * n + i;
+              const double f    = lap(yn, n, i, j, j0, j1, cx, cy, cc);
+              Fnew[k]           = f;
+              Ffn[k]            = (float)f;
+              const double yv   = yc[k];
+              const double d    = yv - yn[k];
+              double e          = 0.8 * d;
+              e                 = __fma_rn(p4h, F0[k], e);
+              e                 = __fma_rn(p4h, f, e);
+              const double wt   = 1.0 / (prm.rtol * fabs(yv) + prm.atol);
+              const double x    = e * wt;
+              xsum::add(ae, x * x, fe);
+            }
+        }
+        else
+        {
+          // stage 1 -> bufs[0]
+          {
+            const double hm1 = h * ct[1].mus;
+            double* y1       = P[bufs[0]];
+            for (int j = j0 + warp; j < j1; j += NW)
+              for (int i = lane; i < n; i += 32)
+              {
+                const long long k = (long long)j * n + i;
+                y1[k]             = __fma_rn(hm1, F0[k], yc[k]);
+              }
+            inst_sync<CL>();
+          }
+          const double* ym2 = yc;
+          for (int jst = 2; jst <= s; ++jst)
+          {
+            const double mu = ct[jst].mu, nu = ct[jst].nu, mus = ct[jst].mus, ajm1 = ct[jst].ajm1;
+            const double hm = h * mus;
+            const double tm = hm * cc;
+            const double gc = mu + tm, gx = hm * cx, gy = hm * cy, gn = nu, g0 = (1.0 - mu) - nu;
+            const double gf = -(hm * ajm1);
+            const double* ym1 = P[bufs[last]];
+            const int nxt     = (last + 1) % 3;
+            double* yj        = P[bufs[nxt]];
+            for (int j = j0 + warp; j < j1; j += NW)
+              for (int i = lane; i < n; i += 32)
+              {
+                const long long k = (long long)j * n + i;
+                const double uw = (i > 0) ? ym1[k - 1] : 0.0;
+                const double ue = (i < n - 1) ? ym1[k + 1] : 0.0;
+                const double us = (j > 0) ? ldrow(&ym1[k - n], j - 1 < j0) : 0.0;
+                const double un = (j < n - 1) ? ldrow(&ym1[k + n], j + 1 >= j1) : 0.0;
+                const double sx = uw + ue, sy = us + un;
+                double acc      = gc * ym1[k];
+                acc             = __fma_rn(gx, sx, acc);
+                acc             = __fma_rn(gy, sy, acc);
+                acc             = __fma_rn(gn, ym2[k], acc);
+                acc             = __fma_rn(g0, yc[k], acc);
+                acc             = __fma_rn(gf, F0[k], acc);
+                yj[k]           = acc;
+              }
+            inst_sync<CL>();
+            ym2  = ym1;
+            last = nxt;
+          }
+          const double* Ys = P[bufs[last]];
+          double* Fnew     = P[iFn];
+          // step end: Fnew = A Ys, err = 0.8 (y - Ys) + 0.4 h (F + Fnew), exact WRMS
+          for (int j = j0 + warp; j < j1; j += NW)
+            for (int i = lane; i < n; i += 32)
+            {
+              const long long k = (long long)j * n + i;
+              const double f    = lap(Ys, n, i, j, j0, j1, cx, cy, cc);
+              Fnew[k]           = f;
+              const double yv   = yc[k];
+              const double d    = yv - Ys[k];
+              double e          = 0.8 * d;
+              e                 = __fma_rn(p4h, F0[k], e);
+              e                 = __fma_rn(p4h, f, e);
+              const double wt   = 1.0 / (prm.rtol * fabs(yv) + prm.atol);
+              const double x    = e * wt;
+              xsum::add(ae, x * x, fe);
+            }
+        }
         const double dsm = sqrt(inst_exact_sum<NT, CL>(ae, fe, sm, climb, &sflags, &sres) / (double)N);
         nfe += s;
         sttot += s;
         if (s > stmax) stmax = s;
         if (dsm <= 1.0)
-        { // accept: y <- Ys (role swap with its stage buffer), F <- Fnew
+        { // accept: y <- Ys (role swap with its stage buffer or with y_new), F <- Fnew
           t = clipped ? prm.tf : t + h;
-          const int ys = bufs[last];
-          bufs[last]   = iy;
-          iy           = ys;
+          if (prm.mixed)
+          {
+            const int yv_ = iyn;
+            iyn           = iy;
+            iy            = yv_;
+            iff           = 1 - iff;
+          }
+          else
+          {
+            const int ys = bufs[last];
+            bufs[last]   = iy;
+            iy           = ys;
+          }
           const int tf_ = iF;
           iF           = iFn;
           iFn          = tf_;
@@ -674,7 +781,7 @@ extern "C" STS_Batch STS_BatchCreate(STS_Context ctx, int ninst, const int* n, c
             STS_CUDA_OK(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming)) &&
             STS_CUDA_OK(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming)) &&
             STS_CUDA_OK(cudaMalloc(&b->y, b->total * sizeof(double))) &&
-            STS_CUDA_OK(cudaMalloc(&b->work, 5 * b->total * sizeof(double))) &&
+            STS_CUDA_OK(cudaMalloc(&b->work, 6 * b->total * sizeof(double))) &&
             STS_CUDA_OK(cudaMemcpy(b->dinst, b->hinst.data(), ninst * sizeof(BatchInst), cudaMemcpyHostToDevice)) &&
             STS_CUDA_OK(cudaMemcpy(b->dorder, order.data(), ninst * sizeof(int), cudaMemcpyHostToDevice)) &&
             STS_CUDA_OK(cudaMemset(b->y, 0, b->total * sizeof(double))) && batch_regroup(b);
@@ -768,6 +875,8 @@ extern "C" int STS_BatchEvolve(STS_Batch b, double tf, int method, double rtol, 
   prm.smax       = smax;
   prm.controller = controller;
   prm.maxsteps   = (int)(maxsteps > 0 ? std::min<long long>(maxsteps, 1LL << 30) : 1000000);
+  prm.mixed      = b->mixed;
+  prm.pad_       = 0;
   if (b->coef_method != method || b->coef_smax != smax)
   {
     const int S = smax + 1;
@@ -829,6 +938,13 @@ extern "C" int STS_BatchGetInstanceStats(STS_Batch b, int inst, STS_Stats* s)
   s->hlast           = I.hlast;
   s->hnext           = I.hnext;
   s->spectral_radius = I.rho;
+  return 0;
+}
+
+extern "C" int STS_BatchSetMixed(STS_Batch b, int mixed)
+{
+  if (!b || (mixed != 0 && mixed != 1)) return STS_ILL_INPUT;
+  b->mixed = mixed;
   return 0;
 }
 

@@ -395,6 +395,10 @@ double STS_BatchLastMilliseconds(STS_Batch b);
 int STS_BatchGetInstanceStats(STS_Batch b, int inst, STS_Stats* stats);
 /* launch shape: threads per CTA (256 or 512) and CTAs per SM */
 int STS_BatchSetLaunch(STS_Batch b, int threads, int ctas_per_sm);
+/* mixed = 1: stages as FP32 increments relative to the FP64 step start (the single-problem
+ * integrator's mixed form: FP32 copy of F_n, FP64 step update, error estimate and exact WRMS);
+ * 0 (default): FP64 stages */
+int STS_BatchSetMixed(STS_Batch b, int mixed);
 /* autotuner: time every launch shape on the probe horizon [0, tf_probe], keep the fastest */
 int STS_BatchAutotune(STS_Batch b, double tf_probe, int method, double rtol, double atol,
                       int smax, int* threads, int* ctas_per_sm, double* ms_best);

@@ -34,6 +34,48 @@ def test_batch_matches_oracle_per_instance(ctx, stslib, oracle, method, controll
         assert np.array_equal(yi, J.y), (i, np.abs(yi - J.y).max())
 
 
+@pytest.mark.parametrize("method,controller", [(1, 0), (0, 0), (1, 3), (0, 5)])
+def test_batch_mixed_matches_oracle_per_instance(ctx, stslib, oracle, method, controller):
+    """FP32 stage increments in the batched launch: every instance equals the oracle's mixed
+    single-problem integrator bit for bit. Against the FP64 batch the two adaptive runs take
+    their own step sequences, so they agree to the tolerance level (1e-5 relative L2 at
+    rtol 1e-6), not to rounding."""
+    inst = small_batch(stslib)
+    B = stslib.Batch(ctx, inst)
+    B.set_mixed(True)
+    B.evolve(0.01, method=method, rtol=1e-6, atol=1e-10, controller=controller)
+    y = B.state()
+    C64 = stslib.Batch(ctx, inst)
+    C64.evolve(0.01, method=method, rtol=1e-6, atol=1e-10, controller=controller)
+    y64 = C64.state()
+    for i, (n, kx, ky, p, q, a) in enumerate(inst):
+        P = oracle.Problem(oracle.UNFORCED, n, n, kx=kx, ky=ky)
+        J = oracle.Integrator(P, P.initial_modes(p, q, a), method=method, rtol=1e-6, atol=1e-10,
+                              controller=controller, mixed=True)
+        assert J.evolve(0.01) == 0
+        yi = B.instance_state(y, i)
+        st, so = B.stats(i), J.stats()
+        assert st["t"] == 0.01
+        for k in ("nst", "nst_attempts", "netf", "stages_total", "stage_max"):
+            assert st[k] == so[k], (i, k, st[k], so[k])
+        assert np.array_equal(yi, J.y), (i, np.abs(yi - J.y).max())
+        ref = C64.instance_state(y64, i)
+        assert np.linalg.norm(yi - ref) <= 1e-5 * np.linalg.norm(ref), i
+
+
+def test_batch_mixed_launch_shapes_agree_bitwise(ctx, stslib):
+    inst = small_batch(stslib, count=12, seed=3)
+    outs = []
+    for threads, cps, cluster in ((256, 1, 1), (512, 2, 1), (256, 2, 2), (256, 4, 8)):
+        B = stslib.Batch(ctx, inst)
+        B.set_mixed(True)
+        assert B.set_launch(threads, cps, cluster, big_n=32) == 0
+        B.evolve(0.005, method=stslib.RKC, rtol=1e-6, atol=1e-10)
+        outs.append(B.state())
+    for o in outs[1:]:
+        assert np.array_equal(outs[0], o)
+
+
 def test_batch_launch_shapes_agree_bitwise(ctx, stslib):
     """Launch shape and thread-block clusters (instances with n >= 32 split over 2, 4 or 8
     CTAs, exact reductions combined through distributed shared memory) change nothing."""
