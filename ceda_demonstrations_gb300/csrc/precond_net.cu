@@ -27,25 +27,7 @@
 #include <random>
 #include <vector>
 
-#include "krylov.cuh"
 #include "sts_internal.cuh"
-
-namespace net {
-// device scalars of the fused flexible CG (below); the collapsed level-0 z kernel can produce
-// beta itself
-struct FcgScal {
-  double beta, alpha, pq_prev, rr, gamma, tolb;
-  int iters, maxit, state, pad_; // state: 0 running, 1 converged, 2 iteration limit, 3 breakdown
-  unsigned long long limbs[2][xsum::NL];
-  unsigned int flags[2];
-  unsigned int ticket, pad2_;
-};
-
-struct FcgOut {
-  int state, iters;
-  double rr;
-};
-} // namespace net
 
 namespace net {
 
@@ -952,35 +934,18 @@ __global__ void __launch_bounds__(PTX * PTY) p0_kernel(const double* __restrict_
 
 // z = (out_scale scale) r + (double)((float)out_scale u), u = conv(v, K) (+ edge corrections)
 // + conv(0.25 up(y1), G); thread = one coarse cell, its 2 x 2 fine pixels
-// BETA: also the flexible-CG scalar beta = -(z . q_prev) / (p_prev . q_prev) from an exact dot
-// of the z values this kernel writes (the separate fcg_beta_kernel pass over z and q_prev
-// disappears); skipped, like the other Krylov kernels, once the solve has stopped.
-template <bool BETA>
 __global__ void __launch_bounds__(ZTX * ZTY) z_kernel(const double* __restrict__ r, double scale, double out_scale,
                                                       int n, const __nv_bfloat16* __restrict__ y1, FoldB fb,
-                                                      double* __restrict__ z, const double* __restrict__ qprev,
-                                                      FcgScal* fs_)
+                                                      double* __restrict__ z)
 {
-  if (BETA && fs_->state != 0) return;
   constexpr int VR = 2 * ZTY + 4, VC = 2 * ZTX + 4; // fine window: rows 2J0-2 .., columns 2I0-2 ..
   constexpr int YR = ZTY + 2, YC = ZTX + 2;         // coarse window: rows J0-1 .., columns I0-1 ..
   __shared__ float vw[VR][VC + 1];
   __shared__ float4 yw[YR][4][YC];
   const int tid = threadIdx.x, tx = tid % ZTX, ty = tid / ZTX;
   const int nc = n / 2;
+  const int I0 = blockIdx.x * ZTX, J0 = blockIdx.y * ZTY;
   const float fs = (float)scale;
-  // tiles of ZTX x ZTY coarse cells; a 2-D grid covers one tile per block, a 1-D grid (BETA:
-  // about six blocks per SM, so that few blocks join the exact reduction) strides over them
-  const int tiles_x = (nc + ZTX - 1) / ZTX, ntiles = tiles_x * ((nc + ZTY - 1) / ZTY);
-  const bool grid1d = gridDim.y == 1 && gridDim.x != (unsigned)tiles_x;
-  xsum::Limbs a[1];
-  unsigned fl[1] = {0};
-  xsum::zero(a[0]);
-  for (int tile = grid1d ? (int)blockIdx.x : (int)(blockIdx.y * tiles_x + blockIdx.x); tile < ntiles;
-       tile += grid1d ? (int)gridDim.x : ntiles)
-  {
-  const int I0 = (tile % tiles_x) * ZTX, J0 = (tile / tiles_x) * ZTY;
-  __syncthreads(); // the previous tile's windows are no longer read
   for (int e = tid; e < VR * VC; e += ZTX * ZTY)
   {
     const int wr = e / VC, wc = e % VC;
@@ -1002,13 +967,10 @@ __global__ void __launch_bounds__(ZTX * ZTY) z_kernel(const double* __restrict__
   }
   __syncthreads();
   const int I = I0 + tx, J = J0 + ty;
-  const bool active = I < nc && J < nc;
-  // threads past the grid's edge run the arithmetic on clamped indices and store nothing, so
-  // that every thread reaches the barriers and the block reduction
-  const int Ic = active ? I : 0, Jc = active ? J : 0;
-  const long long row0 = (long long)(2 * Jc) * n;
-  const double2 r0 = __ldg(reinterpret_cast<const double2*>(r + row0 + 2 * Ic));
-  const double2 r1 = __ldg(reinterpret_cast<const double2*>(r + row0 + n + 2 * Ic));
+  if (I >= nc || J >= nc) return;
+  const long long row0 = (long long)(2 * J) * n;
+  const double2 r0 = __ldg(reinterpret_cast<const double2*>(r + row0 + 2 * I));
+  const double2 r1 = __ldg(reinterpret_cast<const double2*>(r + row0 + n + 2 * I));
   // conv(v, K): window rows 2ty .. 2ty+5, columns 2tx .. 2tx+5
   float u[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
 #pragma unroll
@@ -1089,25 +1051,8 @@ __global__ void __launch_bounds__(ZTX * ZTY) z_kernel(const double* __restrict__
   z0.y = __fma_rn(osc, r0.y, (double)(fo * u[0][1]));
   z1.x = __fma_rn(osc, r1.x, (double)(fo * u[1][0]));
   z1.y = __fma_rn(osc, r1.y, (double)(fo * u[1][1]));
-  if (active)
-  {
-    *reinterpret_cast<double2*>(z + row0 + 2 * I)     = z0;
-    *reinterpret_cast<double2*>(z + row0 + n + 2 * I) = z1;
-  }
-  if (BETA && active)
-  {
-    const double2 q0 = __ldg(reinterpret_cast<const double2*>(qprev + row0 + 2 * I));
-    const double2 q1 = __ldg(reinterpret_cast<const double2*>(qprev + row0 + n + 2 * I));
-    xsum::add(a[0], z0.x * q0.x, fl[0]);
-    xsum::add(a[0], z0.y * q0.y, fl[0]);
-    xsum::add(a[0], z1.x * q1.x, fl[0]);
-    xsum::add(a[0], z1.y * q1.y, fl[0]);
-  }
-  } // tiles
-  if constexpr (BETA)
-    krylov_block_finish<ZTX * ZTY, 1>(a, fl, fs_, [&](const double* v) {
-      fs_->beta = (fs_->iters > 0) ? -v[0] / fs_->pq_prev : 0.0;
-    });
+  *reinterpret_cast<double2*>(z + row0 + 2 * I)     = z0;
+  *reinterpret_cast<double2*>(z + row0 + n + 2 * I) = z1;
 }
 } // namespace l0
 
@@ -1860,11 +1805,8 @@ static void net_forward(STS_Net nt, int n, int nimg, const T* r, double scale, f
 // Inference of one n x n residual (FP64, device) into zout: the input channels are built in the
 // first convolution's tile loader and the sums g_l = h_l + poolT(y_{l+1}) in the transposed
 // convolutions' loaders, so only h_l, p_l and y_l are stored. Bitwise the output of net_forward.
-// With qprev and fcg, the collapsed level-0 z kernel also produces the flexible-CG beta; the
-// return value says whether it did (otherwise the caller runs fcg_beta_kernel).
-static bool net_forward_infer(STS_Net nt, int n, const double* r, double scale, float sk, float sg, double out_scale,
-                              double* zout, const net::l0::FoldA* fa = nullptr, const net::l0::FoldB* fb = nullptr,
-                              const double* qprev = nullptr, net::FcgScal* fcg = nullptr)
+static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, float sk, float sg, double out_scale,
+                              double* zout, const net::l0::FoldA* fa = nullptr, const net::l0::FoldB* fb = nullptr)
 {
   net::Level* L = nt->L;
   net::LoadArgs la;
@@ -1893,7 +1835,7 @@ static bool net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
     lu.sk     = sk;
     lu.sg     = sg;
     conv_tc<2, net::LD_UPADD>(nt, L[0].h, n, nt->wut + net::L_IN * WL, nullptr, zout, out_scale, lu); // z
-    return false;
+    return;
   }
   const bool collapsed = nt->collapse_l0 && fa && fb && n % 2 == 0;
   cudaStream_t st      = nt->ctx->stream;
@@ -1919,18 +1861,8 @@ static bool net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
   {
     const int nc = n / 2;
     dim3 g((unsigned)((nc + net::l0::ZTX - 1) / net::l0::ZTX), (unsigned)((nc + net::l0::ZTY - 1) / net::l0::ZTY));
-    if (qprev && fcg)
-    {
-      const unsigned ntiles = g.x * g.y;
-      unsigned g1           = (unsigned)nt->ctx->num_sms * 6u;
-      if (g1 >= ntiles || g1 == g.x) g1 = ntiles; // one tile per block (never mistaken for the 2-D form)
-      net::l0::z_kernel<true><<<dim3(g1 == ntiles ? g.x : g1, g1 == ntiles ? g.y : 1), net::l0::ZTX * net::l0::ZTY, 0,
-                                st>>>(r, scale, out_scale, n, L[1].y, *fb, zout, qprev, fcg); // z, beta
-      return true;
-    }
-    net::l0::z_kernel<false><<<g, net::l0::ZTX * net::l0::ZTY, 0, st>>>(r, scale, out_scale, n, L[1].y, *fb, zout,
-                                                                        nullptr, nullptr); // z
-    return false;
+    net::l0::z_kernel<<<g, net::l0::ZTX * net::l0::ZTY, 0, st>>>(r, scale, out_scale, n, L[1].y, *fb, zout); // z
+    return;
   }
   lu.coarse = L[1].y;
   lu.r      = r;
@@ -1938,7 +1870,6 @@ static bool net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
   lu.sk     = sk;
   lu.sg     = sg;
   conv_launch<2, net::LD_UPADD>(nt, L[0].h, n, 1, nt->wt + net::L_IN * 576, nullptr, zout, out_scale, nullptr, lu); // z
-  return false;
 }
 
 static void wgrad(STS_Net nt, const __nv_bfloat16* x, const __nv_bfloat16* g, int n, int nimg, int layer)
@@ -2236,7 +2167,22 @@ extern "C" int STS_HarvestPCGPairs(STS_Problem p, double gamma, N_Vector b, int 
 //       p . r and p . q -> alpha                             (40 B/DOF + halo)
 //   KX: x += alpha p, r -= alpha q, r . r -> stop test        (48 B/DOF)
 // ---------------------------------------------------------------------------------------
+#include "krylov.cuh"
+
 namespace net {
+
+struct FcgScal {
+  double beta, alpha, pq_prev, rr, gamma, tolb;
+  int iters, maxit, state, pad_; // state: 0 running, 1 converged, 2 iteration limit, 3 breakdown
+  unsigned long long limbs[2][xsum::NL];
+  unsigned int flags[2];
+  unsigned int ticket, pad2_;
+};
+
+struct FcgOut {
+  int state, iters;
+  double rr;
+};
 
 constexpr int FCG_BATCH = 8; // iterations per graph launch (even: p, q ping-pong)
 
@@ -2464,8 +2410,8 @@ extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b,
       {
         double *pp = P2[k & 1], *pn = P2[(k + 1) & 1];
         double *qp = Q2[k & 1], *qn = Q2[(k + 1) & 1];
-        if (!net_forward_infer(nt, n, r, scale, (float)sk, (float)sg, jac / scale, z, &fa, &fb, qp, d_s))
-          net::fcg_beta_kernel<<<eb, 256, 0, st>>>(N, z, qp, d_s);
+        net_forward_infer(nt, n, r, scale, (float)sk, (float)sg, jac / scale, z, &fa, &fb);
+        net::fcg_beta_kernel<<<eb, 256, 0, st>>>(N, z, qp, d_s);
         net::fcg_pq_march_kernel<<<gm, bq, 0, st>>>(p->dev, z, pp, r, pn, qn, d_s, d_out);
         net::fcg_x_kernel<<<eb, 256, 0, st>>>(N, pn, qn, NVD(x), r, d_s, d_out);
       }
