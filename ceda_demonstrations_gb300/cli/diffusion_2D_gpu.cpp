@@ -5,7 +5,7 @@
 //
 // Problems: --problem periodic (default; the reference code's problem: periodic domain
 // [-pi,pi]x[-6,6], Gaussian x sine initial state, optional --inhomogeneous coefficients),
-// --problem manufactured (BASELINE manufactured Dirichlet problem on [0,1]^2) or unforced.
+// --problem manufactured (the manufactured-solution Dirichlet benchmark problem on [0,1]^2) or unforced.
 // Integrators: rkc, rkl (LSRKStep STS, fused kernels for the Dirichlet problems) and dirk
 // (fixed-step SDIRK2 with the fused Jacobi-PCG, Dirichlet problems, --fixedstep required).
 #include <algorithm>
@@ -182,7 +182,7 @@ int main(int argc, char** argv)
   const bool impl = (o.integrator == "dirk");
   if (!sts && !impl)
   {
-    cerr << "ERROR: illegal integrator (this build provides rkc, rkl and dirk)" << endl;
+    cerr << "ERROR: illegal integrator (this program provides rkc, rkl and dirk)" << endl;
     return 1;
   }
   if (impl && (kind == STS_PROBLEM_PERIODIC || !(o.hfixed > 0.0)))

@@ -49,7 +49,7 @@ def test_cli_manufactured_rkc_with_error_mode(stslib, oracle, controller):
     P = oracle.Problem(oracle.MANUFACTURED, 64, 48)
     J = oracle.Integrator(P, P.initial(), method=oracle.RKC, rtol=1e-6, atol=1e-10,
                           controller=controller)
-    # output times accumulate like the driver's (main.cpp: tout += dTout, capped at tf)
+    # output times accumulate like the reference program's (main.cpp: tout += dTout, capped at tf)
     dt, tout = 0.05 / 5, 0.05 / 5
     for k in range(5):
         assert J.evolve(tout) == 0
