@@ -120,6 +120,20 @@ __device__ double d_controller(int controller, double h, double dsm, double ep1,
   return h * stsm::pow(e1, -1.0 / B_ORD);
 }
 
+// The controller evaluated by one thread of the CTA and broadcast through shared memory: every
+// thread holds the same inputs, so the value is the one each thread would compute (and every
+// CTA of a cluster computes it from the same reduced values), without 256-512 redundant
+// evaluations of the FP64 pow series per step. Called by all threads of the CTA.
+__device__ __forceinline__ double block_control(int controller, double h, double dsm, double ep1, double ep2,
+                                                double hp, long long nhist, double* shn)
+{
+  if (threadIdx.x == 0) *shn = d_controller(controller, h, dsm, ep1, ep2, hp, nhist);
+  __syncthreads();
+  const double v = *shn;
+  __syncthreads(); // read by every thread before the next proposal overwrites it
+  return v;
+}
+
 __device__ int d_stages(int method, double h, double rho, int smax, double* hmax)
 {
   double ss;
@@ -237,6 +251,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
   __shared__ long long climb[xsum::NL];
   __shared__ unsigned sflags;
   __shared__ double sres;
+  __shared__ double shn; // step-size proposal of the controller, computed by one thread
   __shared__ int sidx;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = NT / 32;
@@ -546,7 +561,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
           iFn          = tf_;
           const double hprev = hlast;
           hlast        = h;
-          double hn    = d_controller(prm.controller, h, dsm, ep1, ep2, hprev, nhist);
+          double hn    = block_control(prm.controller, h, dsm, ep1, ep2, hprev, nhist, &shn);
           double eta   = B_SAFETY * hn / h;
           const double emx = (nst == 0) ? B_ETAMX1 : (after_fail ? 1.0 : B_GROWTH);
           if (eta > emx) eta = emx;
@@ -566,7 +581,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
           status = -3;
           break;
         }
-        double hn  = d_controller(prm.controller, h, dsm, ep1, ep2, hlast, nhist);
+        double hn  = block_control(prm.controller, h, dsm, ep1, ep2, hlast, nhist, &shn);
         double eta = B_SAFETY * hn / h;
         if (eta > 1.0) eta = 1.0;
         if (nef >= 2 && eta > B_ETAMXF) eta = B_ETAMXF;
