@@ -415,8 +415,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
           {
             const double mu = ct[jst].mu, nu = ct[jst].nu, mus = ct[jst].mus, ajm1 = ct[jst].ajm1;
             const double hm = h * mus;
-            const double tm = hm * cc;
-            const float gc = (float)(mu + tm), gx = (float)(hm * cx), gy = (float)(hm * cy), gn = (float)nu;
+            const float gs = (float)(((mu + nu) - 1.0) + hm * ((cc + 2.0 * cx) + 2.0 * cy));
+            const float gx = (float)(hm * cx), gy = (float)(hm * cy), gm = (float)(-nu);
             const float gF   = (float)(hm * (1.0 - ajm1));
             const float* dm1 = D[lastd];
             const float* ff  = Ff[iff];
@@ -430,13 +430,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
                 const float de = (i < n - 1) ? dm1[k + 1] : 0.0f;
                 const float ds = (j > 0) ? ldrowf(&dm1[k - n], j - 1 < j0) : 0.0f;
                 const float dn = (j < n - 1) ? ldrowf(&dm1[k + n], j + 1 >= j1) : 0.0f;
-                const float sx = dw + de, sy = ds + dn;
-                float acc      = gc * dm1[k];
-                acc            = __fmaf_rn(gx, sx, acc);
-                acc            = __fmaf_rn(gy, sy, acc);
-                if (dm2) acc = __fmaf_rn(gn, dm2[k], acc);
-                acc   = __fmaf_rn(gF, ff[k], acc);
-                dj[k] = acc;
+                const float m2 = dm2 ? dm2[k] : 0.0f;
+                dj[k] = mixed_point<false>(gs, gx, gy, gm, gF, dm1[k], dw, de, ds, dn, m2, ff[k], 0.f, 0.f, 0.f,
+                                           0.f);
               }
             inst_sync<CL>();
             dm2   = dm1;

@@ -598,10 +598,10 @@ static void autotune_stage32(LSRKMem* m, STS_Problem p)
   // stage coefficients of a mid stage of a 100-stage RKL2 step (any finite values time alike)
   memset(m->h_par, 0, m->par_bytes);
   StageArgs* a = hstage(m) + 2;
-  a->gcf = 0.5f;
+  a->gsf = 0.01f;
   a->gxf = 0.2f;
   a->gyf = 0.05f;
-  a->gnf = -0.9f;
+  a->gmf = 0.9f;
   a->gFf = 1e-5f;
   cudaMemcpyAsync(m->d_par, m->h_par, m->par_bytes, cudaMemcpyHostToDevice, st);
   // scratch only: the stage buffers and the FP32 F of the other parity (the current one may
@@ -799,10 +799,10 @@ static void fill_params(LSRKMem* m, STS_Problem p, double t, double h, int s, co
     a.al            = hm * cd;
     a.be            = -(hm * c) * p->kx;
     a.ga            = -(hm * c) * p->ky;
-    a.gcf           = (float)a.gc;
+    a.gsf           = (float)(((mu[j] + nu[j]) - 1.0) + hm * ((p->cc + 2.0 * p->cx) + 2.0 * p->cy));
     a.gxf           = (float)a.gx;
     a.gyf           = (float)a.gy;
-    a.gnf           = (float)a.gn;
+    a.gmf           = (float)(-nu[j]);
     a.gFf           = (float)(hm * (1.0 - ajm1[j]));
     const double dc  = c - c0;
     const double dcd = cd - cd0;

@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256, K::MINB)
       if (t < ntiles) issue_tile<K, HAS_M2>(smem + k * K::SLOT_BYTES, &bar[k], &mh, &mm2, &mf0, t, tiles_x);
     }
 
-  const float gc = A->gcf, gx = A->gxf, gy = A->gyf, gn = A->gnf, gF = A->gFf;
+  const float gs = A->gsf, gx = A->gxf, gy = A->gyf, gm = A->gmf, gF = A->gFf;
   const float al = A->alf, be = A->bef, ga = A->gaf;
   bool failed = false;
   int k       = 0;
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(256, K::MINB)
     const int x0 = (t % tiles_x) * TW, y0 = (t / tiles_x) * K::TH;
     const int x  = x0 + lane * 4;
     const int c  = 4 + lane * 4; // column of x in the halo tile
-    float Pi[4], Qi[4];
+    float Pi[4] = {0.f, 0.f, 0.f, 0.f}, Qi[4] = {0.f, 0.f, 0.f, 0.f};
     if (FORCED)
     {
 #pragma unroll
@@ -197,18 +197,8 @@ __global__ void __launch_bounds__(256, K::MINB)
       {
         const float uw = (v == 0) ? w : cv[v - 1];
         const float ue = (v == 3) ? e : cv[v + 1];
-        const float sx = uw + ue, sy = uv[v] + dv[v];
-        float acc      = gc * cv[v];
-        acc            = __fmaf_rn(gx, sx, acc);
-        acc            = __fmaf_rn(gy, sy, acc);
-        if (HAS_M2) acc = __fmaf_rn(gn, mv[v], acc);
-        acc = __fmaf_rn(gF, qv[v], acc);
-        if (FORCED)
-        {
-          acc = __fmaf_rn(syj, Pi[v], acc);
-          acc = __fmaf_rn(syyj, Qi[v], acc);
-        }
-        o[v] = acc;
+        o[v] = mixed_point<FORCED>(gs, gx, gy, gm, gF, cv[v], uw, ue, uv[v], dv[v], mv[v], qv[v], syj, Pi[v], syyj,
+                                   Qi[v]);
       }
       if (y < ny && x < nx && STS_IN_BOUNDS(x + 4 <= nx, err))
         *reinterpret_cast<float4*>(out + (long long)y * nx + x) = make_float4(o[0], o[1], o[2], o[3]);

@@ -772,7 +772,8 @@ void orc_state_free(orc_state* st)
 /* ---- stage arithmetic (mirrors the CUDA stage kernels) ---- */
 typedef struct {
   double gc, gx, gy, gn, g0, gf, al, be, ga;
-  float gcf, gxf, gyf, gnf, gFf, alf, bef, gaf;
+  /* mixed (difference) form: gsf = mu + nu - 1 + hm (cc + 2 cx + 2 cy), gmf = -nu */
+  float gsf, gxf, gyf, gmf, gFf, alf, bef, gaf;
 } stage_c;
 
 static void stage_coeffs_j(const orc_prob* p, double t, double h, const double* mu, const double* nu,
@@ -790,10 +791,10 @@ static void stage_coeffs_j(const orc_prob* p, double t, double h, const double* 
   c->gf     = -(hm * ajm1[j]);
   forcing_scalars(p, hm, tj, &c->al, &c->be, &c->ga);
   /* mixed (increment) form */
-  c->gcf    = (float)c->gc;
+  c->gsf    = (float)(((mu[j] + nu[j]) - 1.0) + hm * ((p->cc + 2.0 * p->cx) + 2.0 * p->cy));
   c->gxf    = (float)c->gx;
   c->gyf    = (float)c->gy;
-  c->gnf    = (float)c->gn;
+  c->gmf    = (float)(-nu[j]);
   c->gFf    = (float)(hm * (1.0 - ajm1[j]));
   double dc  = orc_c(tj) - orc_c(t);
   double dcd = orc_cdot(tj) - orc_cdot(t);
@@ -834,6 +835,10 @@ static void stage64(const orc_prob* p, const stage_c* c, const double* ym1, cons
     }
 }
 
+/* Mixed stage in difference form: d_j = d_C + inc, where every FP32 operation of inc rounds a
+ * quantity of the size of the stage-to-stage increment (neighbour differences, d_C - d_{j-2},
+ * the F_0 and forcing terms) and d_C + inc is the only rounding at the scale of d. This is the
+ * product's FP32 arithmetic operation for operation (mixed_point in the CUDA stage kernels). */
 static void stage32(const orc_prob* p, const stage_c* c, const float* dm1, const float* dm2,
                     const float* f0f, const float* Sxf, const float* Sxxf, const float* Syf,
                     const float* Syyf, float* dj)
@@ -845,24 +850,26 @@ static void stage32(const orc_prob* p, const stage_c* c, const float* dm1, const
     for (long i = 0; i < nx; ++i)
     {
       long k    = j * nx + i;
+      float dc  = dm1[k];
       float dw  = (i > 0) ? dm1[k - 1] : 0.0f;
       float de  = (i < nx - 1) ? dm1[k + 1] : 0.0f;
       float ds  = (j > 0) ? dm1[k - nx] : 0.0f;
       float dn  = (j < ny - 1) ? dm1[k + nx] : 0.0f;
-      float sx  = dw + de, sy = ds + dn;
-      float acc = c->gcf * dm1[k];
-      acc       = fmaf(c->gxf, sx, acc);
-      acc       = fmaf(c->gyf, sy, acc);
-      if (dm2) acc = fmaf(c->gnf, dm2[k], acc);
-      acc = fmaf(c->gFf, f0f[k], acc);
+      float m2  = dm2 ? dm2[k] : 0.0f;
+      float lx  = (dw - dc) + (de - dc), ly = (ds - dc) + (dn - dc);
+      float inc = c->gsf * dc;
+      inc       = fmaf(c->gxf, lx, inc);
+      inc       = fmaf(c->gyf, ly, inc);
+      inc       = fmaf(c->gmf, dc - m2, inc);
+      inc       = fmaf(c->gFf, f0f[k], inc);
       if (forced)
       {
         float P = fmaf(c->alf, Sxf[i], c->bef * Sxxf[i]);
         float Q = c->gaf * Sxf[i];
-        acc     = fmaf(Syf[j], P, acc);
-        acc     = fmaf(Syyf[j], Q, acc);
+        inc     = fmaf(Syf[j], P, inc);
+        inc     = fmaf(Syyf[j], Q, inc);
       }
-      dj[k] = acc;
+      dj[k] = dc + inc;
     }
 }
 

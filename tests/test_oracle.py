@@ -265,6 +265,25 @@ def test_mixed_matches_fp64_for_equal_steps(oracle):
     assert rel < 1e-6
 
 
+def test_mixed_difference_form_long_stage_chains(oracle):
+    """The oracle's FP32-increment arithmetic on long stage chains (256^2, kx = 1,
+    ky = 1e-2, fixed RKL2 steps of about 60 stages to t = 0.2): the difference form ends
+    about 8e-8 from FP64, where summing the O(|d|) terms directly ended 1.2e-6."""
+    P = oracle.Problem(oracle.MANUFACTURED, 256, kx=1.0, ky=0.01)
+    rho = 1.01 * abs(P.dom_eig())
+    s, tf = 60, 0.2
+    h = (s * s + s - 2.0) / (2.0 * rho) * 0.999
+    h = tf / math.ceil(tf / h)
+    out = {}
+    for mixed in (False, True):
+        I = oracle.Integrator(P, P.initial(), method=oracle.RKL, mixed=mixed, hfixed=h)
+        assert I.evolve(tf) == 0
+        assert I.stats()["stage_max"] > 50
+        out[mixed] = I.y
+    rel = np.linalg.norm(out[True] - out[False]) / np.linalg.norm(out[False])
+    assert rel < 3e-7, rel
+
+
 def test_oracle_reproduces_golden_runs(oracle):
     """Pins the oracle's integrator across machines (libm may differ by an ulp)."""
     for name in ("oracle_rkc_17x9", "oracle_rkl_32", "oracle_rkl_mixed_32"):
