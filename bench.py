@@ -10,11 +10,13 @@ A "step" is one adaptive LSRK time step (s fused stencil+stage kernels, the fuse
 kernel and the host step control). value = DOF-stages/s of the mixed path (FP32 stage
 increments, FP64 step update) with the state resident in HBM; e2e = the same metric through
 the C-ABI with the state copied in from pinned host memory and back out every step;
-"fp64" gives the plain FP64 GPU path on the same step sequence. Each FP32 stage buffer is
+"fp64" gives the plain FP64 GPU path replaying the mixed arm's step sequence, so both end at
+the same t and "accuracy" compares their fields. Each FP32 stage buffer is
 256 MiB (> 129 MB L2), so no L2 flush is needed between steps.
 
 --impl reference times the CPU restatement of the reference algorithm (the oracle, FP64,
-all host threads) on the same problem: each step is one fixed-step RKL2 step of 20 stages.
+all host threads) on the same workload: the same adaptive RKL2 run from t = 0, the same
+warm-up and timed step counts.
 --full runs the whole t in [0, 0.05] solve for both precisions (time-to-solution).
 """
 import argparse
@@ -134,18 +136,18 @@ def cuda_timer(stream_ptr):
     return T
 
 
-def traffic_from_profiles():
-    """Per-launch DRAM bytes of the mixed stage kernel at 8192^2 from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "stage_kernels_ncu.md")
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.startswith("traffic_bytes_per_launch_mixed_8192:"):
-            try:
-                return float(line.split(":")[1].split()[0])
-            except ValueError:
-                return None
-    return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the mixed stage
+# kernel, from one ncu capture of a smaller case of the same kernel, scaled to 8192^2 by the
+# DOF count (the kernel streams each input once, so its traffic grows with the DOF count):
+#   python bench.py --n 6144 --steps 1 --warmup 3 --no-cpu --stage-kernel 6
+#   ncu --set full --clock-control none -k regex:stage32_tma -s 20 -c 2 -o prof_tma \
+#       python bench.py --n 6144 --steps 1 --warmup 3 --no-cpu --stage-kernel 6
+# 6144^2: 578.1 MB per launch -> x (8192/6144)^2 = 1028 MB.
+TRAFFIC_MIXED_STAGE_6144 = 578.1e6
+
+
+def mixed_stage_traffic(n):
+    return TRAFFIC_MIXED_STAGE_6144 * (n / 6144.0) ** 2
 
 
 def run_gpu(args):
@@ -179,21 +181,32 @@ def run_gpu(args):
 
     res = {}
     clock_samples = []
+    hseq = []  # accepted step sizes of the mixed arm, replayed by the FP64 arm
+    L = sts.lib()
     for mixed in (True, False):
         I = sts.LSRKStep(ctx, G, 0.0, G.initial(), method=METHOD, rtol=RTOL, atol=ATOL,
                          smax=SMAX, mixed=mixed, graphs=True, maxsteps=1000000,
                          stage_kernel=args.stage_kernel if mixed else 0)
         y = G.vector()
-        for _ in range(args.warmup):
+
+        def one_step(k):
+            # the FP64 arm takes the mixed arm's step sequence (ARKodeSetFixedStep before each
+            # step), so that both end at the same t and their fields can be compared
+            if not mixed:
+                L.STS_ARKodeSetFixedStep(I.mem, hseq[k])
             I.evolve(TF, y, sts.ONE_STEP)
+            if mixed:
+                hseq.append(I.stats()["hlast"])
+        for k in range(args.warmup):
+            one_step(k)
         ctx.synchronize()
         barrier()
         s0 = I.stats()
         clocks = Clocks(local)
         clocks.start()
         with timer() as tm:
-            for _ in range(args.steps):
-                I.evolve(TF, y, sts.ONE_STEP)
+            for k in range(args.warmup, args.warmup + args.steps):
+                one_step(k)
         clock_samples.append(clocks.stop())
         s1 = I.stats()
         ms = max_over_ranks(tm.ms)
@@ -213,7 +226,6 @@ def run_gpu(args):
     host = [torch.empty(N2, dtype=torch.float64, pin_memory=True) for _ in range(2)]
     host[0].numpy()[:] = res[True]["y"]
     yv = G.vector()
-    L = sts.lib()
     hp = [C.cast(h.data_ptr(), sts._dp) for h in host]
     t_cur = res[True]["t"]
     k = 0
@@ -234,7 +246,8 @@ def run_gpu(args):
             k = 1 - k
     s1 = I.stats()
     e2e_ms = max_over_ranks(tm.ms)
-    e2e_dof = N2 * (s1["nfe"] - s0["nfe"])
+    # ARKodeReset evaluates F(t, y) once per step: work of the restart, not of the step
+    e2e_dof = N2 * (s1["nfe"] - s0["nfe"] - args.steps)
     # the host link alone (copy engine, pinned buffers, same calls): the part of the e2e step
     # that the data dependence between steps keeps from overlapping the device work
     with timer() as th:
@@ -252,8 +265,9 @@ def run_gpu(args):
         yv_ = res[mixed]["y"]
         out[mixed] = float(np.linalg.norm(yv_ - ex) / np.linalg.norm(ex))
     same_t = res[True]["t"] == res[False]["t"]
-    mix_vs_64 = float(np.linalg.norm(res[True]["y"] - res[False]["y"]) /
-                      np.linalg.norm(res[False]["y"])) if same_t else None
+    if not same_t:
+        raise RuntimeError("the FP64 replay of the mixed step sequence ended at another t")
+    mix_vs_64 = float(np.linalg.norm(res[True]["y"] - res[False]["y"]) / np.linalg.norm(res[False]["y"]))
 
     if rank != 0:
         return
@@ -264,7 +278,7 @@ def run_gpu(args):
     stage_bytes_mixed = 16.0 * N2
     stage_bytes_fp64 = 40.0 * N2
     ach = stage_bytes_mixed / (m["stage_ms"] / 1e3) / 1e9
-    traffic = traffic_from_profiles()
+    traffic = mixed_stage_traffic(n)
     fp64_flops = 17.0 * N2 / (d["stage_ms"] / 1e3)
     line = {
         "metric": "STS DOF-stages/s & solve time at 8192^2: mixed vs FP64 GPU at 1e-6 rel L2 err",
@@ -319,27 +333,35 @@ def cpu_step_setup(n, stages):
     return po, P, I, h
 
 
-def cpu_baseline(args, stages=20):
+def cpu_baseline(args, stages=196, nsteps=2):
+    """A bounded sample of the workload on the CPU oracle: `nsteps` fixed RKL2 steps of
+    `stages` stages (the stage count of the timed GPU steps) after one untimed step."""
     po, P, I, h = cpu_step_setup(args.n, stages)
     I.evolve(TF)  # initialisation + first step (untimed)
     s0 = I.stats()
     t0 = time.perf_counter()
-    I.evolve(TF)
+    for _ in range(nsteps):
+        I.evolve(TF)
     dt = time.perf_counter() - t0
     s1 = I.stats()
     dof = args.n * args.n * (s1["nfe"] - s0["nfe"])
     return {"value": dof / dt, "unit": "DOF-stages/s", "cores": po.lib().orc_nthreads(),
             "kind": "port",
-            "sample": "one fixed-step RKL2 step (%d stages) of the %d^2 FP64 problem on the CPU oracle"
-                      % (s1["nfe"] - s0["nfe"], args.n)}
+            "sample": "%d fixed-step RKL2 steps (%d RHS evaluations) of the %d^2 FP64 problem on the "
+                      "CPU oracle" % (nsteps, s1["nfe"] - s0["nfe"], args.n)}
 
 
 def run_reference(args):
+    """The reference algorithm on the host cores (the CPU oracle, FP64, all threads) on the
+    same workload as the GPU arm: adaptive RKL2 from t = 0 (rtol 1e-6, atol 1e-10, at most
+    200 stages), `warmup` untimed steps, then `steps` timed steps."""
     ws, rank, local = dist_info()
     if rank != 0:
         return
-    po, P, I, h = cpu_step_setup(args.n, 20)
-    I.evolve(TF)
+    from oracle import pyoracle as po
+    n = args.n
+    P = po.Problem(po.MANUFACTURED, n, n, kx=KX, ky=KY)
+    I = po.Integrator(P, P.initial(), method=po.RKL, rtol=RTOL, atol=ATOL, smax=SMAX, maxsteps=1)
     for _ in range(args.warmup):
         I.evolve(TF)
     s0 = I.stats()
@@ -348,18 +370,21 @@ def run_reference(args):
         I.evolve(TF)
     dt = time.perf_counter() - t0
     s1 = I.stats()
-    dof = args.n * args.n * (s1["nfe"] - s0["nfe"])
+    dof = n * n * (s1["nfe"] - s0["nfe"])
     v = dof / dt
-    sample = ("fixed-step RKL2 steps of 20 stages on the %d^2 FP64 problem; CPU restatement of the "
-              "reference algorithm (SUNDIALS is not vendored in the reference, so the reference "
-              "binary cannot be built)" % args.n)
+    sample = ("%d adaptive RKL2 steps (after %d untimed) of the %d^2 FP64 problem, %d RHS evaluations; "
+              "CPU restatement of the reference algorithm (SUNDIALS is not vendored in the reference, "
+              "so the reference binary cannot be built)" % (args.steps, args.warmup, n,
+                                                            s1["nfe"] - s0["nfe"]))
     line = {
         "metric": "STS DOF-stages/s & solve time at 8192^2: mixed vs FP64 GPU at 1e-6 rel L2 err",
         "value": v, "unit": "DOF-stages/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "manufactured 2-D heat %dx%d, kx=1 ky=1e-2, RKL2" % (args.n, args.n),
-                   "nx": args.n, "ny": args.n, "method": "RKL2"},
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (manufactured-solution initial state)",
+        "config": {"workload": "manufactured 2-D heat %dx%d, kx=1 ky=1e-2, RKL2 adaptive, rtol=1e-6 "
+                               "atol=1e-10, smax=200, t in [0,0.05]" % (n, n),
+                   "nx": n, "ny": n, "method": "RKL2", "stages_per_step": s1["stage_max"],
+                   "t_end_of_timed_steps": s1["t"]},
         "impl": "reference",
         "cpu_baseline": {"value": v, "unit": "DOF-stages/s", "cores": po.lib().orc_nthreads(),
                          "kind": "port", "sample": sample},
