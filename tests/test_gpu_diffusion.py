@@ -82,3 +82,34 @@ def test_bad_arguments_fail_loudly(ctx, stslib):
     wrong = stslib.NVector(ctx, 10)
     assert G.rhs(0.0, wrong, wrong) == -1
     assert b"length" in L.STS_GetLastError()
+
+
+def test_periodic_problem_against_the_reference_code(ctx, stslib):
+    """The GPU RHS, initial state and Jacobi PSolve of the reference's periodic problem
+    against outputs of the reference's own sources (oracle/_ref, fixture
+    tests/golden/reference_periodic.npz, made by tests/golden/make_reference_goldens.py).
+    Bit for bit where the host libm rounds sin / exp like the machine that made the
+    fixture; otherwise within a few ulp of the terms' scale."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "reference_periodic.npz"))
+    nx, ny, kx, ky = int(g["nx"]), int(g["ny"]), float(g["kx"]), float(g["ky"])
+    u = g["u"]
+    U = stslib.NVector.from_numpy(ctx, u)
+
+    def close(a, b, scale):
+        return np.array_equal(a, b) or np.max(np.abs(a - b)) <= 8e-16 * scale
+
+    H = stslib.Problem(ctx, kind=2, nx=nx, ny=ny, kx=kx, ky=ky, inhomogeneous=False)
+    I = stslib.Problem(ctx, kind=2, nx=nx, ny=ny, kx=kx, ky=ky, inhomogeneous=True)
+    assert close(H.initial().numpy(), g["ic"], np.max(np.abs(g["ic"])))
+    F = H.vector()
+    assert H.rhs(float(g["t"]), U, F) == 0
+    assert np.array_equal(F.numpy(), g["f_hom"])  # constant coefficients: no libm involved
+    assert I.rhs(float(g["t"]), U, F) == 0
+    dx = (2 * np.pi) / (nx - 1)
+    assert close(F.numpy(), g["f_inh"], 4 * 1.99 * max(kx, ky) / (dx * dx) * np.max(np.abs(u)))
+    Z = H.vector()
+    gamma = float(g["gamma"])
+    assert H.psetup(gamma) == 0 and H.psolve(U, Z, gamma) == 0
+    assert np.array_equal(Z.numpy(), g["z_hom"])
