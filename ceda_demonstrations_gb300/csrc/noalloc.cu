@@ -10,12 +10,18 @@
 // result to a device location the caller provides.
 //
 // The scratch array is small (one accumulator block: ten 64-bit limbs, a word, flags and a
-// ticket, 96 bytes) and lives for as long as the library is loaded, on every device that
-// loads it. Host code cannot use the array's name as a device address, so the first call
-// on each device, with that device current, looks the address up with cudaGetSymbolAddress
-// and caches it; make that first call outside any stream capture. Every call on a device
-// shares the one array: the call clears it with cudaMemsetAsync before its kernel, and
-// calls whose kernels overlap on the GPU (different streams, no ordering) race on it.
+// ticket, 96 bytes) and lives for as long as the library is loaded, in every CUDA context
+// that loads it. Host code cannot use the array's name as a device address: each call looks
+// the address up with cudaGetSymbolAddress in the context current on the calling thread
+// (the lookup allocates nothing). A stream being captured into a CUDA graph may not trigger
+// that lookup (it can load the module), so a call on a capturing stream uses the address
+// found by an earlier call in the same context and fails with a clear error if there was
+// none: make the first call in each context outside any stream capture. The cache is keyed by
+// the context, not the device number, so a driver-API context made current on the same device
+// or the new primary context after cudaDeviceReset gets its own lookup. Every call in a context
+// shares the one array: the call clears it with cudaMemsetAsync before its kernel, and calls
+// whose kernels overlap on the GPU (different streams, no ordering) race on it.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -25,35 +31,81 @@
 
 static constexpr int NOALLOC_MAX_DEVICES = 64;
 
-// The shared scratch: one exact-accumulator block per device (zero at module load).
+// The shared scratch: one exact-accumulator block per context (zero at module load).
 static __device__ __align__(256) RedWork g_noalloc_scratch[1];
 
-static RedWork* g_scratch_addr[NOALLOC_MAX_DEVICES] = {};
-static int g_num_sms[NOALLOC_MAX_DEVICES]           = {};
-static std::mutex g_setup_mu;
+// Address of the scratch and the SM count, per device, for the context they were found in.
+// Written and read under g_mu (an uncontended lock per call, next to a kernel launch).
+struct ScratchSlot {
+  CUcontext ctx = nullptr;
+  RedWork* addr = nullptr;
+  int sms       = 0;
+};
+static ScratchSlot g_slot[NOALLOC_MAX_DEVICES];
+static std::mutex g_mu;
 
-// once per device, with that device current
-static int noalloc_setup(int dev)
+// cuCtxGetCurrent through the runtime's driver entry point (the library links no libcuda)
+static CUresult (*g_ctx_get_current)(CUcontext*) = nullptr;
+static std::once_flag g_ctx_fn_once;
+
+static bool current_context(CUcontext* out)
 {
-  std::lock_guard<std::mutex> lk(g_setup_mu);
-  if (g_scratch_addr[dev]) return 0;
-  void* p       = nullptr;
-  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-  if (e != cudaSuccess || !p)
+  std::call_once(g_ctx_fn_once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_get_current = reinterpret_cast<CUresult (*)(CUcontext*)>(fn);
+  });
+  *out = nullptr;
+  return g_ctx_get_current && g_ctx_get_current(out) == CUDA_SUCCESS && *out;
+}
+
+// the scratch address and SM count for the current context of device `dev`
+static int noalloc_scratch(int dev, bool capturing, RedWork** addr, int* sms)
+{
+  CUcontext cur = nullptr;
+  if (!current_context(&cur))
   {
-    sts_set_error("STS_WrmsNormNoAlloc: cudaGetSymbolAddress failed on device %d: %s", dev,
-                  cudaGetErrorString(e));
+    sts_set_error("STS_WrmsNormNoAlloc: no current CUDA context on device %d", dev);
     return -1;
   }
-  int sms = 0;
-  e       = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess || sms < 1)
+  std::lock_guard<std::mutex> lk(g_mu);
+  ScratchSlot& sl = g_slot[dev];
+  if (capturing)
   {
-    sts_set_error("STS_WrmsNormNoAlloc: cannot query device %d: %s", dev, cudaGetErrorString(e));
-    return -1;
+    if (sl.ctx != cur || !sl.addr)
+    {
+      sts_set_error("STS_WrmsNormNoAlloc: first call in this CUDA context made during stream capture; "
+                    "make one call outside capture first");
+      return -1;
+    }
   }
-  g_num_sms[dev]      = sms;
-  g_scratch_addr[dev] = (RedWork*)p;
+  else
+  {
+    void* p       = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+    {
+      sts_set_error("STS_WrmsNormNoAlloc: cudaGetSymbolAddress failed on device %d: %s", dev, cudaGetErrorString(e));
+      return -1;
+    }
+    if (sl.ctx != cur || sl.sms < 1)
+    {
+      int n = 0;
+      e     = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess || n < 1)
+      {
+        sts_set_error("STS_WrmsNormNoAlloc: cannot query device %d: %s", dev, cudaGetErrorString(e));
+        return -1;
+      }
+      sl.sms = n;
+    }
+    sl.ctx  = cur;
+    sl.addr = (RedWork*)p;
+  }
+  *addr = sl.addr;
+  *sms  = sl.sms;
   return 0;
 }
 
@@ -78,17 +130,25 @@ extern "C" int STS_WrmsNormNoAlloc(const double* x, const double* w, sts_index n
     sts_set_error("STS_WrmsNormNoAlloc: no usable current device");
     return -1;
   }
-  if (!g_scratch_addr[dev] && noalloc_setup(dev)) return -1;
   cudaStream_t s = (cudaStream_t)stream;
-  RedWork* work  = g_scratch_addr[dev];
-  e              = cudaMemsetAsync(work, 0, sizeof(RedWork), s);
+  cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(s, &cap_status);
+  if (e != cudaSuccess)
+  {
+    sts_set_error("STS_WrmsNormNoAlloc: invalid stream: %s", cudaGetErrorString(e));
+    return -1;
+  }
+  RedWork* work = nullptr;
+  int sms       = 0;
+  if (noalloc_scratch(dev, cap_status != cudaStreamCaptureStatusNone, &work, &sms)) return -1;
+  e = cudaMemsetAsync(work, 0, sizeof(RedWork), s);
   if (e != cudaSuccess)
   {
     sts_set_error("STS_WrmsNormNoAlloc: clearing the scratch failed: %s", cudaGetErrorString(e));
     return -1;
   }
   long long blocks = (n + 256 * 4 - 1) / (256 * 4);
-  long long cap    = (long long)g_num_sms[dev] * 8;
+  long long cap    = (long long)sms * 8;
   if (blocks > cap) blocks = cap;
   xred_kernel<1><<<(unsigned)blocks, 256, 0, s>>>(n, x, w, work, result);
   e = cudaGetLastError();

@@ -128,9 +128,12 @@ int N_VDotProdMulti_Sts(int nvec, N_Vector x, N_Vector* Y, double* dots);
  * N_VWrmsNorm_Sts: sqrt(sum_i (x_i w_i)^2 / n) over device arrays x, w of length n, written
  * to the device location `result`, asynchronously on `stream` (a cudaStream_t, NULL = the
  * default stream). It calls no cudaMalloc/cudaFree: its scratch is one fixed 96-byte block
- * per device in a static device array held until the library is unloaded. The first call
- * on each device looks up that block (cudaGetSymbolAddress) and must come before any stream
- * capture. Each call clears the block first; calls that overlap on the GPU race on it.
+ * per CUDA context in a static device array held until the library is unloaded. A call on
+ * a stream that is not being captured looks that block up (cudaGetSymbolAddress, in the
+ * context current on the calling thread); a call on a capturing stream reuses the address
+ * found by an earlier call in the same context, so the first call in each context (also the
+ * new context after a cudaDeviceReset) must come before any stream capture. Each call clears
+ * the block first; calls that overlap on the GPU race on it.
  * n must lie in [1, STS_NOALLOC_MAX_N]; otherwise -1 and STS_GetLastError() says why. */
 #define STS_NOALLOC_MAX_N 2147483647LL
 int STS_WrmsNormNoAlloc(const double* x, const double* w, sts_index n, double* result,

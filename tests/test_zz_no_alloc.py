@@ -35,3 +35,51 @@ def test_no_alloc_rejects_bad_sizes(ctx, stslib):
     assert b"outside" in L.STS_GetLastError()
     assert L.STS_WrmsNormNoAlloc(X.ptr, X.ptr, 2 ** 31, X.ptr, ctx.stream) == -1
     assert b"outside" in L.STS_GetLastError()
+
+
+CHILD = r'''
+import ctypes, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import ceda_demonstrations_gb300 as sts
+L = sts.lib()
+
+def once(seed):
+    ctx = sts.Context(0)
+    rng = np.random.default_rng(seed)
+    n = 300_007
+    X = sts.NVector.from_numpy(ctx, rng.standard_normal(n))
+    W = sts.NVector.from_numpy(ctx, np.abs(rng.standard_normal(n)) + 0.5)
+    out = sts.NVector(ctx, 1)
+    want = X.wrms_norm(W)
+    assert L.STS_WrmsNormNoAlloc(X.ptr, W.ptr, n, out.ptr, ctx.stream) == 0, L.STS_GetLastError()
+    ctx.synchronize()
+    got = out.numpy()[0]
+    for v in (X, W, out):
+        v.destroy()
+    ctx.free()
+    return got == want
+
+assert once(1)
+cudart = None
+for line in open("/proc/self/maps"):
+    if "libcudart.so" in line:
+        cudart = ctypes.CDLL(line.split()[-1])
+        break
+assert cudart is not None
+assert cudart.cudaDeviceReset() == 0  # ends this process's context; the next call makes a new one
+assert once(2)
+print("ok")
+'''
+
+
+def test_no_alloc_after_device_reset(ctx, stslib):
+    """A new CUDA context on the same device (here the primary context that follows
+    cudaDeviceReset, in a child process so the session's context is untouched) gets its own
+    lookup of the scratch address: the entry point still matches the context path."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", CHILD, root], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
