@@ -66,8 +66,25 @@ class Stats(C.Structure):
                 ("hnext", C.c_double), ("spectral_radius", C.c_double)]
 
 
+class ARKStepStats(C.Structure):
+    _fields_ = [(k, _ll) for k in ("nst", "nst_attempts", "netf", "ncfn", "nfe", "nfi", "nfe_ls", "nni", "nnf",
+                                   "nli", "nlcf", "npe", "nps", "njv", "nsetups")] + \
+               [(k, C.c_double) for k in ("t", "h0", "hlast", "hnext")]
+
+
 # (name, restype, argtypes) for every entry point of include/stsgpu.h
 SIGNATURES = [
+    ("STS_ARKStepCreate", _vp, [_vp, _vp, C.c_double, _NV, _vp]),
+    ("STS_ARKodeSetOrder", C.c_int, [_vp, C.c_int]),
+    ("STS_ARKodeSetLinearSolver", C.c_int, [_vp, _vp, _vp]),
+    ("STS_ARKodeSetPreconditioner", C.c_int, [_vp, _vp, _vp]),
+    ("STS_ARKStepSetPrecData", C.c_int, [_vp, _vp]),
+    ("STS_ARKodeSetLSetupFrequency", C.c_int, [_vp, C.c_int]),
+    ("STS_ARKodeSetEpsLin", C.c_int, [_vp, C.c_double]),
+    ("STS_ARKodeSetLinear", C.c_int, [_vp, C.c_int]),
+    ("STS_ARKodeSetNonlinear", C.c_int, [_vp]),
+    ("STS_ARKStepGetStats", C.c_int, [_vp, C.POINTER(ARKStepStats)]),
+    ("STS_ARKStepTable", C.c_int, [C.c_int, C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, _dp]),
     ("STS_ContextCreate", C.c_int, [C.c_int, C.POINTER(_vp)]),
     ("STS_ContextFree", C.c_int, [C.POINTER(_vp)]),
     ("STS_ContextSynchronize", C.c_int, [_vp]),
@@ -624,6 +641,103 @@ class LSRKStep:
             self.free()
         except Exception:
             pass
+
+
+class ARKStep:
+    """ARKStepCreate + ARKode* configuration (diffusion_2D/main.cpp:239-330): implicit DIRK
+    (``implicit=True``, order 2 or 3) with a Newton iteration whose linear systems go to a
+    generic solver (``ls`` "cg" or "gmres", ``maxl`` iterations) preconditioned by nothing
+    (``prec=None``), the Jacobi PSetup/PSolve ("jacobi") or a :class:`PFMG` ("pfmg", with
+    ``pfmg``); or explicit ERK (order 2, 3 or 4). ``problem`` is a :class:`Problem` (its
+    STS_Diffusion RHS)."""
+
+    def __init__(self, ctx, problem, t0, y0, implicit=True, order=2, rtol=1e-5, atol=1e-10,
+                 controller=PID, hfixed=0.0, maxsteps=100000, ls="cg", maxl=20, prec="jacobi",
+                 pfmg=None, msbp=0, epslin=0.0, linear=False, max_restarts=0, gstype=1):
+        L = lib()
+        self.ctx = ctx
+        self.problem = problem
+        self.pfmg = pfmg
+        fn = C.cast(L.STS_Diffusion, _vp)
+        self.mem = L.STS_ARKStepCreate(None if implicit else fn, fn if implicit else None, t0, y0.h, ctx.h)
+        if not self.mem:
+            _err("STS_ARKStepCreate")
+        ctx.live += 1
+        self.n = len(y0)
+        self.LS = None
+        L.STS_ARKodeSetUserData(self.mem, problem.h)
+        if L.STS_ARKodeSetOrder(self.mem, order) != 0:
+            _err("STS_ARKodeSetOrder")
+        L.STS_ARKodeSStolerances(self.mem, rtol, atol)
+        L.STS_ARKodeSetAdaptController(self.mem, controller)
+        L.STS_ARKodeSetMaxNumSteps(self.mem, maxsteps)
+        if hfixed > 0:
+            L.STS_ARKodeSetFixedStep(self.mem, hfixed)
+        if implicit:
+            pretype = 0 if prec is None else 2  # SUN_PREC_NONE / SUN_PREC_RIGHT
+            if ls == "cg":
+                self.LS = L.STS_SUNLinSol_PCG(y0.h, pretype, maxl, ctx.h)
+            else:
+                self.LS = L.STS_SUNLinSol_SPGMR(y0.h, pretype, maxl, ctx.h)
+                L.STS_SUNLinSol_SPGMRSetMaxRestarts(self.LS, max_restarts)
+                L.STS_SUNLinSol_SPGMRSetGSType(self.LS, gstype)
+            L.STS_ARKodeSetLinearSolver(self.mem, self.LS, None)
+            if prec == "jacobi":
+                L.STS_ARKodeSetPreconditioner(self.mem, C.cast(L.STS_PSetup, _vp), C.cast(L.STS_PSolve, _vp))
+            elif prec == "pfmg":
+                # PSetup / PSolve of the PFMG object: its handle is the data they receive
+                L.STS_ARKStepSetPrecData(self.mem, pfmg.h)
+                L.STS_ARKodeSetPreconditioner(self.mem, C.cast(L.STS_PFMGPSetup, _vp),
+                                              C.cast(L.STS_PFMGPSolve, _vp))
+            L.STS_ARKodeSetLSetupFrequency(self.mem, msbp)
+            L.STS_ARKodeSetEpsLin(self.mem, epslin)
+            if linear:
+                L.STS_ARKodeSetLinear(self.mem, 0)
+
+    def evolve(self, tout, yout, itask=NORMAL):
+        t = C.c_double()
+        rc = lib().STS_ARKodeEvolve(self.mem, tout, yout.h, C.byref(t), itask)
+        if rc < TOO_MUCH_WORK:
+            _err("STS_ARKodeEvolve returned %d" % rc)
+        return t.value, rc
+
+    def stats(self):
+        s = ARKStepStats()
+        lib().STS_ARKStepGetStats(self.mem, C.byref(s))
+        return {k: getattr(s, k) for k, _ in ARKStepStats._fields_}
+
+    def print_stats(self):
+        buf = C.create_string_buffer(4096)
+        lib().STS_ARKodePrintAllStats(self.mem, buf, 4096)
+        return buf.value.decode()
+
+    def free(self):
+        if self.mem and not _exiting:
+            m = _vp(self.mem)
+            lib().STS_ARKodeFree(C.byref(m))
+            self.mem = None
+            if self.LS:
+                lib().STS_SUNLinSolFree(self.LS)
+                self.LS = None
+            self.ctx.live -= 1
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def arkstep_table(implicit, order):
+    """(A, b, d, c, q, p) of the ARKStep method table"""
+    import numpy as np
+    s, q, p = C.c_int(), C.c_int(), C.c_int()
+    A, b, d, c = np.zeros(25), np.zeros(5), np.zeros(5), np.zeros(5)
+    if lib().STS_ARKStepTable(int(implicit), order, C.byref(s), C.byref(q), C.byref(p), _dptr(A), _dptr(b),
+                              _dptr(d), _dptr(c)) != 0:
+        raise ValueError("no table")
+    n = s.value
+    return A[:n * n].reshape(n, n), b[:n], d[:n], c[:n], q.value, p.value
 
 
 class PCGSolver:

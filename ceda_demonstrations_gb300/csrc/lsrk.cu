@@ -142,6 +142,11 @@ extern "C" int STS_LSRKStagesNeeded(int method, double h, double rho, int smax, 
 static constexpr double ORD = 3.0, BIAS = 1.5, TINYE = 1.0e-10;
 static double controller_estimate(int controller, double h, double dsm, double ep1, double ep2, double hp,
                                   long long nhist, double ORD);
+double sts_controller_estimate(int controller, double h, double dsm, double ep1, double ep2, double hp,
+                               long long nhist, double ord)
+{
+  return controller_estimate(controller, h, dsm, ep1, ep2, hp, nhist, ord);
+}
 extern "C" double STS_AdaptControllerEstimate(int controller, double h, double dsm, double ep1, double ep2,
                                               double hp, long long nhist)
 {
@@ -199,6 +204,7 @@ struct GraphKey {
 };
 
 struct LSRKMem {
+  uint32_t kind         = STS_MEM_LSRK; // first member: the ARKode* calls dispatch on it
   STS_Context ctx       = nullptr;
   STS_ARKRhsFn rhs      = nullptr;
   void* user_data       = nullptr;
@@ -1484,6 +1490,7 @@ extern "C" int STS_LSRKStepSetNumSSPStages(void* mem, int s)
 extern "C" int STS_ARKodeSStolerances(void* mem, double rtol, double atol)
 {
   CHECK_MEM(mem);
+  if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_sstolerances(mem, rtol, atol);
   if (rtol < 0 || atol < 0) return STS_ILL_INPUT;
   MEM(mem)->rtol = rtol;
   MEM(mem)->atol = atol;
@@ -1492,6 +1499,7 @@ extern "C" int STS_ARKodeSStolerances(void* mem, double rtol, double atol)
 extern "C" int STS_ARKodeSetUserData(void* mem, void* ud)
 {
   CHECK_MEM(mem);
+  if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_set_user_data(mem, ud);
   MEM(mem)->user_data = ud;
   return 0;
 }
@@ -1533,6 +1541,7 @@ extern "C" int STS_LSRKStepSetDomEigSafetyFactor(void* mem, double safety)
 extern "C" int STS_ARKodeSetAdaptController(void* mem, int controller)
 {
   CHECK_MEM(mem);
+  if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_set_controller(mem, controller);
   if (controller < STS_ADAPT_PID || controller > STS_ADAPT_IMEX_GUS) return STS_ILL_INPUT;
   MEM(mem)->controller = controller;
   return 0;
@@ -1540,6 +1549,7 @@ extern "C" int STS_ARKodeSetAdaptController(void* mem, int controller)
 extern "C" int STS_ARKodeSetFixedStep(void* mem, double h)
 {
   CHECK_MEM(mem);
+  if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_set_fixed_step(mem, h);
   MEM(mem)->hfixed = h;
   if (h > 0.0) MEM(mem)->hnext = h;
   return 0;
@@ -1547,12 +1557,14 @@ extern "C" int STS_ARKodeSetFixedStep(void* mem, double h)
 extern "C" int STS_ARKodeSetMaxNumSteps(void* mem, long long mxsteps)
 {
   CHECK_MEM(mem);
+  if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_set_max_steps(mem, mxsteps);
   MEM(mem)->maxsteps = mxsteps;
   return 0;
 }
 extern "C" int STS_ARKodeSetStopTime(void* mem, double tstop)
 {
   CHECK_MEM(mem);
+  if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_set_stop_time(mem, tstop);
   MEM(mem)->tstop = tstop;
   return 0;
 }
@@ -1615,6 +1627,7 @@ extern "C" int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* t
 {
   STS_MARK_REGION("Evolve");
   CHECK_MEM(mem);
+  if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_evolve(mem, tout, yout, tret, itask);
   LSRKMem* m = MEM(mem);
   if (!yout || NVL(yout) != m->n)
   {
@@ -1650,6 +1663,7 @@ extern "C" int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* t
 extern "C" int STS_ARKodeReset(void* mem, double t, N_Vector y)
 {
   CHECK_MEM(mem);
+  if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_reset(mem, t, y);
   LSRKMem* m = MEM(mem);
   if (!y || NVL(y) != m->n) return STS_ILL_INPUT;
   ctx_activate(m->ctx);
@@ -1711,6 +1725,7 @@ extern "C" int STS_LSRKStepTimeStageKernel(void* mem, int nlaunch, double* ms_pe
 extern "C" int STS_ARKodeGetStats(void* mem, STS_Stats* s)
 {
   CHECK_MEM(mem);
+  if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_get_stats(mem, s);
   LSRKMem* m        = MEM(mem);
   s->nst            = m->nst;
   s->nst_attempts   = m->nst_att;
@@ -1732,6 +1747,7 @@ extern "C" int STS_ARKodeGetStats(void* mem, STS_Stats* s)
 extern "C" int STS_ARKodePrintAllStats(void* mem, char* buf, int buflen)
 {
   CHECK_MEM(mem);
+  if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_print_stats(mem, buf, buflen);
   LSRKMem* m = MEM(mem);
   int k      = snprintf(buf, buflen,
                         "Current time                  = %.16g\n"
@@ -1752,6 +1768,12 @@ extern "C" int STS_ARKodePrintAllStats(void* mem, char* buf, int buflen)
 extern "C" void STS_ARKodeFree(void** mem)
 {
   if (!mem || !*mem) return;
+  if (sts_mem_kind(*mem) == STS_MEM_ARKSTEP)
+  {
+    arkstep_free(*mem);
+    *mem = nullptr;
+    return;
+  }
   LSRKMem* m = MEM(*mem);
   ctx_activate(m->ctx);
   cudaStreamSynchronize(m->ctx->stream);

@@ -237,3 +237,24 @@ int sts_rhs_launch(STS_Problem p, double t, const double* u, double* f, bool for
 double sts_dot_exact(STS_Context ctx, const double* x, const double* y, long long n, int slot);
 double sts_wrms_ewt(STS_Context ctx, const double* a, const double* b, const double* y, long long n,
                     double rtol, double atol, int slot);
+
+// Integrator handles (void* arkode_mem) start with a kind word: LSRKStep (lsrk.cu) or ARKStep
+// (arkstep.cu); the ARKode* entry points of lsrk.cu dispatch on it.
+#include <cstdint>
+constexpr uint32_t STS_MEM_LSRK    = 0x4B52534Cu;
+constexpr uint32_t STS_MEM_ARKSTEP = 0x534B5241u;
+inline uint32_t sts_mem_kind(const void* mem) { return *(const uint32_t*)mem; }
+// the step-size controllers of lsrk.cu for an error estimate of order ord
+double sts_controller_estimate(int controller, double h, double dsm, double ep1, double ep2, double hp,
+                               long long nhist, double ord);
+int arkstep_sstolerances(void* mem, double rtol, double atol);
+int arkstep_set_user_data(void* mem, void* ud);
+int arkstep_set_controller(void* mem, int c);
+int arkstep_set_fixed_step(void* mem, double h);
+int arkstep_set_max_steps(void* mem, long long mx);
+int arkstep_set_stop_time(void* mem, double ts);
+int arkstep_evolve(void* mem, double tout, N_Vector yout, double* tret, int itask);
+int arkstep_reset(void* mem, double t, N_Vector y);
+int arkstep_get_stats(void* mem, STS_Stats* s);
+int arkstep_print_stats(void* mem, char* buf, int buflen);
+void arkstep_free(void* mem);

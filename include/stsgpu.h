@@ -275,6 +275,45 @@ int STS_ARKodeGetStats(void* mem, STS_Stats* stats);                  /* ARKodeP
 int STS_ARKodePrintAllStats(void* mem, char* buf, int buflen);
 void STS_ARKodeFree(void** mem);                                     /* main.cpp:505 */
 
+/* ------------------------------------------------------------------------------------
+ * ARKStep (ARKODE's additive RK stepper) in the two forms diffusion_2D/main.cpp:239-253
+ * creates: ARKStepCreate(nullptr, fi, ...) -> implicit DIRK (--integrator dirk) with a
+ * Newton iteration on each stage, its linear systems solved by a SUNLinearSolver with the
+ * user's PSetup / PSolve (main.cpp:199-231, 296-330); ARKStepCreate(fe, nullptr, ...) ->
+ * explicit ERK (--integrator erk with --order >= 0). Methods (ARKodeSetOrder): implicit
+ * 2 = ARKODE_SDIRK_2_1_2, 3 = ARKODE_ARK324L2SA_DIRK_4_2_3 (the default); explicit
+ * 2 = ARKODE_HEUN_EULER_2_1_2, 3 = ARKODE_BOGACKI_SHAMPINE_4_2_3, 4 = ARKODE_ZONNEVELD_5_3_4
+ * (the default). The returned handle takes the ARKode* calls above (tolerances, user data,
+ * controller, fixed step, max steps, stop time, Evolve, Reset, GetStats, PrintAllStats, Free).
+ * ----------------------------------------------------------------------------------*/
+#define STS_CONV_FAILURE -4 /* ARK_CONV_FAILURE */
+typedef int (*STS_ARKLsPrecSetupFn)(double t, N_Vector y, N_Vector fy, int jok, int* jcurPtr,
+                                    double gamma, void* user_data);
+typedef int (*STS_ARKLsPrecSolveFn)(double t, N_Vector y, N_Vector fy, N_Vector r, N_Vector z,
+                                    double gamma, double delta, int lr, void* user_data);
+void* STS_ARKStepCreate(STS_ARKRhsFn fe, STS_ARKRhsFn fi, double t0, N_Vector y0,
+                        STS_Context ctx);                                   /* main.cpp:239-248 */
+int STS_ARKodeSetOrder(void* mem, int order);                               /* main.cpp:272, 297 */
+int STS_ARKodeSetLinearSolver(void* mem, void* LS, void* A);               /* main.cpp:305 */
+int STS_ARKodeSetPreconditioner(void* mem, STS_ARKLsPrecSetupFn psetup,
+                                STS_ARKLsPrecSolveFn psolve);               /* main.cpp:311 */
+/* new: the user data PSetup / PSolve receive, where it differs from the RHS's (the reference
+ * keeps both in one UserData; here e.g. an STS_PFMG beside the STS_Problem). NULL: the RHS's */
+int STS_ARKStepSetPrecData(void* mem, void* pdata);
+int STS_ARKodeSetLSetupFrequency(void* mem, int msbp);                     /* main.cpp:315 */
+int STS_ARKodeSetEpsLin(void* mem, double eplifac);                        /* main.cpp:320 */
+int STS_ARKodeSetLinear(void* mem, int timedepend);                        /* main.cpp:326 */
+int STS_ARKodeSetNonlinear(void* mem); /* the --nonlinear default of ARKODE (main.cpp:630) */
+typedef struct STS_ARKStepStats {
+  long long nst, nst_attempts, netf, ncfn, nfe, nfi, nfe_ls, nni, nnf, nli, nlcf, npe, nps, njv,
+      nsetups;
+  double t, h0, hlast, hnext;
+} STS_ARKStepStats;
+int STS_ARKStepGetStats(void* mem, STS_ARKStepStats* stats); /* ARKodePrintAllStats main.cpp:486 */
+/* host helper: the Butcher table (A row-major s x s, b, embedding d, c) of a method */
+int STS_ARKStepTable(int implicit, int order, int* s, int* q, int* p, double* A, double* b,
+                     double* d, double* c);
+
 /* host-only helpers (no device work): the integrator's coefficient and step-size rules */
 int STS_LSRKStageCoeffs(int method, int s, double* mu, double* nu, double* mus, double* ajm1,
                         double* cjm1);

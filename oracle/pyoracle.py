@@ -29,6 +29,19 @@ class Prob(C.Structure):
                 ("Dxw", _dp), ("Dxe", _dp), ("Dys", _dp), ("Dyn", _dp)]
 
 
+class ArkOpts(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("implicit", "order", "controller", "ls", "maxl", "max_restarts", "gstype",
+                                       "prec", "pfmg_relax", "pfmg_nrelax", "msbp", "linear", "onestep")] + \
+               [("maxsteps", C.c_long)] + [(k, C.c_double) for k in ("rtol", "atol", "hfixed", "eplifac")]
+
+
+class ArkState(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("t", "hnext", "hlast", "h0", "ep1", "ep2", "gamma_setup")] + \
+               [(k, C.c_long) for k in ("nst", "nst_att", "netf", "ncfn", "nfe", "nfi", "nni", "nnf", "nli", "nlcf",
+                                        "npe", "nps", "njv", "nsetups", "nhist", "nst_setup")] + \
+               [(k, C.c_int) for k in ("initialized", "after_fail", "force_setup")]
+
+
 class Opts(C.Structure):
     _fields_ = [("method", C.c_int), ("mixed", C.c_int), ("controller", C.c_int),
                 ("smax", C.c_int), ("internaleig", C.c_int), ("dee_maxiters", C.c_int),
@@ -135,6 +148,10 @@ def lib():
         L.orc_sdirk2_pfmg.restype = C.c_int
         L.orc_sdirk2_pfmg.argtypes = [C.POINTER(Prob), C.c_double, C.c_double, C.c_int, C.c_double, C.c_int,
                                       C.c_int, C.c_int, _dp, C.POINTER(C.c_long)]
+        L.orc_arkstep_evolve.restype = C.c_int
+        L.orc_arkstep_evolve.argtypes = [C.POINTER(Prob), C.POINTER(ArkOpts), C.POINTER(ArkState), C.c_double, _dp]
+        L.orc_ark_table.restype = C.c_int
+        L.orc_ark_table.argtypes = [C.c_int, C.c_int] + [C.POINTER(C.c_int)] * 3 + [_dp] * 4
         L.orc_nthreads.restype = C.c_int
         _lib = L
     return _lib
@@ -366,3 +383,39 @@ def ssp_weights(type_, s):
     if lib().orc_ssp_weights(type_, s, dptr(b), dptr(c), dptr(w)) != 0:
         raise ValueError("invalid SSP method / stage count")
     return b, c, w
+
+
+class ArkIntegrator:
+    """The oracle's ARKStep (orc_arkstep_evolve): implicit DIRK with Newton + PCG / SPGMR
+    (prec None / "jacobi" / "pfmg") or explicit ERK; state persists across evolve calls."""
+
+    def __init__(self, prob, y0, t0=0.0, implicit=True, order=2, rtol=1e-5, atol=1e-10, controller=0,
+                 hfixed=0.0, maxsteps=100000, ls="cg", maxl=20, prec="jacobi", pfmg_relax=2, pfmg_nrelax=2,
+                 msbp=0, epslin=0.0, linear=False, max_restarts=0, gstype=1, onestep=False):
+        self.prob = prob
+        pc = {None: 0, "jacobi": 1, "pfmg": 2}[prec]
+        self.opts = ArkOpts(implicit=int(implicit), order=order, controller=controller,
+                            ls=0 if ls == "cg" else 1, maxl=maxl, max_restarts=max_restarts, gstype=gstype,
+                            prec=pc, pfmg_relax=pfmg_relax, pfmg_nrelax=pfmg_nrelax, msbp=msbp,
+                            linear=int(linear), onestep=int(onestep), maxsteps=maxsteps, rtol=rtol, atol=atol,
+                            hfixed=hfixed, eplifac=epslin if epslin > 0 else 0.05)
+        self.st = ArkState()
+        self.st.t = t0
+        self.st.force_setup = 1
+        self.y = np.array(y0, dtype=np.float64)
+
+    def evolve(self, tout):
+        return lib().orc_arkstep_evolve(self.prob.p, C.byref(self.opts), C.byref(self.st), tout, dptr(self.y))
+
+    def stats(self):
+        return {k: getattr(self.st, k) for k, _ in ArkState._fields_}
+
+
+def ark_table(implicit, order):
+    s, q, p = C.c_int(), C.c_int(), C.c_int()
+    A, b, d, c = np.zeros(25), np.zeros(5), np.zeros(5), np.zeros(5)
+    if lib().orc_ark_table(int(implicit), order, C.byref(s), C.byref(q), C.byref(p), dptr(A), dptr(b), dptr(d),
+                           dptr(c)) != 0:
+        raise ValueError("no table")
+    n = s.value
+    return A[:n * n].reshape(n, n), b[:n], d[:n], c[:n], q.value, p.value

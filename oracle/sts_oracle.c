@@ -1414,9 +1414,13 @@ typedef struct {
   orc_pfmg* mg;
 } gen_op;
 
+/* calls of the callbacks (the ARKStep restatement reports them as Jac-times evals / Prec solves) */
+static long g_gen_atimes_calls = 0, g_gen_psolve_calls = 0;
+
 static void gen_atimes(const gen_op* o, const double* v, double* z)
 {
   long n = (long)o->p->nx * o->p->ny;
+  g_gen_atimes_calls++;
   orc_apply_A(o->p, v, o->tmp);
   v_linsum(n, 1.0, v, -o->gamma, o->tmp, z);
 }
@@ -1425,7 +1429,19 @@ static void gen_atimes(const gen_op* o, const double* v, double* z)
 static void gen_psolve(const gen_op* o, const double* r, double* z, int copy_form)
 {
   long n = (long)o->p->nx * o->p->ny;
+  if (o->jacobi) g_gen_psolve_calls++;
   if (o->jacobi == 2) pfmg_apply(o->mg, r, z);
+  else if (o->jacobi && o->p->kind == ORC_PERIODIC)
+  { /* per-point diagonal of the periodic operator: -((Dxw + Dxe) + (Dys + Dyn)) */
+    const orc_prob* p = o->p;
+    for (long j = 0; j < p->ny; ++j)
+      for (long i = 0; i < p->nx; ++i)
+      {
+        double diag      = -((p->Dxw[i] + p->Dxe[i]) + (p->Dys[j] + p->Dyn[j]));
+        double D         = 1.0 / (1.0 - o->gamma * diag);
+        z[j * p->nx + i] = D * r[j * p->nx + i];
+      }
+  }
   else if (o->jacobi)
     for (long k = 0; k < n; ++k) z[k] = o->D * r[k];
   else if (copy_form) v_linsum(n, 1.0, r, 0.0, r, z);
@@ -1434,17 +1450,16 @@ static void gen_psolve(const gen_op* o, const double* r, double* z, int copy_for
 
 /* SUNLinSol_PCG through callbacks, x0 = 0, stop when ||r|| <= tol ||b|| (0 / 1 = converged /
  * not within maxl iterations) */
-int orc_pcg_generic(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol,
-                    int maxl, int* iters, double* relres)
+/* SUNLinSol_PCG over the operator / preconditioner of `o` (the product's pcg_solve) */
+static int gen_pcg(gen_op* o, const double* b, double* x, double tol, int maxl, int* iters, double* relres)
 {
-  long n = (long)p->nx * p->ny;
-  gen_op o = {p, gamma, 1.0 / (1.0 - gamma * p->cc), jacobi, (double*)malloc(n * sizeof(double)), NULL};
+  long n     = (long)o->p->nx * o->p->ny;
   double* r  = (double*)malloc(n * sizeof(double));
   double* z  = (double*)malloc(n * sizeof(double));
   double* pv = (double*)malloc(n * sizeof(double));
   double* Ap = (double*)malloc(n * sizeof(double));
   int ret = 1;
-  *iters = 0;
+  *iters  = 0;
   *relres = 0.0;
   for (long k = 0; k < n; ++k) x[k] = 0.0;
   v_linsum(n, 1.0, b, 0.0, b, r);
@@ -1454,12 +1469,12 @@ int orc_pcg_generic(const orc_prob* p, double gamma, int jacobi, const double* b
     ret = 0;
     goto out;
   }
-  gen_psolve(&o, r, z, 1);
+  gen_psolve(o, r, z, 1);
   double rz = orc_xdot(r, z, n);
   v_linsum(n, 1.0, z, 0.0, z, pv);
   for (int it = 1; it <= maxl; ++it)
   {
-    gen_atimes(&o, pv, Ap);
+    gen_atimes(o, pv, Ap);
     double pq    = orc_xdot(pv, Ap, n);
     double alpha = rz / pq;
     v_linsum(n, alpha, pv, 1.0, x, x);
@@ -1472,18 +1487,27 @@ int orc_pcg_generic(const orc_prob* p, double gamma, int jacobi, const double* b
       ret = 0;
       goto out;
     }
-    gen_psolve(&o, r, z, 1);
+    gen_psolve(o, r, z, 1);
     double rzn  = orc_xdot(r, z, n);
     double beta = rzn / rz;
     rz          = rzn;
     v_linsum(n, 1.0, z, beta, pv, pv);
   }
 out:
-  free(o.tmp);
   free(r);
   free(z);
   free(pv);
   free(Ap);
+  return ret;
+}
+
+int orc_pcg_generic(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol,
+                    int maxl, int* iters, double* relres)
+{
+  long n   = (long)p->nx * p->ny;
+  gen_op o = {p, gamma, 1.0 / (1.0 - gamma * p->cc), jacobi, (double*)malloc(n * sizeof(double)), NULL};
+  int ret  = gen_pcg(&o, b, x, tol, maxl, iters, relres);
+  free(o.tmp);
   return ret;
 }
 
@@ -1512,12 +1536,13 @@ static void orc_givens(double a, double b, double* c, double* s)
  * x0 = 0, Arnoldi by modified Gram-Schmidt (gstype 1) or classical Gram-Schmidt with one
  * re-orthogonalisation pass (gstype 2), Givens rotations; stop when the residual estimate
  * |g_{j+1}| <= tol ||b||; restart from the true residual. Returns 0 / 1 as orc_pcg_generic. */
-static int spgmr_impl(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol, int maxl,
-                      int max_restarts, int gstype, int flexible, int* iters, double* relres)
+static int spgmr_op(gen_op* op, const double* b, double* x, double tol, int maxl, int max_restarts, int gstype,
+                    int flexible, int* iters, double* relres)
 {
-  long n  = (long)p->nx * p->ny;
-  int m   = maxl;
-  gen_op o = {p, gamma, 1.0 / (1.0 - gamma * p->cc), jacobi, (double*)malloc(n * sizeof(double)), NULL};
+  gen_op o         = *op;
+  const int jacobi = o.jacobi;
+  long n           = (long)o.p->nx * o.p->ny;
+  int m            = maxl;
   double** V = (double**)malloc((m + 1) * sizeof(double*));
   for (int k = 0; k <= m; ++k) V[k] = (double*)malloc(n * sizeof(double));
   /* flexible GMRES keeps the preconditioned basis Z (Saad 1993) */
@@ -1653,7 +1678,6 @@ static int spgmr_impl(const orc_prob* p, double gamma, int jacobi, const double*
   }
 #undef HH
 out:
-  free(o.tmp);
   for (int k = 0; k <= m; ++k) free(V[k]);
   free(V);
   for (int k = 0; k < m; ++k) free(Z[k]);
@@ -1670,6 +1694,16 @@ out:
   free(h2);
   free(cf);
   free(X);
+  return ret;
+}
+
+static int spgmr_impl(const orc_prob* p, double gamma, int jacobi, const double* b, double* x, double tol, int maxl,
+                      int max_restarts, int gstype, int flexible, int* iters, double* relres)
+{
+  long n   = (long)p->nx * p->ny;
+  gen_op o = {p, gamma, 1.0 / (1.0 - gamma * p->cc), jacobi, (double*)malloc(n * sizeof(double)), NULL};
+  int ret  = spgmr_op(&o, b, x, tol, maxl, max_restarts, gstype, flexible, iters, relres);
+  free(o.tmp);
   return ret;
 }
 
@@ -1891,54 +1925,11 @@ int orc_pfmg_vcycle(const orc_prob* p, double gamma, int relax, int nrelax, cons
 int orc_pcg_pfmg(const orc_prob* p, double gamma, int relax, int nrelax, const double* b, double* x, double tol,
                  int maxl, int* iters, double* relres)
 {
-  long n = (long)p->nx * p->ny;
+  long n   = (long)p->nx * p->ny;
   gen_op o = {p, gamma, 0.0, 2, (double*)malloc(n * sizeof(double)), pfmg_create(p, gamma, relax, nrelax)};
-  double* r  = (double*)malloc(n * sizeof(double));
-  double* z  = (double*)malloc(n * sizeof(double));
-  double* pv = (double*)malloc(n * sizeof(double));
-  double* Ap = (double*)malloc(n * sizeof(double));
-  int ret = 1;
-  *iters  = 0;
-  *relres = 0.0;
-  for (long k = 0; k < n; ++k) x[k] = 0.0;
-  v_linsum(n, 1.0, b, 0.0, b, r);
-  double bnorm = sqrt(orc_xdot(b, b, n));
-  if (!(bnorm > 0.0))
-  {
-    ret = 0;
-    goto out;
-  }
-  gen_psolve(&o, r, z, 1);
-  double rz = orc_xdot(r, z, n);
-  v_linsum(n, 1.0, z, 0.0, z, pv);
-  for (int it = 1; it <= maxl; ++it)
-  {
-    gen_atimes(&o, pv, Ap);
-    double pq    = orc_xdot(pv, Ap, n);
-    double alpha = rz / pq;
-    v_linsum(n, alpha, pv, 1.0, x, x);
-    v_linsum(n, -alpha, Ap, 1.0, r, r);
-    double rr = orc_xdot(r, r, n);
-    *iters    = it;
-    *relres   = sqrt(rr) / bnorm;
-    if (sqrt(rr) <= tol * bnorm)
-    {
-      ret = 0;
-      goto out;
-    }
-    gen_psolve(&o, r, z, 1);
-    double rzn  = orc_xdot(r, z, n);
-    double beta = rzn / rz;
-    rz          = rzn;
-    v_linsum(n, 1.0, z, beta, pv, pv);
-  }
-out:
+  int ret  = gen_pcg(&o, b, x, tol, maxl, iters, relres);
   pfmg_destroy(o.mg);
   free(o.tmp);
-  free(r);
-  free(z);
-  free(pv);
-  free(Ap);
   return ret;
 }
 
@@ -2411,5 +2402,366 @@ done:
   free(G);
   free(E);
   free(ynew);
+  return ret;
+}
+
+/* ------------------------------------------------------------------------------------
+ * ARKStep restated in the product's operation sequence (csrc/arkstep.cu): implicit DIRK
+ * (ARKODE_SDIRK_2_1_2, ARKODE_ARK324L2SA_DIRK_4_2_3) with Newton corrections solved by the
+ * generic PCG / SPGMR above (no, Jacobi or PFMG preconditioner), or explicit ERK
+ * (ARKODE_HEUN_EULER_2_1_2, ARKODE_BOGACKI_SHAMPINE_4_2_3, ARKODE_ZONNEVELD_5_3_4); ARKODE's
+ * Newton convergence test, linear tolerance eplifac * 0.1 in the WRMS norm, PSetup schedule,
+ * embedded error estimate and the LSRKStep controllers with order p + 1
+ * (diffusion_2D/main.cpp:239-330 create and configure it).
+ * ----------------------------------------------------------------------------------*/
+static int ark_table(int implicit, int order, int* s, int* q, int* pe, double* A, double* b, double* d, double* c)
+{
+  memset(A, 0, 25 * sizeof(double));
+  if (implicit && order == 2)
+  {
+    *s = 2; *q = 2; *pe = 1;
+    A[0] = 1.0; A[2] = -1.0; A[3] = 1.0;
+    b[0] = 0.5; b[1] = 0.5; d[0] = 1.0; d[1] = 0.0; c[0] = 1.0; c[1] = 0.0;
+  }
+  else if (implicit && order == 3)
+  { /* Kennedy & Carpenter (2003), ARK3(2)4L[2]SA, implicit part */
+    const double g = 1767732205903.0 / 4055673282236.0;
+    *s = 4; *q = 3; *pe = 2;
+    A[4] = g; A[5] = g;
+    A[8] = 2746238789719.0 / 10658868560708.0; A[9] = -640167445237.0 / 6845629431997.0; A[10] = g;
+    A[12] = 1471266399579.0 / 7840856788654.0; A[13] = -4482444167858.0 / 7529755066697.0;
+    A[14] = 11266239266428.0 / 11593286722821.0; A[15] = g;
+    for (int i = 0; i < 4; ++i) b[i] = A[12 + i];
+    d[0] = 2756255671327.0 / 12835298489170.0; d[1] = -10771552573575.0 / 22201958757719.0;
+    d[2] = 9247589265047.0 / 10645013368117.0; d[3] = 2193209047091.0 / 5459859503100.0;
+    c[0] = 0.0; c[1] = 2.0 * g; c[2] = 3.0 / 5.0; c[3] = 1.0;
+  }
+  else if (!implicit && order == 2)
+  { /* Heun-Euler */
+    *s = 2; *q = 2; *pe = 1;
+    A[2] = 1.0; b[0] = 0.5; b[1] = 0.5; d[0] = 1.0; d[1] = 0.0; c[0] = 0.0; c[1] = 1.0;
+  }
+  else if (!implicit && order == 3)
+  { /* Bogacki-Shampine */
+    *s = 4; *q = 3; *pe = 2;
+    A[4] = 0.5; A[9] = 0.75; A[12] = 2.0 / 9.0; A[13] = 1.0 / 3.0; A[14] = 4.0 / 9.0;
+    b[0] = 2.0 / 9.0; b[1] = 1.0 / 3.0; b[2] = 4.0 / 9.0; b[3] = 0.0;
+    d[0] = 7.0 / 24.0; d[1] = 0.25; d[2] = 1.0 / 3.0; d[3] = 0.125;
+    c[0] = 0.0; c[1] = 0.5; c[2] = 0.75; c[3] = 1.0;
+  }
+  else if (!implicit && order == 4)
+  { /* Zonneveld */
+    *s = 5; *q = 4; *pe = 3;
+    A[5] = 0.5; A[11] = 0.5; A[17] = 1.0;
+    A[20] = 5.0 / 32.0; A[21] = 7.0 / 32.0; A[22] = 13.0 / 32.0; A[23] = -1.0 / 32.0;
+    b[0] = 1.0 / 6.0; b[1] = 1.0 / 3.0; b[2] = 1.0 / 3.0; b[3] = 1.0 / 6.0; b[4] = 0.0;
+    d[0] = -0.5; d[1] = 7.0 / 3.0; d[2] = 7.0 / 3.0; d[3] = 13.0 / 6.0; d[4] = -16.0 / 3.0;
+    c[0] = 0.0; c[1] = 0.5; c[2] = 0.5; c[3] = 1.0; c[4] = 0.75;
+  }
+  else return -1;
+  return 0;
+}
+
+int orc_ark_table(int implicit, int order, int* s, int* q, int* pe, double* A, double* b, double* d, double* c)
+{
+  double A5[25], b5[5], d5[5], c5[5];
+  if (ark_table(implicit, order, s, q, pe, A5, b5, d5, c5)) return -1;
+  for (int i = 0; i < *s; ++i)
+  {
+    b[i] = b5[i];
+    d[i] = d5[i];
+    c[i] = c5[i];
+    for (int j = 0; j < *s; ++j) A[i * *s + j] = A5[i * *s + j];
+  }
+  return 0;
+}
+
+typedef struct {
+  const orc_prob* p;
+  const orc_ark_opts* o;
+  orc_ark_state* st;
+  long n;
+  int s, pe;
+  double A[25], b[5], d[5], c[5];
+  double *y, *Fn, *sdata, *z, *res, *del, *ewt, *tmp, *tmp2, *ynew, *F[5];
+  orc_pfmg* mg;
+  double mg_gamma;
+  int fn_current;
+} ark_ws;
+
+static void ark_rhs(ark_ws* w, double t, const double* y, double* f)
+{
+  orc_rhs(w->p, t, y, f);
+  if (w->o->implicit) w->st->nfi++;
+  else w->st->nfe++;
+}
+
+static void ark_ewt(ark_ws* w)
+{
+  for (long k = 0; k < w->n; ++k) w->ewt[k] = 1.0 / (w->o->rtol * fabs(w->y[k]) + w->o->atol);
+}
+
+static int ark_stage(ark_ws* w, int i, double ti, double gamma)
+{
+  const orc_ark_opts* o = w->o;
+  orc_ark_state* st     = w->st;
+  long n                = w->n;
+  const double epslin   = o->eplifac * 0.1;
+  const int msbp        = o->msbp > 0 ? o->msbp : 20;
+  memcpy(w->z, w->y, n * sizeof(double));
+  double crate = 1.0, delp = 0.0;
+  for (int it = 0;; ++it)
+  {
+    ark_rhs(w, ti, w->z, w->F[i]);
+    {
+      double cf[3]       = {1.0, gamma, -1.0};
+      const double* X[3] = {w->sdata, w->F[i], w->z};
+      v_lincomb(n, 3, cf, X, w->res);
+    }
+    if (it == 0 && o->prec)
+    {
+      int need = st->force_setup || st->nsetups == 0 || st->nst >= st->nst_setup + msbp ||
+                 fabs(gamma / st->gamma_setup - 1.0) > 0.2;
+      if (need)
+      {
+        st->npe++;
+        st->nsetups++;
+        st->gamma_setup = gamma;
+        st->nst_setup   = st->nst;
+        st->force_setup = 0;
+        crate           = 1.0;
+      }
+    }
+    double bnrm = orc_wrms(w->res, w->ewt, n);
+    if (bnrm <= epslin)
+      for (long k = 0; k < n; ++k) w->del[k] = 0.0;
+    else
+    {
+      gen_op go = {w->p, gamma, 1.0 / (1.0 - gamma * w->p->cc), o->prec, w->tmp, NULL};
+      if (o->prec == 2)
+      { /* the product's PFMG PSolve rebuilds its hierarchy when gamma changes */
+        if (!w->mg || w->mg_gamma != gamma)
+        {
+          if (w->mg) pfmg_destroy(w->mg);
+          w->mg       = pfmg_create(w->p, gamma, o->pfmg_relax, o->pfmg_nrelax);
+          w->mg_gamma = gamma;
+        }
+        go.mg = w->mg;
+      }
+      long a0 = g_gen_atimes_calls, p0 = g_gen_psolve_calls;
+      int iters = 0;
+      double rel;
+      int lrc = (o->ls == 0) ? gen_pcg(&go, w->res, w->del, epslin / bnrm, o->maxl, &iters, &rel)
+                             : spgmr_op(&go, w->res, w->del, epslin / bnrm, o->maxl, o->max_restarts, o->gstype, 0,
+                                        &iters, &rel);
+      st->njv += g_gen_atimes_calls - a0;
+      st->nps += g_gen_psolve_calls - p0;
+      st->nli += iters;
+      if (lrc > 0) st->nlcf++;
+    }
+    st->nni++;
+    v_linsum(n, 1.0, w->z, 1.0, w->del, w->z);
+    double del = orc_wrms(w->del, w->ewt, n);
+    if (o->linear) break;
+    if (it > 0) crate = fmax(0.3 * crate, del / delp);
+    double dcon = del * fmin(1.0, crate) / 0.1;
+    if (dcon <= 1.0) break;
+    if (it + 1 >= 3 || (it >= 1 && del > 2.3 * delp) || !(del == del)) return 1;
+    delp = del;
+  }
+  ark_rhs(w, ti, w->z, w->F[i]);
+  return 0;
+}
+
+static int ark_attempt(ark_ws* w, double h)
+{
+  const int s = w->s;
+  long n      = w->n;
+  double cf[6];
+  const double* X[6];
+  for (int i = 0; i < s; ++i)
+  {
+    double ti  = w->st->t + w->c[i] * h;
+    double aii = w->A[i * s + i];
+    if (i == 0 && aii == 0.0)
+    {
+      if (!w->fn_current)
+      {
+        ark_rhs(w, w->st->t, w->y, w->Fn);
+        w->fn_current = 1;
+      }
+      memcpy(w->F[0], w->Fn, n * sizeof(double));
+      continue;
+    }
+    cf[0] = 1.0;
+    X[0]  = w->y;
+    for (int j = 0; j < i; ++j)
+    {
+      cf[j + 1] = h * w->A[i * s + j];
+      X[j + 1]  = w->F[j];
+    }
+    v_lincomb(n, i + 1, cf, X, w->sdata);
+    if (aii == 0.0)
+    {
+      ark_rhs(w, ti, w->sdata, w->F[i]);
+      continue;
+    }
+    int rc = ark_stage(w, i, ti, h * aii);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+int orc_arkstep_evolve(const orc_prob* p, const orc_ark_opts* o, orc_ark_state* st, double tout, double* y)
+{
+  ark_ws W;
+  memset(&W, 0, sizeof(W));
+  W.p  = p;
+  W.o  = o;
+  W.st = st;
+  W.n  = (long)p->nx * p->ny;
+  int q;
+  if (ark_table(o->implicit, o->order, &W.s, &q, &W.pe, W.A, W.b, W.d, W.c)) return -22;
+  long n          = W.n;
+  double** bufs[] = {&W.Fn, &W.sdata, &W.z, &W.res, &W.del, &W.ewt, &W.tmp, &W.tmp2, &W.ynew};
+  for (size_t k = 0; k < sizeof(bufs) / sizeof(bufs[0]); ++k) *bufs[k] = (double*)malloc(n * sizeof(double));
+  for (int i = 0; i < W.s; ++i) W.F[i] = (double*)malloc(n * sizeof(double));
+  W.y               = y;
+  const double ordv = (double)(W.pe + 1);
+  if (!st->initialized)
+  {
+    st->hnext       = (o->hfixed > 0.0) ? o->hfixed : 0.0;
+    st->initialized = 1;
+  }
+  W.fn_current     = 0;
+  double target    = tout;
+  long nsteps_call = 0;
+  int ret          = 0;
+  while (st->t < target)
+  {
+    if (nsteps_call >= (o->maxsteps > 0 ? o->maxsteps : 500))
+    {
+      ret = -1;
+      break;
+    }
+    ark_ewt(&W);
+    if (!(st->hnext > 0.0))
+    {
+      if (!W.fn_current)
+      {
+        ark_rhs(&W, st->t, W.y, W.Fn);
+        W.fn_current = 1;
+      }
+      double tdist = target - st->t;
+      double d0    = orc_wrms(W.y, W.ewt, n);
+      double d1    = orc_wrms(W.Fn, W.ewt, n);
+      double h0    = (d0 < 1.0e-5 || d1 < 1.0e-5) ? 1.0e-6 : 0.01 * (d0 / d1);
+      if (h0 > tdist) h0 = tdist;
+      v_linsum(n, h0, W.Fn, 1.0, W.y, W.tmp2);
+      ark_rhs(&W, st->t + h0, W.tmp2, W.tmp);
+      v_linsum(n, 1.0, W.tmp, -1.0, W.Fn, W.tmp);
+      double d2 = orc_wrms(W.tmp, W.ewt, n) / h0;
+      double dm = d1 > d2 ? d1 : d2;
+      double h1 = (dm <= 1.0e-15) ? fmax(1.0e-6, h0 * 1.0e-3) : orc_pow(0.01 / dm, 1.0 / ordv);
+      if (!(h1 > 0.0) || !(h1 < INFINITY)) h1 = h0;
+      double hh = (100.0 * h0 < h1) ? 100.0 * h0 : h1;
+      if (hh > tdist) hh = tdist;
+      if (!(hh > 0.0))
+      {
+        ret = -3;
+        goto out;
+      }
+      st->hnext = hh;
+      st->h0    = hh;
+    }
+    int nef = 0, ncf = 0;
+    for (;;)
+    {
+      double h    = st->hnext;
+      int clipped = 0;
+      if (st->t + h >= target)
+      {
+        h       = target - st->t;
+        clipped = 1;
+      }
+      st->nst_att++;
+      int rc = ark_attempt(&W, h);
+      if (rc == 1)
+      {
+        st->ncfn++;
+        st->nnf++;
+        if (o->hfixed > 0.0 || ++ncf > 10)
+        {
+          ret = -4;
+          goto out;
+        }
+        st->hnext       = 0.25 * h;
+        st->after_fail  = 1;
+        st->force_setup = 1;
+        continue;
+      }
+      double cf[6];
+      const double* X[6];
+      for (int i = 0; i < W.s; ++i)
+      {
+        cf[i] = h * (W.b[i] - W.d[i]);
+        X[i]  = W.F[i];
+      }
+      v_lincomb(n, W.s, cf, X, W.tmp);
+      double dsm = orc_wrms(W.tmp, W.ewt, n);
+      if (o->hfixed > 0.0 || dsm <= 1.0)
+      {
+        cf[0] = 1.0;
+        X[0]  = W.y;
+        for (int i = 0; i < W.s; ++i)
+        {
+          cf[i + 1] = h * W.b[i];
+          X[i + 1]  = W.F[i];
+        }
+        v_lincomb(n, W.s + 1, cf, X, W.ynew);
+        memcpy(W.y, W.ynew, n * sizeof(double));
+        st->t        = clipped ? target : st->t + h;
+        W.fn_current = 0;
+        double hprev = st->hlast;
+        st->hlast    = h;
+        if (o->hfixed > 0.0) st->hnext = o->hfixed;
+        else
+        {
+          double hn  = controller_ord(o->controller, h, dsm, st->ep1, st->ep2, hprev, st->nhist, ordv);
+          double eta = SAFETY * hn / h;
+          double emx = (st->nst == 0) ? ETAMX1 : (st->after_fail ? 1.0 : GROWTH);
+          if (eta > emx) eta = emx;
+          if (eta >= LBOUND && eta <= UBOUND) eta = 1.0;
+          st->hnext = h * eta;
+          st->ep2   = st->ep1;
+          st->ep1   = dsm;
+          st->nhist++;
+        }
+        st->after_fail = 0;
+        st->nst++;
+        nsteps_call++;
+        break;
+      }
+      st->netf++;
+      nef++;
+      if (!(dsm == dsm) || nef > 7)
+      {
+        ret = -3;
+        goto out;
+      }
+      double hn  = controller_ord(o->controller, h, dsm, st->ep1, st->ep2, st->hlast, st->nhist, ordv);
+      double eta = SAFETY * hn / h;
+      if (eta > 1.0) eta = 1.0;
+      if (nef >= SMALL_NEF && eta > ETAMXF) eta = ETAMXF;
+      if (eta < ETAMIN) eta = ETAMIN;
+      st->hnext      = h * eta;
+      st->after_fail = 1;
+    }
+    if (o->onestep) break;
+  }
+out:
+  if (W.mg) pfmg_destroy(W.mg);
+  for (size_t k = 0; k < sizeof(bufs) / sizeof(bufs[0]); ++k) free(*bufs[k]);
+  for (int i = 0; i < W.s; ++i) free(W.F[i]);
   return ret;
 }

@@ -111,6 +111,21 @@ int orc_pcg_pfmg(const orc_prob* p, double gamma, int relax, int nrelax, const d
                  int maxl, int* iters, double* relres);
 int orc_sdirk2_pfmg(const orc_prob* p, double t0, double h, int nsteps, double tol, int maxl, int relax, int nrelax,
                     double* y, long* total_iters);
+/* ARKStep (csrc/arkstep.cu): implicit DIRK (order 2 / 3) with Newton + PCG (ls 0) or SPGMR
+ * (ls 1), preconditioner prec 0 none / 1 Jacobi / 2 PFMG; explicit ERK (order 2 / 3 / 4) */
+typedef struct orc_ark_opts {
+  int implicit, order, controller, ls, maxl, max_restarts, gstype, prec, pfmg_relax, pfmg_nrelax, msbp,
+      linear, onestep;
+  long maxsteps;
+  double rtol, atol, hfixed, eplifac;
+} orc_ark_opts;
+typedef struct orc_ark_state {
+  double t, hnext, hlast, h0, ep1, ep2, gamma_setup;
+  long nst, nst_att, netf, ncfn, nfe, nfi, nni, nnf, nli, nlcf, npe, nps, njv, nsetups, nhist, nst_setup;
+  int initialized, after_fail, force_setup;
+} orc_ark_state;
+int orc_arkstep_evolve(const orc_prob* p, const orc_ark_opts* o, orc_ark_state* st, double tout, double* y);
+int orc_ark_table(int implicit, int order, int* s, int* q, int* pe, double* A, double* b, double* d, double* c);
 int orc_nthreads(void);
 
 #ifdef __cplusplus

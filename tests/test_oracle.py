@@ -430,3 +430,49 @@ def test_oracle_under_address_and_ub_sanitizers():
         pytest.skip("no sanitizer runtime for this compiler")
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
     assert "sanitize_check: ok" in r.stdout
+
+
+@pytest.mark.parametrize("implicit,order", [(True, 2), (True, 3), (False, 2), (False, 3), (False, 4)])
+def test_arkstep_tables_order_conditions_and_parity(oracle, stslib, implicit, order):
+    """The ARKStep Butcher tables (ARKODE_SDIRK_2_1_2, ARKODE_ARK324L2SA_DIRK_4_2_3, Heun-Euler,
+    Bogacki-Shampine, Zonneveld): product and oracle hold the same bits, rows sum to c, the
+    method meets the order conditions of order q and the embedding those of order p."""
+    A, b, d, c, q, p = stslib.arkstep_table(implicit, order)
+    Ao, bo, do, co, qo, po_ = oracle.ark_table(implicit, order)
+    for x, y in ((A, Ao), (b, bo), (d, do), (c, co)):
+        assert np.array_equal(x, y)
+    assert (q, p) == (qo, po_) == (order, order - 1)
+    assert np.allclose(A.sum(axis=1), c, atol=1e-15)
+    if implicit:
+        assert np.all(np.diag(A)[1:] > 0)
+    else:
+        assert np.all(np.triu(A) == 0)
+
+    def conds(w, k):
+        out = [w.sum() - 1.0]
+        if k >= 2:
+            out.append(w @ c - 0.5)
+        if k >= 3:
+            out += [w @ c ** 2 - 1.0 / 3.0, w @ (A @ c) - 1.0 / 6.0]
+        if k >= 4:
+            out += [w @ c ** 3 - 0.25, w @ (c * (A @ c)) - 0.125, w @ (A @ c ** 2) - 1.0 / 12.0,
+                    w @ (A @ (A @ c)) - 1.0 / 24.0]
+        return np.abs(out)
+    assert np.all(conds(b, q) < 1e-14)
+    assert np.all(conds(d, p) < 1e-14)
+    assert conds(d, p + 1).max() > 1e-6  # the embedding is of order p exactly
+
+
+def test_oracle_arkstep_converges_at_its_order(oracle):
+    P = oracle.Problem(oracle.MANUFACTURED, 24, 24, kx=1.0, ky=1.0)
+    for order in (2, 3):
+        ref, errs = None, []
+        for h in (1e-4, 4e-3, 2e-3):
+            I = oracle.ArkIntegrator(P, P.initial(), implicit=True, order=order, hfixed=h, ls="cg", maxl=500,
+                                     prec="jacobi", msbp=1, epslin=1e-6)
+            assert I.evolve(0.08) == 0
+            if ref is None:
+                ref = I.y.copy()
+            else:
+                errs.append(np.linalg.norm(I.y - ref))
+        assert abs(np.log2(errs[0] / errs[1]) - order) < 0.35
