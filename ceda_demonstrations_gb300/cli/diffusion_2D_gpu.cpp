@@ -6,8 +6,10 @@
 // Problems: --problem periodic (default; the reference code's problem: periodic domain
 // [-pi,pi]x[-6,6], Gaussian x sine initial state, optional --inhomogeneous coefficients),
 // --problem manufactured (the manufactured-solution Dirichlet benchmark problem on [0,1]^2) or unforced.
-// Integrators: rkc, rkl (LSRKStep STS, fused kernels for the Dirichlet problems) and dirk
-// (fixed-step SDIRK2 with the fused Jacobi-PCG, Dirichlet problems, --fixedstep required).
+// Integrators (main.cpp:236-400): rkc, rkl (LSRKStep STS, fused kernels); erk with a negative
+// --order (LSRKStep SSP(2,2), SSP(4,3), SSP(10,4)) or a non-negative one (ARKStep ERK); dirk
+// (ARKStep DIRK of --order 2 or 3 with Newton, CG or GMRES and the Jacobi PSetup/PSolve, or
+// the PFMG-role multigrid in a hypre build's place when a --pfmg option is given).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -73,12 +75,13 @@ static void help()
           "  --inhomogeneous : use spatially-varying diffusion coefficients\n"
           "  --tf <time>     : final time\n"
           "\nIntegrator command line options:\n"
-          "  --integrator <dirk|rkc|rkl> --rtol --atol --fixedstep --controller <0..5: PID PI I ExpGus ImpGus ImExGus>\n"
+          "  --integrator <dirk|erk|rkc|rkl> --rtol --atol --fixedstep --controller <0..5: PID PI I ExpGus ImpGus ImExGus>\n"
+          "  --order <dirk: 2, 3; erk: 2, 3, 4, or -2, -3, -4 for SSP(2,2), SSP(4,3), SSP(10,4)>\n"
           "  --maxsteps --onestep <n> --error --internaleig --smax <stages> --mixed --nographs\n"
           "\nDIRK solver command line options:\n"
           "  --order --nonlinear --ls <cg|gmres> --lsinfo --liniters --epslin --noprec --msbp\n"
           "  --pfmg : CG stage solves preconditioned by the structured multigrid (PFMG role)\n"
-          "  --pfmg_relax <type> : 1 = weighted Jacobi, 2 = symmetric red/black Gauss-Seidel\n"
+          "  --pfmg_relax <type> : 1 = weighted Jacobi, 2 = symmetric, 3 = nonsymmetric red/black Gauss-Seidel\n"
           "  --pfmg_nrelax <num> : pre and post relaxation sweeps\n"
           "\nOutput command line options:\n"
           "  --output <level> (0 = none, 1 = stats, 2 = solution)  --nout <nout>\n"
@@ -180,19 +183,32 @@ int main(int argc, char** argv)
   }
   const bool sts  = (o.integrator == "rkc" || o.integrator == "rkl");
   const bool impl = (o.integrator == "dirk");
-  if (!sts && !impl)
-  {
-    cerr << "ERROR: illegal integrator (this program provides rkc, rkl and dirk)" << endl;
-    return 1;
-  }
-  if (impl && (kind == STS_PROBLEM_PERIODIC || !(o.hfixed > 0.0)))
-  {
-    cerr << "ERROR: dirk runs fixed steps (--fixedstep) on the Dirichlet problems" << endl;
+  const bool expl = (o.integrator == "erk");
+  if (!sts && !impl && !expl)
+  { // main.cpp:134-139
+    cerr << "ERROR: illegal integrator" << endl;
     return 1;
   }
   if (impl && o.ls != "cg" && o.ls != "gmres")
   {
     cerr << "ERROR: illegal linear solver (cg or gmres)" << endl;
+    return 1;
+  }
+  if (impl && o.order != 2 && o.order != 3)
+  {
+    cerr << "ERROR: dirk orders 2 (ARKODE_SDIRK_2_1_2) and 3 (ARKODE_ARK324L2SA_DIRK_4_2_3)" << endl;
+    return 1;
+  }
+  if (expl && !(o.order == -2 || o.order == -3 || o.order == -4 || (o.order >= 2 && o.order <= 4)))
+  { // main.cpp:281-283
+    cerr << "ERROR: illegal SSPRK / ERK order (-2, -3, -4 or 2, 3, 4)" << endl;
+    return 1;
+  }
+  if (impl && o.pfmg && o.prec && kind == STS_PROBLEM_PERIODIC)
+  {
+    cerr << "ERROR: the PFMG-role multigrid preconditioner needs a Dirichlet problem (--problem manufactured "
+            "or unforced)"
+         << endl;
     return 1;
   }
   if (o.controller < STS_ADAPT_PID || o.controller > STS_ADAPT_IMEX_GUS)
@@ -239,33 +255,81 @@ int main(int argc, char** argv)
     uerr = N_VClone_Sts(u);
     N_VScale_Sts(1.0, u, uref);
   }
-  void* mem = nullptr;
-  void* ref = nullptr;
-  void* LS  = nullptr; // generic linear solver of the dirk path (--ls gmres, or cg with --noprec)
-  STS_PFMG mg = nullptr; // multigrid preconditioner of the dirk path (--pfmg)
+  void* mem   = nullptr;
+  void* ref   = nullptr;
+  void* LS    = nullptr; // linear solver of the dirk path (main.cpp:199-231)
+  STS_PFMG mg = nullptr; // multigrid preconditioner of the dirk path (--pfmg*)
   if (sts)
   {
     mem = STS_LSRKStepCreateSTS(STS_Diffusion, 0.0, u, ctx);
-    STS_ARKodeSStolerances(mem, o.rtol, o.atol);
-    STS_ARKodeSetUserData(mem, P);
     STS_LSRKStepSetSTSMethod(mem, o.integrator == "rkc" ? STS_LSRK_RKC_2 : STS_LSRK_RKL_2);
     if (o.internaleig) STS_LSRKStepSetDomEigEstimatorPower(mem, 100, 0.01); // main.cpp:344
     else STS_LSRKStepSetDomEigFn(mem, STS_DomEig);
-    if (o.hfixed > 0.0) STS_ARKodeSetFixedStep(mem, o.hfixed);
-    else STS_ARKodeSetAdaptController(mem, o.controller);
-    STS_ARKodeSetMaxNumSteps(mem, o.maxsteps > 0 ? o.maxsteps : 500);
-    STS_ARKodeSetStopTime(mem, o.tf);
     STS_LSRKStepSetMaxNumStages(mem, o.smax);
     STS_LSRKStepSetMixedPrecision(mem, o.mixed);
     STS_LSRKStepSetUseGraphs(mem, o.graphs);
-    if (o.error)
-    { // main.cpp:387-400: reference integrator at rtol 1e-12
-      ref = STS_LSRKStepCreateSTS(STS_Diffusion, 0.0, u, ctx);
-      STS_ARKodeSStolerances(ref, 1.e-12, o.atol);
-      STS_ARKodeSetUserData(ref, P);
-      STS_LSRKStepSetDomEigFn(ref, STS_DomEig);
-      STS_ARKodeSetMaxNumSteps(ref, 100000LL * (o.maxsteps > 0 ? o.maxsteps : 500));
+  }
+  else if (expl && o.order < 0)
+  { // main.cpp:250-253, 274-292: SSP methods with 2, 4 and 10 stages
+    mem            = STS_LSRKStepCreateSSP(STS_Diffusion, 0.0, u, ctx);
+    const int type = o.order == -2 ? STS_LSRK_SSP_S_2 : (o.order == -3 ? STS_LSRK_SSP_S_3 : STS_LSRK_SSP_10_4);
+    const int ns   = o.order == -2 ? 2 : (o.order == -3 ? 4 : 10);
+    if (STS_LSRKStepSetSSPMethod(mem, type) || STS_LSRKStepSetNumSSPStages(mem, ns))
+    {
+      cerr << "ERROR: " << STS_GetLastError() << endl;
+      return 1;
     }
+  }
+  else
+  { // ARKStep (main.cpp:239-248): explicit ERK or implicit DIRK
+    mem = STS_ARKStepCreate(expl ? STS_Diffusion : nullptr, impl ? STS_Diffusion : nullptr, 0.0, u, ctx);
+    if (!mem || STS_ARKodeSetOrder(mem, o.order))
+    {
+      cerr << "ERROR: " << STS_GetLastError() << endl;
+      return 1;
+    }
+  }
+  if (impl)
+  { // main.cpp:199-231, 300-330
+    const int prectype = o.prec ? STS_PREC_RIGHT : STS_PREC_NONE;
+    LS = (o.ls == "cg") ? STS_SUNLinSol_PCG(u, prectype, o.liniters, ctx) : STS_SUNLinSol_SPGMR(u, prectype, o.liniters, ctx);
+    if (!LS || STS_ARKodeSetLinearSolver(mem, LS, nullptr))
+    {
+      cerr << "ERROR: " << STS_GetLastError() << endl;
+      return 1;
+    }
+    if (o.prec)
+    {
+      if (o.pfmg)
+      { // the hypre build's PFMG preconditioner (preconditioner_hypre.cpp) in its role
+        mg = STS_PFMGCreate(P, o.pfmg_relax, o.pfmg_nrelax);
+        if (!mg)
+        {
+          cerr << "ERROR: " << STS_GetLastError() << endl;
+          return 1;
+        }
+        STS_ARKStepSetPrecData(mem, mg);
+        STS_ARKodeSetPreconditioner(mem, STS_PFMGPSetup, STS_PFMGPSolve);
+      }
+      else STS_ARKodeSetPreconditioner(mem, STS_PSetup, STS_PSolve);
+      STS_ARKodeSetLSetupFrequency(mem, o.msbp);
+    }
+    STS_ARKodeSetEpsLin(mem, o.epslin);
+    if (o.linear) STS_ARKodeSetLinear(mem, 0);
+  }
+  STS_ARKodeSStolerances(mem, o.rtol, o.atol);
+  STS_ARKodeSetUserData(mem, P);
+  if (o.hfixed > 0.0) STS_ARKodeSetFixedStep(mem, o.hfixed);
+  else STS_ARKodeSetAdaptController(mem, o.controller);
+  STS_ARKodeSetMaxNumSteps(mem, o.maxsteps > 0 ? o.maxsteps : 500);
+  STS_ARKodeSetStopTime(mem, o.tf);
+  if (o.error)
+  { // main.cpp:387-400: reference integrator (LSRKStep RKC) at rtol 1e-12
+    ref = STS_LSRKStepCreateSTS(STS_Diffusion, 0.0, u, ctx);
+    STS_ARKodeSStolerances(ref, 1.e-12, o.atol);
+    STS_ARKodeSetUserData(ref, P);
+    STS_LSRKStepSetDomEigFn(ref, STS_DomEig);
+    STS_ARKodeSetMaxNumSteps(ref, 100000LL * (o.maxsteps > 0 ? o.maxsteps : 500));
   }
   int nout      = o.nout;
   int itask     = STS_NORMAL;
@@ -297,7 +361,6 @@ int main(int argc, char** argv)
       STS_ARKodeReset(ref, t, uref);
     }
   }
-  long long lin_iters = 0;
   FILE* sol = nullptr;
   cout << scientific << setprecision(numeric_limits<double>::digits10);
   if (o.output > 0)
@@ -323,41 +386,8 @@ int main(int argc, char** argv)
   for (int iout = 0; iout < nout; ++iout)
   {
     auto t0 = chrono::steady_clock::now();
-    int flag = 0;
-    if (sts)
-    {
-      flag = STS_ARKodeEvolve(mem, tout, u, &t, itask);
-    }
-    else
-    {
-      const double h    = o.hfixed;
-      const int nsteps  = (int)llround((tout - t) / h);
-      long long its     = 0;
-      const double tol  = o.epslin > 0 ? o.epslin : 1e-10;
-      if (o.pfmg && o.prec)
-      { // CG + the PFMG-role multigrid (preconditioner_hypre.cpp in a hypre build)
-        if (!mg) mg = STS_PFMGCreate(P, o.pfmg_relax, o.pfmg_nrelax);
-        flag = mg ? STS_SDIRK2EvolvePFMG(P, mg, u, t, h, nsteps, tol, 100000, &its) : -1;
-      }
-      else if (o.ls == "cg" && o.prec) flag = STS_SDIRK2Evolve(P, u, t, h, nsteps, tol, 100000, &its);
-      else
-      { // generic solver object (main.cpp:209-218): PCG without preconditioner, or SPGMR with
-        // maxl = --liniters, restarted up to 10^5 iterations in total
-        if (!LS)
-        {
-          if (o.ls == "cg") LS = STS_SUNLinSol_PCG(u, STS_PREC_NONE, 100000, ctx);
-          else
-          {
-            const int maxl = o.liniters > 0 ? o.liniters : 20;
-            LS = STS_SUNLinSol_SPGMR(u, o.prec ? STS_PREC_RIGHT : STS_PREC_NONE, maxl, ctx);
-            if (LS) STS_SUNLinSol_SPGMRSetMaxRestarts(LS, std::max(0, 100000 / maxl - 1));
-          }
-        }
-        flag = LS ? STS_SDIRK2EvolveLS(P, LS, o.prec ? 1 : 0, u, t, h, nsteps, tol, &its) : -1;
-      }
-      lin_iters += its;
-      t += nsteps * h;
-    }
+    if (o.error) STS_ARKodeSetStopTime(mem, tout); // main.cpp:437-441
+    const int flag = STS_ARKodeEvolve(mem, tout, u, &t, itask);
     STS_ContextSynchronize(ctx);
     simtime += chrono::duration<double>(chrono::steady_clock::now() - t0).count();
     if (flag < 0)
@@ -395,18 +425,12 @@ int main(int argc, char** argv)
   if (o.error) cout << "Maximum relative error = " << errtot << endl;
   cout << "Total simulation time = " << simtime << endl << endl;
   cout << "Final integrator statistics:" << endl;
-  if (sts)
   {
-    char buf[2048];
+    char buf[4096];
     STS_ARKodePrintAllStats(mem, buf, sizeof(buf));
     cout << buf;
   }
-  else
-  {
-    cout << "Steps                         = " << llround(t / o.hfixed) << "\n"
-         << "Error test fails              = 0\n"
-         << "Linear solver iterations      = " << lin_iters << "\n";
-  }
+  if (mg) cout << "Total PFMG iterations        = " << STS_PFMGNumVCycles(mg) << "\n"; // main.cpp:489-492
   if (kind == STS_PROBLEM_MANUFACTURED)
   {
     N_Vector ex = N_VClone_Sts(u);

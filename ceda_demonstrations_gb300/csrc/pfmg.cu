@@ -1,8 +1,9 @@
 // Structured multigrid preconditioner for the implicit comparator, in the role hypre's PFMG
 // plays in diffusion_2D/preconditioner_hypre.cpp (PSetup :13-108, PSolve :111-180): one
 // V-cycle per PSolve (PFMG MaxIter 1, zero initial guess), semicoarsening one direction at a
-// time, non-Galerkin coarse operators (RAPType 1), weighted Jacobi or symmetric red/black
-// Gauss-Seidel relaxation (--pfmg_relax 1 / 2, the reference's default 2) with --pfmg_nrelax
+// time, non-Galerkin coarse operators (RAPType 1), weighted Jacobi, symmetric or nonsymmetric
+// red/black Gauss-Seidel relaxation (--pfmg_relax 1 / 2 / 3; the reference's default 2, its
+// experiment harness passes 3) with --pfmg_nrelax
 // pre and post sweeps (default 2).
 //
 // The restatement (hypre is not in the reference tree):
@@ -232,7 +233,9 @@ static void pfmg_smooth(STS_PFMG mg, PfmgLevel& l, int sweeps, bool post, cudaSt
     for (int s = 0; s < sweeps; ++s)
       for (int h = 0; h < 2; ++h)
       {
-        const int color = post ? 1 - h : h; // red, black before; black, red after
+        // red then black before; after: black then red (relax 2, symmetric) or red then black
+        // again (relax 3, nonsymmetric)
+        const int color = (post && mg->relax == 2) ? 1 - h : h;
         rbgs_kernel<<<g, b, 0, st>>>(l.nx, l.ny, l.ax, l.ay, l.dinv, l.f, l.u, color);
       }
   }
@@ -268,10 +271,10 @@ static void pfmg_vcycle(STS_PFMG mg, cudaStream_t st)
 
 extern "C" STS_PFMG STS_PFMGCreate(STS_Problem p, int relax_type, int nrelax)
 {
-  if (!p || p->kind == STS_PROBLEM_PERIODIC || (relax_type != 1 && relax_type != 2) || nrelax < 1 || nrelax > 16)
+  if (!p || p->kind == STS_PROBLEM_PERIODIC || relax_type < 1 || relax_type > 3 || nrelax < 1 || nrelax > 16)
   {
-    sts_set_error("STS_PFMGCreate: Dirichlet problems, relax 1 (weighted Jacobi) or 2 (symmetric red/black "
-                  "Gauss-Seidel), 1 <= nrelax <= 16");
+    sts_set_error("STS_PFMGCreate: Dirichlet problems, relax 1 (weighted Jacobi), 2 (symmetric red/black "
+                  "Gauss-Seidel) or 3 (nonsymmetric red/black Gauss-Seidel), 1 <= nrelax <= 16");
     return nullptr;
   }
   STS_PFMG mg = new STS_PFMG_();

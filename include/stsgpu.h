@@ -390,8 +390,10 @@ int STS_SDIRK2EvolveLearned(STS_Problem p, STS_Net net, N_Vector y, double t0, d
  * Structured multigrid preconditioner in the role of hypre PFMG
  * (diffusion_2D/preconditioner_hypre.cpp; --pfmg_relax, --pfmg_nrelax of
  * diffusion_2D.cpp:138-150): one V-cycle per PSolve, semicoarsening in the direction of the
- * stronger coupling, non-Galerkin coarse operators, weighted Jacobi (relax_type 1) or
- * symmetric red/black Gauss-Seidel (2, the reference's default) with nrelax pre and post
+ * stronger coupling, non-Galerkin coarse operators, weighted Jacobi (relax_type 1),
+ * symmetric red/black Gauss-Seidel (2, the reference's default) or nonsymmetric red/black
+ * Gauss-Seidel (3, red then black before and after: not symmetric, so a preconditioner for
+ * GMRES or flexible methods; runtests-diffusion2d.py:60,62 pass it) with nrelax pre and post
  * sweeps. Dirichlet problems.
  * ----------------------------------------------------------------------------------*/
 typedef struct STS_PFMG_* STS_PFMG;

@@ -1779,7 +1779,7 @@ static void pfmg_smooth(orc_pfmg* mg, pfmg_level* l, int sweeps, int post)
     for (int s = 0; s < sweeps; ++s)
       for (int h = 0; h < 2; ++h)
       {
-        int color = post ? 1 - h : h;
+        int color = (post && mg->relax == 2) ? 1 - h : h; /* relax 3: red, black also after */
         for (long j = 0; j < l->ny; ++j)
           for (long i = (j + color) & 1; i < l->nx; i += 2)
           {

@@ -23,6 +23,12 @@ def parse_like_runtests(stdout):
             stats["Fails"] = int(txt[4])
         elif ("Maximum" in txt) and ("relative" in txt):
             stats["Accuracy"] = float(txt[4])
+        elif ("Explicit" in txt) and ("RHS" in txt):
+            stats["FEvals"] += int(txt[5])
+        elif ("Implicit" in txt) and ("RHS" in txt):
+            stats["FEvals"] += int(txt[5])
+        elif ("LS" in txt) and ("RHS" in txt):
+            stats["FEvals"] += int(txt[5])
         elif ("RHS" in txt) and ("fn" in txt):
             stats["FEvals"] += int(txt[4])
         elif "simulation" in txt:
@@ -85,8 +91,12 @@ def test_cli_dirk_and_errors(stslib):
     assert parse_like_runtests(out)["Steps"] == 10
     rc, out, err = run(["--bogus"])
     assert rc == 1 and "Unknown inputs" in err
-    rc, out, err = run(["--integrator", "erk"])
-    assert rc == 1
+    rc, out, err = run(["--integrator", "foo"])
+    assert rc == 1 and "illegal integrator" in err
+    rc, out, err = run(["--integrator", "erk", "--order", "5"])
+    assert rc == 1 and "order" in err
+    rc, out, err = run(["--integrator", "dirk", "--pfmg"])  # periodic problem: no PFMG
+    assert rc == 1 and "Dirichlet" in err
     rc, out, err = run(["--controller", "6"])
     assert rc == 1 and "controller" in err
 
@@ -113,3 +123,36 @@ def test_cli_checkpoint_restart_matches_uninterrupted_run(stslib, tmp_path):
     assert last_rms(out2) == last_rms(full)
     assert l2(out2) == l2(full)
     assert parse_like_runtests(out2)["Steps"] == parse_like_runtests(full)["Steps"]
+
+
+# the solver rows of runtests-diffusion2d.py:59-67,95-103 (the hypre rows run the PFMG-role
+# multigrid in hypre's place; the harness builds them as diffusion_2D_mpi_hypre)
+HARNESS_ROWS = {
+    "dirk2-Jacobi": ["--integrator", "dirk", "--order", "2"],
+    "dirk3-Jacobi": ["--integrator", "dirk", "--order", "3"],
+    "erk2": ["--integrator", "erk", "--order", "-2"],
+    "erk3": ["--integrator", "erk", "--order", "-3"],
+    "erk4": ["--integrator", "erk", "--order", "-4"],
+    "rkc": ["--integrator", "rkc"],
+    "rkl": ["--integrator", "rkl"],
+}
+# the common flags of runtests-diffusion2d.py:76-83
+COMMON = ["--inhomogeneous", "--atol", "1.e-11", "--controller", "2", "--error", "--nonlinear", "--msbp", "1",
+          "--maxsteps", "100000", "--internaleig"]
+
+
+@pytest.mark.parametrize("kx", [0.1, 1.0, 10.0])
+def test_cli_runs_the_reference_harness_rows(stslib, kx):
+    """Every solver row of the reference's experiment harness with its common flags, on one
+    process at the harness's smallest grid (32^2), kx in {0.1, 1, 10}, ky = 0, rtol 1e-4,
+    parsed the harness's way (a shorter final time keeps the --error self-oracle short)."""
+    stslib.lib()
+    for name, row in HARNESS_ROWS.items():
+        args = row + ["--nx", "32", "--ny", "32", "--rtol", "%e" % 1e-4, "--kx", "%e" % kx, "--ky", "%e" % 0.0,
+                      "--tf", "0.2"] + COMMON
+        rc, out, err = run(args)
+        assert rc == 0, (name, err)
+        st = parse_like_runtests(out)
+        assert st["Steps"] > 0 and st["Fails"] is not None and st["FEvals"] > st["Steps"], (name, st)
+        assert st["Accuracy"] is not None and st["Accuracy"] < 5e-3, (name, st)
+        assert st["Runtime"] is not None and st["Runtime"] >= 0.0

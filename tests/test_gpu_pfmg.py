@@ -1,6 +1,6 @@
 """The structured multigrid preconditioner in hypre PFMG's role (diffusion_2D/
 preconditioner_hypre.cpp: one V-cycle per PSolve, semicoarsening, non-Galerkin coarse
-operators, weighted Jacobi or symmetric red/black Gauss-Seidel relaxation) on the GPU against
+operators, weighted Jacobi, symmetric or nonsymmetric red/black Gauss-Seidel relaxation) on the GPU against
 the oracle's restatement, bit for bit: the V-cycle itself and CG with it."""
 import numpy as np
 import pytest
@@ -22,7 +22,7 @@ def smooth_rhs(nx, ny, seed):
 CASES = [(32, 24, 0.3, 1e-2), (64, 64, 1e-3, 1e-2), (130, 66, 0.05, 5e-3), (257, 129, 1.0, 1e-3)]
 
 
-@pytest.mark.parametrize("relax", [1, 2], ids=["jacobi", "rbgs"])
+@pytest.mark.parametrize("relax", [1, 2, 3], ids=["jacobi", "rbgs", "rbgs_nonsym"])
 @pytest.mark.parametrize("nx,ny,ky,gamma", CASES)
 def test_vcycle_bitwise(ctx, stslib, oracle, relax, nx, ny, ky, gamma):
     pk = dict(kind=0, nx=nx, ny=ny, kx=1.0, ky=ky)
@@ -59,8 +59,26 @@ def test_pfmg_rejects_periodic_and_bad_options(ctx, stslib):
     with pytest.raises(stslib.STSError):
         stslib.PFMG(P)
     D = stslib.Problem(ctx, kind=0, nx=32, ny=32)
-    with pytest.raises(stslib.STSError):
-        stslib.PFMG(D, relax=3)
+    for bad in (dict(relax=0), dict(relax=4), dict(nrelax=0), dict(nrelax=17)):
+        with pytest.raises(stslib.STSError):
+            stslib.PFMG(D, **bad)
+
+
+def test_nonsymmetric_rbgs_in_gmres_bitwise(ctx, stslib, oracle):
+    """--pfmg_relax 3 (nonsymmetric red/black Gauss-Seidel, runtests-diffusion2d.py:60,62):
+    the V-cycle is not symmetric, so it preconditions GMRES here; GPU and oracle agree bit for
+    bit in a DIRK run with it (ARKStep, SPGMR)."""
+    pk = dict(kind=0, nx=48, ny=40, kx=1.0, ky=0.2)
+    G, O = stslib.Problem(ctx, **pk), oracle.Problem(**pk)
+    mg = stslib.PFMG(G, relax=3, nrelax=3)
+    ak = dict(implicit=True, order=2, rtol=1e-5, atol=1e-10, controller=2, ls="gmres", maxl=20, msbp=1)
+    I = stslib.ARKStep(ctx, G, 0.0, G.initial(), prec="pfmg", pfmg=mg, **ak)
+    J = oracle.ArkIntegrator(O, O.initial(), prec="pfmg", pfmg_relax=3, pfmg_nrelax=3, **ak)
+    y = G.vector()
+    I.evolve(0.05, y)
+    assert J.evolve(0.05) == 0
+    assert I.stats()["nli"] == J.stats()["nli"] > 0
+    assert np.array_equal(y.numpy(), J.y)
 
 
 def test_sdirk2_pfmg_bitwise(ctx, stslib, oracle):
@@ -82,16 +100,18 @@ def test_cli_dirk_pfmg(stslib):
     stslib.lib()
     exe = os.path.join(os.path.dirname(stslib.__file__), "_build", "diffusion_2D_gpu")
     out = {}
-    for extra in ([], ["--pfmg_relax", "1", "--pfmg_nrelax", "3"], ["--pfmg"]):
+    for extra in ([], ["--pfmg_relax", "1", "--pfmg_nrelax", "3"], ["--pfmg"],
+                  ["--pfmg_relax", "3", "--ls", "gmres"]):
         r = subprocess.run([exe, "--problem", "manufactured", "--nx", "48", "--ny", "48", "--integrator", "dirk",
-                            "--fixedstep", "1e-3", "--tf", "0.01", "--nout", "2"] + extra,
+                            "--fixedstep", "1e-3", "--tf", "0.01", "--nout", "2", "--epslin", "1e-6",
+                            "--liniters", "400"] + extra,
                            capture_output=True, text=True, timeout=600)
         assert r.returncode == 0, r.stderr
         line = [l for l in r.stdout.split("\n") if l.startswith("Relative L2 error vs exact")][0]
-        its = [l for l in r.stdout.split("\n") if l.startswith("Linear solver iterations")][0]
+        its = [l for l in r.stdout.split("\n") if l.startswith("LS iters ")][0]
         out[" ".join(extra)] = (float(line.split("=")[1]), int(its.split("=")[1]))
         if extra:
-            assert "pfmg relaxtype" in r.stdout
+            assert "pfmg relaxtype" in r.stdout and "Total PFMG iterations" in r.stdout
     base = out[""]
     for k, (err, its) in out.items():
         assert abs(err - base[0]) <= 1e-6 * base[0]

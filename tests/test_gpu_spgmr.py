@@ -182,10 +182,10 @@ def test_cli_dirk_gmres_matches_cg(stslib):
     for ls in ("cg", "gmres"):
         r = subprocess.run([exe, "--problem", "manufactured", "--nx", "48", "--ny", "48", "--integrator",
                             "dirk", "--fixedstep", "1e-3", "--tf", "0.01", "--nout", "2", "--ls", ls,
-                            "--liniters", "25"], capture_output=True, text=True, timeout=600)
+                            "--liniters", "25", "--epslin", "1e-6"], capture_output=True, text=True, timeout=600)
         assert r.returncode == 0, r.stderr
         line = [l for l in r.stdout.split("\n") if l.startswith("Relative L2 error vs exact")][0]
-        its = [l for l in r.stdout.split("\n") if l.startswith("Linear solver iterations")][0]
+        its = [l for l in r.stdout.split("\n") if l.startswith("LS iters ")][0]
         outs[ls] = (float(line.split("=")[1]), int(its.split("=")[1]))
     assert abs(outs["gmres"][0] - outs["cg"][0]) <= 1e-6 * outs["cg"][0]
     assert outs["gmres"][1] > 0 and outs["cg"][1] > 0
