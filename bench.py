@@ -142,8 +142,8 @@ def cuda_timer(stream_ptr):
 #   python bench.py --n 6144 --steps 1 --warmup 3 --no-cpu --stage-kernel 6
 #   ncu --set full --clock-control none -k regex:stage32_tma -s 20 -c 2 -o prof_tma \
 #       python bench.py --n 6144 --steps 1 --warmup 3 --no-cpu --stage-kernel 6
-# 6144^2: 578.1 MB per launch -> x (8192/6144)^2 = 1028 MB.
-TRAFFIC_MIXED_STAGE_6144 = 578.1e6
+# 6144^2: 578.6 MB per launch -> x (8192/6144)^2 = 1028.7 MB.
+TRAFFIC_MIXED_STAGE_6144 = 578.6e6
 
 
 def mixed_stage_traffic(n):
