@@ -204,13 +204,6 @@ int main(int argc, char** argv)
     cerr << "ERROR: illegal SSPRK / ERK order (-2, -3, -4 or 2, 3, 4)" << endl;
     return 1;
   }
-  if (impl && o.pfmg && o.prec && kind == STS_PROBLEM_PERIODIC)
-  {
-    cerr << "ERROR: the PFMG-role multigrid preconditioner needs a Dirichlet problem (--problem manufactured "
-            "or unforced)"
-         << endl;
-    return 1;
-  }
   if (o.controller < STS_ADAPT_PID || o.controller > STS_ADAPT_IMEX_GUS)
   {
     cerr << "ERROR: illegal controller (0 PID, 1 PI, 2 I, 3 ExpGus, 4 ImpGus, 5 ImExGus)" << endl;

@@ -39,6 +39,10 @@ struct PfmgLevel {
   double ax = 0, ay = 0, d = 1, dinv = 1, wd = 1;
   int dir = -1;                 // direction coarsened towards the next level (0 x, 1 y), -1 coarsest
   double *f = nullptr, *u = nullptr, *t = nullptr; // right side, iterate, scratch (residual / Jacobi)
+  // periodic problems: coupling of each x face (i + 1/2, i = 0..nx-1, the last one wrapping to
+  // column 0) and y face, on the device and the host
+  double *axf = nullptr, *ayf = nullptr;
+  std::vector<double> hax, hay;
 };
 
 __device__ __forceinline__ double at(const double* u, long long nx, long long ny, long long i, long long j)
@@ -140,7 +144,144 @@ __global__ void prolong_kernel(long long nx, long long ny, int dir, long long cn
   u[j * nx + i] += e;
 }
 
+// ---- periodic levels (the reference's problem): variable face couplings, wrapped neighbours.
+// M u = d u - (w u_W + e u_E + s u_S + n u_N), w = axf[i-1], e = axf[i], s = ayf[j-1], n = ayf[j],
+// d = 1 + ((w + e) + (s + n)).
+__device__ __forceinline__ long long wrap(long long i, long long n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+struct PerPoint {
+  double w, e, s, n, d, uW, uE, uS, uN;
+};
+
+__device__ __forceinline__ PerPoint per_point(const double* u, long long nx, long long ny, long long i, long long j,
+                                              const double* axf, const double* ayf)
+{
+  PerPoint q;
+  const long long iw = wrap(i - 1, nx), ie = wrap(i + 1, nx), js = wrap(j - 1, ny), jn = wrap(j + 1, ny);
+  q.w  = axf[iw];
+  q.e  = axf[i];
+  q.s  = ayf[js];
+  q.n  = ayf[j];
+  q.d  = 1.0 + ((q.w + q.e) + (q.s + q.n));
+  q.uW = u[j * nx + iw];
+  q.uE = u[j * nx + ie];
+  q.uS = u[js * nx + i];
+  q.uN = u[jn * nx + i];
+  return q;
+}
+
+__device__ __forceinline__ double per_m(const PerPoint& q, double uc)
+{
+  double m = q.d * uc;
+  m        = __fma_rn(-q.w, q.uW, m);
+  m        = __fma_rn(-q.e, q.uE, m);
+  m        = __fma_rn(-q.s, q.uS, m);
+  m        = __fma_rn(-q.n, q.uN, m);
+  return m;
+}
+
+__global__ void per_jacobi_kernel(long long nx, long long ny, const double* __restrict__ axf,
+                                  const double* __restrict__ ayf, const double* __restrict__ f,
+                                  const double* __restrict__ in, double* __restrict__ out)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long j = (long long)blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const long long k = j * nx + i;
+  const PerPoint q  = per_point(in, nx, ny, i, j, axf, ayf);
+  const double wd   = PFMG_OMEGA * (1.0 / q.d);
+  out[k]            = __fma_rn(wd, f[k] - per_m(q, in[k]), in[k]);
+}
+
+// one colour of red/black Gauss-Seidel from `in` into `out` (the other colour copied): on odd
+// periodic sizes, where two points of one colour meet across the wrap, the sweep stays
+// deterministic
+__global__ void per_rbgs_kernel(long long nx, long long ny, const double* __restrict__ axf,
+                                const double* __restrict__ ayf, const double* __restrict__ f,
+                                const double* __restrict__ in, double* __restrict__ out, int color)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long j = (long long)blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const long long k = j * nx + i;
+  if (((i + j) & 1) != color)
+  {
+    out[k] = in[k];
+    return;
+  }
+  const PerPoint q = per_point(in, nx, ny, i, j, axf, ayf);
+  double v         = __fma_rn(q.w, q.uW, f[k]);
+  v                = __fma_rn(q.e, q.uE, v);
+  v                = __fma_rn(q.s, q.uS, v);
+  v                = __fma_rn(q.n, q.uN, v);
+  out[k]           = v / q.d;
+}
+
+__global__ void per_residual_kernel(long long nx, long long ny, const double* __restrict__ axf,
+                                    const double* __restrict__ ayf, const double* __restrict__ f,
+                                    const double* __restrict__ u, double* __restrict__ r)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long j = (long long)blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const PerPoint q = per_point(u, nx, ny, i, j, axf, ayf);
+  r[j * nx + i]    = f[j * nx + i] - per_m(q, u[j * nx + i]);
+}
+
+// full weighting with wrap: coarse I <- fine 2I, 2I+1, 2I+2 (mod n)
+__global__ void per_restrict_kernel(long long nx, long long ny, int dir, long long cnx, long long cny,
+                                    const double* __restrict__ r, double* __restrict__ fc)
+{
+  const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long J = (long long)blockIdx.y * blockDim.y + threadIdx.y;
+  if (I >= cnx || J >= cny) return;
+  double a, b, c;
+  if (dir == 0)
+  {
+    a = r[J * nx + 2 * I];
+    b = r[J * nx + 2 * I + 1];
+    c = r[J * nx + wrap(2 * I + 2, nx)];
+  }
+  else
+  {
+    a = r[(2 * J) * nx + I];
+    b = r[(2 * J + 1) * nx + I];
+    c = r[wrap(2 * J + 2, ny) * nx + I];
+  }
+  fc[J * cnx + I] = __fma_rn(0.5, b, 0.25 * (a + c));
+}
+
+// u += P uc with wrap: fine 2Q+1 <- coarse Q, fine 2Q <- mean of coarse Q-1 (mod) and Q
+__global__ void per_prolong_kernel(long long nx, long long ny, int dir, long long cnx, long long cny,
+                                   const double* __restrict__ uc, double* __restrict__ u)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long j = (long long)blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const long long q = dir == 0 ? i : j;
+  const long long Q = q >> 1;
+  double e;
+  if (q & 1) e = dir == 0 ? uc[j * cnx + Q] : uc[Q * cnx + i];
+  else
+  {
+    const long long Qm = wrap(Q - 1, dir == 0 ? cnx : cny);
+    const double lo    = dir == 0 ? uc[j * cnx + Qm] : uc[Qm * cnx + i];
+    const double hi    = dir == 0 ? uc[j * cnx + Q] : uc[Q * cnx + i];
+    e                  = 0.5 * (lo + hi);
+  }
+  u[j * nx + i] += e;
+}
+
 dim3 blocks2d(long long nx, long long ny, dim3 b) { return dim3((unsigned)((nx + b.x - 1) / b.x), (unsigned)((ny + b.y - 1) / b.y)); }
+
+// coarse coupling of two fine faces in series (twice the spacing): 0.5 a1 a2 / (a1 + a2)
+double series_coupling(double a1, double a2)
+{
+  const double s = a1 + a2;
+  if (!(s > 0.0)) return 0.0;
+  const double t = a1 * a2;
+  return 0.5 * (t / s);
+}
 
 } // namespace
 
@@ -149,6 +290,8 @@ struct STS_PFMG_ {
   STS_Context ctx = nullptr; // kept separately: freeing the PFMG must not need the problem
   int relax       = 2;
   int nrelax      = 2;
+  bool periodic   = false;
+  std::vector<double> dxe, dyn; // periodic problems: the problem's face coefficients (host copy)
   double gamma    = NAN; // the gamma the hierarchy and graph were built for
   std::vector<PfmgLevel> L;
   cudaGraphExec_t graph = nullptr;
@@ -162,6 +305,8 @@ static void pfmg_free_levels(STS_PFMG mg)
     cudaFree(l.f);
     cudaFree(l.u);
     cudaFree(l.t);
+    if (l.axf) cudaFree(l.axf);
+    if (l.ayf) cudaFree(l.ayf);
   }
   mg->L.clear();
   if (mg->graph) cudaGraphExecDestroy(mg->graph);
@@ -169,9 +314,67 @@ static void pfmg_free_levels(STS_PFMG mg)
 }
 
 // the level hierarchy of M = I - gamma A (host rules, restated in the oracle)
+// periodic problems: per-face couplings; coarsening of an even direction with a coupling at
+// least the other's (largest face), the coarse faces two fine faces in series
+static bool pfmg_build_periodic(STS_PFMG mg, double gamma)
+{
+  STS_Problem p = mg->p;
+  PfmgLevel l;
+  l.nx = p->nx;
+  l.ny = p->ny;
+  l.hax.resize(l.nx);
+  l.hay.resize(l.ny);
+  for (long long i = 0; i < l.nx; ++i) l.hax[i] = gamma * mg->dxe[i];
+  for (long long j = 0; j < l.ny; ++j) l.hay[j] = gamma * mg->dyn[j];
+  for (int lev = 0; lev < PFMG_MAX_LEVELS; ++lev)
+  {
+    if (lev > 0)
+    {
+      const PfmgLevel& f = mg->L.back();
+      PfmgLevel c;
+      c.nx  = f.dir == 0 ? f.nx / 2 : f.nx;
+      c.ny  = f.dir == 1 ? f.ny / 2 : f.ny;
+      c.hax = f.hax;
+      c.hay = f.hay;
+      if (f.dir == 0)
+      {
+        c.hax.resize(c.nx);
+        for (long long I = 0; I < c.nx; ++I) c.hax[I] = series_coupling(f.hax[2 * I + 1], f.hax[(2 * I + 2) % f.nx]);
+      }
+      else
+      {
+        c.hay.resize(c.ny);
+        for (long long J = 0; J < c.ny; ++J) c.hay[J] = series_coupling(f.hay[2 * J + 1], f.hay[(2 * J + 2) % f.ny]);
+      }
+      l = c;
+    }
+    double axm = 0.0, aym = 0.0;
+    for (double a : l.hax) axm = a > axm ? a : axm;
+    for (double a : l.hay) aym = a > aym ? a : aym;
+    const bool cx = l.nx > 2 && l.nx % 2 == 0, cy = l.ny > 2 && l.ny % 2 == 0;
+    if (cx && (axm >= aym || !cy)) l.dir = 0;
+    else if (cy) l.dir = 1;
+    else l.dir = -1;
+    const size_t bytes = (size_t)(l.nx * l.ny) * sizeof(double);
+    if (!STS_CUDA_OK(cudaMalloc(&l.f, bytes)) || !STS_CUDA_OK(cudaMalloc(&l.u, bytes)) ||
+        !STS_CUDA_OK(cudaMalloc(&l.t, bytes)) || !STS_CUDA_OK(cudaMalloc(&l.axf, l.nx * sizeof(double))) ||
+        !STS_CUDA_OK(cudaMalloc(&l.ayf, l.ny * sizeof(double))) ||
+        !STS_CUDA_OK(cudaMemcpy(l.axf, l.hax.data(), l.nx * sizeof(double), cudaMemcpyHostToDevice)) ||
+        !STS_CUDA_OK(cudaMemcpy(l.ayf, l.hay.data(), l.ny * sizeof(double), cudaMemcpyHostToDevice)))
+    {
+      mg->L.push_back(l);
+      return false;
+    }
+    mg->L.push_back(l);
+    if (l.dir < 0) break;
+  }
+  return mg->L.back().dir < 0;
+}
+
 static bool pfmg_build(STS_PFMG mg, double gamma)
 {
   pfmg_free_levels(mg);
+  if (mg->periodic) return pfmg_build_periodic(mg, gamma);
   STS_Problem p = mg->p;
   PfmgLevel l0;
   l0.nx = p->nx;
@@ -217,6 +420,32 @@ static bool pfmg_build(STS_PFMG mg, double gamma)
 static void pfmg_smooth(STS_PFMG mg, PfmgLevel& l, int sweeps, bool post, cudaStream_t st)
 {
   const dim3 b(32, 8);
+  if (mg->periodic)
+  { // every half sweep reads one buffer and writes the other; the result ends in u
+    const size_t bytes = (size_t)(l.nx * l.ny) * sizeof(double);
+    int nw             = 0;
+    for (int s = 0; s < sweeps; ++s)
+    {
+      if (mg->relax == 1)
+      {
+        const double* in = (nw & 1) ? l.t : l.u;
+        double* out      = (nw & 1) ? l.u : l.t;
+        per_jacobi_kernel<<<blocks2d(l.nx, l.ny, b), b, 0, st>>>(l.nx, l.ny, l.axf, l.ayf, l.f, in, out);
+        ++nw;
+      }
+      else
+        for (int h = 0; h < 2; ++h)
+        {
+          const int color  = (post && mg->relax == 2) ? 1 - h : h;
+          const double* in = (nw & 1) ? l.t : l.u;
+          double* out      = (nw & 1) ? l.u : l.t;
+          per_rbgs_kernel<<<blocks2d(l.nx, l.ny, b), b, 0, st>>>(l.nx, l.ny, l.axf, l.ayf, l.f, in, out, color);
+          ++nw;
+        }
+    }
+    if (nw & 1) cudaMemcpyAsync(l.u, l.t, bytes, cudaMemcpyDeviceToDevice, st);
+    return;
+  }
   if (mg->relax == 1)
   {
     for (int s = 0; s < sweeps; ++s)
@@ -256,32 +485,53 @@ static void pfmg_vcycle(STS_PFMG mg, cudaStream_t st)
       break;
     }
     pfmg_smooth(mg, l, mg->nrelax, false, st);
-    residual_kernel<<<blocks2d(l.nx, l.ny, b), b, 0, st>>>(l.nx, l.ny, l.ax, l.ay, l.d, l.f, l.u, l.t);
     PfmgLevel& c = mg->L[lev + 1];
+    if (mg->periodic)
+    {
+      per_residual_kernel<<<blocks2d(l.nx, l.ny, b), b, 0, st>>>(l.nx, l.ny, l.axf, l.ayf, l.f, l.u, l.t);
+      per_restrict_kernel<<<blocks2d(c.nx, c.ny, b), b, 0, st>>>(l.nx, l.ny, l.dir, c.nx, c.ny, l.t, c.f);
+      continue;
+    }
+    residual_kernel<<<blocks2d(l.nx, l.ny, b), b, 0, st>>>(l.nx, l.ny, l.ax, l.ay, l.d, l.f, l.u, l.t);
     restrict_kernel<<<blocks2d(c.nx, c.ny, b), b, 0, st>>>(l.nx, l.ny, l.dir, c.nx, c.ny, l.t, c.f);
   }
   for (int lev = nl - 2; lev >= 0; --lev)
   {
     PfmgLevel& l = mg->L[lev];
     const PfmgLevel& c = mg->L[lev + 1];
-    prolong_kernel<<<blocks2d(l.nx, l.ny, b), b, 0, st>>>(l.nx, l.ny, l.dir, c.nx, c.ny, c.u, l.u);
+    if (mg->periodic)
+      per_prolong_kernel<<<blocks2d(l.nx, l.ny, b), b, 0, st>>>(l.nx, l.ny, l.dir, c.nx, c.ny, c.u, l.u);
+    else prolong_kernel<<<blocks2d(l.nx, l.ny, b), b, 0, st>>>(l.nx, l.ny, l.dir, c.nx, c.ny, c.u, l.u);
     pfmg_smooth(mg, l, mg->nrelax, true, st);
   }
 }
 
 extern "C" STS_PFMG STS_PFMGCreate(STS_Problem p, int relax_type, int nrelax)
 {
-  if (!p || p->kind == STS_PROBLEM_PERIODIC || relax_type < 1 || relax_type > 3 || nrelax < 1 || nrelax > 16)
+  if (!p || relax_type < 1 || relax_type > 3 || nrelax < 1 || nrelax > 16)
   {
-    sts_set_error("STS_PFMGCreate: Dirichlet problems, relax 1 (weighted Jacobi), 2 (symmetric red/black "
-                  "Gauss-Seidel) or 3 (nonsymmetric red/black Gauss-Seidel), 1 <= nrelax <= 16");
+    sts_set_error("STS_PFMGCreate: relax 1 (weighted Jacobi), 2 (symmetric red/black Gauss-Seidel) or 3 "
+                  "(nonsymmetric red/black Gauss-Seidel), 1 <= nrelax <= 16");
     return nullptr;
   }
-  STS_PFMG mg = new STS_PFMG_();
-  mg->p       = p;
-  mg->ctx     = p->ctx;
-  mg->relax   = relax_type;
-  mg->nrelax  = nrelax;
+  STS_PFMG mg   = new STS_PFMG_();
+  mg->p         = p;
+  mg->ctx       = p->ctx;
+  mg->relax     = relax_type;
+  mg->nrelax    = nrelax;
+  mg->periodic  = p->kind == STS_PROBLEM_PERIODIC;
+  if (mg->periodic)
+  { // the face coefficients / d^2 of the problem's operator (diffusion.cpp:36-46)
+    mg->dxe.resize(p->nx);
+    mg->dyn.resize(p->ny);
+    ctx_activate(p->ctx);
+    if (!STS_CUDA_OK(cudaMemcpy(mg->dxe.data(), p->dev.Dxe, p->nx * sizeof(double), cudaMemcpyDeviceToHost)) ||
+        !STS_CUDA_OK(cudaMemcpy(mg->dyn.data(), p->dev.Dyn, p->ny * sizeof(double), cudaMemcpyDeviceToHost)))
+    {
+      delete mg;
+      return nullptr;
+    }
+  }
   return mg;
 }
 

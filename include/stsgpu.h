@@ -394,7 +394,9 @@ int STS_SDIRK2EvolveLearned(STS_Problem p, STS_Net net, N_Vector y, double t0, d
  * symmetric red/black Gauss-Seidel (2, the reference's default) or nonsymmetric red/black
  * Gauss-Seidel (3, red then black before and after: not symmetric, so a preconditioner for
  * GMRES or flexible methods; runtests-diffusion2d.py:60,62 pass it) with nrelax pre and post
- * sweeps. Dirichlet problems.
+ * sweeps. Dirichlet problems (constant couplings, coarse coupling a/4) and the periodic problem
+ * (per-face couplings, including k (1 + 0.99 sin); coarse faces two fine faces in series,
+ * 0.5 a1 a2 / (a1 + a2); an odd direction is not coarsened).
  * ----------------------------------------------------------------------------------*/
 typedef struct STS_PFMG_* STS_PFMG;
 STS_PFMG STS_PFMGCreate(STS_Problem p, int relax_type, int nrelax);

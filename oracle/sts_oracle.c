@@ -1725,8 +1725,10 @@ int orc_spfgmr(const orc_prob* p, double gamma, int jacobi, const double* b, dou
  * Structured multigrid V-cycle in the role of hypre PFMG (diffusion_2D/preconditioner_hypre.cpp
  * :13-180): semicoarsening in the direction of the larger coupling (coarse point I = fine
  * 2I + 1, coupling / 4), non-Galerkin coarse operators d = 1 + 2 (a_x + a_y), linear
- * interpolation, full-weighting restriction, weighted Jacobi (omega 0.8) or symmetric red/black
- * Gauss-Seidel relaxation, 8 sweeps on the coarsest level (at most 2 x 2); the product's
+ * interpolation, full-weighting restriction, weighted Jacobi (omega 0.8), symmetric or
+ * nonsymmetric red/black Gauss-Seidel relaxation, 8 sweeps on the coarsest level (at most 2 x 2);
+ * on the periodic problem per-face couplings (coarse faces: two fine faces in series, 0.5 a1 a2 /
+ * (a1 + a2)), wrapped neighbours and sweeps from one buffer into the other; the product's
  * operation order (csrc/pfmg.cu).
  * ----------------------------------------------------------------------------------*/
 typedef struct {
@@ -1734,12 +1736,206 @@ typedef struct {
   double ax, ay, d, dinv, wd;
   int dir;
   double *f, *u, *t;
+  double *axf, *ayf; /* periodic: coupling of each x / y face (i + 1/2, wrapping) */
 } pfmg_level;
 
 struct orc_pfmg {
-  int relax, nrelax, nl;
+  int relax, nrelax, nl, periodic;
   pfmg_level L[64];
 };
+
+/* ---- periodic levels (csrc/pfmg.cu per_* kernels): M u = d u - (w uW + e uE + s uS + n uN) */
+static long pwrap(long i, long n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+typedef struct {
+  double w, e, s, n, d, uW, uE, uS, uN;
+} per_pt;
+
+static per_pt per_point(const double* u, const pfmg_level* l, long i, long j)
+{
+  per_pt q;
+  long iw = pwrap(i - 1, l->nx), ie = pwrap(i + 1, l->nx), js = pwrap(j - 1, l->ny), jn = pwrap(j + 1, l->ny);
+  q.w  = l->axf[iw];
+  q.e  = l->axf[i];
+  q.s  = l->ayf[js];
+  q.n  = l->ayf[j];
+  q.d  = 1.0 + ((q.w + q.e) + (q.s + q.n));
+  q.uW = u[j * l->nx + iw];
+  q.uE = u[j * l->nx + ie];
+  q.uS = u[js * l->nx + i];
+  q.uN = u[jn * l->nx + i];
+  return q;
+}
+
+static double per_m(const per_pt* q, double uc)
+{
+  double m = q->d * uc;
+  m        = fma(-q->w, q->uW, m);
+  m        = fma(-q->e, q->uE, m);
+  m        = fma(-q->s, q->uS, m);
+  m        = fma(-q->n, q->uN, m);
+  return m;
+}
+
+static double series_coupling(double a1, double a2)
+{
+  double s = a1 + a2;
+  if (!(s > 0.0)) return 0.0;
+  double t = a1 * a2;
+  return 0.5 * (t / s);
+}
+
+static void per_smooth(orc_pfmg* mg, pfmg_level* l, int sweeps, int post)
+{
+  long n = l->nx * l->ny;
+  int nw = 0;
+  for (int s = 0; s < sweeps; ++s)
+  {
+    int halves = mg->relax == 1 ? 1 : 2;
+    for (int h = 0; h < halves; ++h)
+    {
+      const double* in = (nw & 1) ? l->t : l->u;
+      double* out      = (nw & 1) ? l->u : l->t;
+      int color        = (post && mg->relax == 2) ? 1 - h : h;
+      for (long j = 0; j < l->ny; ++j)
+        for (long i = 0; i < l->nx; ++i)
+        {
+          long k = j * l->nx + i;
+          if (mg->relax == 1)
+          {
+            per_pt q  = per_point(in, l, i, j);
+            double wd = 0.8 * (1.0 / q.d);
+            out[k]    = fma(wd, l->f[k] - per_m(&q, in[k]), in[k]);
+          }
+          else if (((i + j) & 1) != color) out[k] = in[k];
+          else
+          {
+            per_pt q = per_point(in, l, i, j);
+            double v = fma(q.w, q.uW, l->f[k]);
+            v        = fma(q.e, q.uE, v);
+            v        = fma(q.s, q.uS, v);
+            v        = fma(q.n, q.uN, v);
+            out[k]   = v / q.d;
+          }
+        }
+      ++nw;
+    }
+  }
+  if (nw & 1) memcpy(l->u, l->t, n * sizeof(double));
+}
+
+static orc_pfmg* pfmg_create_periodic(const orc_prob* p, double gamma, int relax, int nrelax)
+{
+  orc_pfmg* mg = (orc_pfmg*)calloc(1, sizeof(orc_pfmg));
+  mg->relax    = relax;
+  mg->nrelax   = nrelax;
+  mg->periodic = 1;
+  for (int lev = 0; lev < 64; ++lev)
+  {
+    pfmg_level l;
+    memset(&l, 0, sizeof(l));
+    if (lev == 0)
+    {
+      l.nx  = p->nx;
+      l.ny  = p->ny;
+      l.axf = (double*)malloc(l.nx * sizeof(double));
+      l.ayf = (double*)malloc(l.ny * sizeof(double));
+      for (long i = 0; i < l.nx; ++i) l.axf[i] = gamma * p->Dxe[i];
+      for (long j = 0; j < l.ny; ++j) l.ayf[j] = gamma * p->Dyn[j];
+    }
+    else
+    {
+      const pfmg_level* f = &mg->L[lev - 1];
+      l.nx  = f->dir == 0 ? f->nx / 2 : f->nx;
+      l.ny  = f->dir == 1 ? f->ny / 2 : f->ny;
+      l.axf = (double*)malloc(l.nx * sizeof(double));
+      l.ayf = (double*)malloc(l.ny * sizeof(double));
+      for (long I = 0; I < l.nx; ++I)
+        l.axf[I] = f->dir == 0 ? series_coupling(f->axf[2 * I + 1], f->axf[(2 * I + 2) % f->nx]) : f->axf[I];
+      for (long J = 0; J < l.ny; ++J)
+        l.ayf[J] = f->dir == 1 ? series_coupling(f->ayf[2 * J + 1], f->ayf[(2 * J + 2) % f->ny]) : f->ayf[J];
+    }
+    double axm = 0.0, aym = 0.0;
+    for (long i = 0; i < l.nx; ++i) axm = l.axf[i] > axm ? l.axf[i] : axm;
+    for (long j = 0; j < l.ny; ++j) aym = l.ayf[j] > aym ? l.ayf[j] : aym;
+    int cx = l.nx > 2 && l.nx % 2 == 0, cy = l.ny > 2 && l.ny % 2 == 0;
+    if (cx && (axm >= aym || !cy)) l.dir = 0;
+    else if (cy) l.dir = 1;
+    else l.dir = -1;
+    long n = l.nx * l.ny;
+    l.f    = (double*)calloc(n, sizeof(double));
+    l.u    = (double*)calloc(n, sizeof(double));
+    l.t    = (double*)calloc(n, sizeof(double));
+    mg->L[lev] = l;
+    mg->nl     = lev + 1;
+    if (l.dir < 0) break;
+  }
+  return mg;
+}
+
+static void per_apply(orc_pfmg* mg, const double* r, double* z)
+{
+  pfmg_level* L = mg->L;
+  memcpy(L[0].f, r, (size_t)(L[0].nx * L[0].ny) * sizeof(double));
+  for (int lev = 0; lev < mg->nl; ++lev)
+  {
+    pfmg_level* l = &L[lev];
+    memset(l->u, 0, (size_t)(l->nx * l->ny) * sizeof(double));
+    if (l->dir < 0)
+    {
+      per_smooth(mg, l, 8, 0);
+      break;
+    }
+    per_smooth(mg, l, mg->nrelax, 0);
+    for (long j = 0; j < l->ny; ++j)
+      for (long i = 0; i < l->nx; ++i)
+      {
+        per_pt q               = per_point(l->u, l, i, j);
+        l->t[j * l->nx + i] = l->f[j * l->nx + i] - per_m(&q, l->u[j * l->nx + i]);
+      }
+    pfmg_level* c = &L[lev + 1];
+    for (long J = 0; J < c->ny; ++J)
+      for (long I = 0; I < c->nx; ++I)
+      {
+        double a, b, cc;
+        if (l->dir == 0)
+        {
+          a  = l->t[J * l->nx + 2 * I];
+          b  = l->t[J * l->nx + 2 * I + 1];
+          cc = l->t[J * l->nx + pwrap(2 * I + 2, l->nx)];
+        }
+        else
+        {
+          a  = l->t[(2 * J) * l->nx + I];
+          b  = l->t[(2 * J + 1) * l->nx + I];
+          cc = l->t[pwrap(2 * J + 2, l->ny) * l->nx + I];
+        }
+        c->f[J * c->nx + I] = fma(0.5, b, 0.25 * (a + cc));
+      }
+  }
+  for (int lev = mg->nl - 2; lev >= 0; --lev)
+  {
+    pfmg_level* l = &L[lev];
+    pfmg_level* c = &L[lev + 1];
+    for (long j = 0; j < l->ny; ++j)
+      for (long i = 0; i < l->nx; ++i)
+      {
+        long q = l->dir == 0 ? i : j, Q = q >> 1;
+        double e;
+        if (q & 1) e = l->dir == 0 ? c->u[j * c->nx + Q] : c->u[Q * c->nx + i];
+        else
+        {
+          long Qm   = pwrap(Q - 1, l->dir == 0 ? c->nx : c->ny);
+          double lo = l->dir == 0 ? c->u[j * c->nx + Qm] : c->u[Qm * c->nx + i];
+          double hi = l->dir == 0 ? c->u[j * c->nx + Q] : c->u[Q * c->nx + i];
+          e         = 0.5 * (lo + hi);
+        }
+        l->u[j * l->nx + i] += e;
+      }
+    per_smooth(mg, l, mg->nrelax, 1);
+  }
+  memcpy(z, L[0].u, (size_t)(L[0].nx * L[0].ny) * sizeof(double));
+}
 
 static double pat(const double* u, long nx, long ny, long i, long j)
 {
@@ -1795,12 +1991,14 @@ static void pfmg_smooth(orc_pfmg* mg, pfmg_level* l, int sweeps, int post)
 
 static orc_pfmg* pfmg_create(const orc_prob* p, double gamma, int relax, int nrelax)
 {
+  if (p->kind == ORC_PERIODIC) return pfmg_create_periodic(p, gamma, relax, nrelax);
   orc_pfmg* mg = (orc_pfmg*)calloc(1, sizeof(orc_pfmg));
   mg->relax    = relax;
   mg->nrelax   = nrelax;
   for (int lev = 0; lev < 64; ++lev)
   {
     pfmg_level l;
+    memset(&l, 0, sizeof(l));
     if (lev == 0)
     {
       l.nx = p->nx;
@@ -1847,12 +2045,19 @@ static void pfmg_destroy(orc_pfmg* mg)
     free(mg->L[k].f);
     free(mg->L[k].u);
     free(mg->L[k].t);
+    free(mg->L[k].axf);
+    free(mg->L[k].ayf);
   }
   free(mg);
 }
 
 static void pfmg_apply(orc_pfmg* mg, const double* r, double* z)
 {
+  if (mg->periodic)
+  {
+    per_apply(mg, r, z);
+    return;
+  }
   pfmg_level* L = mg->L;
   memcpy(L[0].f, r, (size_t)(L[0].nx * L[0].ny) * sizeof(double));
   for (int lev = 0; lev < mg->nl; ++lev)

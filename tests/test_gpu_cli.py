@@ -95,8 +95,8 @@ def test_cli_dirk_and_errors(stslib):
     assert rc == 1 and "illegal integrator" in err
     rc, out, err = run(["--integrator", "erk", "--order", "5"])
     assert rc == 1 and "order" in err
-    rc, out, err = run(["--integrator", "dirk", "--pfmg"])  # periodic problem: no PFMG
-    assert rc == 1 and "Dirichlet" in err
+    rc, out, err = run(["--integrator", "dirk", "--order", "4"])
+    assert rc == 1 and "order" in err
     rc, out, err = run(["--controller", "6"])
     assert rc == 1 and "controller" in err
 
@@ -126,10 +126,13 @@ def test_cli_checkpoint_restart_matches_uninterrupted_run(stslib, tmp_path):
 
 
 # the solver rows of runtests-diffusion2d.py:59-67,95-103 (the hypre rows run the PFMG-role
-# multigrid in hypre's place; the harness builds them as diffusion_2D_mpi_hypre)
+# multigrid in hypre's place, with the harness's --pfmg_relax 3 and the --pfmg_nrelax of its
+# one-process grid, :23-24,89; the harness builds them as diffusion_2D_mpi_hypre)
 HARNESS_ROWS = {
     "dirk2-Jacobi": ["--integrator", "dirk", "--order", "2"],
+    "dirk2-hypre": ["--integrator", "dirk", "--order", "2", "--pfmg_relax", "3", "--pfmg_nrelax", "3"],
     "dirk3-Jacobi": ["--integrator", "dirk", "--order", "3"],
+    "dirk3-hypre": ["--integrator", "dirk", "--order", "3", "--pfmg_relax", "3", "--pfmg_nrelax", "3"],
     "erk2": ["--integrator", "erk", "--order", "-2"],
     "erk3": ["--integrator", "erk", "--order", "-3"],
     "erk4": ["--integrator", "erk", "--order", "-4"],
@@ -156,3 +159,5 @@ def test_cli_runs_the_reference_harness_rows(stslib, kx):
         assert st["Steps"] > 0 and st["Fails"] is not None and st["FEvals"] > st["Steps"], (name, st)
         assert st["Accuracy"] is not None and st["Accuracy"] < 5e-3, (name, st)
         assert st["Runtime"] is not None and st["Runtime"] >= 0.0
+        if "hypre" in name:
+            assert "Total PFMG iterations" in out

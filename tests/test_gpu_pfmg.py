@@ -54,14 +54,64 @@ def test_pcg_pfmg_bitwise_and_fast(ctx, stslib, oracle, relax):
     assert it * 10 < it_j  # multigrid against the Jacobi-preconditioned iteration count
 
 
-def test_pfmg_rejects_periodic_and_bad_options(ctx, stslib):
-    P = stslib.Problem(ctx, stslib.PERIODIC, 32, 32, 1.0, 1.0)
-    with pytest.raises(stslib.STSError):
-        stslib.PFMG(P)
+def test_pfmg_rejects_bad_options(ctx, stslib):
     D = stslib.Problem(ctx, kind=0, nx=32, ny=32)
     for bad in (dict(relax=0), dict(relax=4), dict(nrelax=0), dict(nrelax=17)):
         with pytest.raises(stslib.STSError):
             stslib.PFMG(D, **bad)
+
+
+PERIODIC_CASES = [(32, 32, 0.0, False, 5e-2), (48, 40, 0.3, True, 1e-2), (30, 18, 1.0, True, 2e-2),
+                  (64, 16, 0.05, False, 1e-3)]
+
+
+@pytest.mark.parametrize("relax", [1, 2, 3], ids=["jacobi", "rbgs", "rbgs_nonsym"])
+@pytest.mark.parametrize("nx,ny,ky,inh,gamma", PERIODIC_CASES)
+def test_periodic_vcycle_bitwise(ctx, stslib, oracle, relax, nx, ny, ky, inh, gamma):
+    """The V-cycle on the reference's periodic problem (per-face couplings, homogeneous or
+    k (1 + 0.99 sin), ky = 0 as in the harness, odd coarse sizes), GPU and oracle bit for bit."""
+    pk = dict(kind=2, nx=nx, ny=ny, kx=1.0, ky=ky, inhomogeneous=inh)
+    G = stslib.Problem(ctx, **pk)
+    r = np.random.default_rng(nx * ny).standard_normal(nx * ny)
+    mg = stslib.PFMG(G, relax=relax, nrelax=2)
+    R = stslib.NVector.from_numpy(ctx, r)
+    Z = G.vector()
+    mg.psolve(R, Z, gamma)
+    z_o, nl = oracle.Problem(**pk).pfmg_vcycle(gamma, r, relax=relax, nrelax=2)
+    assert mg.levels() == nl
+    assert np.array_equal(Z.numpy(), z_o)
+
+
+def test_periodic_pcg_pfmg_bitwise_and_fast(ctx, stslib, oracle):
+    pk = dict(kind=2, nx=64, ny=64, kx=1.0, ky=0.0, inhomogeneous=True)
+    G, O = stslib.Problem(ctx, **pk), oracle.Problem(**pk)
+    b = np.random.default_rng(9).standard_normal(64 * 64)
+    mg = stslib.PFMG(G, relax=2)
+    B = stslib.NVector.from_numpy(ctx, b)
+    X = G.vector()
+    it, rel, rc = stslib.implicit_solve_pfmg(G, 0.05, mg, B, X, tol=1e-10)
+    x_o, rc_o, it_o, rel_o = O.pcg_pfmg(0.05, b, tol=1e-10, relax=2)
+    assert rc == rc_o == 0 and it == it_o and rel == rel_o <= 1e-10
+    assert np.array_equal(X.numpy(), x_o)
+    _, rc_j, it_j, _ = O.pcg_generic(0.05, b, tol=1e-10, maxl=100000, jacobi=True)
+    assert it * 4 < it_j
+
+
+def test_dirk_with_periodic_pfmg_bitwise(ctx, stslib, oracle):
+    """ARKStep DIRK on the harness's problem with the PFMG-role preconditioner, --pfmg_relax 3
+    --pfmg_nrelax 3 (runtests-diffusion2d.py:60,62,89), GPU and oracle bit for bit."""
+    pk = dict(kind=2, nx=32, ny=32, kx=1.0, ky=0.0, inhomogeneous=True)
+    G, O = stslib.Problem(ctx, **pk), oracle.Problem(**pk)
+    mg = stslib.PFMG(G, relax=3, nrelax=3)
+    ak = dict(implicit=True, order=3, rtol=1e-4, atol=1e-11, controller=2, ls="cg", maxl=20, msbp=1)
+    I = stslib.ARKStep(ctx, G, 0.0, G.initial(), prec="pfmg", pfmg=mg, **ak)
+    J = oracle.ArkIntegrator(O, O.initial(), prec="pfmg", pfmg_relax=3, pfmg_nrelax=3, **ak)
+    y = G.vector()
+    I.evolve(0.2, y)
+    assert J.evolve(0.2) == 0
+    sg, so = I.stats(), J.stats()
+    assert (sg["nst"], sg["nli"], sg["nps"]) == (so["nst"], so["nli"], so["nps"])
+    assert np.array_equal(y.numpy(), J.y)
 
 
 def test_nonsymmetric_rbgs_in_gmres_bitwise(ctx, stslib, oracle):
