@@ -5,7 +5,7 @@
  * problem callbacks). Each declaration names the reference interface it replaces
  * (file:line, paths relative to the sundials-codes/ceda-demonstrations tree). SUNDIALS is
  * an empty submodule there, so SUNDIALS functions are cited at their call sites in
- * diffusion_2D/main.cpp and gkeyll_diffusion/*.c.
+ * diffusion_2D/main.cpp and the gkeyll_diffusion C sources.
  *
  * Conventions
  *   - plain C types only: double, float, int, long long, opaque handles, raw pointers;
