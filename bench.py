@@ -431,6 +431,40 @@ def run_full(args):
     print(json.dumps({"full_solve": out, "n": n, "tf": tf, "kx": kx, "ky": ky}), flush=True)
 
 
+def run_reference_mode(args):
+    """The reference's own problem (periodic, Gaussian x sine initial state, inhomogeneous
+    faces k (1 + 0.99 sin)) at 2048^2, RKL2 rtol 1e-5: FP64 and mixed reference mode from
+    t = 0.01 (untimed) to t = 0.05 (timed, CUDA events), DOF-stages/s of each."""
+    import numpy as np
+    import ceda_demonstrations_gb300 as sts
+    ctx = sts.Context(0)
+    timer = cuda_timer(ctx.stream)
+    n = args.refmode_n
+    out = {}
+    ys = {}
+    for mixed in (False, True):
+        G = sts.Problem(ctx, sts.PERIODIC, n, n, 1.0, 1.0, inhomogeneous=True)
+        I = sts.LSRKStep(ctx, G, 0.0, G.initial(), method=sts.RKL, rtol=1e-5, atol=1e-9, mixed=mixed,
+                         maxsteps=1000000)
+        y = G.vector()
+        I.evolve(0.01, y)
+        ctx.synchronize()
+        s0 = I.stats()
+        with timer() as tm:
+            I.evolve(0.05, y)
+        s1 = I.stats()
+        dof = n * n * (s1["nfe"] - s0["nfe"])
+        key = "mixed" if mixed else "fp64"
+        out[key] = {"seconds": tm.ms / 1e3, "steps": s1["nst"] - s0["nst"], "rhs_evals": s1["nfe"] - s0["nfe"],
+                    "stage_max": s1["stage_max"], "dof_stages_per_s": dof / (tm.ms / 1e3)}
+        ys[mixed] = y.numpy()
+        print(key, json.dumps(out[key]), flush=True)
+        I.free()
+    rel = float(np.linalg.norm(ys[True] - ys[False]) / np.linalg.norm(ys[False]))
+    print(json.dumps({"reference_mode": out, "n": n, "mixed_vs_fp64_rel_l2_adaptive": rel,
+                      "speedup": out["fp64"]["seconds"] / out["mixed"]["seconds"]}), flush=True)
+
+
 def run_batch(args):
     """512 independent heat problems in one persistent launch (n uniform from
     {64,...,512}, kx, ky log-uniform in [1e-2, 1], 8 random sine modes, RKL2 rtol 1e-6 to
@@ -689,6 +723,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--stage-kernel", type=int, default=0,
                     help="mixed stage kernel: 0 autotune, 1 register marching, 2+k TMA configuration k")
+    ap.add_argument("--reference-mode", action="store_true")
+    ap.add_argument("--refmode-n", type=int, default=2048)
     ap.add_argument("--batch", action="store_true")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-tf", type=float, default=0.01)
@@ -709,6 +745,8 @@ def main():
         run_reference(args)
     elif args.full:
         run_full(args)
+    elif args.reference_mode:
+        run_reference_mode(args)
     elif args.batch:
         run_batch(args)
     elif args.precond:

@@ -253,6 +253,7 @@ struct LSRKMem {
   double* Y[3]  = {nullptr, nullptr, nullptr};
   float* D[3]   = {nullptr, nullptr, nullptr};
   double* evec  = nullptr;
+  float* per_faces = nullptr; // mixed reference mode: FP32 Dxw | Dxe | Dys | Dyn
   int par       = 0; // current parity: yb[par] = y_n
   N_Vector nv_y = nullptr, nv_F = nullptr, nv_tmp[3] = {nullptr, nullptr, nullptr};
 
@@ -467,6 +468,8 @@ static void free_device(LSRKMem* m)
   }
   cudaFree(m->evec);
   m->evec = nullptr;
+  cudaFree(m->per_faces);
+  m->per_faces = nullptr;
   cudaFree(m->d_par);
   cudaFreeHost(m->h_par);
   m->d_par = m->h_par = nullptr;
@@ -1208,6 +1211,58 @@ __global__ void __launch_bounds__(256) periodic_err_kernel(long long n, const do
   xsum_block_finish<256>(acc, flags, w, slot, 1, (double)n);
 }
 
+// Mixed reference mode: FP32 increments d_j = Y_j - Y_0 of the periodic problem in the
+// difference form of the Dirichlet mixed stage (kernels.cuh): with A d = sum over the four faces
+// D_face (d_nb - d_C) (exact: the diagonal is minus the sum of the faces),
+//   d_j = d_C + inc, inc = gs d_C + hm A d + gm (d_C - d_{j-2}) + gF F_0,
+//   gs = mu + nu - 1, gm = -nu, gF = hm (1 - a_{j-1}), FP32 face tables.
+// The step end forms y_{n+1} = y_n + d_s in FP64; F(y_{n+1}), the error and the WRMS stay FP64.
+__global__ void __launch_bounds__(256) periodic_stage32_kernel(ProbDev P, const float* __restrict__ faces, float gs,
+                                                               float hmf, float gm, float gF,
+                                                               const float* __restrict__ dm1,
+                                                               const float* __restrict__ dm2,
+                                                               const float* __restrict__ f0f, float* __restrict__ dj)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long j = (long long)blockIdx.y * blockDim.y + threadIdx.y;
+  const long long nx = P.nx, ny = P.ny;
+  if (i >= nx || j >= ny) return;
+  const float* Dxwf = faces;
+  const float* Dxef = faces + nx;
+  const float* Dysf = faces + 2 * nx;
+  const float* Dynf = faces + 2 * nx + ny;
+  const long long iw = (i == 0) ? nx - 1 : i - 1, ie = (i == nx - 1) ? 0 : i + 1;
+  const long long js = (j == 0) ? ny - 1 : j - 1, jn = (j == ny - 1) ? 0 : j + 1;
+  const long long k  = j * nx + i;
+  const float dC = dm1[k], dW = dm1[j * nx + iw], dE = dm1[j * nx + ie], dS = dm1[js * nx + i],
+              dN = dm1[jn * nx + i];
+  const float m2 = dm2 ? dm2[k] : 0.0f;
+  float a        = __fmul_rn(Dxwf[i], __fsub_rn(dW, dC));
+  a              = __fmaf_rn(Dxef[i], __fsub_rn(dE, dC), a);
+  a              = __fmaf_rn(Dysf[j], __fsub_rn(dS, dC), a);
+  a              = __fmaf_rn(Dynf[j], __fsub_rn(dN, dC), a);
+  float inc      = __fmul_rn(gs, dC);
+  inc            = __fmaf_rn(hmf, a, inc);
+  inc            = __fmaf_rn(gm, __fsub_rn(dC, m2), inc);
+  inc            = __fmaf_rn(gF, f0f[k], inc);
+  dj[k]          = __fadd_rn(dC, inc);
+}
+
+__global__ void __launch_bounds__(256) scale32_kernel(long long n, float c, const float* __restrict__ x,
+                                                      float* __restrict__ z)
+{
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) z[k] = __fmul_rn(c, x[k]);
+}
+
+__global__ void __launch_bounds__(256) add_increment_kernel(long long n, const double* __restrict__ y,
+                                                            const float* __restrict__ d, double* __restrict__ out)
+{
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
+    out[k] = __dadd_rn(y[k], (double)d[k]);
+}
+
 static bool periodic_fusable(const LSRKMem* m)
 {
   return !m->ssp && m->rhs == STS_Diffusion && m->user_data != nullptr &&
@@ -1310,12 +1365,48 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
       if (choose_step(m, target, &h, &s, &clipped)) return STS_ILL_INPUT;
       STS_LSRKStageCoeffs(m->method, s, mu.data(), nu.data(), mus.data(), ajm1.data(), cjm1.data());
       m->nst_att++;
-      // Y_1 = y_n + h mus_1 F_n
-      N_VLinearSum_Sts(h * mus[1], F, 1.0, y, m->g_Y[0]);
+      const bool pf = periodic_fusable(m);
+      const bool pm = pf && m->mixed; // mixed reference mode
       N_Vector ym2 = y, ym1 = m->g_Y[0], yj = m->g_Y[0];
       int bi = 1, frc = 0;
-      const bool pf = periodic_fusable(m);
-      for (int j = 2; j <= s && frc == 0; ++j)
+      if (pm)
+      {
+        STS_Problem p   = (STS_Problem)m->user_data;
+        STS_Context ctx = m->ctx;
+        const long long n = m->n;
+        if (!m->per_faces)
+        {
+          if (!STS_CUDA_OK(cudaMalloc(&m->per_faces, (2 * p->nx + 2 * p->ny) * sizeof(float)))) return STS_ERR_FAILURE;
+          for (int b = 0; b < 3; ++b)
+            if (!m->D[b] && !STS_CUDA_OK(cudaMalloc(&m->D[b], n * sizeof(float)))) return STS_ERR_FAILURE;
+          if (!m->Ffb[0] && !STS_CUDA_OK(cudaMalloc(&m->Ffb[0], n * sizeof(float)))) return STS_ERR_FAILURE;
+          sts_f64_to_f32(ctx, p->dev.Dxw, m->per_faces, p->nx);
+          sts_f64_to_f32(ctx, p->dev.Dxe, m->per_faces + p->nx, p->nx);
+          sts_f64_to_f32(ctx, p->dev.Dys, m->per_faces + 2 * p->nx, p->ny);
+          sts_f64_to_f32(ctx, p->dev.Dyn, m->per_faces + 2 * p->nx + p->ny, p->ny);
+        }
+        sts_f64_to_f32(ctx, NVD(F), m->Ffb[0], n); // FP32 copy of F_n
+        const int g1 = ew_blocks(ctx, n, 256 * 4);
+        scale32_kernel<<<g1, 256, 0, ctx->stream>>>(n, (float)(h * mus[1]), m->Ffb[0], m->D[0]);
+        const dim3 b(64, 4), g((unsigned)((p->nx + 63) / 64), (unsigned)((p->ny + 3) / 4));
+        int im1 = 0, im2 = -1;
+        for (int j = 2; j <= s; ++j)
+        {
+          const int io   = (im1 + 1) % 3;
+          const double hm = h * mus[j];
+          periodic_stage32_kernel<<<g, b, 0, ctx->stream>>>(
+            p->dev, m->per_faces, (float)((mu[j] + nu[j]) - 1.0), (float)hm, (float)(-nu[j]),
+            (float)(hm * (1.0 - ajm1[j])), m->D[im1], im2 >= 0 ? m->D[im2] : nullptr, m->Ffb[0], m->D[io]);
+          im2 = im1;
+          im1 = io;
+        }
+        add_increment_kernel<<<g1, 256, 0, ctx->stream>>>(n, NVD(y), m->D[im1], NVD(m->g_Y[0]));
+        yj = m->g_Y[0];
+      }
+      else
+        // Y_1 = y_n + h mus_1 F_n
+        N_VLinearSum_Sts(h * mus[1], F, 1.0, y, m->g_Y[0]);
+      for (int j = 2; j <= s && frc == 0 && !pm; ++j)
       {
         const double hm = h * mus[j];
         double c[5]    = {mu[j], nu[j], (1.0 - mu[j]) - nu[j], hm, -(hm * ajm1[j])};

@@ -1099,6 +1099,66 @@ int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double 
          * Y_j = mu Y_{j-1} + nu Y_{j-2} + (1 - mu - nu) Y_0 + h mus F_j - h mus a_{j-1} F_0
          * (N_VLinearCombination order); error 0.8 Y_0 - 0.8 Y_s + 0.4 h F_0 + 0.4 h F_s and
          * ewt = 1 / (rtol |y| + atol) as N_VScale, N_VAddConst, N_VInv */
+        if (o->mixed)
+        { /* mixed reference mode (the product's periodic_stage32_kernel): FP32 increments in the
+           * difference form with FP32 face tables, y_{n+1} = y_n + d_s in FP64 */
+          long nx = p->nx, ny = p->ny;
+          float* fc = (float*)malloc((2 * nx + 2 * ny) * sizeof(float));
+          for (long i = 0; i < nx; ++i)
+          {
+            fc[i]      = (float)p->Dxw[i];
+            fc[nx + i] = (float)p->Dxe[i];
+          }
+          for (long j = 0; j < ny; ++j)
+          {
+            fc[2 * nx + j]      = (float)p->Dys[j];
+            fc[2 * nx + ny + j] = (float)p->Dyn[j];
+          }
+          float* Ff32 = (float*)malloc(n * sizeof(float));
+          for (long k = 0; k < n; ++k) Ff32[k] = (float)st->F[k];
+          float hm1f = (float)(h * mus[1]);
+          for (long k = 0; k < n; ++k) da[k] = hm1f * Ff32[k];
+          float* dbufs[3] = {da, db, dc};
+          int im1 = 0, im2 = -1;
+          for (int j = 2; j <= s; ++j)
+          {
+            int io    = (im1 + 1) % 3;
+            double hm = h * mus[j];
+            float gs = (float)((mu[j] + nu[j]) - 1.0), hmf = (float)hm, gm = (float)(-nu[j]);
+            float gF = (float)(hm * (1.0 - ajm1[j]));
+            const float* dm1 = dbufs[im1];
+            const float* dm2 = im2 >= 0 ? dbufs[im2] : NULL;
+            float* out       = dbufs[io];
+#pragma omp parallel for schedule(static)
+            for (long jj = 0; jj < ny; ++jj)
+              for (long ii = 0; ii < nx; ++ii)
+              {
+                long iw = (ii == 0) ? nx - 1 : ii - 1, ie = (ii == nx - 1) ? 0 : ii + 1;
+                long js = (jj == 0) ? ny - 1 : jj - 1, jn = (jj == ny - 1) ? 0 : jj + 1;
+                long k  = jj * nx + ii;
+                float dC = dm1[k], dW = dm1[jj * nx + iw], dE = dm1[jj * nx + ie], dS = dm1[js * nx + ii],
+                      dN = dm1[jn * nx + ii];
+                float m2  = dm2 ? dm2[k] : 0.0f;
+                float a   = fc[ii] * (dW - dC);
+                a         = fmaf(fc[nx + ii], dE - dC, a);
+                a         = fmaf(fc[2 * nx + jj], dS - dC, a);
+                a         = fmaf(fc[2 * nx + ny + jj], dN - dC, a);
+                float inc = gs * dC;
+                inc       = fmaf(hmf, a, inc);
+                inc       = fmaf(gm, dC - m2, inc);
+                inc       = fmaf(gF, Ff32[k], inc);
+                out[k]    = dC + inc;
+              }
+            im2 = im1;
+            im1 = io;
+          }
+          for (long k = 0; k < n; ++k) ynew[k] = y[k] + (double)dbufs[im1][k];
+          free(fc);
+          free(Ff32);
+          st->nfe += s;
+        }
+        else
+        {
         double hm1 = h * mus[1];
         for (long k = 0; k < n; ++k) Ya[k] = fma(hm1, st->F[k], y[k]);
         const double *ym2 = y, *ym1 = Ya;
@@ -1126,7 +1186,10 @@ int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double 
         }
         st->nfe += s;
         memcpy(ynew, yj, n * sizeof(double));
+        }
         orc_rhs(p, st->t + h, ynew, Fnew);
+        if (o->mixed)
+          for (long k = 0; k < n; ++k) Fnewf[k] = (float)Fnew[k];
         const double p4h = 0.4 * h;
         XREDUCE(n, ({
                   double e = 0.8 * y[i];

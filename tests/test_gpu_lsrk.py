@@ -59,6 +59,33 @@ def test_reference_mode_periodic_bitwise(ctx, stslib, oracle, method, inhomogene
     run_pair(ctx, stslib, oracle, pk, ok, [0.002, 0.01])
 
 
+@pytest.mark.parametrize("method", [0, 1])
+@pytest.mark.parametrize("inhomogeneous", [False, True])
+def test_reference_mode_mixed_bitwise(ctx, stslib, oracle, method, inhomogeneous):
+    """The mixed form on the reference's own periodic problem (FP32 increments in the
+    difference form with FP32 face tables, diffusion.cpp:36-46 coefficients): GPU and the
+    oracle's mixed integrator bit for bit, adaptive steps."""
+    pk = dict(kind=2, nx=64, ny=48, kx=1.0, ky=0.5, inhomogeneous=inhomogeneous)
+    ok = dict(method=method, rtol=1e-5, atol=1e-9, mixed=True)
+    run_pair(ctx, stslib, oracle, pk, ok, [0.05, 0.2])
+
+
+@pytest.mark.parametrize("method,inhomogeneous", [(0, False), (1, False), (0, True)])
+def test_reference_mode_mixed_within_1e6_of_fp64(ctx, stslib, method, inhomogeneous):
+    """Same step sequence (fixed h): mixed reference mode against the FP64 reference mode at
+    256^2 stays far inside 1e-6 relative L2 (about 1e-9)."""
+    pk = dict(kind=2, nx=256, ny=256, kx=1.0, ky=0.5, inhomogeneous=inhomogeneous)
+    out = {}
+    for mixed in (False, True):
+        G = stslib.Problem(ctx, **pk)
+        I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), method=method, mixed=mixed, hfixed=1e-3)
+        y = G.vector()
+        I.evolve(0.5, y)
+        out[mixed] = y.numpy()
+    rel = np.linalg.norm(out[True] - out[False]) / np.linalg.norm(out[False])
+    assert np.isfinite(rel) and rel < 1e-7, rel
+
+
 @pytest.mark.parametrize("controller", [0, 1, 2, 3, 4, 5])
 def test_controllers_bitwise(ctx, stslib, oracle, controller):
     pk = dict(kind=0, nx=48, ny=40, kx=1.0, ky=0.01)
