@@ -465,6 +465,37 @@ def run_reference_mode(args):
                       "speedup": out["fp64"]["seconds"] / out["mixed"]["seconds"]}), flush=True)
 
 
+def run_batch_profile(args):
+    """A small batch for counter captures: `--batch-count` seeded instances, a fixed launch
+    shape (256 threads, 4 CTAs/SM, 8-CTA clusters for n >= 256: the autotuner's usual choice),
+    one FP64 evolve and one mixed evolve to `--batch-tf`. Prints the DOF-stages and DOF-steps
+    of each (the per-launch normalisation of the counters) and the time of each evolve."""
+    import ceda_demonstrations_gb300 as sts
+    ctx = sts.Context(0)
+    inst = sts.make_batch_instances(count=args.batch_count, seed=20261203)
+    res = {}
+    for mixed in (False, True):
+        B = sts.Batch(ctx, inst)
+        B.set_mixed(mixed)
+        B.set_launch(256, 4, 8, 256)
+        B.evolve(args.batch_tf, method=sts.RKL, rtol=1e-6, atol=1e-10, smax=SMAX)  # warm-up
+        B2 = sts.Batch(ctx, inst)
+        B2.set_mixed(mixed)
+        B2.set_launch(256, 4, 8, 256)
+        ms = B2.evolve(args.batch_tf, method=sts.RKL, rtol=1e-6, atol=1e-10, smax=SMAX)
+        st = [B2.stats(i) for i in range(len(inst))]
+        dof_stages = sum(inst[i][0] ** 2 * st[i]["nfe"] for i in range(len(inst)))
+        dof_steps = sum(inst[i][0] ** 2 * st[i]["nst_attempts"] for i in range(len(inst)))
+        res["mixed" if mixed else "fp64"] = {
+            "ms": ms, "dof_stages": dof_stages, "dof_step_attempts": dof_steps,
+            "stages_per_step": dof_stages / dof_steps, "dof_stages_per_s": dof_stages / (ms / 1e3),
+            "largest_instance_share": max(inst[i][0] ** 2 * st[i]["nfe"] for i in range(len(inst))) / dof_stages,
+            "sizes": sorted(set(int(x[0]) for x in inst))}
+        B.free()
+        B2.free()
+    print(json.dumps({"batch_profile": res, "count": len(inst), "tf": args.batch_tf}), flush=True)
+
+
 def run_batch(args):
     """512 independent heat problems in one persistent launch (n uniform from
     {64,...,512}, kx, ky log-uniform in [1e-2, 1], 8 random sine modes, RKL2 rtol 1e-6 to
@@ -726,6 +757,7 @@ def main():
     ap.add_argument("--reference-mode", action="store_true")
     ap.add_argument("--refmode-n", type=int, default=2048)
     ap.add_argument("--batch", action="store_true")
+    ap.add_argument("--batch-profile", action="store_true")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-tf", type=float, default=0.01)
     ap.add_argument("--precond", action="store_true")
@@ -747,6 +779,8 @@ def main():
         run_full(args)
     elif args.reference_mode:
         run_reference_mode(args)
+    elif args.batch_profile:
+        run_batch_profile(args)
     elif args.batch:
         run_batch(args)
     elif args.precond:
