@@ -74,6 +74,7 @@ class ARKStepStats(C.Structure):
 
 # (name, restype, argtypes) for every entry point of include/stsgpu.h
 SIGNATURES = [
+    ("STS_ProbeFP64Rate", C.c_int, [_vp, _dp]),
     ("STS_ARKStepCreate", _vp, [_vp, _vp, C.c_double, _NV, _vp]),
     ("STS_ARKodeSetOrder", C.c_int, [_vp, C.c_int]),
     ("STS_ARKodeSetLinearSolver", C.c_int, [_vp, _vp, _vp]),

@@ -314,6 +314,11 @@ int STS_ARKStepGetStats(void* mem, STS_ARKStepStats* stats); /* ARKodePrintAllSt
 int STS_ARKStepTable(int implicit, int order, int* s, int* q, int* p, double* A, double* b,
                      double* d, double* c);
 
+/* new (measurement): the FP64 FMA rate of the current device in TFLOP/s (2 flops per FMA),
+ * from a probe kernel of independent FMA chains timed with CUDA events; the denominator the
+ * FP64 stage kernel's rate is reported against */
+int STS_ProbeFP64Rate(STS_Context ctx, double* tflops);
+
 /* host-only helpers (no device work): the integrator's coefficient and step-size rules */
 int STS_LSRKStageCoeffs(int method, int s, double* mu, double* nu, double* mus, double* ajm1,
                         double* cjm1);
