@@ -109,6 +109,23 @@ __device__ __forceinline__ float mixed_point(float gs, float gx, float gy, float
   return __fadd_rn(dc, inc);
 }
 
+// Error weight of the mixed form's step end, 1 / (rtol |y| + atol) to within a few ulp with five
+// FP64-pipe operations instead of a correctly rounded division (about ten on GB300, whose FP64
+// pipe bounds this kernel): den = fma(rtol, |y|, atol), the correctly rounded FP32 reciprocal of
+// the FP32-rounded den as the seed, one Newton step in FP64 (relative error below 1e-14). A den
+// outside [2^-120, 2^120] takes the division. The oracle's step end restates it.
+__device__ __forceinline__ double mixed_weight(double rtol, double atol, double y)
+{
+  const double den = __fma_rn(rtol, fabs(y), atol);
+  if (den >= 0x1p-120 && den <= 0x1p120)
+  {
+    const double r0 = (double)__frcp_rn(__double2float_rn(den));
+    const double e1 = __fma_rn(-den, r0, 1.0);
+    return __fma_rn(r0, e1, r0);
+  }
+  return 1.0 / den;
+}
+
 // ---------------------------------------------------------------------------------------
 // vector load/store helpers
 // ---------------------------------------------------------------------------------------
@@ -340,7 +357,8 @@ static __global__ void __launch_bounds__(256) stage1_32_kernel(long long n, cons
 // Step end. Fnew = F(t+h, ynew); err = 0.8 (yn - ynew) + 0.4 h (Fn + Fnew);
 // dsm = sqrt(sum (err/(rtol |yn| + atol))^2 / N) with the exact accumulator.
 // MIXED: ynew = yn + (double) ds is formed on the fly (also at the stencil neighbours) and
-// written out together with Fnew and its FP32 copy.
+// written out together with Fnew and its FP32 copy; yn - ynew is taken as -ds and the weight
+// comes from mixed_weight.
 // Grid: blockDim.x columns per block, blocks stride over rows.
 // ---------------------------------------------------------------------------------------
 template <bool MIXED, bool FORCED>
@@ -405,11 +423,12 @@ __global__ void __launch_bounds__(256) stepend_kernel(ProbDev P, const StepArgs*
         Fnewf[k] = (float)f;
       }
       const double y = yn[k];
-      const double d = y - uc;
+      // the mixed form takes y_n - y_{n+1} as -d_s itself (exact) and the fast weight
+      const double d = MIXED ? -(double)ds[k] : y - uc;
       double e       = 0.8 * d;
       e              = __fma_rn(p4h, Fn[k], e);
       e              = __fma_rn(p4h, f, e);
-      const double wt = 1.0 / (rtol * fabs(y) + atol);
+      const double wt = MIXED ? mixed_weight(rtol, atol, y) : 1.0 / (rtol * fabs(y) + atol);
       const double x  = e * wt;
       xsum::add(acc, x * x, flags);
     }
@@ -502,6 +521,13 @@ __global__ void __launch_bounds__(256) stepend_march_kernel(ProbDev P, const Ste
       const double2 ynv = __ldg(reinterpret_cast<const double2*>(yn + k));
       const double2 fnv = __ldg(reinterpret_cast<const double2*>(Fn + k));
       const double yv[2] = {ynv.x, ynv.y}, fv[2] = {fnv.x, fnv.y};
+      float dsv[2] = {0.f, 0.f};
+      if (MIXED)
+      {
+        const float2 t = __ldg(reinterpret_cast<const float2*>(ds + k));
+        dsv[0]         = t.x;
+        dsv[1]         = t.y;
+      }
       double syj = 0.0, syyj = 0.0;
       if (FORCED)
       {
@@ -525,11 +551,11 @@ __global__ void __launch_bounds__(256) stepend_march_kernel(ProbDev P, const Ste
           f = __fma_rn(syyj, Qi[v], f);
         }
         fo[v]           = f;
-        const double d  = yv[v] - uc;
+        const double d  = MIXED ? -(double)dsv[v] : yv[v] - uc;
         double e        = 0.8 * d;
         e               = __fma_rn(p4h, fv[v], e);
         e               = __fma_rn(p4h, f, e);
-        const double wt = 1.0 / (rtol * fabs(yv[v]) + atol);
+        const double wt = MIXED ? mixed_weight(rtol, atol, yv[v]) : 1.0 / (rtol * fabs(yv[v]) + atol);
         const double x  = e * wt;
         xsum::add(acc, x * x, flags);
       }

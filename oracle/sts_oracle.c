@@ -873,8 +873,25 @@ static void stage32(const orc_prob* p, const stage_c* c, const float* dm1, const
     }
 }
 
+/* Error weight of the mixed step end: den = fma(rtol, |y|, atol); the correctly rounded FP32
+ * reciprocal of (float)den, one Newton step in FP64; outside [2^-120, 2^120] the division. */
+static double mixed_weight(double rtol, double atol, double y)
+{
+  double den = fma(rtol, fabs(y), atol);
+  if (den >= 0x1p-120 && den <= 0x1p120)
+  {
+    float df  = (float)den;
+    float rf  = 1.0f / df;
+    double r0 = (double)rf;
+    double e1 = fma(-den, r0, 1.0);
+    return fma(r0, e1, r0);
+  }
+  return 1.0 / den;
+}
+
 /* Step end: Fnew = F(t+h, ynew), err = 0.8 (yn - ynew) + 0.4 h (Fn + Fnew),
- * dsm = ||err||_WRMS with ewt = 1/(rtol |yn| + atol). For the mixed form ynew = yn + ds. */
+ * dsm = ||err||_WRMS with ewt = 1/(rtol |yn| + atol). For the mixed form ynew = yn + ds,
+ * yn - ynew is taken as -ds and ewt comes from mixed_weight. */
 static double step_end(const orc_prob* p, const orc_opts* o, double t, double h, const double* yn,
                        const double* Fn, double* ynew, const float* ds, double* Fnew, float* Fnewf)
 {
@@ -892,6 +909,20 @@ static double step_end(const orc_prob* p, const orc_opts* o, double t, double h,
   }
   double p4h = 0.4 * h;
   double s;
+  if (ds)
+  { /* mixed form: y_n - y_{n+1} as -d_s, the fast weight (mixed_weight in csrc/kernels.cuh) */
+    XREDUCE(n, ({
+              double d = -(double)ds[i];
+              double e = 0.8 * d;
+              e        = fma(p4h, Fn[i], e);
+              e        = fma(p4h, Fnew[i], e);
+              double w = mixed_weight(o->rtol, o->atol, yn[i]);
+              double x = e * w;
+              x * x;
+            }));
+    s = xacc_result(&tot);
+  }
+  else
   {
     XREDUCE(n, ({
               double d = yn[i] - ynew[i];
