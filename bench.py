@@ -109,7 +109,7 @@ class Clocks:
 
 
 def merge_clocks(parts):
-    """Clock record over both timed regions (mixed and FP64)."""
+    """Clock record over the timed regions (mixed, FP64 and end to end)."""
     sm = [p["sm_mhz"] for p in parts if p.get("sm_mhz") is not None]
     mx = [p["sm_max_mhz"] for p in parts if p.get("sm_max_mhz") is not None]
     reasons = sorted(set(r for p in parts for r in p.get("reasons", [])))
@@ -237,6 +237,8 @@ def run_gpu(args):
         k = 1 - k
     barrier()
     s0 = I.stats()
+    clocks = Clocks(local)
+    clocks.start()
     with timer() as tm:
         for _ in range(args.steps):
             L.N_VCopyFromHost_Sts(yv.h, hp[k])
@@ -244,8 +246,12 @@ def run_gpu(args):
             t_cur, _ = I.evolve(TF, yv, sts.ONE_STEP)
             L.N_VCopyToHost_Sts(yv.h, hp[1 - k])
             k = 1 - k
+    e2e_clocks = clocks.stop()
+    clock_samples.append(e2e_clocks)
     s1 = I.stats()
     e2e_ms = max_over_ranks(tm.ms)
+    e2e_stages = (s1["stages_total"] - s0["stages_total"]) / args.steps
+    e2e_attempts = s1["nst_attempts"] - s0["nst_attempts"]
     # ARKodeReset evaluates F(t, y) once per step: work of the restart, not of the step
     e2e_dof = N2 * (s1["nfe"] - s0["nfe"] - args.steps)
     # the host link alone (copy engine, pinned buffers, same calls): the part of the e2e step
@@ -302,7 +308,8 @@ def run_gpu(args):
         "e2e": {"value": ws * e2e_dof / (e2e_ms / 1e3), "unit": "DOF-stages/s",
                 "h2d_bytes_per_step": 8 * N2, "d2h_bytes_per_step": 8 * N2,
                 "ms_per_step": e2e_ms / args.steps, "h2d_ms": h2d_ms, "d2h_ms": d2h_ms,
-                "h2d_gbs": 8 * N2 / (h2d_ms / 1e3) / 1e9, "d2h_gbs": 8 * N2 / (d2h_ms / 1e3) / 1e9},
+                "h2d_gbs": 8 * N2 / (h2d_ms / 1e3) / 1e9, "d2h_gbs": 8 * N2 / (d2h_ms / 1e3) / 1e9,
+                "stages_per_step": e2e_stages, "step_attempts": e2e_attempts, "sm_mhz": e2e_clocks["sm_mhz"]},
         "gpu_launches": m["launches"],
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": ach / peak, "traffic": traffic,
@@ -415,6 +422,7 @@ def run_full(args):
             for mixed in (True, False):
                 I = sts.LSRKStep(ctx, G, 0.0, G.initial(), method=method, rtol=rtol, atol=ATOL,
                                  smax=SMAX, mixed=mixed, graphs=True, maxsteps=1000000)
+                I.set_stop_time(tf)  # the last step ends on tf (diffusion_2D/main.cpp:384)
                 y = G.vector()
                 with timer() as tm:
                     I.evolve(tf, y)
@@ -454,6 +462,7 @@ def run_reference_mode(args):
         I.evolve(0.01, y)
         ctx.synchronize()
         s0 = I.stats()
+        I.set_stop_time(0.05)
         with timer() as tm:
             I.evolve(0.05, y)
         s1 = I.stats()
@@ -525,7 +534,8 @@ def run_batch(args):
     for i in sample:
         n, kx, ky, p, q, a = inst[i]
         P = po.Problem(po.UNFORCED, n, n, kx=kx, ky=ky)
-        J = po.Integrator(P, P.initial_modes(p, q, a), method=po.RKL, rtol=1e-6, atol=1e-10)
+        J = po.Integrator(P, P.initial_modes(p, q, a), method=po.RKL, rtol=1e-6, atol=1e-10,
+                          tstop=args.batch_tf)  # the batch ends every instance on tf
         J.evolve(args.batch_tf)
         cpu_dof += n * n * J.stats()["nfe"]
         yi = B.instance_state(y, i)
@@ -545,7 +555,7 @@ def run_batch(args):
         n, kx, ky, p, q, a = inst[i]
         P = po.Problem(po.UNFORCED, n, n, kx=kx, ky=ky)
         J = po.Integrator(P, P.initial_modes(p, q, a), method=po.RKL, rtol=1e-6, atol=1e-10,
-                          mixed=True)
+                          mixed=True, tstop=args.batch_tf)
         J.evolve(args.batch_tf)
         yi = M.instance_state(ym, i)
         mmax_or = max(mmax_or, float(np.linalg.norm(yi - J.y) / np.linalg.norm(J.y)))

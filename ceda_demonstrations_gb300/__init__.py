@@ -32,6 +32,7 @@ MODIFIED_GS, CLASSICAL_GS = 1, 2
 MANUFACTURED, UNFORCED, PERIODIC = 0, 1, 2
 NORMAL, ONE_STEP = 1, 2
 TOO_MUCH_WORK = -1
+TSTOP_RETURN = 1
 
 _dp = C.POINTER(C.c_double)
 _fp = C.POINTER(C.c_float)
@@ -584,8 +585,11 @@ class LSRKStep:
             L.STS_LSRKStepSetDomEigFn(self.mem, C.cast(L.STS_DomEig, _vp))
 
     def evolve(self, tout, yout, itask=NORMAL):
-        """Returns (t, flag); flag TOO_MUCH_WORK (-1) means the step limit of this call was
-        reached before tout (the state at t is valid); other negative flags raise."""
+        """ARKodeEvolve: returns (tret, flag). NORMAL mode steps past tout (never past a stop
+        time) and returns the dense output at tret = tout; a reached stop time returns y_n with
+        flag TSTOP_RETURN (1) and is cleared; ONE_STEP returns y_n after one step. Flag
+        TOO_MUCH_WORK (-1): the step limit of this call was reached before tout (y_n at tret);
+        other negative flags raise."""
         t = C.c_double()
         rc = lib().STS_ARKodeEvolve(self.mem, tout, yout.h, C.byref(t), itask)
         if rc < TOO_MUCH_WORK:
@@ -696,11 +700,15 @@ class ARKStep:
                 L.STS_ARKodeSetLinear(self.mem, 0)
 
     def evolve(self, tout, yout, itask=NORMAL):
+        """ARKodeEvolve with the return rules of LSRKStep.evolve."""
         t = C.c_double()
         rc = lib().STS_ARKodeEvolve(self.mem, tout, yout.h, C.byref(t), itask)
         if rc < TOO_MUCH_WORK:
             _err("STS_ARKodeEvolve returned %d" % rc)
         return t.value, rc
+
+    def set_stop_time(self, tstop):
+        lib().STS_ARKodeSetStopTime(self.mem, tstop)
 
     def stats(self):
         s = ARKStepStats()

@@ -28,12 +28,16 @@
 //   p + 1 (p = embedding order); a Newton failure retries with h / 4 (at most 10 per step),
 //   at most 7 error-test failures per step. The first stage of an ESDIRK / ERK table reuses
 //   f(t_n, y_n), evaluated once per step start.
+//   Output: the return rules of STS_ARKodeEvolve (lsrk.cu) with the Hermite dense output of
+//   degree min(q - 1, 5); a degree >= 2 output evaluates f(t_n, y_n) when no step start has.
 #include <cuda_runtime.h>
 
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #include "portable_math.cuh"
@@ -127,6 +131,10 @@ struct ARKStepMem {
   long long nst = 0, nst_att = 0, netf = 0, ncfn = 0, nfe = 0, nfi = 0, nni = 0, nnf = 0, nli = 0, nlcf = 0;
   long long npe = 0, nps = 0, njv = 0, nsetups = 0, nfe_dq = 0, nhist = 0, nst_setup = 0;
   bool initialized = false, after_fail = false, fn_current = false, force_setup = true;
+  // stop time and dense output: after an accepted step `ynew` holds y_old (the vectors are
+  // swapped) and F[0] holds f(t_old, y_old) for the explicit-first-stage tables
+  bool tstopset = false, interp_ready = false;
+  double tretlast = 0;
   // vectors
   N_Vector y = nullptr, Fn = nullptr, sdata = nullptr, z = nullptr, res = nullptr, del = nullptr, ewt = nullptr,
            tmp = nullptr, tmp2 = nullptr, ynew = nullptr;
@@ -310,7 +318,9 @@ static double ark_controller(ARKStepMem* m, double h, double dsm, double hp)
   return sts_controller_estimate(m->controller, h, dsm, m->ep1, m->ep2, hp, m->nhist, (double)(m->T.p + 1));
 }
 
-static int ark_evolve(ARKStepMem* m, double target, int itask)
+// step loop: NORMAL mode until t >= tout, ONE_STEP mode one step; steps clipped only at `clip`
+// (the stop time or +inf)
+static int ark_evolve(ARKStepMem* m, double tout, double clip, int itask)
 {
   const int s = m->T.s;
   if (!m->initialized)
@@ -323,7 +333,8 @@ static int ark_evolve(ARKStepMem* m, double target, int itask)
   std::vector<N_Vector> X(s + 1);
   long long nsteps_call = 0;
   int ret               = STS_SUCCESS;
-  while (m->t < target)
+  const double target   = tout < clip ? tout : clip; // initial-step distance
+  while (m->t < clip && (itask == STS_ONE_STEP || m->t < tout))
   {
     if (nsteps_call >= (m->maxsteps > 0 ? m->maxsteps : 500))
     {
@@ -370,13 +381,14 @@ static int ark_evolve(ARKStepMem* m, double target, int itask)
     {
       double h     = m->hnext;
       bool clipped = false;
-      if (m->t + h >= target)
+      if (m->t + h >= clip)
       {
-        h       = target - m->t;
+        h       = clip - m->t;
         clipped = true;
       }
       m->nst_att++;
-      const int rc = attempt(m, h);
+      m->interp_ready = false; // the attempt overwrites F[0]
+      const int rc    = attempt(m, h);
       if (rc < 0) return STS_ERR_FAILURE;
       if (rc == 1 || rc == 2)
       { // Newton failure or recoverable RHS failure: retry with a quarter step
@@ -415,8 +427,9 @@ static int ark_evolve(ARKStepMem* m, double target, int itask)
           X[i + 1]  = m->F[i];
         }
         N_VLinearCombination_Sts(s + 1, cf.data(), X.data(), m->ynew);
-        N_VScale_Sts(1.0, m->ynew, m->y);
-        m->t               = clipped ? target : m->t + h;
+        std::swap(m->y, m->ynew); // y_{n+1}; y_n stays in ynew for the dense output
+        m->interp_ready    = true;
+        m->t               = clipped ? clip : m->t + h;
         m->fn_current      = false;
         const double hprev = m->hlast;
         m->hlast           = h;
@@ -622,8 +635,41 @@ int arkstep_set_max_steps(void* mem, long long mx)
 }
 int arkstep_set_stop_time(void* mem, double ts)
 {
-  AM(mem)->tstop = ts;
+  AM(mem)->tstop    = ts;
+  AM(mem)->tstopset = true;
   return 0;
+}
+
+// dense output at tq on the last step (the Hermite rule of sts_hermite, degree min(q - 1, 5));
+// f(t_n, y_n) is evaluated here when no step start has (counted like any RHS evaluation) and
+// then serves the next step's explicit first stage
+static int ark_output(ARKStepMem* m, N_Vector yout, double tq, bool interp)
+{
+  if (!interp || tq == m->t)
+  {
+    N_VScale_Sts(1.0, m->y, yout);
+    return 0;
+  }
+  const double tfuzz = 100.0 * DBL_EPSILON * (fabs(m->t) + fabs(m->hlast));
+  if (tq < m->t - m->hlast - tfuzz)
+  {
+    sts_set_error("ARKodeEvolve: tout = %g is behind the last step [%g, %g]", tq, m->t - m->hlast, m->t);
+    return STS_ILL_INPUT;
+  }
+  const int deg = m->T.q - 1 < 5 ? m->T.q - 1 : 5;
+  if (deg >= 2 && !m->fn_current)
+  {
+    const int frc = rhs(m, m->t, m->y, m->Fn);
+    if (frc != 0)
+    {
+      sts_set_error("ARKStep: RHS failure in the dense output at t = %g", m->t);
+      return STS_RHSFUNC_FAIL;
+    }
+    m->fn_current = true;
+  }
+  sts_hermite(m->ctx, m->n, deg, (tq - m->t) / m->hlast, m->hlast, NVD(m->ynew), NVD(m->y), NVD(m->F[0]),
+              NVD(m->Fn), NVD(yout));
+  return STS_CUDA_OK(cudaGetLastError()) ? 0 : STS_ERR_FAILURE;
 }
 
 int arkstep_evolve(void* mem, double tout, N_Vector yout, double* tret, int itask)
@@ -642,13 +688,45 @@ int arkstep_evolve(void* mem, double tout, N_Vector yout, double* tret, int itas
   }
   ctx_activate(m->ctx);
   while ((int)m->F.size() < m->T.s) m->F.push_back(N_VClone_Sts(m->y));
-  const double target = tout < m->tstop ? tout : m->tstop;
-  int ret             = ark_evolve(m, target, itask);
-  N_VScale_Sts(1.0, m->y, yout);
-  if (!STS_CUDA_OK(cudaStreamSynchronize(m->ctx->stream))) return STS_ERR_FAILURE;
-  if (tret) *tret = m->t;
-  if (ret == STS_SUCCESS && m->t >= m->tstop) ret = STS_TSTOP_RETURN;
-  return ret;
+  auto finish = [&](int ret, double tr) {
+    if (!STS_CUDA_OK(cudaStreamSynchronize(m->ctx->stream))) return (int)STS_ERR_FAILURE;
+    if (tret) *tret = tr;
+    m->tretlast = tr;
+    return ret;
+  };
+  // the return rules of STS_ARKodeEvolve (lsrk.cu)
+  if (m->interp_ready && itask != STS_ONE_STEP && m->t >= tout)
+  {
+    const int rc = ark_output(m, yout, tout, true);
+    return rc ? rc : finish(STS_SUCCESS, tout);
+  }
+  if (m->interp_ready && itask == STS_ONE_STEP && m->t != m->tretlast)
+  {
+    ark_output(m, yout, m->t, false);
+    return finish(STS_SUCCESS, m->t);
+  }
+  if (m->tstopset && m->t >= m->tstop)
+  {
+    m->tstopset = false;
+    ark_output(m, yout, m->t, false);
+    return finish(STS_TSTOP_RETURN, m->t);
+  }
+  int ret     = ark_evolve(m, tout, m->tstopset ? m->tstop : INFINITY, itask);
+  double tr   = m->t;
+  bool interp = false;
+  if (m->tstopset && m->t >= m->tstop)
+  {
+    m->tstopset = false;
+    if (ret == STS_SUCCESS) ret = STS_TSTOP_RETURN;
+  }
+  else if (ret == STS_SUCCESS && itask != STS_ONE_STEP && m->t >= tout)
+  {
+    interp = true;
+    tr     = tout;
+  }
+  const int rc = ark_output(m, yout, tr, interp);
+  if (rc) return rc;
+  return finish(ret, tr);
 }
 
 int arkstep_reset(void* mem, double t, N_Vector y)
@@ -656,8 +734,10 @@ int arkstep_reset(void* mem, double t, N_Vector y)
   ARKStepMem* m = AM(mem);
   if (!y || NVL(y) != m->n) return STS_ILL_INPUT;
   ctx_activate(m->ctx);
-  m->t          = t;
-  m->fn_current = false;
+  m->t            = t;
+  m->tretlast     = t;
+  m->interp_ready = false;
+  m->fn_current   = false;
   N_VScale_Sts(1.0, y, m->y);
   return 0;
 }

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -229,6 +230,7 @@ struct LSRKMem {
   long long dom_eig_freq = 25;
   long long maxsteps    = 500;
   double tstop          = INFINITY;
+  bool tstopset         = false; // ARKodeSetStopTime: cleared when the stop time is returned
   bool mixed            = false;
   bool use_graphs       = true;
   int stage_variant     = 0; // 0: autotuned (TMA configurations + register kernel), 1: register marching
@@ -245,6 +247,10 @@ struct LSRKMem {
             stages_total = 0, nhist = 0, steps_since_dee = -1;
   bool initialized = false, after_fail = false;
   int last_s = 0;
+  // dense output: the last accepted step's y_old (and f_old) are still held (fused: the other
+  // parity buffer; generic: g_yold / g_Fold); tretlast = the time last returned to the caller
+  bool interp_ready = false;
+  double tretlast   = 0.0;
 
   // device buffers
   double* yb[2] = {nullptr, nullptr}; // y_n / y_{n+1} (parity)
@@ -265,7 +271,7 @@ struct LSRKMem {
 
   // generic path temporaries
   N_Vector g_Y[3] = {nullptr, nullptr, nullptr}, g_F = nullptr, g_Fnew = nullptr, g_err = nullptr,
-           g_ewt = nullptr, g_y = nullptr, g_Fn = nullptr;
+           g_ewt = nullptr, g_y = nullptr, g_Fn = nullptr, g_yold = nullptr, g_Fold = nullptr;
 };
 
 static bool fused(const LSRKMem* m)
@@ -474,7 +480,8 @@ static void free_device(LSRKMem* m)
   cudaFreeHost(m->h_par);
   m->d_par = m->h_par = nullptr;
   N_Vector* vs[] = {&m->nv_y, &m->nv_F, &m->nv_tmp[0], &m->nv_tmp[1], &m->nv_tmp[2], &m->g_Y[0], &m->g_Y[1],
-                    &m->g_Y[2], &m->g_F, &m->g_Fnew, &m->g_err, &m->g_ewt, &m->g_y, &m->g_Fn};
+                    &m->g_Y[2], &m->g_F, &m->g_Fnew, &m->g_err, &m->g_ewt, &m->g_y, &m->g_Fn,
+                    &m->g_yold, &m->g_Fold};
   for (N_Vector* v : vs)
   {
     if (*v) N_VDestroy_Sts(*v);
@@ -917,6 +924,7 @@ double sts_wrms_ewt(STS_Context ctx, const double* a, const double* b, const dou
 // controller update after an accepted step of size h with error dsm
 static void accept_control(LSRKMem* m, double h, double dsm)
 {
+  m->interp_ready = true;
   const double hprev = m->hlast; // previous accepted step (implicit Gustafsson controller)
   m->hlast           = h;
   if (m->hfixed > 0.0)
@@ -979,7 +987,9 @@ static int choose_step(LSRKMem* m, double target, double* hout, int* sout, bool*
 // ---------------------------------------------------------------------------------------
 // fused evolve
 // ---------------------------------------------------------------------------------------
-static int evolve_fused(LSRKMem* m, double target, int itask)
+// Step loop of ARKodeEvolve: NORMAL mode steps until t >= tout, ONE_STEP mode takes one step;
+// steps are clipped only at `clip` (the stop time, or +inf), which they then end on exactly.
+static int evolve_fused(LSRKMem* m, double tout, double clip, int itask)
 {
   STS_Problem p   = (STS_Problem)m->user_data;
   cudaStream_t st = m->ctx->stream;
@@ -1002,7 +1012,8 @@ static int evolve_fused(LSRKMem* m, double target, int itask)
   std::vector<double> mu(m->smax + 1), nu(m->smax + 1), mus(m->smax + 1), ajm1(m->smax + 1), cjm1(m->smax + 1);
   long long nsteps_call = 0;
   int ret               = STS_SUCCESS;
-  while (m->t < target)
+  const double tdist_to = tout < clip ? tout : clip; // initial-step distance
+  while (m->t < clip && (itask == STS_ONE_STEP || m->t < tout))
   {
     if (nsteps_call >= (m->maxsteps > 0 ? m->maxsteps : 500))
     {
@@ -1016,7 +1027,7 @@ static int evolve_fused(LSRKMem* m, double target, int itask)
       if (dee_update(m, m->nv_y, m->nv_F)) return STS_ERR_FAILURE;
     if (!(m->hnext > 0.0))
     {
-      double h0 = initial_step(m, m->yb[m->par], m->Fb[m->par], target - m->t);
+      double h0 = initial_step(m, m->yb[m->par], m->Fb[m->par], tdist_to - m->t);
       if (!(h0 > 0.0))
       {
         sts_set_error("LSRKStep: no usable initial step (RHS failure or non-finite state)");
@@ -1030,12 +1041,13 @@ static int evolve_fused(LSRKMem* m, double target, int itask)
       double h;
       int s;
       bool clipped;
-      int rc = choose_step(m, target, &h, &s, &clipped);
+      int rc = choose_step(m, clip, &h, &s, &clipped);
       if (rc) return STS_ILL_INPUT;
       STS_LSRKStageCoeffs(m->method, s, mu.data(), nu.data(), mus.data(), ajm1.data(), cjm1.data());
       m->nst_att++;
       fill_params(m, p, m->t, h, s, mu, nu, mus, ajm1, cjm1);
       if (run_step_fused(m, p, s)) return STS_ERR_FAILURE;
+      m->interp_ready = false; // the attempt wrote y_{n+1} over the other parity buffer
       if (!STS_CUDA_OK(cudaStreamSynchronize(st))) return STS_ERR_FAILURE;
       if (const int ew = *(volatile int*)m->ctx->h_err)
       {
@@ -1050,7 +1062,7 @@ static int evolve_fused(LSRKMem* m, double target, int itask)
       m->last_s = s;
       if (m->hfixed > 0.0 || dsm <= 1.0)
       {
-        m->t     = clipped ? target : m->t + h;
+        m->t     = clipped ? clip : m->t + h;
         m->par   = 1 - m->par;
         accept_control(m, h, dsm);
         m->nst++;
@@ -1269,7 +1281,7 @@ static bool periodic_fusable(const LSRKMem* m)
          ((STS_Problem)m->user_data)->kind == STS_PROBLEM_PERIODIC && m->use_fused_periodic;
 }
 
-static int evolve_generic(LSRKMem* m, double target, int itask)
+static int evolve_generic(LSRKMem* m, double tout, double clip, int itask)
 {
   N_Vector y = m->g_y, F = m->g_Fn;
   if (!m->g_Y[0])
@@ -1279,6 +1291,8 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
     m->g_Fnew = N_VClone_Sts(y);
     m->g_err  = N_VClone_Sts(y);
     m->g_ewt  = N_VClone_Sts(y);
+    m->g_yold = N_VClone_Sts(y);
+    m->g_Fold = N_VClone_Sts(y);
   }
   if (!m->initialized)
   {
@@ -1291,7 +1305,8 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
   std::vector<double> mu(m->smax + 1), nu(m->smax + 1), mus(m->smax + 1), ajm1(m->smax + 1), cjm1(m->smax + 1);
   long long nsteps_call = 0;
   int ret               = STS_SUCCESS;
-  while (m->t < target)
+  const double tdist_to = tout < clip ? tout : clip;
+  while (m->t < clip && (itask == STS_ONE_STEP || m->t < tout))
   {
     if (nsteps_call >= (m->maxsteps > 0 ? m->maxsteps : 500))
     {
@@ -1303,7 +1318,7 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
       if (dee_update(m, y, F)) return STS_ERR_FAILURE;
     if (!(m->hnext > 0.0))
     {
-      double h0 = initial_step(m, NVD(y), NVD(F), target - m->t);
+      double h0 = initial_step(m, NVD(y), NVD(F), tdist_to - m->t);
       if (!(h0 > 0.0))
       {
         sts_set_error("LSRKStep: no usable initial step (RHS failure or non-finite state)");
@@ -1318,12 +1333,12 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
       int s;
       bool clipped;
       if (m->ssp)
-      { // fixed stage count; the step only clipped at the target
+      { // fixed stage count; the step only clipped at the stop time
         h       = m->hnext;
         clipped = false;
-        if (m->t + h >= target)
+        if (m->t + h >= clip)
         {
-          h       = target - m->t;
+          h       = clip - m->t;
           clipped = true;
         }
         s = m->ssp_stages;
@@ -1347,7 +1362,9 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
         if (s > m->stage_max) m->stage_max = s;
         if (m->hfixed > 0.0 || dsm <= 1.0)
         {
-          m->t = clipped ? target : m->t + h;
+          m->t = clipped ? clip : m->t + h;
+          cudaMemcpyAsync(NVD(m->g_yold), NVD(y), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
+          cudaMemcpyAsync(NVD(m->g_Fold), NVD(F), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
           cudaMemcpyAsync(NVD(y), NVD(m->g_Fnew), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
           if (m->rhs(m->t, y, F, m->user_data) != 0) return STS_RHSFUNC_FAIL; // F(y_{n+1}) for the next step
           m->nfe++;
@@ -1362,7 +1379,7 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
         reject_control(m, h, dsm, nef);
         continue;
       }
-      if (choose_step(m, target, &h, &s, &clipped)) return STS_ILL_INPUT;
+      if (choose_step(m, clip, &h, &s, &clipped)) return STS_ILL_INPUT;
       STS_LSRKStageCoeffs(m->method, s, mu.data(), nu.data(), mus.data(), ajm1.data(), cjm1.data());
       m->nst_att++;
       const bool pf = periodic_fusable(m);
@@ -1466,7 +1483,8 @@ static int evolve_generic(LSRKMem* m, double target, int itask)
       if (s > m->stage_max) m->stage_max = s;
       if (m->hfixed > 0.0 || dsm <= 1.0)
       {
-        m->t = clipped ? target : m->t + h;
+        m->t = clipped ? clip : m->t + h;
+        cudaMemcpyAsync(NVD(m->g_yold), NVD(y), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
         cudaMemcpyAsync(NVD(y), NVD(yj), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
         cudaMemcpyAsync(NVD(F), NVD(m->g_Fnew), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
         accept_control(m, h, dsm);
@@ -1656,7 +1674,8 @@ extern "C" int STS_ARKodeSetStopTime(void* mem, double tstop)
 {
   CHECK_MEM(mem);
   if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_set_stop_time(mem, tstop);
-  MEM(mem)->tstop = tstop;
+  MEM(mem)->tstop    = tstop;
+  MEM(mem)->tstopset = true;
   return 0;
 }
 extern "C" int STS_LSRKStepSetMixedPrecision(void* mem, int on)
@@ -1714,6 +1733,44 @@ extern "C" int STS_LSRKStepSetFusedPeriodic(void* mem, int on)
   return 0;
 }
 
+// ARKodeEvolve's return rules (ARKODE's documented behaviour, restated):
+//  - a stop time (ARKodeSetStopTime) clips the step that would pass it; the call that ends on
+//    it returns y_n with STS_TSTOP_RETURN and clears it;
+//  - NORMAL mode steps until t_n >= tout and returns the dense output at tout (tret = tout;
+//    a step ending exactly on tout returns y_n); a call whose tout the last step already passed
+//    interpolates without stepping;
+//  - ONE_STEP mode takes one step and returns y_n, t_n; a call that finds t_n not yet returned
+//    (an earlier NORMAL call interpolated behind it) returns it without stepping.
+static int lsrk_interp_degree(const LSRKMem* m)
+{ // min(q - 1, 5): RKC2, RKL2 and SSP(s,2) 1, SSP(s,3) 2, SSP(10,4) 3
+  if (m->ssp && m->method == SSP_S_3) return 2;
+  if (m->ssp && m->method == SSP_10_4) return 3;
+  return 1;
+}
+
+static int lsrk_output(LSRKMem* m, N_Vector yout, double tq, bool interp)
+{
+  const bool fz      = fused(m) && m->yb[0];
+  const double* ycur = fz ? m->yb[m->par] : NVD(m->g_y);
+  cudaStream_t st    = m->ctx->stream;
+  if (!interp || tq == m->t)
+    return STS_CUDA_OK(cudaMemcpyAsync(NVD(yout), ycur, m->n * sizeof(double), cudaMemcpyDeviceToDevice, st))
+               ? 0
+               : STS_ERR_FAILURE;
+  const double tfuzz = 100.0 * DBL_EPSILON * (fabs(m->t) + fabs(m->hlast));
+  if (tq < m->t - m->hlast - tfuzz)
+  {
+    sts_set_error("ARKodeEvolve: tout = %g is behind the last step [%g, %g]", tq, m->t - m->hlast, m->t);
+    return STS_ILL_INPUT;
+  }
+  const double* yold = fz ? m->yb[1 - m->par] : NVD(m->g_yold);
+  const double* fold = fz ? m->Fb[1 - m->par] : NVD(m->g_Fold);
+  const double* fnew = fz ? m->Fb[m->par] : NVD(m->g_Fn);
+  sts_hermite(m->ctx, m->n, lsrk_interp_degree(m), (tq - m->t) / m->hlast, m->hlast, yold, ycur, fold, fnew,
+              NVD(yout));
+  return STS_CUDA_OK(cudaGetLastError()) ? 0 : STS_ERR_FAILURE;
+}
+
 extern "C" int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* tret, int itask)
 {
   STS_MARK_REGION("Evolve");
@@ -1726,9 +1783,33 @@ extern "C" int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* t
     return STS_ILL_INPUT;
   }
   ctx_activate(m->ctx);
+  cudaStream_t st = m->ctx->stream;
+  auto finish     = [&](int ret, double tr) {
+    if (!STS_CUDA_OK(cudaStreamSynchronize(st))) return (int)STS_ERR_FAILURE;
+    if (tret) *tret = tr;
+    m->tretlast = tr;
+    return ret;
+  };
+  // calls that return without stepping
+  if (m->interp_ready && itask != STS_ONE_STEP && m->t >= tout)
+  {
+    const int rc = lsrk_output(m, yout, tout, true);
+    return rc ? rc : finish(STS_SUCCESS, tout);
+  }
+  if (m->interp_ready && itask == STS_ONE_STEP && m->t != m->tretlast)
+  {
+    const int rc = lsrk_output(m, yout, m->t, false);
+    return rc ? rc : finish(STS_SUCCESS, m->t);
+  }
+  if (m->tstopset && m->t >= m->tstop)
+  {
+    m->tstopset  = false;
+    const int rc = lsrk_output(m, yout, m->t, false);
+    return rc ? rc : finish(STS_TSTOP_RETURN, m->t);
+  }
   // start every evolve from a clean reduction workspace (a failed launch could leave it dirty)
-  cudaMemsetAsync(m->ctx->d_work, 0, sizeof(RedWork), m->ctx->stream);
-  double target = tout < m->tstop ? tout : m->tstop;
+  cudaMemsetAsync(m->ctx->d_work, 0, sizeof(RedWork), st);
+  const double clip = m->tstopset ? m->tstop : INFINITY;
   int ret;
   if (fused(m))
   {
@@ -1737,18 +1818,24 @@ extern "C" int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* t
       if (m->mixed && ((STS_Problem)m->user_data)->kind == STS_PROBLEM_PERIODIC) return STS_ILL_INPUT;
       if (alloc_fused(m, NVD(m->g_y))) return STS_ERR_FAILURE;
     }
-    ret = evolve_fused(m, target, itask);
-    cudaMemcpyAsync(NVD(yout), m->yb[m->par], m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
+    ret = evolve_fused(m, tout, clip, itask);
   }
-  else
+  else ret = evolve_generic(m, tout, clip, itask);
+  double tr = m->t;
+  bool interp = false;
+  if (m->tstopset && m->t >= m->tstop)
   {
-    ret = evolve_generic(m, target, itask);
-    cudaMemcpyAsync(NVD(yout), NVD(m->g_y), m->n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream);
+    m->tstopset = false;
+    if (ret == STS_SUCCESS) ret = STS_TSTOP_RETURN;
   }
-  if (!STS_CUDA_OK(cudaStreamSynchronize(m->ctx->stream))) return STS_ERR_FAILURE;
-  if (tret) *tret = m->t;
-  if (ret == STS_SUCCESS && m->t >= m->tstop) ret = STS_TSTOP_RETURN;
-  return ret;
+  else if (ret == STS_SUCCESS && itask != STS_ONE_STEP && m->t >= tout)
+  {
+    interp = true;
+    tr     = tout;
+  }
+  const int rc = lsrk_output(m, yout, tr, interp);
+  if (rc) return rc;
+  return finish(ret, tr);
 }
 
 extern "C" int STS_ARKodeReset(void* mem, double t, N_Vector y)
@@ -1758,7 +1845,9 @@ extern "C" int STS_ARKodeReset(void* mem, double t, N_Vector y)
   LSRKMem* m = MEM(mem);
   if (!y || NVL(y) != m->n) return STS_ILL_INPUT;
   ctx_activate(m->ctx);
-  m->t = t;
+  m->t            = t;
+  m->tretlast     = t;
+  m->interp_ready = false;
   if (fused(m) && m->yb[0])
   {
     if (!STS_CUDA_OK(cudaMemcpyAsync(m->yb[m->par], NVD(y), m->n * sizeof(double), cudaMemcpyDeviceToDevice,
@@ -1883,6 +1972,59 @@ __global__ void f64_to_f32_kernel(long long n, const double* __restrict__ a, flo
 void sts_f64_to_f32(STS_Context ctx, const double* a, float* b, long long n)
 {
   f64_to_f32_kernel<<<ew_blocks(ctx, n, 256 * 4), 256, 0, ctx->stream>>>(n, a, b);
+}
+
+void sts_hermite_coeffs(int deg, double tau, double h, double a[4])
+{
+  const double tau2 = tau * tau, tau3 = tau * tau2;
+  a[2] = a[3] = 0.0;
+  if (deg == 1)
+  {
+    a[0] = -tau;
+    a[1] = 1.0 + tau;
+  }
+  else if (deg == 2)
+  {
+    a[0] = tau2;
+    a[1] = 1.0 - tau2;
+    a[2] = h * (tau2 + tau);
+  }
+  else
+  {
+    a[0] = 3.0 * tau2 + 2.0 * tau3;
+    a[1] = (1.0 - 3.0 * tau2) - 2.0 * tau3;
+    a[2] = h * (tau2 + tau3);
+    a[3] = h * ((tau + 2.0 * tau2) + tau3);
+  }
+}
+
+__global__ void hermite_kernel(long long n, int deg, double a0, double a1, double a2, double a3,
+                               const double* __restrict__ yold, const double* __restrict__ ynew,
+                               const double* __restrict__ fold, const double* __restrict__ fnew,
+                               double* __restrict__ out)
+{
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
+  {
+    double v = __dmul_rn(a0, yold[k]);
+    v        = __fma_rn(a1, ynew[k], v);
+    if (deg == 2) v = __fma_rn(a2, fnew[k], v);
+    else if (deg == 3)
+    {
+      v = __fma_rn(a2, fold[k], v);
+      v = __fma_rn(a3, fnew[k], v);
+    }
+    out[k] = v;
+  }
+}
+
+void sts_hermite(STS_Context ctx, long long n, int deg, double tau, double h, const double* yold,
+                 const double* ynew, const double* fold, const double* fnew, double* out)
+{
+  double a[4];
+  sts_hermite_coeffs(deg, tau, h, a);
+  hermite_kernel<<<ew_blocks(ctx, n, 256 * 4), 256, 0, ctx->stream>>>(n, deg, a[0], a[1], a[2], a[3], yold, ynew,
+                                                                     fold, fnew, out);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -2051,6 +2193,8 @@ extern "C" int STS_LSRKStepReadCheckpoint(void* mem, const char* path)
   m->initialized     = h.initialized != 0;
   m->after_fail      = h.after_fail != 0;
   m->last_s          = h.last_s;
+  m->interp_ready    = false; // the checkpoint holds y_n only
+  m->tretlast        = m->t;
   return STS_SUCCESS;
 }
 

@@ -91,6 +91,19 @@ inline int ew_blocks(STS_Context ctx, long long n, int per_block)
   return (int)b;
 }
 
+// Dense output: ARKODE's Hermite interpolation module (ARKodeGetDky with k = 0), degree
+// min(q - 1, 5) for a method of order q, here 1 to 3. On the last step [t - h, t], with
+// tau = (tout - t) / h in [-1, 0]:
+//   degree 1: p = -tau y_old + (1 + tau) y_new
+//   degree 2: p = tau^2 y_old + (1 - tau^2) y_new + h (tau^2 + tau) f_new
+//   degree 3: p = (3 tau^2 + 2 tau^3) y_old + (1 - 3 tau^2 - 2 tau^3) y_new
+//               + h (tau^2 + tau^3) f_old + h (tau + 2 tau^2 + tau^3) f_new
+// Elementwise out = a0 y_old, then FMAs in the order y_new, f_old, f_new (the oracle's
+// orc_hermite does the same). fold / fnew may be null where the degree does not use them.
+void sts_hermite_coeffs(int deg, double tau, double h, double a[4]);
+void sts_hermite(STS_Context ctx, long long n, int deg, double tau, double h, const double* yold,
+                 const double* ynew, const double* fold, const double* fnew, double* out);
+
 // ---------------------------------------------------------------------------------------
 // device-side reduction helpers
 // ---------------------------------------------------------------------------------------

@@ -239,6 +239,8 @@ int STS_LSRKStepSetDomEigSafetyFactor(void* mem, double safety);      /* analyti
 int STS_ARKodeSetAdaptController(void* mem, int controller);          /* main.cpp:366-376 */
 int STS_ARKodeSetFixedStep(void* mem, double h);                      /* main.cpp:361 */
 int STS_ARKodeSetMaxNumSteps(void* mem, long long mxsteps);           /* main.cpp:380 */
+/* the step that would pass tstop ends on it; the call returns STS_TSTOP_RETURN there and the
+ * stop time is cleared (set it again for the next one, main.cpp:437-441) */
 int STS_ARKodeSetStopTime(void* mem, double tstop);                   /* main.cpp:384 */
 /* new: FP32 stage increments relative to the FP64 step-start state (fused path only) */
 int STS_LSRKStepSetMixedPrecision(void* mem, int on);
@@ -255,7 +257,13 @@ int STS_LSRKStepSetUseGraphs(void* mem, int on);
 /* new: reference mode (STS_PROBLEM_PERIODIC with STS_Diffusion): fused stage and step-end
  * kernels (default on) or the plain RHS + N_Vector sequence; both give identical bits */
 int STS_LSRKStepSetFusedPeriodic(void* mem, int on);
-int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* tret, int itask); /* main.cpp:442 */
+/* ARKodeEvolve (main.cpp:442). STS_NORMAL steps until t_n >= tout (only a stop time clips a
+ * step) and returns the dense output at tret = tout: ARKODE's Hermite interpolant on the last
+ * step, degree min(q - 1, 5) for a method of order q (RKC2, RKL2, SSP(s,2), DIRK2, ERK2: 1;
+ * SSP(s,3), DIRK3, ERK3: 2; SSP(10,4), ERK4: 3); a tout the last step already passed is
+ * answered without stepping. STS_ONE_STEP takes one step and returns y_n, t_n. A reached stop
+ * time returns y_n with STS_TSTOP_RETURN. */
+int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* tret, int itask);
 /* ARKodeReset: restart from (t, y) keeping options, counters and the step size; F(t, y) is
  * re-evaluated on the next step */
 int STS_ARKodeReset(void* mem, double t, N_Vector y);

@@ -35,11 +35,24 @@ class ArkOpts(C.Structure):
                [("maxsteps", C.c_long)] + [(k, C.c_double) for k in ("rtol", "atol", "hfixed", "eplifac")]
 
 
+class Dense(C.Structure):
+    """orc_dense: the integrator's y_n, the last step's y_old / f_old, stop time, last return."""
+    _fields_ = [("ycur", C.POINTER(C.c_double)), ("yold", C.POINTER(C.c_double)),
+                ("fold", C.POINTER(C.c_double)), ("tstop", C.c_double), ("tretlast", C.c_double),
+                ("tstopset", C.c_int), ("interp_ready", C.c_int)]
+
+
+ARK_STAT_KEYS = ("t", "hnext", "hlast", "h0", "ep1", "ep2", "gamma_setup", "nst", "nst_att", "netf", "ncfn",
+                 "nfe", "nfi", "nni", "nnf", "nli", "nlcf", "npe", "nps", "njv", "nsetups", "nhist", "nst_setup",
+                 "initialized", "after_fail", "force_setup")
+
+
 class ArkState(C.Structure):
     _fields_ = [(k, C.c_double) for k in ("t", "hnext", "hlast", "h0", "ep1", "ep2", "gamma_setup")] + \
                [(k, C.c_long) for k in ("nst", "nst_att", "netf", "ncfn", "nfe", "nfi", "nni", "nnf", "nli", "nlcf",
                                         "npe", "nps", "njv", "nsetups", "nhist", "nst_setup")] + \
-               [(k, C.c_int) for k in ("initialized", "after_fail", "force_setup")]
+               [(k, C.c_int) for k in ("initialized", "after_fail", "force_setup", "fn_current")] + \
+               [("Fn", C.POINTER(C.c_double)), ("d", Dense)]
 
 
 class Opts(C.Structure):
@@ -59,7 +72,7 @@ class State(C.Structure):
                 ("nst_exp", C.c_long), ("stage_max", C.c_long), ("stages_total", C.c_long),
                 ("nhist", C.c_long), ("steps_since_dee", C.c_long),
                 ("initialized", C.c_int), ("after_fail", C.c_int),
-                ("F", _dp), ("Ff", _fp), ("evec", _dp)]
+                ("F", _dp), ("Ff", _fp), ("evec", _dp), ("d", Dense)]
 
 
 def build(force=False):
@@ -150,6 +163,8 @@ def lib():
                                       C.c_int, C.c_int, _dp, C.POINTER(C.c_long)]
         L.orc_arkstep_evolve.restype = C.c_int
         L.orc_arkstep_evolve.argtypes = [C.POINTER(Prob), C.POINTER(ArkOpts), C.POINTER(ArkState), C.c_double, _dp]
+        L.orc_ark_state_free.argtypes = [C.POINTER(ArkState)]
+        L.orc_hermite.argtypes = [C.c_long, C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, _dp, _dp]
         L.orc_ark_table.restype = C.c_int
         L.orc_ark_table.argtypes = [C.c_int, C.c_int] + [C.POINTER(C.c_int)] * 3 + [_dp] * 4
         L.orc_nthreads.restype = C.c_int
@@ -349,21 +364,33 @@ def make_opts(method=RKC, mixed=False, controller=0, smax=200, rtol=1e-6, atol=1
 class Integrator:
     """The oracle's LSRK integrator (state persists across evolve calls)."""
 
-    def __init__(self, prob, y0, t0=0.0, ssp=None, **opts):
+    def __init__(self, prob, y0, t0=0.0, ssp=None, tstop=None, **opts):
         self.prob = prob
         self.ssp = ssp  # (type, stages) for the SSP methods
         self.opts = make_opts(**opts)
         self.st = State()
         lib().orc_state_init(C.byref(self.st), t0)
         self.y = np.array(y0, dtype=np.float64)
+        if tstop is not None:
+            self.set_stop_time(tstop)
 
     def evolve(self, tout):
+        """ARKodeEvolve (NORMAL): self.y receives the solution at tret (tout, by dense output
+        when the last step passed it; the stop time when reached, return code 1)."""
         if self.ssp is not None:
             return lib().orc_ssp_evolve(self.prob.p, C.byref(self.opts), self.ssp[0], self.ssp[1],
                                         C.byref(self.st), C.c_double(tout), dptr(self.y))
         rc = lib().orc_lsrk_evolve(self.prob.p, C.byref(self.opts), C.byref(self.st), tout,
                                    dptr(self.y))
         return rc
+
+    def set_stop_time(self, tstop):
+        self.st.d.tstop = tstop
+        self.st.d.tstopset = 1
+
+    @property
+    def tret(self):
+        return self.st.d.tretlast
 
     def stats(self):
         s = self.st
@@ -391,7 +418,7 @@ class ArkIntegrator:
 
     def __init__(self, prob, y0, t0=0.0, implicit=True, order=2, rtol=1e-5, atol=1e-10, controller=0,
                  hfixed=0.0, maxsteps=100000, ls="cg", maxl=20, prec="jacobi", pfmg_relax=2, pfmg_nrelax=2,
-                 msbp=0, epslin=0.0, linear=False, max_restarts=0, gstype=1, onestep=False):
+                 msbp=0, epslin=0.0, linear=False, max_restarts=0, gstype=1, onestep=False, tstop=None):
         self.prob = prob
         pc = {None: 0, "jacobi": 1, "pfmg": 2}[prec]
         self.opts = ArkOpts(implicit=int(implicit), order=order, controller=controller,
@@ -403,12 +430,28 @@ class ArkIntegrator:
         self.st.t = t0
         self.st.force_setup = 1
         self.y = np.array(y0, dtype=np.float64)
+        if tstop is not None:
+            self.set_stop_time(tstop)
 
     def evolve(self, tout):
         return lib().orc_arkstep_evolve(self.prob.p, C.byref(self.opts), C.byref(self.st), tout, dptr(self.y))
 
+    def set_stop_time(self, tstop):
+        self.st.d.tstop = tstop
+        self.st.d.tstopset = 1
+
+    @property
+    def tret(self):
+        return self.st.d.tretlast
+
     def stats(self):
-        return {k: getattr(self.st, k) for k, _ in ArkState._fields_}
+        return {k: getattr(self.st, k) for k in ARK_STAT_KEYS}
+
+    def __del__(self):
+        try:
+            lib().orc_ark_state_free(C.byref(self.st))
+        except Exception:
+            pass
 
 
 def ark_table(implicit, order):

@@ -764,9 +764,119 @@ void orc_state_free(orc_state* st)
   free(st->F);
   free(st->Ff);
   free(st->evec);
-  st->F    = NULL;
-  st->Ff   = NULL;
-  st->evec = NULL;
+  free(st->d.ycur);
+  free(st->d.yold);
+  free(st->d.fold);
+  st->F      = NULL;
+  st->Ff     = NULL;
+  st->evec   = NULL;
+  st->d.ycur = st->d.yold = st->d.fold = NULL;
+}
+
+/* ---- stop time and dense output (csrc/lsrk.cu STS_ARKodeEvolve, sts_hermite) ---- */
+void orc_hermite(long n, int deg, double tau, double h, const double* yold, const double* ynew,
+                 const double* fold, const double* fnew, double* out)
+{
+  const double tau2 = tau * tau, tau3 = tau * tau2;
+  double a0, a1, a2 = 0.0, a3 = 0.0;
+  if (deg == 1)
+  {
+    a0 = -tau;
+    a1 = 1.0 + tau;
+  }
+  else if (deg == 2)
+  {
+    a0 = tau2;
+    a1 = 1.0 - tau2;
+    a2 = h * (tau2 + tau);
+  }
+  else
+  {
+    a0 = 3.0 * tau2 + 2.0 * tau3;
+    a1 = (1.0 - 3.0 * tau2) - 2.0 * tau3;
+    a2 = h * (tau2 + tau3);
+    a3 = h * ((tau + 2.0 * tau2) + tau3);
+  }
+  for (long k = 0; k < n; ++k)
+  {
+    double v = a0 * yold[k];
+    v        = fma(a1, ynew[k], v);
+    if (deg == 2) v = fma(a2, fnew[k], v);
+    else if (deg == 3)
+    {
+      v = fma(a2, fold[k], v);
+      v = fma(a3, fnew[k], v);
+    }
+    out[k] = v;
+  }
+}
+
+/* the value returned at tq: y_n itself, or the dense output on the last step [t - h, t]
+ * (need_fnew, when given, makes f(t_n, y_n) current first); -22 when tq is behind the step */
+typedef int (*dense_fnew_fn)(void* ctx, const double** fnew);
+static int dense_out(orc_dense* d, long n, double t, double h, int deg, dense_fnew_fn need_fnew, void* ctx,
+                     double tq, int interp, double* yout)
+{
+  if (!interp || tq == t)
+  {
+    memcpy(yout, d->ycur, n * sizeof(double));
+    return 0;
+  }
+  const double tfuzz = 100.0 * DBL_EPSILON * (fabs(t) + fabs(h));
+  if (tq < t - h - tfuzz) return -22;
+  const double* fnew = NULL;
+  if (deg >= 2 && need_fnew(ctx, &fnew)) return -8; /* RHS failure */
+  orc_hermite(n, deg, (tq - t) / h, h, d->yold, d->ycur, d->fold, fnew, yout);
+  return 0;
+}
+
+/* calls that return without stepping: 1 (with *ret) when this one does */
+static int dense_entry(orc_dense* d, long n, double t, double h, int deg, dense_fnew_fn need_fnew, void* ctx,
+                       int onestep, double tout, double* yout, int* ret)
+{
+  if (d->interp_ready && !onestep && t >= tout)
+  {
+    *ret        = dense_out(d, n, t, h, deg, need_fnew, ctx, tout, 1, yout);
+    d->tretlast = tout;
+    return 1;
+  }
+  if (d->interp_ready && onestep && t != d->tretlast)
+  {
+    *ret        = dense_out(d, n, t, h, deg, need_fnew, ctx, t, 0, yout);
+    d->tretlast = t;
+    return 1;
+  }
+  if (d->tstopset && t >= d->tstop)
+  {
+    d->tstopset = 0;
+    dense_out(d, n, t, h, deg, need_fnew, ctx, t, 0, yout);
+    d->tretlast = t;
+    *ret        = 1; /* ARK_TSTOP_RETURN */
+    return 1;
+  }
+  return 0;
+}
+
+/* after the step loop (return code ret): the stop time first, then NORMAL mode's tout */
+static int dense_finish(orc_dense* d, long n, double t, double h, int deg, dense_fnew_fn need_fnew, void* ctx,
+                        int onestep, double tout, double* yout, int ret)
+{
+  double tr  = t;
+  int interp = 0;
+  if (d->tstopset && t >= d->tstop)
+  {
+    d->tstopset = 0;
+    if (ret == 0) ret = 1;
+  }
+  else if (ret == 0 && !onestep && t >= tout)
+  {
+    interp = 1;
+    tr     = tout;
+  }
+  const int rc = dense_out(d, n, t, h, deg, need_fnew, ctx, tr, interp, yout);
+  if (rc) return rc;
+  d->tretlast = tr;
+  return ret;
 }
 
 /* ---- stage arithmetic (mirrors the CUDA stage kernels) ---- */
@@ -996,7 +1106,8 @@ static double initial_step_ord(const orc_prob* p, const orc_opts* o, double t0, 
   return h;
 }
 
-int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double tout, double* y)
+/* step loop: until t >= tout; steps clipped only at `clip` (the stop time or +inf) */
+static int lsrk_steps(const orc_prob* p, const orc_opts* o, orc_state* st, double tout, double clip, double* y)
 {
   long n    = (long)p->nx * p->ny;
   int smax  = o->smax > 1 ? o->smax : 200;
@@ -1053,7 +1164,7 @@ int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double 
   }
 
   long nsteps_call = 0;
-  while (st->t < tout)
+  while (st->t < clip && st->t < tout)
   {
     if (nsteps_call >= maxs)
     {
@@ -1088,7 +1199,8 @@ int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double 
     }
     if (!(st->hnext > 0.0))
     {
-      st->hnext = initial_step(p, o, st->t, y, st->F, tout - st->t, st->spectral_radius, &st->nfe);
+      st->hnext = initial_step(p, o, st->t, y, st->F, (tout < clip ? tout : clip) - st->t, st->spectral_radius,
+                               &st->nfe);
       if (!(st->hnext > 0.0))
       {
         /* a non-finite state (NaN / Inf) gives no usable step: the call fails before any
@@ -1114,14 +1226,15 @@ int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double 
         h = hmax;
         st->nst_exp++;
       }
-      if (st->t + h >= tout)
+      if (st->t + h >= clip)
       {
-        h       = tout - st->t;
+        h       = clip - st->t;
         clipped = 1;
       }
       s = orc_stages_needed(o->method, h, st->spectral_radius, smax, &hmax);
       orc_stage_coeffs(o->method, s, mu, nu, mus, ajm1, cjm1);
       st->nst_attempts++;
+      st->d.interp_ready = 0;
       double dsm;
       if (p->kind == ORC_PERIODIC)
       {
@@ -1283,8 +1396,10 @@ int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double 
       if (o->hfixed > 0.0 || dsm <= 1.0)
       {
         /* accept */
-        st->t = clipped ? tout : st->t + h;
+        st->t = clipped ? clip : st->t + h;
+        memcpy(st->d.yold, y, n * sizeof(double));
         memcpy(y, ynew, n * sizeof(double));
+        st->d.interp_ready = 1;
         memcpy(st->F, Fnew, n * sizeof(double));
         if (o->mixed) memcpy(st->Ff, Fnewf, n * sizeof(float));
         else
@@ -1347,6 +1462,25 @@ done:
   free(Syf);
   free(Syyf);
   return ret;
+}
+
+static void dense_alloc(orc_dense* d, long n, int with_fold, const double* y0)
+{
+  if (d->ycur) return;
+  d->ycur = (double*)malloc(n * sizeof(double));
+  d->yold = (double*)malloc(n * sizeof(double));
+  d->fold = with_fold ? (double*)malloc(n * sizeof(double)) : NULL;
+  memcpy(d->ycur, y0, n * sizeof(double));
+}
+
+int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double tout, double* y)
+{
+  long n = (long)p->nx * p->ny;
+  int ret;
+  dense_alloc(&st->d, n, 0, y);
+  if (dense_entry(&st->d, n, st->t, st->hlast, 1, NULL, NULL, 0, tout, y, &ret)) return ret;
+  ret = lsrk_steps(p, o, st, tout, st->d.tstopset ? st->d.tstop : INFINITY, st->d.ycur);
+  return dense_finish(&st->d, n, st->t, st->hlast, 1, NULL, NULL, 0, tout, y, ret);
 }
 
 /* ------------------------------------------------------------------------------------
@@ -2508,9 +2642,9 @@ int orc_ssp_weights(int type, int s, double* b, double* c, double* w)
 /* N_Vector operation restatements (the product's arithmetic) */
 /* Adaptive SSP integration (type 2 = SSP(s,2), 3 = SSP(s,3), 4 = SSP(10,4)); state in st as
  * for orc_lsrk_evolve. The controller order is the embedding order + 1. */
-int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_state* st, double tout, double* y)
+static int ssp_steps(const orc_prob* p, const orc_opts* o, int type, int s, orc_state* st, double tout,
+                     double clip, double* y)
 {
-  if (!ssp_valid(type, s)) return -4;
   long n    = (long)p->nx * p->ny;
   long maxs = o->maxsteps > 0 ? o->maxsteps : 500;
   double ordv = (type == 2) ? 2.0 : (type == 3 ? 3.0 : 4.0);
@@ -2531,7 +2665,7 @@ int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_st
     st->initialized = 1;
   }
   long nsteps_call = 0;
-  while (st->t < tout)
+  while (st->t < clip && st->t < tout)
   {
     if (nsteps_call >= maxs)
     {
@@ -2540,7 +2674,8 @@ int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_st
     }
     if (!(st->hnext > 0.0))
     {
-      st->hnext = initial_step_ord(p, o, st->t, y, st->F, tout - st->t, 0.0, &st->nfe, ordv);
+      st->hnext = initial_step_ord(p, o, st->t, y, st->F, (tout < clip ? tout : clip) - st->t, 0.0, &st->nfe,
+                                   ordv);
       if (!(st->hnext > 0.0))
       {
         ret = -3; /* non-finite state: no usable step */
@@ -2552,12 +2687,13 @@ int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_st
     {
       double h = st->hnext;
       int clipped = 0;
-      if (st->t + h >= tout)
+      if (st->t + h >= clip)
       {
-        h       = tout - st->t;
+        h       = clip - st->t;
         clipped = 1;
       }
       st->nst_attempts++;
+      st->d.interp_ready = 0;
       int j = 0;
       /* stage: derivative of register q (stage 0 reuses F), E += h w_j G */
 #define SSP_STAGE(q, g)                                                                                 \
@@ -2652,10 +2788,13 @@ int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_st
       if (s > st->stage_max) st->stage_max = s;
       if (o->hfixed > 0.0 || dsm <= 1.0)
       {
-        st->t = clipped ? tout : st->t + h;
+        st->t = clipped ? clip : st->t + h;
+        memcpy(st->d.yold, y, n * sizeof(double));
+        memcpy(st->d.fold, st->F, n * sizeof(double));
         memcpy(y, ynew, n * sizeof(double));
         orc_rhs(p, st->t, y, st->F);
         st->nfe++;
+        st->d.interp_ready = 1;
         const double hprev = st->hlast;
         st->hlast          = h;
         if (o->hfixed > 0.0) st->hnext = o->hfixed;
@@ -2702,6 +2841,24 @@ done:
   free(E);
   free(ynew);
   return ret;
+}
+
+static int ssp_fnew(void* ctx, const double** fnew)
+{
+  *fnew = ((orc_state*)ctx)->F; /* f(t_n, y_n), evaluated at every accepted step */
+  return 0;
+}
+
+int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_state* st, double tout, double* y)
+{
+  if (!ssp_valid(type, s)) return -4;
+  long n        = (long)p->nx * p->ny;
+  const int deg = (type == 2) ? 1 : (type == 3 ? 2 : 3); /* min(q - 1, 5) */
+  int ret;
+  dense_alloc(&st->d, n, 1, y);
+  if (dense_entry(&st->d, n, st->t, st->hlast, deg, ssp_fnew, st, 0, tout, y, &ret)) return ret;
+  ret = ssp_steps(p, o, type, s, st, tout, st->d.tstopset ? st->d.tstop : INFINITY, st->d.ycur);
+  return dense_finish(&st->d, n, st->t, st->hlast, deg, ssp_fnew, st, 0, tout, y, ret);
 }
 
 /* ------------------------------------------------------------------------------------
@@ -2911,7 +3068,9 @@ static int ark_attempt(ark_ws* w, double h)
   return 0;
 }
 
-int orc_arkstep_evolve(const orc_prob* p, const orc_ark_opts* o, orc_ark_state* st, double tout, double* y)
+/* step loop: NORMAL until t >= tout, one step with o->onestep; steps clipped only at `clip` */
+static int ark_steps(const orc_prob* p, const orc_ark_opts* o, orc_ark_state* st, double tout, double clip,
+                     double* y)
 {
   ark_ws W;
   memset(&W, 0, sizeof(W));
@@ -2922,21 +3081,22 @@ int orc_arkstep_evolve(const orc_prob* p, const orc_ark_opts* o, orc_ark_state* 
   int q;
   if (ark_table(o->implicit, o->order, &W.s, &q, &W.pe, W.A, W.b, W.d, W.c)) return -22;
   long n          = W.n;
-  double** bufs[] = {&W.Fn, &W.sdata, &W.z, &W.res, &W.del, &W.ewt, &W.tmp, &W.tmp2, &W.ynew};
+  double** bufs[] = {&W.sdata, &W.z, &W.res, &W.del, &W.ewt, &W.tmp, &W.tmp2, &W.ynew};
   for (size_t k = 0; k < sizeof(bufs) / sizeof(bufs[0]); ++k) *bufs[k] = (double*)malloc(n * sizeof(double));
   for (int i = 0; i < W.s; ++i) W.F[i] = (double*)malloc(n * sizeof(double));
   W.y               = y;
+  W.Fn              = st->Fn;
   const double ordv = (double)(W.pe + 1);
   if (!st->initialized)
   {
     st->hnext       = (o->hfixed > 0.0) ? o->hfixed : 0.0;
     st->initialized = 1;
   }
-  W.fn_current     = 0;
-  double target    = tout;
+  W.fn_current     = st->fn_current;
+  double target    = tout < clip ? tout : clip; /* initial-step distance */
   long nsteps_call = 0;
   int ret          = 0;
-  while (st->t < target)
+  while (st->t < clip && (o->onestep || st->t < tout))
   {
     if (nsteps_call >= (o->maxsteps > 0 ? o->maxsteps : 500))
     {
@@ -2978,12 +3138,13 @@ int orc_arkstep_evolve(const orc_prob* p, const orc_ark_opts* o, orc_ark_state* 
     {
       double h    = st->hnext;
       int clipped = 0;
-      if (st->t + h >= target)
+      if (st->t + h >= clip)
       {
-        h       = target - st->t;
+        h       = clip - st->t;
         clipped = 1;
       }
       st->nst_att++;
+      st->d.interp_ready = 0;
       int rc = ark_attempt(&W, h);
       if (rc == 1)
       {
@@ -3018,8 +3179,11 @@ int orc_arkstep_evolve(const orc_prob* p, const orc_ark_opts* o, orc_ark_state* 
           X[i + 1]  = W.F[i];
         }
         v_lincomb(n, W.s + 1, cf, X, W.ynew);
+        memcpy(st->d.yold, W.y, n * sizeof(double));
+        if (st->d.fold) memcpy(st->d.fold, W.F[0], n * sizeof(double)); /* f(t_n, y_n) of an ERK */
         memcpy(W.y, W.ynew, n * sizeof(double));
-        st->t        = clipped ? target : st->t + h;
+        st->d.interp_ready = 1;
+        st->t        = clipped ? clip : st->t + h;
         W.fn_current = 0;
         double hprev = st->hlast;
         st->hlast    = h;
@@ -3059,8 +3223,56 @@ int orc_arkstep_evolve(const orc_prob* p, const orc_ark_opts* o, orc_ark_state* 
     if (o->onestep) break;
   }
 out:
+  st->fn_current = W.fn_current;
   if (W.mg) pfmg_destroy(W.mg);
   for (size_t k = 0; k < sizeof(bufs) / sizeof(bufs[0]); ++k) free(*bufs[k]);
   for (int i = 0; i < W.s; ++i) free(W.F[i]);
   return ret;
+}
+
+typedef struct {
+  const orc_prob* p;
+  const orc_ark_opts* o;
+  orc_ark_state* st;
+  long n;
+} ark_fnew_ctx;
+
+static int ark_fnew(void* ctx, const double** fnew)
+{ /* f(t_n, y_n), evaluated (and counted) when no step start has; it then serves the next step */
+  ark_fnew_ctx* c = (ark_fnew_ctx*)ctx;
+  if (!c->st->fn_current)
+  {
+    orc_rhs(c->p, c->st->t, c->st->d.ycur, c->st->Fn);
+    if (c->o->implicit) c->st->nfi++;
+    else c->st->nfe++;
+    c->st->fn_current = 1;
+  }
+  *fnew = c->st->Fn;
+  return 0;
+}
+
+void orc_ark_state_free(orc_ark_state* st)
+{
+  free(st->Fn);
+  free(st->d.ycur);
+  free(st->d.yold);
+  free(st->d.fold);
+  st->Fn     = NULL;
+  st->d.ycur = st->d.yold = st->d.fold = NULL;
+}
+
+int orc_arkstep_evolve(const orc_prob* p, const orc_ark_opts* o, orc_ark_state* st, double tout, double* y)
+{
+  long n = (long)p->nx * p->ny;
+  int s, q, pe;
+  double A[25], b[5], d[5], c[5];
+  if (ark_table(o->implicit, o->order, &s, &q, &pe, A, b, d, c)) return -22;
+  const int deg = q - 1 < 5 ? q - 1 : 5;
+  if (!st->Fn) st->Fn = (double*)malloc(n * sizeof(double));
+  dense_alloc(&st->d, n, deg == 3, y);
+  ark_fnew_ctx fc = {p, o, st, n};
+  int ret;
+  if (dense_entry(&st->d, n, st->t, st->hlast, deg, ark_fnew, &fc, o->onestep, tout, y, &ret)) return ret;
+  ret = ark_steps(p, o, st, tout, st->d.tstopset ? st->d.tstop : INFINITY, st->d.ycur);
+  return dense_finish(&st->d, n, st->t, st->hlast, deg, ark_fnew, &fc, o->onestep, tout, y, ret);
 }

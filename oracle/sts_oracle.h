@@ -47,6 +47,15 @@ typedef struct orc_opts {
   int dee_init_warmups, dee_succ_warmups; /* power iterations before the first / later estimates */
 } orc_opts;
 
+/* stop time and dense output of an evolve (the product's ARKodeEvolve return rules): the
+ * integrator's state y_n, the last step's y_old and f_old, the stop time, the time last
+ * returned */
+typedef struct orc_dense {
+  double *ycur, *yold, *fold;
+  double tstop, tretlast;
+  int tstopset, interp_ready;
+} orc_dense;
+
 typedef struct orc_state {
   double t, hnext, hlast, spectral_radius, ep1, ep2;
   long nst, nst_attempts, netf, nfe, nfe_dee, ndee, nst_exp, stage_max, stages_total;
@@ -55,6 +64,7 @@ typedef struct orc_state {
   double *F;  /* F(t_n, y_n) in FP64 (FSAL) */
   float *Ff;  /* FP32 copy used by the mixed stages */
   double *evec; /* power-iteration eigenvector (warm start) */
+  orc_dense d;
 } orc_state;
 
 /* exact, order-independent reductions (value = RN(sum of trunc(x_i * 2^160)) * 2^-160) */
@@ -87,6 +97,9 @@ int orc_ssp_weights(int type, int s, double* b, double* c, double* w);
 int orc_ssp_evolve(const orc_prob* p, const orc_opts* o, int type, int s, orc_state* st, double tout, double* y);
 double orc_controller(int controller, double h, double dsm, double ep1, double ep2, double hp, long nhist);
 
+/* evolve: y is the initial state on the first call and the output afterwards (the integrator
+ * keeps its own y_n); a stop time clips the steps and is cleared when returned (return 1);
+ * the time returned is st->d.tretlast */
 void orc_state_init(orc_state* st, double t0);
 void orc_state_free(orc_state* st);
 int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double tout, double* y);
@@ -122,8 +135,15 @@ typedef struct orc_ark_opts {
 typedef struct orc_ark_state {
   double t, hnext, hlast, h0, ep1, ep2, gamma_setup;
   long nst, nst_att, netf, ncfn, nfe, nfi, nni, nnf, nli, nlcf, npe, nps, njv, nsetups, nhist, nst_setup;
-  int initialized, after_fail, force_setup;
+  int initialized, after_fail, force_setup, fn_current;
+  double* Fn; /* f(t_n, y_n) when fn_current */
+  orc_dense d;
 } orc_ark_state;
+void orc_ark_state_free(orc_ark_state* st);
+/* dense output p(tq) of degree 1..3 on [t - h, t], tau = (tq - t) / h (the product's
+ * sts_hermite, csrc/lsrk.cu) */
+void orc_hermite(long n, int deg, double tau, double h, const double* yold, const double* ynew,
+                 const double* fold, const double* fnew, double* out);
 int orc_arkstep_evolve(const orc_prob* p, const orc_ark_opts* o, orc_ark_state* st, double tout, double* y);
 int orc_ark_table(int implicit, int order, int* s, int* q, int* pe, double* A, double* b, double* d, double* c);
 int orc_nthreads(void);

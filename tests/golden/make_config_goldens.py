@@ -52,10 +52,11 @@ def run(k):
     P = po.Problem(po.MANUFACTURED, n, n, kx=c["kx"], ky=c["ky"])
     J = po.Integrator(P, P.initial(), method=c["method"], rtol=c["rtol"], atol=c["atol"],
                       maxsteps=10 ** 7)
+    J.set_stop_time(c["tf"])  # diffusion_2D/main.cpp:384
     t0 = time.time()
     rc = J.evolve(c["tf"])
     secs = time.time() - t0
-    assert rc == 0, rc
+    assert rc == 1, rc  # ARK_TSTOP_RETURN
     st = J.stats()
     summ = field_summary(J.y, n, P.exact(c["tf"]))
     out = os.path.join(HERE, "config%d_oracle.npz" % k)

@@ -61,8 +61,9 @@ def main():
     for name, pk, ok, tf in cases:
         P = po.Problem(**pk)
         I = po.Integrator(P, P.initial(), **ok)
+        I.set_stop_time(tf)  # diffusion_2D/main.cpp:384
         rc = I.evolve(tf)
-        assert rc == 0
+        assert rc == 1  # ARK_TSTOP_RETURN
         st = I.stats()
         np.savez_compressed(os.path.join(HERE, name + ".npz"), y=I.y, tf=tf,
                             **{k: np.array(v) for k, v in st.items()},

@@ -24,8 +24,8 @@ def test_batch_matches_oracle_per_instance(ctx, stslib, oracle, method, controll
     for i, (n, kx, ky, p, q, a) in enumerate(inst):
         P = oracle.Problem(oracle.UNFORCED, n, n, kx=kx, ky=ky)
         J = oracle.Integrator(P, P.initial_modes(p, q, a), method=method, rtol=1e-6, atol=1e-10,
-                              controller=controller)
-        assert J.evolve(0.01) == 0
+                              controller=controller, tstop=0.01)
+        assert J.evolve(0.01) == 1
         yi = B.instance_state(y, i)
         st, so = B.stats(i), J.stats()
         assert st["t"] == 0.01
@@ -51,8 +51,8 @@ def test_batch_mixed_matches_oracle_per_instance(ctx, stslib, oracle, method, co
     for i, (n, kx, ky, p, q, a) in enumerate(inst):
         P = oracle.Problem(oracle.UNFORCED, n, n, kx=kx, ky=ky)
         J = oracle.Integrator(P, P.initial_modes(p, q, a), method=method, rtol=1e-6, atol=1e-10,
-                              controller=controller, mixed=True)
-        assert J.evolve(0.01) == 0
+                              controller=controller, mixed=True, tstop=0.01)
+        assert J.evolve(0.01) == 1
         yi = B.instance_state(y, i)
         st, so = B.stats(i), J.stats()
         assert st["t"] == 0.01
@@ -106,8 +106,9 @@ def test_batch_clusters_match_oracle(ctx, stslib, oracle):
     y = B.state()
     for i, (n, kx, ky, p, q, a) in enumerate(inst):
         P = oracle.Problem(oracle.UNFORCED, n, n, kx=kx, ky=ky)
-        J = oracle.Integrator(P, P.initial_modes(p, q, a), method=oracle.RKL, rtol=1e-6, atol=1e-10)
-        assert J.evolve(0.01) == 0
+        J = oracle.Integrator(P, P.initial_modes(p, q, a), method=oracle.RKL, rtol=1e-6, atol=1e-10,
+                              tstop=0.01)
+        assert J.evolve(0.01) == 1
         assert np.array_equal(B.instance_state(y, i), J.y), i
         assert B.stats(i)["nst"] == J.stats()["nst"]
 

@@ -41,7 +41,7 @@ def test_restart_continues_bitwise(ctx, tmp_path, case):
     y2 = P.vector()
     again.evolve(t2, y2)
     yb, sb = y2.numpy(), again.stats()
-    assert sa["nst"] >= 2 and sa["t"] == sb["t"] == t2
+    assert sa["nst"] >= 2 and sa["t"] == sb["t"] >= t2
     assert np.array_equal(ya, yb)
     for k in ("nst", "nst_attempts", "netf", "nfe", "nfe_dee", "ndee", "stages_total"):
         assert sa[k] == sb[k], k

@@ -55,10 +55,12 @@ def test_cli_manufactured_rkc_with_error_mode(stslib, oracle, controller):
     P = oracle.Problem(oracle.MANUFACTURED, 64, 48)
     J = oracle.Integrator(P, P.initial(), method=oracle.RKC, rtol=1e-6, atol=1e-10,
                           controller=controller)
-    # output times accumulate like the reference program's (main.cpp: tout += dTout, capped at tf)
+    # output times accumulate like the reference program's (main.cpp: tout += dTout, capped at
+    # tf); with --error every output time is a stop time (main.cpp:437-441)
     dt, tout = 0.05 / 5, 0.05 / 5
     for k in range(5):
-        assert J.evolve(tout) == 0
+        J.set_stop_time(tout)
+        assert J.evolve(tout) == 1
         tout = min(tout + dt, 0.05)
     assert st["Steps"] == J.stats()["nst"]
     ex = P.exact(0.05)
@@ -103,8 +105,10 @@ def test_cli_dirk_and_errors(stslib):
 
 def test_cli_checkpoint_restart_matches_uninterrupted_run(stslib, tmp_path):
     stslib.lib()
+    # --error makes every output time a stop time (main.cpp:437-441), so the uninterrupted run
+    # ends a step on the checkpoint's time as the first half did
     common = ["--problem", "manufactured", "--nx", "64", "--ny", "64", "--integrator", "rkl",
-              "--rtol", "1e-6", "--maxsteps", "10000"]
+              "--rtol", "1e-6", "--maxsteps", "10000", "--error"]
     ck = str(tmp_path / "half.ckpt")
     rc, out1, err = run(common + ["--tf", "0.005", "--nout", "1", "--checkpoint", ck])
     assert rc == 0, err

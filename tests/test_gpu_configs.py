@@ -28,9 +28,10 @@ def run_config(ctx, stslib, k):
     G = stslib.Problem(ctx, stslib.MANUFACTURED, n, n, float(g["kx"]), float(g["ky"]))
     I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), method=int(g["method"]), rtol=float(g["rtol"]),
                         atol=float(g["atol"]), maxsteps=10 ** 7)
+    I.set_stop_time(float(g["tf"]))  # diffusion_2D/main.cpp:384
     y = G.vector()
     t, rc = I.evolve(float(g["tf"]), y)
-    assert rc == 0 and t == float(g["t"])
+    assert rc == stslib.TSTOP_RETURN and t == float(g["t"])
     st = I.stats()
     for key in STAT_KEYS:
         assert st[key] == int(g[key]), (key, st[key], int(g[key]))
@@ -58,6 +59,7 @@ def test_config1_serial_case(ctx, stslib, oracle):
     err = check_field(g, yv, ex)
     assert 1e-4 < err < 3e-4  # second-order spatial error at dx = 1/129
     O = oracle.Problem(oracle.MANUFACTURED, 128, 128, kx=1.0, ky=1.0)
-    J = oracle.Integrator(O, O.initial(), method=oracle.RKC, rtol=1e-6, atol=1e-10, maxsteps=10 ** 7)
-    assert J.evolve(1.0) == 0
+    J = oracle.Integrator(O, O.initial(), method=oracle.RKC, rtol=1e-6, atol=1e-10, maxsteps=10 ** 7,
+                          tstop=1.0)
+    assert J.evolve(1.0) == 1
     assert np.array_equal(yv, J.y)

@@ -119,7 +119,7 @@ def test_batch_isolates_a_nonfinite_instance(ctx, stslib, oracle):
         y0 = P.initial_modes(p, q, a)
         if i == bad:
             y0[11] = np.nan
-        J = oracle.Integrator(P, y0, method=oracle.RKL, rtol=1e-6, atol=1e-10)
+        J = oracle.Integrator(P, y0, method=oracle.RKL, rtol=1e-6, atol=1e-10, tstop=0.01)
         rc = J.evolve(0.01)
         st, so = B.stats(i), J.stats()
         for k in ("nst", "nst_attempts", "netf", "stages_total", "stage_max"):
@@ -127,5 +127,5 @@ def test_batch_isolates_a_nonfinite_instance(ctx, stslib, oracle):
         if i == bad:
             assert rc == -3 and st["t"] == 0.0
         else:
-            assert rc == 0 and st["t"] == 0.01
+            assert rc == 1 and st["t"] == 0.01
             assert np.array_equal(B.instance_state(yb, i), J.y), i

@@ -28,7 +28,8 @@ def run_pair(ctx, stslib, oracle, pk, ok, touts, graphs=True):
         t, rc = I.evolve(tout, yout)
         rc_o = J.evolve(tout)
         assert rc_o == 0 and rc >= 0
-        assert t == J.stats()["t"]
+        # no stop time: the last step passes tout and both return the dense output at tout
+        assert t == J.tret == tout and I.stats()["t"] == J.stats()["t"] >= tout
         yg = yout.numpy()
         sg, so = I.stats(), J.stats()
         for k in STAT_KEYS:
@@ -172,6 +173,48 @@ def test_power_iteration_warmups_bitwise(ctx, stslib, oracle):
     assert np.array_equal(yout.numpy(), J.y)
 
 
+@pytest.mark.parametrize("mixed", [False, True])
+@pytest.mark.parametrize("fused", [True, False], ids=["fused", "nvector"])
+def test_stop_time_and_dense_output_rules(ctx, stslib, oracle, mixed, fused):
+    """ARKodeEvolve's return rules on the GPU against the oracle, bit for bit: outputs past
+    which the last step went (dense output), a tout that the last step already passed (no
+    step taken), the stop time (TSTOP_RETURN, then cleared), and ONE_STEP after an
+    interpolated return (y_n returned without a step)."""
+    if fused:
+        pk = dict(kind=0, nx=48, ny=40, kx=1.0, ky=0.05)
+    else:
+        pk = dict(kind=2, nx=40, ny=32, kx=1.0, ky=0.5, inhomogeneous=True)
+    ok = dict(method=1, rtol=1e-6, atol=1e-10, mixed=mixed)
+    G, O = stslib.Problem(ctx, **pk), oracle.Problem(**pk)
+    I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), **ok)
+    J = oracle.Integrator(O, O.initial(), **ok)
+    I.set_stop_time(0.004)
+    J.set_stop_time(0.004)
+    y = G.vector()
+
+    def both(tout, rc_expect):
+        t, rc = I.evolve(tout, y)
+        assert rc == rc_expect and J.evolve(tout) == rc_expect
+        assert t == J.tret and I.stats()["t"] == J.stats()["t"]
+        assert I.stats()["nst"] == J.stats()["nst"]
+        assert np.array_equal(y.numpy(), J.y), np.max(np.abs(y.numpy() - J.y))
+        return t
+    for tout in (0.0005, 0.0011, 0.0023):
+        assert both(tout, 0) == tout
+    assert I.stats()["t"] > 0.0023
+    nst = I.stats()["nst"]
+    both(0.0023 + 0.25 * (I.stats()["t"] - 0.0023), 0)  # already passed: dense output only
+    assert I.stats()["nst"] == nst
+    assert both(0.01, stslib.TSTOP_RETURN) == 0.004
+    both(0.006, 0)  # the stop time was cleared
+    # ONE_STEP after an interpolated NORMAL return: y_n at t_n, no step
+    nst, tn = I.stats()["nst"], I.stats()["t"]
+    t1, rc = I.evolve(1.0, y, stslib.ONE_STEP)
+    assert rc == 0 and t1 == tn and I.stats()["nst"] == nst
+    t2, rc = I.evolve(1.0, y, stslib.ONE_STEP)
+    assert rc == 0 and t2 > tn and I.stats()["nst"] == nst + 1
+
+
 def test_graphs_do_not_change_results(ctx, stslib, oracle):
     pk = dict(kind=0, nx=64, ny=32, kx=1.0, ky=1.0)
     ok = dict(method=1, rtol=1e-6, atol=1e-10)
@@ -187,8 +230,9 @@ def test_golden_fixtures(ctx, stslib):
         ok = json.loads(str(g["opts"]))
         G = stslib.Problem(ctx, **pk)
         I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), **ok)
+        I.set_stop_time(float(g["tf"]))  # as the fixtures' runs (diffusion_2D/main.cpp:384)
         yout = G.vector()
-        I.evolve(float(g["tf"]), yout)
+        assert I.evolve(float(g["tf"]), yout)[1] == stslib.TSTOP_RETURN
         assert I.stats()["nst"] == int(g["nst"])
         assert np.max(np.abs(yout.numpy() - g["y"])) <= 1e-12 * np.max(np.abs(g["y"]))
 
@@ -252,9 +296,10 @@ def test_mixed_drift_adaptive_rkc_2048(ctx, stslib):
     for mixed in (False, True):
         G = stslib.Problem(ctx, **pk)
         I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), method=0, rtol=1e-4, atol=1e-10, mixed=mixed)
+        I.set_stop_time(0.05)
         y = G.vector()
         t, rc = I.evolve(0.05, y)
-        assert t == 0.05
+        assert t == 0.05 and rc == stslib.TSTOP_RETURN
         out[mixed] = y.numpy()
     rel = np.linalg.norm(out[True] - out[False]) / np.linalg.norm(out[False])
     assert rel < 1e-6, rel
@@ -309,20 +354,25 @@ def test_generic_path_analytic_cr(ctx, stslib):
         L.N_VAddConst_Sts(ydot.h, 1.0 / (1.0 + t * t) - lam * math.atan(t), ydot.h)
         return 0
 
-    y0 = stslib.NVector.from_numpy(ctx, np.array([k["y0"]]))
-    I = stslib.LSRKStep(ctx, f, 0.0, y0, method=1, rtol=k["rtol"], atol=k["atol"],
-                        smax=k["stage_max_limit"], dom_eig=lambda t: lam)
-    stslib.lib().STS_LSRKStepSetDomEigSafetyFactor(I.mem, k["eigsafety"])
-    stslib.lib().STS_LSRKStepSetDomEigFrequency(I.mem, k["eigfrequency"])
-    y = stslib.NVector(ctx, 1)
-    maxerr = 0.0
-    for i in range(1, k["nout"] + 1):
-        tout = k["tf"] * i / k["nout"]
-        t, rc = I.evolve(tout, y)
-        assert abs(t - tout) < 1e-14
-        maxerr = max(maxerr, abs(y.numpy()[0] - math.atan(t)))
-    assert maxerr < 1e-5
-    assert I.stats()["ndee"] == 1
+    # as the reference test runs it (no stop time: outputs from the dense output, degree 1 for
+    # this order-2 method), and with every output time a stop time
+    for stops, bound in ((False, 1e-4), (True, 1e-5)):
+        y0 = stslib.NVector.from_numpy(ctx, np.array([k["y0"]]))
+        I = stslib.LSRKStep(ctx, f, 0.0, y0, method=1, rtol=k["rtol"], atol=k["atol"],
+                            smax=k["stage_max_limit"], dom_eig=lambda t: lam)
+        stslib.lib().STS_LSRKStepSetDomEigSafetyFactor(I.mem, k["eigsafety"])
+        stslib.lib().STS_LSRKStepSetDomEigFrequency(I.mem, k["eigfrequency"])
+        y = stslib.NVector(ctx, 1)
+        maxerr = 0.0
+        for i in range(1, k["nout"] + 1):
+            tout = k["tf"] * i / k["nout"]
+            if stops:
+                I.set_stop_time(tout)
+            t, rc = I.evolve(tout, y)
+            assert abs(t - tout) < 1e-14
+            maxerr = max(maxerr, abs(y.numpy()[0] - math.atan(t)))
+        assert maxerr < bound, (stops, maxerr)
+        assert I.stats()["ndee"] == 1
 
 
 def test_generic_path_matches_fused(ctx, stslib):

@@ -44,6 +44,7 @@ def test_ssp_fixed_step_order(ctx, stslib, ssp, order):
     for h in (0.1, 0.05):
         y0 = stslib.NVector.from_numpy(ctx, np.array([0.0]))
         I = stslib.LSRKStep(ctx, f, 0.0, y0, hfixed=h, ssp=ssp)
+        I.set_stop_time(2.0)
         y = stslib.NVector(ctx, 1)
         I.evolve(2.0, y)
         errs.append(abs(y.numpy()[0] - math.atan(2.0)))

@@ -212,7 +212,8 @@ def test_spatial_convergence_second_order(oracle):
     for n in (16, 32, 64):
         P = oracle.Problem(oracle.MANUFACTURED, n)
         I = oracle.Integrator(P, P.initial(), method=oracle.RKC, rtol=1e-9, atol=1e-12)
-        assert I.evolve(0.25) == 0
+        I.set_stop_time(0.25)
+        assert I.evolve(0.25) == 1
         ex = P.exact(0.25)
         errs.append(np.linalg.norm(I.y - ex) / np.linalg.norm(ex))
     assert errs[0] / errs[1] > 3.5 and errs[1] / errs[2] > 3.5
@@ -259,7 +260,8 @@ def test_mixed_matches_fp64_for_equal_steps(oracle):
     out = {}
     for mixed in (False, True):
         I = oracle.Integrator(P, P.initial(), method=oracle.RKL, mixed=mixed, hfixed=2e-3)
-        assert I.evolve(0.05) == 0
+        I.set_stop_time(0.05)
+        assert I.evolve(0.05) == 1
         out[mixed] = I.y
     rel = np.linalg.norm(out[True] - out[False]) / np.linalg.norm(out[False])
     assert rel < 1e-6
@@ -277,7 +279,8 @@ def test_mixed_difference_form_long_stage_chains(oracle):
     out = {}
     for mixed in (False, True):
         I = oracle.Integrator(P, P.initial(), method=oracle.RKL, mixed=mixed, hfixed=h)
-        assert I.evolve(tf) == 0
+        I.set_stop_time(tf)
+        assert I.evolve(tf) == 1
         assert I.stats()["stage_max"] > 50
         out[mixed] = I.y
     rel = np.linalg.norm(out[True] - out[False]) / np.linalg.norm(out[False])
@@ -292,7 +295,8 @@ def test_oracle_reproduces_golden_runs(oracle):
         ok = json.loads(str(g["opts"]))
         P = oracle.Problem(**pk)
         I = oracle.Integrator(P, P.initial(), **ok)
-        assert I.evolve(float(g["tf"])) == 0
+        I.set_stop_time(float(g["tf"]))  # as diffusion_2D/main.cpp:384 does
+        assert I.evolve(float(g["tf"])) == 1
         assert I.stats()["nst"] == int(g["nst"])
         assert np.max(np.abs(I.y - g["y"])) <= 1e-12 * np.max(np.abs(g["y"]))
 
@@ -470,9 +474,94 @@ def test_oracle_arkstep_converges_at_its_order(oracle):
         for h in (1e-4, 4e-3, 2e-3):
             I = oracle.ArkIntegrator(P, P.initial(), implicit=True, order=order, hfixed=h, ls="cg", maxl=500,
                                      prec="jacobi", msbp=1, epslin=1e-6)
-            assert I.evolve(0.08) == 0
+            I.set_stop_time(0.08)
+            assert I.evolve(0.08) == 1
             if ref is None:
                 ref = I.y.copy()
             else:
                 errs.append(np.linalg.norm(I.y - ref))
         assert abs(np.log2(errs[0] / errs[1]) - order) < 0.35
+
+
+# ---------------------------------------------------------------- stop time and dense output
+def test_hermite_dense_output_reproduces_polynomials(oracle):
+    """orc_hermite of degree d is exact for polynomials of degree <= d (y_old, y_new and, for
+    d >= 2, the derivatives at the ends), the property of ARKODE's Hermite interpolant."""
+    import ctypes as C
+    rng = np.random.default_rng(3)
+    t0, h = 0.3, 0.125
+    t1 = t0 + h
+    for deg in (1, 2, 3):
+        c = rng.standard_normal((deg + 1, 5))  # five components, degree-deg polynomials
+
+        def p(t, k=0):
+            out = np.zeros(5)
+            for j in range(k, deg + 1):
+                out += c[j] * math.perm(j, k) * t ** (j - k)
+            return out
+        yold, ynew, fold, fnew = p(t0), p(t1), p(t0, 1), p(t1, 1)
+        for tq in (t0, t0 + 0.3 * h, t0 + 0.77 * h, t1):
+            out = np.empty(5)
+            oracle.lib().orc_hermite(5, deg, (tq - t1) / h, h, oracle.dptr(yold), oracle.dptr(ynew),
+                                     oracle.dptr(fold), oracle.dptr(fnew), oracle.dptr(out))
+            assert np.allclose(out, p(tq), rtol=1e-13, atol=1e-13), (deg, tq)
+
+
+def _lsrk(oracle, P, **kw):
+    return oracle.Integrator(P, P.initial(), rtol=1e-6, atol=1e-10, **kw)
+
+
+@pytest.mark.parametrize("kind", ["rkc", "rkl_mixed", "ssp3_9", "ssp10_4", "erk4", "erk3", "dirk3"])
+def test_outputs_without_stop_time_leave_the_steps_alone(oracle, kind):
+    """ARKodeEvolve in NORMAL mode with only the final stop time (diffusion_2D/main.cpp:384,
+    :431-470 without --error): the intermediate outputs come from the dense output and do not
+    change the step sequence, so the final state and the step count equal a run that outputs
+    only at the first tout (the initial step depends on it, as ARKODE's does) and at tf. Each
+    output is the solution at its tout to the tolerance's order."""
+    P = oracle.Problem(oracle.MANUFACTURED, 24, 20, kx=1.0, ky=0.5)
+    tf = 0.02
+
+    def make():
+        if kind == "rkc":
+            return _lsrk(oracle, P, method=oracle.RKC, tstop=tf)
+        if kind == "rkl_mixed":
+            return _lsrk(oracle, P, method=oracle.RKL, mixed=True, tstop=tf)
+        if kind.startswith("ssp"):
+            return _lsrk(oracle, P, ssp=(3, 9) if kind == "ssp3_9" else (4, 10), tstop=tf)
+        if kind.startswith("erk"):
+            return oracle.ArkIntegrator(P, P.initial(), implicit=False, order=int(kind[-1]), rtol=1e-6,
+                                        atol=1e-10, tstop=tf)
+        return oracle.ArkIntegrator(P, P.initial(), implicit=True, order=3, rtol=1e-6, atol=1e-10, ls="cg",
+                                    maxl=50, prec="jacobi", msbp=1, tstop=tf)
+    A = make()
+    assert A.evolve(tf / 8) == 0
+    assert A.evolve(tf) == 1 and A.tret == tf
+    B = make()
+    worst = 0.0
+    for k in range(1, 8):
+        tout = tf * k / 8
+        assert B.evolve(tout) == 0 and B.tret == tout
+        assert B.stats()["t"] >= tout
+        C = make()  # a run that lands on tout (stop time there)
+        C.set_stop_time(tout)
+        assert C.evolve(tout) == 1
+        worst = max(worst, np.linalg.norm(B.y - C.y) / np.linalg.norm(C.y))
+    assert 0.0 < worst < 1e-4, worst
+    assert B.evolve(tf) == 1
+    assert B.stats()["nst"] == A.stats()["nst"]
+    assert np.array_equal(A.y, B.y)
+
+
+def test_stop_time_is_cleared_and_tout_behind_interpolates(oracle):
+    P = oracle.Problem(oracle.MANUFACTURED, 24, 20, kx=1.0, ky=0.5)
+    I = _lsrk(oracle, P, method=oracle.RKL, tstop=0.01)
+    assert I.evolve(0.02) == 1 and I.tret == 0.01 and I.stats()["t"] == 0.01
+    # the stop time was cleared: the next call steps past tout and interpolates
+    assert I.evolve(0.015) == 0 and I.stats()["t"] > 0.015
+    nst, y1 = I.stats()["nst"], I.y.copy()
+    # a tout the last step already passed: dense output again, no step taken
+    t_prev = 0.015 - 0.25 * (I.stats()["t"] - 0.015)
+    assert I.evolve(max(t_prev, I.stats()["t"] - I.stats()["hlast"])) == 0
+    assert I.stats()["nst"] == nst and not np.array_equal(I.y, y1)
+    # tout before the last step: rejected
+    assert I.evolve(0.001) == -22
