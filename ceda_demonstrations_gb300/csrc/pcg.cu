@@ -7,9 +7,14 @@
 // iteration needs no host round trip. Iterations are issued in batches captured in a CUDA
 // graph; kernels return immediately once the device-side flag says the solve has stopped,
 // and the host reads the flag between batches. Per iteration:
-//   KP: p = beta p + D r                                   (24 B/DOF)
-//   KQ: q = p - gamma A p, p.q -> alpha = rz / p.q          (16 B/DOF + halo)
-//   KX: x += alpha p, r -= alpha q, r.r, r.(D r) -> beta    (48 B/DOF)
+//   KP: p = beta p + D r                                   (24 B/DOF, 2 FP64)
+//   KQ: q = (I - gamma A) p, p.q -> alpha = rz / p.q        (16 B/DOF + halo, 6 FP64)
+//   KX: x += alpha p, r -= alpha q, r.r -> beta             (48 B/DOF, 3 FP64)
+// The Jacobi scaling D is one constant for these constant-coefficient problems, so
+// r.z = r.(D r) is taken as D (r.r): one exact sum per iteration. GB300 issues FP64 at a
+// small fraction of its FP32 rate (about 5e11 FP64 instructions/s measured), so these 11 FP64
+// instructions per point, not the 88 bytes, bound an iteration; the elementwise kernels
+// keep four independent points in flight per thread to hide the memory latency.
 // All dot products use the exact accumulator, so the iterates match the CPU oracle bit
 // for bit and do not depend on the launch shape.
 #include <cuda_runtime.h>
@@ -52,25 +57,40 @@ struct PcgWork {
 
 static constexpr int PCG_BATCH = 8; // iterations per graph launch (even: p ping-pong)
 
-// initial scalars: rz = r.(D r) with r = b, bnorm via b.b
+// reduction kernels: two grid-strided points per thread and trip (independent loads in
+// flight) on one wave of resident blocks, so each block pays the exact-sum combine once
+// (a 2048^2 sweep of unroll depth and grid on GB300: 45 us against 59 us for four points
+// on eight blocks per SM)
+constexpr int PCG_U = 2;
+
+// one wave of resident blocks of a 256-thread reduction kernel, at most one trip's worth
+template <typename K>
+static int resident_blocks(STS_Context ctx, K kernel, long long n, int per_thread)
+{
+  int occ = 0;
+  if (!STS_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0)) || occ < 1) occ = 1;
+  long long b         = (long long)ctx->num_sms * occ;
+  const long long cap = (n + 256LL * per_thread - 1) / (256LL * per_thread);
+  if (b > cap) b = cap;
+  return b < 1 ? 1 : (int)b;
+}
+
+// initial scalars: rr = b.b, rz = D rr (r = b)
 __global__ void __launch_bounds__(256) pcg_init_kernel(long long n, const double* __restrict__ b,
                                                        PcgScal* s)
 {
-  const double D = s->D;
-  xsum::Limbs a[2];
-  unsigned fl[2] = {0, 0};
+  xsum::Limbs a[1];
+  unsigned fl[1] = {0};
   xsum::zero(a[0]);
-  xsum::zero(a[1]);
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
   {
     const double r = b[k];
-    xsum::add(a[0], r * (D * r), fl[0]);
-    xsum::add(a[1], r * r, fl[1]);
+    xsum::add(a[0], r * r, fl[0]);
   }
-  krylov_block_finish<256, 2>(a, fl, s, [&](const double* v) {
-    s->rz   = v[0];
-    s->rr   = v[1];
+  krylov_block_finish<256, 1>(a, fl, s, [&](const double* v) {
+    s->rr   = v[0];
+    s->rz   = s->D * v[0];
     s->beta = 0.0;
   });
 }
@@ -86,12 +106,14 @@ __global__ void __launch_bounds__(256) pcg_p_kernel(long long n, const double* _
     pnew[k] = __fma_rn(beta, pold[k], D * r[k]);
 }
 
-// q = p - gamma A p (Dirichlet operator), accumulate p.q; alpha = rz / p.q
+// q = (I - gamma A) p (Dirichlet operator) with the coefficients folded,
+// q = c0 p_C + c1 (p_W + p_E) + c2 (p_S + p_N); accumulate p.q; alpha = rz / p.q
 __global__ void __launch_bounds__(256) pcg_q_kernel(ProbDev P, const double* __restrict__ p,
                                                     double* __restrict__ q, PcgScal* s)
 {
   if (s->state != 0) return;
   const double gamma = s->gamma;
+  const double c0 = 1.0 - gamma * P.cc, c1 = -gamma * P.cx, c2 = -gamma * P.cy;
   xsum::Limbs a[1];
   unsigned fl[1] = {0};
   xsum::zero(a[0]);
@@ -107,10 +129,7 @@ __global__ void __launch_bounds__(256) pcg_q_kernel(ProbDev P, const double* __r
       const double ps   = (j > 0) ? p[k - nx] : 0.0;
       const double pn   = (j < ny - 1) ? p[k + nx] : 0.0;
       const double sx = pw + pe, sy = ps + pn;
-      double acc = P.cc * pc;
-      acc        = __fma_rn(P.cx, sx, acc);
-      acc        = __fma_rn(P.cy, sy, acc);
-      const double qk = __fma_rn(-gamma, acc, pc);
+      const double qk = __fma_rn(c1, sx, __fma_rn(c2, sy, c0 * pc));
       q[k]            = qk;
       xsum::add(a[0], pc * qk, fl[0]);
     }
@@ -125,21 +144,38 @@ __global__ void __launch_bounds__(256) pcg_x_kernel(long long n, const double* _
                                                     double* __restrict__ r, PcgScal* s, PcgOut* out)
 {
   if (s->state != 0) return;
-  const double alpha = s->alpha, D = s->D;
-  xsum::Limbs a[2];
-  unsigned fl[2] = {0, 0};
+  const double alpha = s->alpha;
+  xsum::Limbs a[1];
+  unsigned fl[1] = {0};
   xsum::zero(a[0]);
-  xsum::zero(a[1]);
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
+  for (long long k0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += PCG_U * stride)
   {
-    x[k]           = __fma_rn(alpha, p[k], x[k]);
-    const double rk = __fma_rn(-alpha, q[k], r[k]);
-    r[k]           = rk;
-    xsum::add(a[0], rk * rk, fl[0]);
-    xsum::add(a[1], rk * (D * rk), fl[1]);
+    double pv[PCG_U], qv[PCG_U], xv[PCG_U], rv[PCG_U];
+#pragma unroll
+    for (int u = 0; u < PCG_U; ++u)
+    {
+      const long long k = k0 + u * stride;
+      const bool in     = k < n;
+      pv[u]             = in ? p[k] : 0.0;
+      qv[u]             = in ? q[k] : 0.0;
+      xv[u]             = in ? x[k] : 0.0;
+      rv[u]             = in ? r[k] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < PCG_U; ++u)
+    {
+      const long long k = k0 + u * stride;
+      if (k < n)
+      {
+        x[k]            = __fma_rn(alpha, pv[u], xv[u]);
+        const double rk = __fma_rn(-alpha, qv[u], rv[u]);
+        r[k]            = rk;
+        xsum::add(a[0], rk * rk, fl[0]);
+      }
+    }
   }
-  krylov_block_finish<256, 2>(a, fl, s, [&](const double* v) {
+  krylov_block_finish<256, 1>(a, fl, s, [&](const double* v) {
     s->rr = v[0];
     s->iters += 1;
     if (sqrt(v[0]) <= s->tolb) s->state = 1;
@@ -147,8 +183,9 @@ __global__ void __launch_bounds__(256) pcg_x_kernel(long long n, const double* _
     else if (!(v[0] == v[0])) s->state = 3;
     else
     {
-      s->beta = v[1] / s->rz;
-      s->rz   = v[1];
+      const double rzn = s->D * v[0];
+      s->beta          = rzn / s->rz;
+      s->rz            = rzn;
     }
     out->state = s->state;
     out->iters = s->iters;
@@ -195,9 +232,13 @@ static void pcg_record_batch(PcgWork* w, STS_Problem p, double* x)
   cudaStream_t st = w->ctx->stream;
   const long long n = w->n;
   const int eb      = ew_blocks(w->ctx, n, 256 * 2);
+  const int ex      = resident_blocks(w->ctx, pcg_x_kernel, n, PCG_U);
   dim3 bq(256, 1);
   unsigned gx = (unsigned)((p->nx + 255) / 256);
-  long long gy_cap = (long long)w->ctx->num_sms * 8 / gx;
+  int occ_q   = 0;
+  if (!STS_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_q, pcg_q_kernel, 256, 0)) || occ_q < 1)
+    occ_q = 1;
+  long long gy_cap = (long long)w->ctx->num_sms * occ_q / gx; // one wave of resident blocks
   if (gy_cap < 1) gy_cap = 1;
   dim3 gq(gx, (unsigned)(p->ny < gy_cap ? p->ny : gy_cap));
   for (int it = 0; it < PCG_BATCH; ++it)
@@ -206,7 +247,7 @@ static void pcg_record_batch(PcgWork* w, STS_Problem p, double* x)
     double* pnew       = w->p[(it + 1) & 1];
     pcg_p_kernel<<<eb, 256, 0, st>>>(n, w->r, pold, pnew, w->d_s);
     pcg_q_kernel<<<gq, bq, 0, st>>>(p->dev, pnew, w->q, w->d_s);
-    pcg_x_kernel<<<eb, 256, 0, st>>>(n, pnew, w->q, x, w->r, w->d_s, w->d_out);
+    pcg_x_kernel<<<ex, 256, 0, st>>>(n, pnew, w->q, x, w->r, w->d_s, w->d_out);
   }
 }
 

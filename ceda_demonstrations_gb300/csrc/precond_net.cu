@@ -2172,7 +2172,7 @@ extern "C" int STS_HarvestPCGPairs(STS_Problem p, double gamma, N_Vector b, int 
 namespace net {
 
 struct FcgScal {
-  double beta, alpha, pq_prev, rr, gamma, tolb;
+  double beta, alpha, pq_prev, rr, gamma, tolb, pr;
   int iters, maxit, state, pad_; // state: 0 running, 1 converged, 2 iteration limit, 3 breakdown
   unsigned long long limbs[2][xsum::NL];
   unsigned int flags[2];
@@ -2185,6 +2185,7 @@ struct FcgOut {
 };
 
 constexpr int FCG_BATCH = 8; // iterations per graph launch (even: p, q ping-pong)
+constexpr int FCG_U     = 2; // grid-strided points per thread and trip (independent loads in flight)
 
 __global__ void __launch_bounds__(256) fcg_beta_kernel(long long n, const double* __restrict__ z,
                                                        const double* __restrict__ qprev, FcgScal* s)
@@ -2194,84 +2195,96 @@ __global__ void __launch_bounds__(256) fcg_beta_kernel(long long n, const double
   unsigned fl[1] = {0};
   xsum::zero(a[0]);
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
-    xsum::add(a[0], z[k] * qprev[k], fl[0]);
+  for (long long k0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += FCG_U * stride)
+  {
+    double zv[FCG_U], qv[FCG_U];
+#pragma unroll
+    for (int u = 0; u < FCG_U; ++u)
+    {
+      const long long k = k0 + u * stride;
+      zv[u]             = k < n ? z[k] : 0.0;
+      qv[u]             = k < n ? qprev[k] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < FCG_U; ++u)
+      if (k0 + u * stride < n) xsum::add(a[0], zv[u] * qv[u], fl[0]);
+  }
   krylov_block_finish<256, 1>(a, fl, s, [&](const double* v) {
     s->beta = (s->iters > 0) ? -v[0] / s->pq_prev : 0.0;
   });
 }
 
-// KP: p = z + beta p_prev, q = (I - gamma A) p, p.r and p.q -> alpha. A block owns 256
-// columns of a segment of FCG_ROWS rows and marches down it: each row of p (with one halo
-// column on each side) is formed once into a 3-row shared ring, and q is taken from the ring
-// as q = (1 - gamma cc) p_C - gamma cx (p_W + p_E) - gamma cy (p_S + p_N). Eight FP64
-// instructions per point (p, stencil, the two dot products): GB300 issues FP64 at 1/64 of
-// the FP32 rate, so these kernels are bounded by the FP64 pipe rather than by HBM.
-constexpr int FCG_ROWS = 16;
-__global__ void __launch_bounds__(256) fcg_pq_march_kernel(ProbDev P, const double* __restrict__ z,
-                                                           const double* __restrict__ pp,
-                                                           const double* __restrict__ r, double* __restrict__ p,
-                                                           double* __restrict__ q, FcgScal* s, FcgOut* out)
+// KP: p = z + beta p_prev and p.r. KQ: q = (I - gamma A) p with the coefficients folded,
+// q = (1 - gamma cc) p_C - gamma cx (p_W + p_E) - gamma cy (p_S + p_N), and p.q -> alpha =
+// p.r / p.q. Eight FP64 instructions per point in the two (p, stencil, the two dot products):
+// GB300 issues FP64 at a small fraction of its FP32 rate (about 5e11 instructions/s
+// measured), so these kernels are bounded by the FP64 pipe rather than by HBM.
+__global__ void __launch_bounds__(256) fcg_p_kernel(long long n, const double* __restrict__ z,
+                                                    const double* __restrict__ pp, const double* __restrict__ r,
+                                                    double* __restrict__ p, FcgScal* s)
 {
-  __shared__ double ring[3][256 + 2];
   if (s->state != 0) return;
-  const double gamma = s->gamma, beta = s->beta;
-  const double c0 = 1.0 - gamma * P.cc, c1 = -gamma * P.cx, c2 = -gamma * P.cy;
-  xsum::Limbs a[2];
-  unsigned fl[2] = {0, 0};
+  const double beta = s->beta;
+  xsum::Limbs a[1];
+  unsigned fl[1] = {0};
   xsum::zero(a[0]);
-  xsum::zero(a[1]);
-  const long long nx = P.nx, ny = P.ny;
-  const int tid      = threadIdx.x;
-  const long long x0 = (long long)blockIdx.x * 256;
-  const long long i  = x0 + tid;
-  const bool col     = i < nx;
-  const long long j0 = (long long)blockIdx.y * FCG_ROWS;
-  const long long j1 = j0 + FCG_ROWS < ny ? j0 + FCG_ROWS : ny;
-  auto pval = [&](long long ii, long long jj) -> double {
-    if (ii < 0 || ii >= nx || jj < 0 || jj >= ny) return 0.0;
-    const long long k = jj * nx + ii;
-    return __fma_rn(beta, pp[k], z[k]);
-  };
-  // row jj of p into ring slot sl: own column, threads 0 / 255 also the halo columns
-  auto stage_row = [&](long long jj, int sl) {
-    double* rw  = ring[sl];
-    rw[tid + 1] = pval(i, jj);
-    if (tid == 0) rw[0] = pval(x0 - 1, jj);
-    if (tid == 255) rw[257] = pval(x0 + 256, jj);
-  };
-  int sm = 0, sc = 1, sn = 2; // ring slots of rows j-1, j, j+1 (rotated, no modulo)
-  stage_row(j0 - 1, sm);
-  stage_row(j0, sc);
-  for (long long j = j0; j < j1; ++j)
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += FCG_U * stride)
   {
-    stage_row(j + 1, sn);
-    const double rk = col ? r[j * nx + i] : 0.0;
-    __syncthreads();
-    if (col)
+    double zv[FCG_U], pv[FCG_U], rv[FCG_U];
+#pragma unroll
+    for (int u = 0; u < FCG_U; ++u)
     {
-      const double* rm = ring[sm];
-      const double* rc = ring[sc];
-      const double* rn = ring[sn];
-      const double pc = rc[tid + 1];
-      const double sx = rc[tid] + rc[tid + 2], sy = rm[tid + 1] + rn[tid + 1];
-      const double qk = __fma_rn(c1, sx, __fma_rn(c2, sy, c0 * pc));
-      const long long k = j * nx + i;
-      p[k]              = pc;
-      q[k]              = qk;
-      xsum::add(a[0], pc * rk, fl[0]);
-      xsum::add(a[1], pc * qk, fl[1]);
+      const long long k = k0 + u * stride;
+      const bool in     = k < n;
+      zv[u]             = in ? z[k] : 0.0;
+      pv[u]             = in ? pp[k] : 0.0;
+      rv[u]             = in ? r[k] : 0.0;
     }
-    __syncthreads(); // row j-1's slot receives row j+2 in the next iteration
-    const int t = sm;
-    sm          = sc;
-    sc          = sn;
-    sn          = t;
+#pragma unroll
+    for (int u = 0; u < FCG_U; ++u)
+    {
+      const long long k = k0 + u * stride;
+      if (k < n)
+      {
+        const double pk = __fma_rn(beta, pv[u], zv[u]);
+        p[k]            = pk;
+        xsum::add(a[0], pk * rv[u], fl[0]);
+      }
+    }
   }
-  krylov_block_finish<256, 2>(a, fl, s, [&](const double* v) {
-    s->alpha   = v[0] / v[1];
-    s->pq_prev = v[1];
-    if (!(v[1] != 0.0) || !(v[1] == v[1]))
+  krylov_block_finish<256, 1>(a, fl, s, [&](const double* v) { s->pr = v[0]; });
+}
+
+__global__ void __launch_bounds__(256) fcg_q_kernel(ProbDev P, const double* __restrict__ p,
+                                                    double* __restrict__ q, FcgScal* s, FcgOut* out)
+{
+  if (s->state != 0) return;
+  const double gamma = s->gamma;
+  const double c0 = 1.0 - gamma * P.cc, c1 = -gamma * P.cx, c2 = -gamma * P.cy;
+  xsum::Limbs a[1];
+  unsigned fl[1] = {0};
+  xsum::zero(a[0]);
+  const long long nx = P.nx, ny = P.ny;
+  const long long i  = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nx)
+    for (long long j = blockIdx.y; j < ny; j += gridDim.y)
+    {
+      const long long k = j * nx + i;
+      const double pc   = p[k];
+      const double pw   = (i > 0) ? p[k - 1] : 0.0;
+      const double pe   = (i < nx - 1) ? p[k + 1] : 0.0;
+      const double ps   = (j > 0) ? p[k - nx] : 0.0;
+      const double pn   = (j < ny - 1) ? p[k + nx] : 0.0;
+      const double sx = pw + pe, sy = ps + pn;
+      const double qk = __fma_rn(c1, sx, __fma_rn(c2, sy, c0 * pc));
+      q[k]            = qk;
+      xsum::add(a[0], pc * qk, fl[0]);
+    }
+  krylov_block_finish<256, 1>(a, fl, s, [&](const double* v) {
+    s->alpha   = s->pr / v[0];
+    s->pq_prev = v[0];
+    if (!(v[0] != 0.0) || !(v[0] == v[0]))
     {
       s->state   = 3; // breakdown: p . q = 0 or not a number
       out->state = 3;
@@ -2289,12 +2302,31 @@ __global__ void __launch_bounds__(256) fcg_x_kernel(long long n, const double* _
   unsigned fl[1] = {0};
   xsum::zero(a[0]);
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride)
+  for (long long k0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += FCG_U * stride)
   {
-    x[k]            = __fma_rn(alpha, p[k], x[k]);
-    const double rk = __fma_rn(-alpha, q[k], r[k]);
-    r[k]            = rk;
-    xsum::add(a[0], rk * rk, fl[0]);
+    double pv[FCG_U], qv[FCG_U], xv[FCG_U], rv[FCG_U];
+#pragma unroll
+    for (int u = 0; u < FCG_U; ++u)
+    {
+      const long long k = k0 + u * stride;
+      const bool in     = k < n;
+      pv[u]             = in ? p[k] : 0.0;
+      qv[u]             = in ? q[k] : 0.0;
+      xv[u]             = in ? x[k] : 0.0;
+      rv[u]             = in ? r[k] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < FCG_U; ++u)
+    {
+      const long long k = k0 + u * stride;
+      if (k < n)
+      {
+        x[k]            = __fma_rn(alpha, pv[u], xv[u]);
+        const double rk = __fma_rn(-alpha, qv[u], rv[u]);
+        r[k]            = rk;
+        xsum::add(a[0], rk * rk, fl[0]);
+      }
+    }
   }
   krylov_block_finish<256, 1>(a, fl, s, [&](const double* v) {
     s->rr = v[0];
@@ -2394,10 +2426,25 @@ extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b,
     hs.pq_prev = 1.0;
     memset(h_out, 0, sizeof(net::FcgOut));
     cudaMemcpyAsync(d_s, &hs, sizeof(hs), cudaMemcpyHostToDevice, st);
-    const int eb = ew_blocks(ctx, N, 256 * 2);
+    // the reduction kernels run one wave of resident blocks (each block combines its exact
+    // sums once), two grid-strided points per thread and trip
+    auto resident = [&](auto kernel) {
+      int occ = 0;
+      if (!STS_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, 0)) || occ < 1) occ = 1;
+      long long b         = (long long)ctx->num_sms * occ;
+      const long long cap = (N + 256LL * net::FCG_U - 1) / (256LL * net::FCG_U);
+      return (int)(b < cap ? b : (cap < 1 ? 1 : cap));
+    };
+    const int eb_beta = resident(net::fcg_beta_kernel), eb_p = resident(net::fcg_p_kernel),
+              eb_x = resident(net::fcg_x_kernel);
     dim3 bq(256, 1);
     const unsigned gx = (unsigned)((p->nx + 255) / 256);
-    dim3 gm(gx, (unsigned)((p->ny + net::FCG_ROWS - 1) / net::FCG_ROWS));
+    int occ_q         = 0;
+    if (!STS_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_q, net::fcg_q_kernel, 256, 0)) || occ_q < 1)
+      occ_q = 1;
+    long long gy_cap = (long long)ctx->num_sms * occ_q / gx; // one wave of resident blocks
+    if (gy_cap < 1) gy_cap = 1;
+    dim3 gq(gx, (unsigned)(p->ny < gy_cap ? p->ny : gy_cap));
     cudaGraph_t g;
     cudaGraphExec_t ge = nullptr;
     net::l0::FoldA fa;
@@ -2411,9 +2458,10 @@ extern "C" int STS_FCGSolve(STS_Problem p, double gamma, STS_Net nt, N_Vector b,
         double *pp = P2[k & 1], *pn = P2[(k + 1) & 1];
         double *qp = Q2[k & 1], *qn = Q2[(k + 1) & 1];
         net_forward_infer(nt, n, r, scale, (float)sk, (float)sg, jac / scale, z, &fa, &fb);
-        net::fcg_beta_kernel<<<eb, 256, 0, st>>>(N, z, qp, d_s);
-        net::fcg_pq_march_kernel<<<gm, bq, 0, st>>>(p->dev, z, pp, r, pn, qn, d_s, d_out);
-        net::fcg_x_kernel<<<eb, 256, 0, st>>>(N, pn, qn, NVD(x), r, d_s, d_out);
+        net::fcg_beta_kernel<<<eb_beta, 256, 0, st>>>(N, z, qp, d_s);
+        net::fcg_p_kernel<<<eb_p, 256, 0, st>>>(N, z, pp, r, pn, d_s);
+        net::fcg_q_kernel<<<gq, bq, 0, st>>>(p->dev, pn, qn, d_s, d_out);
+        net::fcg_x_kernel<<<eb_x, 256, 0, st>>>(N, pn, qn, NVD(x), r, d_s, d_out);
       }
       ok = STS_CUDA_OK(cudaStreamEndCapture(st, &g));
       if (ok)

@@ -1490,18 +1490,27 @@ int orc_lsrk_evolve(const orc_prob* p, const orc_opts* o, orc_state* st, double 
  * x starts at zero; stop when ||r||_2 <= tol ||b||_2. Arithmetic mirrors the fused CUDA
  * kernels: K1 forms p = beta p + D r, q = M p, p.q; K2 updates x, r and r.r, r.(D r).
  * ----------------------------------------------------------------------------------*/
-static void apply_M(const orc_prob* p, double gamma, const double* v, double* w)
+/* q = (I - gamma A) v with the coefficients folded: c0 v_C + c1 (v_W + v_E) + c2 (v_S + v_N),
+ * c0 = 1 - gamma cc, c1 = -gamma cx, c2 = -gamma cy (the fused kernels pcg_q / fcg_q) */
+static void apply_M_folded(const orc_prob* p, double gamma, const double* v, double* w)
 {
   long nx = p->nx, ny = p->ny;
+  const double c0 = 1.0 - gamma * p->cc, c1 = -gamma * p->cx, c2 = -gamma * p->cy;
 #pragma omp parallel for schedule(static)
   for (long j = 0; j < ny; ++j)
     for (long i = 0; i < nx; ++i)
     {
-      double a      = lap_point(p, v, i, j);
-      w[j * nx + i] = fma(-gamma, a, v[j * nx + i]);
+      long k   = j * nx + i;
+      double w_ = (i > 0) ? v[k - 1] : 0.0, e = (i < nx - 1) ? v[k + 1] : 0.0;
+      double s_ = (j > 0) ? v[k - nx] : 0.0, nn = (j < ny - 1) ? v[k + nx] : 0.0;
+      double sx = w_ + e, sy = s_ + nn;
+      w[k]      = fma(c1, sx, fma(c2, sy, c0 * v[k]));
     }
 }
 
+/* The fused Jacobi-PCG (csrc/pcg.cu): SUNLinSol_PCG with the constant Jacobi scaling D of
+ * preconditioner_jacobi.cpp:9-61 for constant coefficients, so r.z = D (r.r) (one exact sum
+ * per iteration, rounded once, times D) */
 int orc_pcg(const orc_prob* p, double gamma, int jacobi, const double* b, double* x,
             double tol, int maxit, double* relres)
 {
@@ -1515,7 +1524,8 @@ int orc_pcg(const orc_prob* p, double gamma, int jacobi, const double* b, double
     x[k] = 0.0;
     r[k] = b[k];
   }
-  double bnorm = sqrt(orc_xdot(b, b, n));
+  const double bb = orc_xdot(b, b, n);
+  double bnorm    = sqrt(bb);
   if (!(bnorm > 0.0))
   {
     *relres = 0.0;
@@ -1524,17 +1534,13 @@ int orc_pcg(const orc_prob* p, double gamma, int jacobi, const double* b, double
     free(q);
     return 0;
   }
-  double rz;
-  {
-    XREDUCE(n, r[i] * (D * r[i]));
-    rz = xacc_result(&tot);
-  }
+  double rz = D * bb;
   double beta = 0.0, rr = 0.0;
   int it;
   for (it = 1; it <= maxit; ++it)
   {
     for (long k = 0; k < n; ++k) pv[k] = fma(beta, pv[k], D * r[k]);
-    apply_M(p, gamma, pv, q);
+    apply_M_folded(p, gamma, pv, q);
     double pq    = orc_xdot(pv, q, n);
     double alpha = rz / pq;
     for (long k = 0; k < n; ++k)
@@ -1542,15 +1548,11 @@ int orc_pcg(const orc_prob* p, double gamma, int jacobi, const double* b, double
       x[k] = fma(alpha, pv[k], x[k]);
       r[k] = fma(-alpha, q[k], r[k]);
     }
-    double rzn;
     {
       XREDUCE(n, r[i] * r[i]);
       rr = xacc_result(&tot);
     }
-    {
-      XREDUCE(n, r[i] * (D * r[i]));
-      rzn = xacc_result(&tot);
-    }
+    const double rzn = D * rr;
     if (sqrt(rr) <= tol * bnorm) break;
     beta = rzn / rz;
     rz   = rzn;
