@@ -443,6 +443,46 @@ def run_full(args):
     print(json.dumps({"full_solve": out, "n": n, "tf": tf, "kx": kx, "ky": ky}), flush=True)
 
 
+def run_config1(args):
+    """The serial CPU configuration (128^2, kx = ky = 1, manufactured problem, RKC adaptive,
+    rtol 1e-6, atol 1e-10, t in [0, 1], stop time 1): time to solution of the FP64 GPU path
+    (CUDA events around the evolve) and of the CPU oracle on one thread (the reference's serial
+    single-rank run) and on all host threads, with the final fields compared."""
+    import numpy as np
+    import ceda_demonstrations_gb300 as sts
+    from oracle import pyoracle as po
+    ctx = sts.Context(0)
+    timer = cuda_timer(ctx.stream)
+    n, tf = 128, 1.0
+    G = sts.Problem(ctx, sts.MANUFACTURED, n, n, 1.0, 1.0)
+    out = {}
+    for rep in range(2):  # the first run warms up the graphs and the autotuner
+        I = sts.LSRKStep(ctx, G, 0.0, G.initial(), method=sts.RKC, rtol=1e-6, atol=1e-10, maxsteps=10 ** 6)
+        I.set_stop_time(tf)
+        y = G.vector()
+        with timer() as tm:
+            I.evolve(tf, y)
+        st = I.stats()
+        yg = y.numpy()
+        I.free()
+    ex = G.exact(tf).numpy()
+    out["gpu"] = {"seconds": tm.ms / 1e3, "steps": st["nst"], "rhs_evals": st["nfe"],
+                  "rel_l2_vs_exact": float(np.linalg.norm(yg - ex) / np.linalg.norm(ex))}
+    P = po.Problem(po.MANUFACTURED, n, n, kx=1.0, ky=1.0)
+    allt = po.lib().orc_nthreads()
+    for label, nth in (("cpu_1_thread", 1), ("cpu_all_threads", allt)):
+        po.lib().orc_set_nthreads(nth)
+        J = po.Integrator(P, P.initial(), method=po.RKC, rtol=1e-6, atol=1e-10, maxsteps=10 ** 6, tstop=tf)
+        t0 = time.perf_counter()
+        J.evolve(tf)
+        sec = time.perf_counter() - t0
+        out[label] = {"seconds": sec, "threads": nth, "steps": J.stats()["nst"],
+                      "same_bits_as_gpu": bool(np.array_equal(J.y, yg))}
+    po.lib().orc_set_nthreads(allt)
+    out["gpu_speedup_vs_1_thread"] = out["cpu_1_thread"]["seconds"] / out["gpu"]["seconds"]
+    print(json.dumps({"config1": out, "n": n, "tf": tf}), flush=True)
+
+
 def run_reference_mode(args):
     """The reference's own problem (periodic, Gaussian x sine initial state, inhomogeneous
     faces k (1 + 0.99 sin)) at 2048^2, RKL2 rtol 1e-5: FP64 and mixed reference mode from
@@ -769,6 +809,7 @@ def main():
     ap.add_argument("--stage-kernel", type=int, default=0,
                     help="mixed stage kernel: 0 autotune, 1 register marching, 2+k TMA configuration k")
     ap.add_argument("--reference-mode", action="store_true")
+    ap.add_argument("--config1", action="store_true")
     ap.add_argument("--refmode-n", type=int, default=2048)
     ap.add_argument("--batch", action="store_true")
     ap.add_argument("--batch-profile", action="store_true")
@@ -793,6 +834,8 @@ def main():
         run_full(args)
     elif args.reference_mode:
         run_reference_mode(args)
+    elif args.config1:
+        run_config1(args)
     elif args.batch_profile:
         run_batch_profile(args)
     elif args.batch:

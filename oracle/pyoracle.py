@@ -168,6 +168,7 @@ def lib():
         L.orc_ark_table.restype = C.c_int
         L.orc_ark_table.argtypes = [C.c_int, C.c_int] + [C.POINTER(C.c_int)] * 3 + [_dp] * 4
         L.orc_nthreads.restype = C.c_int
+        L.orc_set_nthreads.argtypes = [C.c_int]
         _lib = L
     return _lib
 

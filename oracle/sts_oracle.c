@@ -33,6 +33,16 @@ int orc_nthreads(void)
 #endif
 }
 
+/* threads of the oracle's parallel loops from here on (1: the reference's serial run) */
+void orc_set_nthreads(int n)
+{
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
 /* ------------------------------------------------------------------------------------
  * Exact accumulation. Replaces the MPI_Allreduce-backed sums of NVECTOR_PARALLEL and the
  * gkyl_array_reduce_range + gkyl_comm_allreduce pair of nvector_gkylzero.c:234-404.

@@ -147,6 +147,7 @@ void orc_hermite(long n, int deg, double tau, double h, const double* yold, cons
 int orc_arkstep_evolve(const orc_prob* p, const orc_ark_opts* o, orc_ark_state* st, double tout, double* y);
 int orc_ark_table(int implicit, int order, int* s, int* q, int* pe, double* A, double* b, double* d, double* c);
 int orc_nthreads(void);
+void orc_set_nthreads(int n);
 
 #ifdef __cplusplus
 }
