@@ -868,9 +868,9 @@ __global__ void __launch_bounds__(tc::COLS) conv3x3_tc_kernel(const __nv_bfloat1
 //     removed by 5-tap 1-D corrections along the edge (and added back once at the corners);
 //   conv(0.25 up(y1), G) takes, per fine pixel parity, a 2x2 coarse kernel per channel.
 // So the fine level reads v (the FP64 residual) twice and y1 once and writes p0 and z: about
-// 32 bytes per fine pixel instead of ~100, with 64 + 25 + 64 FP32 FMAs per pixel on the CUDA
-// cores. The folded kernels are formed on the host from the BF16 weights and passed as kernel
-// parameters (constant bank, uniform reads).
+// 32 bytes per fine pixel instead of ~100. p0 runs on the tensor cores (TF32 MMAs), z with
+// 25 + 64 FP32 FMAs per fine pixel on the CUDA cores. The folded kernels are formed on the
+// host from the BF16 weights and passed as kernel parameters.
 // ---------------------------------------------------------------------------------------
 namespace l0 {
 struct FoldA {
@@ -886,16 +886,29 @@ struct FoldB {
 // halo) into shared memory, computes, stores; many small CTAs per SM hide the memory latency.
 // The folded weights are kernel parameters indexed with compile-time offsets, so they are read
 // from the constant bank as FMA operands and take no registers.
-constexpr int PTX = 64, PTY = 4; // p0 tile: coarse columns x rows (256 threads, one coarse pixel each)
+constexpr int PTX = 64, PTY = 4; // p0 tile: coarse columns x rows (256 threads, 8 warps of 32 coarse pixels)
 constexpr int ZTX = 32, ZTY = 4; // z tile: coarse cells (128 threads, one 2 x 2 fine cell each)
 
-// p0 = pool(conv(v, F)): stride-2 4x4 convolution, all 16 channels per thread
+// p0 = pool(conv(v, F)): stride-2 4x4 convolution as a small GEMM on the tensor cores,
+// [coarse pixels x 16 taps] x [16 taps x 16 channels], mma.sync m16n8k8 TF32 -> FP32 (the
+// window values and the folded weights rounded to TF32, 10-bit mantissa, below the BF16
+// rounding of the output). A warp owns 32 coarse pixels of one tile row (two 16-row M tiles),
+// two k steps of 8 taps and two n tiles of 8 channels: 8 MMAs instead of 512 FP32 FMA
+// instructions per thread pair of pixels on the CUDA cores.
+__device__ __forceinline__ uint32_t tf32_bits(float x)
+{
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
 __global__ void __launch_bounds__(PTX * PTY) p0_kernel(const double* __restrict__ r, double scale, int n, FoldA fa,
                                                        __nv_bfloat16* __restrict__ p0)
 {
   constexpr int WR = 2 * PTY + 2, WC = 2 * PTX + 2; // fine window: rows 2J0-1 .., columns 2I0-1 ..
   __shared__ float vw[WR][WC + 2];
-  const int tid = threadIdx.x, tx = tid % PTX, ty = tid / PTX;
+  __shared__ uint32_t kb[CH][16]; // folded weights as TF32 bits, [channel][tap]
+  const int tid = threadIdx.x;
   const int nc = n / 2;
   const int I0 = blockIdx.x * PTX, J0 = blockIdx.y * PTY;
   const float fs = (float)scale;
@@ -905,31 +918,66 @@ __global__ void __launch_bounds__(PTX * PTY) p0_kernel(const double* __restrict_
     const int y = 2 * J0 - 1 + wr, x = 2 * I0 - 1 + wc;
     vw[wr][wc] = (y >= 0 && y < n && x >= 0 && x < n) ? (float)__ldg(r + (long long)y * n + x) * fs : 0.f;
   }
+  // the tap index is fixed per thread here (tid = c * 16 + k): a uniform constant-bank read
+  // per warp and tap is not possible, so the weights go through shared memory once
+  kb[tid >> 4][tid & 15] = tf32_bits(fa.Kp[tid >> 4][tid & 15]);
   __syncthreads();
-  const int I = I0 + tx, J = J0 + ty;
-  if (I >= nc || J >= nc) return;
-  float win[16];
+  const int lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int ty = warp >> 1;               // tile row of this warp
+  const int txw = (warp & 1) * 32;        // first tile column of this warp
+  // B fragments (k x n = 8 x 8, column major): b0 = B[t][g], b1 = B[t + 4][g], B[k][c] = Kp[c][k]
+  uint32_t b[2][2][2]; // [k step][n tile][reg]
 #pragma unroll
-  for (int qy = 0; qy < 4; ++qy)
+  for (int ks = 0; ks < 2; ++ks)
 #pragma unroll
-    for (int qx = 0; qx < 4; ++qx) win[qy * 4 + qx] = vw[2 * ty + qy][2 * tx + qx];
-  uint32_t o[8];
-#pragma unroll
-  for (int c = 0; c < CH; c += 2)
-  {
-    float a0 = 0.f, a1 = 0.f;
-#pragma unroll
-    for (int k = 0; k < 16; ++k)
+    for (int nt = 0; nt < 2; ++nt)
     {
-      a0 = fmaf(fa.Kp[c][k], win[k], a0);
-      a1 = fmaf(fa.Kp[c + 1][k], win[k], a1);
+      b[ks][nt][0] = kb[nt * 8 + g][ks * 8 + t];
+      b[ks][nt][1] = kb[nt * 8 + g][ks * 8 + t + 4];
     }
-    __nv_bfloat162 h = __floats2bfloat162_rn(a0, a1);
-    o[c / 2]         = *reinterpret_cast<uint32_t*>(&h);
+  const int J = J0 + ty;
+#pragma unroll
+  for (int m = 0; m < 2; ++m)
+  {
+    const int tx0 = txw + m * 16; // tile column of M-tile row 0
+    // A fragments (m x k = 16 x 8, row major): a0 = A[g][t], a1 = A[g + 8][t], a2 = A[g][t + 4],
+    // a3 = A[g + 8][t + 4]; A[p][k] = v at tap k = 4 qy + qx of pixel tx0 + p
+    float d[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks)
+    {
+      uint32_t a[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+      {
+        const int p  = g + ((q & 1) ? 8 : 0);
+        const int k  = ks * 8 + t + ((q & 2) ? 4 : 0);
+        const int qy = k >> 2, qx = k & 3;
+        a[q]         = tf32_bits(vw[2 * ty + qy][2 * (tx0 + p) + qx]);
+      }
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt)
+        asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                     "{%0,%1,%2,%3};"
+                     : "+f"(d[nt][0]), "+f"(d[nt][1]), "+f"(d[nt][2]), "+f"(d[nt][3])
+                     : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[ks][nt][0]), "r"(b[ks][nt][1]));
+    }
+    // D fragments: d0 = D[g][2t], d1 = D[g][2t + 1], d2 = D[g + 8][2t], d3 = D[g + 8][2t + 1]
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+    {
+      const int I = I0 + tx0 + g + 8 * h;
+      if (I >= nc || J >= nc) continue;
+      __nv_bfloat16* dst = p0 + ((long long)J * nc + I) * CH;
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt)
+      {
+        __nv_bfloat162 v = __floats2bfloat162_rn(d[nt][2 * h], d[nt][2 * h + 1]);
+        *reinterpret_cast<__nv_bfloat162*>(dst + nt * 8 + 2 * t) = v;
+      }
+    }
   }
-  uint4* dst = reinterpret_cast<uint4*>(p0 + ((long long)J * nc + I) * CH);
-  dst[0]     = make_uint4(o[0], o[1], o[2], o[3]);
-  dst[1]     = make_uint4(o[4], o[5], o[6], o[7]);
 }
 
 // z = (out_scale scale) r + (double)((float)out_scale u), u = conv(v, K) (+ edge corrections)
