@@ -139,3 +139,43 @@ def test_print_stats_has_the_harness_labels(ctx, stslib):
         elif ("LS" in txt) and ("RHS" in txt):
             fe += int(txt[5])
     assert fe == st["nfe"] + st["nfi"] + st["nfe_ls"]
+
+
+@pytest.mark.parametrize("implicit,order", [(True, 3), (False, 4)])
+def test_stop_time_and_dense_output_rules(ctx, stslib, oracle, implicit, order):
+    """ARKStep's return rules against the oracle, bit for bit: dense output of degree 2 (DIRK3,
+    with f(t_n, y_n) evaluated for it) and 3 (ERK4), a tout the last step already passed, the
+    stop time (returned once, then cleared); then ONE_STEP after an interpolated return."""
+    pk = dict(kind=0, nx=24, ny=20, kx=1.0, ky=0.5)
+    ak = dict(implicit=implicit, order=order, rtol=1e-6, atol=1e-10, controller=0)
+    if implicit:
+        ak.update(ls="cg", maxl=50, prec="jacobi", msbp=1)
+    G, O = stslib.Problem(ctx, **pk), oracle.Problem(**pk)
+    I = stslib.ARKStep(ctx, G, 0.0, G.initial(), **ak)
+    J = oracle.ArkIntegrator(O, O.initial(), **ak)
+    I.set_stop_time(0.004)
+    J.set_stop_time(0.004)
+    y = G.vector()
+
+    def both(tout, rc_expect):
+        t, rc = I.evolve(tout, y)
+        assert rc == rc_expect and J.evolve(tout) == rc_expect
+        sg, so = I.stats(), J.stats()
+        assert t == J.tret and sg["t"] == so["t"]
+        for kg, ko in KEYS_G2O.items():
+            assert sg[kg] == so[ko], (kg, sg[kg], so[ko])
+        assert np.array_equal(y.numpy(), J.y), np.max(np.abs(y.numpy() - J.y))
+        return t
+    for tout in (0.0004, 0.0011, 0.0019):
+        assert both(tout, 0) == tout
+    tn = I.stats()["t"]
+    assert tn > 0.0019
+    both(0.0019 + 0.5 * (tn - 0.0019), 0)  # already passed: dense output, no step
+    assert I.stats()["t"] == tn
+    assert both(0.01, stslib.TSTOP_RETURN) == 0.004
+    both(0.005, 0)
+    nst, tn = I.stats()["nst"], I.stats()["t"]
+    t1, rc = I.evolve(1.0, y, stslib.ONE_STEP)
+    assert rc == 0 and t1 == tn and I.stats()["nst"] == nst
+    t2, rc = I.evolve(1.0, y, stslib.ONE_STEP)
+    assert rc == 0 and t2 > tn and I.stats()["nst"] == nst + 1
