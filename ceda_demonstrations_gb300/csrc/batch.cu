@@ -411,6 +411,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
           }
           const float* dm2 = nullptr; // d_{j-2}; none at stage 2
           int lastd        = 0;
+          double* yn       = P[iyn];
           for (int jst = 2; jst <= s; ++jst)
           {
             const double mu = ct[jst].mu, nu = ct[jst].nu, mus = ct[jst].mus, ajm1 = ct[jst].ajm1;
@@ -431,23 +432,17 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
                 const float ds = (j > 0) ? ldrowf(&dm1[k - n], j - 1 < j0) : 0.0f;
                 const float dn = (j < n - 1) ? ldrowf(&dm1[k + n], j + 1 >= j1) : 0.0f;
                 const float m2 = dm2 ? dm2[k] : 0.0f;
-                dj[k] = mixed_point<false>(gs, gx, gy, gm, gF, dm1[k], dw, de, ds, dn, m2, ff[k], 0.f, 0.f, 0.f,
-                                           0.f);
+                const float dv = mixed_point<false>(gs, gx, gy, gm, gF, dm1[k], dw, de, ds, dn, m2, ff[k], 0.f, 0.f,
+                                                    0.f, 0.f);
+                dj[k] = dv;
+                if (jst == s) yn[k] = yc[k] + (double)dv; // the last stage also forms y_new = y + d_s
               }
             inst_sync<CL>();
             dm2   = dm1;
             lastd = nxt;
           }
-          // step end: y_new = y + d_s (FP64), then F_new = A y_new, its FP32 copy and the error
+          // step end: F_new = A y_new, its FP32 copy and the error
           const float* dsv = D[lastd];
-          double* yn       = P[iyn];
-          for (int j = j0 + warp; j < j1; j += NW)
-            for (int i = lane; i < n; i += 32)
-            {
-              const long long k = (long long)j * n + i;
-              yn[k]             = yc[k] + (double)dsv[k];
-            }
-          inst_sync<CL>();
           double* Fnew = P[iFn];
           float* Ffn   = Ff[1 - iff];
           for (int j = j0 + warp; j < j1; j += NW)
