@@ -150,6 +150,24 @@ def mixed_stage_traffic(n):
     return TRAFFIC_MIXED_STAGE_6144 * (n / 6144.0) ** 2
 
 
+def replica_barrier(ws):
+    """Host barrier of the N-replica run (one process per GPU, gloo): no data-path collective."""
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def replica_max(x, ws):
+    """The slowest rank's time: every rank's timed region is bracketed by the barrier."""
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_gpu(args):
     import numpy as np
     import ceda_demonstrations_gb300 as sts
@@ -167,17 +185,10 @@ def run_gpu(args):
     N2 = n * n
 
     def barrier():
-        if ws > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        replica_barrier(ws)
 
     def max_over_ranks(x):
-        if ws == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replica_max(x, ws)
 
     res = {}
     clock_samples = []
