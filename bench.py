@@ -803,6 +803,33 @@ def run_precond_profile(args):
                       "pcg_iters": it2, "pcg_ms_per_iter": 1e3 * (t2 - t1) / max(1, it2)}), flush=True)
 
 
+def run_net_apply(args):
+    """One application of the (untrained) network at 2048^2 on each inference path: the
+    convolutions of levels 1-3 on mma.sync (0) or on tcgen05 + TMEM (1), level 0 collapsed in
+    both; CUDA events over 50 applications after 5 untimed ones."""
+    import numpy as np
+    import ceda_demonstrations_gb300 as sts
+    ctx = sts.Context(0)
+    timer = cuda_timer(ctx.stream)
+    n = args.precond_n
+    rng = np.random.default_rng(5)
+    net = sts.Net(ctx, n, seed=1)
+    rv = sts.NVector.from_numpy(ctx, sts.smooth_field(n, rng))
+    zv = sts.NVector(ctx, n * n)
+    out = {}
+    for path in (0, 1):
+        net.set_tensor_path(path)
+        for _ in range(5):
+            net.apply(n, rv.ptr, zv.ptr, 0.3, -0.2, 0.5, 1.0)
+        ctx.synchronize()
+        with timer() as t:
+            for _ in range(50):
+                net.apply(n, rv.ptr, zv.ptr, 0.3, -0.2, 0.5, 1.0)
+        out["mma_sync" if path == 0 else "tcgen05"] = {"us_per_application": t.ms / 50 * 1e3}
+    net.set_tensor_path(0)
+    print(json.dumps({"net_apply": out, "n": n}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -828,6 +855,7 @@ def main():
     ap.add_argument("--batch-tf", type=float, default=0.01)
     ap.add_argument("--precond", action="store_true")
     ap.add_argument("--precond-profile", action="store_true")
+    ap.add_argument("--net-apply", action="store_true")
     ap.add_argument("--precond-n", type=int, default=2048)
     ap.add_argument("--precond-crop", type=int, default=128)
     ap.add_argument("--precond-crops", type=int, default=4)
@@ -855,6 +883,8 @@ def main():
         run_precond(args)
     elif args.precond_profile:
         run_precond_profile(args)
+    elif args.net_apply:
+        run_net_apply(args)
     else:
         run_gpu(args)
 

@@ -1863,12 +1863,21 @@ static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
   la.sk    = sk;
   la.sg    = sg;
   net::LoadArgs lu;
-  lu.cscale = 0.25f;
+  lu.cscale            = 0.25f;
+  const bool collapsed = nt->collapse_l0 && fa && fb && n % 2 == 0;
+  cudaStream_t st      = nt->ctx->stream;
   if (nt->tensor_path == 1)
-  { // tcgen05 + TMEM
+  { // tcgen05 + TMEM for the 16-channel levels; level 0 collapsed when it can be
     const net::LoadArgs lp;
     const int WL = 9 * 256;
-    conv_tc<0, net::LD_R64, true>(nt, nullptr, n, nt->wu + net::L_IN * WL, L[0].h, nullptr, 0.0, la, L[1].p); // h0, p0
+    if (collapsed)
+    {
+      const int nc = n / 2;
+      dim3 g((unsigned)((nc + net::l0::PTX - 1) / net::l0::PTX), (unsigned)((nc + net::l0::PTY - 1) / net::l0::PTY));
+      net::l0::p0_kernel<<<g, net::l0::PTX * net::l0::PTY, 0, st>>>(r, scale, n, *fa, L[1].p); // p0
+    }
+    else
+      conv_tc<0, net::LD_R64, true>(nt, nullptr, n, nt->wu + net::L_IN * WL, L[0].h, nullptr, 0.0, la, L[1].p); // h0, p0
     conv_tc<0, net::LD_PLAIN, true>(nt, L[1].p, n / 2, nt->wu + net::L_1 * WL, L[1].h, nullptr, 0.0, lp, L[2].p); // h1, p1
     conv_tc<0, net::LD_PLAIN, true>(nt, L[2].p, n / 4, nt->wu + net::L_2 * WL, L[2].h, nullptr, 0.0, lp, L[3].p); // h2, p2
     conv_tc<0>(nt, L[3].p, n / 8, nt->wu + net::L_3 * WL, L[3].h, nullptr, 0.0, lp);                             // h3
@@ -1877,6 +1886,13 @@ static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
     conv_tc<0, net::LD_UPADD>(nt, L[2].h, n / 4, nt->wut + net::L_2 * WL, L[2].y, nullptr, 0.0, lu); // y2
     lu.coarse = L[2].y;
     conv_tc<0, net::LD_UPADD>(nt, L[1].h, n / 2, nt->wut + net::L_1 * WL, L[1].y, nullptr, 0.0, lu); // y1
+    if (collapsed)
+    {
+      const int nc = n / 2;
+      dim3 g((unsigned)((nc + net::l0::ZTX - 1) / net::l0::ZTX), (unsigned)((nc + net::l0::ZTY - 1) / net::l0::ZTY));
+      net::l0::z_kernel<<<g, net::l0::ZTX * net::l0::ZTY, 0, st>>>(r, scale, out_scale, n, L[1].y, *fb, zout); // z
+      return;
+    }
     lu.coarse = L[1].y;
     lu.r      = r;
     lu.scale  = scale;
@@ -1885,8 +1901,6 @@ static void net_forward_infer(STS_Net nt, int n, const double* r, double scale, 
     conv_tc<2, net::LD_UPADD>(nt, L[0].h, n, nt->wut + net::L_IN * WL, nullptr, zout, out_scale, lu); // z
     return;
   }
-  const bool collapsed = nt->collapse_l0 && fa && fb && n % 2 == 0;
-  cudaStream_t st      = nt->ctx->stream;
   // level 0 collapsed (p0 straight from r, z straight from r and y1), or the mma.sync path
   if (collapsed)
   {
