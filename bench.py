@@ -265,6 +265,21 @@ def run_gpu(args):
     e2e_attempts = s1["nst_attempts"] - s0["nst_attempts"]
     # ARKodeReset evaluates F(t, y) once per step: work of the restart, not of the step
     e2e_dof = N2 * (s1["nfe"] - s0["nfe"] - args.steps)
+    # the same calls phase by phase (CUDA events around each, three more steps): where the e2e
+    # step goes; the difference to ms_per_step is host time between the calls
+    phase = {"h2d": 0.0, "reset": 0.0, "evolve": 0.0, "d2h": 0.0}
+    for _ in range(3):
+        with timer() as p1:
+            L.N_VCopyFromHost_Sts(yv.h, hp[k])
+        with timer() as p2:
+            I.reset(t_cur, yv)
+        with timer() as p3:
+            t_cur, _ = I.evolve(TF, yv, sts.ONE_STEP)
+        with timer() as p4:
+            L.N_VCopyToHost_Sts(yv.h, hp[1 - k])
+        k = 1 - k
+        for key, tt in zip(phase, (p1, p2, p3, p4)):
+            phase[key] += tt.ms / 3
     # the host link alone (copy engine, pinned buffers, same calls): the part of the e2e step
     # that the data dependence between steps keeps from overlapping the device work
     with timer() as th:
@@ -320,7 +335,8 @@ def run_gpu(args):
                 "h2d_bytes_per_step": 8 * N2, "d2h_bytes_per_step": 8 * N2,
                 "ms_per_step": e2e_ms / args.steps, "h2d_ms": h2d_ms, "d2h_ms": d2h_ms,
                 "h2d_gbs": 8 * N2 / (h2d_ms / 1e3) / 1e9, "d2h_gbs": 8 * N2 / (d2h_ms / 1e3) / 1e9,
-                "stages_per_step": e2e_stages, "step_attempts": e2e_attempts, "sm_mhz": e2e_clocks["sm_mhz"]},
+                "stages_per_step": e2e_stages, "step_attempts": e2e_attempts, "sm_mhz": e2e_clocks["sm_mhz"],
+                "phase_ms": {q: round(v, 3) for q, v in phase.items()}},
         "gpu_launches": m["launches"],
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": ach / peak, "traffic": traffic,
