@@ -15,6 +15,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 STAT_KEYS = ("nst", "nst_attempts", "netf", "nfe", "ndee", "nst_exp", "stage_max", "stages_total")
+STS_ILL_INPUT = -22  # include/stsgpu.h
 
 
 def run_pair(ctx, stslib, oracle, pk, ok, touts, graphs=True):
@@ -418,3 +419,27 @@ def test_recoverable_rhs_failure_retries(ctx, stslib):
     J = stslib.LSRKStep(ctx, broken, 0.0, G.initial(), method=0, dom_eig=lambda t: G.dom_eig())
     with pytest.raises(stslib.STSError):
         J.evolve(0.01, y)
+
+
+def test_evolve_rejects_bad_arguments(ctx, stslib):
+    """The C ABI turns misuse into error codes and keeps the integrator usable: a NULL or
+    wrong-length output vector, a tout behind the last step (no dense output there), an
+    invalid task, a stage count beyond the fixed-step limit."""
+    import ctypes as C
+    L = stslib.lib()
+    G = stslib.Problem(ctx, kind=0, nx=32, ny=24, kx=1.0, ky=0.5)
+    I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), method=1, rtol=1e-6, atol=1e-10)
+    y = G.vector()
+    t = C.c_double()
+    assert L.STS_ARKodeEvolve(I.mem, 0.01, None, C.byref(t), stslib.NORMAL) == STS_ILL_INPUT
+    short = stslib.NVector(ctx, 32 * 24 - 1)
+    assert L.STS_ARKodeEvolve(I.mem, 0.01, short.h, C.byref(t), stslib.NORMAL) == STS_ILL_INPUT
+    t1, rc = I.evolve(0.01, y)
+    assert rc == 0 and t1 == 0.01
+    tn, hl = I.stats()["t"], I.stats()["hlast"]
+    assert L.STS_ARKodeEvolve(I.mem, tn - 3.0 * hl, y.h, C.byref(t), stslib.NORMAL) == STS_ILL_INPUT
+    t2, rc = I.evolve(0.02, y)  # still usable
+    assert rc == 0 and t2 == 0.02 and np.isfinite(y.numpy()).all()
+    J = stslib.LSRKStep(ctx, G, 0.0, G.initial(), method=1, hfixed=1.0, smax=10)
+    assert L.STS_ARKodeEvolve(J.mem, 0.5, y.h, C.byref(t), stslib.NORMAL) == STS_ILL_INPUT
+
