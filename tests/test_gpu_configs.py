@@ -1,7 +1,7 @@
 """The FP64 benchmark configurations end to end on the GPU against the oracle's fixtures.
 
-config 1: 128^2, kx = ky = 1, RKC adaptive (rtol 1e-6, atol 1e-10), t in [0, 1].
-config 2: 4096^2, kx = ky = 1, RKL2 adaptive (rtol 1e-6, atol 1e-10), t in [0, 0.1]
+the serial CPU workload: 128^2, kx = ky = 1, RKC adaptive (rtol 1e-6, atol 1e-10), t in [0, 1];
+the FP64 GPU workload: 4096^2, kx = ky = 1, RKL2 adaptive (rtol 1e-6, atol 1e-10), t in [0, 0.1]
           (about 2.3e12 DOF-stages; the oracle's run is kept in tests/golden/config2_oracle.npz,
           made by tests/golden/make_config_goldens.py).
 

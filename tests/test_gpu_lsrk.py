@@ -266,7 +266,7 @@ def test_mixed_drift_long_stage_chains(ctx, stslib, oracle, method):
     with the per-step stage count of the full run (about 190): at 1024^2 that is 19-23 fixed
     steps. This is the regime where the FP32 stage arithmetic accumulates: summing the
     O(|d|) terms directly ended 2.2e-6 (RKC2) / 1.7e-6 (RKL2) from FP64 here; the difference
-    form ends near 1e-8. The bar of the benchmark spec is 1e-6; the test holds 1e-7. The mixed
+    form ends near 1e-8. The accuracy target is 1e-6; the test holds 1e-7. The mixed
     result also equals the oracle's mixed integrator bit for bit."""
     pk = dict(kind=0, nx=1024, ny=1024, kx=1.0, ky=0.01)
     tf = 0.05
