@@ -1775,6 +1775,11 @@ extern "C" int STS_ARKodeEvolve(void* mem, double tout, N_Vector yout, double* t
 {
   STS_MARK_REGION("Evolve");
   CHECK_MEM(mem);
+  if (itask != STS_NORMAL && itask != STS_ONE_STEP)
+  {
+    sts_set_error("ARKodeEvolve: itask must be STS_NORMAL or STS_ONE_STEP");
+    return STS_ILL_INPUT;
+  }
   if (sts_mem_kind(mem) == STS_MEM_ARKSTEP) return arkstep_evolve(mem, tout, yout, tret, itask);
   LSRKMem* m = MEM(mem);
   if (!yout || NVL(yout) != m->n)

@@ -423,8 +423,8 @@ def test_recoverable_rhs_failure_retries(ctx, stslib):
 
 def test_evolve_rejects_bad_arguments(ctx, stslib):
     """The C ABI turns misuse into error codes and keeps the integrator usable: a NULL or
-    wrong-length output vector, a tout behind the last step (no dense output there), an
-    invalid task, a stage count beyond the fixed-step limit."""
+    wrong-length output vector, an invalid task, a tout behind the last step (no dense output
+    there), a stage count beyond the fixed-step limit."""
     import ctypes as C
     L = stslib.lib()
     G = stslib.Problem(ctx, kind=0, nx=32, ny=24, kx=1.0, ky=0.5)
@@ -434,6 +434,7 @@ def test_evolve_rejects_bad_arguments(ctx, stslib):
     assert L.STS_ARKodeEvolve(I.mem, 0.01, None, C.byref(t), stslib.NORMAL) == STS_ILL_INPUT
     short = stslib.NVector(ctx, 32 * 24 - 1)
     assert L.STS_ARKodeEvolve(I.mem, 0.01, short.h, C.byref(t), stslib.NORMAL) == STS_ILL_INPUT
+    assert L.STS_ARKodeEvolve(I.mem, 0.01, y.h, C.byref(t), 7) == STS_ILL_INPUT  # no such task
     t1, rc = I.evolve(0.01, y)
     assert rc == 0 and t1 == 0.01
     tn, hl = I.stats()["t"], I.stats()["hlast"]
