@@ -242,7 +242,7 @@ __device__ __forceinline__ double lap(const double* __restrict__ u, int n, int i
 // owns rows [j0, j1) of every sweep; sweeps are separated by cluster barriers and the exact
 // reductions are combined through distributed shared memory. Every CTA of the cluster
 // evaluates the step control from the same reduced values, so all take the same decisions.
-template <int NT, int CL>
+template <int NT, int CL, bool MIXED>
 __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restrict__ insts, const int* __restrict__ order,
                                                    int ninst, int* queue, double* __restrict__ yall,
                                                    double* __restrict__ work, long long total, BatchParams prm)
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
         const long long k = (long long)j * n + i;
         const double f    = lap(P[iy], n, i, j, j0, j1, cx, cy, cc);
         P[iF][k]          = f;
-        if (prm.mixed) Ff[0][k] = (float)f;
+        if (MIXED) Ff[0][k] = (float)f;
       }
     inst_sync<CL>();
     long long nfe = 1, nst = 0, natt = 0, netf = 0, nexp = 0, stmax = 0, sttot = 0, nhist = 0;
@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
         unsigned fe      = 0;
         const double p4h = 0.4 * h;
         int last         = 0; // FP64 stages: index into bufs of Y_{j-1}
-        if (prm.mixed)
+        if constexpr (MIXED)
         {
           // stage 1: d_1 = (h mus_1) F_0 in FP32
           {
@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
         if (dsm <= 1.0)
         { // accept: y <- Ys (role swap with its stage buffer or with y_new), F <- Fnew
           t = clipped ? prm.tf : t + h;
-          if (prm.mixed)
+          if constexpr (MIXED)
           {
             const int yv_ = iyn;
             iyn           = iy;
@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(BatchInst* __restr
 // ---------------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------------
-template <int NT, int CL>
+template <int NT, int CL, bool MIXED>
 static bool launch_group(const STS_Batch b, const BatchParams& prm, const int* order, int count, int* queue, int grid,
                          cudaStream_t st)
 {
@@ -625,7 +625,7 @@ static bool launch_group(const STS_Batch b, const BatchParams& prm, const int* o
     if (fits < 0)
     {
       fits = 0;
-      if (cudaFuncSetAttribute(batch_kernel<NT, CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
+      if (cudaFuncSetAttribute(batch_kernel<NT, CL, MIXED>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
       {
         cudaLaunchConfig_t q = {};
         q.gridDim            = dim3(CL, 1, 1);
@@ -638,7 +638,7 @@ static bool launch_group(const STS_Batch b, const BatchParams& prm, const int* o
         q.attrs                = qa;
         q.numAttrs             = 1;
         int nc                 = 0;
-        if (cudaOccupancyMaxActiveClusters(&nc, batch_kernel<NT, CL>, &q) == cudaSuccess && nc > 0) fits = 1;
+        if (cudaOccupancyMaxActiveClusters(&nc, batch_kernel<NT, CL, MIXED>, &q) == cudaSuccess && nc > 0) fits = 1;
       }
       cudaGetLastError();
     }
@@ -660,22 +660,32 @@ static bool launch_group(const STS_Batch b, const BatchParams& prm, const int* o
   attr[0].val.clusterDim.z = 1;
   cfg.attrs                = attr;
   cfg.numAttrs             = CL > 1 ? 1 : 0;
-  return STS_CUDA_OK(cudaLaunchKernelEx(&cfg, batch_kernel<NT, CL>, b->dinst, order, count, queue, b->y, b->work,
+  return STS_CUDA_OK(cudaLaunchKernelEx(&cfg, batch_kernel<NT, CL, MIXED>, b->dinst, order, count, queue, b->y, b->work,
                                         b->total, prm));
+}
+
+// the FP64 and the mixed forms are separate instantiations: each gets its own register
+// allocation (the kernel runs at the 64-register cap of four 256-thread CTAs per SM)
+template <int NT, bool MIXED>
+static bool launch_cl_m(const STS_Batch b, const BatchParams& prm, int cl, const int* order, int count, int* queue,
+                        int grid, cudaStream_t st)
+{
+  switch (cl)
+  {
+  case 2: return launch_group<NT, 2, MIXED>(b, prm, order, count, queue, grid, st);
+  case 4: return launch_group<NT, 4, MIXED>(b, prm, order, count, queue, grid, st);
+  case 8: return launch_group<NT, 8, MIXED>(b, prm, order, count, queue, grid, st);
+  case 16: return launch_group<NT, 16, MIXED>(b, prm, order, count, queue, grid, st);
+  default: return launch_group<NT, 1, MIXED>(b, prm, order, count, queue, grid, st);
+  }
 }
 
 template <int NT>
 static bool launch_cl(const STS_Batch b, const BatchParams& prm, int cl, const int* order, int count, int* queue,
                       int grid, cudaStream_t st)
 {
-  switch (cl)
-  {
-  case 2: return launch_group<NT, 2>(b, prm, order, count, queue, grid, st);
-  case 4: return launch_group<NT, 4>(b, prm, order, count, queue, grid, st);
-  case 8: return launch_group<NT, 8>(b, prm, order, count, queue, grid, st);
-  case 16: return launch_group<NT, 16>(b, prm, order, count, queue, grid, st);
-  default: return launch_group<NT, 1>(b, prm, order, count, queue, grid, st);
-  }
+  return prm.mixed ? launch_cl_m<NT, true>(b, prm, cl, order, count, queue, grid, st)
+                   : launch_cl_m<NT, false>(b, prm, cl, order, count, queue, grid, st);
 }
 
 // One launch (cluster size 1), or two concurrent launches: instances with n >= big_n on
