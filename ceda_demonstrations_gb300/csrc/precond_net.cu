@@ -1739,8 +1739,8 @@ static MarchGrid march_grid(STS_Net nt, int n, int nimg)
   long long segs = (want + (long long)strips * nimg - 1) / ((long long)strips * nimg);
   if (segs < 1) segs = 1;
   int rows = (int)((n + segs - 1) / segs);
-  if (rows < 8) rows = 8;
-  rows += rows & 1; // even: row pairs stay in one CTA (fused pooling)
+  if (rows < 2) rows = 2; // short segments keep the small coarse levels from running on a few CTAs
+  rows += rows & 1;       // even: row pairs stay in one CTA (fused pooling)
   MarchGrid m;
   m.rows = rows;
   m.grid = dim3((unsigned)strips, (unsigned)((n + rows - 1) / rows), (unsigned)nimg);
