@@ -69,6 +69,28 @@ def test_cli_manufactured_rkc_with_error_mode(stslib, oracle, controller):
     assert abs(float(line.split("=")[1]) - rel) <= 1e-12 * rel
 
 
+def test_cli_outputs_without_error_mode_follow_the_dense_output(stslib, oracle):
+    """The reference program's default run (no --error): the stop time is the final time
+    (main.cpp:384) and the intermediate outputs come from the dense output, so the steps pass
+    them; the step count and the final field equal the oracle's run under the same rules."""
+    stslib.lib()
+    rc, out, err = run(["--problem", "manufactured", "--nx", "64", "--ny", "48", "--integrator", "rkc",
+                        "--rtol", "1e-6", "--atol", "1e-10", "--tf", "0.05", "--nout", "5", "--maxsteps", "10000"])
+    assert rc == 0, err
+    st = parse_like_runtests(out)
+    P = oracle.Problem(oracle.MANUFACTURED, 64, 48)
+    J = oracle.Integrator(P, P.initial(), method=oracle.RKC, rtol=1e-6, atol=1e-10, tstop=0.05)
+    dt, tout = 0.05 / 5, 0.05 / 5
+    for k in range(5):
+        assert J.evolve(tout) == (1 if k == 4 else 0)
+        tout = min(tout + dt, 0.05)
+    assert st["Steps"] == J.stats()["nst"]
+    ex = P.exact(0.05)
+    rel = np.linalg.norm(J.y - ex) / np.linalg.norm(ex)
+    line = [l for l in out.split("\n") if l.startswith("Relative L2 error vs exact")][0]
+    assert abs(float(line.split("=")[1]) - rel) <= 1e-12 * rel
+
+
 def test_cli_reference_mode_and_solution_file(stslib, tmp_path):
     stslib.lib()
     rc, out, err = run(["--nx", "40", "--ny", "32", "--integrator", "rkl", "--inhomogeneous",
