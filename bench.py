@@ -150,6 +150,15 @@ def mixed_stage_traffic(n):
     return TRAFFIC_MIXED_STAGE_6144 * (n / 6144.0) ** 2
 
 
+# DRAM bytes of one launch of the fused four-stage kernel (120 x 64 tiles), same method:
+# measured on a 4096^2 case and scaled by the DOF count. None until captured.
+TRAFFIC_FUSED4_4096 = None
+
+
+def fused_stage_traffic(n):
+    return None if TRAFFIC_FUSED4_4096 is None else TRAFFIC_FUSED4_4096 * (n / 4096.0) ** 2
+
+
 def replica_barrier(ws):
     """Host barrier of the N-replica run (one process per GPU, gloo): no data-path collective."""
     if ws > 1:
@@ -197,7 +206,8 @@ def run_gpu(args):
     for mixed in (True, False):
         I = sts.LSRKStep(ctx, G, 0.0, G.initial(), method=METHOD, rtol=RTOL, atol=ATOL,
                          smax=SMAX, mixed=mixed, graphs=True, maxsteps=1000000,
-                         stage_kernel=args.stage_kernel if mixed else 0)
+                         stage_kernel=args.stage_kernel if mixed else 0,
+                         stage_fusion=(args.stage_fusion, args.fusion_rows) if mixed else (1, 0))
         y = G.vector()
 
         def one_step(k):
@@ -221,10 +231,17 @@ def run_gpu(args):
         clock_samples.append(clocks.stop())
         s1 = I.stats()
         ms = max_over_ranks(tm.ms)
-        launches = (s1["stages_total"] - s0["stages_total"]) + (s1["nst_attempts"] - s0["nst_attempts"])
+        stages = s1["stages_total"] - s0["stages_total"]
+        attempts = s1["nst_attempts"] - s0["nst_attempts"]
         dof_stages = N2 * (s1["nfe"] - s0["nfe"])
         stage_ms = I.time_stage_kernel(20)
         kinfo = I.stage_kernel_info()
+        kinfo["fusion"] = I.stage_fusion_info()
+        # kernels per attempt: stage 1, the stages 2..s (one launch per stage, or per group of
+        # ks with a shorter last group), the step end (the timed steps all have s stages)
+        ks = kinfo["fusion"]["ks"]
+        s_att = stages // attempts if attempts else 0
+        launches = attempts * (2 + (s_att - 2 + ks) // ks) if ks > 1 else stages + attempts
         res[mixed] = dict(ms=ms, dof_stages=dof_stages, launches=launches, stage_ms=stage_ms, kinfo=kinfo,
                           t=s1["t"], s=s1["stage_max"], stats=s1, y=y.numpy(), I=I,
                           steps=s1["nst"] - s0["nst"])
@@ -307,10 +324,19 @@ def run_gpu(args):
     m, d = res[True], res[False]
     value = ws * m["dof_stages"] / (m["ms"] / 1e3)
     fp64_value = ws * d["dof_stages"] / (d["ms"] / 1e3)
-    stage_bytes_mixed = 16.0 * N2
+    # the dominant kernel's algorithmic bytes per launch: one stage reads d_{j-1}, d_{j-2}, F_0
+    # and writes d_j (16 B per point); a group of ks stages reads the same three and writes its
+    # last two stages (20 B per point for ks stages)
+    ks = m["kinfo"]["fusion"]["ks"]
+    stage_bytes_mixed = (20.0 if ks > 1 else 16.0) * N2
     stage_bytes_fp64 = 40.0 * N2
     ach = stage_bytes_mixed / (m["stage_ms"] / 1e3) / 1e9
-    traffic = mixed_stage_traffic(n)
+    traffic = fused_stage_traffic(n) if ks > 1 else mixed_stage_traffic(n)
+    if ks > 1:
+        kdesc = ("mixed stages, %d per launch on 120x%d shared-memory tiles (20 B per point and launch, "
+                 "%.1f B/DOF-stage): %s" % (ks, m["kinfo"]["fusion"]["tile_rows"], 20.0 / ks, m["kinfo"]["name"]))
+    else:
+        kdesc = "mixed stage kernel (16 B/DOF-stage), autotuned: %s" % m["kinfo"]["name"]
     fp64_flops = 17.0 * N2 / (d["stage_ms"] / 1e3)
     fp64_peak = C.c_double()
     fp64_peak_tflops = fp64_peak.value if sts.lib().STS_ProbeFP64Rate(ctx.h, C.byref(fp64_peak)) == 0 else None
@@ -339,8 +365,9 @@ def run_gpu(args):
                 "phase_ms": {q: round(v, 3) for q, v in phase.items()}},
         "gpu_launches": m["launches"],
         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                     "frac": ach / peak, "traffic": traffic,
-                     "kernel": "mixed stage kernel (16 B/DOF-stage), autotuned: %s" % m["kinfo"]["name"],
+                     "frac": ach / peak, "traffic": traffic, "kernel": kdesc,
+                     "ms_per_launch": m["stage_ms"], "dof_stages_per_launch": ks * N2,
+                     "kernel_dof_stages_per_s": ks * N2 / (m["stage_ms"] / 1e3),
                      "peak_source": peak_kind},
         "clocks": merge_clocks(clock_samples),
         "fp64": {"value": fp64_value, "unit": "DOF-stages/s", "ms_per_step": d["ms"] / args.steps,
@@ -860,6 +887,9 @@ def main():
     ap.add_argument("--both-methods", action="store_true")
     ap.add_argument("--both-rtols", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--stage-fusion", type=int, default=0,
+                    help="mixed stages per launch: 0 autotuned, 1 off, 2-4 (STS_LSRKStepSetStageFusion)")
+    ap.add_argument("--fusion-rows", type=int, default=0, help="fused tile rows: 0 autotuned, 32 or 64")
     ap.add_argument("--stage-kernel", type=int, default=0,
                     help="mixed stage kernel: 0 autotune, 1 register marching, 2+k TMA configuration k")
     ap.add_argument("--reference-mode", action="store_true")

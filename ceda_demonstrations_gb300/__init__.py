@@ -150,6 +150,8 @@ SIGNATURES = [
     ("STS_LSRKStepSetMixedPrecision", C.c_int, [_vp, C.c_int]),
     ("STS_LSRKStepSetStageKernel", C.c_int, [_vp, C.c_int]),
     ("STS_LSRKStepGetStageKernelInfo", C.c_int, [_vp, _ip, _dp, C.c_char_p, C.c_int]),
+    ("STS_LSRKStepSetStageFusion", C.c_int, [_vp, C.c_int, C.c_int]),
+    ("STS_LSRKStepGetStageFusion", C.c_int, [_vp, _ip, _ip, _dp]),
     ("STS_LSRKStepSetUseGraphs", C.c_int, [_vp, C.c_int]),
     ("STS_LSRKStepSetFusedPeriodic", C.c_int, [_vp, C.c_int]),
     ("STS_ARKodeEvolve", C.c_int, [_vp, C.c_double, _NV, _dp, C.c_int]),
@@ -523,11 +525,14 @@ class LSRKStep:
     """LSRKStepCreateSTS + ARKode* configuration and evolve (diffusion_2D/main.cpp:257-486).
 
     ``rhs`` is either a :class:`Problem` (its built-in STS_Diffusion RHS; fused kernels) or a
-    Python callable ``f(t, y: NVector, ydot: NVector) -> int`` (generic path)."""
+    Python callable ``f(t, y: NVector, ydot: NVector) -> int`` (generic path).
+    ``stage_fusion = (stages per launch, tile rows)`` sets the mixed form's temporal blocking
+    (``STS_LSRKStepSetStageFusion``; (0, 0) autotuned, (1, 0) off)."""
 
     def __init__(self, ctx, rhs, t0, y0, method=RKC, rtol=1e-6, atol=1e-10, controller=PID,
                  smax=200, mixed=False, graphs=True, dom_eig=None, power=None, maxsteps=100000,
-                 hfixed=0.0, stage_kernel=0, dee_warmups=(0, 0), ssp=None, fused_periodic=True):
+                 hfixed=0.0, stage_kernel=0, dee_warmups=(0, 0), ssp=None, fused_periodic=True,
+                 stage_fusion=(0, 0)):
         self.ctx = ctx
         L = lib()
         self._keep = []
@@ -565,6 +570,8 @@ class LSRKStep:
         L.STS_LSRKStepSetUseGraphs(self.mem, int(graphs))
         L.STS_LSRKStepSetFusedPeriodic(self.mem, int(fused_periodic))
         L.STS_LSRKStepSetStageKernel(self.mem, int(stage_kernel))
+        if L.STS_LSRKStepSetStageFusion(self.mem, int(stage_fusion[0]), int(stage_fusion[1])) != 0:
+            _err("STS_LSRKStepSetStageFusion")
         L.STS_ARKodeSetMaxNumSteps(self.mem, maxsteps)
         L.STS_LSRKStepSetNumDomEigEstInitPreprocessIters(self.mem, int(dee_warmups[0]))
         L.STS_LSRKStepSetNumDomEigEstPreprocessIters(self.mem, int(dee_warmups[1]))
@@ -614,6 +621,13 @@ class LSRKStep:
         buf = C.create_string_buffer(64)
         lib().STS_LSRKStepGetStageKernelInfo(self.mem, C.byref(v), C.byref(ms), buf, 64)
         return {"variant": v.value, "ms": ms.value, "name": buf.value.decode()}
+
+    def stage_fusion_info(self):
+        """Stages per launch in use (1: one launch per stage), tile rows and the autotuner's
+        milliseconds per four-stage launch."""
+        ks, rows, ms = C.c_int(), C.c_int(), C.c_double()
+        lib().STS_LSRKStepGetStageFusion(self.mem, C.byref(ks), C.byref(rows), C.byref(ms))
+        return {"ks": ks.value, "tile_rows": rows.value, "ms": ms.value}
 
     def time_stage_kernel(self, nlaunch=20):
         ms = C.c_double()

@@ -238,6 +238,12 @@ struct LSRKMem {
   int tma_variant       = -1; // chosen TMA configuration (-1: register-marching kernel)
   bool tuned            = false;
   double tune_ms[TMA_STAGE32_NVARIANTS + 1] = {};
+  // fused stages: requested group size (0: autotuned, 1: off, 2..4) and tile configuration
+  // (-1: autotuned); the chosen ones (fuse_ks 1: single-stage launches) and the time per
+  // launch of each tile configuration at 4 stages
+  int fuse_req = 0, fuse_tile_req = -1;
+  int fuse_ks = 1, fuse_ti = -1;
+  double fuse_ms[TMA_FUSED_NTILES] = {};
   long long n           = 0;
 
   // state (mirrors the oracle's orc_state)
@@ -257,7 +263,7 @@ struct LSRKMem {
   double* Fb[2] = {nullptr, nullptr}; // F_n / F_{n+1}
   float* Ffb[2] = {nullptr, nullptr}; // FP32 copies (mixed)
   double* Y[3]  = {nullptr, nullptr, nullptr};
-  float* D[3]   = {nullptr, nullptr, nullptr};
+  float* D[4]   = {nullptr, nullptr, nullptr, nullptr}; // D[3]: fused stages only
   double* evec  = nullptr;
   float* per_faces = nullptr; // mixed reference mode: FP32 Dxw | Dxe | Dys | Dyn
   int par       = 0; // current parity: yb[par] = y_n
@@ -468,8 +474,11 @@ static void free_device(LSRKMem* m)
   for (int b = 0; b < 3; ++b)
   {
     cudaFree(m->Y[b]);
-    cudaFree(m->D[b]);
     m->Y[b] = nullptr;
+  }
+  for (int b = 0; b < 4; ++b)
+  {
+    cudaFree(m->D[b]);
     m->D[b] = nullptr;
   }
   cudaFree(m->evec);
@@ -523,10 +532,18 @@ static int ensure_stage_buffers(LSRKMem* m)
     if (!m->mixed && !m->Y[b] && !STS_CUDA_OK(cudaMalloc(&m->Y[b], n8))) return -1;
     if (m->mixed && !m->D[b] && !STS_CUDA_OK(cudaMalloc(&m->D[b], n4))) return -1;
   }
-  if (m->mixed && !m->tma.ok && m->stage_variant != 1)
+  // fused stages need a fourth buffer (a group reads two and writes two); the tensor maps of
+  // the single-stage and the fused kernels cover every allocated buffer
+  const bool want_fused = m->mixed && m->fuse_req != 1 && m->stage_variant != 1;
+  if (m->mixed && m->stage_variant != 1 && (!m->tma.ok || (want_fused && !m->tma.fz_ok)))
   {
     STS_Problem p = (STS_Problem)m->user_data;
-    if (tma_stage32_supported(p->nx, p->ny)) tma_stage32_prepare(&m->tma, m->D, m->Ffb, p->nx, p->ny);
+    if (tma_stage32_supported(p->nx, p->ny))
+    {
+      if (want_fused && !m->D[3] && !STS_CUDA_OK(cudaMalloc(&m->D[3], n4))) return -1;
+      if (tma_stage32_prepare(&m->tma, m->D, m->Ffb, p->nx, p->ny) && want_fused)
+        tma_fused_prepare(&m->tma, m->D, m->Ffb, p->nx, p->ny);
+    }
   }
   return 0;
 }
@@ -609,6 +626,8 @@ static void autotune_stage32(LSRKMem* m, STS_Problem p)
 {
   m->tuned       = true;
   m->tma_variant = -1;
+  m->fuse_ks     = 1;
+  m->fuse_ti     = -1;
   if (m->stage_variant != 0 || !m->tma.ok) return;
   cudaStream_t st = m->ctx->stream;
   // stage coefficients of a mid stage of a 100-stage RKL2 step (any finite values time alike)
@@ -645,6 +664,42 @@ static void autotune_stage32(LSRKMem* m, STS_Problem p)
     {
       best           = per;
       m->tma_variant = v;
+    }
+  }
+  // fused groups of four stages, per tile configuration, against the best single stage
+  m->fuse_ks = 1;
+  m->fuse_ti = -1;
+  if (m->tma.fz_ok && m->fuse_req != 1 && m->smax >= 5)
+  {
+    for (int k = 3; k <= 5; ++k) hstage(m)[k] = *a;
+    cudaMemcpyAsync(m->d_par, m->h_par, m->par_bytes, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(m->D[2], 0, m->n * sizeof(float), st);
+    double best_f = 1e30;
+    for (int ti = 0; ti < TMA_FUSED_NTILES; ++ti)
+    {
+      if (m->fuse_tile_req >= 0 && ti != m->fuse_tile_req) continue;
+      auto one = [&]() {
+        return tma_fused_launch(&m->tma, ti, 4, m->ctx->num_sms, p->dev, dstage(m) + 2, 0, 1, fpar, m->D[2], m->D[3],
+                                m->ctx->d_err, st);
+      };
+      bool ok = one() && one();
+      cudaEventRecord(e0, st);
+      for (int k = 0; k < 5 && ok; ++k) ok = one();
+      cudaEventRecord(e1, st);
+      if (!ok || cudaEventSynchronize(e1) != cudaSuccess) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      m->fuse_ms[ti] = ms / 5.0;
+      if (m->fuse_ms[ti] < best_f)
+      {
+        best_f     = m->fuse_ms[ti];
+        m->fuse_ti = ti;
+      }
+    }
+    if (m->fuse_ti >= 0)
+    {
+      if (m->fuse_req >= 2) m->fuse_ks = m->fuse_req;
+      else if (best_f / 4.0 < best) m->fuse_ks = 4;
     }
   }
   cudaEventDestroy(e0);
@@ -743,14 +798,35 @@ static void record_step(LSRKMem* m, STS_Problem p, int s, int par)
   else
   {
     stage1_32_kernel<<<eb, 256, 0, st>>>(n, dstep(m), m->Ffb[par], m->D[0]);
-    int im2 = -1, im1 = 0, bi = 1;
-    for (int j = 2; j <= s; ++j)
+    int im2 = -1, im1 = 0;
+    const int nbuf = m->fuse_ks > 1 ? 4 : 3;
+    auto free_buf = [&](int skip) { // a stage buffer that is neither input nor `skip`
+      for (int b = 0; b < nbuf; ++b)
+        if (b != im1 && b != im2 && b != skip) return b;
+      return -1;
+    };
+    for (int j = 2; j <= s;)
     {
-      const int ij = bi;
-      bi           = (bi + 1) % 3;
+      const int ks = std::min(m->fuse_ks, s - j + 1);
+      if (ks >= 2)
+      {
+        // stages j .. j+ks-1 in one launch; the group's last two stages land in the two
+        // buffers that are not its inputs
+        const int o2 = free_buf(-1), o1 = free_buf(o2);
+        if (tma_fused_launch(&m->tma, m->fuse_ti, ks, m->ctx->num_sms, p->dev, dstage(m) + j, im1, im2, par,
+                             m->D[o2], m->D[o1], m->ctx->d_err, st))
+        {
+          im2 = o2;
+          im1 = o1;
+          j += ks;
+          continue;
+        }
+      }
+      const int ij = free_buf(-1);
       launch_stage32_idx(m, p, dstage(m) + j, im1, im2, par, ij);
       im2 = im1;
       im1 = ij;
+      ++j;
     }
     launch_stepend(m, p, par, nullptr, m->D[im1]);
   }
@@ -1714,8 +1790,42 @@ extern "C" int STS_LSRKStepGetStageKernelInfo(void* mem, int* variant, double* m
   if (name && namelen > 0)
   {
     const char* nm = m->mixed ? tma_stage32_variant_name(v) : "fp64_register_marching";
-    snprintf(name, namelen, "%s", nm);
+    if (m->mixed && m->fuse_ks > 1)
+      snprintf(name, namelen, "fused%d_tile120x%d (single stages: %s)", m->fuse_ks,
+               tma_fused_tile_rows(m->fuse_ti), nm);
+    else snprintf(name, namelen, "%s", nm);
   }
+  return 0;
+}
+
+extern "C" int STS_LSRKStepSetStageFusion(void* mem, int ks, int tile_rows)
+{
+  CHECK_MEM(mem);
+  int ti = -1;
+  for (int k = 0; k < TMA_FUSED_NTILES; ++k)
+    if (tile_rows == tma_fused_tile_rows(k)) ti = k;
+  if (ks < 0 || ks > 4 || (tile_rows != 0 && ti < 0))
+  {
+    sts_set_error("LSRKStepSetStageFusion: stages per launch 0 (autotuned), 1 (off) or 2-4; tile rows 0, 32 or 64");
+    return STS_ILL_INPUT;
+  }
+  LSRKMem* m = MEM(mem);
+  for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+  m->graphs.clear();
+  m->fuse_req      = ks;
+  m->fuse_tile_req = ti;
+  m->tuned         = false;
+  return 0;
+}
+
+extern "C" int STS_LSRKStepGetStageFusion(void* mem, int* ks, int* tile_rows, double* ms_per_launch)
+{
+  CHECK_MEM(mem);
+  LSRKMem* m = MEM(mem);
+  const bool on = m->mixed && m->fuse_ks > 1;
+  if (ks) *ks = on ? m->fuse_ks : 1;
+  if (tile_rows) *tile_rows = on ? tma_fused_tile_rows(m->fuse_ti) : 0;
+  if (ms_per_launch) *ms_per_launch = on ? m->fuse_ms[m->fuse_ti] : 0.0;
   return 0;
 }
 
@@ -1890,8 +2000,14 @@ extern "C" int STS_LSRKStepTimeStageKernel(void* mem, int nlaunch, double* ms_pe
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   // the parameter block of the last step is still on the device
+  // fused stages: one launch of the step's stage groups (stages j .. j+ks-1)
+  const int ks = (m->mixed && m->fuse_ks > 1 && m->last_s >= m->fuse_ks + 1) ? m->fuse_ks : 1;
+  const int jf = (ks > 1 && j + ks - 1 > m->last_s) ? 2 : j;
   auto one = [&](int k) {
-    if (m->mixed) launch_stage32_idx(m, p, dstage(m) + j, k % 3, (k + 1) % 3, m->par, (k + 2) % 3);
+    if (ks > 1)
+      tma_fused_launch(&m->tma, m->fuse_ti, ks, m->ctx->num_sms, p->dev, dstage(m) + jf, k % 4, (k + 1) % 4, m->par,
+                       m->D[(k + 2) % 4], m->D[(k + 3) % 4], m->ctx->d_err, st);
+    else if (m->mixed) launch_stage32_idx(m, p, dstage(m) + j, k % 3, (k + 1) % 3, m->par, (k + 2) % 3);
     else launch_stage64(m, p, dstage(m) + j, m->Y[k % 3], m->Y[(k + 1) % 3], m->yb[m->par], m->Fb[m->par], m->Y[(k + 2) % 3]);
   };
   one(0); // warm

@@ -229,6 +229,178 @@ __global__ void __launch_bounds__(256, K::MINB)
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Fused stages (temporal blocking): KS consecutive mixed stages j .. j+KS-1 in one pass.
+//
+// A CTA loads one 128 x (TH+8) tile of d_{j-1}, d_{j-2} and F_0 (4-cell halo on every side:
+// x from x0-4 keeps the 16-byte alignment, out-of-range parts arrive zero-filled) and runs
+// the stages in shared memory. Stage l of the group (l = 0 .. KS-1) is evaluated on the tile
+// rows [-(KS-1-l), TH+KS-1-l) and on all 128 columns; the cone of valid values shrinks by one
+// cell per stage and per side, so after KS <= 4 stages the 120 x TH output block is exact.
+// (Column 0 and 127 of the shared tile see a zero in place of their missing outer neighbour:
+// the error they carry moves inward by one column per stage and never reaches the output
+// columns 4 .. 123.) Each stage reads d_{j+l-2} only at the point itself, so its result is
+// written over that array in place: two stage arrays and F_0, 3 x 128 x (TH+8) floats.
+// Points outside the domain are set to zero after every stage (homogeneous Dirichlet ghost
+// values), exactly what the single-stage kernels read there. Only the group's last two
+// stages are stored to global memory (o2 = d_{j+KS-2}, o1 = d_{j+KS-1}): the next group, or
+// the step end, needs nothing else. Per point the arithmetic is mixed_point with the
+// operands of the single-stage kernels, so a group gives the bits of KS single launches.
+//
+// HBM traffic per point and group: 12 B read (d_{j-1}, d_{j-2}, F_0; the halo overlap of
+// neighbouring tiles is mostly served by L2) + 8 B written, 20 / KS B per DOF-stage against
+// 16 B for a single-stage launch.
+// ---------------------------------------------------------------------------------------
+constexpr int FW  = 128;    // loaded tile width (floats): 32 lanes x 4 columns
+constexpr int FH  = 4;      // halo rows / columns of the loaded tiles (KS <= FH)
+constexpr int FOW = FW - 2 * FH; // output columns per tile
+
+template <int TH_, int MINB_>
+struct FCfg {
+  static constexpr int TH = TH_, MINB = MINB_;
+  static constexpr int AH         = TH + 2 * FH;
+  static constexpr int ARR_BYTES  = FW * AH * 4;
+  static constexpr int SMEM_BYTES = 3 * ARR_BYTES + 16;
+};
+
+template <class K, int KS, bool FORCED, bool HAS_M2>
+__global__ void __launch_bounds__(256, K::MINB)
+  stage32_fused_kernel(const __grid_constant__ CUtensorMap mm1, const __grid_constant__ CUtensorMap mm2,
+                       const __grid_constant__ CUtensorMap mf0, ProbDev P, const StageArgs* __restrict__ A,
+                       float* __restrict__ o2, float* __restrict__ o1, int* err)
+{
+  static_assert(KS >= 2 && KS <= FH, "group of 2 .. 4 stages");
+  extern __shared__ __align__(128) unsigned char smem[];
+  float* arr0   = reinterpret_cast<float*>(smem);                    // d_{j-1}, then stages j+1, j+3
+  float* arr1   = reinterpret_cast<float*>(smem + K::ARR_BYTES);     // d_{j-2}, then stages j, j+2
+  float* f0s    = reinterpret_cast<float*>(smem + 2 * K::ARR_BYTES); // F_0 (FP32)
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 3 * K::ARR_BYTES);
+  const int nx = (int)P.nx, ny = (int)P.ny;
+  const int tiles_x = (nx + FOW - 1) / FOW;
+  const int ntiles  = tiles_x * ((ny + K::TH - 1) / K::TH);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int c = lane * 4; // this lane's first column in the shared tile
+
+  if (tid == 0)
+  {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  uint32_t parity = 0;
+  bool failed     = false;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
+  {
+    const int x0 = (t % tiles_x) * FOW, y0 = (t / tiles_x) * K::TH;
+    if (tid == 0)
+    {
+      // the previous tile's shared-memory reads and writes are ordered before these copies
+      // by the barrier that ended it
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(bar, (HAS_M2 ? 3 : 2) * K::ARR_BYTES);
+      tma_load_2d(arr0, &mm1, bar, x0 - FH, y0 - FH);
+      if (HAS_M2) tma_load_2d(arr1, &mm2, bar, x0 - FH, y0 - FH);
+      tma_load_2d(f0s, &mf0, bar, x0 - FH, y0 - FH);
+    }
+    const bool ok = mbar_wait_bounded(bar, parity);
+    parity ^= 1u;
+    if (__syncthreads_or(!ok))
+    {
+      failed = true;
+      break;
+    }
+    const int x        = x0 - FH + c; // global column of this lane's first point
+    const bool quad_in = x >= 0 && x < nx; // nx % 4 == 0: a quad is wholly inside or outside
+    const bool store_q = lane >= 1 && lane <= 30 && quad_in && STS_IN_BOUNDS(x + 4 <= nx, err);
+    float sx[4] = {0.f, 0.f, 0.f, 0.f}, sxx[4] = {0.f, 0.f, 0.f, 0.f};
+    if (FORCED && quad_in)
+    {
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+      {
+        sx[v]  = __ldg(P.Sxf + x + v);
+        sxx[v] = __ldg(P.Sxxf + x + v);
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < KS; ++l)
+    {
+      const float* X = (l & 1) ? arr1 : arr0; // d_{j+l-1}: centre and neighbours
+      float* Y       = (l & 1) ? arr0 : arr1; // d_{j+l-2} at the point, overwritten by d_{j+l}
+      const StageArgs* a = A + l;
+      const float gs = a->gsf, gx = a->gxf, gy = a->gyf, gm = a->gmf, gF = a->gFf;
+      float Pi[4] = {0.f, 0.f, 0.f, 0.f}, Qi[4] = {0.f, 0.f, 0.f, 0.f};
+      if (FORCED)
+      {
+        const float al = a->alf, be = a->bef, ga = a->gaf;
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+        {
+          Pi[v] = __fmaf_rn(al, sx[v], be * sxx[v]);
+          Qi[v] = ga * sx[v];
+        }
+      }
+      const int h     = KS - 1 - l; // rows of this stage: [-h, TH + h)
+      const int rows  = K::TH + 2 * h;
+      const int chunk = (rows + 7) / 8;
+      const int ra    = -h + warp * chunk;
+      const int rb    = min(ra + chunk, K::TH + h);
+      if (ra < rb) // warp-uniform
+      {
+        float4 up  = *reinterpret_cast<const float4*>(X + (ra - 1 + FH) * FW + c);
+        float4 cur = *reinterpret_cast<const float4*>(X + (ra + FH) * FW + c);
+        for (int r = ra; r < rb; ++r)
+        {
+          const float4 dn = *reinterpret_cast<const float4*>(X + (r + 1 + FH) * FW + c);
+          float w         = __shfl_up_sync(0xffffffffu, cur.w, 1);
+          float e         = __shfl_down_sync(0xffffffffu, cur.x, 1);
+          if (lane == 0) w = 0.0f;  // column -1 of the tile: not loaded (see above)
+          if (lane == 31) e = 0.0f; // column 128
+          float4 m2 = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (HAS_M2 || l > 0) m2 = *reinterpret_cast<const float4*>(Y + (r + FH) * FW + c);
+          const float4 q0   = *reinterpret_cast<const float4*>(f0s + (r + FH) * FW + c);
+          const int y       = y0 + r;
+          const bool row_in = y >= 0 && y < ny;
+          float syj = 0.0f, syyj = 0.0f;
+          if (FORCED && row_in)
+          {
+            syj  = __ldg(P.Syf + y);
+            syyj = __ldg(P.Syyf + y);
+          }
+          const float cv[4] = {cur.x, cur.y, cur.z, cur.w};
+          const float uv[4] = {up.x, up.y, up.z, up.w};
+          const float dv[4] = {dn.x, dn.y, dn.z, dn.w};
+          const float mv[4] = {m2.x, m2.y, m2.z, m2.w};
+          const float qv[4] = {q0.x, q0.y, q0.z, q0.w};
+          float o[4];
+#pragma unroll
+          for (int v = 0; v < 4; ++v)
+          {
+            const float uw = (v == 0) ? w : cv[v - 1];
+            const float ue = (v == 3) ? e : cv[v + 1];
+            o[v] = mixed_point<FORCED>(gs, gx, gy, gm, gF, cv[v], uw, ue, uv[v], dv[v], mv[v], qv[v], syj, Pi[v],
+                                       syyj, Qi[v]);
+          }
+          const bool in   = quad_in && row_in;
+          const float4 ov = in ? make_float4(o[0], o[1], o[2], o[3]) : make_float4(0.f, 0.f, 0.f, 0.f);
+          *reinterpret_cast<float4*>(Y + (r + FH) * FW + c) = ov;
+          if (l >= KS - 2 && r >= 0 && r < K::TH && row_in && store_q)
+            *reinterpret_cast<float4*>((l == KS - 1 ? o1 : o2) + (long long)y * nx + x) = ov;
+          up  = cur;
+          cur = dn;
+        }
+      }
+      __syncthreads(); // stage l complete before stage l+1 reads its neighbours (and before
+                       // the next tile's copies overwrite the arrays)
+    }
+  }
+  if (failed && tid == 0)
+  {
+    *(volatile int*)err = 1;
+    mbar_wait_bounded(bar, parity ^ 1u); // drain this tile's copies (bounded)
+  }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -298,6 +470,54 @@ bool launch_any(const TmaStage32* t, int num_sms, const ProbDev& P, const StageA
                     : launch_cfg<K, false, false>(t, num_sms, P, A, im1, im2, if0, out, err, st);
 }
 
+template <class K, int KS, bool F, bool M2>
+bool fused_launch_cfg(const TmaStage32* t, int ti, int num_sms, const ProbDev& P, const StageArgs* A, int im1,
+                      int im2, int if0, float* o2, float* o1, int* err, cudaStream_t st)
+{
+  static bool attr = false;
+  if (!attr)
+    attr = cudaFuncSetAttribute(stage32_fused_kernel<K, KS, F, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                K::SMEM_BYTES) == cudaSuccess;
+  if (!attr) return false;
+  const CUtensorMap& mm2 = t->fz[ti][im2 >= 0 ? im2 : im1];
+  const long long tiles  = ((P.nx + FOW - 1) / FOW) * ((P.ny + K::TH - 1) / K::TH);
+  const long long cap    = (long long)num_sms * K::MINB;
+  const int grid         = (int)(tiles < cap ? tiles : cap);
+  stage32_fused_kernel<K, KS, F, M2><<<grid, 256, K::SMEM_BYTES, st>>>(t->fz[ti][im1], mm2, t->fzf[ti][if0], P, A,
+                                                                        o2, o1, err);
+  return true;
+}
+
+template <class K, int KS>
+bool fused_launch_ks(const TmaStage32* t, int ti, int num_sms, const ProbDev& P, const StageArgs* A, int im1, int im2,
+                     int if0, float* o2, float* o1, int* err, cudaStream_t st)
+{
+  const bool forced = P.kind == STS_PROBLEM_MANUFACTURED;
+  if (forced)
+    return (im2 >= 0) ? fused_launch_cfg<K, KS, true, true>(t, ti, num_sms, P, A, im1, im2, if0, o2, o1, err, st)
+                      : fused_launch_cfg<K, KS, true, false>(t, ti, num_sms, P, A, im1, im2, if0, o2, o1, err, st);
+  return (im2 >= 0) ? fused_launch_cfg<K, KS, false, true>(t, ti, num_sms, P, A, im1, im2, if0, o2, o1, err, st)
+                    : fused_launch_cfg<K, KS, false, false>(t, ti, num_sms, P, A, im1, im2, if0, o2, o1, err, st);
+}
+
+template <class K>
+bool fused_launch_any(const TmaStage32* t, int ti, int ks, int num_sms, const ProbDev& P, const StageArgs* A, int im1,
+                      int im2, int if0, float* o2, float* o1, int* err, cudaStream_t st)
+{
+  switch (ks)
+  {
+  case 2: return fused_launch_ks<K, 2>(t, ti, num_sms, P, A, im1, im2, if0, o2, o1, err, st);
+  case 3: return fused_launch_ks<K, 3>(t, ti, num_sms, P, A, im1, im2, if0, o2, o1, err, st);
+  case 4: return fused_launch_ks<K, 4>(t, ti, num_sms, P, A, im1, im2, if0, o2, o1, err, st);
+  default: return false;
+  }
+}
+
+// fused-stage tile configurations (output rows per tile, CTAs per SM): 3 x 61 KB and
+// 2 x 111 KB of shared memory per SM
+using F0c = FCfg<32, 3>;
+using F1c = FCfg<64, 2>;
+
 // the configurations the autotuner chooses from (rows per tile, ring depth, CTAs per SM)
 using C0 = Cfg<32, 3, 1>;
 using C1 = Cfg<16, 4, 2>;
@@ -322,28 +542,72 @@ bool tma_stage32_supported(long long nx, long long ny)
   return nx % 4 == 0 && nx >= 8 && ny >= 2 && nx < (1LL << 30) && ny < (1LL << 30) && encode_fn() != nullptr;
 }
 
-bool tma_stage32_prepare(TmaStage32* t, float* const D[3], float* const Ff[2], long long nx, long long ny)
+bool tma_stage32_prepare(TmaStage32* t, float* const D[4], float* const Ff[2], long long nx, long long ny)
 {
   t->ok = false;
   if (!tma_stage32_supported(nx, ny)) return false;
   const int heights[] = {8, 16, 24, 32};
   for (int th : heights)
   {
-    for (int b = 0; b < 3; ++b)
+    for (int b = 0; b < 4; ++b)
     {
+      t->have[b] = false;
+      if (!D[b])
+      {
+        if (b < 3) return false;
+        continue;
+      }
       if (!encode(&t->halo[th][b], D[b], nx, ny, HW, th + 2)) return false;
       if (!encode(&t->plain[th][b], D[b], nx, ny, TW, th)) return false;
     }
     for (int b = 0; b < 2; ++b)
       if (!encode(&t->f0[th][b], Ff[b], nx, ny, TW, th)) return false;
   }
+  for (int b = 0; b < 4; ++b) t->have[b] = D[b] != nullptr;
   t->ok = true;
   return true;
+}
+
+int tma_fused_tile_rows(int ti)
+{
+  return ti == 0 ? F0c::TH : (ti == 1 ? F1c::TH : 0);
+}
+
+bool tma_fused_prepare(TmaStage32* t, float* const D[4], float* const Ff[2], long long nx, long long ny)
+{
+  t->fz_ok = false;
+  // the single-stage maps must cover D[3] too: a step's odd stage runs on any two buffers
+  if (!t->ok || !D[3] || !tma_stage32_supported(nx, ny)) return false;
+  for (int ti = 0; ti < TMA_FUSED_NTILES; ++ti)
+  {
+    const int th = tma_fused_tile_rows(ti);
+    for (int b = 0; b < 4; ++b)
+      if (!encode(&t->fz[ti][b], D[b], nx, ny, FW, th + 2 * FH)) return false;
+    for (int b = 0; b < 2; ++b)
+      if (!encode(&t->fzf[ti][b], Ff[b], nx, ny, FW, th + 2 * FH)) return false;
+  }
+  t->fz_ok = true;
+  return true;
+}
+
+bool tma_fused_launch(const TmaStage32* t, int ti, int ks, int num_sms, const ProbDev& P, const StageArgs* A, int im1,
+                      int im2, int if0, float* o2, float* o1, int* err, cudaStream_t st)
+{
+  if (!t->fz_ok || im1 < 0 || im1 > 3 || im2 > 3 || if0 < 0 || if0 > 1) return false;
+  switch (ti)
+  {
+  case 0: return fused_launch_any<F0c>(t, ti, ks, num_sms, P, A, im1, im2, if0, o2, o1, err, st);
+  case 1: return fused_launch_any<F1c>(t, ti, ks, num_sms, P, A, im1, im2, if0, o2, o1, err, st);
+  default: return false;
+  }
 }
 
 bool tma_stage32_launch(const TmaStage32* t, int variant, int num_sms, const ProbDev& P, const StageArgs* A, int im1,
                         int im2, int if0, float* out, int* err, cudaStream_t st)
 {
+  // only buffers whose maps were encoded (the caller falls back to the register kernel)
+  if (im1 < 0 || im1 > 3 || !t->have[im1] || im2 > 3 || (im2 >= 0 && !t->have[im2]) || if0 < 0 || if0 > 1)
+    return false;
   switch (variant)
   {
   case 0: return launch_any<C0>(t, num_sms, P, A, im1, im2, if0, out, err, st);

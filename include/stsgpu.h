@@ -252,6 +252,15 @@ int STS_LSRKStepSetStageKernel(void* mem, int variant);
 /* new: the autotuner's choice (-1 = register-marching), its time per launch and its name */
 int STS_LSRKStepGetStageKernelInfo(void* mem, int* variant, double* ms_per_launch, char* name,
                                    int namelen);
+/* new: mixed form, several stages per launch (temporal blocking on 120 x 32 or 120 x 64 tiles
+   in shared memory, the same bits as one launch per stage). ks: 0 = autotuned (default: four
+   stages per launch when the autotuner times that faster than one), 1 = off, 2..4 = that
+   many; tile_rows: 0 = autotuned, 32 or 64. Applies with the autotuned stage kernel
+   (STS_LSRKStepSetStageKernel variant 0). */
+int STS_LSRKStepSetStageFusion(void* mem, int ks, int tile_rows);
+/* new: the stages per launch in use (1: none), the tile rows and the autotuner's time per
+   four-stage launch */
+int STS_LSRKStepGetStageFusion(void* mem, int* ks, int* tile_rows, double* ms_per_launch);
 /* new: capture the fixed-s stage loop of the fused path in CUDA graphs (default on) */
 int STS_LSRKStepSetUseGraphs(void* mem, int on);
 /* new: reference mode (STS_PROBLEM_PERIODIC with STS_Diffusion): fused stage and step-end
@@ -277,7 +286,8 @@ int STS_LSRKStepWriteCheckpoint(void* arkode_mem, const char* path);
 int STS_LSRKStepReadCheckpoint(void* arkode_mem, const char* path);
 /* CUDA-event timing of the fused stage kernel on the integrator's current buffers (after at
  * least one evolve): average milliseconds per launch over nlaunch launches of stage j = s/2
- * of the last step, launched on the context stream exactly as the integrator does */
+ * of the last step (with several stages per launch: of the group starting there), launched
+ * on the context stream exactly as the integrator does */
 int STS_LSRKStepTimeStageKernel(void* mem, int nlaunch, double* ms_per_launch);
 int STS_ARKodeGetStats(void* mem, STS_Stats* stats);                  /* ARKodePrintAllStats main.cpp:486 */
 int STS_ARKodePrintAllStats(void* mem, char* buf, int buflen);

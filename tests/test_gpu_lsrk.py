@@ -123,6 +123,69 @@ def test_tma_stage_kernel_matches_register_kernel(ctx, stslib, oracle, nx, ny):
     assert np.array_equal(out[0][0], J.y)
 
 
+@pytest.mark.parametrize("nx,ny,kx", [(8, 8, 200.0), (96, 64, 1.0), (260, 70, 1.0), (248, 130, 1.0)])
+@pytest.mark.parametrize("kind", [0, 1])
+def test_fused_stage_groups_bitwise(ctx, stslib, oracle, nx, ny, kx, kind):
+    """Several mixed stages per launch (temporal blocking on 120 x 32 and 120 x 64 shared-memory
+    tiles with a 4-cell halo) give the oracle's bits: groups of 2, 3 and 4 stages, both tile
+    heights, the forced (kind 0) and unforced (kind 1) problems, ragged tiles, and the shorter
+    last group of every step whose stage count leaves a remainder (steps of 9 to 42 stages)."""
+    pk = dict(kind=kind, nx=nx, ny=ny, kx=kx, ky=0.05 * kx)
+    pm, qm, amp = [1, 3, 7], [2, 5, 1], [1.0, -0.5, 0.25]
+    O = oracle.Problem(**pk)
+    ok = dict(method=1, rtol=1e-6 if kind == 0 else 1e-3, atol=1e-10 if kind == 0 else 1e-6, mixed=True)
+    J = oracle.Integrator(O, O.initial() if kind == 0 else O.initial_modes(pm, qm, amp), **ok)
+    assert J.evolve(0.01) == 0
+    so = J.stats()
+    assert so["stage_max"] >= 5
+    for ks in (2, 3, 4):
+        for rows in (32, 64):
+            G = stslib.Problem(ctx, **pk)
+            y0 = G.initial() if kind == 0 else G.initial_modes(pm, qm, amp)
+            I = stslib.LSRKStep(ctx, G, 0.0, y0, stage_fusion=(ks, rows), **ok)
+            y = G.vector()
+            I.evolve(0.01, y)
+            info = I.stage_fusion_info()
+            assert info["ks"] == ks and info["tile_rows"] == rows, info
+            sg = I.stats()
+            for k in STAT_KEYS:
+                assert sg[k] == so[k], (ks, rows, k, sg[k], so[k])
+            assert np.array_equal(y.numpy(), J.y), (ks, rows, np.max(np.abs(y.numpy() - J.y)))
+
+
+def test_fused_stage_groups_1024(ctx, stslib, oracle):
+    """Four stages per launch on a 1024 x 1000 grid (nine tile columns, the last one 64 wide)
+    against one launch per stage and against the oracle; the autotuned choice, whichever it is,
+    gives the same bits."""
+    pk = dict(kind=0, nx=1024, ny=1000, kx=1.0, ky=0.05)
+    ok = dict(method=0, rtol=1e-6, atol=1e-10, mixed=True)
+    out = []
+    for fusion in ((1, 0), (4, 32), (4, 64), (0, 0)):
+        G = stslib.Problem(ctx, **pk)
+        I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), stage_fusion=fusion, **ok)
+        y = G.vector()
+        I.evolve(0.002, y)
+        out.append((y.numpy(), I.stats(), I.stage_fusion_info()))
+    assert out[0][2]["ks"] == 1 and out[1][2]["ks"] == 4 and out[2][2]["tile_rows"] == 64
+    for y, st, _ in out[1:]:
+        assert np.array_equal(out[0][0], y)
+        assert all(st[k] == out[0][1][k] for k in STAT_KEYS)
+    O = oracle.Problem(**pk)
+    J = oracle.Integrator(O, O.initial(), **ok)
+    assert J.evolve(0.002) == 0
+    assert np.array_equal(out[0][0], J.y)
+
+
+def test_stage_fusion_rejects_bad_arguments(ctx, stslib):
+    G = stslib.Problem(ctx, kind=0, nx=32, ny=32)
+    I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), mixed=True)
+    L = stslib.lib()
+    assert L.STS_LSRKStepSetStageFusion(I.mem, 5, 0) == STS_ILL_INPUT
+    assert L.STS_LSRKStepSetStageFusion(I.mem, 4, 48) == STS_ILL_INPUT
+    assert L.STS_LSRKStepSetStageFusion(I.mem, -1, 0) == STS_ILL_INPUT
+    assert L.STS_LSRKStepSetStageFusion(I.mem, 4, 64) == 0
+
+
 def test_unforced_and_small_stage_cap_bitwise(ctx, stslib, oracle):
     pk = dict(kind=1, nx=128, ny=80, kx=0.2, ky=0.9)
     ok = dict(method=1, rtol=1e-3, atol=1e-6, smax=4)
