@@ -207,7 +207,7 @@ def run_gpu(args):
         I = sts.LSRKStep(ctx, G, 0.0, G.initial(), method=METHOD, rtol=RTOL, atol=ATOL,
                          smax=SMAX, mixed=mixed, graphs=True, maxsteps=1000000,
                          stage_kernel=args.stage_kernel if mixed else 0,
-                         stage_fusion=(args.stage_fusion, args.fusion_rows) if mixed else (1, 0))
+                         stage_fusion=(args.stage_fusion, args.fusion_config) if mixed else (1, 0))
         y = G.vector()
 
         def one_step(k):
@@ -889,7 +889,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--stage-fusion", type=int, default=0,
                     help="mixed stages per launch: 0 autotuned, 1 off, 2-4 (STS_LSRKStepSetStageFusion)")
-    ap.add_argument("--fusion-rows", type=int, default=0, help="fused tile rows: 0 autotuned, 32 or 64")
+    ap.add_argument("--fusion-config", type=int, default=0,
+                    help="fused tile configuration: 0 autotuned, 1-4 (STS_LSRKStepSetStageFusion)")
     ap.add_argument("--stage-kernel", type=int, default=0,
                     help="mixed stage kernel: 0 autotune, 1 register marching, 2+k TMA configuration k")
     ap.add_argument("--reference-mode", action="store_true")

@@ -151,7 +151,7 @@ SIGNATURES = [
     ("STS_LSRKStepSetStageKernel", C.c_int, [_vp, C.c_int]),
     ("STS_LSRKStepGetStageKernelInfo", C.c_int, [_vp, _ip, _dp, C.c_char_p, C.c_int]),
     ("STS_LSRKStepSetStageFusion", C.c_int, [_vp, C.c_int, C.c_int]),
-    ("STS_LSRKStepGetStageFusion", C.c_int, [_vp, _ip, _ip, _dp]),
+    ("STS_LSRKStepGetStageFusion", C.c_int, [_vp, _ip, _ip, _ip, _dp]),
     ("STS_LSRKStepSetUseGraphs", C.c_int, [_vp, C.c_int]),
     ("STS_LSRKStepSetFusedPeriodic", C.c_int, [_vp, C.c_int]),
     ("STS_ARKodeEvolve", C.c_int, [_vp, C.c_double, _NV, _dp, C.c_int]),
@@ -526,8 +526,8 @@ class LSRKStep:
 
     ``rhs`` is either a :class:`Problem` (its built-in STS_Diffusion RHS; fused kernels) or a
     Python callable ``f(t, y: NVector, ydot: NVector) -> int`` (generic path).
-    ``stage_fusion = (stages per launch, tile rows)`` sets the mixed form's temporal blocking
-    (``STS_LSRKStepSetStageFusion``; (0, 0) autotuned, (1, 0) off)."""
+    ``stage_fusion = (stages per launch, tile configuration)`` sets the mixed form's temporal
+    blocking (``STS_LSRKStepSetStageFusion``; (0, 0) autotuned, (1, 0) off)."""
 
     def __init__(self, ctx, rhs, t0, y0, method=RKC, rtol=1e-6, atol=1e-10, controller=PID,
                  smax=200, mixed=False, graphs=True, dom_eig=None, power=None, maxsteps=100000,
@@ -623,11 +623,11 @@ class LSRKStep:
         return {"variant": v.value, "ms": ms.value, "name": buf.value.decode()}
 
     def stage_fusion_info(self):
-        """Stages per launch in use (1: one launch per stage), tile rows and the autotuner's
-        milliseconds per four-stage launch."""
-        ks, rows, ms = C.c_int(), C.c_int(), C.c_double()
-        lib().STS_LSRKStepGetStageFusion(self.mem, C.byref(ks), C.byref(rows), C.byref(ms))
-        return {"ks": ks.value, "tile_rows": rows.value, "ms": ms.value}
+        """Stages per launch in use (1: one launch per stage), the tile configuration (0: none)
+        and its rows, and the autotuner's milliseconds per four-stage launch."""
+        ks, cfg, rows, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        lib().STS_LSRKStepGetStageFusion(self.mem, C.byref(ks), C.byref(cfg), C.byref(rows), C.byref(ms))
+        return {"ks": ks.value, "config": cfg.value, "tile_rows": rows.value, "ms": ms.value}
 
     def time_stage_kernel(self, nlaunch=20):
         ms = C.c_double()

@@ -109,6 +109,34 @@ __device__ __forceinline__ float mixed_point(float gs, float gx, float gy, float
   return __fadd_rn(dc, inc);
 }
 
+// mixed_point on two points at once with the paired FP32 instructions of sm_100 and later
+// (__fadd2_rn, __fmul2_rn, __ffma2_rn: per component the same rounding as __fadd_rn,
+// __fmul_rn, __fmaf_rn). A difference a - b is taken as a + (-b), which IEEE arithmetic gives
+// exactly, signed zeros included; the negations are multiplications by -1 (exact). The two
+// components are bit-identical to two mixed_point calls. Operands are (point 0, point 1)
+// pairs; the scalars arrive duplicated.
+template <bool FORCED>
+__device__ __forceinline__ float2 mixed_pair(float2 gs, float2 gx, float2 gy, float2 gm, float2 gF, float2 dc,
+                                             float2 dw, float2 de, float2 ds, float2 dn, float2 m2, float2 q0,
+                                             float2 syj, float2 pi, float2 syyj, float2 qi)
+{
+  const float2 neg1 = make_float2(-1.0f, -1.0f);
+  const float2 ndc  = __fmul2_rn(dc, neg1);
+  const float2 lx   = __fadd2_rn(__fadd2_rn(dw, ndc), __fadd2_rn(de, ndc));
+  const float2 ly   = __fadd2_rn(__fadd2_rn(ds, ndc), __fadd2_rn(dn, ndc));
+  float2 inc        = __fmul2_rn(gs, dc);
+  inc               = __ffma2_rn(gx, lx, inc);
+  inc               = __ffma2_rn(gy, ly, inc);
+  inc               = __ffma2_rn(gm, __fadd2_rn(dc, __fmul2_rn(m2, neg1)), inc);
+  inc               = __ffma2_rn(gF, q0, inc);
+  if (FORCED)
+  {
+    inc = __ffma2_rn(syj, pi, inc);
+    inc = __ffma2_rn(syyj, qi, inc);
+  }
+  return __fadd2_rn(dc, inc);
+}
+
 // Error weight of the mixed form's step end, 1 / (rtol |y| + atol) to within a few ulp with five
 // FP64-pipe operations instead of a correctly rounded division (about ten on GB300, whose FP64
 // pipe bounds this kernel): den = fma(rtol, |y|, atol), the correctly rounded FP32 reciprocal of

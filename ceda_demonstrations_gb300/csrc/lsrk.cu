@@ -1791,39 +1791,38 @@ extern "C" int STS_LSRKStepGetStageKernelInfo(void* mem, int* variant, double* m
   {
     const char* nm = m->mixed ? tma_stage32_variant_name(v) : "fp64_register_marching";
     if (m->mixed && m->fuse_ks > 1)
-      snprintf(name, namelen, "fused%d_tile120x%d (single stages: %s)", m->fuse_ks,
-               tma_fused_tile_rows(m->fuse_ti), nm);
+      snprintf(name, namelen, "fused%d_%s (single stages: %s)", m->fuse_ks, tma_fused_config_name(m->fuse_ti), nm);
     else snprintf(name, namelen, "%s", nm);
   }
   return 0;
 }
 
-extern "C" int STS_LSRKStepSetStageFusion(void* mem, int ks, int tile_rows)
+extern "C" int STS_LSRKStepSetStageFusion(void* mem, int ks, int config)
 {
   CHECK_MEM(mem);
-  int ti = -1;
-  for (int k = 0; k < TMA_FUSED_NTILES; ++k)
-    if (tile_rows == tma_fused_tile_rows(k)) ti = k;
-  if (ks < 0 || ks > 4 || (tile_rows != 0 && ti < 0))
+  if (ks < 0 || ks > 4 || config < 0 || config > TMA_FUSED_NTILES)
   {
-    sts_set_error("LSRKStepSetStageFusion: stages per launch 0 (autotuned), 1 (off) or 2-4; tile rows 0, 32 or 64");
+    sts_set_error("LSRKStepSetStageFusion: stages per launch 0 (autotuned), 1 (off) or 2-4; tile configuration 0 "
+                  "(autotuned) or 1-%d",
+                  TMA_FUSED_NTILES);
     return STS_ILL_INPUT;
   }
   LSRKMem* m = MEM(mem);
   for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
   m->graphs.clear();
   m->fuse_req      = ks;
-  m->fuse_tile_req = ti;
+  m->fuse_tile_req = config - 1;
   m->tuned         = false;
   return 0;
 }
 
-extern "C" int STS_LSRKStepGetStageFusion(void* mem, int* ks, int* tile_rows, double* ms_per_launch)
+extern "C" int STS_LSRKStepGetStageFusion(void* mem, int* ks, int* config, int* tile_rows, double* ms_per_launch)
 {
   CHECK_MEM(mem);
   LSRKMem* m = MEM(mem);
   const bool on = m->mixed && m->fuse_ks > 1;
   if (ks) *ks = on ? m->fuse_ks : 1;
+  if (config) *config = on ? m->fuse_ti + 1 : 0;
   if (tile_rows) *tile_rows = on ? tma_fused_tile_rows(m->fuse_ti) : 0;
   if (ms_per_launch) *ms_per_launch = on ? m->fuse_ms[m->fuse_ti] : 0.0;
   return 0;

@@ -14,8 +14,8 @@ struct TmaStage32 {
   bool ok = false;
   bool have[4] = {false, false, false, false}; // maps encoded for buffer b
   // fused stages: 128 x (TH+8) boxes of the four stage buffers and of F_n, per tile height
-  CUtensorMap fz[2][4];
-  CUtensorMap fzf[2][2];
+  CUtensorMap fz[4][4];
+  CUtensorMap fzf[4][2];
   bool fz_ok = false;
 };
 
@@ -32,8 +32,9 @@ bool tma_stage32_launch(const TmaStage32* t, int variant, int num_sms, const Pro
 // consecutive entries), d_{j-1} = D[im1], d_{j-2} = D[im2] (im2 < 0: j = 2), F_0 = Ff[if0];
 // writes d_{j+ks-2} to o2 and d_{j+ks-1} to o1 (neither may be an input buffer). Tile
 // configuration ti in [0, TMA_FUSED_NTILES).
-constexpr int TMA_FUSED_NTILES = 2;
+constexpr int TMA_FUSED_NTILES = 4;
 int tma_fused_tile_rows(int ti);
+const char* tma_fused_config_name(int ti);
 bool tma_fused_prepare(TmaStage32* t, float* const D[4], float* const Ff[2], long long nx, long long ny);
 bool tma_fused_launch(const TmaStage32* t, int ti, int ks, int num_sms, const ProbDev& P, const StageArgs* A, int im1,
                       int im2, int if0, float* o2, float* o1, int* err, cudaStream_t st);

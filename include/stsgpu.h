@@ -252,15 +252,16 @@ int STS_LSRKStepSetStageKernel(void* mem, int variant);
 /* new: the autotuner's choice (-1 = register-marching), its time per launch and its name */
 int STS_LSRKStepGetStageKernelInfo(void* mem, int* variant, double* ms_per_launch, char* name,
                                    int namelen);
-/* new: mixed form, several stages per launch (temporal blocking on 120 x 32 or 120 x 64 tiles
-   in shared memory, the same bits as one launch per stage). ks: 0 = autotuned (default: four
-   stages per launch when the autotuner times that faster than one), 1 = off, 2..4 = that
-   many; tile_rows: 0 = autotuned, 32 or 64. Applies with the autotuned stage kernel
-   (STS_LSRKStepSetStageKernel variant 0). */
-int STS_LSRKStepSetStageFusion(void* mem, int ks, int tile_rows);
-/* new: the stages per launch in use (1: none), the tile rows and the autotuner's time per
-   four-stage launch */
-int STS_LSRKStepGetStageFusion(void* mem, int* ks, int* tile_rows, double* ms_per_launch);
+/* new: mixed form, several stages per launch (temporal blocking on 120-column tiles in shared
+   memory, the same bits as one launch per stage). ks: 0 = autotuned (default: four stages per
+   launch when the autotuner times that faster than one), 1 = off, 2..4 = that many; config:
+   0 = autotuned, 1..4 = tile configuration (1: 120 x 32, three CTAs per SM; 2: 120 x 64, two
+   CTAs per SM; 3: 120 x 64 and 4: 120 x 48, one 512-thread CTA per SM with two tile buffers).
+   Applies with the autotuned stage kernel (STS_LSRKStepSetStageKernel variant 0). */
+int STS_LSRKStepSetStageFusion(void* mem, int ks, int config);
+/* new: the stages per launch in use (1: none), the tile configuration (0: none) and its rows,
+   and the autotuner's time per four-stage launch */
+int STS_LSRKStepGetStageFusion(void* mem, int* ks, int* config, int* tile_rows, double* ms_per_launch);
 /* new: capture the fixed-s stage loop of the fused path in CUDA graphs (default on) */
 int STS_LSRKStepSetUseGraphs(void* mem, int on);
 /* new: reference mode (STS_PROBLEM_PERIODIC with STS_Diffusion): fused stage and step-end

@@ -139,18 +139,18 @@ def test_fused_stage_groups_bitwise(ctx, stslib, oracle, nx, ny, kx, kind):
     so = J.stats()
     assert so["stage_max"] >= 5
     for ks in (2, 3, 4):
-        for rows in (32, 64):
+        for cfg in (1, 2, 3, 4):
             G = stslib.Problem(ctx, **pk)
             y0 = G.initial() if kind == 0 else G.initial_modes(pm, qm, amp)
-            I = stslib.LSRKStep(ctx, G, 0.0, y0, stage_fusion=(ks, rows), **ok)
+            I = stslib.LSRKStep(ctx, G, 0.0, y0, stage_fusion=(ks, cfg), **ok)
             y = G.vector()
             I.evolve(0.01, y)
             info = I.stage_fusion_info()
-            assert info["ks"] == ks and info["tile_rows"] == rows, info
+            assert info["ks"] == ks and info["config"] == cfg, info
             sg = I.stats()
             for k in STAT_KEYS:
-                assert sg[k] == so[k], (ks, rows, k, sg[k], so[k])
-            assert np.array_equal(y.numpy(), J.y), (ks, rows, np.max(np.abs(y.numpy() - J.y)))
+                assert sg[k] == so[k], (ks, cfg, k, sg[k], so[k])
+            assert np.array_equal(y.numpy(), J.y), (ks, cfg, np.max(np.abs(y.numpy() - J.y)))
 
 
 def test_fused_stage_groups_1024(ctx, stslib, oracle):
@@ -160,13 +160,14 @@ def test_fused_stage_groups_1024(ctx, stslib, oracle):
     pk = dict(kind=0, nx=1024, ny=1000, kx=1.0, ky=0.05)
     ok = dict(method=0, rtol=1e-6, atol=1e-10, mixed=True)
     out = []
-    for fusion in ((1, 0), (4, 32), (4, 64), (0, 0)):
+    for fusion in ((1, 0), (4, 1), (4, 2), (4, 3), (4, 4), (0, 0)):
         G = stslib.Problem(ctx, **pk)
         I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), stage_fusion=fusion, **ok)
         y = G.vector()
         I.evolve(0.002, y)
         out.append((y.numpy(), I.stats(), I.stage_fusion_info()))
-    assert out[0][2]["ks"] == 1 and out[1][2]["ks"] == 4 and out[2][2]["tile_rows"] == 64
+    assert out[0][2]["ks"] == 1 and out[1][2]["ks"] == 4
+    assert [o[2]["tile_rows"] for o in out[1:5]] == [32, 64, 64, 48]
     for y, st, _ in out[1:]:
         assert np.array_equal(out[0][0], y)
         assert all(st[k] == out[0][1][k] for k in STAT_KEYS)
@@ -181,9 +182,9 @@ def test_stage_fusion_rejects_bad_arguments(ctx, stslib):
     I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), mixed=True)
     L = stslib.lib()
     assert L.STS_LSRKStepSetStageFusion(I.mem, 5, 0) == STS_ILL_INPUT
-    assert L.STS_LSRKStepSetStageFusion(I.mem, 4, 48) == STS_ILL_INPUT
+    assert L.STS_LSRKStepSetStageFusion(I.mem, 4, 5) == STS_ILL_INPUT
     assert L.STS_LSRKStepSetStageFusion(I.mem, -1, 0) == STS_ILL_INPUT
-    assert L.STS_LSRKStepSetStageFusion(I.mem, 4, 64) == 0
+    assert L.STS_LSRKStepSetStageFusion(I.mem, 4, 3) == 0
 
 
 def test_unforced_and_small_stage_cap_bitwise(ctx, stslib, oracle):
