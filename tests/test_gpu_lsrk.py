@@ -139,7 +139,7 @@ def test_fused_stage_groups_bitwise(ctx, stslib, oracle, nx, ny, kx, kind):
     so = J.stats()
     assert so["stage_max"] >= 5
     for ks in (2, 3, 4):
-        for cfg in (1, 2, 3, 4):
+        for cfg in range(1, 7):
             G = stslib.Problem(ctx, **pk)
             y0 = G.initial() if kind == 0 else G.initial_modes(pm, qm, amp)
             I = stslib.LSRKStep(ctx, G, 0.0, y0, stage_fusion=(ks, cfg), **ok)
@@ -154,20 +154,20 @@ def test_fused_stage_groups_bitwise(ctx, stslib, oracle, nx, ny, kx, kind):
 
 
 def test_fused_stage_groups_1024(ctx, stslib, oracle):
-    """Four stages per launch on a 1024 x 1000 grid (nine tile columns, the last one 64 wide)
-    against one launch per stage and against the oracle; the autotuned choice, whichever it is,
-    gives the same bits."""
+    """Four stages per launch on a 1024 x 1000 grid (nine tile columns, the last one 64 wide),
+    every tile configuration, against one launch per stage and against the oracle; the
+    autotuned choice, whichever it is, gives the same bits."""
     pk = dict(kind=0, nx=1024, ny=1000, kx=1.0, ky=0.05)
     ok = dict(method=0, rtol=1e-6, atol=1e-10, mixed=True)
     out = []
-    for fusion in ((1, 0), (4, 1), (4, 2), (4, 3), (4, 4), (0, 0)):
+    for fusion in ((1, 0),) + tuple((4, cfg) for cfg in range(1, 7)) + ((0, 0),):
         G = stslib.Problem(ctx, **pk)
         I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), stage_fusion=fusion, **ok)
         y = G.vector()
         I.evolve(0.002, y)
         out.append((y.numpy(), I.stats(), I.stage_fusion_info()))
     assert out[0][2]["ks"] == 1 and out[1][2]["ks"] == 4
-    assert [o[2]["tile_rows"] for o in out[1:5]] == [32, 64, 64, 48]
+    assert [o[2]["tile_rows"] for o in out[1:7]] == [32, 64, 64, 64, 64, 64]
     for y, st, _ in out[1:]:
         assert np.array_equal(out[0][0], y)
         assert all(st[k] == out[0][1][k] for k in STAT_KEYS)
@@ -182,7 +182,7 @@ def test_stage_fusion_rejects_bad_arguments(ctx, stslib):
     I = stslib.LSRKStep(ctx, G, 0.0, G.initial(), mixed=True)
     L = stslib.lib()
     assert L.STS_LSRKStepSetStageFusion(I.mem, 5, 0) == STS_ILL_INPUT
-    assert L.STS_LSRKStepSetStageFusion(I.mem, 4, 5) == STS_ILL_INPUT
+    assert L.STS_LSRKStepSetStageFusion(I.mem, 4, 7) == STS_ILL_INPUT
     assert L.STS_LSRKStepSetStageFusion(I.mem, -1, 0) == STS_ILL_INPUT
     assert L.STS_LSRKStepSetStageFusion(I.mem, 4, 3) == 0
 
