@@ -150,13 +150,18 @@ def mixed_stage_traffic(n):
     return TRAFFIC_MIXED_STAGE_6144 * (n / 6144.0) ** 2
 
 
-# DRAM bytes of one launch of the fused four-stage kernel (120 x 64 tiles), same method:
-# measured on a 4096^2 case and scaled by the DOF count. None until captured.
-TRAFFIC_FUSED4_4096 = None
+# DRAM bytes of one launch of the fused four-stage kernel (120 x 64 tiles, two CTAs per SM,
+# with d_{j-2} input), same method: a 6144^2 capture scaled by the DOF count:
+#   python bench.py --n 6144 --steps 1 --warmup 3 --no-cpu --stage-fusion 4 --fusion-config 2
+#   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum \
+#       --clock-control none -k regex:stage32_fused -s 10 -c 2 --csv --log-file ncu_fused_6144.csv \
+#       python bench.py --n 6144 --steps 1 --warmup 3 --no-cpu --stage-fusion 4 --fusion-config 2
+# 6144^2: 459.5 MB read + 260.0 MB written = 719.5 MB per launch (algorithmic 754.9 MB).
+TRAFFIC_FUSED4_6144 = 719.5e6
 
 
 def fused_stage_traffic(n):
-    return None if TRAFFIC_FUSED4_4096 is None else TRAFFIC_FUSED4_4096 * (n / 4096.0) ** 2
+    return TRAFFIC_FUSED4_6144 * (n / 6144.0) ** 2
 
 
 def replica_barrier(ws):
@@ -210,6 +215,8 @@ def run_gpu(args):
                          stage_fusion=(args.stage_fusion, args.fusion_config) if mixed else (1, 0))
         y = G.vector()
 
+        step_stages = []  # stages_total after each mixed step: the stage count of every attempt
+
         def one_step(k):
             # the FP64 arm takes the mixed arm's step sequence (ARKodeSetFixedStep before each
             # step), so that both end at the same t and their fields can be compared
@@ -217,7 +224,9 @@ def run_gpu(args):
                 L.STS_ARKodeSetFixedStep(I.mem, hseq[k])
             I.evolve(TF, y, sts.ONE_STEP)
             if mixed:
-                hseq.append(I.stats()["hlast"])
+                st = I.stats()
+                hseq.append(st["hlast"])
+                step_stages.append(st["stages_total"])
         for k in range(args.warmup):
             one_step(k)
         ctx.synchronize()
@@ -238,10 +247,18 @@ def run_gpu(args):
         kinfo = I.stage_kernel_info()
         kinfo["fusion"] = I.stage_fusion_info()
         # kernels per attempt: stage 1, the stages 2..s (one launch per stage, or per group of
-        # ks with a shorter last group), the step end (the timed steps all have s stages)
+        # ks with a shorter last group), the step end; the timed steps take no rejected attempt
+        # here, so the stage counts of the accepted steps are those of the attempts
         ks = kinfo["fusion"]["ks"]
-        s_att = stages // attempts if attempts else 0
-        launches = attempts * (2 + (s_att - 2 + ks) // ks) if ks > 1 else stages + attempts
+        if ks > 1 and mixed and attempts == args.steps:
+            marks = [s0["stages_total"]] + step_stages[args.warmup:]
+            per = [b - a for a, b in zip(marks, marks[1:])]
+            launches = sum(2 + (sa - 2 + ks) // ks for sa in per)
+        elif ks > 1:
+            s_att = stages // attempts if attempts else 0
+            launches = attempts * (2 + (s_att - 2 + ks) // ks)
+        else:
+            launches = stages + attempts
         res[mixed] = dict(ms=ms, dof_stages=dof_stages, launches=launches, stage_ms=stage_ms, kinfo=kinfo,
                           t=s1["t"], s=s1["stage_max"], stats=s1, y=y.numpy(), I=I,
                           steps=s1["nst"] - s0["nst"])
