@@ -118,12 +118,7 @@ __global__ void __launch_bounds__(K::NT, K::MINB)
         const float v = (y >= 0 && y < ny) ? __ldg((r < K::AH ? P.Syf : P.Syyf) + y) : 0.0f;
         sys[r]        = make_float2(v, v);
       }
-    const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((k / K::NSET) & 1));
-    if (__syncthreads_or(!ok))
-    {
-      failed = true;
-      break;
-    }
+    // this lane's forcing columns load while the tile's copies are in flight
     const int x        = x0 - FH + c; // global column of this lane's first point
     const bool quad_in = x >= 0 && x < nx; // nx % 4 == 0: a quad is wholly inside or outside
     const bool store_q = lane >= 1 && lane <= 30 && quad_in && STS_IN_BOUNDS(x + 4 <= nx, err);
@@ -136,6 +131,12 @@ __global__ void __launch_bounds__(K::NT, K::MINB)
         sx[v]  = __ldg(P.Sxf + x + v);
         sxx[v] = __ldg(P.Sxxf + x + v);
       }
+    }
+    const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((k / K::NSET) & 1));
+    if (__syncthreads_or(!ok))
+    {
+      failed = true;
+      break;
     }
     // tiles whose loaded region lies inside the domain need no masking of outside points
     const bool interior = x0 - FH >= 0 && x0 + FOW + FH <= nx && y0 - FH >= 0 && y0 + K::TH + FH <= ny;
