@@ -111,14 +111,8 @@ __global__ void __launch_bounds__(K::NT, K::MINB)
     float* arr1  = arr(b, 1); // d_{j-2}, then stages j, j+2
     const float* f0s = arr(b, 2);
     float2* sys  = reinterpret_cast<float2*>(arr(b, 3)); // Sy rows, then Syy rows, duplicated
-    if (FORCED)
-      for (int r = tid; r < 2 * K::AH; r += K::NT)
-      {
-        const int y   = y0 - FH + (r % K::AH);
-        const float v = (y >= 0 && y < ny) ? __ldg((r < K::AH ? P.Syf : P.Syyf) + y) : 0.0f;
-        sys[r]        = make_float2(v, v);
-      }
-    // this lane's forcing columns load while the tile's copies are in flight
+    // the forcing columns of this lane and the forcing rows of the tile load while the tile's
+    // copies are in flight (all loads issued before the first shared-memory store)
     const int x        = x0 - FH + c; // global column of this lane's first point
     const bool quad_in = x >= 0 && x < nx; // nx % 4 == 0: a quad is wholly inside or outside
     const bool store_q = lane >= 1 && lane <= 30 && quad_in && STS_IN_BOUNDS(x + 4 <= nx, err);
@@ -131,6 +125,14 @@ __global__ void __launch_bounds__(K::NT, K::MINB)
         sx[v]  = __ldg(P.Sxf + x + v);
         sxx[v] = __ldg(P.Sxxf + x + v);
       }
+    }
+    if (FORCED)
+    {
+      static_assert(2 * K::AH <= K::NT, "one forcing row per thread");
+      const int r = tid % K::AH, y = y0 - FH + r;
+      float v = 0.0f;
+      if (tid < 2 * K::AH && y >= 0 && y < ny) v = __ldg((tid < K::AH ? P.Syf : P.Syyf) + y);
+      if (tid < 2 * K::AH) sys[tid] = make_float2(v, v);
     }
     const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((k / K::NSET) & 1));
     if (__syncthreads_or(!ok))
@@ -198,7 +200,8 @@ __global__ void __launch_bounds__(K::NT, K::MINB)
               pi23, syyj, qi23);
             float4 ov = make_float4(o01.x, o01.y, o23.x, o23.y);
             if (MASK && !(quad_in && y >= 0 && y < ny)) ov = make_float4(0.f, 0.f, 0.f, 0.f);
-            *reinterpret_cast<float4*>(Y + (r + FH) * FW + c) = ov;
+            if (l < KS - 1) // the last stage is read by no later stage of this group
+              *reinterpret_cast<float4*>(Y + (r + FH) * FW + c) = ov;
             if (l >= KS - 2 && r >= 0 && r < K::TH && (!MASK || y < ny) && store_q)
               *reinterpret_cast<float4*>((l == KS - 1 ? o1 : o2) + (long long)y * nx + x) = ov;
           };
