@@ -145,7 +145,12 @@ __device__ __forceinline__ float2 mixed_pair(float2 gs, float2 gx, float2 gy, fl
 __device__ __forceinline__ double mixed_weight(double rtol, double atol, double y)
 {
   const double den = __fma_rn(rtol, fabs(y), atol);
-  if (den >= 0x1p-120 && den <= 0x1p120)
+  // den in [2^-120, 2^120], decided on the bit pattern: for doubles with the sign bit clear the
+  // order of the bit patterns as signed integers is the order of the values, and every
+  // negative value, zero, infinity and NaN falls outside the range exactly as with the two
+  // floating-point comparisons (which would take the FP64 pipe)
+  const long long u = __double_as_longlong(den);
+  if (u >= 0x3870000000000000LL && u <= 0x4770000000000000LL)
   {
     const double r0 = (double)__frcp_rn(__double2float_rn(den));
     const double e1 = __fma_rn(-den, r0, 1.0);
