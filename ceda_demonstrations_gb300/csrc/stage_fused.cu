@@ -300,9 +300,9 @@ bool fused_launch_any(const TmaStage32* t, int ti, int ks, int num_sms, const Pr
 // the autotuner times them on the problem's own buffers
 using F0c = FCfg<32, 256, 3, 1>; // 3 x 62 KB of shared memory per SM
 using F1c = FCfg<64, 256, 2, 1>; // 2 x 112 KB
-using F2c = FCfg<64, 512, 1, 2>; // 1 x 224 KB: the next tile loads while this one computes
+using F2c = FCfg<60, 256, 2, 1>; // 2 x 105 KB: stage rows 66..60 split 9/8/8/8 over 8 warps
 using F3c = FCfg<64, 384, 2, 1>; // 2 x 112 KB, 12 warps per CTA
-using F4c = FCfg<64, 320, 2, 1>; // 2 x 112 KB, 10 warps per CTA
+using F4c = FCfg<58, 256, 2, 1>; // 2 x 102 KB: stage rows 64..58 split 8 per warp
 using F5c = FCfg<64, 256, 1, 2>; // 1 x 224 KB, double buffered, 8 warps
 
 } // namespace
@@ -315,8 +315,8 @@ int tma_fused_tile_rows(int ti)
 
 const char* tma_fused_config_name(int ti)
 {
-  static const char* names[] = {"tile120x32_3cta",         "tile120x64_2cta",         "tile120x64_1cta512_2buf",
-                                "tile120x64_2cta384",      "tile120x64_2cta320",      "tile120x64_1cta256_2buf"};
+  static const char* names[] = {"tile120x32_3cta",    "tile120x64_2cta",    "tile120x60_2cta",
+                                "tile120x64_2cta384", "tile120x58_2cta",    "tile120x64_1cta256_2buf"};
   return (ti >= 0 && ti < TMA_FUSED_NTILES) ? names[ti] : "none";
 }
 

@@ -255,9 +255,9 @@ int STS_LSRKStepGetStageKernelInfo(void* mem, int* variant, double* ms_per_launc
 /* new: mixed form, several stages per launch (temporal blocking on 120-column tiles in shared
    memory, the same bits as one launch per stage). ks: 0 = autotuned (default: four stages per
    launch when the autotuner times that faster than one), 1 = off, 2..4 = that many; config:
-   0 = autotuned, 1..6 = tile configuration (1: 120 x 32, three CTAs per SM; 2, 4, 5: 120 x 64,
-   two CTAs of 256, 384 or 320 threads per SM; 3, 6: 120 x 64, one CTA of 512 or 256 threads
-   per SM with two tile buffers).
+   0 = autotuned, 1..6 = tile configuration (1: 120 x 32, three CTAs per SM; 2, 3, 5: 120 x 64,
+   120 x 60 and 120 x 58, two CTAs of 256 threads per SM; 4: 120 x 64, two CTAs of 384 threads;
+   6: 120 x 64, one CTA of 256 threads per SM with two tile buffers).
    Applies with the autotuned stage kernel (STS_LSRKStepSetStageKernel variant 0). */
 int STS_LSRKStepSetStageFusion(void* mem, int ks, int config);
 /* new: the stages per launch in use (1: none), the tile configuration (0: none) and its rows,

@@ -167,7 +167,7 @@ def test_fused_stage_groups_1024(ctx, stslib, oracle):
         I.evolve(0.002, y)
         out.append((y.numpy(), I.stats(), I.stage_fusion_info()))
     assert out[0][2]["ks"] == 1 and out[1][2]["ks"] == 4
-    assert [o[2]["tile_rows"] for o in out[1:7]] == [32, 64, 64, 64, 64, 64]
+    assert [o[2]["tile_rows"] for o in out[1:7]] == [32, 64, 60, 64, 58, 64]
     for y, st, _ in out[1:]:
         assert np.array_equal(out[0][0], y)
         assert all(st[k] == out[0][1][k] for k in STAT_KEYS)
