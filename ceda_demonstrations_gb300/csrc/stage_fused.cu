@@ -31,8 +31,11 @@ namespace {
 // inside the domain skip that mask. The forcing rows of the tile and the group's stage
 // scalars are staged in shared memory once. Only the group's last two
 // stages are stored to global memory (o2 = d_{j+KS-2}, o1 = d_{j+KS-1}): the next group, or
-// the step end, needs nothing else. Per point the arithmetic is mixed_point with the
-// operands of the single-stage kernels, so a group gives the bits of KS single launches.
+// the step end, needs nothing else. Per point the arithmetic is mixed_point's with the
+// operands of the single-stage kernels, evaluated two columns at a time by mixed_pair (the
+// paired FP32 instructions, the same rounding per component), so a group gives the bits of
+// KS single launches. Rows march three per trip, so the row window rotates through registers
+// without copies.
 //
 // HBM traffic per point and group: 12 B read (d_{j-1}, d_{j-2}, F_0; the halo overlap of
 // neighbouring tiles is mostly served by L2) + 8 B written, 20 / KS B per DOF-stage against
