@@ -1,7 +1,7 @@
 """Debug-bounds build (-DSTS_DEBUG_BOUNDS) in place of a sanitizer on the GPU.
 
-The library is rebuilt with index-range checks in the stage, step-end, TMA-stage and batched
-kernels (a violation writes the context's error word and skips the access; nothing traps),
+The library is rebuilt with index-range checks in the stage, step-end, TMA-stage, fused-stage
+and batched kernels (a violation writes the context's error word and skips the access; nothing traps),
 and the bitwise parity tests of those kernels run against it in a child process: a check that
 fired would fail its step, and the results must still equal the oracle's bit for bit."""
 import os
@@ -14,6 +14,7 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 SUBSET = ("fused_fp64_bitwise or mixed_bitwise or tma_stage_kernel_matches or controllers_bitwise"
+          " or fused_stage_groups"
           " or batch_matches_oracle_per_instance or batch_launch_shapes or batch_clusters")
 
 
