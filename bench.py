@@ -164,6 +164,15 @@ def fused_stage_traffic(n):
     return TRAFFIC_FUSED4_6144 * (n / 6144.0) ** 2
 
 
+def step_launches(stages, ks):
+    """Kernels one step attempt of `stages` stages launches on the fused mixed path: stage 1,
+    the stages 2..s one per launch (ks = 1) or in groups of ks with a shorter last group (a
+    last group of one stage runs as a single-stage launch), and the step end."""
+    if ks <= 1:
+        return stages + 1
+    return 2 + (stages - 2 + ks) // ks
+
+
 def replica_barrier(ws):
     """Host barrier of the N-replica run (one process per GPU, gloo): no data-path collective."""
     if ws > 1:
@@ -252,11 +261,9 @@ def run_gpu(args):
         ks = kinfo["fusion"]["ks"]
         if ks > 1 and mixed and attempts == args.steps:
             marks = [s0["stages_total"]] + step_stages[args.warmup:]
-            per = [b - a for a, b in zip(marks, marks[1:])]
-            launches = sum(2 + (sa - 2 + ks) // ks for sa in per)
+            launches = sum(step_launches(b - a, ks) for a, b in zip(marks, marks[1:]))
         elif ks > 1:
-            s_att = stages // attempts if attempts else 0
-            launches = attempts * (2 + (s_att - 2 + ks) // ks)
+            launches = attempts * step_launches(stages // attempts if attempts else 0, ks)
         else:
             launches = stages + attempts
         res[mixed] = dict(ms=ms, dof_stages=dof_stages, launches=launches, stage_ms=stage_ms, kinfo=kinfo,
