@@ -392,6 +392,9 @@ def run_gpu(args):
                      "frac": ach / peak, "traffic": traffic, "kernel": kdesc,
                      "ms_per_launch": m["stage_ms"], "dof_stages_per_launch": ks * N2,
                      "kernel_dof_stages_per_s": ks * N2 / (m["stage_ms"] / 1e3),
+                     # the DOF-stage rate against the HBM bound of one launch per stage
+                     # (16 B per DOF-stage at the same peak): above 1 only with stage groups
+                     "vs_single_stage_hbm_bound": (ks * N2 / (m["stage_ms"] / 1e3)) / (peak * 1e9 / 16.0),
                      "peak_source": peak_kind},
         "clocks": merge_clocks(clock_samples),
         "fp64": {"value": fp64_value, "unit": "DOF-stages/s", "ms_per_step": d["ms"] / args.steps,
